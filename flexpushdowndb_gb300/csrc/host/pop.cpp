@@ -1,0 +1,587 @@
+#include "pop.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace gfpdb::pop {
+
+const char* message_type_name(MessageType t) {
+  switch (t) {
+    case MessageType::START: return "START";
+    case MessageType::TUPLESET: return "TUPLESET";
+    case MessageType::BLOOM_FILTER: return "BLOOM_FILTER";
+    case MessageType::COMPLETE: return "COMPLETE";
+    case MessageType::ERROR: return "ERROR";
+  }
+  return "?";
+}
+
+// ------------------------------------------------------- LocalPOpDirectory
+
+void LocalPOpDirectory::add(const std::string& name, POpRelationshipType rel) { entries_[name].rels.insert(rel); }
+
+void LocalPOpDirectory::setComplete(const std::string& name) {
+  auto it = entries_.find(name);
+  if (it != entries_.end()) it->second.complete = true;
+}
+
+bool LocalPOpDirectory::isComplete(const std::string& name) const {
+  auto it = entries_.find(name);
+  return it != entries_.end() && it->second.complete;
+}
+
+bool LocalPOpDirectory::allComplete(POpRelationshipType rel) const {
+  for (auto& kv : entries_)
+    if (kv.second.rels.count(rel) && !kv.second.complete) return false;
+  return true;
+}
+
+bool LocalPOpDirectory::has(const std::string& name, POpRelationshipType rel) const {
+  auto it = entries_.find(name);
+  return it != entries_.end() && it->second.rels.count(rel) > 0;
+}
+
+std::vector<std::string> LocalPOpDirectory::names(POpRelationshipType rel) const {
+  std::vector<std::string> out;
+  for (auto& kv : entries_)
+    if (kv.second.rels.count(rel)) out.push_back(kv.first);
+  return out;
+}
+
+// -------------------------------------------------------------- POpContext
+
+void POpContext::tell(Message msg) { tell(std::move(msg), op_->consumers()); }
+
+void POpContext::tell(Message msg, const std::vector<std::string>& consumers) {
+  msg.sender = op_->name();
+  for (auto& c : consumers) exec_->post(c, msg);
+}
+
+void POpContext::notifyComplete() {
+  if (complete_) return;
+  complete_ = true;
+  Message m;
+  m.type = MessageType::COMPLETE;
+  tell(m);
+  exec_->markComplete(op_->name());
+  op_->clear();
+}
+
+void POpContext::notifyError(const std::string& error) { exec_->error(op_->name(), error); }
+
+LocalPOpDirectory& POpContext::operatorMap() { return op_->directory(); }
+
+cudaStream_t POpContext::stream() const { return exec_->stream(); }
+
+// ------------------------------------------------------------------ ops
+
+namespace {
+
+bool is_producer_complete(PhysicalOp& op) { return op.ctx()->operatorMap().allComplete(POpRelationshipType::Producer); }
+
+// Emits an input table (FileScanAbstractPOp::readAndSendTuples,
+// fpdb-executor/src/physical/file/FileScanAbstractPOp.cpp:73-130, reading a
+// table the caller handed over instead of a file), optionally split into
+// zero-copy row slices.
+class TableScanPOp : public PhysicalOp {
+ public:
+  TableScanPOp(std::string name, std::string table, std::vector<std::string> columns, int64_t chunk_rows)
+      : PhysicalOp(std::move(name), "TableScanPOp"), table_(std::move(table)), columns_(std::move(columns)),
+        chunk_rows_(chunk_rows) {}
+
+  void setExecution(Execution* e) { exec_ = e; }
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type != MessageType::START) return;
+    const InputTable& in = exec_->input(table_);
+    TupleSetPtr ts = in.device ? in.device : import_tupleset(in.schema, in.array, ctx()->stream());
+    if (!columns_.empty()) ts = ts->project(columns_);
+    const int64_t n = ts->num_rows();
+    if (chunk_rows_ <= 0 || n <= chunk_rows_) {
+      send(ts);
+    } else {
+      for (int64_t at = 0; at < n; at += chunk_rows_) send(slice(ts, at, std::min(chunk_rows_, n - at)));
+    }
+    ctx()->notifyComplete();
+  }
+
+ private:
+  static TupleSetPtr slice(const TupleSetPtr& ts, int64_t at, int64_t len) {
+    std::vector<ColumnPtr> cols;
+    for (int i = 0; i < ts->num_columns(); ++i) {
+      const auto& c = ts->column(i);
+      auto s = std::make_shared<Column>(*c);
+      s->length = len;
+      if (c->type == DType::Utf8) s->offsets = c->offsets + at;
+      else s->data = static_cast<const char*>(c->data) + at * dtype_width(c->type);
+      cols.push_back(s);
+    }
+    return TupleSet::make(ts->fields(), std::move(cols), len);
+  }
+  void send(const TupleSetPtr& ts) {
+    Message out;
+    out.type = MessageType::TUPLESET;
+    out.tuples = ts;
+    ctx()->tell(out);
+  }
+
+  Execution* exec_ = nullptr;
+  std::string table_;
+  std::vector<std::string> columns_;
+  int64_t chunk_rows_;
+};
+
+// FilterPOp (fpdb-executor/src/physical/filter/FilterPOp.cpp:83-138,297-339,
+// 475-482): predicate compiled once against the first TupleSet's schema
+// (buildFilter), each TupleSet filtered and projected on the device.
+class FilterPOp : public PhysicalOp {
+ public:
+  FilterPOp(std::string name, ExprPtr predicate) : PhysicalOp(std::move(name), "FilterPOp"), pred_(std::move(predicate)) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      const TupleSet& ts = *m.tuples;
+      if (!compiled_) {
+        // checkApplicability (FilterPOp.cpp:638-646): predicate columns must exist.
+        compiled_.reset(new CompiledPredicate(compile_predicate(pred_, ts.fields())));
+      }
+      std::vector<std::string> proj;
+      bool all = projectColumnNames_.empty();
+      if (!all)
+        for (auto& c : projectColumnNames_)
+          if (ts.column_index(c) >= 0) proj.push_back(c);
+      Message out;
+      out.type = MessageType::TUPLESET;
+      out.tuples = select_rows(ts, compiled_.get(), {}, proj, all, ctx()->stream());
+      ctx()->tell(out);
+    } else if (m.type == MessageType::COMPLETE) {
+      if (is_producer_complete(*this)) ctx()->notifyComplete();
+    }
+  }
+
+  void clear() override { compiled_.reset(); }
+
+ private:
+  ExprPtr pred_;
+  std::unique_ptr<CompiledPredicate> compiled_;
+};
+
+// BloomFilterCreatePOp (fpdb-executor/src/physical/bloomfilter/BloomFilterCreatePOp.cpp:18-137):
+// forwards every TupleSet to its ordinary consumers, keeps the key columns,
+// and once all producers are complete builds the filter on the device and
+// sends it to the BloomFilterUsePOps.
+class BloomFilterCreatePOp : public PhysicalOp {
+ public:
+  BloomFilterCreatePOp(std::string name, std::string column, int bits, int hashes, std::vector<std::string> uses)
+      : PhysicalOp(std::move(name), "BloomFilterCreatePOp"), column_(std::move(column)), bits_(bits),
+        hashes_(hashes), uses_(std::move(uses)) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      m.tuples->require_column(column_);
+      buffered_.push_back(m.tuples);
+      std::vector<std::string> pass;
+      for (auto& c : consumers_)
+        if (std::find(uses_.begin(), uses_.end(), c) == uses_.end()) pass.push_back(c);
+      Message out;
+      out.type = MessageType::TUPLESET;
+      out.tuples = m.tuples;
+      ctx()->tell(out, pass);
+    } else if (m.type == MessageType::COMPLETE) {
+      if (!is_producer_complete(*this)) return;
+      std::vector<const Column*> parts;
+      for (auto& t : buffered_) parts.push_back(t->column(column_).get());
+      Message out;
+      out.type = MessageType::BLOOM_FILTER;
+      out.bloom = bloom_build(parts, bits_, hashes_, ctx()->stream());
+      ctx()->tell(out, uses_);
+      ctx()->notifyComplete();
+    }
+  }
+
+  void clear() override { buffered_.clear(); }
+
+ private:
+  std::string column_;
+  int bits_, hashes_;
+  std::vector<std::string> uses_;
+  std::vector<TupleSetPtr> buffered_;
+};
+
+// BloomFilterUsePOp (fpdb-executor/src/physical/bloomfilter/BloomFilterUsePOp.cpp:71-142):
+// buffers TupleSets until the filter arrives, then filters each one.
+class BloomFilterUsePOp : public PhysicalOp {
+ public:
+  BloomFilterUsePOp(std::string name, std::string column)
+      : PhysicalOp(std::move(name), "BloomFilterUsePOp"), column_(std::move(column)) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      if (bloom_) filterAndSend(m.tuples);
+      else buffered_.push_back(m.tuples);
+    } else if (m.type == MessageType::BLOOM_FILTER) {
+      bloom_ = m.bloom;
+      for (auto& t : buffered_) filterAndSend(t);
+      buffered_.clear();
+    } else if (m.type == MessageType::COMPLETE) {
+      if (!is_producer_complete(*this)) return;
+      if (!bloom_ && !buffered_.empty())
+        fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name_ + "': producers completed without a bloom filter");
+      ctx()->notifyComplete();
+    }
+  }
+
+  void clear() override {
+    buffered_.clear();
+    bloom_.reset();
+  }
+
+ private:
+  void filterAndSend(const TupleSetPtr& ts) {
+    Message out;
+    out.type = MessageType::TUPLESET;
+    out.tuples = select_rows(*ts, nullptr, {BloomProbe{bloom_, column_}}, {}, true, ctx()->stream());
+    ctx()->tell(out);
+  }
+  std::string column_;
+  BloomPtr bloom_;
+  std::vector<TupleSetPtr> buffered_;
+};
+
+// HashJoinArrowPOp (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowPOp.cpp:85-153):
+// routes TupleSets by sender to the build or probe side, builds the table
+// once every build producer is complete, probes as probe input arrives.
+class HashJoinArrowPOp : public PhysicalOp {
+ public:
+  HashJoinArrowPOp(std::string name, std::vector<std::string> build_producers, std::vector<std::string> probe_producers,
+                   std::string build_key, std::string probe_key, double load_factor)
+      : PhysicalOp(std::move(name), "HashJoinArrowPOp"), build_producers_(std::move(build_producers)),
+        probe_producers_(std::move(probe_producers)), build_key_(std::move(build_key)),
+        probe_key_(std::move(probe_key)), load_factor_(load_factor) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      if (is_build(m.sender)) {
+        if (built_) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': build input after the table was built");
+        build_.push_back(m.tuples);
+      } else {
+        if (built_) probe(m.tuples);
+        else probe_buffer_.push_back(m.tuples);
+      }
+    } else if (m.type == MessageType::COMPLETE) {
+      auto& dir = ctx()->operatorMap();
+      bool build_done = true;
+      for (auto& b : build_producers_) build_done &= dir.isComplete(b);
+      if (build_done && !built_) {
+        finalizeBuild();
+        for (auto& t : probe_buffer_) probe(t);
+        probe_buffer_.clear();
+      }
+      if (is_producer_complete(*this)) {
+        if (!built_) finalizeBuild();
+        ctx()->notifyComplete();
+      }
+    }
+  }
+
+  void clear() override {
+    build_.clear();
+    probe_buffer_.clear();
+    table_ = JoinTable{};
+  }
+
+ private:
+  bool is_build(const std::string& sender) const {
+    return std::find(build_producers_.begin(), build_producers_.end(), sender) != build_producers_.end();
+  }
+
+  void finalizeBuild() {
+    if (build_.empty()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': no build-side input");
+    table_.build = TupleSet::concatenate(build_, ctx()->stream());
+    table_.key_col = table_.build->require_column(build_key_);
+    join_build_table(table_, load_factor_, ctx()->stream());
+    build_.clear();
+    built_ = true;
+  }
+
+  void probe(const TupleSetPtr& ts) {
+    const int pk = ts->require_column(probe_key_);
+    BufferPtr pidx, bidx;
+    int64_t n = 0;
+    join_probe_pairs(table_, *ts, pk, &pidx, &bidx, &n, ctx()->stream());
+    // Output: probe fields then build fields (HashJoinArrowKernel.cpp:148-162),
+    // each filtered to the needed columns.
+    std::vector<GatherSpec> specs;
+    std::vector<Field> fields;
+    auto needed = [&](const std::string& c) {
+      return projectColumnNames_.empty() ||
+             std::find(projectColumnNames_.begin(), projectColumnNames_.end(), c) != projectColumnNames_.end();
+    };
+    for (int i = 0; i < ts->num_columns(); ++i)
+      if (needed(ts->field(i).name)) {
+        fields.push_back(ts->field(i));
+        specs.push_back(GatherSpec{ts->column(i).get(), pidx->as<int32_t>()});
+      }
+    const TupleSet& b = *table_.build;
+    for (int i = 0; i < b.num_columns(); ++i)
+      if (needed(b.field(i).name)) {
+        for (auto& f : fields)
+          if (f.name == b.field(i).name)
+            fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': column '" + f.name + "' is on both sides");
+        fields.push_back(b.field(i));
+        specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
+      }
+    auto cols = gather_columns(specs, n, ctx()->stream());
+    Message out;
+    out.type = MessageType::TUPLESET;
+    out.tuples = TupleSet::make(std::move(fields), std::move(cols), n);
+    ctx()->tell(out);
+  }
+
+  std::vector<std::string> build_producers_, probe_producers_;
+  std::string build_key_, probe_key_;
+  double load_factor_;
+  std::vector<TupleSetPtr> build_, probe_buffer_;
+  JoinTable table_;
+  bool built_ = false;
+};
+
+// GroupPOp (fpdb-executor/src/physical/group/GroupPOp.cpp:14-85): group each
+// TupleSet as it arrives, finalise when all producers are complete.
+class GroupPOp : public PhysicalOp {
+ public:
+  GroupPOp(std::string name, std::vector<std::string> group_cols, std::vector<GroupAggregate> aggs, int64_t hint)
+      : PhysicalOp(std::move(name), "GroupPOp") {
+    table_ = group_table_create(group_cols, aggs, hint);
+  }
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      group_table_update(*table_, *m.tuples, ctx()->stream());
+    } else if (m.type == MessageType::COMPLETE) {
+      if (!is_producer_complete(*this)) return;
+      Message out;
+      out.type = MessageType::TUPLESET;
+      out.tuples = group_table_finalize(*table_, ctx()->stream());
+      if (!projectColumnNames_.empty()) out.tuples = out.tuples->project_exist(projectColumnNames_);
+      ctx()->tell(out);
+      ctx()->notifyComplete();
+    }
+  }
+
+  void clear() override { table_.reset(); }
+
+ private:
+  std::shared_ptr<GroupTable> table_;
+};
+
+// CollatePOp (fpdb-executor/src/physical/collate/CollatePOp.cpp:67-150):
+// concatenates everything it receives into the query result.
+class CollatePOp : public PhysicalOp {
+ public:
+  explicit CollatePOp(std::string name) : PhysicalOp(std::move(name), "CollatePOp") {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      received_.push_back(m.tuples);
+    } else if (m.type == MessageType::COMPLETE) {
+      if (!is_producer_complete(*this)) return;
+      if (!received_.empty()) result_ = TupleSet::concatenate(received_, ctx()->stream());
+      ctx()->notifyComplete();
+    }
+  }
+
+  TupleSetPtr tuples() const { return result_; }
+
+ private:
+  std::vector<TupleSetPtr> received_;
+  TupleSetPtr result_;
+};
+
+AggFn agg_fn(const std::string& f) {
+  if (f == "SUM" || f == "sum" || f == "Sum") return AGG_SUM;
+  if (f == "COUNT" || f == "count" || f == "Count") return AGG_COUNT;
+  if (f == "MIN" || f == "min" || f == "Min") return AGG_MIN;
+  if (f == "MAX" || f == "max" || f == "Max") return AGG_MAX;
+  if (f == "AVG" || f == "avg" || f == "Avg") return AGG_AVG;
+  fail(GFPDB_EUNSUPPORTED, "aggregate function '" + f + "'");
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- Execution
+
+void Execution::add(std::unique_ptr<PhysicalOp> op) {
+  if (by_name_.count(op->name())) fail(GFPDB_EINVAL, "duplicate operator name '" + op->name() + "'");
+  op->setContext(std::make_unique<POpContext>(this, op.get()));
+  by_name_[op->name()] = op.get();
+  ops_.push_back(std::move(op));
+}
+
+PhysicalOp* Execution::op(const std::string& name) {
+  auto it = by_name_.find(name);
+  if (it == by_name_.end()) fail(GFPDB_EINVAL, "unknown operator '" + name + "'");
+  return it->second;
+}
+
+void Execution::connect() {
+  for (auto& o : ops_)
+    for (auto& c : o->consumers()) {
+      PhysicalOp* dst = op(c);
+      if (std::find(dst->producers().begin(), dst->producers().end(), o->name()) == dst->producers().end())
+        dst->producers().push_back(o->name());
+    }
+  for (auto& o : ops_) {
+    for (auto& p : o->producers()) o->directory().add(p, POpRelationshipType::Producer);
+    for (auto& c : o->consumers()) o->directory().add(c, POpRelationshipType::Consumer);
+  }
+  stats_.num_ops = static_cast<int64_t>(ops_.size());
+}
+
+const InputTable& Execution::input(const std::string& name) const {
+  auto it = inputs_.find(name);
+  if (it == inputs_.end()) fail(GFPDB_EINVAL, "plan scans table '" + name + "' but no such table was passed");
+  return it->second;
+}
+
+void Execution::post(const std::string& to, Message msg) { mailbox_.emplace_back(to, std::move(msg)); }
+
+void Execution::markComplete(const std::string&) {}
+
+void Execution::error(const std::string& from, const std::string& msg) {
+  if (error_.empty()) error_ = "operator '" + from + "': " + msg;
+}
+
+TupleSetPtr Execution::execute() {
+  const uint64_t launches0 = g_kernel_launches.load();
+  const CopyCounters c0 = copy_counters();
+  for (auto& o : ops_) {
+    Message start;
+    start.type = MessageType::START;
+    start.sender = "root";
+    post(o->name(), start);
+  }
+  int32_t code = GFPDB_EINVAL;
+  while (!mailbox_.empty() && error_.empty()) {
+    auto [to, msg] = std::move(mailbox_.front());
+    mailbox_.pop_front();
+    PhysicalOp* dst = op(to);
+    if (dst->ctx()->isComplete()) continue;
+    ++stats_.messages;
+    if (msg.type == MessageType::COMPLETE) dst->directory().setComplete(msg.sender);
+    try {
+      dst->onReceive(Envelope{msg});
+    } catch (const Error& e) {
+      code = e.code();
+      dst->ctx()->notifyError(e.what());
+    } catch (const std::exception& e) {
+      dst->ctx()->notifyError(e.what());
+    }
+  }
+  if (!error_.empty()) fail(code, error_);
+  std::string incomplete;
+  CollatePOp* collate = nullptr;
+  for (auto& o : ops_) {
+    if (!o->ctx()->isComplete()) incomplete += (incomplete.empty() ? "" : ", ") + o->name();
+    if (auto* c = dynamic_cast<CollatePOp*>(o.get())) collate = c;
+  }
+  if (!incomplete.empty()) fail(GFPDB_EINVAL, "plan finished with incomplete operators: " + incomplete);
+  if (collate == nullptr) fail(GFPDB_EINVAL, "plan has no CollatePOp");
+  stats_.kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
+  stats_.h2d_bytes = copy_counters().h2d - c0.h2d;
+  stats_.d2h_bytes = copy_counters().d2h - c0.d2h;
+  TupleSetPtr r = collate->tuples();
+  if (!r) fail(GFPDB_EINVAL, "CollatePOp received no TupleSet");
+  return r;
+}
+
+// ------------------------------------------------------------ plan parsing
+
+namespace {
+
+std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
+  const std::string type = o.at("type").str();
+  const std::string name = o.at("name").str();
+  std::unique_ptr<PhysicalOp> op;
+  if (type == "TableScanPOp") {
+    auto s = std::make_unique<TableScanPOp>(name, o.at("table").str(), o.str_list("columns"), o.get_int("chunkRows", 0));
+    s->setExecution(exec);
+    op = std::move(s);
+  } else if (type == "FilterPOp") {
+    op = std::make_unique<FilterPOp>(name, parse_expr(o.at("predicate")));
+  } else if (type == "BloomFilterCreatePOp") {
+    op = std::make_unique<BloomFilterCreatePOp>(name, o.at("bloomFilterColumn").str(),
+                                                static_cast<int>(o.get_int("bitsPerKey", 10)),
+                                                static_cast<int>(o.get_int("numHashes", 3)),
+                                                o.str_list("bloomFilterUsePOps"));
+  } else if (type == "BloomFilterUsePOp") {
+    op = std::make_unique<BloomFilterUsePOp>(name, o.at("bloomFilterColumn").str());
+  } else if (type == "HashJoinArrowPOp") {
+    std::string jt = o.get_str("joinType", "INNER");
+    if (jt != "INNER") fail(GFPDB_EUNSUPPORTED, "join type '" + jt + "' (only INNER runs on the GPU path)");
+    op = std::make_unique<HashJoinArrowPOp>(name, o.str_list("buildProducers"), o.str_list("probeProducers"),
+                                            o.at("buildKey").str(), o.at("probeKey").str(),
+                                            o.get_num("loadFactor", 0.5));
+  } else if (type == "GroupPOp") {
+    std::vector<GroupAggregate> aggs;
+    for (auto& a : o.at("aggregates").array()) {
+      GroupAggregate g;
+      g.fn = agg_fn(a.at("function").str());
+      g.name = a.at("name").str();
+      if (a.contains("expr") && a.at("expr").kind != json::Value::Null) g.expr = parse_expr(a.at("expr"));
+      else if (g.fn == AGG_COUNT) g.fn = AGG_COUNT_STAR;
+      aggs.push_back(g);
+    }
+    op = std::make_unique<GroupPOp>(name, o.str_list("groupColumnNames"), aggs, o.get_int("groupsHint", 0));
+  } else if (type == "CollatePOp") {
+    op = std::make_unique<CollatePOp>(name);
+  } else {
+    fail(GFPDB_EUNSUPPORTED, "operator type '" + type + "'");
+  }
+  op->consumers() = o.str_list("consumers");
+  op->setProjectColumnNames(o.str_list("projectColumnNames"));
+  return op;
+}
+
+}  // namespace
+
+std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream) {
+  auto ex = std::make_unique<Execution>(stream);
+  for (auto& o : plan.at("ops").array()) ex->add(make_op(o, ex.get()));
+  for (auto& o : plan.at("ops").array()) {
+    // BloomFilterCreatePOp's use-ops are consumers too (they wait for its COMPLETE).
+    if (o.at("type").str() == "BloomFilterCreatePOp")
+      for (auto& u : o.str_list("bloomFilterUsePOps")) {
+        auto& cons = ex->op(o.at("name").str())->consumers();
+        if (std::find(cons.begin(), cons.end(), u) == cons.end()) cons.push_back(u);
+      }
+  }
+  ex->connect();
+  return ex;
+}
+
+void validate_plan(const json::Value& plan) {
+  // Host-only structural check: operators parse, names are unique, every
+  // consumer exists and there is exactly one CollatePOp.
+  std::set<std::string> names;
+  int collates = 0;
+  for (auto& o : plan.at("ops").array()) {
+    const std::string name = o.at("name").str();
+    if (!names.insert(name).second) fail(GFPDB_EINVAL, "duplicate operator name '" + name + "'");
+    if (o.at("type").str() == "CollatePOp") ++collates;
+    (void)make_op(o, nullptr);
+  }
+  for (auto& o : plan.at("ops").array())
+    for (auto& c : o.str_list("consumers"))
+      if (!names.count(c)) fail(GFPDB_EINVAL, "operator '" + o.at("name").str() + "' sends to unknown '" + c + "'");
+  if (collates != 1) fail(GFPDB_EINVAL, "a plan needs exactly one CollatePOp");
+}
+
+}  // namespace gfpdb::pop

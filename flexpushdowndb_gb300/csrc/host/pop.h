@@ -1,0 +1,174 @@
+// Physical operators: the GPU-backed drop-ins for the reference's
+// fpdb::executor::physical operators.
+//
+// The interface mirrors the reference's operator contract
+// (fpdb-executor/include/fpdb/executor/physical/PhysicalOp.h:41-84,
+// .../physical/POpContext.h:35-40, .../message/MessageType.h:10-35):
+//   - an operator is driven only through onReceive(const Envelope&),
+//     clear() and getTypeString();
+//   - it sees START, TUPLESET, BLOOM_FILTER and COMPLETE messages;
+//   - it emits through ctx()->tell(msg), ctx()->notifyComplete() and
+//     ctx()->notifyError(msg);
+//   - it acts on completion when
+//     ctx()->operatorMap().allComplete(POpRelationshipType::Producer) holds
+//     (fpdb-executor/src/physical/LocalPOpDirectory.cpp:52-58).
+// TupleSets are shared, never mutated after they are sent.
+//
+// The CAF actor runtime (one actor per operator, serial mailboxes,
+// fpdb-executor/src/physical/POpActor.cpp:25-135) is replaced by one host
+// thread delivering messages in FIFO order while every operator enqueues its
+// device work on the execution's CUDA stream.
+#pragma once
+
+#include <deque>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../kernels/launch.h"
+#include "expr.h"
+#include "json.h"
+#include "tupleset.h"
+
+namespace gfpdb::pop {
+
+enum class MessageType { START, TUPLESET, BLOOM_FILTER, COMPLETE, ERROR };
+const char* message_type_name(MessageType t);
+
+struct Message {
+  MessageType type = MessageType::START;
+  std::string sender;
+  TupleSetPtr tuples;   // TUPLESET
+  BloomPtr bloom;       // BLOOM_FILTER
+  std::string error;    // ERROR
+};
+
+// The reference wraps a message in an Envelope; here the envelope is the
+// message itself plus its receiver.
+struct Envelope {
+  Message message;
+  const Message& getMessage() const { return message; }
+};
+
+enum class POpRelationshipType { Producer, Consumer };
+
+class LocalPOpDirectory {
+ public:
+  void add(const std::string& name, POpRelationshipType rel);
+  void setComplete(const std::string& name);
+  bool isComplete(const std::string& name) const;
+  bool allComplete(POpRelationshipType rel) const;
+  bool has(const std::string& name, POpRelationshipType rel) const;
+  std::vector<std::string> names(POpRelationshipType rel) const;
+
+ private:
+  struct Entry {
+    std::set<POpRelationshipType> rels;
+    bool complete = false;
+  };
+  std::map<std::string, Entry> entries_;
+};
+
+class Execution;
+class PhysicalOp;
+
+class POpContext {
+ public:
+  POpContext(Execution* exec, PhysicalOp* op) : exec_(exec), op_(op) {}
+  // Send to every consumer, or to the named ones.
+  void tell(Message msg);
+  void tell(Message msg, const std::vector<std::string>& consumers);
+  void notifyComplete();
+  void notifyError(const std::string& error);
+  LocalPOpDirectory& operatorMap();
+  cudaStream_t stream() const;
+  bool isComplete() const { return complete_; }
+
+ private:
+  Execution* exec_;
+  PhysicalOp* op_;
+  bool complete_ = false;
+};
+
+class PhysicalOp {
+ public:
+  PhysicalOp(std::string name, std::string type) : name_(std::move(name)), type_(std::move(type)) {}
+  virtual ~PhysicalOp() = default;
+
+  virtual void onReceive(const Envelope& msg) = 0;
+  virtual void clear() {}
+  virtual std::string getTypeString() const { return type_; }
+
+  const std::string& name() const { return name_; }
+  std::vector<std::string>& producers() { return producers_; }
+  std::vector<std::string>& consumers() { return consumers_; }
+  void setProjectColumnNames(std::vector<std::string> c) { projectColumnNames_ = std::move(c); }
+  const std::vector<std::string>& getProjectColumnNames() const { return projectColumnNames_; }
+
+  POpContext* ctx() { return ctx_.get(); }
+  void setContext(std::unique_ptr<POpContext> c) { ctx_ = std::move(c); }
+  LocalPOpDirectory& directory() { return directory_; }
+
+ protected:
+  std::string name_;
+  std::string type_;
+  std::vector<std::string> producers_;
+  std::vector<std::string> consumers_;
+  std::vector<std::string> projectColumnNames_;
+  std::unique_ptr<POpContext> ctx_;
+  LocalPOpDirectory directory_;
+};
+
+// Input tables of a plan, by name.
+struct InputTable {
+  TupleSetPtr device;                 // already resident
+  const ArrowSchema* schema = nullptr;  // or imported at scan time
+  const ArrowDeviceArray* array = nullptr;
+};
+
+struct ExecStats {
+  int64_t kernel_launches = 0;
+  int64_t h2d_bytes = 0;
+  int64_t d2h_bytes = 0;
+  int64_t messages = 0;
+  int64_t num_ops = 0;
+};
+
+class Execution {
+ public:
+  Execution(cudaStream_t stream) : stream_(stream) {}
+
+  void add(std::unique_ptr<PhysicalOp> op);
+  PhysicalOp* op(const std::string& name);
+  void connect();  // fill producers from consumers and each op's directory
+  void setInputs(std::map<std::string, InputTable> inputs) { inputs_ = std::move(inputs); }
+  const InputTable& input(const std::string& name) const;
+
+  // START every operator, deliver messages until all are complete, return
+  // the CollatePOp's TupleSet (Execution::execute, fpdb-executor/src/Execution.cpp:44-50).
+  TupleSetPtr execute();
+
+  void post(const std::string& to, Message msg);
+  void markComplete(const std::string& name);
+  void error(const std::string& from, const std::string& msg);
+  cudaStream_t stream() const { return stream_; }
+  ExecStats stats() const { return stats_; }
+
+ private:
+  cudaStream_t stream_;
+  std::vector<std::unique_ptr<PhysicalOp>> ops_;
+  std::map<std::string, PhysicalOp*> by_name_;
+  std::deque<std::pair<std::string, Message>> mailbox_;
+  std::map<std::string, InputTable> inputs_;
+  std::string error_;
+  ExecStats stats_;
+};
+
+// Build an Execution from a JSON plan (format documented with
+// gfpdb_execute_plan in include/gfpdb.h).
+std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream);
+void validate_plan(const json::Value& plan);
+
+}  // namespace gfpdb::pop

@@ -1,0 +1,210 @@
+#include "runtime.h"
+
+#include <mutex>
+#include <vector>
+
+namespace gfpdb {
+
+std::atomic<uint64_t> g_kernel_launches{0};
+
+void fail(int32_t code, const std::string& msg) { throw Error(code, msg); }
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    fail(e == cudaErrorMemoryAllocation ? GFPDB_ENOMEM : GFPDB_ECUDA,
+         std::string("CUDA error in ") + what + ": " + cudaGetErrorName(e) + " (" +
+             cudaGetErrorString(e) + ")");
+  }
+}
+
+void after_launch(const char* kernel_name) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fail(GFPDB_ECUDA, std::string("launch of ") + kernel_name + " failed: " + cudaGetErrorName(e) +
+                          " (" + cudaGetErrorString(e) + ")");
+  }
+  count_launch();
+}
+
+CopyCounters& copy_counters() {
+  thread_local CopyCounters c;
+  return c;
+}
+
+namespace {
+struct DeviceInfo {
+  bool ready = false;
+  int sms = 0;
+  int smem_optin = 0;
+};
+std::mutex g_dev_mu;
+std::vector<DeviceInfo> g_devs;
+}  // namespace
+
+int current_device() {
+  int d = 0;
+  GF_CUDA(cudaGetDevice(&d));
+  return d;
+}
+
+static DeviceInfo& info_for(int dev) {
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (g_devs.empty()) {
+    int n = 0;
+    GF_CUDA(cudaGetDeviceCount(&n));
+    if (n <= 0) fail(GFPDB_ECUDA, "no CUDA device is visible");
+    g_devs.resize(n);
+  }
+  if (dev < 0 || dev >= static_cast<int>(g_devs.size())) fail(GFPDB_EINVAL, "device index out of range");
+  DeviceInfo& di = g_devs[dev];
+  if (!di.ready) {
+    cudaDeviceProp prop;
+    GF_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (prop.major < 10) {
+      fail(GFPDB_EUNSUPPORTED, std::string("device ") + prop.name + " is not a Blackwell (sm_10x) GPU");
+    }
+    di.sms = prop.multiProcessorCount;
+    di.smem_optin = static_cast<int>(prop.sharedMemPerBlockOptin);
+    cudaMemPool_t pool;
+    GF_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t threshold = UINT64_MAX;
+    GF_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+    di.ready = true;
+  }
+  return di;
+}
+
+void ensure_device() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) check_cuda(e, "cudaGetDevice");
+  info_for(dev);
+}
+
+int num_sms() { return info_for(current_device()).sms; }
+int max_smem_optin() { return info_for(current_device()).smem_optin; }
+
+DeviceBuffer::DeviceBuffer(int64_t bytes, cudaStream_t stream) : bytes_(bytes), owned_(true), stream_(stream) {
+  if (bytes < 0) fail(GFPDB_EINVAL, "negative allocation size");
+  // Zero-byte buffers still get a distinct valid pointer so Arrow consumers
+  // never see NULL data buffers for empty columns.
+  int64_t n = bytes > 0 ? bytes : 16;
+  GF_CUDA(cudaMallocAsync(&ptr_, static_cast<size_t>(n), stream));
+}
+
+DeviceBuffer::~DeviceBuffer() {
+  if (owned_ && ptr_ != nullptr) {
+    // Errors are swallowed: destructors must not throw, and a failing free
+    // means the context is already gone.
+    (void)cudaFreeAsync(ptr_, stream_);
+  }
+}
+
+void memcpy_h2d(void* dst, const void* src, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  GF_CUDA(cudaMemcpyAsync(dst, src, static_cast<size_t>(n), cudaMemcpyHostToDevice, s));
+  copy_counters().h2d += n;
+}
+
+void memcpy_d2h(void* dst, const void* src, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  GF_CUDA(cudaMemcpyAsync(dst, src, static_cast<size_t>(n), cudaMemcpyDeviceToHost, s));
+  copy_counters().d2h += n;
+}
+
+void sync(cudaStream_t s) { GF_CUDA(cudaStreamSynchronize(s)); }
+
+namespace {
+struct ProfRecord {
+  std::string name;
+  cudaEvent_t start = nullptr;
+  cudaEvent_t stop = nullptr;
+  double bytes = 0;
+};
+std::mutex g_prof_mu;
+std::vector<ProfRecord> g_prof;
+std::atomic<bool> g_prof_on{false};
+}  // namespace
+
+ProfScope::ProfScope(const char* name, cudaStream_t s) : stream_(s) {
+  if (!g_prof_on.load(std::memory_order_relaxed)) return;
+  ProfRecord r;
+  r.name = name;
+  GF_CUDA(cudaEventCreate(&r.start));
+  GF_CUDA(cudaEventCreate(&r.stop));
+  GF_CUDA(cudaEventRecord(r.start, s));
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  index_ = static_cast<int64_t>(g_prof.size());
+  g_prof.push_back(r);
+}
+
+void ProfScope::stop(double bytes) {
+  if (index_ < 0) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  GF_CUDA(cudaEventRecord(g_prof[index_].stop, stream_));
+  g_prof[index_].bytes = bytes;
+}
+
+void ProfScope::set_bytes(double bytes) {
+  if (index_ < 0) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof[index_].bytes = bytes;
+}
+
+void prof_enable(bool on) { g_prof_on.store(on); }
+
+void prof_reset() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (auto& r : g_prof) {
+    if (r.start) cudaEventDestroy(r.start);
+    if (r.stop) cudaEventDestroy(r.stop);
+  }
+  g_prof.clear();
+}
+
+void prof_read(const std::string& name, int64_t* launches, double* ms, double* bytes) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  int64_t n = 0;
+  double t = 0, b = 0;
+  for (auto& r : g_prof) {
+    if (r.name != name) continue;
+    GF_CUDA(cudaEventSynchronize(r.stop));
+    float e = 0;
+    GF_CUDA(cudaEventElapsedTime(&e, r.start, r.stop));
+    ++n;
+    t += e;
+    b += r.bytes;
+  }
+  *launches = n;
+  *ms = t;
+  *bytes = b;
+}
+
+std::string prof_kernels() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  std::vector<std::string> seen;
+  std::string out;
+  for (auto& r : g_prof) {
+    bool dup = false;
+    for (auto& s : seen) dup |= s == r.name;
+    if (dup) continue;
+    seen.push_back(r.name);
+    out += r.name + "\n";
+  }
+  return out;
+}
+
+void raise_device_status(const DevStatus& st, const char* where) {
+  if (st.code == 0) return;
+  std::string what;
+  switch (st.code) {
+    case GFPDB_ETIMEDOUT: what = "a bounded device wait gave up"; break;
+    case GFPDB_EDEVICE: what = "device error"; break;
+    case GFPDB_ENOMEM: what = "device table or arena full"; break;
+    case GFPDB_EINVAL: what = "invalid value on device"; break;
+    default: what = "device status " + std::to_string(st.code);
+  }
+  fail(st.code, std::string(where) + ": " + what + " (detail " + std::to_string(st.detail) + ")");
+}
+
+}  // namespace gfpdb

@@ -1,0 +1,120 @@
+// Host runtime: errors, CUDA checks, device buffers, launch accounting.
+//
+// The reference reports failures as tl::expected<T, std::string> and turns
+// them into ErrorMessages (fpdb-executor/src/physical/POpContext.cpp:190-195).
+// Inside this library a failure is a gfpdb::Error exception carrying one of
+// the GFPDB_E* codes; the C-ABI layer converts it to a status code plus a
+// thread-local message.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "../../../include/gfpdb.h"
+
+namespace gfpdb {
+
+class Error : public std::runtime_error {
+ public:
+  Error(int32_t code, const std::string& msg) : std::runtime_error(msg), code_(code) {}
+  int32_t code() const { return code_; }
+
+ private:
+  int32_t code_;
+};
+
+[[noreturn]] void fail(int32_t code, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what);
+#define GF_CUDA(call) ::gfpdb::check_cuda((call), #call)
+
+// Every kernel launch in the library goes through this counter so a caller
+// can tell how many device kernels a call issued.
+extern std::atomic<uint64_t> g_kernel_launches;
+inline void count_launch(uint64_t n = 1) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
+// Checks the launch that was just issued and counts it.
+void after_launch(const char* kernel_name);
+
+// Per-thread byte counters of host<->device copies, read by plan execution.
+struct CopyCounters {
+  int64_t h2d = 0;
+  int64_t d2h = 0;
+};
+CopyCounters& copy_counters();
+
+int current_device();
+void ensure_device();            // gfpdb_device_init on first use
+int num_sms();                   // SM count of the current device
+int max_smem_optin();            // opt-in shared memory per block
+
+// Stream-ordered device allocation. Memory comes from the device's default
+// memory pool with an unbounded release threshold, so repeated queries reuse
+// pages instead of returning them to the driver.
+class DeviceBuffer {
+ public:
+  DeviceBuffer(int64_t bytes, cudaStream_t stream);
+  // Borrowed memory: never freed by this object.
+  DeviceBuffer(void* borrowed, int64_t bytes) : ptr_(borrowed), bytes_(bytes), owned_(false) {}
+  ~DeviceBuffer();
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+
+  void* data() const { return ptr_; }
+  int64_t size() const { return bytes_; }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(ptr_);
+  }
+
+ private:
+  void* ptr_ = nullptr;
+  int64_t bytes_ = 0;
+  bool owned_ = true;
+  cudaStream_t stream_ = nullptr;
+};
+using BufferPtr = std::shared_ptr<DeviceBuffer>;
+
+inline BufferPtr make_buffer(int64_t bytes, cudaStream_t stream) {
+  return std::make_shared<DeviceBuffer>(bytes, stream);
+}
+
+void memcpy_h2d(void* dst, const void* src, int64_t n, cudaStream_t s);
+void memcpy_d2h(void* dst, const void* src, int64_t n, cudaStream_t s);
+void sync(cudaStream_t s);
+
+// Per-call status block that every kernel of one operator call shares: a
+// device error word (first error code + detail) and counters, zeroed by a
+// single memset. Read back with read_status() after the call's kernels.
+struct DevStatus {
+  int32_t code;     // 0 = ok, else a GFPDB_E* code raised on the device
+  int32_t detail;   // kernel-specific detail (e.g. which wait gave up)
+  int64_t value;    // kernel-specific (e.g. rows produced)
+  int64_t aux[6];
+};
+static_assert(sizeof(DevStatus) == 64, "status block is one 64-byte line");
+
+void raise_device_status(const DevStatus& st, const char* where);
+
+// Optional per-launch timing (gfpdb_profile_*): events on the launching
+// stream around one kernel plus its algorithmic bytes.
+class ProfScope {
+ public:
+  ProfScope(const char* name, cudaStream_t s);
+  // Record the stop event; bytes may be refined later with set_bytes().
+  void stop(double bytes);
+  void set_bytes(double bytes);
+
+ private:
+  int64_t index_ = -1;
+  cudaStream_t stream_;
+};
+void prof_enable(bool on);
+void prof_reset();
+void prof_read(const std::string& name, int64_t* launches, double* ms, double* bytes);
+std::string prof_kernels();
+
+}  // namespace gfpdb

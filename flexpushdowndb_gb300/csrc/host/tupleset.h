@@ -1,0 +1,101 @@
+// Device-resident TupleSet: the GPU form of fpdb::tuple::TupleSet
+// (fpdb-tuple/include/fpdb/tuple/TupleSet.h:31-207).
+//
+// The reference wraps an arrow::Table of chunked columns that operators share
+// by shared_ptr and never mutate after sending (concatenate instead of append,
+// fpdb-executor/src/physical/bloomfilter/BloomFilterCreateAbstractKernel.cpp:22-38).
+// Here each column is one contiguous device buffer (Arrow layout: values for
+// fixed-width types, int32 offsets + bytes for utf8); columns are immutable and
+// shared between TupleSets by shared_ptr, so projection is free and a
+// TupleSet sent to several consumers is never copied.
+#pragma once
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "runtime.h"
+
+namespace gfpdb {
+
+enum class DType : int8_t { Int32 = 0, Int64 = 1, Date32 = 2, Float64 = 3, Utf8 = 4 };
+
+const char* dtype_name(DType t);
+int dtype_width(DType t);  // bytes per value; 0 for utf8
+DType dtype_from_format(const char* format);
+const char* dtype_format(DType t);
+DType dtype_from_name(const std::string& name);  // "int32", "int64", "date32", "float64", "utf8"
+
+struct Column {
+  DType type = DType::Int32;
+  int64_t length = 0;
+  BufferPtr data_buf;      // keeps the value (or utf8 byte) memory alive
+  BufferPtr offsets_buf;   // utf8 only
+  const void* data = nullptr;        // first value of this column
+  const int32_t* offsets = nullptr;  // utf8: length + 1 offsets into `data`
+
+  int64_t value_bytes() const;  // bytes of values (utf8: bytes spanned by offsets)
+};
+using ColumnPtr = std::shared_ptr<const Column>;
+
+struct Field {
+  std::string name;
+  DType type;
+};
+
+class TupleSet;
+using TupleSetPtr = std::shared_ptr<const TupleSet>;
+
+class TupleSet {
+ public:
+  TupleSet(std::vector<Field> fields, std::vector<ColumnPtr> columns, int64_t num_rows);
+
+  static TupleSetPtr make(std::vector<Field> fields, std::vector<ColumnPtr> columns, int64_t num_rows);
+  static TupleSetPtr make_empty(const std::vector<Field>& fields, cudaStream_t s);
+
+  int64_t num_rows() const { return num_rows_; }
+  int num_columns() const { return static_cast<int>(columns_.size()); }
+  const std::vector<Field>& fields() const { return fields_; }
+  const Field& field(int i) const { return fields_.at(i); }
+  const ColumnPtr& column(int i) const { return columns_.at(i); }
+  int column_index(const std::string& name) const;  // -1 when absent
+  int require_column(const std::string& name) const;  // throws GFPDB_EINVAL
+  ColumnPtr column(const std::string& name) const { return columns_[require_column(name)]; }
+
+  // Keep the named columns that exist, in the given order
+  // (TupleSet::projectExist, fpdb-tuple/src/TupleSet.cpp).
+  TupleSetPtr project_exist(const std::vector<std::string>& names) const;
+  TupleSetPtr project(const std::vector<std::string>& names) const;  // all must exist
+
+  int64_t bytes() const;
+
+  // Row-wise concatenation into fresh device buffers
+  // (TupleSet::concatenate, fpdb-tuple/src/TupleSet.cpp).
+  static TupleSetPtr concatenate(const std::vector<TupleSetPtr>& sets, cudaStream_t s);
+
+ private:
+  std::vector<Field> fields_;
+  std::vector<ColumnPtr> columns_;
+  int64_t num_rows_;
+};
+
+// Column factories.
+ColumnPtr make_fixed_column(DType t, int64_t length, BufferPtr buf, const void* data = nullptr);
+ColumnPtr make_utf8_column(int64_t length, BufferPtr offsets, BufferPtr bytes);
+
+// ---- Arrow C Data / Device Data Interface ----
+
+// Import a struct-typed (ArrowSchema "+s", ArrowDeviceArray) pair. Device
+// arrays are borrowed (the caller keeps them alive for the duration of the
+// call) unless copy_device is set; host arrays are copied to the device on
+// stream `s`.
+TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* array, cudaStream_t s,
+                            bool copy_device = false);
+std::vector<Field> import_schema(const ArrowSchema* schema);
+
+// Export a TupleSet. With to_host, values are copied to host memory (stream
+// synchronized) and the array's device_type is ARROW_DEVICE_CPU.
+void export_tupleset(const TupleSetPtr& ts, ArrowSchema* schema_out, ArrowDeviceArray* array_out,
+                     bool to_host, cudaStream_t s);
+
+}  // namespace gfpdb

@@ -1,0 +1,238 @@
+// Row gathers (fixed-width and utf8), utf8 concatenation and a single-pass
+// exclusive prefix sum. These materialise the outputs of join probes, group
+// finalisation and utf8 projections, the GPU form of the
+// arrow::compute::Take / ArrayAppender work the reference does per row
+// (fpdb-executor/src/physical/join/hashjoin/RecordBatchHashJoiner.cpp:83-119).
+#include "common.cuh"
+#include "launch.h"
+
+#include <cstring>
+
+namespace gfpdb {
+
+namespace {
+
+constexpr int kGatherMax = kMaxCols * 2;
+
+struct GatherFixedParams {
+  int64_t n;
+  int32_t n_cols;
+  int32_t pad;
+  const void* src[kGatherMax];
+  void* dst[kGatherMax];
+  const int32_t* idx[kGatherMax];
+  int32_t width[kGatherMax];
+};
+
+__global__ void __launch_bounds__(256) gather_fixed_kernel(const __grid_constant__ GatherFixedParams p) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < p.n; r += stride) {
+    for (int c = 0; c < p.n_cols; ++c) {
+      const int32_t i = __ldg(p.idx[c] + r);
+      if (p.width[c] == 8) {
+        static_cast<long long*>(p.dst[c])[r] = __ldg(static_cast<const long long*>(p.src[c]) + i);
+      } else {
+        static_cast<int*>(p.dst[c])[r] = __ldg(static_cast<const int*>(p.src[c]) + i);
+      }
+    }
+  }
+}
+
+__global__ void utf8_lengths_kernel(const int32_t* __restrict__ offs, const int32_t* __restrict__ idx,
+                                    int32_t* __restrict__ len, int64_t n) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int32_t i = idx[r];
+    len[r] = offs[i + 1] - offs[i];
+  }
+}
+
+__global__ void utf8_copy_kernel(const int32_t* __restrict__ src_offs, const uint8_t* __restrict__ src_bytes,
+                                 const int32_t* __restrict__ idx, const int32_t* __restrict__ dst_offs,
+                                 uint8_t* __restrict__ dst_bytes, int64_t n) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int32_t i = idx[r];
+    const int32_t b = src_offs[i];
+    const int32_t len = src_offs[i + 1] - b;
+    const int32_t o = dst_offs[r];
+    for (int32_t k = 0; k < len; ++k) dst_bytes[o + k] = src_bytes[b + k];
+  }
+}
+
+__global__ void rebase_offsets_kernel(const int32_t* __restrict__ src, int32_t* __restrict__ dst, int64_t n,
+                                      int32_t sub, int32_t add) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride)
+    dst[r] = src[r] - sub + add;
+}
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_i32_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n, int64_t n_tiles,
+                    uint64_t* tile_status, uint32_t* ticket, DevStatus* st) {
+  __shared__ int s_warp[kScanThreads / 32 + 1];
+  __shared__ uint32_t s_tile;
+  __shared__ uint64_t s_base;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const int64_t tile = s_tile;
+    if (tile >= n_tiles) break;
+    const int64_t row0 = tile * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+    int v[kScanItems];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      v[k] = row0 + k < n ? in[row0 + k] : 0;
+      sum += v[k];
+    }
+    int total;
+    int excl = block_exclusive_sum<kScanThreads>(sum, &total, s_warp);
+    if (threadIdx.x < 32) {
+      uint64_t b = lookback_exclusive(tile_status, tile, static_cast<uint64_t>(total), st);
+      if (threadIdx.x == 0) s_base = b;
+    }
+    __syncthreads();
+    int64_t run = static_cast<int64_t>(s_base) + excl;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      if (row0 + k < n) out[row0 + k] = static_cast<int32_t>(run);
+      run += v[k];
+    }
+    if (tile == n_tiles - 1 && threadIdx.x == 0) {
+      st->value = static_cast<int64_t>(s_base) + total;
+      out[n] = static_cast<int32_t>(s_base + total);
+    }
+    __syncthreads();
+  }
+}
+
+int grid_for(int64_t n, int threads) {
+  int64_t blocks = (n + threads - 1) / threads;
+  int64_t cap = static_cast<int64_t>(num_sms()) * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return static_cast<int>(blocks);
+}
+
+}  // namespace
+
+int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
+  if (n == 0) {
+    GF_CUDA(cudaMemsetAsync(out, 0, 4, s));
+    return 0;
+  }
+  const int64_t n_tiles = (n + kScanTile - 1) / kScanTile;
+  // scratch: status block, ticket, tile words
+  auto scratch = make_buffer(sizeof(DevStatus) + 64 + n_tiles * 8, s);
+  char* base = scratch->as<char>();
+  DevStatus* st = reinterpret_cast<DevStatus*>(base);
+  uint32_t* ticket = reinterpret_cast<uint32_t*>(base + sizeof(DevStatus));
+  uint64_t* tiles = reinterpret_cast<uint64_t*>(base + sizeof(DevStatus) + 64);
+  GF_CUDA(cudaMemsetAsync(base, 0, scratch->size(), s));
+  int grid = static_cast<int>(n_tiles < num_sms() * 4 ? n_tiles : num_sms() * 4);
+  scan_i32_kernel<<<grid, kScanThreads, 0, s>>>(in, out, n, n_tiles, tiles, ticket, st);
+  after_launch("scan_i32_kernel");
+  DevStatus hs;
+  GF_CUDA(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  sync(s);
+  raise_device_status(hs, "prefix sum");
+  if (hs.value > INT32_MAX) fail(GFPDB_EUNSUPPORTED, "utf8 column exceeds 2 GiB of bytes");
+  return hs.value;
+}
+
+std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s) {
+  std::vector<ColumnPtr> out(specs.size());
+  GatherFixedParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.n = n;
+  std::vector<std::pair<size_t, BufferPtr>> fixed;
+  for (size_t i = 0; i < specs.size(); ++i) {
+    const Column& c = *specs[i].src;
+    if (c.type == DType::Utf8) continue;
+    int w = dtype_width(c.type);
+    auto buf = make_buffer(n * w, s);
+    if (p.n_cols >= kGatherMax) fail(GFPDB_EUNSUPPORTED, "too many columns to gather");
+    p.src[p.n_cols] = c.data;
+    p.dst[p.n_cols] = buf->data();
+    p.idx[p.n_cols] = specs[i].idx;
+    p.width[p.n_cols] = w;
+    ++p.n_cols;
+    out[i] = make_fixed_column(c.type, n, buf);
+  }
+  if (p.n_cols > 0 && n > 0) {
+    ProfScope prof("gather_fixed_kernel", s);
+    gather_fixed_kernel<<<grid_for(n, 256), 256, 0, s>>>(p);
+    after_launch("gather_fixed_kernel");
+    double w = 0;
+    for (int c = 0; c < p.n_cols; ++c) w += 2.0 * p.width[c] + 4.0;
+    prof.stop(static_cast<double>(n) * w);
+  }
+  for (size_t i = 0; i < specs.size(); ++i) {
+    const Column& c = *specs[i].src;
+    if (c.type != DType::Utf8) continue;
+    auto offs = make_buffer((n + 1) * 4, s);
+    int64_t total = 0;
+    if (n > 0) {
+      auto lens = make_buffer(n * 4, s);
+      utf8_lengths_kernel<<<grid_for(n, 256), 256, 0, s>>>(c.offsets, specs[i].idx, lens->as<int32_t>(), n);
+      after_launch("utf8_lengths_kernel");
+      total = exclusive_scan_i32(lens->as<int32_t>(), offs->as<int32_t>(), n, s);
+    } else {
+      GF_CUDA(cudaMemsetAsync(offs->data(), 0, 4, s));
+    }
+    auto bytes = make_buffer(total, s);
+    if (n > 0 && total > 0) {
+      utf8_copy_kernel<<<grid_for(n, 256), 256, 0, s>>>(c.offsets, static_cast<const uint8_t*>(c.data),
+                                                       specs[i].idx, offs->as<int32_t>(), bytes->as<uint8_t>(), n);
+      after_launch("utf8_copy_kernel");
+    }
+    out[i] = make_utf8_column(n, offs, bytes);
+  }
+  return out;
+}
+
+ColumnPtr concat_utf8(const std::vector<const Column*>& parts, cudaStream_t s) {
+  int64_t n = 0;
+  std::vector<std::pair<int32_t, int32_t>> ends(parts.size());
+  for (size_t i = 0; i < parts.size(); ++i) {
+    n += parts[i]->length;
+    int32_t e[2] = {0, 0};
+    if (parts[i]->length > 0) {
+      GF_CUDA(cudaMemcpyAsync(&e[0], parts[i]->offsets, 4, cudaMemcpyDeviceToHost, s));
+      GF_CUDA(cudaMemcpyAsync(&e[1], parts[i]->offsets + parts[i]->length, 4, cudaMemcpyDeviceToHost, s));
+    }
+    sync(s);
+    ends[i] = {e[0], e[1]};
+  }
+  int64_t total = 0;
+  for (auto& e : ends) total += e.second - e.first;
+  if (total > INT32_MAX) fail(GFPDB_EUNSUPPORTED, "utf8 column exceeds 2 GiB of bytes");
+  auto offs = make_buffer((n + 1) * 4, s);
+  auto bytes = make_buffer(total, s);
+  int64_t row = 0;
+  int32_t at = 0;
+  for (size_t i = 0; i < parts.size(); ++i) {
+    const Column* c = parts[i];
+    if (c->length > 0) {
+      rebase_offsets_kernel<<<grid_for(c->length, 256), 256, 0, s>>>(c->offsets, offs->as<int32_t>() + row,
+                                                                     c->length, ends[i].first, at);
+      after_launch("rebase_offsets_kernel");
+      int32_t nb = ends[i].second - ends[i].first;
+      if (nb > 0)
+        GF_CUDA(cudaMemcpyAsync(bytes->as<char>() + at, static_cast<const char*>(c->data) + ends[i].first, nb,
+                                cudaMemcpyDeviceToDevice, s));
+      at += nb;
+      row += c->length;
+    }
+  }
+  GF_CUDA(cudaMemcpyAsync(offs->as<int32_t>() + n, &at, 4, cudaMemcpyHostToDevice, s));
+  sync(s);  // `at` lives on this stack frame
+  return make_utf8_column(n, offs, bytes);
+}
+
+}  // namespace gfpdb

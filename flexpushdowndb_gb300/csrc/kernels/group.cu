@@ -1,0 +1,815 @@
+// Hash group-by with exact integer aggregates.
+//
+// Replaces the Arrow hash aggregate (hash_sum / hash_count / hash_min_max)
+// that GroupArrowKernel drives (fpdb-executor/src/physical/group/GroupArrowKernel.cpp:127-154,
+// fpdb-executor/src/physical/aggregate/function/Sum.cpp:63-74, Count.cpp:91-104)
+// and the native GroupKernel (fpdb-executor/src/physical/group/GroupKernel.cpp:263-300).
+//
+// Keys: up to two key columns packed into one 64-bit word (32 bits per int32 /
+// date32 column, 64 bits for one int64 column); a utf8 key column is first
+// mapped to dense int32 codes by a device string dictionary that persists
+// across batches. The all-ones word marks an empty slot, so the one key that
+// packs to all-ones gets a dedicated extra slot at index `capacity`.
+//
+// Aggregation: each CTA first folds its rows into a shared-memory table
+// (64-bit atomicCAS on keys, 64-bit atomics on accumulators) and merges the
+// table into the global open-addressing table once at the end, so
+// low-cardinality group-bys (a handful to a few thousand groups) cost one
+// global atomic per group per CTA rather than per row. Rows whose key does
+// not fit the shared table go straight to the global table. Integer sums are
+// 64-bit two's-complement additions, which are associative and commutative,
+// so results are bit-exact whatever order the atomics land in.
+#include <cstring>
+
+#include "eval.cuh"
+#include "launch.h"
+
+namespace gfpdb {
+
+namespace {
+
+constexpr int kGroupThreads = 256;
+constexpr uint32_t kDictSpinLimit = 1u << 20;
+
+struct AccDev {
+  int8_t fn;  // AGG_SUM / AGG_COUNT / AGG_MIN / AGG_MAX / AGG_COUNT_STAR
+  int8_t vt;
+  int16_t pad;
+  int32_t pad2;
+  Operand in;
+};
+
+struct GroupParams {
+  int64_t n_rows;
+  int32_t n_keys;
+  int32_t n_acc;
+  int32_t key_bits[2];
+  DevCol key_cols[2];
+  AccDev acc[kMaxAggs];
+  DevCol cols[kMaxCols];
+  uint64_t* keys;
+  unsigned long long* accs;
+  uint64_t mask;
+  int32_t use_smem;
+  int32_t sm_slots;
+  DevStatus* st;  // aux[0]: groups claimed, aux[1]: special slot used
+  Program prog;
+};
+
+__device__ __forceinline__ uint64_t pack_key(const GroupParams& p, int64_t row) {
+  if (p.n_keys == 1) {
+    const int64_t v = load_int(p.key_cols[0], row);
+    return p.key_bits[0] == 64 ? static_cast<uint64_t>(v) : static_cast<uint64_t>(static_cast<uint32_t>(v));
+  }
+  const uint32_t a = static_cast<uint32_t>(load_int(p.key_cols[0], row));
+  const uint32_t b = static_cast<uint32_t>(load_int(p.key_cols[1], row));
+  return (static_cast<uint64_t>(a) << 32) | b;
+}
+
+// Identity of each accumulator: 0 for sums and counts, +inf / INT64_MAX for
+// MIN, -inf / INT64_MIN for MAX (as bit patterns).
+__device__ __forceinline__ unsigned long long acc_init(int fn, int vt) {
+  if (fn == AGG_MIN) return vt == VT_F64 ? 0x7ff0000000000000ull : static_cast<unsigned long long>(INT64_MAX);
+  if (fn == AGG_MAX) return vt == VT_F64 ? 0xfff0000000000000ull : static_cast<unsigned long long>(INT64_MIN);
+  return 0ull;
+}
+
+__device__ __forceinline__ void acc_combine(unsigned long long* addr, int fn, int vt, unsigned long long v) {
+  switch (fn) {
+    case AGG_SUM:
+      if (vt == VT_F64) atomicAdd(reinterpret_cast<double*>(addr), __longlong_as_double(static_cast<long long>(v)));
+      else atomicAdd(addr, v);
+      break;
+    case AGG_COUNT:
+    case AGG_COUNT_STAR: atomicAdd(addr, v); break;
+    case AGG_MIN:
+    case AGG_MAX: {
+      if (vt == VT_F64) {
+        const double x = __longlong_as_double(static_cast<long long>(v));
+        unsigned long long old = *reinterpret_cast<volatile unsigned long long*>(addr);
+        for (;;) {
+          const double cur = __longlong_as_double(static_cast<long long>(old));
+          const bool better = fn == AGG_MIN ? x < cur : x > cur;
+          if (!better) break;
+          const unsigned long long prev = atomicCAS(addr, old, v);
+          if (prev == old) break;
+          old = prev;
+        }
+      } else if (fn == AGG_MIN) {
+        atomicMin(reinterpret_cast<long long*>(addr), static_cast<long long>(v));
+      } else {
+        atomicMax(reinterpret_cast<long long*>(addr), static_cast<long long>(v));
+      }
+      break;
+    }
+  }
+}
+
+// Global slot of a key; claims an empty slot for a new key. Returns
+// UINT64_MAX (and raises GFPDB_ENOMEM) if the table is full.
+__device__ __forceinline__ uint64_t global_slot(const GroupParams& p, uint64_t key) {
+  if (key == kEmptySlot) {
+    if (atomicExch(reinterpret_cast<unsigned long long*>(&p.st->aux[1]), 1ull) == 0ull)
+      atomicAdd(reinterpret_cast<unsigned long long*>(&p.st->aux[0]), 1ull);
+    return p.mask + 1;
+  }
+  uint64_t slot = hash_key(static_cast<int64_t>(key)) & p.mask;
+  for (uint64_t i = 0; i <= p.mask; ++i) {
+    uint64_t s = *reinterpret_cast<volatile uint64_t*>(p.keys + slot);
+    if (s == kEmptySlot) {
+      s = atomicCAS(reinterpret_cast<unsigned long long*>(p.keys + slot), static_cast<unsigned long long>(kEmptySlot),
+                    static_cast<unsigned long long>(key));
+      if (s == kEmptySlot) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&p.st->aux[0]), 1ull);
+        return slot;
+      }
+    }
+    if (s == key) return slot;
+    slot = (slot + 1) & p.mask;
+  }
+  raise_status(p.st, GFPDB_ENOMEM, 20);
+  return UINT64_MAX;
+}
+
+__device__ __forceinline__ unsigned long long row_value(const GroupParams& p, const AccDev& a, int64_t row) {
+  if (a.fn == AGG_COUNT || a.fn == AGG_COUNT_STAR) return 1ull;
+  return static_cast<unsigned long long>(operand_row(p.prog, p.cols, a.in, row, p.st));
+}
+
+__global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __grid_constant__ GroupParams p) {
+  extern __shared__ unsigned long long s_mem[];
+  uint64_t* s_keys = reinterpret_cast<uint64_t*>(s_mem);
+  unsigned long long* s_acc = s_mem + p.sm_slots;
+  const int sm_mask = p.sm_slots - 1;
+  if (p.use_smem) {
+    for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads) {
+      s_keys[i] = kEmptySlot;
+      for (int a = 0; a < p.n_acc; ++a) s_acc[i * p.n_acc + a] = acc_init(p.acc[a].fn, p.acc[a].vt);
+    }
+    __syncthreads();
+  }
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * kGroupThreads;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * kGroupThreads + threadIdx.x; r < p.n_rows; r += stride) {
+    const uint64_t key = pack_key(p, r);
+    int found = -1;
+    if (p.use_smem && key != kEmptySlot) {
+      int slot = static_cast<int>(hash_key(static_cast<int64_t>(key)) & sm_mask);
+      for (int i = 0; i < 16; ++i) {
+        uint64_t s = *reinterpret_cast<volatile uint64_t*>(s_keys + slot);
+        if (s == kEmptySlot) {
+          s = atomicCAS(reinterpret_cast<unsigned long long*>(s_keys + slot),
+                        static_cast<unsigned long long>(kEmptySlot), static_cast<unsigned long long>(key));
+          if (s == kEmptySlot) s = key;
+        }
+        if (s == key) {
+          found = slot;
+          break;
+        }
+        slot = (slot + 1) & sm_mask;
+      }
+    }
+    if (found >= 0) {
+      for (int a = 0; a < p.n_acc; ++a)
+        acc_combine(s_acc + found * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, row_value(p, p.acc[a], r));
+    } else {
+      const uint64_t g = global_slot(p, key);
+      if (g != UINT64_MAX)
+        for (int a = 0; a < p.n_acc; ++a)
+          acc_combine(p.accs + g * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, row_value(p, p.acc[a], r));
+    }
+  }
+  if (p.use_smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads) {
+      const uint64_t key = s_keys[i];
+      if (key == kEmptySlot) continue;
+      const uint64_t g = global_slot(p, key);
+      if (g == UINT64_MAX) continue;
+      for (int a = 0; a < p.n_acc; ++a) acc_combine(p.accs + g * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, s_acc[i * p.n_acc + a]);
+    }
+  }
+}
+
+__global__ void group_init_kernel(uint64_t* keys, unsigned long long* accs, uint64_t n_slots, AccDev acc0, int n_acc,
+                                  const int8_t* fns, const int8_t* vts) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
+    keys[i] = kEmptySlot;
+    for (int a = 0; a < n_acc; ++a) accs[i * n_acc + a] = acc_init(fns[a], vts[a]);
+  }
+}
+
+// Move every group of an old table into a larger one (accumulators copied).
+__global__ void group_rehash_kernel(const uint64_t* old_keys, const unsigned long long* old_accs, uint64_t old_cap,
+                                    uint64_t* keys, unsigned long long* accs, uint64_t mask, int n_acc, DevStatus* st) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i <= old_cap; i += stride) {
+    const uint64_t key = old_keys[i];
+    uint64_t dst;
+    if (i == old_cap) {
+      dst = mask + 1;  // special slot stays special
+      if (key == kEmptySlot) {
+        // the special slot's key word is never written; copy its accumulators
+      }
+    } else {
+      if (key == kEmptySlot) continue;
+      uint64_t slot = hash_key(static_cast<int64_t>(key)) & mask;
+      bool ok = false;
+      for (uint64_t k = 0; k <= mask; ++k) {
+        const unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long*>(keys + slot),
+                                                  static_cast<unsigned long long>(kEmptySlot),
+                                                  static_cast<unsigned long long>(key));
+        if (prev == kEmptySlot) {
+          ok = true;
+          break;
+        }
+        slot = (slot + 1) & mask;
+      }
+      if (!ok) {
+        raise_status(st, GFPDB_ENOMEM, 21);
+        continue;
+      }
+      dst = slot;
+    }
+    for (int a = 0; a < n_acc; ++a) accs[dst * n_acc + a] = old_accs[i * n_acc + a];
+  }
+}
+
+struct OutAggDev {
+  int8_t kind;  // 0: copy accumulator, 1: avg = sum / count
+  int8_t out_type;  // DType code of the output column
+  int8_t vt;
+  int8_t pad;
+  int32_t a0, a1;  // accumulator indices
+  void* dst;
+};
+
+struct FinalParams {
+  const uint64_t* keys;
+  const unsigned long long* accs;
+  uint64_t cap;  // special slot at index cap
+  int32_t special_used;
+  int32_t n_acc;
+  int32_t n_keys;
+  int32_t n_out;
+  int32_t key_bits[2];
+  void* key_dst[2];
+  int32_t key_type[2];
+  OutAggDev outs[kMaxAggs];
+  unsigned long long* counter;
+};
+
+__device__ __forceinline__ void store_typed(void* dst, int64_t pos, int type, int64_t v) {
+  if (type == CT_I64 || type == CT_F64) static_cast<long long*>(dst)[pos] = v;
+  else static_cast<int*>(dst)[pos] = static_cast<int32_t>(v);
+}
+
+__global__ void __launch_bounds__(256) group_finalize_kernel(const __grid_constant__ FinalParams p) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t n_slots = p.cap + 1;
+  const uint64_t warp0 = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t base = warp0 * 32; base < n_slots; base += n_warps * 32) {
+    const uint64_t i = base + lane;
+    bool live = false;
+    uint64_t key = 0;
+    if (i < p.cap) {
+      key = p.keys[i];
+      live = key != kEmptySlot;
+    } else if (i == p.cap) {
+      key = kEmptySlot;
+      live = p.special_used != 0;
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, live);
+    if (m == 0) continue;
+    unsigned long long at = 0;
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) at = atomicAdd(p.counter, static_cast<unsigned long long>(__popc(m)));
+    at = __shfl_sync(0xffffffffu, at, leader);
+    if (!live) continue;
+    const int64_t pos = static_cast<int64_t>(at) + __popc(m & ((1u << lane) - 1u));
+    if (p.n_keys == 1) {
+      const int64_t v = p.key_bits[0] == 64 ? static_cast<int64_t>(key) : static_cast<int32_t>(static_cast<uint32_t>(key));
+      store_typed(p.key_dst[0], pos, p.key_type[0], v);
+    } else {
+      store_typed(p.key_dst[0], pos, p.key_type[0], static_cast<int32_t>(static_cast<uint32_t>(key >> 32)));
+      store_typed(p.key_dst[1], pos, p.key_type[1], static_cast<int32_t>(static_cast<uint32_t>(key)));
+    }
+    for (int j = 0; j < p.n_out; ++j) {
+      const OutAggDev& o = p.outs[j];
+      const unsigned long long a = p.accs[i * p.n_acc + o.a0];
+      if (o.kind == 0) {
+        store_typed(o.dst, pos, o.out_type, static_cast<int64_t>(a));
+      } else {
+        const unsigned long long c = p.accs[i * p.n_acc + o.a1];
+        const double s = o.vt == VT_F64 ? __longlong_as_double(static_cast<long long>(a))
+                                        : static_cast<double>(static_cast<long long>(a));
+        const double avg = c == 0 ? 0.0 : s / static_cast<double>(c);
+        static_cast<double*>(o.dst)[pos] = avg;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- string dictionary
+
+struct DictDev {
+  uint64_t* slot_hash;
+  uint32_t* slot_code;  // 0 = not published yet, else code + 1
+  int64_t* code_off;
+  int32_t* code_len;
+  uint8_t* heap;
+  uint64_t mask;
+  int64_t code_cap;
+  int64_t heap_cap;
+  DevStatus* st;  // aux[0]: codes, aux[1]: heap bytes
+};
+
+__device__ __forceinline__ uint64_t dict_hash(const uint8_t* s, int32_t n) {
+  uint64_t h = hash_bytes(s, n);
+  return h == kEmptySlot ? kEmptySlot - 1 : h;
+}
+
+__global__ void __launch_bounds__(256) dict_encode_kernel(const int32_t* __restrict__ offs, const uint8_t* __restrict__ bytes,
+                                                          int64_t n, int32_t* __restrict__ out_codes, DictDev d) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int32_t b = offs[r];
+    const int32_t len = offs[r + 1] - b;
+    const uint8_t* str = bytes + b;
+    const uint64_t h = dict_hash(str, len);
+    uint64_t slot = h & d.mask;
+    int32_t code = -1;
+    for (uint64_t i = 0; i <= d.mask && code < 0; ++i, slot = (slot + 1) & d.mask) {
+      uint64_t s = *reinterpret_cast<volatile uint64_t*>(d.slot_hash + slot);
+      if (s == kEmptySlot) {
+        s = atomicCAS(reinterpret_cast<unsigned long long*>(d.slot_hash + slot),
+                      static_cast<unsigned long long>(kEmptySlot), static_cast<unsigned long long>(h));
+        if (s == kEmptySlot) {
+          // This thread owns the new entry: store its bytes, then publish.
+          const unsigned long long c = atomicAdd(reinterpret_cast<unsigned long long*>(&d.st->aux[0]), 1ull);
+          const unsigned long long off = atomicAdd(reinterpret_cast<unsigned long long*>(&d.st->aux[1]),
+                                                   static_cast<unsigned long long>(len));
+          if (static_cast<int64_t>(c) >= d.code_cap || static_cast<int64_t>(off) + len > d.heap_cap) {
+            raise_status(d.st, GFPDB_ENOMEM, 30);
+            st_release32(d.slot_code + slot, 0xFFFFFFFFu);
+            break;
+          }
+          for (int32_t k = 0; k < len; ++k) d.heap[off + k] = str[k];
+          d.code_off[c] = static_cast<int64_t>(off);
+          d.code_len[c] = len;
+          __threadfence();
+          st_release32(d.slot_code + slot, static_cast<uint32_t>(c) + 1u);
+          code = static_cast<int32_t>(c);
+          break;
+        }
+      }
+      if (s != h) continue;
+      // Same hash: wait (bounded) until the owner has published, then compare bytes.
+      uint32_t pub = 0;
+      for (uint32_t spin = 0; spin < kDictSpinLimit; ++spin) {
+        pub = ld_acquire32(d.slot_code + slot);
+        if (pub != 0) break;
+        __nanosleep(32);
+      }
+      if (pub == 0) {
+        raise_status(d.st, GFPDB_ETIMEDOUT, 31);
+        break;
+      }
+      if (pub == 0xFFFFFFFFu) break;  // owner ran out of space; error already raised
+      const int32_t c = static_cast<int32_t>(pub - 1u);
+      if (d.code_len[c] != len) continue;
+      const uint8_t* other = d.heap + d.code_off[c];
+      bool eq = true;
+      for (int32_t k = 0; eq && k < len; ++k) eq = other[k] == str[k];
+      if (eq) code = c;
+    }
+    if (code < 0) raise_status(d.st, GFPDB_ENOMEM, 32);
+    out_codes[r] = code < 0 ? 0 : code;
+  }
+}
+
+__global__ void dict_rehash_kernel(DictDev d, int64_t n_codes) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < n_codes; c += stride) {
+    const uint64_t h = dict_hash(d.heap + d.code_off[c], d.code_len[c]);
+    uint64_t slot = h & d.mask;
+    for (uint64_t i = 0; i <= d.mask; ++i, slot = (slot + 1) & d.mask) {
+      const unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long*>(d.slot_hash + slot),
+                                                static_cast<unsigned long long>(kEmptySlot),
+                                                static_cast<unsigned long long>(h));
+      if (prev == kEmptySlot) {
+        d.slot_code[slot] = static_cast<uint32_t>(c) + 1u;
+        break;
+      }
+    }
+  }
+}
+
+__global__ void dict_lengths_kernel(const int32_t* codes, int64_t n, const int32_t* code_len, int32_t* lens) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride)
+    lens[r] = code_len[codes[r]];
+}
+
+__global__ void dict_copy_kernel(const int32_t* codes, int64_t n, const int64_t* code_off, const uint8_t* heap,
+                                 const int32_t* offs, uint8_t* out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const uint8_t* src = heap + code_off[codes[r]];
+    const int32_t o = offs[r], len = offs[r + 1] - o;
+    for (int32_t k = 0; k < len; ++k) out[o + k] = src[k];
+  }
+}
+
+int grid_for(int64_t n) {
+  int64_t blocks = (n + 255) / 256;
+  int64_t cap = static_cast<int64_t>(num_sms()) * 8;
+  if (blocks > cap) blocks = cap;
+  return static_cast<int>(blocks < 1 ? 1 : blocks);
+}
+
+uint64_t next_pow2(uint64_t x) {
+  uint64_t c = 1;
+  while (c < x) c <<= 1;
+  return c;
+}
+
+DevStatus read_status(const DevStatus* d, cudaStream_t s) {
+  DevStatus h;
+  GF_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+  sync(s);
+  return h;
+}
+
+class StringDict {
+ public:
+  BufferPtr slot_hash, slot_code, code_off, code_len, heap, status;
+  uint64_t cap = 0;
+  int64_t code_cap = 0, heap_cap = 0;
+  int64_t codes_upper = 0, heap_upper = 0;  // host-side upper bounds
+
+  DictDev dev() const {
+    DictDev d;
+    d.slot_hash = slot_hash->as<uint64_t>();
+    d.slot_code = slot_code->as<uint32_t>();
+    d.code_off = code_off->as<int64_t>();
+    d.code_len = code_len->as<int32_t>();
+    d.heap = heap->as<uint8_t>();
+    d.mask = cap - 1;
+    d.code_cap = code_cap;
+    d.heap_cap = heap_cap;
+    d.st = status->as<DevStatus>();
+    return d;
+  }
+
+  void ensure(int64_t more_codes, int64_t more_bytes, cudaStream_t s) {
+    if (!status) {
+      status = make_buffer(sizeof(DevStatus), s);
+      GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    }
+    int64_t codes_real = 0, bytes_real = 0;
+    const bool grow_slots = static_cast<uint64_t>(2 * (codes_upper + more_codes)) > cap;
+    const bool grow_codes = codes_upper + more_codes > code_cap;
+    const bool grow_heap = heap_upper + more_bytes > heap_cap;
+    if (!(grow_slots || grow_codes || grow_heap)) return;
+    if (cap > 0) {
+      DevStatus h = read_status(status->as<DevStatus>(), s);
+      raise_device_status(h, "string dictionary");
+      codes_real = h.aux[0];
+      bytes_real = h.aux[1];
+      codes_upper = codes_real;
+      heap_upper = bytes_real;
+    }
+    const int64_t need_codes = codes_upper + more_codes;
+    const int64_t need_bytes = heap_upper + more_bytes;
+    if (need_codes > code_cap) {
+      int64_t nc = static_cast<int64_t>(next_pow2(static_cast<uint64_t>(need_codes < 1024 ? 1024 : need_codes)));
+      auto off = make_buffer(nc * 8, s), len = make_buffer(nc * 4, s);
+      if (codes_real > 0) {
+        GF_CUDA(cudaMemcpyAsync(off->data(), code_off->data(), codes_real * 8, cudaMemcpyDeviceToDevice, s));
+        GF_CUDA(cudaMemcpyAsync(len->data(), code_len->data(), codes_real * 4, cudaMemcpyDeviceToDevice, s));
+      }
+      code_off = off;
+      code_len = len;
+      code_cap = nc;
+    }
+    if (need_bytes > heap_cap) {
+      int64_t nb = static_cast<int64_t>(next_pow2(static_cast<uint64_t>(need_bytes < 4096 ? 4096 : need_bytes)));
+      auto hp = make_buffer(nb, s);
+      if (bytes_real > 0) GF_CUDA(cudaMemcpyAsync(hp->data(), heap->data(), bytes_real, cudaMemcpyDeviceToDevice, s));
+      heap = hp;
+      heap_cap = nb;
+    }
+    uint64_t want = next_pow2(static_cast<uint64_t>(2 * need_codes < 1024 ? 1024 : 2 * need_codes));
+    if (want > cap) {
+      slot_hash = make_buffer(static_cast<int64_t>(want) * 8, s);
+      slot_code = make_buffer(static_cast<int64_t>(want) * 4, s);
+      GF_CUDA(cudaMemsetAsync(slot_hash->data(), 0xFF, want * 8, s));
+      GF_CUDA(cudaMemsetAsync(slot_code->data(), 0, want * 4, s));
+      cap = want;
+      if (codes_real > 0) {
+        dict_rehash_kernel<<<grid_for(codes_real), 256, 0, s>>>(dev(), codes_real);
+        after_launch("dict_rehash_kernel");
+      }
+    }
+  }
+
+  BufferPtr encode(const Column& c, cudaStream_t s) {
+    const int64_t n = c.length;
+    int32_t ends[2] = {0, 0};
+    if (n > 0) {
+      GF_CUDA(cudaMemcpyAsync(&ends[0], c.offsets, 4, cudaMemcpyDeviceToHost, s));
+      GF_CUDA(cudaMemcpyAsync(&ends[1], c.offsets + n, 4, cudaMemcpyDeviceToHost, s));
+      sync(s);
+    }
+    ensure(n, ends[1] - ends[0], s);
+    auto codes = make_buffer(n * 4, s);
+    if (n > 0) {
+      dict_encode_kernel<<<grid_for(n), 256, 0, s>>>(c.offsets, static_cast<const uint8_t*>(c.data), n,
+                                                     codes->as<int32_t>(), dev());
+      after_launch("dict_encode_kernel");
+    }
+    codes_upper += n;
+    heap_upper += ends[1] - ends[0];
+    return codes;
+  }
+
+  ColumnPtr decode(const int32_t* codes, int64_t n, cudaStream_t s) {
+    auto offs = make_buffer((n + 1) * 4, s);
+    int64_t total = 0;
+    if (n > 0) {
+      auto lens = make_buffer(n * 4, s);
+      dict_lengths_kernel<<<grid_for(n), 256, 0, s>>>(codes, n, code_len->as<int32_t>(), lens->as<int32_t>());
+      after_launch("dict_lengths_kernel");
+      total = exclusive_scan_i32(lens->as<int32_t>(), offs->as<int32_t>(), n, s);
+    } else {
+      GF_CUDA(cudaMemsetAsync(offs->data(), 0, 4, s));
+    }
+    auto bytes = make_buffer(total, s);
+    if (n > 0 && total > 0) {
+      dict_copy_kernel<<<grid_for(n), 256, 0, s>>>(codes, n, code_off->as<int64_t>(), heap->as<uint8_t>(),
+                                                   offs->as<int32_t>(), bytes->as<uint8_t>());
+      after_launch("dict_copy_kernel");
+    }
+    return make_utf8_column(n, offs, bytes);
+  }
+};
+
+}  // namespace
+
+class GroupTable {
+ public:
+  std::vector<std::string> group_cols;
+  std::vector<GroupAggregate> aggs;
+  int64_t hint = 0;
+
+  bool compiled = false;
+  std::vector<DType> key_types;
+  std::vector<int32_t> key_bits;
+  std::vector<AccDev> accs;           // internal accumulators
+  std::vector<OutAggDev> outs;        // user aggregates -> accumulators
+  std::vector<DType> out_types;
+  Program prog{};
+  ColumnSlots slots;
+  std::vector<std::unique_ptr<StringDict>> dicts;  // per key column (utf8 only)
+
+  BufferPtr keys, accbuf, status, fnvt;
+  uint64_t cap = 0;
+  int64_t groups_upper = 0;
+
+  void compile(const TupleSet& ts) {
+    if (group_cols.empty()) fail(GFPDB_EUNSUPPORTED, "group-by without group columns (use an aggregate)");
+    if (group_cols.size() > 2) fail(GFPDB_EUNSUPPORTED, "group-by over more than two key columns");
+    int bits = 0;
+    for (auto& g : group_cols) {
+      DType t = ts.field(ts.require_column(g)).type;
+      if (t == DType::Float64) fail(GFPDB_EUNSUPPORTED, "float64 group keys");
+      key_types.push_back(t);
+      int b = t == DType::Int64 ? 64 : 32;
+      key_bits.push_back(b);
+      bits += b;
+      dicts.emplace_back(t == DType::Utf8 ? new StringDict() : nullptr);
+    }
+    if (bits > 64) fail(GFPDB_EUNSUPPORTED, "group keys wider than 64 bits");
+    std::memset(&prog, 0, sizeof(prog));
+    for (auto& a : aggs) {
+      OutAggDev o{};
+      auto add_acc = [&](int8_t fn, int8_t vt, Operand in) {
+        if (static_cast<int>(accs.size()) >= kMaxAggs) fail(GFPDB_EUNSUPPORTED, "too many aggregates");
+        AccDev d{};
+        d.fn = fn;
+        d.vt = vt;
+        d.in = in;
+        accs.push_back(d);
+        return static_cast<int32_t>(accs.size() - 1);
+      };
+      if (a.fn == AGG_COUNT_STAR || (a.fn == AGG_COUNT && !a.expr)) {
+        Operand none{};
+        none.kind = OPND_LIT;
+        o.kind = 0;
+        o.a0 = add_acc(AGG_COUNT_STAR, VT_I64, none);
+        o.out_type = static_cast<int8_t>(DType::Int64);
+        out_types.push_back(DType::Int64);
+      } else {
+        if (!a.expr) fail(GFPDB_EINVAL, "aggregate '" + a.name + "' needs an input expression");
+        DType in_t;
+        Operand in = compile_value(a.expr, ts.fields(), prog, slots, &in_t);
+        const int8_t vt = in_t == DType::Float64 ? VT_F64 : VT_I64;
+        if (a.fn == AGG_SUM) {
+          o.a0 = add_acc(AGG_SUM, vt, in);
+          DType ot = vt == VT_F64 ? DType::Float64 : DType::Int64;
+          o.out_type = static_cast<int8_t>(ot);
+          out_types.push_back(ot);
+        } else if (a.fn == AGG_COUNT) {
+          o.a0 = add_acc(AGG_COUNT, VT_I64, in);
+          o.out_type = static_cast<int8_t>(DType::Int64);
+          out_types.push_back(DType::Int64);
+        } else if (a.fn == AGG_MIN || a.fn == AGG_MAX) {
+          o.a0 = add_acc(a.fn, vt, in);
+          o.out_type = static_cast<int8_t>(in_t);
+          out_types.push_back(in_t);
+        } else {  // AVG: sum and count, divided at finalisation
+          o.kind = 1;
+          o.vt = vt;
+          o.a0 = add_acc(AGG_SUM, vt, in);
+          Operand none{};
+          none.kind = OPND_LIT;
+          o.a1 = add_acc(AGG_COUNT_STAR, VT_I64, none);
+          o.out_type = static_cast<int8_t>(DType::Float64);
+          out_types.push_back(DType::Float64);
+        }
+      }
+      outs.push_back(o);
+    }
+    compiled = true;
+  }
+
+  void init_table(uint64_t new_cap, cudaStream_t s) {
+    const int na = static_cast<int>(accs.size());
+    auto nk = make_buffer(static_cast<int64_t>(new_cap + 1) * 8, s);
+    auto na_buf = make_buffer(static_cast<int64_t>(new_cap + 1) * 8 * (na > 0 ? na : 1), s);
+    if (!fnvt) {
+      fnvt = make_buffer(2 * kMaxAggs, s);
+      int8_t h[2 * kMaxAggs] = {};
+      for (int a = 0; a < na; ++a) {
+        h[a] = accs[a].fn;
+        h[kMaxAggs + a] = accs[a].vt;
+      }
+      GF_CUDA(cudaMemcpyAsync(fnvt->data(), h, sizeof(h), cudaMemcpyHostToDevice, s));
+      sync(s);
+    }
+    AccDev dummy{};
+    group_init_kernel<<<grid_for(static_cast<int64_t>(new_cap + 1)), 256, 0, s>>>(
+        nk->as<uint64_t>(), na_buf->as<unsigned long long>(), new_cap + 1, dummy, na, fnvt->as<int8_t>(),
+        fnvt->as<int8_t>() + kMaxAggs);
+    after_launch("group_init_kernel");
+    if (!status) {
+      status = make_buffer(sizeof(DevStatus), s);
+      GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    }
+    if (cap > 0) {
+      group_rehash_kernel<<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(
+          keys->as<uint64_t>(), accbuf->as<unsigned long long>(), cap, nk->as<uint64_t>(),
+          na_buf->as<unsigned long long>(), new_cap - 1, na, status->as<DevStatus>());
+      after_launch("group_rehash_kernel");
+    }
+    keys = nk;
+    accbuf = na_buf;
+    cap = new_cap;
+  }
+
+  void update(const TupleSet& ts, cudaStream_t s) {
+    if (!compiled) compile(ts);
+    const int64_t n = ts.num_rows();
+    if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "group-by batch must have fewer than 2^31 rows");
+    // Size the table so that it stays at most half full.
+    int64_t bound = groups_upper + n;
+    if (hint > 0 && bound > hint) bound = groups_upper > hint ? groups_upper : hint;
+    uint64_t want = next_pow2(static_cast<uint64_t>(2 * bound < 1024 ? 1024 : 2 * bound));
+    if (want > cap && cap > 0) {
+      // Upper bound says grow: read the real group count first.
+      DevStatus h = read_status(status->as<DevStatus>(), s);
+      raise_device_status(h, "group-by");
+      groups_upper = h.aux[0];
+      bound = groups_upper + n;
+      if (hint > 0 && bound > hint) bound = groups_upper > hint ? groups_upper : hint;
+      want = next_pow2(static_cast<uint64_t>(2 * bound < 1024 ? 1024 : 2 * bound));
+    }
+    if (want > cap) init_table(want, s);
+    if (n == 0) return;
+
+    GroupParams* pp = new GroupParams;
+    std::unique_ptr<GroupParams> holder(pp);
+    GroupParams& p = *pp;
+    std::memset(&p, 0, sizeof(p));
+    p.n_rows = n;
+    p.n_keys = static_cast<int32_t>(group_cols.size());
+    p.n_acc = static_cast<int32_t>(accs.size());
+    std::vector<BufferPtr> code_bufs;
+    for (int k = 0; k < p.n_keys; ++k) {
+      const auto& c = ts.column(group_cols[k]);
+      if (c->type != key_types[k]) fail(GFPDB_EINVAL, "group key column changed type between batches");
+      p.key_bits[k] = key_bits[k];
+      if (c->type == DType::Utf8) {
+        auto codes = dicts[k]->encode(*c, s);
+        code_bufs.push_back(codes);
+        p.key_cols[k] = DevCol{codes->data(), nullptr, CT_I32, 0};
+      } else {
+        p.key_cols[k] = DevCol{c->data, nullptr, static_cast<int32_t>(c->type), 0};
+      }
+    }
+    for (int a = 0; a < p.n_acc; ++a) p.acc[a] = accs[a];
+    bind_columns(slots, ts, p.cols, kMaxCols);
+    p.prog = prog;
+    p.keys = keys->as<uint64_t>();
+    p.accs = accbuf->as<unsigned long long>();
+    p.mask = cap - 1;
+    p.st = status->as<DevStatus>();
+    // Shared-memory pre-aggregation unless the caller expects many groups.
+    const int per_slot = 8 + 8 * p.n_acc;
+    int sm_slots = 1024;
+    while (sm_slots * per_slot > 48 * 1024) sm_slots >>= 1;
+    p.use_smem = (hint == 0 || hint <= 4096) ? 1 : 0;
+    p.sm_slots = sm_slots;
+    const size_t dyn = p.use_smem ? static_cast<size_t>(sm_slots) * per_slot : 0;
+    int64_t blocks = (n + kGroupThreads * 16 - 1) / (kGroupThreads * 16);
+    int64_t max_blocks = static_cast<int64_t>(num_sms()) * 4;
+    if (blocks > max_blocks) blocks = max_blocks;
+    if (blocks < 1) blocks = 1;
+    ProfScope prof("group_update_kernel", s);
+    group_update_kernel<<<static_cast<int>(blocks), kGroupThreads, dyn, s>>>(p);
+    after_launch("group_update_kernel");
+    double w = 0;
+    for (int k = 0; k < p.n_keys; ++k) w += p.key_bits[k] / 8;
+    for (size_t i = 0; i < slots.types.size(); ++i) w += dtype_width(slots.types[i]);
+    prof.stop(static_cast<double>(n) * w);
+    groups_upper += n;
+    if (hint > 0 && groups_upper > hint) groups_upper = hint;
+  }
+
+  TupleSetPtr finalize(const TupleSet* schema_src, cudaStream_t s) {
+    std::vector<Field> fields;
+    for (size_t k = 0; k < group_cols.size(); ++k)
+      fields.push_back(Field{group_cols[k], compiled ? key_types[k] : DType::Int64});
+    for (size_t j = 0; j < aggs.size(); ++j)
+      fields.push_back(Field{aggs[j].name, compiled ? out_types[j] : DType::Int64});
+    if (!compiled || cap == 0) return TupleSet::make_empty(fields, s);
+    (void)schema_src;
+    DevStatus h = read_status(status->as<DevStatus>(), s);
+    raise_device_status(h, "group-by");
+    for (auto& d : dicts)
+      if (d) raise_device_status(read_status(d->status->as<DevStatus>(), s), "string dictionary");
+    const int64_t n_groups = h.aux[0];
+    FinalParams fp;
+    std::memset(&fp, 0, sizeof(fp));
+    fp.keys = keys->as<uint64_t>();
+    fp.accs = accbuf->as<unsigned long long>();
+    fp.cap = cap;
+    fp.special_used = h.aux[1] != 0;
+    fp.n_acc = static_cast<int32_t>(accs.size());
+    fp.n_keys = static_cast<int32_t>(group_cols.size());
+    std::vector<BufferPtr> key_out(group_cols.size());
+    for (size_t k = 0; k < group_cols.size(); ++k) {
+      DType t = key_types[k] == DType::Utf8 ? DType::Int32 : key_types[k];
+      key_out[k] = make_buffer(n_groups * dtype_width(t), s);
+      fp.key_dst[k] = key_out[k]->data();
+      fp.key_type[k] = static_cast<int32_t>(t);
+      fp.key_bits[k] = key_bits[k];
+    }
+    std::vector<BufferPtr> agg_out(aggs.size());
+    fp.n_out = static_cast<int32_t>(aggs.size());
+    for (size_t j = 0; j < aggs.size(); ++j) {
+      agg_out[j] = make_buffer(n_groups * dtype_width(out_types[j]), s);
+      fp.outs[j] = outs[j];
+      fp.outs[j].dst = agg_out[j]->data();
+    }
+    auto counter = make_buffer(8, s);
+    GF_CUDA(cudaMemsetAsync(counter->data(), 0, 8, s));
+    fp.counter = counter->as<unsigned long long>();
+    group_finalize_kernel<<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(fp);
+    after_launch("group_finalize_kernel");
+    std::vector<ColumnPtr> cols;
+    for (size_t k = 0; k < group_cols.size(); ++k) {
+      if (key_types[k] == DType::Utf8) cols.push_back(dicts[k]->decode(key_out[k]->as<int32_t>(), n_groups, s));
+      else cols.push_back(make_fixed_column(key_types[k], n_groups, key_out[k]));
+    }
+    for (size_t j = 0; j < aggs.size(); ++j) cols.push_back(make_fixed_column(out_types[j], n_groups, agg_out[j]));
+    return TupleSet::make(std::move(fields), std::move(cols), n_groups);
+  }
+};
+
+std::shared_ptr<GroupTable> group_table_create(const std::vector<std::string>& group_cols,
+                                               const std::vector<GroupAggregate>& aggs, int64_t groups_hint) {
+  auto g = std::make_shared<GroupTable>();
+  g->group_cols = group_cols;
+  g->aggs = aggs;
+  g->hint = groups_hint;
+  return g;
+}
+
+void group_table_update(GroupTable& g, const TupleSet& batch, cudaStream_t s) { g.update(batch, s); }
+
+TupleSetPtr group_table_finalize(GroupTable& g, cudaStream_t s) { return g.finalize(nullptr, s); }
+
+}  // namespace gfpdb

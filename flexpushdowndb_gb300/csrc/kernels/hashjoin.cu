@@ -1,0 +1,185 @@
+// Hash join build and probe on an open-addressing table.
+//
+// Replaces the hash table of Arrow's hashjoin exec node that
+// HashJoinArrowKernel drives (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:252,334)
+// and the native TupleSetIndex unordered_multimap
+// (fpdb-tuple/src/TupleSetIndex.cpp:44-88,238-245).
+//
+// Table: a power-of-two array of 64-bit slots, each (tag << 32 | build row),
+// all-ones when empty, filled with one 64-bit atomicCAS per build row and
+// linear probing. For 32-bit keys the tag is the key itself, so a probe
+// decides a match from the slot alone; for 64-bit keys the tag is the high
+// half of the hash and a tag hit is confirmed against the build key column.
+// Duplicate build keys occupy separate slots (multimap semantics). Probing
+// is one thread per probe row walking its run; matches leave through a
+// warp-aggregated atomic cursor as (probe row, build row) pairs that a
+// gather turns into output columns.
+#include "common.cuh"
+#include "launch.h"
+
+namespace gfpdb {
+
+namespace {
+
+__global__ void __launch_bounds__(256)
+    join_build_kernel(DevCol key, int64_t n, uint64_t* __restrict__ slots, uint64_t mask, int key32, DevStatus* st) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  int64_t my_max = 0;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int64_t k = load_int(key, r);
+    const uint64_t h = hash_key(k);
+    const uint32_t tag = key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
+    const uint64_t packed = (static_cast<uint64_t>(tag) << 32) | static_cast<uint32_t>(r);
+    uint64_t slot = h & mask;
+    uint64_t probe = 0;
+    for (; probe <= mask; ++probe) {
+      const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(slots + slot),
+                                               static_cast<unsigned long long>(kEmptySlot),
+                                               static_cast<unsigned long long>(packed));
+      if (old == kEmptySlot) break;
+      slot = (slot + 1) & mask;
+    }
+    if (probe > mask) raise_status(st, GFPDB_ENOMEM, 10);  // table full: cannot happen at load <= 1
+    if (static_cast<int64_t>(probe) > my_max) my_max = static_cast<int64_t>(probe);
+  }
+  // longest probe run, for diagnostics
+  for (int d = 16; d > 0; d >>= 1) {
+    int64_t o = __shfl_down_sync(0xffffffffu, my_max, d);
+    if (o > my_max) my_max = o;
+  }
+  if ((threadIdx.x & 31) == 0 && my_max > 0)
+    atomicMax(reinterpret_cast<unsigned long long*>(&st->aux[0]), static_cast<unsigned long long>(my_max));
+}
+
+__global__ void __launch_bounds__(256)
+    join_probe_kernel(DevCol pkey, int64_t n, const uint64_t* __restrict__ slots, uint64_t mask, DevCol bkey,
+                      int key32, int32_t* __restrict__ out_p, int32_t* __restrict__ out_b, int64_t cap,
+                      DevStatus* st) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(&st->value);
+  for (int64_t base = warp_global * 32; base < n; base += n_warps * 32) {
+    const int64_t r = base + lane;
+    bool active = r < n;
+    int64_t k = 0;
+    uint32_t tag = 0;
+    uint64_t slot = 0;
+    if (active) {
+      k = load_int(pkey, r);
+      const uint64_t h = hash_key(k);
+      tag = key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
+      slot = h & mask;
+    }
+    uint64_t steps = 0;
+    while (__any_sync(0xffffffffu, active)) {
+      bool emit = false;
+      int32_t brow = 0;
+      if (active) {
+        const uint64_t s = __ldg(reinterpret_cast<const unsigned long long*>(slots + slot));
+        if (s == kEmptySlot || ++steps > mask + 1) {
+          active = false;
+        } else {
+          if (static_cast<uint32_t>(s >> 32) == tag) {
+            brow = static_cast<int32_t>(static_cast<uint32_t>(s));
+            emit = key32 ? true : (load_int(bkey, brow) == k);
+          }
+          slot = (slot + 1) & mask;
+        }
+      }
+      const uint32_t em = __ballot_sync(0xffffffffu, emit);
+      if (em != 0) {
+        unsigned long long at = 0;
+        const int leader = __ffs(em) - 1;
+        if (lane == leader) at = atomicAdd(cursor, static_cast<unsigned long long>(__popc(em)));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (emit) {
+          const int64_t pos = static_cast<int64_t>(at) + __popc(em & ((1u << lane) - 1u));
+          if (pos < cap) {
+            out_p[pos] = static_cast<int32_t>(r);
+            out_b[pos] = brow;
+          }
+        }
+      }
+    }
+  }
+}
+
+int grid_for(int64_t n) {
+  int64_t blocks = (n + 255) / 256;
+  int64_t cap = static_cast<int64_t>(num_sms()) * 8;
+  if (blocks > cap) blocks = cap;
+  return static_cast<int>(blocks < 1 ? 1 : blocks);
+}
+
+}  // namespace
+
+void join_build_table(JoinTable& t, double load_factor, cudaStream_t s) {
+  if (!(load_factor > 0.0 && load_factor <= 0.9)) fail(GFPDB_EINVAL, "hash join load factor must be in (0, 0.9]");
+  const int64_t n = t.build->num_rows();
+  if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join build side must have fewer than 2^31 rows");
+  uint64_t cap = 64;
+  while (static_cast<double>(cap) * load_factor < static_cast<double>(n)) cap <<= 1;
+  t.capacity = cap;
+  t.slots = make_buffer(static_cast<int64_t>(cap) * 8 + sizeof(DevStatus), s);
+  GF_CUDA(cudaMemsetAsync(t.slots->data(), 0xFF, cap * 8, s));
+  DevStatus* st = reinterpret_cast<DevStatus*>(t.slots->as<char>() + cap * 8);
+  GF_CUDA(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
+  const auto& kc = t.build->column(t.key_col);
+  t.key_type = kc->type;
+  if (n > 0) {
+    DevCol k{kc->data, nullptr, static_cast<int32_t>(kc->type), 0};
+    const int key32 = kc->type != DType::Int64;
+    ProfScope prof("join_build_kernel", s);
+    join_build_kernel<<<grid_for(n), 256, 0, s>>>(k, n, t.slots->as<uint64_t>(), cap - 1, key32, st);
+    after_launch("join_build_kernel");
+    prof.stop(static_cast<double>(n) * dtype_width(kc->type));
+  }
+}
+
+void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,
+                      BufferPtr* build_idx, int64_t* n_out, cudaStream_t s) {
+  const int64_t n = probe.num_rows();
+  if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join probe batch must have fewer than 2^31 rows");
+  const auto& pc = probe.column(probe_key);
+  if (pc->type == DType::Utf8 || pc->type == DType::Float64)
+    fail(GFPDB_EUNSUPPORTED, "hash join keys must be integer columns");
+  // A 32-bit build key stores the key as the tag; a 64-bit probe key must
+  // then also fit 32 bits to match, which the tag comparison handles because
+  // the tag is the low 32 bits of the sign-extended value and the full value
+  // is compared below when either side is 64-bit.
+  const bool key32 = t.key_type != DType::Int64 && pc->type != DType::Int64;
+  if (!key32 && t.key_type != DType::Int64)
+    fail(GFPDB_EUNSUPPORTED, "int64 probe key against an int32 build key");
+  const auto& bk = t.build->column(t.key_col);
+  DevCol pk{pc->data, nullptr, static_cast<int32_t>(pc->type), 0};
+  DevCol bkc{bk->data, nullptr, static_cast<int32_t>(bk->type), 0};
+  int64_t cap = n > 0 ? n : 1;
+  auto status = make_buffer(sizeof(DevStatus), s);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    *probe_idx = make_buffer(cap * 4, s);
+    *build_idx = make_buffer(cap * 4, s);
+    GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    if (n > 0 && t.build->num_rows() > 0) {
+      ProfScope prof("join_probe_kernel", s);
+      join_probe_kernel<<<grid_for(n), 256, 0, s>>>(pk, n, t.slots->as<uint64_t>(), t.capacity - 1, bkc,
+                                                   key32 ? 1 : 0, (*probe_idx)->as<int32_t>(),
+                                                   (*build_idx)->as<int32_t>(), cap, status->as<DevStatus>());
+      after_launch("join_probe_kernel");
+      prof.stop(static_cast<double>(n) * dtype_width(pc->type));
+    }
+    DevStatus hs;
+    GF_CUDA(cudaMemcpyAsync(&hs, status->data(), sizeof(hs), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    raise_device_status(hs, "hash join probe");
+    if (hs.value <= cap) {
+      *n_out = hs.value;
+      return;
+    }
+    if (hs.value >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join output exceeds 2^31 rows");
+    cap = hs.value;  // many-to-many: rerun with the exact output size
+  }
+  fail(GFPDB_EDEVICE, "hash join output size changed between passes");
+}
+
+}  // namespace gfpdb

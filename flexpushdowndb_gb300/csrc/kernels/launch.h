@@ -1,0 +1,110 @@
+// Host-side entry points of the CUDA kernels (implemented in the .cu files
+// of this directory). Everything here runs on the caller's stream.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../host/expr.h"
+#include "../host/tupleset.h"
+
+namespace gfpdb {
+
+// ------------------------------------------------------------- gather.cu
+
+// Concatenate utf8 columns into one, rebasing offsets.
+ColumnPtr concat_utf8(const std::vector<const Column*>& parts, cudaStream_t s);
+
+// Gather rows `idx[0..n)` of each source column into new columns. All
+// fixed-width columns are gathered by one launch; utf8 columns take a length
+// pass, a prefix sum and a byte copy.
+struct GatherSpec {
+  const Column* src;
+  const int32_t* idx;  // row ids into src
+};
+std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s);
+
+// Exclusive prefix sum of n int32 values into n+1 int32 offsets (offsets[n] =
+// total). Returns the total (synchronizes the stream).
+int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
+
+// ------------------------------------------------------------- bloom.cu
+
+struct BloomFilterDev {
+  BufferPtr blocks;     // num_blocks * 8 uint32 words
+  int64_t num_blocks = 0;
+  int64_t num_keys = 0;
+  int32_t num_hashes = 3;
+  int32_t bits_per_key = 10;
+  bool valid = true;
+};
+using BloomPtr = std::shared_ptr<const BloomFilterDev>;
+
+BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_per_key, int32_t num_hashes,
+                     cudaStream_t s);
+
+// ------------------------------------------------------------- select.cu
+
+struct BloomProbe {
+  BloomPtr bloom;
+  std::string column;
+};
+
+struct SelectStats {
+  int64_t rows_in = 0;
+  int64_t rows_out = 0;
+};
+
+// Fused predicate + bloom probes + stable compaction + projection.
+// `project` lists output column names (empty + all_columns = every column).
+TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const std::vector<BloomProbe>& probes,
+                        const std::vector<std::string>& project, bool all_columns, cudaStream_t s,
+                        SelectStats* stats = nullptr);
+
+// ---------------------------------------------------------- hashjoin.cu
+
+struct JoinTable {
+  BufferPtr slots;          // capacity uint64 (tag << 32 | build row)
+  uint64_t capacity = 0;    // power of two
+  TupleSetPtr build;        // concatenated build side
+  int key_col = -1;
+  DType key_type = DType::Int32;
+  int64_t max_probe = 0;
+};
+
+void join_build_table(JoinTable& t, double load_factor, cudaStream_t s);
+
+// Probe `probe` on column `probe_key`; returns matching (probe row, build
+// row) pairs as two device int32 arrays of length *n_out.
+void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,
+                      BufferPtr* build_idx, int64_t* n_out, cudaStream_t s);
+
+// ------------------------------------------------------------- group.cu
+
+struct GroupAggregate {
+  AggFn fn;
+  std::string name;
+  ExprPtr expr;  // null for count(*)
+  // filled when compiled against the first batch
+  DType in_type = DType::Int64;
+};
+
+class GroupTable;
+std::shared_ptr<GroupTable> group_table_create(const std::vector<std::string>& group_cols,
+                                               const std::vector<GroupAggregate>& aggs, int64_t groups_hint);
+void group_table_update(GroupTable& g, const TupleSet& batch, cudaStream_t s);
+TupleSetPtr group_table_finalize(GroupTable& g, cudaStream_t s);
+
+// --------------------------------------------------------------- csv.cu
+
+struct CsvField {
+  std::string name;
+  DType type;
+  bool decimal = false;  // text with a fractional part -> int64 scaled by 10^scale
+  int32_t scale = 0;
+};
+
+TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, bool has_header,
+                      const std::vector<CsvField>& fields, const std::vector<int>& emit, cudaStream_t s);
+
+}  // namespace gfpdb

@@ -1,0 +1,458 @@
+// Fused selection: predicate (CNF leaf program) + bloom probes + stable
+// compaction + projection in one pass.
+//
+// Replaces, as one kernel, what the reference runs as separate passes per
+// 100k-row batch: Gandiva's selection vector (Filter::computeSelectionVector),
+// the pass-through projector gather (Filter::evaluateBySelectionVector,
+// fpdb-expression-gandiva/src/Filter.cpp:178-225), and the bloom hash / find /
+// arrow::compute::Filter chain (BloomFilterUseKernel::filterRecordBatch,
+// fpdb-executor/src/physical/bloomfilter/BloomFilterUseKernel.cpp:180-207).
+//
+// Work decomposition: persistent CTAs of 256 threads take 2048-row tiles in
+// increasing order from an atomic ticket; each thread owns 8 consecutive rows
+// (one 32-byte sector of an int32 column, read with two 128-bit loads). Leaves
+// and probes are evaluated in order and a later column is only loaded for the
+// rows still alive, so a selective early term saves the DRAM sectors of later
+// columns. Selected rows are ranked with a block scan plus decoupled
+// look-back, giving stable (input-order) output in a single pass; the tile's
+// selected row ids go through shared memory so every output column is written
+// with coalesced stores. Small bloom filters are staged in shared memory once
+// per CTA.
+#include <cstring>
+#include <type_traits>
+
+#include "bloom.cuh"
+#include "eval.cuh"
+#include "launch.h"
+
+namespace gfpdb {
+
+namespace {
+
+constexpr int kSelThreads = 256;
+constexpr int kSelItems = 8;
+constexpr int kSelTile = kSelThreads * kSelItems;
+constexpr int kBloomSmemBudget = 96 * 1024;
+
+struct BloomDev {
+  const uint32_t* blocks;
+  uint32_t num_blocks;
+  int16_t col;
+  int8_t num_hashes;
+  int8_t valid;
+  int32_t smem_word;  // < 0: probe from global memory
+  int32_t pad;
+};
+
+struct OutCol {
+  const void* src;
+  void* dst;
+  int32_t width;
+  int32_t pad;
+};
+
+struct SelectParams {
+  int64_t n_rows;
+  int64_t n_tiles;
+  int32_t n_cols;
+  int32_t n_probes;
+  int32_t n_out;
+  int32_t smem_words;
+  int32_t aligned;
+  int32_t pad;
+  DevCol cols[kMaxCols];
+  BloomDev probes[kMaxBlooms];
+  OutCol outs[kMaxCols];
+  int32_t* out_rowids;
+  uint64_t* tile_status;
+  uint32_t* ticket;
+  DevStatus* status;
+  Program prog;
+};
+
+__device__ __forceinline__ void load8(const DevCol& c, int64_t row0, uint32_t need, bool vec, int64_t v[8]) {
+  if (c.type == CT_I64 || c.type == CT_F64) {
+    const long long* p = static_cast<const long long*>(c.data) + row0;
+    if (vec) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if ((need >> (4 * h)) & 0xFu) {
+          const longlong2 a = __ldg(reinterpret_cast<const longlong2*>(p) + 2 * h);
+          const longlong2 b = __ldg(reinterpret_cast<const longlong2*>(p) + 2 * h + 1);
+          v[4 * h + 0] = a.x;
+          v[4 * h + 1] = a.y;
+          v[4 * h + 2] = b.x;
+          v[4 * h + 3] = b.y;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kSelItems; ++k)
+        if ((need >> k) & 1u) v[k] = __ldg(p + k);
+    }
+  } else {
+    const int* p = static_cast<const int*>(c.data) + row0;
+    if (vec) {
+      const int4 a = __ldg(reinterpret_cast<const int4*>(p));
+      const int4 b = __ldg(reinterpret_cast<const int4*>(p) + 1);
+      v[0] = a.x;
+      v[1] = a.y;
+      v[2] = a.z;
+      v[3] = a.w;
+      v[4] = b.x;
+      v[5] = b.y;
+      v[6] = b.z;
+      v[7] = b.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < kSelItems; ++k)
+        if ((need >> k) & 1u) v[k] = __ldg(p + k);
+    }
+  }
+}
+
+__device__ __forceinline__ void operand8(const SelectParams& p, const Operand& o, int64_t row0, uint32_t need,
+                                         bool vec, int64_t v[8]) {
+  if (o.kind == OPND_COL) {
+    load8(p.cols[o.col], row0, need, vec, v);
+  } else if (o.kind == OPND_LIT) {
+#pragma unroll
+    for (int k = 0; k < kSelItems; ++k) v[k] = o.lit.i;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kSelItems; ++k)
+      if ((need >> k) & 1u) v[k] = eval_prog(p.prog, p.cols, o.prog_begin, o.prog_len, row0 + k, p.status);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t compare8(int op, const int64_t a[8], const int64_t b[8]) {
+  uint32_t r = 0;
+  auto val = [](int64_t x) -> T {
+    if constexpr (std::is_floating_point_v<T>) {
+      return __longlong_as_double(x);
+    } else {
+      return static_cast<T>(x);
+    }
+  };
+  switch (op) {
+    case LO_LT:
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r |= static_cast<uint32_t>(val(a[k]) < val(b[k])) << k;
+      break;
+    case LO_LE:
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r |= static_cast<uint32_t>(val(a[k]) <= val(b[k])) << k;
+      break;
+    case LO_GT:
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r |= static_cast<uint32_t>(val(a[k]) > val(b[k])) << k;
+      break;
+    case LO_GE:
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r |= static_cast<uint32_t>(val(a[k]) >= val(b[k])) << k;
+      break;
+    case LO_EQ:
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r |= static_cast<uint32_t>(val(a[k]) == val(b[k])) << k;
+      break;
+    default:
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r |= static_cast<uint32_t>(val(a[k]) != val(b[k])) << k;
+      break;
+  }
+  return r;
+}
+
+__device__ __forceinline__ uint32_t leaf8(const SelectParams& p, const Leaf& L, int64_t row0, uint32_t need,
+                                          bool vec) {
+  if (need == 0) return 0;
+  if (L.op == LO_TRUE) return need;
+  if (L.op == LO_FALSE) return 0;
+  if (L.op == LO_STR_EQ || L.op == LO_STR_NE) {
+    const DevCol& c = p.cols[L.lhs.col];
+    const uint8_t* bytes = static_cast<const uint8_t*>(c.data);
+    uint32_t r = 0;
+    for (int k = 0; k < kSelItems; ++k) {
+      if (!((need >> k) & 1u)) continue;
+      const int32_t b = c.offsets[row0 + k], e = c.offsets[row0 + k + 1];
+      bool eq = (e - b) == L.str_len;
+      for (int i = 0; eq && i < L.str_len; ++i) eq = bytes[b + i] == static_cast<uint8_t>(p.prog.strpool[L.str_begin + i]);
+      if (eq == (L.op == LO_STR_EQ)) r |= 1u << k;
+    }
+    return r;
+  }
+  int64_t a[8], b[8];
+  operand8(p, L.lhs, row0, need, vec, a);
+  operand8(p, L.rhs, row0, need, vec, b);
+  const uint32_t r = L.cmp_vt == VT_F64 ? compare8<double>(L.op, a, b) : compare8<int64_t>(L.op, a, b);
+  return r & need;
+}
+
+__global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_constant__ SelectParams p) {
+  extern __shared__ uint32_t s_bloom[];
+  __shared__ int32_t s_rows[kSelTile];
+  __shared__ int s_warp[kSelThreads / 32 + 1];
+  __shared__ uint32_t s_tile;
+  __shared__ uint64_t s_base;
+
+  // Stage the small bloom filters in shared memory once per CTA.
+  for (int pi = 0; pi < p.n_probes; ++pi) {
+    const BloomDev& b = p.probes[pi];
+    if (b.smem_word < 0 || !b.valid) continue;
+    const uint4* src = reinterpret_cast<const uint4*>(b.blocks);
+    uint4* dst = reinterpret_cast<uint4*>(s_bloom + b.smem_word);
+    for (uint32_t i = threadIdx.x; i < b.num_blocks * 2; i += kSelThreads) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(p.ticket, 1u);
+    __syncthreads();
+    const int64_t tile = s_tile;
+    if (tile >= p.n_tiles) break;
+    const int64_t row0 = tile * kSelTile + static_cast<int64_t>(threadIdx.x) * kSelItems;
+    const bool full = row0 + kSelItems <= p.n_rows;
+    const bool vec = full && p.aligned;
+    uint32_t mask;
+    if (full) {
+      mask = 0xFFu;
+    } else {
+      const int64_t rem = p.n_rows - row0;
+      mask = rem <= 0 ? 0u : ((1u << rem) - 1u);
+    }
+
+    // Bloom probes (the predicate-transfer chain), most selective first as
+    // the caller ordered them.
+    for (int pi = 0; pi < p.n_probes; ++pi) {
+      const BloomDev& b = p.probes[pi];
+      if (!b.valid || mask == 0) continue;
+      int64_t keys[8];
+      load8(p.cols[b.col], row0, mask, vec, keys);
+      uint32_t keep = 0;
+#pragma unroll
+      for (int k = 0; k < kSelItems; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const uint64_t h = hash_key(keys[k]);
+        const uint32_t blk = bloom_block_of(h, b.num_blocks);
+        const uint32_t* words = b.smem_word >= 0 ? s_bloom + b.smem_word + blk * 8 : b.blocks + static_cast<uint64_t>(blk) * 8;
+        bool ok;
+        if (b.smem_word >= 0) {
+          ok = bloom_test(words, h, b.num_hashes);
+        } else {
+          uint32_t w[8];
+          const uint4 lo = __ldg(reinterpret_cast<const uint4*>(words));
+          const uint4 hi = __ldg(reinterpret_cast<const uint4*>(words) + 1);
+          w[0] = lo.x; w[1] = lo.y; w[2] = lo.z; w[3] = lo.w;
+          w[4] = hi.x; w[5] = hi.y; w[6] = hi.z; w[7] = hi.w;
+          ok = bloom_test(w, h, b.num_hashes);
+        }
+        keep |= static_cast<uint32_t>(ok) << k;
+      }
+      mask &= keep;
+    }
+
+    // Predicate in CNF.
+    for (int c = 0; c < p.prog.n_clauses; ++c) {
+      if (mask == 0) break;
+      uint32_t cm = 0;
+      for (int l = p.prog.clause_begin[c]; l < p.prog.clause_begin[c + 1]; ++l)
+        cm |= leaf8(p, p.prog.leaves[l], row0, mask & ~cm, vec);
+      mask &= cm;
+    }
+
+    // Rank the selected rows: block scan + decoupled look-back.
+    const int cnt = __popc(mask);
+    int tile_total;
+    const int excl = block_exclusive_sum<kSelThreads>(cnt, &tile_total, s_warp);
+    if (threadIdx.x < 32) {
+      const uint64_t b = lookback_exclusive(p.tile_status, tile, static_cast<uint64_t>(tile_total), p.status);
+      if (threadIdx.x == 0) s_base = b;
+    }
+    {
+      int o = excl;
+#pragma unroll
+      for (int k = 0; k < kSelItems; ++k)
+        if ((mask >> k) & 1u) s_rows[o++] = static_cast<int32_t>(threadIdx.x) * kSelItems + k;
+    }
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(s_base);
+    const int64_t tile_row0 = tile * kSelTile;
+    for (int j = 0; j < p.n_out; ++j) {
+      const OutCol& oc = p.outs[j];
+      if (oc.width == 8) {
+        const long long* src = static_cast<const long long*>(oc.src) + tile_row0;
+        long long* dst = static_cast<long long*>(oc.dst) + base;
+        for (int i = threadIdx.x; i < tile_total; i += kSelThreads) dst[i] = __ldg(src + s_rows[i]);
+      } else {
+        const int* src = static_cast<const int*>(oc.src) + tile_row0;
+        int* dst = static_cast<int*>(oc.dst) + base;
+        for (int i = threadIdx.x; i < tile_total; i += kSelThreads) dst[i] = __ldg(src + s_rows[i]);
+      }
+    }
+    if (p.out_rowids != nullptr) {
+      for (int i = threadIdx.x; i < tile_total; i += kSelThreads)
+        p.out_rowids[base + i] = static_cast<int32_t>(tile_row0 + s_rows[i]);
+    }
+    if (tile == p.n_tiles - 1 && threadIdx.x == 0) p.status->value = base + tile_total;
+    __syncthreads();
+  }
+}
+
+int g_select_blocks_per_sm = 0;
+
+}  // namespace
+
+TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const std::vector<BloomProbe>& probes,
+                        const std::vector<std::string>& project, bool all_columns, cudaStream_t s,
+                        SelectStats* stats) {
+  const int64_t n = in.num_rows();
+  if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "a TupleSet passed to select must have fewer than 2^31 rows");
+  if (static_cast<int>(probes.size()) > kMaxBlooms) fail(GFPDB_EUNSUPPORTED, "too many bloom probes in one select");
+
+  auto* pp = new SelectParams;  // large; keep off the stack
+  std::unique_ptr<SelectParams> holder(pp);
+  SelectParams& p = *pp;
+  std::memset(&p, 0, sizeof(p));
+  p.n_rows = n;
+
+  ColumnSlots slots;
+  if (pred != nullptr) {
+    p.prog = pred->prog;
+    slots = pred->slots;
+  }
+  // bloom key columns take slots after the predicate's
+  std::vector<int> probe_slot;
+  for (auto& pr : probes) {
+    int ci = in.require_column(pr.column);
+    DType t = in.field(ci).type;
+    if (t != DType::Int32 && t != DType::Int64 && t != DType::Date32)
+      fail(GFPDB_EUNSUPPORTED, "bloom key column '" + pr.column + "' must be an integer column");
+    probe_slot.push_back(slots.slot_for(pr.column, t));
+  }
+  bind_columns(slots, in, p.cols, kMaxCols);
+  p.n_cols = static_cast<int32_t>(slots.names.size());
+  bool aligned = true;
+  for (int i = 0; i < p.n_cols; ++i)
+    if ((reinterpret_cast<uintptr_t>(p.cols[i].data) & 15u) != 0) aligned = false;
+  p.aligned = aligned ? 1 : 0;
+
+  int smem_words = 0;
+  p.n_probes = static_cast<int32_t>(probes.size());
+  for (size_t i = 0; i < probes.size(); ++i) {
+    const auto& bf = *probes[i].bloom;
+    BloomDev& b = p.probes[i];
+    b.blocks = bf.blocks->as<uint32_t>();
+    if (bf.num_blocks >= (int64_t{1} << 32)) fail(GFPDB_EUNSUPPORTED, "bloom filter too large");
+    b.num_blocks = static_cast<uint32_t>(bf.num_blocks);
+    b.col = static_cast<int16_t>(probe_slot[i]);
+    b.num_hashes = static_cast<int8_t>(bf.num_hashes);
+    b.valid = bf.valid ? 1 : 0;
+    const int words = static_cast<int>(bf.num_blocks * 8);
+    if (bf.valid && (smem_words + words) * 4 <= kBloomSmemBudget) {
+      b.smem_word = smem_words;
+      smem_words += words;
+    } else {
+      b.smem_word = -1;
+    }
+  }
+  p.smem_words = smem_words;
+
+  // outputs
+  std::vector<std::string> out_names = project;
+  if (all_columns) {
+    out_names.clear();
+    for (auto& f : in.fields()) out_names.push_back(f.name);
+  }
+  std::vector<Field> out_fields;
+  std::vector<ColumnPtr> out_cols(out_names.size());
+  std::vector<BufferPtr> out_bufs(out_names.size());
+  bool need_rowids = false;
+  for (size_t j = 0; j < out_names.size(); ++j) {
+    int ci = in.require_column(out_names[j]);
+    out_fields.push_back(in.field(ci));
+    const auto& c = in.column(ci);
+    if (c->type == DType::Utf8) {
+      need_rowids = true;
+      continue;
+    }
+    const int w = dtype_width(c->type);
+    out_bufs[j] = make_buffer(n * w, s);
+    OutCol& oc = p.outs[p.n_out++];
+    oc.src = c->data;
+    oc.dst = out_bufs[j]->data();
+    oc.width = w;
+  }
+  BufferPtr rowids;
+  if (need_rowids) {
+    rowids = make_buffer(n * 4, s);
+    p.out_rowids = rowids->as<int32_t>();
+  }
+
+  const int64_t n_tiles = (n + kSelTile - 1) / kSelTile;
+  p.n_tiles = n_tiles;
+  auto scratch = make_buffer(sizeof(DevStatus) + 64 + n_tiles * 8, s);
+  char* sb = scratch->as<char>();
+  p.status = reinterpret_cast<DevStatus*>(sb);
+  p.ticket = reinterpret_cast<uint32_t*>(sb + sizeof(DevStatus));
+  p.tile_status = reinterpret_cast<uint64_t*>(sb + sizeof(DevStatus) + 64);
+  GF_CUDA(cudaMemsetAsync(sb, 0, scratch->size(), s));
+
+  int64_t count = 0;
+  if (n_tiles > 0) {
+    const size_t dyn = static_cast<size_t>(smem_words) * 4;
+    if (g_select_blocks_per_sm == 0) {
+      GF_CUDA(cudaFuncSetAttribute(select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBloomSmemBudget));
+    }
+    int per_sm = 0;
+    GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_kernel, kSelThreads, dyn));
+    if (per_sm < 1) per_sm = 1;
+    g_select_blocks_per_sm = per_sm;
+    int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
+    if (grid > n_tiles) grid = n_tiles;
+    ProfScope prof("select_kernel", s);
+    select_kernel<<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
+    after_launch("select_kernel");
+    prof.stop(0);
+    DevStatus hs;
+    GF_CUDA(cudaMemcpyAsync(&hs, p.status, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    raise_device_status(hs, "select");
+    count = hs.value;
+    // Algorithmic bytes: every evaluated column read once over all rows, the
+    // selected rows of the other projected columns read once, every projected
+    // value written once.
+    double read_all = 0, proj_read = 0, proj_write = 0;
+    for (int i = 0; i < p.n_cols; ++i) read_all += dtype_width(static_cast<DType>(p.cols[i].type));
+    for (int j = 0; j < p.n_out; ++j) {
+      proj_write += p.outs[j].width;
+      bool evaluated = false;
+      for (int i = 0; i < p.n_cols; ++i) evaluated |= p.cols[i].data == p.outs[j].src;
+      if (!evaluated) proj_read += p.outs[j].width;
+    }
+    prof.set_bytes(static_cast<double>(n) * read_all + static_cast<double>(count) * (proj_read + proj_write));
+  }
+
+  for (size_t j = 0; j < out_names.size(); ++j) {
+    if (out_fields[j].type == DType::Utf8) continue;
+    out_cols[j] = make_fixed_column(out_fields[j].type, count, out_bufs[j]);
+  }
+  if (need_rowids) {
+    std::vector<GatherSpec> specs;
+    std::vector<size_t> which;
+    for (size_t j = 0; j < out_names.size(); ++j) {
+      if (out_fields[j].type != DType::Utf8) continue;
+      specs.push_back(GatherSpec{in.column(in.require_column(out_names[j])).get(), rowids->as<int32_t>()});
+      which.push_back(j);
+    }
+    auto g = gather_columns(specs, count, s);
+    for (size_t k = 0; k < which.size(); ++k) out_cols[which[k]] = g[k];
+  }
+  if (stats) {
+    stats->rows_in = n;
+    stats->rows_out = count;
+  }
+  return TupleSet::make(std::move(out_fields), std::move(out_cols), count);
+}
+
+}  // namespace gfpdb

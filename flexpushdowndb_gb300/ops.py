@@ -1,0 +1,232 @@
+"""Python handles on the operator-level C ABI (one class per reference kernel).
+
+These mirror the kernel seams of the reference's operators so tests read like
+the reference's own: Filter (fpdb-expression-gandiva Filter::make / compile /
+evaluate), BloomFilter (BloomFilterCreateArrowKernel / BloomFilterUseKernel),
+HashJoin (HashJoinArrowKernel joinBuildTupleSet / finalizeInput /
+joinProbeTupleSet), Group (GroupArrowKernel group / finalise) and csv_read
+(CSVReader::read). Every call runs CUDA kernels inside libgfpdb.so.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import json
+from typing import Sequence
+
+import numpy as np
+
+from . import _abi
+from .expression import Expr, to_json
+from .tupleset import DeviceTable, Exported, Table, export_host, import_result, new_output
+
+
+def _export(t) -> Exported:
+    if isinstance(t, Exported):
+        return t
+    if isinstance(t, DeviceTable):
+        return t.export()
+    if isinstance(t, Table):
+        return export_host(t)
+    raise TypeError(f"cannot export {type(t)}")
+
+
+def _names(cols: Sequence[str] | None):
+    if cols is None:
+        return None, -1
+    return _abi.cstr_array(list(cols)), len(cols)
+
+
+def init(device: int = 0) -> None:
+    _abi.check(_abi.lib().gfpdb_device_init(device))
+
+
+def kernel_launches() -> int:
+    return int(_abi.lib().gfpdb_kernel_launch_count())
+
+
+class Filter:
+    """A compiled predicate (Filter::make + Filter::compile)."""
+
+    def __init__(self, predicate: Expr, schema_of):
+        self._h = ctypes.c_void_p()
+        ex = _export(schema_of)
+        _abi.check(_abi.lib().gfpdb_filter_compile(to_json(predicate).encode(), ex.schema_ptr, ctypes.byref(self._h)))
+
+    def evaluate(self, table, project: Sequence[str] | None = None, stream=None) -> Table:
+        ex = _export(table)
+        names, n = _names(project)
+        s, a = new_output()
+        _abi.check(_abi.lib().gfpdb_filter_evaluate(self._h, ex.schema_ptr, ex.array_ptr, names, n, ctypes.byref(s),
+                                                    ctypes.byref(a), stream))
+        return import_result(s, a)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _abi.lib().gfpdb_filter_free(self._h)
+            self._h = ctypes.c_void_p()
+
+
+class BloomFilter:
+    """Blocked bloom filter built on the device (BloomFilterCreateArrowKernel)."""
+
+    def __init__(self, batches: Sequence, key_column: str, bits_per_key: int = 10, num_hashes: int = 3, stream=None):
+        exs = [_export(b) for b in batches]
+        if not exs:
+            raise ValueError("BloomFilter needs at least one batch (the schema comes from it)")
+        arr = (ctypes.POINTER(_abi.ArrowDeviceArray) * len(exs))(*[e.array_ptr for e in exs])
+        self._h = ctypes.c_void_p()
+        _abi.check(_abi.lib().gfpdb_bloom_create(exs[0].schema_ptr, arr, len(exs), key_column.encode(), bits_per_key,
+                                                 num_hashes, ctypes.byref(self._h), stream))
+
+    def info(self) -> dict:
+        nb, nk = ctypes.c_int64(), ctypes.c_int64()
+        valid, nh = ctypes.c_int32(), ctypes.c_int32()
+        ptr = ctypes.c_void_p()
+        _abi.check(_abi.lib().gfpdb_bloom_info(self._h, ctypes.byref(nb), ctypes.byref(nk), ctypes.byref(valid),
+                                               ctypes.byref(nh), ctypes.byref(ptr)))
+        return {"num_blocks": nb.value, "num_keys": nk.value, "valid": bool(valid.value), "num_hashes": nh.value,
+                "device_ptr": ptr.value}
+
+    def words(self) -> np.ndarray:
+        """The filter's uint32 words, copied to the host."""
+        info = self.info()
+        out = np.zeros(info["num_blocks"] * 8, dtype=np.uint32)
+        if out.nbytes:
+            _abi.check(_abi.lib().gfpdb_memcpy(out.ctypes.data, info["device_ptr"], out.nbytes, 2, None))
+        return out
+
+    def use(self, table, key_column: str, stream=None) -> Table:
+        ex = _export(table)
+        s, a = new_output()
+        _abi.check(_abi.lib().gfpdb_bloom_use(self._h, ex.schema_ptr, ex.array_ptr, key_column.encode(),
+                                              ctypes.byref(s), ctypes.byref(a), stream))
+        return import_result(s, a)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _abi.lib().gfpdb_bloom_free(self._h)
+            self._h = ctypes.c_void_p()
+
+
+def select(table, predicate: Filter | None = None, blooms: Sequence[tuple[BloomFilter, str]] = (),
+           project: Sequence[str] | None = None, stream=None) -> Table:
+    """Fused predicate + bloom probes + compaction (gfpdb_select)."""
+    ex = _export(table)
+    nb = len(blooms)
+    bh = (ctypes.c_void_p * max(1, nb))(*[b._h.value for b, _ in blooms])
+    bc = _abi.cstr_array([c for _, c in blooms])
+    names, n = _names(project)
+    s, a = new_output()
+    _abi.check(_abi.lib().gfpdb_select(predicate._h if predicate else None, nb, bh, bc, ex.schema_ptr, ex.array_ptr,
+                                       names, n, ctypes.byref(s), ctypes.byref(a), stream))
+    return import_result(s, a)
+
+
+class HashJoin:
+    """Inner hash join (HashJoinArrowKernel). Output: probe columns, then build columns."""
+
+    def __init__(self, build_key: str, probe_key: str, needed: Sequence[str] | None = None, load_factor: float = 0.5):
+        names, n = _names(needed)
+        self._h = ctypes.c_void_p()
+        _abi.check(_abi.lib().gfpdb_hashjoin_create(0, build_key.encode(), probe_key.encode(), names, n, load_factor,
+                                                    ctypes.byref(self._h)))
+
+    def put_build(self, table, stream=None) -> None:
+        ex = _export(table)
+        _abi.check(_abi.lib().gfpdb_hashjoin_put_build(self._h, ex.schema_ptr, ex.array_ptr, stream))
+
+    def finalize_build(self, stream=None) -> None:
+        _abi.check(_abi.lib().gfpdb_hashjoin_finalize_build(self._h, stream))
+
+    def probe(self, table, stream=None) -> Table:
+        ex = _export(table)
+        s, a = new_output()
+        _abi.check(_abi.lib().gfpdb_hashjoin_probe(self._h, ex.schema_ptr, ex.array_ptr, ctypes.byref(s),
+                                                   ctypes.byref(a), stream))
+        return import_result(s, a)
+
+    def info(self) -> dict:
+        b, c, m = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _abi.check(_abi.lib().gfpdb_hashjoin_info(self._h, ctypes.byref(b), ctypes.byref(c), ctypes.byref(m)))
+        return {"build_rows": b.value, "capacity": c.value, "max_probe": m.value}
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _abi.lib().gfpdb_hashjoin_free(self._h)
+            self._h = ctypes.c_void_p()
+
+
+def aggregate(function: str, name: str, expr: Expr | None = None) -> dict:
+    a = {"function": function, "name": name}
+    if expr is not None:
+        a["expr"] = expr
+    return a
+
+
+class Group:
+    """Hash group-by (GroupArrowKernel): group() per TupleSet, finalise() once."""
+
+    def __init__(self, group_columns: Sequence[str], aggregates: Sequence[dict], groups_hint: int = 0):
+        spec = {"groupColumnNames": list(group_columns), "aggregates": list(aggregates), "groupsHint": groups_hint}
+        self._h = ctypes.c_void_p()
+        _abi.check(_abi.lib().gfpdb_group_create(json.dumps(spec).encode(), ctypes.byref(self._h)))
+
+    def group(self, table, stream=None) -> None:
+        ex = _export(table)
+        _abi.check(_abi.lib().gfpdb_group_update(self._h, ex.schema_ptr, ex.array_ptr, stream))
+
+    def finalise(self, stream=None) -> Table:
+        s, a = new_output()
+        _abi.check(_abi.lib().gfpdb_group_finalize(self._h, ctypes.byref(s), ctypes.byref(a), stream))
+        return import_result(s, a)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _abi.lib().gfpdb_group_free(self._h)
+            self._h = ctypes.c_void_p()
+
+
+def csv_read(text: bytes | np.ndarray, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
+             delimiter: str = ",", has_header: bool = False, device_ptr: int | None = None, stream=None) -> Table:
+    """Parse delimited text (CSVReader::read). ``fields`` lists (name, type)
+    for every field of a line; a type "decimal(p,s)" parses into int64
+    scaled by 10^s."""
+    schema_children = []
+    for name, ty in fields:
+        if ty.startswith("decimal"):
+            inner = ty[ty.index("(") + 1 : ty.index(")")]
+            schema_children.append((name, ("d:" + inner.replace(" ", "")).encode()))
+        else:
+            from .tupleset import FORMATS
+
+            schema_children.append((name, FORMATS[ty]))
+    keep = []
+    kids = (_abi.ArrowSchema * len(schema_children))()
+    kid_ptrs = (ctypes.POINTER(_abi.ArrowSchema) * len(schema_children))()
+    from .tupleset import _noop_schema_release
+
+    for i, (name, fmt) in enumerate(schema_children):
+        bn = name.encode()
+        keep += [bn, fmt]
+        kids[i].format = fmt
+        kids[i].name = bn
+        kids[i].release = _noop_schema_release
+        kid_ptrs[i] = ctypes.pointer(kids[i])
+    sch = _abi.ArrowSchema()
+    sch.format = b"+s"
+    sch.n_children = len(schema_children)
+    sch.children = ctypes.cast(kid_ptrs, ctypes.POINTER(ctypes.POINTER(_abi.ArrowSchema)))
+    sch.release = _noop_schema_release
+    names, n = _names(columns)
+    s, a = new_output()
+    if device_ptr is not None:
+        nbytes = len(text) if not isinstance(text, int) else text
+        ptr, dev_type = device_ptr, _abi.ARROW_DEVICE_CUDA
+    else:
+        buf = np.frombuffer(text, dtype=np.uint8) if isinstance(text, (bytes, bytearray)) else text
+        keep.append(buf)
+        nbytes, ptr, dev_type = buf.nbytes, buf.ctypes.data, _abi.ARROW_DEVICE_CPU
+    _abi.check(_abi.lib().gfpdb_csv_read(ptr, nbytes, dev_type, delimiter.encode(), 1 if has_header else 0,
+                                         ctypes.byref(sch), names, n, ctypes.byref(s), ctypes.byref(a), stream))
+    return import_result(s, a)

@@ -1,0 +1,154 @@
+"""Seeded synthetic workloads and their plans.
+
+Inputs come from SplitMix64 (Steele, Lea, Flood, "Fast splittable
+pseudorandom number generators", OOPSLA 2014) evaluated counter-style, so
+any column of any partition can be regenerated from (seed, index) alone.
+Seeds: config id * 1000 + partition, plus a per-column stream number.
+
+Workloads (shapes of the reference's evaluation, all synthetic):
+  two_table  - fact 1,000,000 x {fk, qty, price_cents}; dim 20,000 x
+               {pk, category, region}; filter category < 5, join fk = pk,
+               group by region -> sum(price_cents * qty), count(*).
+  star       - SSB-SF1-shaped star: fact 6,000,000 x {fk1..fk4, qty,
+               price_cents, discount}; dims of 30,000 / 200,000 / 2,000 /
+               2,556 rows x {pk, f, g}; dim filters f = const keeping 1/5,
+               1/25, 1/7, 1/7; forward + backward bloom predicate transfer,
+               4-way join, group by (d2_g, d4_g) (~175 groups) ->
+               sum(price*qty), sum(price*discount), count(*).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .expression import col, eq, lt, num_lit, times
+from .ops import aggregate
+from .plan import Plan
+from .tupleset import Column, Table
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, start: int = 0) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        i = np.arange(start + 1, start + n + 1, dtype=np.uint64)
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + i * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, stream: int, n: int, lo: int, hi: int, start: int = 0) -> np.ndarray:
+    """Integers uniform on [lo, hi] (inclusive), as int64."""
+    r = splitmix64(seed * 1_000_003 + stream, n, start)
+    span = np.uint64(hi - lo + 1)
+    return (r % span).astype(np.int64) + lo
+
+
+REGIONS = ["AFRICA  ", "AMERICA ", "ASIA    ", "EUROPE  ", "MIDEAST "]
+
+
+# ------------------------------------------------------------------ two-table
+
+
+def two_table_tables(fact_rows: int = 1_000_000, dim_rows: int = 20_000, seed: int = 1000) -> dict[str, Table]:
+    fk = uniform(seed, 1, fact_rows, 1, dim_rows)
+    qty = uniform(seed, 2, fact_rows, 1, 50)
+    price = uniform(seed, 3, fact_rows, 90_000, 10_500_000)
+    pk = np.arange(1, dim_rows + 1, dtype=np.int64)
+    cat = uniform(seed, 4, dim_rows, 0, 24)
+    reg = uniform(seed, 5, dim_rows, 0, len(REGIONS) - 1)
+    fact = Table([Column("fk", "int32", fk), Column("qty", "int32", qty), Column("price_cents", "int64", price)])
+    dim = Table([Column("pk", "int32", pk), Column("category", "int32", cat),
+                 Column("region", "utf8", [REGIONS[i] for i in reg])])
+    return {"fact": fact, "dim": dim}
+
+
+def two_table_plan(category_lt: int = 5, chunk_rows: int = 0) -> Plan:
+    p = Plan()
+    p.scan("scan_dim", "dim", ["pk", "category", "region"])
+    p.filter("filter_dim", "scan_dim", lt(col("category"), num_lit(category_lt, "int32")), ["pk", "region"])
+    p.scan("scan_fact", "fact", ["fk", "qty", "price_cents"], chunk_rows=chunk_rows)
+    p.hash_join("join", "filter_dim", "scan_fact", "pk", "fk", ["region", "qty", "price_cents"])
+    p.group("group", "join", ["region"],
+            [aggregate("SUM", "revenue", times(col("price_cents"), col("qty"))), aggregate("COUNT", "cnt")],
+            groups_hint=8)
+    p.collate("collate", "group")
+    return p
+
+
+# ----------------------------------------------------------------------- star
+
+STAR_DIM_ROWS = (30_000, 200_000, 2_000, 2_556)
+STAR_FILTER_VALUES = (5, 25, 7, 7)   # f uniform over this many values
+STAR_GROUP_VALUES = (10, 25, 10, 7)  # g uniform over this many values (d2_g x d4_g = 175 groups)
+STAR_DEFAULT_CONSTS = (1, 3, 2, 5)   # dim filter: f == const
+
+
+def star_dims(seed: int = 2000) -> dict[str, Table]:
+    out = {}
+    for i, n in enumerate(STAR_DIM_ROWS, start=1):
+        out[f"d{i}"] = Table([
+            Column(f"d{i}_pk", "int32", np.arange(1, n + 1, dtype=np.int64)),
+            Column(f"d{i}_f", "int32", uniform(seed, 10 + i, n, 0, STAR_FILTER_VALUES[i - 1] - 1)),
+            Column(f"d{i}_g", "int32", uniform(seed, 20 + i, n, 0, STAR_GROUP_VALUES[i - 1] - 1)),
+        ])
+    return out
+
+
+def star_fact(rows: int = 6_000_000, seed: int = 2000, start: int = 0) -> Table:
+    cols = [Column(f"fk{i}", "int32", uniform(seed, i, rows, 1, n, start)) for i, n in enumerate(STAR_DIM_ROWS, 1)]
+    cols += [
+        Column("qty", "int32", uniform(seed, 5, rows, 1, 50, start)),
+        Column("price_cents", "int64", uniform(seed, 6, rows, 90_000, 10_500_000, start)),
+        Column("discount", "int32", uniform(seed, 7, rows, 0, 10, start)),
+    ]
+    return Table(cols)
+
+
+def star_tables(fact_rows: int = 6_000_000, seed: int = 2000) -> dict[str, Table]:
+    t = star_dims(seed)
+    t["fact"] = star_fact(fact_rows, seed)
+    return t
+
+
+def star_plan(consts=STAR_DEFAULT_CONSTS, bits_per_key: int = 10, num_hashes: int = 3, chunk_rows: int = 0,
+              backward: bool = True) -> Plan:
+    """Forward + backward bloom predicate transfer, then the 4-way join and
+    group-by, in the shape SmallToLargePredTransOrder builds
+    (fpdb-executor/src/physical/transform/pred-trans/SmallToLargePredTransOrder.cpp:38-214)."""
+    p = Plan()
+    dim_tail = {}
+    fwd = {}
+    for i in range(1, 5):
+        p.scan(f"scan_d{i}", f"d{i}", [f"d{i}_pk", f"d{i}_f", f"d{i}_g"])
+        keep = [f"d{i}_pk", f"d{i}_g"] if i in (2, 4) else [f"d{i}_pk"]
+        p.filter(f"filter_d{i}", f"scan_d{i}", eq(col(f"d{i}_f"), num_lit(int(consts[i - 1]), "int32")), keep)
+        fwd[i] = p.bloom_create(f"bf_fwd_create_d{i}", f"filter_d{i}", f"d{i}_pk", bits_per_key, num_hashes)
+        dim_tail[i] = fwd[i]
+    p.scan("scan_fact", "fact", ["fk1", "fk2", "fk3", "fk4", "qty", "price_cents", "discount"], chunk_rows=chunk_rows)
+    tail = "scan_fact"
+    # forward: the most selective filters first (1/25, 1/7, 1/7, 1/5)
+    for i in (2, 3, 4, 1):
+        tail = p.bloom_use(f"bf_fwd_use_fk{i}", tail, fwd[i], f"fk{i}")
+    if backward:
+        for i in range(1, 5):
+            c = p.bloom_create(f"bf_bwd_create_fk{i}", tail, f"fk{i}", bits_per_key, num_hashes)
+            dim_tail[i] = p.bloom_use(f"bf_bwd_use_d{i}", dim_tail[i], c, f"d{i}_pk")
+            tail = c
+    fact_cols = ["fk1", "fk2", "fk3", "fk4", "qty", "price_cents", "discount"]
+    carried: list[str] = []
+    for i in range(1, 5):
+        fact_cols = [c for c in fact_cols if c != f"fk{i}"]
+        if i in (2, 4):
+            carried.append(f"d{i}_g")
+        tail = p.hash_join(f"join_d{i}", dim_tail[i], tail, f"d{i}_pk", f"fk{i}", fact_cols + carried)
+    p.group("group", tail, ["d2_g", "d4_g"], [
+        aggregate("SUM", "revenue", times(col("price_cents"), col("qty"))),
+        aggregate("SUM", "discount_revenue", times(col("price_cents"), col("discount"))),
+        aggregate("COUNT", "cnt"),
+    ], groups_hint=256)
+    p.collate("collate", "group")
+    return p

@@ -1,0 +1,278 @@
+/*
+ * gfpdb — C ABI of the GB300-native relational hot path (sm_103a).
+ *
+ * Every entry point is a plain C function over the Arrow C Data / C Device
+ * Data Interface (gfpdb_arrow.h): plain pointers, sizes and status codes, no
+ * C++ or torch types. Each one replaces one kernel seam of the reference's
+ * fpdb-executor physical operators; the comment above it names the reference
+ * interface (file:line) it stands in for.
+ *
+ * Conventions
+ *  - Return value: GFPDB_OK (0) or a GFPDB_E* code. The message of the last
+ *    failure on the calling thread is returned by gfpdb_last_error(); this is
+ *    the C rendering of the reference's tl::expected<T, std::string> results.
+ *  - A TupleSet crosses the boundary as (ArrowSchema "+s", ArrowDeviceArray
+ *    whose struct array has one child per column). Input arrays may live in
+ *    device memory (ARROW_DEVICE_CUDA) or in host memory (ARROW_DEVICE_CPU /
+ *    ARROW_DEVICE_CUDA_HOST); host inputs are copied to the device on the
+ *    given stream. Outputs are device arrays owned by the library until the
+ *    caller invokes their release callbacks (Arrow spec semantics).
+ *  - Supported column formats: "i" int32, "l" int64, "tdD" date32, "g"
+ *    float64, "u" utf8. Decimals are carried as int64 cents.
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream). Calls are
+ *    reentrant across streams. There is no CPU fallback: every compute entry
+ *    point launches CUDA kernels and fails with GFPDB_ECUDA when no device is
+ *    usable.
+ */
+#ifndef GFPDB_H
+#define GFPDB_H
+
+#include <stdint.h>
+#include "gfpdb_arrow.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFPDB_OK 0
+#define GFPDB_EINVAL 1        /* bad argument, schema, plan or expression */
+#define GFPDB_ECUDA 2         /* CUDA runtime error (no device, launch failure) */
+#define GFPDB_EDEVICE 3       /* a kernel raised its device error word */
+#define GFPDB_ETIMEDOUT 4     /* a bounded device-side wait gave up */
+#define GFPDB_ENOMEM 5        /* device allocation failed or HBM budget exceeded */
+#define GFPDB_EUNSUPPORTED 6  /* valid request outside what this build implements */
+
+/* Join types, numbered like fpdb::plan::prephysical::JoinType. */
+#define GFPDB_JOIN_INNER 0
+#define GFPDB_JOIN_LEFT 1
+#define GFPDB_JOIN_RIGHT 2
+#define GFPDB_JOIN_FULL 3
+
+typedef struct gfpdb_filter gfpdb_filter;
+typedef struct gfpdb_bloom gfpdb_bloom;
+typedef struct gfpdb_hashjoin gfpdb_hashjoin;
+typedef struct gfpdb_group gfpdb_group;
+
+/* ---------------------------------------------------------------- runtime */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* gfpdb_last_error(void);
+
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int32_t gfpdb_version(void);
+
+/* Select the CUDA device for this thread and set up its memory pool.
+ * Idempotent. Replaces nothing in the reference (its operators are CPU-only);
+ * it is the device-side counterpart of Executor::start
+ * (fpdb-executor/src/Executor.cpp:40-65). */
+int32_t gfpdb_device_init(int32_t device);
+
+/* Number of kernels this library has launched in this process. */
+uint64_t gfpdb_kernel_launch_count(void);
+
+/* Stream-ordered copies between host and device memory, for callers that
+ * hold raw device buffers (kind: 1 = host->device, 2 = device->host,
+ * 3 = device->device). Synchronous when stream is NULL. */
+int32_t gfpdb_memcpy(void* dst, const void* src, int64_t n_bytes, int32_t kind, void* stream);
+
+/* Page-locked host allocation, so that host inputs can be copied at full
+ * link bandwidth. */
+int32_t gfpdb_host_alloc(void** ptr, int64_t n_bytes);
+int32_t gfpdb_host_free(void* ptr);
+
+/* Wait for all work queued on `stream`. */
+int32_t gfpdb_stream_synchronize(void* stream);
+
+/* Kernel timing: while enabled, every kernel launch of the library is
+ * bracketed by CUDA events on its own stream, and its algorithmic byte count
+ * (input bytes it must read plus output bytes it writes, at row granularity)
+ * is recorded. gfpdb_profile_read returns, for one kernel name, the number of
+ * launches, their summed event time in milliseconds and their summed
+ * algorithmic bytes (it waits for the recorded events). The tracing
+ * counterpart of the reference's per-operator timing (SHOW_OP_TIMES,
+ * fpdb-executor/src/Execution.cpp:420). */
+int32_t gfpdb_profile_enable(int32_t enable);
+int32_t gfpdb_profile_reset(void);
+int32_t gfpdb_profile_read(const char* kernel_name, int64_t* launches, double* total_ms, double* total_bytes);
+/* Names of the kernels recorded since the last reset, '\n'-separated. */
+int32_t gfpdb_profile_kernels(char* buf, int64_t buf_len);
+
+/* ----------------------------------------------------------------- filter */
+
+/* Compile a predicate expression tree against a schema.
+ * Replaces fpdb::expression::gandiva::Filter::make + Filter::compile
+ * (fpdb-expression-gandiva/src/Filter.cpp:227-271): the Gandiva LLVM JIT
+ * becomes a lowering to a conjunctive leaf program that the fused selection
+ * kernel evaluates. `predicate_json` uses the reference's expression JSON
+ * node names (Expression::fromJson, fpdb-expression-gandiva/src/Expression.cpp:52-148). */
+int32_t gfpdb_filter_compile(const char* predicate_json, const struct ArrowSchema* schema,
+                             gfpdb_filter** out);
+
+/* Evaluate a compiled predicate over one TupleSet and emit the selected rows
+ * (input order kept) projected to `project_columns` (all columns when
+ * n_project < 0). Replaces Filter::evaluate(const TupleSet&)
+ * (fpdb-expression-gandiva/src/Filter.cpp:87-176) as called by
+ * FilterPOp::filterTuplesRegular (fpdb-executor/src/physical/filter/FilterPOp.cpp:316-339). */
+int32_t gfpdb_filter_evaluate(const gfpdb_filter* filter, const struct ArrowSchema* in_schema,
+                              const struct ArrowDeviceArray* in, const char* const* project_columns,
+                              int32_t n_project, struct ArrowSchema* out_schema,
+                              struct ArrowDeviceArray* out, void* stream);
+
+void gfpdb_filter_free(gfpdb_filter* filter);
+
+/* ------------------------------------------------------------------ bloom */
+
+/* Build a blocked bloom filter (256-bit blocks, `num_hashes` bits per key set
+ * inside one block, sized `bits_per_key` bits per key) over the key column of
+ * one or more TupleSets. Replaces BloomFilterCreateArrowKernel::buildBloomFilter
+ * (fpdb-executor/src/physical/bloomfilter/BloomFilterCreateArrowKernel.cpp:17-34)
+ * and ArrowBloomFilter::build (.../bloomfilter/ArrowBloomFilter.cpp:29-75).
+ * Above GFPDB_BLOOM_MAX_INPUT_SIZE keys the filter is marked invalid and every
+ * probe passes, as BLOOM_FILTER_MAX_INPUT_SIZE does in the reference
+ * (fpdb-executor/include/fpdb/executor/physical/Globals.h:55,
+ * .../bloomfilter/BloomFilterUseKernel.cpp:17-19). */
+#define GFPDB_BLOOM_MAX_INPUT_SIZE 20000000
+int32_t gfpdb_bloom_create(const struct ArrowSchema* schema,
+                           const struct ArrowDeviceArray* const* batches, int32_t n_batches,
+                           const char* key_column, int32_t bits_per_key, int32_t num_hashes,
+                           gfpdb_bloom** out, void* stream);
+
+/* Keep the rows whose key column may be in the filter; all columns are kept.
+ * Replaces BloomFilterUseKernel::filter(tupleSet, bloomFilter, columnNames)
+ * (fpdb-executor/src/physical/bloomfilter/BloomFilterUseKernel.cpp:12-32). */
+int32_t gfpdb_bloom_use(const gfpdb_bloom* bloom, const struct ArrowSchema* in_schema,
+                        const struct ArrowDeviceArray* in, const char* key_column,
+                        struct ArrowSchema* out_schema, struct ArrowDeviceArray* out, void* stream);
+
+/* Filter structure, for tests and for shipping a filter to another device:
+ * block count, keys inserted, whether the filter is valid, and the device
+ * address of its num_blocks * 8 uint32 words. */
+int32_t gfpdb_bloom_info(const gfpdb_bloom* bloom, int64_t* num_blocks, int64_t* num_keys,
+                         int32_t* valid, int32_t* num_hashes, const void** device_blocks);
+
+void gfpdb_bloom_free(gfpdb_bloom* bloom);
+
+/* ----------------------------------------------- fused scan (filter+bloom) */
+
+/* One fused pass over a TupleSet: an optional compiled predicate AND a chain
+ * of bloom probes, followed by stable compaction and projection. This is the
+ * GPU form of a FilterPOp followed by a chain of BloomFilterUsePOps
+ * (FilterPOp.cpp:316-339; BloomFilterUsePOp.cpp:116-142), which the reference
+ * runs as separate passes. `filter` may be NULL; n_blooms may be 0. */
+int32_t gfpdb_select(const gfpdb_filter* filter, int32_t n_blooms, const gfpdb_bloom* const* blooms,
+                     const char* const* bloom_key_columns, const struct ArrowSchema* in_schema,
+                     const struct ArrowDeviceArray* in, const char* const* project_columns,
+                     int32_t n_project, struct ArrowSchema* out_schema,
+                     struct ArrowDeviceArray* out, void* stream);
+
+/* -------------------------------------------------------------- hash join */
+
+/* Create a hash join with the given key columns (one key column per side).
+ * Output columns are the probe side's needed columns followed by the build
+ * side's, as HashJoinArrowKernel::makeOutputSchema orders them
+ * (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:148-162).
+ * `needed_columns` NULL / n_needed < 0 keeps every column.
+ * Replaces HashJoinArrowKernel::make (HashJoinArrowKernel.h:48-54). */
+int32_t gfpdb_hashjoin_create(int32_t join_type, const char* build_key, const char* probe_key,
+                              const char* const* needed_columns, int32_t n_needed,
+                              double load_factor, gfpdb_hashjoin** out);
+
+/* Append a build-side TupleSet. Replaces HashJoinArrowKernel::joinBuildTupleSet
+ * (HashJoinArrowKernel.cpp:35-63). */
+int32_t gfpdb_hashjoin_put_build(gfpdb_hashjoin* join, const struct ArrowSchema* schema,
+                                 const struct ArrowDeviceArray* batch, void* stream);
+
+/* All build input has arrived: build the open-addressing table.
+ * Replaces HashJoinArrowKernel::finalizeInput(true) (HashJoinArrowKernel.cpp:95-124). */
+int32_t gfpdb_hashjoin_finalize_build(gfpdb_hashjoin* join, void* stream);
+
+/* Probe one TupleSet against the built table and emit the joined rows.
+ * Replaces HashJoinArrowKernel::joinProbeTupleSet + getOutputBuffer
+ * (HashJoinArrowKernel.cpp:65-93). */
+int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const struct ArrowSchema* schema,
+                             const struct ArrowDeviceArray* batch, struct ArrowSchema* out_schema,
+                             struct ArrowDeviceArray* out, void* stream);
+
+/* Build-table statistics: rows, slots, longest probe run seen while building. */
+int32_t gfpdb_hashjoin_info(const gfpdb_hashjoin* join, int64_t* build_rows, int64_t* capacity,
+                            int64_t* max_probe);
+
+void gfpdb_hashjoin_free(gfpdb_hashjoin* join);
+
+/* --------------------------------------------------------------- group-by */
+
+/* Create a hash group-by from a JSON spec:
+ *   {"groupColumnNames": ["a", ...],
+ *    "aggregates": [{"function": "SUM"|"COUNT"|"MIN"|"MAX"|"AVG",
+ *                    "name": "out", "expr": <expression JSON, absent for count(*)>}],
+ *    "groupsHint": N}
+ * Output columns are the group columns followed by the aggregates in the
+ * given order (GroupArrowKernel::makeOutputSchema,
+ * fpdb-executor/src/physical/group/GroupArrowKernel.cpp:156-200). SUM over
+ * integers is an int64 two's-complement (wrapping) sum, COUNT an int64, as
+ * Arrow's hash_sum / hash_count (Sum.cpp:63-74, Count.cpp:91-104). */
+int32_t gfpdb_group_create(const char* group_spec_json, gfpdb_group** out);
+
+/* Fold one TupleSet into the group table. Replaces GroupAbstractKernel::group
+ * (fpdb-executor/include/fpdb/executor/physical/group/GroupAbstractKernel.h:32)
+ * as GroupArrowKernel::group implements it (GroupArrowKernel.cpp:16-39). */
+int32_t gfpdb_group_update(gfpdb_group* group, const struct ArrowSchema* schema,
+                           const struct ArrowDeviceArray* batch, void* stream);
+
+/* Emit one row per group. Replaces GroupAbstractKernel::finalise
+ * (GroupAbstractKernel.h:39; GroupArrowKernel.cpp:41-68). */
+int32_t gfpdb_group_finalize(gfpdb_group* group, struct ArrowSchema* out_schema,
+                             struct ArrowDeviceArray* out, void* stream);
+
+void gfpdb_group_free(gfpdb_group* group);
+
+/* -------------------------------------------------------------------- CSV */
+
+/* Parse delimiter-separated text into typed columns. `target_schema` ("+s")
+ * names and types every field of a line in file order; `columns` selects the
+ * fields to emit (all when n_columns < 0). Field types: int32, int64, date32
+ * (YYYY-MM-DD), utf8, and int64 with metadata-free format "l" for decimals
+ * when the schema child's name ends with no marker: decimal(15,2) text is
+ * selected by giving the child the format "d:15,2" and is emitted as int64
+ * cents. `text` may be host or device memory (text_device_type).
+ * Replaces CSVReader::read(columnNames) (fpdb-tuple/src/csv/CSVReader.cpp:15-21)
+ * and its SIMD parser (CSVToArrowSIMDChunkParser.cpp:183-409). */
+int32_t gfpdb_csv_read(const void* text, int64_t n_bytes, int32_t text_device_type, char delimiter,
+                       int32_t has_header, const struct ArrowSchema* target_schema,
+                       const char* const* columns, int32_t n_columns,
+                       struct ArrowSchema* out_schema, struct ArrowDeviceArray* out, void* stream);
+
+/* -------------------------------------------------------- plan execution */
+
+typedef struct gfpdb_exec_stats {
+  int64_t elapsed_ns;        /* host wall time of the call */
+  int64_t kernel_launches;   /* kernels launched by this call */
+  int64_t h2d_bytes;         /* host->device bytes copied by this call */
+  int64_t d2h_bytes;         /* device->host bytes copied by this call */
+  int64_t num_ops;           /* physical operators in the plan */
+  int64_t messages;          /* messages delivered between operators */
+} gfpdb_exec_stats;
+
+/* Run a physical plan of the reference's operators (TableScanPOp, FilterPOp,
+ * BloomFilterCreatePOp, BloomFilterUsePOp, HashJoinArrowPOp, GroupPOp,
+ * ProjectPOp, CollatePOp) on one GPU, delivering START / TUPLESET /
+ * BLOOM_FILTER / COMPLETE messages between them in the reference's protocol,
+ * and return the CollatePOp's TupleSet. Input tables are named; host tables
+ * are copied to the device by their scan operator. With result_to_host != 0
+ * the result is returned in host memory.
+ * Replaces Executor::execute(PhysicalPlan) (fpdb-executor/src/Executor.cpp:87-122)
+ * driving Execution::execute (fpdb-executor/src/Execution.cpp:44-280). */
+int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* const* table_names,
+                           const struct ArrowSchema* const* schemas,
+                           const struct ArrowDeviceArray* const* arrays, int32_t result_to_host,
+                           struct ArrowSchema* out_schema, struct ArrowDeviceArray* out,
+                           gfpdb_exec_stats* stats, void* stream);
+
+/* Parse and check a plan without running it (host only, no CUDA calls). */
+int32_t gfpdb_plan_validate(const char* plan_json);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFPDB_H */

@@ -1,0 +1,85 @@
+"""ctypes wrapper of oracle/baseline.c (BENCHMARK / TEST INFRASTRUCTURE ONLY)."""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from flexpushdowndb_gb300.tupleset import Column, Table
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+
+class _Fact(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("fk", ctypes.c_void_p * 4), ("qty", ctypes.c_void_p),
+                ("price", ctypes.c_void_p), ("disc", ctypes.c_void_p)]
+
+
+class _Dim(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("pk", ctypes.c_void_p), ("f", ctypes.c_void_p), ("g", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+        _lib = ctypes.CDLL(str(LIB))
+        _lib.orc_star_query.restype = ctypes.c_int64
+    return _lib
+
+
+class StarInputs:
+    """Arrays of a star workload laid out for the C baseline (kept alive)."""
+
+    def __init__(self, tables: dict[str, Table]):
+        f = tables["fact"]
+        self.keep = []
+
+        def arr(t: Table, name: str, dt):
+            a = np.ascontiguousarray(t[name], dtype=dt)
+            self.keep.append(a)
+            return a.ctypes.data
+
+        self.fact = _Fact()
+        self.fact.n = f.num_rows
+        for i in range(4):
+            self.fact.fk[i] = arr(f, f"fk{i + 1}", np.int32)
+        self.fact.qty = arr(f, "qty", np.int32)
+        self.fact.price = arr(f, "price_cents", np.int64)
+        self.fact.disc = arr(f, "discount", np.int32)
+        self.dims = (_Dim * 4)()
+        for i in range(4):
+            d = tables[f"d{i + 1}"]
+            self.dims[i].n = d.num_rows
+            self.dims[i].pk = arr(d, f"d{i + 1}_pk", np.int32)
+            self.dims[i].f = arr(d, f"d{i + 1}_f", np.int32)
+            self.dims[i].g = arr(d, f"d{i + 1}_g", np.int32)
+
+
+def star_query(inputs: StarInputs, consts=(1, 3, 2, 5), bits: int = 10, nh: int = 3, threads: int | None = None,
+               max_groups: int = 4096) -> Table:
+    threads = threads or os.cpu_count() or 1
+    c = (ctypes.c_int32 * 4)(*consts)
+    g2 = np.zeros(max_groups, np.int32)
+    g4 = np.zeros(max_groups, np.int32)
+    rev = np.zeros(max_groups, np.int64)
+    drev = np.zeros(max_groups, np.int64)
+    cnt = np.zeros(max_groups, np.int64)
+    n = lib().orc_star_query(ctypes.byref(inputs.fact), inputs.dims, c, bits, nh, threads,
+                             g2.ctypes.data_as(ctypes.c_void_p), g4.ctypes.data_as(ctypes.c_void_p),
+                             rev.ctypes.data_as(ctypes.c_void_p), drev.ctypes.data_as(ctypes.c_void_p),
+                             cnt.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(max_groups))
+    if n < 0:
+        raise RuntimeError("too many groups")
+    return Table([Column("d2_g", "int32", g2[:n]), Column("d4_g", "int32", g4[:n]),
+                  Column("revenue", "int64", rev[:n]), Column("discount_revenue", "int64", drev[:n]),
+                  Column("cnt", "int64", cnt[:n])])

@@ -1,0 +1,119 @@
+"""The C ABI without a GPU: the library loads, exports every declared symbol,
+and host-only entry points (plan validation, expression and spec compilation)
+report errors the way the reference does (a status plus a message)."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from flexpushdowndb_gb300 import _abi, ops, plan, workloads
+from flexpushdowndb_gb300.expression import and_, col, eq, gt, in_, lt, not_, num_lit, or_, str_lit, times
+from flexpushdowndb_gb300.tupleset import Column, Table, export_host
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        names |= set(re.findall(r"\b(gfpdb_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported():
+    L = _abi.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    for s in syms:
+        assert hasattr(L, s), f"{s} declared in include/ but not exported"
+        assert s in _abi.SIGNATURES, f"{s} has no ctypes signature"
+
+
+def test_version_and_error_string():
+    L = _abi.lib()
+    assert L.gfpdb_version() >= 100
+    assert isinstance(L.gfpdb_last_error(), bytes)
+
+
+def test_plan_validation_accepts_workload_plans():
+    plan.validate(workloads.two_table_plan())
+    plan.validate(workloads.star_plan())
+
+
+@pytest.mark.parametrize(
+    "bad,fragment",
+    [
+        ('{"ops": []}', "CollatePOp"),
+        ('{"ops": [{"type": "CollatePOp", "name": "c"}, {"type": "CollatePOp", "name": "c"}]}', "duplicate"),
+        ('{"ops": [{"type": "FilterPOp", "name": "f", "predicate": {"type": "Like"}, "consumers": ["c"]},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "Like"),
+        ('{"ops": [{"type": "TableScanPOp", "name": "s", "table": "t", "consumers": ["nope"]},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "unknown"),
+        ('{"ops": [{"type": "HashJoinArrowPOp", "name": "j", "buildKey": "a", "probeKey": "b", "joinType": "FULL"},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "FULL"),
+        ("{not json", "JSON"),
+    ],
+)
+def test_plan_validation_errors(bad, fragment):
+    with pytest.raises(_abi.GfpdbError) as ei:
+        plan.validate(bad)
+    assert fragment in ei.value.message
+
+
+def small_table():
+    return Table([Column("a", "int32", [1, 2, 3]), Column("b", "int64", [4, 5, 6]),
+                  Column("s", "utf8", ["x", "y", "z"]), Column("f", "float64", [0.5, 1.5, 2.5])])
+
+
+@pytest.mark.parametrize(
+    "pred",
+    [
+        lt(col("a"), num_lit(2)),
+        and_(gt(col("b"), num_lit(4, "int64")), not_(eq(col("s"), str_lit("y")))),
+        or_(in_(col("a"), [1, 3]), lt(times(col("a"), col("b")), num_lit(10, "int64"))),
+        gt(col("f"), num_lit(1.0, "float64")),
+    ],
+)
+def test_filter_compiles_without_gpu(pred):
+    ops.Filter(pred, small_table())  # compile touches no device
+
+
+@pytest.mark.parametrize(
+    "pred,fragment",
+    [
+        (lt(col("missing"), num_lit(2)), "missing"),
+        ({"type": "Like", "left": col("s"), "right": str_lit("%x")}, "Like"),
+        (lt(col("s"), str_lit("x")), "strings"),
+        (times(col("a"), col("b")), "boolean"),
+    ],
+)
+def test_filter_compile_errors(pred, fragment):
+    with pytest.raises(_abi.GfpdbError) as ei:
+        ops.Filter(pred, small_table())
+    assert fragment in ei.value.message
+
+
+def test_group_spec_errors():
+    with pytest.raises(_abi.GfpdbError):
+        ops.Group(["a"], [{"function": "MEDIAN", "name": "m", "expr": col("a")}])
+    with pytest.raises(_abi.GfpdbError):
+        ops.Group(["a"], [{"function": "SUM", "name": "s"}])
+    ops.Group(["a"], [ops.aggregate("SUM", "s", col("b")), ops.aggregate("COUNT", "c")])
+
+
+def test_hashjoin_rejects_outer_joins():
+    L = _abi.lib()
+    h = ctypes.c_void_p()
+    rc = L.gfpdb_hashjoin_create(3, b"a", b"b", None, -1, 0.5, ctypes.byref(h))
+    assert rc == _abi.GFPDB_EUNSUPPORTED
+
+
+def test_export_host_roundtrip_structure():
+    t = small_table()
+    ex = export_host(t)
+    assert ex.schema.n_children == 4
+    assert ex.array.array.length == 3
+    assert ex.schema.children[2].contents.format == b"u"

@@ -1,0 +1,264 @@
+"""Operator parity on the GPU: every kernel path against the oracle, bit-exact.
+
+Filter / select outputs keep input order and are compared row by row; join
+and group outputs have no order and are compared as sorted multisets.
+"""
+
+import numpy as np
+import pytest
+
+from flexpushdowndb_gb300 import ops, workloads
+from flexpushdowndb_gb300.expression import (and_, cast, col, divide, eq, gt, gte, in_, isNull, lt, lte, minus, neq,
+                                             not_, num_lit, or_, plus, str_lit, times)
+from flexpushdowndb_gb300.tupleset import Column, DeviceTable, Table
+from oracle import ops as oops
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_table(n, seed=1):
+    rng = np.random.default_rng(seed)
+    return Table([
+        Column("i32", "int32", rng.integers(-1000, 1000, n)),
+        Column("i64", "int64", rng.integers(-10**12, 10**12, n)),
+        Column("d", "date32", rng.integers(8000, 11000, n)),
+        Column("f", "float64", rng.normal(0, 100, n)),
+        Column("k", "int32", rng.integers(0, 50, n)),
+        Column("s", "utf8", [("ab" * int(x))[: int(x) % 7] + str(int(x) % 5) for x in rng.integers(0, 40, n)]),
+    ])
+
+
+PREDICATES = [
+    lt(col("i32"), num_lit(0)),
+    and_(gte(col("i32"), num_lit(-100)), lt(col("i32"), num_lit(250)), gt(col("d"), num_lit(9000, "date32"))),
+    or_(eq(col("k"), num_lit(3)), eq(col("k"), num_lit(7)), lt(col("i64"), num_lit(0, "int64"))),
+    not_(and_(lt(col("i32"), num_lit(10)), gt(col("k"), num_lit(20)))),
+    in_(col("k"), [1, 2, 3, 40, 41], "int32"),
+    not_(in_(col("k"), [1, 2, 3], "int32")),
+    gt(col("f"), num_lit(12.5, "float64")),
+    lt(times(col("i32"), col("k")), num_lit(-5000, "int64")),
+    gt(plus(col("i64"), cast(col("i32"), "int64")), num_lit(0, "int64")),
+    lte(minus(col("i32"), col("k")), num_lit(7)),
+    eq(divide(col("i32"), num_lit(7)), num_lit(3)),
+    eq(col("s"), str_lit("ab3")),
+    and_(neq(col("s"), str_lit("0")), lt(col("k"), num_lit(25))),
+    in_(col("s"), ["1", "ab2", "abab4"], "utf8"),
+    not_(isNull(col("i32"))),
+    isNull(col("i32")),
+    gt(col("i32"), num_lit(10**6)),  # selects nothing
+]
+
+
+@pytest.mark.parametrize("pi", range(len(PREDICATES)))
+@pytest.mark.parametrize("n", [0, 1, 2047, 2048, 2049, 100_003])
+def test_filter_parity(gpu, pi, n):
+    t = rand_table(n, seed=n + pi)
+    pred = PREDICATES[pi]
+    f = ops.Filter(pred, t)
+    got = f.evaluate(t)
+    want = oops.filter_table(t, pred)
+    assert got.names == want.names
+    assert got.rows() == want.rows()
+
+
+def test_filter_projection_and_device_input(gpu):
+    t = rand_table(50_000, seed=3)
+    pred = and_(gt(col("k"), num_lit(10)), lt(col("i32"), num_lit(500)))
+    f = ops.Filter(pred, t)
+    got = f.evaluate(DeviceTable.from_host(t), project=["s", "i64", "nonexistent"][:2])
+    want = oops.filter_table(t, pred, ["s", "i64"])
+    assert got.names == ["s", "i64"]
+    assert got.rows() == want.rows()
+
+
+def test_bloom_bits_exact_and_no_false_negatives(gpu):
+    rng = np.random.default_rng(11)
+    keys = rng.choice(10**7, size=30_000, replace=False).astype(np.int64)
+    t = Table([Column("key", "int32", keys)])
+    parts = [t.slice(0, 10_000), t.slice(10_000, 30_000)]
+    bf = ops.BloomFilter(parts, "key", 10, 3)
+    info = bf.info()
+    assert info["num_blocks"] == oops.bloom_num_blocks(30_000, 10)
+    assert np.array_equal(bf.words(), oops.bloom_words(keys, 10, 3))
+    probe = Table([Column("key", "int32", np.concatenate([keys, rng.integers(0, 10**7, 100_000)]))])
+    got = bf.use(probe, "key")
+    want = oops.bloom_use(probe, oops.bloom_words(keys, 10, 3), "key")
+    assert got.rows() == want.rows()
+    assert set(keys.tolist()) <= set(got["key"].tolist())
+
+
+@pytest.mark.parametrize("n_keys", [0, 1, 7, 5000])
+def test_bloom_small_and_int64_keys(gpu, n_keys):
+    keys = (np.arange(n_keys, dtype=np.int64) * 7919 - 10**10)
+    t = Table([Column("k", "int64", keys), Column("v", "int32", np.arange(n_keys))])
+    bf = ops.BloomFilter([t], "k", 12, 4)
+    assert np.array_equal(bf.words(), oops.bloom_words(keys, 12, 4))
+    probe = Table([Column("k", "int64", np.arange(-50, 50, dtype=np.int64) * 7919 - 10**10)])
+    got = bf.use(probe, "k")
+    assert got.rows() == oops.bloom_use(probe, oops.bloom_words(keys, 12, 4), "k", 4).rows()
+
+
+def test_select_fused_chain_equals_sequential(gpu):
+    tabs = workloads.star_tables(fact_rows=300_000)
+    fact = tabs["fact"]
+    blooms = []
+    seq = fact
+    for i, c in ((2, 3), (3, 2), (4, 5), (1, 1)):
+        d = oops.filter_table(tabs[f"d{i}"], eq(col(f"d{i}_f"), num_lit(c)))
+        blooms.append((ops.BloomFilter([d], f"d{i}_pk"), f"fk{i}"))
+        seq = oops.bloom_use(seq, oops.bloom_words(d[f"d{i}_pk"]), f"fk{i}")
+    pred = gt(col("qty"), num_lit(10))
+    got = ops.select(DeviceTable.from_host(fact), ops.Filter(pred, fact), blooms)
+    want = oops.filter_table(seq, pred)
+    assert got.rows() == want.rows()
+
+
+@pytest.mark.parametrize("build_n,probe_n,dup", [(0, 10, 1), (10, 0, 1), (1000, 50_000, 1), (5000, 200_000, 3),
+                                                 (200_000, 300_000, 1)])
+def test_join_parity(gpu, build_n, probe_n, dup):
+    rng = np.random.default_rng(build_n + probe_n)
+    bkeys = np.repeat(np.arange(build_n // dup, dtype=np.int64), dup)[:build_n]
+    build = Table([Column("pk", "int32", bkeys), Column("bv", "int64", rng.integers(0, 10**9, len(bkeys))),
+                   Column("bs", "utf8", [f"s{x % 13}" for x in bkeys])])
+    probe = Table([Column("fk", "int32", rng.integers(-5, max(1, build_n // dup) + 5, probe_n)),
+                   Column("pv", "int32", rng.integers(0, 100, probe_n))])
+    j = ops.HashJoin("pk", "fk")
+    j.put_build(build)
+    j.finalize_build()
+    got = j.probe(DeviceTable.from_host(probe))
+    want = oops.hash_join(build, probe, "pk", "fk")
+    assert got.names == want.names == ["fk", "pv", "pk", "bv", "bs"]
+    assert got.sorted_rows() == want.sorted_rows()
+
+
+def test_join_int64_keys_and_multiple_build_batches(gpu):
+    rng = np.random.default_rng(5)
+    b1 = Table([Column("k", "int64", rng.integers(-2**40, 2**40, 3000)), Column("x", "int32", np.arange(3000))])
+    b2 = Table([Column("k", "int64", b1["k"][:500] + 1), Column("x", "int32", np.arange(500))])
+    probe = Table([Column("pk", "int64", np.concatenate([b1["k"], b2["k"], rng.integers(-2**40, 2**40, 3000)]))])
+    j = ops.HashJoin("k", "pk", needed=["pk", "x"])
+    j.put_build(b1)
+    j.put_build(b2)
+    j.finalize_build()
+    got = j.probe(probe)
+    b = Table([Column("k", "int64", np.concatenate([b1["k"], b2["k"]])),
+               Column("x", "int32", np.concatenate([b1["x"], b2["x"]]))])
+    want = oops.hash_join(b, probe, "k", "pk", ["pk", "x"])
+    assert got.sorted_rows() == want.sorted_rows()
+
+
+AGGS = [
+    {"function": "SUM", "name": "s", "expr": times(col("v"), col("w"))},
+    {"function": "COUNT", "name": "c"},
+    {"function": "MIN", "name": "mn", "expr": col("w")},
+    {"function": "MAX", "name": "mx", "expr": col("v")},
+    {"function": "SUM", "name": "s32", "expr": col("w")},
+]
+
+
+@pytest.mark.parametrize("n,groups,hint", [(0, 1, 0), (1, 1, 0), (10_000, 5, 0), (100_000, 175, 256),
+                                           (300_000, 50_000, 0), (300_000, 200_000, 400_000)])
+def test_group_parity(gpu, n, groups, hint):
+    rng = np.random.default_rng(n + groups)
+    t = Table([Column("g", "int32", rng.integers(0, groups, n)), Column("v", "int64", rng.integers(-10**15, 10**15, n)),
+               Column("w", "int32", rng.integers(-1000, 1000, n))])
+    g = ops.Group(["g"], AGGS, hint)
+    g.group(t)
+    got = g.finalise()
+    want = oops.group_by(t, ["g"], AGGS)
+    assert got.names == want.names
+    assert got.sorted_rows() == want.sorted_rows()
+
+
+def test_group_two_keys_utf8_key_and_batches(gpu):
+    rng = np.random.default_rng(9)
+    parts = []
+    for b in range(3):
+        n = 20_000 + b
+        parts.append(Table([Column("r", "utf8", [workloads.REGIONS[x] for x in rng.integers(0, 5, n)]),
+                            Column("a", "int32", rng.integers(0, 25, n)),
+                            Column("b", "int32", rng.integers(-3, 4, n)),
+                            Column("v", "int64", rng.integers(0, 10**7, n))]))
+    aggs = [{"function": "SUM", "name": "s", "expr": col("v")}, {"function": "COUNT", "name": "c"},
+            {"function": "AVG", "name": "avg", "expr": col("v")}]
+    g2 = ops.Group(["a", "b"], aggs)
+    gs = ops.Group(["r"], aggs)
+    for p in parts:
+        g2.group(p)
+        gs.group(DeviceTable.from_host(p))
+    allt = Table([Column(c.name, c.type, np.concatenate([p.column(c.name).values for p in parts])
+                         if c.type != "utf8" else sum((p[c.name] for p in parts), []))
+                  for c in parts[0].columns])
+    for g, keys in ((g2, ["a", "b"]), (gs, ["r"])):
+        got = g.finalise()
+        want = oops.group_by(allt, keys, aggs)
+        gr = sorted(got.rows())
+        wr = sorted(want.rows())
+        assert [r[:-1] for r in gr] == [r[:-1] for r in wr]
+        assert np.allclose([r[-1] for r in gr], [r[-1] for r in wr], rtol=1e-12)
+
+
+def test_group_special_key_and_int64_wrap(gpu):
+    big = np.iinfo(np.int64).max
+    t = Table([Column("g", "int64", [-1, -1, 0, 5, -1]), Column("v", "int64", [big, big, 1, 2, 3])])
+    aggs = [{"function": "SUM", "name": "s", "expr": col("v")}, {"function": "COUNT", "name": "c"}]
+    g = ops.Group(["g"], aggs)
+    g.group(t)
+    got = g.finalise()
+    assert got.sorted_rows() == oops.group_by(t, ["g"], aggs).sorted_rows()
+
+
+CSV_FIELDS = [("i", "int32"), ("l", "int64"), ("p", "decimal(15,2)"), ("dt", "date32"), ("s", "utf8")]
+
+
+def csv_text(n, seed=0, crlf=False, header=True, trailing=True):
+    rng = np.random.default_rng(seed)
+    lines = ["i|l|p|dt|s"] if header else []
+    for r in range(n):
+        cents = int(rng.integers(0, 10_000_000))
+        frac = ["", ".5", f".{cents % 100:02d}"][r % 3]
+        y, m, d = 1992 + r % 7, 1 + r % 12, 1 + r % 28
+        s = "".join(chr(65 + int(x)) for x in rng.integers(0, 26, r % 11))
+        if r % 5 == 0:
+            s = f'"{s}"'
+        lines.append(f"{int(rng.integers(-2**31, 2**31))}|{int(rng.integers(-2**62, 2**62))}|"
+                     f"{'-' if r % 4 == 0 else ''}{cents // 100}{frac}|{y:04d}-{m:02d}-{d:02d}|{s}")
+    text = ("\r\n" if crlf else "\n").join(lines)
+    if trailing:
+        text += "\r\n" if crlf else "\n"
+    return text.encode()
+
+
+@pytest.mark.parametrize("n,crlf,trailing", [(0, False, True), (1, False, False), (1000, True, True),
+                                             (50_000, False, True), (50_001, False, False)])
+def test_csv_parity(gpu, n, crlf, trailing):
+    text = csv_text(n, seed=n, crlf=crlf, trailing=trailing)
+    got = ops.csv_read(text, CSV_FIELDS, delimiter="|", has_header=True)
+    want = oops.csv_parse(text, CSV_FIELDS, delimiter="|", has_header=True)
+    assert got.names == want.names
+    assert got.rows() == want.rows()
+
+
+def test_csv_projection_and_malformed(gpu):
+    text = csv_text(3000, seed=2)
+    got = ops.csv_read(text, CSV_FIELDS, columns=["s", "p"], delimiter="|", has_header=True)
+    want = oops.csv_parse(text, CSV_FIELDS, columns=["s", "p"], delimiter="|", has_header=True)
+    assert got.rows() == want.rows()
+    from flexpushdowndb_gb300 import GfpdbError
+
+    with pytest.raises(GfpdbError) as ei:
+        ops.csv_read(b"1|2|x|1992-01-01|a\n", CSV_FIELDS, delimiter="|")
+    assert "malformed" in ei.value.message
+    with pytest.raises(GfpdbError):
+        ops.csv_read(b"1|2|3\n", CSV_FIELDS, delimiter="|")
+
+
+def test_error_reporting_leaves_device_usable(gpu):
+    from flexpushdowndb_gb300 import GfpdbError
+
+    t = Table([Column("a", "int32", [1, 2, 0]), Column("b", "int32", [1, 0, 3])])
+    with pytest.raises(GfpdbError) as ei:
+        ops.Filter(eq(divide(col("a"), col("b")), num_lit(1)), t).evaluate(t)
+    assert ei.value.code == 3  # device error word: integer divide by zero
+    ok = ops.Filter(gt(col("a"), num_lit(0)), t).evaluate(t)
+    assert ok.rows() == [(1, 1), (2, 0)]
