@@ -353,6 +353,18 @@ Operand operand_for(const ExprPtr& e, DType want, const std::vector<Field>& sche
   o.prog_begin = static_cast<int16_t>(p.n_instrs);
   emit_value(e, want, schema, p, slots);
   o.prog_len = static_cast<int16_t>(p.n_instrs - o.prog_begin);
+  // The device evaluates programs on a fixed stack of kStackDepth values:
+  // check the depth here so a kernel can never index past it.
+  int depth = 0, max_depth = 0;
+  for (int pc = o.prog_begin; pc < o.prog_begin + o.prog_len; ++pc) {
+    const int op = p.instrs[pc].op;
+    if (op == IO_COL || op == IO_LIT) ++depth;
+    else if (op == IO_ADD || op == IO_SUB || op == IO_MUL || op == IO_DIV) --depth;
+    if (depth < 1) fail(GFPDB_EINVAL, "internal: malformed arithmetic program");
+    max_depth = std::max(max_depth, depth);
+  }
+  if (depth != 1) fail(GFPDB_EINVAL, "internal: malformed arithmetic program");
+  if (max_depth > kStackDepth) fail(GFPDB_EUNSUPPORTED, "arithmetic expression nests too deeply for one kernel");
   return o;
 }
 

@@ -224,6 +224,9 @@ __global__ void __launch_bounds__(kCsvThreads) csv_convert_kernel(const __grid_c
       }
     }
     fs[F] = static_cast<int32_t>(e + 1 - b);
+    // A short row leaves its missing fields empty (start = end of row), so
+    // phase B never reads outside the row; the row is reported as malformed.
+    for (int j = k; j < F; ++j) fs[j] = fs[F];
     if (k != F) raise_status(p.st, GFPDB_EINVAL, static_cast<int32_t>(row < INT32_MAX ? row : INT32_MAX));
   }
   __syncthreads();
@@ -238,6 +241,7 @@ __global__ void __launch_bounds__(kCsvThreads) csv_convert_kernel(const __grid_c
     const int64_t rb = p.starts[row0 + r];
     int64_t b = rb + fs[o.field];
     int64_t e = rb + fs[o.field + 1] - 1;
+    if (e < b) e = b;
     trim_quotes(p.text, b, e);
     const int64_t orow = row0 + r;
     bool ok = true;

@@ -759,7 +759,7 @@ class GroupTable {
     DevStatus h = read_status(status->as<DevStatus>(), s);
     raise_device_status(h, "group-by");
     for (auto& d : dicts)
-      if (d) raise_device_status(read_status(d->status->as<DevStatus>(), s), "string dictionary");
+      if (d && d->status) raise_device_status(read_status(d->status->as<DevStatus>(), s), "string dictionary");
     const int64_t n_groups = h.aux[0];
     FinalParams fp;
     std::memset(&fp, 0, sizeof(fp));
