@@ -117,6 +117,7 @@ SIGNATURES = {
     "gfpdb_filter_compile": (_I32, [ctypes.c_char_p, _S, ctypes.POINTER(_P)]),
     "gfpdb_filter_evaluate": (_I32, [_P, _S, _A, _CP, _I32, _S, _A, _P]),
     "gfpdb_filter_free": (None, [_P]),
+    "gfpdb_filter_evaluate_noalloc": (_I32, [_P, _S, _A, _CP, _I32, ctypes.POINTER(_P), ctypes.POINTER(_I64), _P]),
     "gfpdb_bloom_create": (_I32, [_S, ctypes.POINTER(_A), _I32, ctypes.c_char_p, _I32, _I32, ctypes.POINTER(_P), _P]),
     "gfpdb_bloom_use": (_I32, [_P, _S, _A, ctypes.c_char_p, _S, _A, _P]),
     "gfpdb_bloom_info": (

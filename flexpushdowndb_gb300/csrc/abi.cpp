@@ -7,55 +7,13 @@
 #include <string>
 
 #include "../../include/gfpdb.h"
+#include "host/handles.h"
 #include "host/pop.h"
 #include "kernels/launch.h"
 
 using namespace gfpdb;
 
-struct gfpdb_filter {
-  CompiledPredicate pred;
-};
-
-struct gfpdb_bloom {
-  BloomPtr bloom;
-};
-
-struct gfpdb_hashjoin {
-  int32_t join_type = GFPDB_JOIN_INNER;
-  std::string build_key, probe_key;
-  std::vector<std::string> needed;
-  bool all_columns = true;
-  double load_factor = 0.5;
-  std::vector<TupleSetPtr> build;
-  JoinTable table;
-  bool built = false;
-};
-
-struct gfpdb_group {
-  std::shared_ptr<GroupTable> table;
-};
-
 namespace {
-
-thread_local std::string g_last_error;
-
-template <typename F>
-int32_t guarded(F&& f) {
-  try {
-    g_last_error.clear();
-    f();
-    return GFPDB_OK;
-  } catch (const Error& e) {
-    g_last_error = e.what();
-    return e.code();
-  } catch (const std::bad_alloc&) {
-    g_last_error = "host allocation failed";
-    return GFPDB_ENOMEM;
-  } catch (const std::exception& e) {
-    g_last_error = e.what();
-    return GFPDB_EINVAL;
-  }
-}
 
 cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
@@ -76,7 +34,7 @@ void require(bool cond, const char* what) {
 
 extern "C" {
 
-const char* gfpdb_last_error(void) { return g_last_error.c_str(); }
+const char* gfpdb_last_error(void) { return last_error().c_str(); }
 
 int32_t gfpdb_version(void) { return 100; }
 

@@ -9,6 +9,11 @@ std::atomic<uint64_t> g_kernel_launches{0};
 
 void fail(int32_t code, const std::string& msg) { throw Error(code, msg); }
 
+std::string& last_error() {
+  thread_local std::string msg;
+  return msg;
+}
+
 void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) {
     fail(e == cudaErrorMemoryAllocation ? GFPDB_ENOMEM : GFPDB_ECUDA,

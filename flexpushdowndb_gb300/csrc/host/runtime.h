@@ -29,6 +29,29 @@ class Error : public std::runtime_error {
 };
 
 [[noreturn]] void fail(int32_t code, const std::string& msg);
+
+// Message of the last failed C-ABI call on this thread.
+std::string& last_error();
+
+// Run `f` for a C entry point: GFPDB_OK, or the failure's code with its
+// message stored in last_error().
+template <typename F>
+int32_t guarded(F&& f) {
+  try {
+    last_error().clear();
+    f();
+    return GFPDB_OK;
+  } catch (const Error& e) {
+    last_error() = e.what();
+    return e.code();
+  } catch (const std::bad_alloc&) {
+    last_error() = "host allocation failed";
+    return GFPDB_ENOMEM;
+  } catch (const std::exception& e) {
+    last_error() = e.what();
+    return GFPDB_EINVAL;
+  }
+}
 void check_cuda(cudaError_t e, const char* what);
 #define GF_CUDA(call) ::gfpdb::check_cuda((call), #call)
 

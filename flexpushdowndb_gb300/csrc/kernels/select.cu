@@ -19,8 +19,10 @@
 // with coalesced stores. Small bloom filters are staged in shared memory once
 // per CTA.
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
+#include "../host/handles.h"
 #include "bloom.cuh"
 #include "eval.cuh"
 #include "launch.h"
@@ -190,7 +192,7 @@ __device__ __forceinline__ uint32_t leaf8(const SelectParams& p, const Leaf& L, 
 }
 
 __global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_constant__ SelectParams p) {
-  extern __shared__ uint32_t s_bloom[];
+  extern __shared__ __align__(16) uint32_t s_bloom[];
   __shared__ int32_t s_rows[kSelTile];
   __shared__ int s_warp[kSelThreads / 32 + 1];
   __shared__ uint32_t s_tile;
@@ -456,3 +458,149 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
 }
 
 }  // namespace gfpdb
+
+// ---------------------------------------------------------------------------
+// Filter evaluation that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc at all: code running while a CUDA graph
+// is being captured, engines that hand the library a fixed arena and forbid
+// it from growing the device heap, and embedders whose allocator is owned by
+// another runtime. For them gfpdb_filter_evaluate_noalloc runs the same
+// select_kernel with its scratch (the call's status block, the tile ticket
+// and one look-back word per 2048-row tile) in the file-scope array below
+// instead of a per-call allocation. The array is sized for
+// kNoAllocMaxRows input rows (about 1 MiB) and, being a __device__ variable,
+// lives on every GPU that loads this library until the process exits.
+namespace gfpdb {
+namespace {
+
+constexpr int64_t kNoAllocMaxRows = int64_t{1} << 28;  // 268,435,456 rows
+constexpr int64_t kNoAllocMaxTiles = kNoAllocMaxRows / kSelTile;
+constexpr size_t kNoAllocHeader = 128;  // DevStatus (64 B) + ticket line (64 B)
+constexpr size_t kNoAllocScratchBytes = kNoAllocHeader + static_cast<size_t>(kNoAllocMaxTiles) * 8;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch for each device, looked up once per
+// device with that device current (host code only has a host-side stand-in
+// for the symbol, which must never be passed to a kernel).
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};
+
+void* noalloc_scratch_address(int device) {
+  if (device < 0 || device >= 64) fail(GFPDB_EUNSUPPORTED, "device index above 63");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_addr[device] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) check_cuda(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_addr[device] = p;
+  }
+  return g_noalloc_addr[device];
+}
+
+int find_child(const ArrowSchema* schema, const char* name) {
+  for (int64_t i = 0; i < schema->n_children; ++i) {
+    const char* cn = schema->children[i]->name;
+    if (cn != nullptr && std::strcmp(cn, name) == 0) return static_cast<int>(i);
+  }
+  return -1;
+}
+
+}  // namespace
+}  // namespace gfpdb
+
+extern "C" int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, const ArrowSchema* in_schema,
+                                                 const ArrowDeviceArray* in, const char* const* project_columns,
+                                                 int32_t n_project, void* const* out_columns, int64_t* out_num_rows,
+                                                 void* stream) {
+  using namespace gfpdb;
+  return guarded([&] {
+    if (filter == nullptr || in_schema == nullptr || in == nullptr || out_num_rows == nullptr)
+      fail(GFPDB_EINVAL, "null argument");
+    if (n_project < 0 || (n_project > 0 && (project_columns == nullptr || out_columns == nullptr)))
+      fail(GFPDB_EINVAL, "project_columns and out_columns must list the output columns");
+    if (n_project > kMaxCols) fail(GFPDB_EUNSUPPORTED, "too many output columns");
+    if (in_schema->format == nullptr || std::strcmp(in_schema->format, "+s") != 0)
+      fail(GFPDB_EINVAL, "a TupleSet schema must be a struct (format \"+s\")");
+    if (in->device_type != ARROW_DEVICE_CUDA)
+      fail(GFPDB_EINVAL, "gfpdb_filter_evaluate_noalloc needs device-resident input (ARROW_DEVICE_CUDA)");
+    const ArrowArray& arr = in->array;
+    if (arr.n_children != in_schema->n_children) fail(GFPDB_EINVAL, "ArrowArray child count does not match the schema");
+    const int64_t n = arr.length;
+    if (n < 0) fail(GFPDB_EINVAL, "negative row count");
+    if (n > kNoAllocMaxRows)
+      fail(GFPDB_EINVAL, "gfpdb_filter_evaluate_noalloc: " + std::to_string(n) + " rows exceed its maximum of " +
+                             std::to_string(kNoAllocMaxRows) + " rows");
+    int device = 0;
+    GF_CUDA(cudaGetDevice(&device));
+    // First call on this device: look up the scratch address (no allocation).
+    void* scratch = noalloc_scratch_address(device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    SelectParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.n_rows = n;
+    const CompiledPredicate& pred = filter->pred;
+    p.prog = pred.prog;
+    // Bind the predicate's columns straight from the Arrow structures.
+    bool aligned = true;
+    for (size_t i = 0; i < pred.slots.names.size(); ++i) {
+      const int ci = find_child(in_schema, pred.slots.names[i].c_str());
+      if (ci < 0) fail(GFPDB_EINVAL, "column '" + pred.slots.names[i] + "' not found in TupleSet");
+      const DType t = dtype_from_format(in_schema->children[ci]->format);
+      if (t != pred.slots.types[i]) fail(GFPDB_EINVAL, "column '" + pred.slots.names[i] + "' changed type");
+      const ArrowArray* c = arr.children[ci];
+      if (c->null_count != 0 && c->buffers[0] != nullptr) fail(GFPDB_EUNSUPPORTED, "nullable inputs are not supported");
+      const int64_t off = c->offset + arr.offset;
+      if (t == DType::Utf8) {
+        p.cols[i].offsets = static_cast<const int32_t*>(c->buffers[1]) + off;
+        p.cols[i].data = c->buffers[2];
+      } else {
+        p.cols[i].data = static_cast<const char*>(c->buffers[1]) + off * dtype_width(t);
+        if ((reinterpret_cast<uintptr_t>(p.cols[i].data) & 15u) != 0) aligned = false;
+      }
+      p.cols[i].type = static_cast<int32_t>(t);
+    }
+    p.n_cols = static_cast<int32_t>(pred.slots.names.size());
+    p.aligned = aligned ? 1 : 0;
+    // Outputs: fixed-width columns written straight into the caller's buffers.
+    for (int32_t j = 0; j < n_project; ++j) {
+      if (project_columns[j] == nullptr || out_columns[j] == nullptr) fail(GFPDB_EINVAL, "null output column");
+      const int ci = find_child(in_schema, project_columns[j]);
+      if (ci < 0) fail(GFPDB_EINVAL, std::string("column '") + project_columns[j] + "' not found in TupleSet");
+      const DType t = dtype_from_format(in_schema->children[ci]->format);
+      if (t == DType::Utf8) fail(GFPDB_EUNSUPPORTED, "utf8 outputs need allocation; use gfpdb_filter_evaluate");
+      const ArrowArray* c = arr.children[ci];
+      OutCol& oc = p.outs[p.n_out++];
+      oc.src = static_cast<const char*>(c->buffers[1]) + (c->offset + arr.offset) * dtype_width(t);
+      oc.dst = out_columns[j];
+      oc.width = dtype_width(t);
+    }
+    const int64_t n_tiles = (n + kSelTile - 1) / kSelTile;
+    p.n_tiles = n_tiles;
+    char* sb = static_cast<char*>(scratch);
+    p.status = reinterpret_cast<DevStatus*>(sb);
+    p.ticket = reinterpret_cast<uint32_t*>(sb + sizeof(DevStatus));
+    p.tile_status = reinterpret_cast<uint64_t*>(sb + kNoAllocHeader);
+    // The array keeps the previous call's contents: clear the status block,
+    // the ticket and this call's tile words.
+    GF_CUDA(cudaMemsetAsync(sb, 0, kNoAllocHeader + static_cast<size_t>(n_tiles) * 8, s));
+    int64_t count = 0;
+    if (n_tiles > 0) {
+      int per_sm = 0;
+      GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_kernel, kSelThreads, 0));
+      if (per_sm < 1) per_sm = 1;
+      int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
+      if (grid > n_tiles) grid = n_tiles;
+      select_kernel<<<static_cast<int>(grid), kSelThreads, 0, s>>>(p);
+      after_launch("select_kernel");
+      DevStatus hs;
+      GF_CUDA(cudaMemcpyAsync(&hs, p.status, sizeof(hs), cudaMemcpyDeviceToHost, s));
+      GF_CUDA(cudaStreamSynchronize(s));
+      raise_device_status(hs, "select");
+      count = hs.value;
+    }
+    *out_num_rows = count;
+  });
+}

@@ -120,6 +120,30 @@ int32_t gfpdb_filter_evaluate(const gfpdb_filter* filter, const struct ArrowSche
 
 void gfpdb_filter_free(gfpdb_filter* filter);
 
+/* The filter of gfpdb_filter_evaluate for callers that cannot allocate device
+ * memory (code running under CUDA graph capture, engines that own a fixed
+ * device arena, embedders whose allocator belongs to another runtime). It has
+ * no counterpart in the reference. It allocates nothing: the kernel's scratch
+ * (status block, tile ticket, one look-back word per 2048-row tile) lives in a
+ * file-scope __device__ array of about 1 MiB that every GPU loading the
+ * library keeps until exit, and the caller passes the outputs.
+ *  - Input must be device-resident (ARROW_DEVICE_CUDA) and at most
+ *    268,435,456 rows; larger inputs are rejected with GFPDB_EINVAL.
+ *  - out_columns[j] is a device buffer for project_columns[j] with room for
+ *    in->array.length values of that column's width; only fixed-width columns
+ *    (int32, int64, date32, float64) can be outputs.
+ *  - *out_num_rows receives the number of selected rows (the call waits for
+ *    its stream).
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - All calls share the one array, and each call clears the part it uses, so
+ *    calls that overlap on the GPU (other streams, other threads) race:
+ *    serialise them. */
+int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, const struct ArrowSchema* in_schema,
+                                      const struct ArrowDeviceArray* in, const char* const* project_columns,
+                                      int32_t n_project, void* const* out_columns, int64_t* out_num_rows,
+                                      void* stream);
+
 /* ------------------------------------------------------------------ bloom */
 
 /* Build a blocked bloom filter (256-bit blocks, `num_hashes` bits per key set
