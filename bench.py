@@ -9,11 +9,18 @@ synthetic data (SplitMix64), generated on the host.
 
 A step is one execution of the physical plan (TableScan -> Filter ->
 BloomFilterCreate / BloomFilterUse chains -> HashJoinArrow x4 -> Group ->
-Collate) through the C ABI gfpdb_execute_plan.
-  value : fact rows/s with every input table already resident in HBM.
-  e2e   : the same call with the tables in pinned host memory; the
-          host-to-device copies of every input and the device-to-host copy of
-          the result are inside the timed region.
+Collate) through the C ABI gfpdb_execute_plan, every kernel re-run on the
+inputs each step.
+  value : fact rows/s, inputs resident in HBM, the plan's operator pipeline
+          captured once as a CUDA graph and replayed each step
+          ("cudaGraph": true; deferred row counts, one synchronization).
+  plain : the same plan launched operator by operator each step (the
+          drop-in per-operator path), reported beside value.
+  e2e   : the graph path with the tables in pinned host memory: every input's
+          host-to-device copy and the result's device-to-host copy are inside
+          the timed region.
+The dominant kernel's roofline comes from a separate profiled pass of the
+plain path (CUDA events around every launch on its own stream).
 With --gpus N (torchrun), each rank runs its own fact partition (weak
 scaling, no collective on the data path); value = all ranks' fact rows / the
 slowest rank's time.
@@ -25,6 +32,7 @@ all host threads) on the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -51,7 +59,7 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling while the benchmark runs."""
 
     QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -72,7 +80,7 @@ class ClockSampler:
                     self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(0.1)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
@@ -140,6 +148,54 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_case(args):
+    """Single-kernel cases for profiling (ncu) and kernel tuning; prints one
+    JSON line with the case's own timing. `select`: the forward bloom probe of
+    the star query (fk2 against the 1/25 dim filter) over the 6M-row fact
+    table, as one BloomFilterUsePOp runs it; `select4`: all four forward
+    probes fused in one pass."""
+    import torch
+
+    from flexpushdowndb_gb300 import ops, workloads
+    from flexpushdowndb_gb300.expression import col, eq, num_lit
+    from flexpushdowndb_gb300.tupleset import DeviceTable
+    from oracle import ops as oops
+
+    ops.init(0)
+    tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
+    fact = DeviceTable.from_host(tabs["fact"])
+    if args.case in ("plan", "plan-graph"):
+        from flexpushdowndb_gb300 import plan
+
+        d = json.loads(workloads.star_plan().to_json())
+        if args.case == "plan-graph":
+            d["cudaGraph"] = True
+        text = json.dumps(d)
+        inputs = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
+        fn = lambda: plan.execute(text, inputs).table  # noqa: E731
+    elif args.case == "select":
+        d2 = oops.filter_table(tabs["d2"], eq(col("d2_f"), num_lit(3)))
+        bf = ops.BloomFilter([d2], "d2_pk")
+        fn = lambda: ops.select(fact, blooms=[(bf, "fk2")])  # noqa: E731
+    elif args.case == "select4":
+        blooms = []
+        for i, c in ((2, 3), (3, 2), (4, 5), (1, 1)):
+            d = oops.filter_table(tabs[f"d{i}"], eq(col(f"d{i}_f"), num_lit(c)))
+            blooms.append((ops.BloomFilter([d], f"d{i}_pk"), f"fk{i}"))
+        fn = lambda: ops.select(fact, blooms=blooms)  # noqa: E731
+    else:
+        raise SystemExit(f"unknown case {args.case}")
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = fn()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    print(json.dumps({"case": args.case, "rows": args.rows, "ms_per_call": 1e3 * dt, "rows_out": out.num_rows}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -148,7 +204,11 @@ def main():
     ap.add_argument("--impl", default="gfpdb", choices=["gfpdb", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph")
+    ap.add_argument("--rows", type=int, default=FACT_ROWS)
     args = ap.parse_args()
+    if args.case:
+        return run_case(args)
     if args.warmup < 3:
         args.warmup = 3
 
@@ -158,7 +218,6 @@ def main():
     if args.impl == "reference":
         return run_reference(args, rank, world if "RANK" in os.environ else 1)
 
-    import numpy as np
     import torch
 
     dist = None
@@ -170,70 +229,99 @@ def main():
 
     from flexpushdowndb_gb300 import _abi, ops, plan, workloads
     from flexpushdowndb_gb300.tupleset import DeviceTable
+    from oracle import queries
 
     torch.cuda.set_device(local)
     ops.init(local)
     L = _abi.lib()
     stream = torch.cuda.current_stream()
-    sptr = ctypes_stream(stream)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
 
     tables = workloads.star_tables(fact_rows=FACT_ROWS, seed=2000 + 7 * rank)
-    star = workloads.star_plan()
-    text = star.to_json()
+    plan_d = json.loads(workloads.star_plan().to_json())
+    plain_text = json.dumps(plan_d)
+    graph_text = json.dumps(dict(plan_d, cudaGraph=True))
     dev_inputs = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tables.items()})
     host_inputs = plan.PreparedInputs(tables, pinned=True)
     input_bytes = sum(t.nbytes() for t in tables.values())
-
-    # parity check (outside the timed region): bit-exact against the oracle
-    from oracle import queries
-
-    got = plan.execute(text, dev_inputs, stream=sptr).table
-    want = queries.star_query(tables)
-    parity = got.sorted_rows() == want.sorted_rows()
+    want = queries.star_query(tables).sorted_rows()
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- value: device-resident inputs
-    for _ in range(args.warmup):
-        plan.execute(text, dev_inputs, stream=sptr)
-    _abi.check(L.gfpdb_profile_reset())
-    _abi.check(L.gfpdb_profile_enable(1))
-    launches0 = ops.kernel_launches()
-    step_ms = []
-    with ClockSampler(local) as clocks:
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(text, inputs, steps):
+        """K steps bracketed by barrier + synchronize; CUDA events on the
+        stream for the region and for each step."""
         barrier()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        per = []
+        stats = None
         ev0.record(stream)
-        for _ in range(args.steps):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            plan.execute(text, dev_inputs, stream=sptr)
+            r = plan.execute(text, inputs, stream=sptr)
             b.record(stream)
-            step_ms.append((a, b))
+            per.append((a, b))
+            stats = r.stats
         ev1.record(stream)
         barrier()
-    _abi.check(L.gfpdb_profile_enable(0))
-    launches = (ops.kernel_launches() - launches0) / args.steps
-    total_ms = ev0.elapsed_time(ev1)
-    per_step = [a.elapsed_time(b) for a, b in step_ms]
-    ms = total_ms / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = FACT_ROWS * world / (ms / 1e3)
+        return ev0.elapsed_time(ev1) / steps, [a.elapsed_time(b) for a, b in per], stats, r
 
-    # per-kernel live timings from the timed region
-    buf = ctypes_buffer(4096)
+    with ClockSampler(local) as clocks:
+        # parity of every path (outside the timed regions), bit-exact
+        parity = all(plan.execute(t, i, stream=sptr).table.sorted_rows() == want
+                     for t, i in ((plain_text, dev_inputs), (graph_text, dev_inputs), (graph_text, dev_inputs),
+                                  (graph_text, host_inputs), (graph_text, host_inputs)))
+        # ---- value: captured plan, device-resident inputs
+        for _ in range(args.warmup):
+            plan.execute(graph_text, dev_inputs, stream=sptr)
+        launches0 = ops.kernel_launches()
+        ms, per_step, _, last = timed(graph_text, dev_inputs, args.steps)
+        launches = (ops.kernel_launches() - launches0) / args.steps
+        parity = parity and last.table.sorted_rows() == want
+        ms = max_over_ranks(ms)
+        value = FACT_ROWS * world / (ms / 1e3)
+        # ---- plain per-operator path, same inputs
+        for _ in range(args.warmup):
+            plan.execute(plain_text, dev_inputs, stream=sptr)
+        plain_ms, plain_steps, _, _ = timed(plain_text, dev_inputs, args.steps)
+        plain_ms = max_over_ranks(plain_ms)
+        # ---- e2e: pinned host inputs through the same C-ABI call
+        for _ in range(args.warmup):
+            plan.execute(graph_text, host_inputs, stream=sptr)
+        barrier()
+        e2e_times = []
+        h2d = d2h = 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = plan.execute(graph_text, host_inputs, stream=sptr)
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
+            h2d, d2h = r.stats["h2d_bytes"], r.stats["d2h_bytes"]
+        barrier()
+        e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times))
+        # ---- profiled pass: every kernel launch of the plain path timed with
+        # CUDA events on its stream, algorithmic bytes per launch
+        _abi.check(L.gfpdb_profile_reset())
+        _abi.check(L.gfpdb_profile_enable(1))
+        timed(plain_text, dev_inputs, args.steps)
+        _abi.check(L.gfpdb_profile_enable(0))
+
+    buf = ctypes.create_string_buffer(4096)
     _abi.check(L.gfpdb_profile_kernels(buf, 4096))
     kernels = {}
     for name in buf.value.decode().split():
-        n, t_ms, by = ctypes_i64(), ctypes_f64(), ctypes_f64()
+        n, t_ms, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
         _abi.check(L.gfpdb_profile_read(name.encode(), n, t_ms, by))
         kernels[name] = {"launches": n.value, "ms": t_ms.value, "bytes": by.value}
     gpu_ms_total = sum(k["ms"] for k in kernels.values())
@@ -248,51 +336,39 @@ def main():
         if tp.exists():
             traffic = json.loads(tp.read_text()).get(top)
         roofline = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                    if peak_kind == "measured" else "fallback 6.8 TB/s",
+                    "frac": achieved / peak,
+                    "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                    else "fallback 6.8 TB/s",
                     "traffic": traffic, "launches_per_step": k["launches"] / args.steps,
                     "avg_launch_us": 1e3 * k["ms"] / max(1, k["launches"]),
                     "algorithmic_bytes_per_launch": k["bytes"] / max(1, k["launches"]),
                     "share_of_kernel_time": k["ms"] / gpu_ms_total if gpu_ms_total else None}
 
-    # ---- e2e: pinned host inputs, copies inside the timed region
-    for _ in range(args.warmup):
-        plan.execute(text, host_inputs, stream=sptr)
-    barrier()
-    e2e_times = []
-    h2d = d2h = 0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        r = plan.execute(text, host_inputs, stream=sptr)
-        torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t0)
-        h2d, d2h = r.stats["h2d_bytes"], r.stats["d2h_bytes"]
-    barrier()
-    e2e_s = sum(e2e_times) / len(e2e_times)
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-
     if rank != 0:
-        dist.destroy_process_group() if dist is not None else None
+        if dist is not None:
+            dist.destroy_process_group()
         return
     base = None
     if world == 1 and not args.no_cpu_baseline:
         b = cpu_baseline(tables, 3, 1, budget_s=args.cpu_seconds)
         base = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
     lat = sorted(per_step)
+    plat = sorted(plain_steps)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic (SplitMix64-seeded), generated on the host",
         "config": {"workload": "star query with bloom predicate transfer, fact 6,000,000 rows (SSB-SF1 shape)",
                    "fact_rows_per_gpu": FACT_ROWS, "dims": [30000, 200000, 2000, 2556],
-                   "bloom": "10 bits/key, 3 hashes, forward + backward", "path": "plain per-operator plan",
-                   "l2": "inputs (%.0f MB) larger than the 129 MB L2" % (input_bytes / 1e6),
+                   "bloom": "10 bits/key, 3 hashes, forward + backward",
+                   "path": "plan captured as a CUDA graph (deferred row counts), replayed per step",
+                   "l2": "inputs (%.0f MB) larger than the 129 MB L2; no flush needed" % (input_bytes / 1e6),
                    "parallelism": f"replicas x{world}"},
         "queries_per_s": world * 1e3 / ms,
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "plain": {"value": FACT_ROWS * world / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                  "queries_per_s": world * 1e3 / plain_ms,
+                  "latency_ms": {"p50": plat[len(plat) // 2], "p99": plat[min(len(plat) - 1, int(0.99 * len(plat)))]}},
         "parity": parity,
         "e2e": {"value": FACT_ROWS * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s},
@@ -306,30 +382,6 @@ def main():
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
-
-
-def ctypes_stream(stream):
-    import ctypes
-
-    return ctypes.c_void_p(stream.cuda_stream)
-
-
-def ctypes_buffer(n):
-    import ctypes
-
-    return ctypes.create_string_buffer(n)
-
-
-def ctypes_i64():
-    import ctypes
-
-    return ctypes.c_int64()
-
-
-def ctypes_f64():
-    import ctypes
-
-    return ctypes.c_double()
 
 
 if __name__ == "__main__":

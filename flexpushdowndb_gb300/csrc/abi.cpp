@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "../../include/gfpdb.h"
@@ -28,6 +30,217 @@ std::vector<std::string> names_of(const char* const* names, int32_t n) {
 
 void require(bool cond, const char* what) {
   if (!cond) fail(GFPDB_EINVAL, what);
+}
+
+// ---- captured plans
+//
+// A plan run with "cudaGraph": true is captured once per (device, plan text,
+// input buffers) into a CUDA graph whose allocations come from a bump arena
+// sized from an ordinary run, so every replay finds its inputs, outputs and
+// status blocks at the same addresses. A replay is one graph launch plus the
+// same end-of-plan status checks as an ordinary deferred run.
+struct CapturedPlan {
+  std::unique_ptr<Arena> arena;
+  cudaGraphExec_t exec = nullptr;
+  // Epilogue graph: packs every status block and the result (row count and
+  // columns) into one arena buffer and copies it to pinned host memory.
+  cudaGraphExec_t epilogue = nullptr;
+  char* pinned = nullptr;
+  int64_t pinned_bytes = 0;
+  std::vector<int64_t> status_off;
+  int64_t count_off = -1;  // result row count (deferred result), else exact_rows
+  int64_t exact_rows = 0;
+  std::vector<std::vector<int64_t>> col_off;  // per result column, its buffers
+  TupleSetPtr result;
+  std::vector<DeferredCheck> checks;
+  uint64_t kernels = 0;
+  int64_t num_ops = 0, messages = 0, h2d = 0;
+  bool capturable = true;
+  ~CapturedPlan() {
+    if (exec) (void)cudaGraphExecDestroy(exec);
+    if (epilogue) (void)cudaGraphExecDestroy(epilogue);
+    if (pinned) (void)cudaFreeHost(pinned);
+  }
+};
+
+// Capture the epilogue of a captured plan (see CapturedPlan::epilogue).
+bool capture_epilogue(CapturedPlan& cp, cudaStream_t cs) {
+  std::vector<CopySpan> spans;
+  int64_t off = 0;
+  auto add = [&](const void* src, int64_t bytes) {
+    const int64_t o = off;
+    spans.push_back(CopySpan{src, bytes, o});
+    off += (bytes + 255) / 256 * 256;
+    return o;
+  };
+  for (auto& c : cp.checks) cp.status_off.push_back(add(c.status, sizeof(DevStatus)));
+  const TupleSet& r = *cp.result;
+  const int64_t cap = r.num_rows();
+  if (r.exact()) cp.exact_rows = cap;
+  else cp.count_off = add(r.rows_dev(), sizeof(int64_t));
+  for (int i = 0; i < r.num_columns(); ++i) {
+    const auto& c = r.column(i);
+    if (c->type == DType::Utf8) {
+      if (!c->data_buf) return false;
+      const int64_t o1 = add(c->offsets, (cap + 1) * 4);
+      const int64_t o2 = add(c->data, c->data_buf->size());
+      cp.col_off.push_back({o1, o2});
+    } else {
+      cp.col_off.push_back({add(c->data, cap * dtype_width(c->type))});
+    }
+  }
+  cp.pinned_bytes = off > 0 ? off : 256;
+  GF_CUDA(cudaMallocHost(reinterpret_cast<void**>(&cp.pinned), cp.pinned_bytes));
+  void* dev = cp.arena->take(cp.pinned_bytes);
+  cudaGraph_t graph = nullptr;
+  bool ok = true;
+  GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  try {
+    pack_spans(spans, dev, cs);
+    GF_CUDA(cudaMemcpyAsync(cp.pinned, dev, cp.pinned_bytes, cudaMemcpyDeviceToHost, cs));
+  } catch (const std::exception&) {
+    ok = false;
+  }
+  if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) ok = false;
+  if (ok && cudaGraphInstantiate(&cp.epilogue, graph, 0) != cudaSuccess) ok = false;
+  if (graph) (void)cudaGraphDestroy(graph);
+  (void)cudaGetLastError();
+  return ok;
+}
+
+std::mutex g_graph_mu;
+std::map<std::string, std::shared_ptr<CapturedPlan>> g_graphs;
+
+std::string plan_key(const char* plan_json, int32_t n_tables, const char* const* names,
+                     const ArrowDeviceArray* const* arrays) {
+  std::string key = std::to_string(current_device()) + "|" + plan_json;
+  for (int32_t i = 0; i < n_tables; ++i) {
+    const ArrowArray& a = arrays[i]->array;
+    key += "|" + std::string(names[i]) + ":" + std::to_string(arrays[i]->device_type) + ":" +
+           std::to_string(a.length) + ":" + std::to_string(a.offset);
+    for (int64_t c = 0; c < a.n_children; ++c)
+      for (int64_t b = 0; b < a.children[c]->n_buffers; ++b)
+        key += ":" + std::to_string(reinterpret_cast<uintptr_t>(a.children[c]->buffers[b]));
+  }
+  return key;
+}
+
+struct ArenaGuard {
+  explicit ArenaGuard(Arena* a) { set_thread_arena(a); }
+  ~ArenaGuard() { set_thread_arena(nullptr); }
+};
+
+std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::map<std::string, pop::InputTable>& inputs,
+                                           int64_t arena_bytes) {
+  auto cp = std::make_shared<CapturedPlan>();
+  cudaStream_t cs = nullptr;
+  GF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { (void)cudaStreamDestroy(s); }
+  } sg{cs};
+  // The arena outlives the capture stream: allocate it on the legacy stream.
+  cp->arena = std::make_unique<Arena>(arena_bytes, nullptr);
+  sync(nullptr);
+  const uint64_t k0 = g_kernel_launches.load();
+  const int64_t h2d0 = copy_counters().h2d;
+  cudaGraph_t graph = nullptr;
+  bool ok = true;
+  {
+    ArenaGuard ag(cp->arena.get());
+    GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+      auto ex = pop::build_execution(plan, cs);
+      ex->setInputs(inputs);
+      ex->setDeferred(true);
+      ex->setCapturing(true);
+      cp->result = ex->execute();
+      cp->checks = ex->takeCapturedChecks();
+      cp->num_ops = ex->stats().num_ops;
+      cp->messages = ex->stats().messages;
+    } catch (const std::exception&) {
+      ok = false;  // something in the plan needs the host mid-run
+    }
+    const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (e != cudaSuccess) ok = false;
+  }
+  (void)cudaGetLastError();
+  if (ok && graph != nullptr && cudaGraphInstantiate(&cp->exec, graph, 0) != cudaSuccess) ok = false;
+  if (graph != nullptr) (void)cudaGraphDestroy(graph);
+  (void)cudaGetLastError();
+  cp->h2d = copy_counters().h2d - h2d0;
+  if (ok) {
+    try {
+      ok = capture_epilogue(*cp, cs);
+    } catch (const std::exception&) {
+      ok = false;
+    }
+  }
+  cp->kernels = g_kernel_launches.load() - k0;
+  if (!ok) {
+    if (cp->epilogue) {
+      (void)cudaGraphExecDestroy(cp->epilogue);
+      cp->epilogue = nullptr;
+    }
+    cp->capturable = false;
+    cp->result.reset();
+    cp->checks.clear();
+  }
+  return cp;
+}
+
+// A device copy of the first n rows of an arena-backed result (the next
+// replay reuses the arena).
+TupleSetPtr device_copy(const TupleSet& r, int64_t n, cudaStream_t s) {
+  std::vector<ColumnPtr> cols;
+  for (int i = 0; i < r.num_columns(); ++i) {
+    const auto& c = r.column(i);
+    if (c->type == DType::Utf8) {
+      Column part = *c;
+      part.length = n;
+      cols.push_back(concat_utf8({&part}, s));
+    } else {
+      const int w = dtype_width(c->type);
+      auto b = make_buffer(n * w, s);
+      if (n > 0) GF_CUDA(cudaMemcpyAsync(b->data(), c->data, n * w, cudaMemcpyDeviceToDevice, s));
+      cols.push_back(make_fixed_column(c->type, n, b));
+    }
+  }
+  return TupleSet::make(r.fields(), std::move(cols), n);
+}
+
+// Replay a captured plan. Returns false when a deferred output overflowed
+// (the caller then runs the plan with exact sizes).
+bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowDeviceArray* out, cudaStream_t s) {
+  GF_CUDA(cudaGraphLaunch(cp.exec, s));
+  GF_CUDA(cudaGraphLaunch(cp.epilogue, s));
+  count_launch(cp.kernels);
+  sync(s);
+  copy_counters().h2d += cp.h2d;
+  copy_counters().d2h += cp.pinned_bytes;
+  bool fits = true;
+  for (size_t i = 0; i < cp.checks.size(); ++i) {
+    const DevStatus* st = reinterpret_cast<const DevStatus*>(cp.pinned + cp.status_off[i]);
+    raise_device_status(*st, cp.checks[i].where);
+    if (cp.checks[i].capacity > 0 && st->value > cp.checks[i].capacity) fits = false;
+  }
+  if (!fits) return false;
+  const TupleSet& r = *cp.result;
+  int64_t n = cp.count_off >= 0 ? *reinterpret_cast<const int64_t*>(cp.pinned + cp.count_off) : cp.exact_rows;
+  if (n < 0 || n > r.num_rows()) fail(GFPDB_EDEVICE, "captured plan produced an out-of-range row count");
+  if (to_host) {
+    std::vector<std::vector<const void*>> bufs;
+    for (auto& offs : cp.col_off) {
+      std::vector<const void*> b;
+      for (int64_t o : offs) b.push_back(cp.pinned + o);
+      bufs.push_back(b);
+    }
+    export_host_columns(r.fields(), n, bufs, out_schema, out);
+  } else {
+    export_tupleset(device_copy(r, n, s), out_schema, out, false, s);
+    sync(s);
+  }
+  return true;
 }
 
 }  // namespace
@@ -413,6 +626,33 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
     ensure_device();
     cudaStream_t s = as_stream(stream);
     const CopyCounters c0 = copy_counters();
+    const uint64_t launches0 = g_kernel_launches.load();
+    auto fill_stats = [&](int64_t num_ops, int64_t messages) {
+      if (stats == nullptr) return;
+      stats->kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
+      stats->h2d_bytes = copy_counters().h2d - c0.h2d;
+      stats->d2h_bytes = copy_counters().d2h - c0.d2h;
+      stats->num_ops = num_ops;
+      stats->messages = messages;
+      stats->elapsed_ns =
+          std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    };
+    // Replay of a captured plan: found before any parsing or import.
+    const bool maybe_graph = std::strstr(plan_json, "\"cudaGraph\"") != nullptr;
+    std::string key;
+    if (maybe_graph) {
+      key = plan_key(plan_json, n_tables, table_names, arrays);
+      std::shared_ptr<CapturedPlan> cp;
+      {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) cp = it->second;
+      }
+      if (cp && cp->capturable && replay_plan(*cp, result_to_host != 0, out_schema, out, s)) {
+        fill_stats(cp->num_ops, cp->messages);
+        return;
+      }
+    }
     json::Value plan;
     try {
       plan = json::parse(plan_json);
@@ -431,21 +671,51 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
       }
       inputs[table_names[i]] = t;
     }
-    auto ex = pop::build_execution(plan, s);
-    ex->setInputs(std::move(inputs));
-    auto result = ex->execute();
+    const bool deferred = plan.get_bool("deferredSizes", true);
+    const bool use_graph = deferred && plan.get_bool("cudaGraph", false);
+    TupleSetPtr result;
+    pop::ExecStats xs;
+    auto run_plain = [&](bool defer) {
+      auto ex = pop::build_execution(plan, s);
+      ex->setInputs(inputs);
+      ex->setDeferred(defer);
+      auto r = ex->execute();
+      xs = ex->stats();
+      return r;
+    };
+    auto run = [&]() {
+      try {
+        return run_plain(deferred);
+      } catch (const pop::NeedsExactSizes&) {
+        // A join met repeated build keys and overflowed its deferred
+        // capacity: run the plan again with exact (synchronized) sizes.
+        return run_plain(false);
+      }
+    };
+    if (!use_graph) {
+      result = run();
+    } else {
+      std::shared_ptr<CapturedPlan> cp;
+      {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) cp = it->second;
+      }
+      // First call for these inputs: an ordinary run (which also measures the
+      // memory the plan needs), then the capture; a replay that overflowed
+      // lands here too and gets the exact re-run.
+      const int64_t a0 = thread_alloc_bytes();
+      result = run();
+      if (!cp) {
+        const int64_t bytes = thread_alloc_bytes() - a0;
+        cp = capture_plan(plan, inputs, bytes + bytes / 4 + (int64_t{1} << 20));
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        g_graphs[key] = cp;
+      }
+    }
     export_tupleset(result, out_schema, out, result_to_host != 0, s);
     sync(s);
-    if (stats != nullptr) {
-      auto st = ex->stats();
-      stats->kernel_launches = st.kernel_launches;
-      stats->h2d_bytes = copy_counters().h2d - c0.h2d;
-      stats->d2h_bytes = copy_counters().d2h - c0.d2h;
-      stats->num_ops = st.num_ops;
-      stats->messages = st.messages;
-      stats->elapsed_ns =
-          std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
-    }
+    fill_stats(xs.num_ops, xs.messages);
   });
 }
 

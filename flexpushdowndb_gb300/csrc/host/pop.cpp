@@ -193,10 +193,14 @@ class BloomFilterCreatePOp : public PhysicalOp {
     } else if (m.type == MessageType::COMPLETE) {
       if (!is_producer_complete(*this)) return;
       std::vector<const Column*> parts;
-      for (auto& t : buffered_) parts.push_back(t->column(column_).get());
+      std::vector<const int64_t*> rows;
+      for (auto& t : buffered_) {
+        parts.push_back(t->column(column_).get());
+        rows.push_back(t->rows_dev());
+      }
       Message out;
       out.type = MessageType::BLOOM_FILTER;
-      out.bloom = bloom_build(parts, bits_, hashes_, ctx()->stream());
+      out.bloom = bloom_build(parts, bits_, hashes_, ctx()->stream(), rows);
       ctx()->tell(out, uses_);
       ctx()->notifyComplete();
     }
@@ -311,9 +315,10 @@ class HashJoinArrowPOp : public PhysicalOp {
 
   void probe(const TupleSetPtr& ts) {
     const int pk = ts->require_column(probe_key_);
-    BufferPtr pidx, bidx;
+    BufferPtr pidx, bidx, count_owner;
+    const int64_t* count_dev = nullptr;
     int64_t n = 0;
-    join_probe_pairs(table_, *ts, pk, &pidx, &bidx, &n, ctx()->stream());
+    join_probe_pairs(table_, *ts, pk, &pidx, &bidx, &n, ctx()->stream(), &count_owner, &count_dev);
     // Output: probe fields then build fields (HashJoinArrowKernel.cpp:148-162),
     // each filtered to the needed columns.
     std::vector<GatherSpec> specs;
@@ -336,10 +341,23 @@ class HashJoinArrowPOp : public PhysicalOp {
         fields.push_back(b.field(i));
         specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
       }
-    auto cols = gather_columns(specs, n, ctx()->stream());
+    bool utf8 = false;
+    for (auto& f : fields) utf8 |= f.type == DType::Utf8;
     Message out;
     out.type = MessageType::TUPLESET;
-    out.tuples = TupleSet::make(std::move(fields), std::move(cols), n);
+    if (count_dev != nullptr && utf8) {
+      // utf8 outputs are sized from the exact pair count
+      int64_t exact = 0;
+      GF_CUDA(cudaMemcpyAsync(&exact, count_dev, sizeof(exact), cudaMemcpyDeviceToHost, ctx()->stream()));
+      sync(ctx()->stream());
+      n = exact < n ? exact : n;
+      count_dev = nullptr;
+    }
+    auto cols = gather_columns(specs, n, ctx()->stream(), count_dev, count_owner);
+    if (count_dev != nullptr)
+      out.tuples = TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev);
+    else
+      out.tuples = TupleSet::make(std::move(fields), std::move(cols), n);
     ctx()->tell(out);
   }
 
@@ -469,6 +487,11 @@ TupleSetPtr Execution::execute() {
     post(o->name(), start);
   }
   int32_t code = GFPDB_EINVAL;
+  clear_deferred_checks();
+  set_deferred_mode(deferred_);
+  struct ModeGuard {
+    ~ModeGuard() { set_deferred_mode(false); }
+  } mode_guard;
   while (!mailbox_.empty() && error_.empty()) {
     auto [to, msg] = std::move(mailbox_.front());
     mailbox_.pop_front();
@@ -485,7 +508,20 @@ TupleSetPtr Execution::execute() {
       dst->ctx()->notifyError(e.what());
     }
   }
-  if (!error_.empty()) fail(code, error_);
+  set_deferred_mode(false);
+  if (!error_.empty()) {
+    clear_deferred_checks();
+    fail(code, error_);
+  }
+  if (capturing_) {
+    // Under graph capture nothing may wait: the checks run after each replay.
+    captured_checks_ = take_deferred_checks();
+  } else if (deferred_) {
+    // One synchronization for the whole plan: device errors of every
+    // operator, and whether every deferred output fit its capacity.
+    sync(stream_);
+    if (!run_deferred_checks(stream_)) throw NeedsExactSizes();
+  }
   std::string incomplete;
   CollatePOp* collate = nullptr;
   for (auto& o : ops_) {

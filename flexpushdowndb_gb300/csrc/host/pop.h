@@ -136,9 +136,25 @@ struct ExecStats {
   int64_t num_ops = 0;
 };
 
+// Thrown by Execution::execute when a deferred output overflowed the
+// capacity it was given (a join whose build keys repeat): the caller runs the
+// plan again with exact sizes.
+struct NeedsExactSizes : std::exception {
+  const char* what() const noexcept override { return "deferred output overflowed its capacity"; }
+};
+
 class Execution {
  public:
   Execution(cudaStream_t stream) : stream_(stream) {}
+
+  // Deferred sizes (default): operators chain on the stream without waiting
+  // for row counts; the plan synchronizes once at the end.
+  void setDeferred(bool on) { deferred_ = on; }
+  // Capture mode: execute() only enqueues (no final synchronization) and
+  // hands the status checks to the caller, which runs them after each
+  // replay of the captured graph.
+  void setCapturing(bool on) { capturing_ = on; }
+  std::vector<DeferredCheck> takeCapturedChecks() { return std::move(captured_checks_); }
 
   void add(std::unique_ptr<PhysicalOp> op);
   PhysicalOp* op(const std::string& name);
@@ -164,6 +180,9 @@ class Execution {
   std::map<std::string, InputTable> inputs_;
   std::string error_;
   ExecStats stats_;
+  bool deferred_ = true;
+  bool capturing_ = false;
+  std::vector<DeferredCheck> captured_checks_;
 };
 
 // Build an Execution from a JSON plan (format documented with

@@ -89,11 +89,40 @@ void ensure_device() {
 int num_sms() { return info_for(current_device()).sms; }
 int max_smem_optin() { return info_for(current_device()).smem_optin; }
 
+namespace {
+thread_local Arena* g_thread_arena = nullptr;
+thread_local int64_t g_thread_alloc = 0;
+}  // namespace
+
+void set_thread_arena(Arena* a) { g_thread_arena = a; }
+int64_t thread_alloc_bytes() { return g_thread_alloc; }
+
+Arena::Arena(int64_t bytes, cudaStream_t s) : size_(bytes) {
+  Arena* saved = g_thread_arena;
+  g_thread_arena = nullptr;  // the arena's own memory comes from the pool
+  base_ = make_buffer(bytes, s);
+  g_thread_arena = saved;
+}
+
+void* Arena::take(int64_t bytes) {
+  const int64_t n = (bytes + 255) / 256 * 256;
+  if (used_ + n > size_) fail(GFPDB_ENOMEM, "plan arena exhausted");
+  void* p = base_->as<char>() + used_;
+  used_ += n;
+  return p;
+}
+
 DeviceBuffer::DeviceBuffer(int64_t bytes, cudaStream_t stream) : bytes_(bytes), owned_(true), stream_(stream) {
   if (bytes < 0) fail(GFPDB_EINVAL, "negative allocation size");
   // Zero-byte buffers still get a distinct valid pointer so Arrow consumers
   // never see NULL data buffers for empty columns.
   int64_t n = bytes > 0 ? bytes : 16;
+  g_thread_alloc += (n + 255) / 256 * 256;
+  if (g_thread_arena != nullptr) {
+    ptr_ = g_thread_arena->take(n);
+    owned_ = false;
+    return;
+  }
   GF_CUDA(cudaMallocAsync(&ptr_, static_cast<size_t>(n), stream));
 }
 
@@ -125,6 +154,14 @@ struct ProfRecord {
   cudaEvent_t start = nullptr;
   cudaEvent_t stop = nullptr;
   double bytes = 0;
+  // optional byte model evaluated at read time
+  bool model = false;
+  const int64_t* rows_in_dev = nullptr;
+  int64_t rows_in = 0;
+  double per_in = 0;
+  const int64_t* rows_out_dev = nullptr;
+  double per_out = 0;
+  std::shared_ptr<DeviceBuffer> keep, keep2;
 };
 std::mutex g_prof_mu;
 std::vector<ProfRecord> g_prof;
@@ -133,6 +170,8 @@ std::atomic<bool> g_prof_on{false};
 
 ProfScope::ProfScope(const char* name, cudaStream_t s) : stream_(s) {
   if (!g_prof_on.load(std::memory_order_relaxed)) return;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) return;
   ProfRecord r;
   r.name = name;
   GF_CUDA(cudaEventCreate(&r.start));
@@ -154,6 +193,22 @@ void ProfScope::set_bytes(double bytes) {
   if (index_ < 0) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_prof[index_].bytes = bytes;
+}
+
+void ProfScope::set_bytes_model(const int64_t* rows_in_dev, int64_t rows_in, double per_in,
+                                const int64_t* rows_out_dev, double per_out, std::shared_ptr<DeviceBuffer> keep,
+                                std::shared_ptr<DeviceBuffer> keep2) {
+  if (index_ < 0) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  ProfRecord& r = g_prof[index_];
+  r.model = true;
+  r.rows_in_dev = rows_in_dev;
+  r.rows_in = rows_in;
+  r.per_in = per_in;
+  r.rows_out_dev = rows_out_dev;
+  r.per_out = per_out;
+  r.keep = std::move(keep);
+  r.keep2 = std::move(keep2);
 }
 
 void prof_enable(bool on) { g_prof_on.store(on); }
@@ -178,7 +233,15 @@ void prof_read(const std::string& name, int64_t* launches, double* ms, double* b
     GF_CUDA(cudaEventElapsedTime(&e, r.start, r.stop));
     ++n;
     t += e;
-    b += r.bytes;
+    if (r.model) {
+      int64_t in = r.rows_in, out = 0;
+      if (r.rows_in_dev) GF_CUDA(cudaMemcpy(&in, r.rows_in_dev, sizeof(in), cudaMemcpyDeviceToHost));
+      if (r.rows_out_dev) GF_CUDA(cudaMemcpy(&out, r.rows_out_dev, sizeof(out), cudaMemcpyDeviceToHost));
+      if (in > r.rows_in) in = r.rows_in;
+      b += r.per_in * static_cast<double>(in) + r.per_out * static_cast<double>(out);
+    } else {
+      b += r.bytes;
+    }
   }
   *launches = n;
   *ms = t;
@@ -197,6 +260,44 @@ std::string prof_kernels() {
     out += r.name + "\n";
   }
   return out;
+}
+
+namespace {
+thread_local bool g_deferred = false;
+thread_local std::vector<DeferredCheck> g_checks;
+}  // namespace
+
+bool deferred_mode() { return g_deferred; }
+void set_deferred_mode(bool on) { g_deferred = on; }
+
+void defer_check(BufferPtr owner, const DevStatus* status, const char* where, int64_t capacity) {
+  g_checks.push_back(DeferredCheck{std::move(owner), status, where, capacity});
+}
+
+void clear_deferred_checks() { g_checks.clear(); }
+
+std::vector<DeferredCheck> take_deferred_checks() {
+  std::vector<DeferredCheck> out;
+  out.swap(g_checks);
+  return out;
+}
+
+bool run_checks(const std::vector<DeferredCheck>& checks, cudaStream_t s) {
+  bool fits = true;
+  std::vector<DevStatus> host(checks.size());
+  for (size_t i = 0; i < checks.size(); ++i)
+    GF_CUDA(cudaMemcpyAsync(&host[i], checks[i].status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  sync(s);
+  for (size_t i = 0; i < checks.size(); ++i) {
+    raise_device_status(host[i], checks[i].where);
+    if (checks[i].capacity > 0 && host[i].value > checks[i].capacity) fits = false;
+  }
+  return fits;
+}
+
+bool run_deferred_checks(cudaStream_t s) {
+  auto checks = take_deferred_checks();
+  return run_checks(checks, s);
 }
 
 void raise_device_status(const DevStatus& st, const char* where) {

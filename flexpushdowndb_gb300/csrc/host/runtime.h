@@ -14,6 +14,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "../../../include/gfpdb.h"
 
@@ -105,6 +106,28 @@ inline BufferPtr make_buffer(int64_t bytes, cudaStream_t stream) {
   return std::make_shared<DeviceBuffer>(bytes, stream);
 }
 
+// A bump arena over one device allocation. While an arena is active on a
+// thread, every DeviceBuffer that thread creates is carved from it and is
+// never freed on its own: the arena's memory is reused as a whole. Used to
+// capture a plan into a CUDA graph, whose kernels then see fixed addresses.
+class Arena {
+ public:
+  Arena(int64_t bytes, cudaStream_t s);
+  void* take(int64_t bytes);  // 256-byte aligned; throws GFPDB_ENOMEM when full
+  int64_t used() const { return used_; }
+  int64_t size() const { return size_; }
+  void reset() { used_ = 0; }
+
+ private:
+  BufferPtr base_;
+  int64_t size_ = 0;
+  int64_t used_ = 0;
+};
+// Activate `a` for this thread (nullptr deactivates).
+void set_thread_arena(Arena* a);
+// Bytes this thread has allocated through DeviceBuffer (rounded to 256).
+int64_t thread_alloc_bytes();
+
 void memcpy_h2d(void* dst, const void* src, int64_t n, cudaStream_t s);
 void memcpy_d2h(void* dst, const void* src, int64_t n, cudaStream_t s);
 void sync(cudaStream_t s);
@@ -122,6 +145,38 @@ static_assert(sizeof(DevStatus) == 64, "status block is one 64-byte line");
 
 void raise_device_status(const DevStatus& st, const char* where);
 
+// Deferred sizes. While a plan runs in deferred mode, operators do not wait
+// for their kernels: outputs are allocated at an upper bound and carry their
+// true row count in device memory, and each call's status block is recorded
+// here instead of being read back. The plan executor synchronizes once at the
+// end and checks them all. A record with `capacity` > 0 also checks that the
+// count its kernel produced (DevStatus::value) fit the allocated capacity;
+// a miss means the plan must be re-run with exact sizes.
+struct DeferredCheck {
+  BufferPtr owner;
+  const DevStatus* status;
+  const char* where;
+  int64_t capacity;
+};
+bool deferred_mode();
+void set_deferred_mode(bool on);
+void defer_check(BufferPtr owner, const DevStatus* status, const char* where, int64_t capacity = 0);
+// Reads every recorded status (the stream must be synchronized). Raises the
+// first device error; returns false if some output overflowed its capacity.
+bool run_deferred_checks(cudaStream_t s);
+void clear_deferred_checks();
+// Move the recorded checks out (a captured plan keeps them for its replays),
+// and run a kept list (the stream must be synchronized).
+std::vector<DeferredCheck> take_deferred_checks();
+bool run_checks(const std::vector<DeferredCheck>& checks, cudaStream_t s);
+
+// Device row count of a TupleSet-like input: min(*n_dev, capacity) or capacity.
+__host__ __device__ inline int64_t clamp_rows(const int64_t* n_dev, int64_t capacity) {
+  if (n_dev == nullptr) return capacity;
+  const int64_t n = *n_dev;
+  return n < capacity ? (n < 0 ? 0 : n) : capacity;
+}
+
 // Optional per-launch timing (gfpdb_profile_*): events on the launching
 // stream around one kernel plus its algorithmic bytes.
 class ProfScope {
@@ -130,6 +185,11 @@ class ProfScope {
   // Record the stop event; bytes may be refined later with set_bytes().
   void stop(double bytes);
   void set_bytes(double bytes);
+  // Bytes = per_in * rows_in + per_out * rows_out, with either row count
+  // read from device memory when the profile is read (deferred sizes).
+  void set_bytes_model(const int64_t* rows_in_dev, int64_t rows_in, double per_in, const int64_t* rows_out_dev,
+                       double per_out, std::shared_ptr<class DeviceBuffer> keep,
+                       std::shared_ptr<class DeviceBuffer> keep2 = nullptr);
 
  private:
   int64_t index_ = -1;

@@ -97,6 +97,29 @@ TupleSetPtr TupleSet::make(std::vector<Field> fields, std::vector<ColumnPtr> col
   return std::make_shared<const TupleSet>(std::move(fields), std::move(columns), num_rows);
 }
 
+TupleSetPtr TupleSet::make_deferred(std::vector<Field> fields, std::vector<ColumnPtr> columns, int64_t capacity,
+                                    BufferPtr rows_owner, const int64_t* rows_dev) {
+  auto ts = std::make_shared<TupleSet>(std::move(fields), std::move(columns), capacity);
+  ts->rows_owner_ = std::move(rows_owner);
+  ts->rows_dev_ = rows_dev;
+  return ts;
+}
+
+TupleSetPtr TupleSet::resolve(cudaStream_t s) const {
+  if (exact()) return make(fields_, columns_, num_rows_);
+  int64_t n = 0;
+  GF_CUDA(cudaMemcpyAsync(&n, rows_dev_, sizeof(n), cudaMemcpyDeviceToHost, s));
+  sync(s);
+  if (n < 0 || n > num_rows_) fail(GFPDB_EDEVICE, "deferred row count out of range");
+  std::vector<ColumnPtr> cols;
+  for (auto& c : columns_) {
+    auto r = std::make_shared<Column>(*c);
+    r->length = n;
+    cols.push_back(r);
+  }
+  return make(fields_, std::move(cols), n);
+}
+
 TupleSetPtr TupleSet::make_empty(const std::vector<Field>& fields, cudaStream_t s) {
   std::vector<ColumnPtr> cols;
   for (auto& f : fields) {
@@ -133,7 +156,8 @@ TupleSetPtr TupleSet::project_exist(const std::vector<std::string>& names) const
       c.push_back(columns_[i]);
     }
   }
-  return make(std::move(f), std::move(c), num_rows_);
+  if (exact()) return make(std::move(f), std::move(c), num_rows_);
+  return make_deferred(std::move(f), std::move(c), num_rows_, rows_owner_, rows_dev_);
 }
 
 TupleSetPtr TupleSet::project(const std::vector<std::string>& names) const {
@@ -144,7 +168,8 @@ TupleSetPtr TupleSet::project(const std::vector<std::string>& names) const {
     f.push_back(fields_[i]);
     c.push_back(columns_[i]);
   }
-  return make(std::move(f), std::move(c), num_rows_);
+  if (exact()) return make(std::move(f), std::move(c), num_rows_);
+  return make_deferred(std::move(f), std::move(c), num_rows_, rows_owner_, rows_dev_);
 }
 
 int64_t TupleSet::bytes() const {
@@ -156,6 +181,12 @@ int64_t TupleSet::bytes() const {
 TupleSetPtr TupleSet::concatenate(const std::vector<TupleSetPtr>& sets, cudaStream_t s) {
   if (sets.empty()) fail(GFPDB_EINVAL, "concatenate: no TupleSets");
   if (sets.size() == 1) return sets[0];
+  for (auto& t : sets)
+    if (!t->exact()) {
+      std::vector<TupleSetPtr> exact_sets;
+      for (auto& u : sets) exact_sets.push_back(resolved(u, s));
+      return concatenate(exact_sets, s);
+    }
   const auto& fields = sets[0]->fields();
   int64_t total = 0;
   for (auto& t : sets) {
@@ -317,7 +348,8 @@ void release_array(ArrowArray* a) {
 
 }  // namespace
 
-void export_tupleset(const TupleSetPtr& ts, ArrowSchema* so, ArrowDeviceArray* ao, bool to_host, cudaStream_t s) {
+void export_tupleset(const TupleSetPtr& ts_in, ArrowSchema* so, ArrowDeviceArray* ao, bool to_host, cudaStream_t s) {
+  const TupleSetPtr ts = resolved(ts_in, s);
   const int nc = ts->num_columns();
   // schema
   auto* sh = new SchemaHolder();
@@ -422,6 +454,74 @@ void export_tupleset(const TupleSetPtr& ts, ArrowSchema* so, ArrowDeviceArray* a
   ao->device_type = to_host ? ARROW_DEVICE_CPU : ARROW_DEVICE_CUDA;
   ao->device_id = to_host ? -1 : current_device();
   ao->sync_event = nullptr;
+}
+
+void export_host_columns(const std::vector<Field>& fields, int64_t n,
+                         const std::vector<std::vector<const void*>>& bufs, ArrowSchema* so, ArrowDeviceArray* ao) {
+  const int nc = static_cast<int>(fields.size());
+  auto* sh = new SchemaHolder();
+  sh->names.reserve(nc);
+  sh->child_structs.resize(nc);
+  sh->child_ptrs.resize(nc);
+  for (int i = 0; i < nc; ++i) {
+    sh->names.push_back(fields[i].name);
+    ArrowSchema& c = sh->child_structs[i];
+    std::memset(&c, 0, sizeof(c));
+    c.format = dtype_format(fields[i].type);
+    c.name = sh->names.back().c_str();
+    c.release = release_child_schema;
+    sh->child_ptrs[i] = &c;
+  }
+  std::memset(so, 0, sizeof(*so));
+  so->format = "+s";
+  so->name = "";
+  so->n_children = nc;
+  so->children = nc > 0 ? sh->child_ptrs.data() : nullptr;
+  so->release = release_schema;
+  so->private_data = sh;
+
+  auto* ah = new ArrayHolder();
+  ah->child_structs.resize(nc);
+  ah->child_ptrs.resize(nc);
+  ah->child_buffers.resize(nc);
+  for (int i = 0; i < nc; ++i) {
+    if (fields[i].type == DType::Utf8) {
+      const int32_t* offs = static_cast<const int32_t*>(bufs[i][0]);
+      const char* bytes = static_cast<const char*>(bufs[i][1]);
+      const int32_t first = n > 0 ? offs[0] : 0, last = n > 0 ? offs[n] : 0;
+      auto* ho = static_cast<int32_t*>(std::malloc((n + 1) * 4));
+      char* hb = static_cast<char*>(std::malloc(last - first > 0 ? last - first : 1));
+      for (int64_t k = 0; k <= n; ++k) ho[k] = n > 0 ? offs[k] - first : 0;
+      if (last > first) std::memcpy(hb, bytes + first, last - first);
+      ah->host_allocs.push_back(ho);
+      ah->host_allocs.push_back(hb);
+      ah->child_buffers[i] = {nullptr, ho, hb};
+    } else {
+      const int64_t b = n * dtype_width(fields[i].type);
+      void* h = std::malloc(b > 0 ? b : 1);
+      if (b > 0) std::memcpy(h, bufs[i][0], b);
+      ah->host_allocs.push_back(h);
+      ah->child_buffers[i] = {nullptr, h};
+    }
+    ArrowArray& c = ah->child_structs[i];
+    std::memset(&c, 0, sizeof(c));
+    c.length = n;
+    c.n_buffers = static_cast<int64_t>(ah->child_buffers[i].size());
+    c.buffers = ah->child_buffers[i].data();
+    c.release = release_child_array;
+    ah->child_ptrs[i] = &c;
+  }
+  ah->struct_buffers = {nullptr};
+  std::memset(ao, 0, sizeof(*ao));
+  ao->array.length = n;
+  ao->array.n_buffers = 1;
+  ao->array.buffers = ah->struct_buffers.data();
+  ao->array.n_children = nc;
+  ao->array.children = nc > 0 ? ah->child_ptrs.data() : nullptr;
+  ao->array.release = release_array;
+  ao->array.private_data = ah;
+  ao->device_type = ARROW_DEVICE_CPU;
+  ao->device_id = -1;
 }
 
 }  // namespace gfpdb

@@ -53,6 +53,20 @@ class TupleSet {
   static TupleSetPtr make(std::vector<Field> fields, std::vector<ColumnPtr> columns, int64_t num_rows);
   static TupleSetPtr make_empty(const std::vector<Field>& fields, cudaStream_t s);
 
+  // A TupleSet whose true row count is only known on the device (written
+  // there by the kernel that produced it): `capacity` rows of every column
+  // are allocated and *rows_dev holds the count. Operators chained on the
+  // same stream consume it without a host round trip; resolve() reads the
+  // count when the host needs it.
+  static TupleSetPtr make_deferred(std::vector<Field> fields, std::vector<ColumnPtr> columns, int64_t capacity,
+                                   BufferPtr rows_owner, const int64_t* rows_dev);
+  bool exact() const { return rows_dev_ == nullptr; }
+  const int64_t* rows_dev() const { return rows_dev_; }
+  const BufferPtr& rows_owner() const { return rows_owner_; }
+  // Same columns with the exact row count (synchronizes `s` when deferred).
+  TupleSetPtr resolve(cudaStream_t s) const;
+
+  // Exact row count, or the capacity (upper bound) of a deferred TupleSet.
   int64_t num_rows() const { return num_rows_; }
   int num_columns() const { return static_cast<int>(columns_.size()); }
   const std::vector<Field>& fields() const { return fields_; }
@@ -77,7 +91,12 @@ class TupleSet {
   std::vector<Field> fields_;
   std::vector<ColumnPtr> columns_;
   int64_t num_rows_;
+  BufferPtr rows_owner_;
+  const int64_t* rows_dev_ = nullptr;
 };
+
+// `ts` itself when exact, else its resolved copy (synchronizes `s`).
+inline TupleSetPtr resolved(const TupleSetPtr& ts, cudaStream_t s) { return ts->exact() ? ts : ts->resolve(s); }
 
 // Column factories.
 ColumnPtr make_fixed_column(DType t, int64_t length, BufferPtr buf, const void* data = nullptr);
@@ -97,5 +116,12 @@ std::vector<Field> import_schema(const ArrowSchema* schema);
 // synchronized) and the array's device_type is ARROW_DEVICE_CPU.
 void export_tupleset(const TupleSetPtr& ts, ArrowSchema* schema_out, ArrowDeviceArray* array_out,
                      bool to_host, cudaStream_t s);
+
+// Export columns that already sit in host memory (copied into fresh host
+// allocations). Per column: {values} for fixed-width types, {offsets, bytes}
+// for utf8 (offsets are rebased to start at 0).
+void export_host_columns(const std::vector<Field>& fields, int64_t n,
+                         const std::vector<std::vector<const void*>>& bufs, ArrowSchema* schema_out,
+                         ArrowDeviceArray* array_out);
 
 }  // namespace gfpdb

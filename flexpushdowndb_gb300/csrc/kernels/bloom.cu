@@ -3,6 +3,11 @@
 // Replaces ArrowBloomFilter::build / BlockedBloomFilter::Insert
 // (fpdb-executor/src/physical/bloomfilter/ArrowBloomFilter.cpp:29-75;
 // fpdb-tuple/src/arrow/exec/BloomFilter.cpp:110-137).
+//
+// When the key columns come from deferred TupleSets (row counts known only
+// on the device), the filter is allocated for the upper bound and a one-thread
+// kernel sizes it from the device counts (same formula as the host path), so
+// the filter is bit-identical to one built from exact inputs.
 #include "bloom.cuh"
 #include "launch.h"
 
@@ -10,14 +15,56 @@ namespace gfpdb {
 
 namespace {
 
+struct BloomHeader {
+  uint64_t num_blocks;
+  int32_t valid;
+  int32_t pad;
+  int64_t num_keys;
+};
+
+constexpr int kMaxBloomParts = 64;
+
+struct BloomSizeParams {
+  const int64_t* n_dev[kMaxBloomParts];
+  int64_t cap[kMaxBloomParts];
+  int32_t n_parts;
+  int32_t bits_per_key;
+  BloomHeader* hdr;
+};
+
+// Filter size from the device key counts (same formula as the host path);
+// every thread of every build launch computes it, and the first thread of the
+// first launch records it in the header for the probes.
+__device__ __forceinline__ void bloom_size(const BloomSizeParams& p, uint64_t* nb, bool* valid) {
+  int64_t total = 0;
+  for (int i = 0; i < p.n_parts; ++i) total += clamp_rows(p.n_dev[i], p.cap[i]);
+  int64_t blocks = (total * p.bits_per_key + 255) / 256;
+  if (blocks < 1) blocks = 1;
+  *nb = static_cast<uint64_t>(blocks);
+  *valid = total <= GFPDB_BLOOM_MAX_INPUT_SIZE;
+  if (p.hdr != nullptr && blockIdx.x == 0 && threadIdx.x == 0 && p.n_parts >= 0) {
+    p.hdr->num_keys = total;
+    p.hdr->valid = *valid ? 1 : 0;
+    p.hdr->num_blocks = *nb;
+  }
+}
+
 __global__ void __launch_bounds__(256)
-    bloom_build_kernel(DevCol key, int64_t n, uint32_t* __restrict__ blocks, uint64_t num_blocks, int num_hashes) {
+    bloom_build_kernel(DevCol key, int64_t cap, const int64_t* n_dev, uint32_t* __restrict__ blocks,
+                       uint64_t num_blocks, const __grid_constant__ BloomSizeParams sp, int num_hashes) {
+  const int64_t n = clamp_rows(n_dev, cap);
+  uint64_t nb = num_blocks;
+  if (sp.hdr != nullptr) {
+    bool valid = true;
+    bloom_size(sp, &nb, &valid);
+    if (!valid) return;
+  }
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     const uint64_t h = hash_key(load_int(key, r));
     uint32_t m[8];
     bloom_masks(h, num_hashes, m);
-    uint32_t* blk = blocks + static_cast<uint64_t>(bloom_block_of(h, num_blocks)) * 8;
+    uint32_t* blk = blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8;
 #pragma unroll
     for (int w = 0; w < 8; ++w)
       if (m[w] != 0) atomicOr(blk + w, m[w]);
@@ -27,10 +74,12 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_per_key, int32_t num_hashes,
-                     cudaStream_t s) {
+                     cudaStream_t s, const std::vector<const int64_t*>& part_rows_dev) {
   if (bits_per_key < 1 || bits_per_key > 64) fail(GFPDB_EINVAL, "bits_per_key must be in [1, 64]");
   if (num_hashes < 1 || num_hashes > 4) fail(GFPDB_EINVAL, "num_hashes must be in [1, 4]");
-  int64_t n = 0;
+  bool deferred = false;
+  for (auto* d : part_rows_dev) deferred |= d != nullptr;
+  int64_t n = 0;  // exact key count, or its upper bound when deferred
   for (auto* c : key_parts) {
     if (c->type != DType::Int32 && c->type != DType::Int64 && c->type != DType::Date32)
       fail(GFPDB_EUNSUPPORTED, "bloom filter keys must be int32, int64 or date32");
@@ -40,26 +89,50 @@ BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_p
   bf->num_keys = n;
   bf->num_hashes = num_hashes;
   bf->bits_per_key = bits_per_key;
-  if (n > GFPDB_BLOOM_MAX_INPUT_SIZE) {
+  if (!deferred && n > GFPDB_BLOOM_MAX_INPUT_SIZE) {
     // Too many keys: the filter is invalid and every probe passes.
     bf->valid = false;
     bf->num_blocks = 0;
     bf->blocks = make_buffer(32, s);
     return bf;
   }
-  int64_t nb = (n * bits_per_key + 255) / 256;
+  const int64_t n_alloc = n < GFPDB_BLOOM_MAX_INPUT_SIZE ? n : GFPDB_BLOOM_MAX_INPUT_SIZE;
+  int64_t nb = (n_alloc * bits_per_key + 255) / 256;
   if (nb < 1) nb = 1;
-  bf->num_blocks = nb;
+  bf->num_blocks = nb;  // exact size, or the capacity of a device-sized filter
   bf->blocks = make_buffer(nb * 32, s);
   GF_CUDA(cudaMemsetAsync(bf->blocks->data(), 0, nb * 32, s));
-  for (auto* c : key_parts) {
-    if (c->length == 0) continue;
+  BloomSizeParams sp{};
+  if (deferred) {
+    if (key_parts.size() > static_cast<size_t>(kMaxBloomParts))
+      fail(GFPDB_EUNSUPPORTED, "too many deferred bloom inputs");
+    bf->header = make_buffer(sizeof(BloomHeader), s);
+    BloomHeader* hdr = bf->header->as<BloomHeader>();
+    sp.n_parts = static_cast<int32_t>(key_parts.size());
+    sp.bits_per_key = bits_per_key;
+    sp.hdr = hdr;
+    for (size_t i = 0; i < key_parts.size(); ++i) {
+      sp.n_dev[i] = i < part_rows_dev.size() ? part_rows_dev[i] : nullptr;
+      sp.cap[i] = key_parts[i]->length;
+    }
+    bf->nblocks_dev = &hdr->num_blocks;
+    bf->valid_dev = &hdr->valid;
+  }
+  bool header_written = !deferred;
+  for (size_t i = 0; i < key_parts.size(); ++i) {
+    const Column* c = key_parts[i];
+    // The first launch of a device-sized filter also writes its header, so
+    // it runs even for an empty part.
+    if (c->length == 0 && header_written) continue;
+    header_written = true;
     DevCol k{c->data, nullptr, static_cast<int32_t>(c->type), 0};
+    const int64_t* n_dev = i < part_rows_dev.size() ? part_rows_dev[i] : nullptr;
     int64_t blocks = (c->length + 255) / 256;
     int64_t cap = static_cast<int64_t>(num_sms()) * 8;
     ProfScope prof("bloom_build_kernel", s);
+    if (blocks < 1) blocks = 1;
     bloom_build_kernel<<<static_cast<int>(blocks < cap ? blocks : cap), 256, 0, s>>>(
-        k, c->length, bf->blocks->as<uint32_t>(), static_cast<uint64_t>(nb), num_hashes);
+        k, c->length, n_dev, bf->blocks->as<uint32_t>(), static_cast<uint64_t>(nb), sp, num_hashes);
     after_launch("bloom_build_kernel");
     prof.stop(static_cast<double>(c->length) * dtype_width(c->type));
   }

@@ -6,6 +6,7 @@
 #include "common.cuh"
 #include "launch.h"
 
+#include <algorithm>
 #include <cstring>
 
 namespace gfpdb {
@@ -15,7 +16,8 @@ namespace {
 constexpr int kGatherMax = kMaxCols * 2;
 
 struct GatherFixedParams {
-  int64_t n;
+  int64_t n;              // exact count, or the capacity when n_dev is set
+  const int64_t* n_dev;   // device count (deferred sizes)
   int32_t n_cols;
   int32_t pad;
   const void* src[kGatherMax];
@@ -25,8 +27,9 @@ struct GatherFixedParams {
 };
 
 __global__ void __launch_bounds__(256) gather_fixed_kernel(const __grid_constant__ GatherFixedParams p) {
+  const int64_t n = clamp_rows(p.n_dev, p.n);
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < p.n; r += stride) {
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     for (int c = 0; c < p.n_cols; ++c) {
       const int32_t i = __ldg(p.idx[c] + r);
       if (p.width[c] == 8) {
@@ -111,6 +114,29 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
+constexpr int kPackMax = 128;
+
+struct PackParams {
+  int32_t n;
+  int32_t pad;
+  char* dst;
+  CopySpan spans[kPackMax];
+};
+
+__global__ void __launch_bounds__(256) pack_spans_kernel(const __grid_constant__ PackParams p) {
+  const CopySpan& sp = p.spans[blockIdx.x];
+  const char* src = static_cast<const char*>(sp.src);
+  char* dst = p.dst + sp.dst_off;
+  const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) | sp.bytes) & 15u) == 0;
+  if (vec) {
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int64_t i = threadIdx.x; i < sp.bytes / 16; i += blockDim.x) d4[i] = s4[i];
+  } else {
+    for (int64_t i = threadIdx.x; i < sp.bytes; i += blockDim.x) dst[i] = src[i];
+  }
+}
+
 int grid_for(int64_t n, int threads) {
   int64_t blocks = (n + threads - 1) / threads;
   int64_t cap = static_cast<int64_t>(num_sms()) * 8;
@@ -120,6 +146,18 @@ int grid_for(int64_t n, int threads) {
 }
 
 }  // namespace
+
+void pack_spans(const std::vector<CopySpan>& spans, void* dst, cudaStream_t s) {
+  for (size_t at = 0; at < spans.size(); at += kPackMax) {
+    PackParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.dst = static_cast<char*>(dst);
+    p.n = static_cast<int32_t>(std::min(spans.size() - at, static_cast<size_t>(kPackMax)));
+    for (int i = 0; i < p.n; ++i) p.spans[i] = spans[at + i];
+    pack_spans_kernel<<<p.n, 256, 0, s>>>(p);
+    after_launch("pack_spans_kernel");
+  }
+}
 
 int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
   if (n == 0) {
@@ -145,11 +183,23 @@ int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStrea
   return hs.value;
 }
 
-std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s) {
+std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s,
+                                      const int64_t* n_dev, BufferPtr n_owner) {
   std::vector<ColumnPtr> out(specs.size());
   GatherFixedParams p;
   std::memset(&p, 0, sizeof(p));
   p.n = n;
+  p.n_dev = n_dev;
+  bool has_utf8 = false;
+  for (auto& sp : specs) has_utf8 |= sp.src->type == DType::Utf8;
+  if (has_utf8 && n_dev != nullptr) {
+    // utf8 outputs are sized from the exact count
+    int64_t exact = 0;
+    GF_CUDA(cudaMemcpyAsync(&exact, n_dev, sizeof(exact), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    p.n = n = exact < n ? exact : n;
+    p.n_dev = n_dev = nullptr;
+  }
   std::vector<std::pair<size_t, BufferPtr>> fixed;
   for (size_t i = 0; i < specs.size(); ++i) {
     const Column& c = *specs[i].src;
@@ -171,6 +221,7 @@ std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int6
     double w = 0;
     for (int c = 0; c < p.n_cols; ++c) w += 2.0 * p.width[c] + 4.0;
     prof.stop(static_cast<double>(n) * w);
+    if (n_dev) prof.set_bytes_model(nullptr, 0, 0, n_dev, w, n_owner);
   }
   for (size_t i = 0; i < specs.size(); ++i) {
     const Column& c = *specs[i].src;

@@ -40,7 +40,8 @@ struct AccDev {
 };
 
 struct GroupParams {
-  int64_t n_rows;
+  int64_t n_rows;          // exact, or the capacity when n_dev is set
+  const int64_t* n_dev;    // device row count of a deferred batch
   int32_t n_keys;
   int32_t n_acc;
   int32_t key_bits[2];
@@ -141,6 +142,10 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
   uint64_t* s_keys = reinterpret_cast<uint64_t*>(s_mem);
   unsigned long long* s_acc = s_mem + p.sm_slots;
   const int sm_mask = p.sm_slots - 1;
+  const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
+  // A grid sized for a capacity can be far larger than the rows that arrive:
+  // CTAs without rows leave before touching shared memory (uniform per CTA).
+  if (static_cast<int64_t>(blockIdx.x) * kGroupThreads >= n_rows) return;
   if (p.use_smem) {
     for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads) {
       s_keys[i] = kEmptySlot;
@@ -149,7 +154,7 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
     __syncthreads();
   }
   const int64_t stride = static_cast<int64_t>(gridDim.x) * kGroupThreads;
-  for (int64_t r = static_cast<int64_t>(blockIdx.x) * kGroupThreads + threadIdx.x; r < p.n_rows; r += stride) {
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * kGroupThreads + threadIdx.x; r < n_rows; r += stride) {
     const uint64_t key = pack_key(p, r);
     int found = -1;
     if (p.use_smem && key != kEmptySlot) {
@@ -190,12 +195,17 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
   }
 }
 
-__global__ void group_init_kernel(uint64_t* keys, unsigned long long* accs, uint64_t n_slots, AccDev acc0, int n_acc,
-                                  const int8_t* fns, const int8_t* vts) {
+struct AccKinds {
+  int8_t fn[kMaxAggs];
+  int8_t vt[kMaxAggs];
+};
+
+__global__ void group_init_kernel(uint64_t* keys, unsigned long long* accs, uint64_t n_slots, int n_acc,
+                                  AccKinds kinds) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n_slots; i += stride) {
     keys[i] = kEmptySlot;
-    for (int a = 0; a < n_acc; ++a) accs[i * n_acc + a] = acc_init(fns[a], vts[a]);
+    for (int a = 0; a < n_acc; ++a) accs[i * n_acc + a] = acc_init(kinds.fn[a], kinds.vt[a]);
   }
 }
 
@@ -248,7 +258,7 @@ struct FinalParams {
   const uint64_t* keys;
   const unsigned long long* accs;
   uint64_t cap;  // special slot at index cap
-  int32_t special_used;
+  const int64_t* special_dev;  // non-zero once the all-ones key has a group
   int32_t n_acc;
   int32_t n_keys;
   int32_t n_out;
@@ -278,7 +288,7 @@ __global__ void __launch_bounds__(256) group_finalize_kernel(const __grid_consta
       live = key != kEmptySlot;
     } else if (i == p.cap) {
       key = kEmptySlot;
-      live = p.special_used != 0;
+      live = *p.special_dev != 0;
     }
     const uint32_t m = __ballot_sync(0xffffffffu, live);
     if (m == 0) continue;
@@ -649,20 +659,13 @@ class GroupTable {
     const int na = static_cast<int>(accs.size());
     auto nk = make_buffer(static_cast<int64_t>(new_cap + 1) * 8, s);
     auto na_buf = make_buffer(static_cast<int64_t>(new_cap + 1) * 8 * (na > 0 ? na : 1), s);
-    if (!fnvt) {
-      fnvt = make_buffer(2 * kMaxAggs, s);
-      int8_t h[2 * kMaxAggs] = {};
-      for (int a = 0; a < na; ++a) {
-        h[a] = accs[a].fn;
-        h[kMaxAggs + a] = accs[a].vt;
-      }
-      GF_CUDA(cudaMemcpyAsync(fnvt->data(), h, sizeof(h), cudaMemcpyHostToDevice, s));
-      sync(s);
+    AccKinds kinds{};
+    for (int a = 0; a < na; ++a) {
+      kinds.fn[a] = accs[a].fn;
+      kinds.vt[a] = accs[a].vt;
     }
-    AccDev dummy{};
     group_init_kernel<<<grid_for(static_cast<int64_t>(new_cap + 1)), 256, 0, s>>>(
-        nk->as<uint64_t>(), na_buf->as<unsigned long long>(), new_cap + 1, dummy, na, fnvt->as<int8_t>(),
-        fnvt->as<int8_t>() + kMaxAggs);
+        nk->as<uint64_t>(), na_buf->as<unsigned long long>(), new_cap + 1, na, kinds);
     after_launch("group_init_kernel");
     if (!status) {
       status = make_buffer(sizeof(DevStatus), s);
@@ -679,8 +682,19 @@ class GroupTable {
     cap = new_cap;
   }
 
-  void update(const TupleSet& ts, cudaStream_t s) {
-    if (!compiled) compile(ts);
+  void update(const TupleSet& batch, cudaStream_t s) {
+    if (!compiled) compile(batch);
+    // String keys are dictionary-encoded from exact inputs; other batches
+    // may carry their row count on the device.
+    TupleSetPtr exact_holder;
+    const TupleSet* tsp = &batch;
+    bool utf8_key = false;
+    for (auto t : key_types) utf8_key |= t == DType::Utf8;
+    if (utf8_key && !batch.exact()) {
+      exact_holder = batch.resolve(s);
+      tsp = exact_holder.get();
+    }
+    const TupleSet& ts = *tsp;
     const int64_t n = ts.num_rows();
     if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "group-by batch must have fewer than 2^31 rows");
     // Size the table so that it stays at most half full.
@@ -704,6 +718,7 @@ class GroupTable {
     GroupParams& p = *pp;
     std::memset(&p, 0, sizeof(p));
     p.n_rows = n;
+    p.n_dev = ts.rows_dev();
     p.n_keys = static_cast<int32_t>(group_cols.size());
     p.n_acc = static_cast<int32_t>(accs.size());
     std::vector<BufferPtr> code_bufs;
@@ -744,6 +759,7 @@ class GroupTable {
     for (int k = 0; k < p.n_keys; ++k) w += p.key_bits[k] / 8;
     for (size_t i = 0; i < slots.types.size(); ++i) w += dtype_width(slots.types[i]);
     prof.stop(static_cast<double>(n) * w);
+    if (p.n_dev) prof.set_bytes_model(p.n_dev, n, w, nullptr, 0, ts.rows_owner());
     groups_upper += n;
     if (hint > 0 && groups_upper > hint) groups_upper = hint;
   }
@@ -756,17 +772,27 @@ class GroupTable {
       fields.push_back(Field{aggs[j].name, compiled ? out_types[j] : DType::Int64});
     if (!compiled || cap == 0) return TupleSet::make_empty(fields, s);
     (void)schema_src;
-    DevStatus h = read_status(status->as<DevStatus>(), s);
-    raise_device_status(h, "group-by");
-    for (auto& d : dicts)
-      if (d && d->status) raise_device_status(read_status(d->status->as<DevStatus>(), s), "string dictionary");
-    const int64_t n_groups = h.aux[0];
+    bool utf8_key = false;
+    for (auto t : key_types) utf8_key |= t == DType::Utf8;
+    // Deferred: outputs sized for every slot, the group count stays on the
+    // device and the status block is checked at the end of the plan.
+    const bool defer = deferred_mode() && !utf8_key;
+    int64_t n_groups = static_cast<int64_t>(cap) + 1;
+    if (defer) {
+      defer_check(status, status->as<DevStatus>(), "group-by");
+    } else {
+      DevStatus h = read_status(status->as<DevStatus>(), s);
+      raise_device_status(h, "group-by");
+      for (auto& d : dicts)
+        if (d && d->status) raise_device_status(read_status(d->status->as<DevStatus>(), s), "string dictionary");
+      n_groups = h.aux[0];
+    }
     FinalParams fp;
     std::memset(&fp, 0, sizeof(fp));
     fp.keys = keys->as<uint64_t>();
     fp.accs = accbuf->as<unsigned long long>();
     fp.cap = cap;
-    fp.special_used = h.aux[1] != 0;
+    fp.special_dev = &status->as<DevStatus>()->aux[1];
     fp.n_acc = static_cast<int32_t>(accs.size());
     fp.n_keys = static_cast<int32_t>(group_cols.size());
     std::vector<BufferPtr> key_out(group_cols.size());
@@ -795,6 +821,9 @@ class GroupTable {
       else cols.push_back(make_fixed_column(key_types[k], n_groups, key_out[k]));
     }
     for (size_t j = 0; j < aggs.size(); ++j) cols.push_back(make_fixed_column(out_types[j], n_groups, agg_out[j]));
+    if (defer)
+      return TupleSet::make_deferred(std::move(fields), std::move(cols), n_groups, counter,
+                                     reinterpret_cast<const int64_t*>(counter->data()));
     return TupleSet::make(std::move(fields), std::move(cols), n_groups);
   }
 };

@@ -22,9 +22,12 @@ namespace gfpdb {
 namespace {
 
 __global__ void __launch_bounds__(256)
-    join_build_kernel(DevCol key, int64_t n, uint64_t* __restrict__ slots, uint64_t mask, int key32, DevStatus* st) {
+    join_build_kernel(DevCol key, int64_t cap, const int64_t* n_dev, uint64_t* __restrict__ slots, uint64_t mask,
+                      int key32, DevStatus* st) {
+  const int64_t n = clamp_rows(n_dev, cap);
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   int64_t my_max = 0;
+  bool dup = false;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     const int64_t k = load_int(key, r);
     const uint64_t h = hash_key(k);
@@ -37,6 +40,11 @@ __global__ void __launch_bounds__(256)
                                                static_cast<unsigned long long>(kEmptySlot),
                                                static_cast<unsigned long long>(packed));
       if (old == kEmptySlot) break;
+      // A key met again on its own run: the build side has duplicates, so a
+      // probe row can match several build rows.
+      if (static_cast<uint32_t>(old >> 32) == tag &&
+          (key32 || load_int(key, static_cast<uint32_t>(old)) == k))
+        dup = true;
       slot = (slot + 1) & mask;
     }
     if (probe > mask) raise_status(st, GFPDB_ENOMEM, 10);  // table full: cannot happen at load <= 1
@@ -49,12 +57,14 @@ __global__ void __launch_bounds__(256)
   }
   if ((threadIdx.x & 31) == 0 && my_max > 0)
     atomicMax(reinterpret_cast<unsigned long long*>(&st->aux[0]), static_cast<unsigned long long>(my_max));
+  if (dup) st->aux[1] = 1;
 }
 
 __global__ void __launch_bounds__(256)
-    join_probe_kernel(DevCol pkey, int64_t n, const uint64_t* __restrict__ slots, uint64_t mask, DevCol bkey,
-                      int key32, int32_t* __restrict__ out_p, int32_t* __restrict__ out_b, int64_t cap,
-                      DevStatus* st) {
+    join_probe_kernel(DevCol pkey, int64_t n_cap, const int64_t* n_dev, const uint64_t* __restrict__ slots,
+                      uint64_t mask, DevCol bkey, int key32, int32_t* __restrict__ out_p,
+                      int32_t* __restrict__ out_b, int64_t cap, DevStatus* st) {
+  const int64_t n = clamp_rows(n_dev, n_cap);
   const int lane = threadIdx.x & 31;
   const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -131,14 +141,16 @@ void join_build_table(JoinTable& t, double load_factor, cudaStream_t s) {
     DevCol k{kc->data, nullptr, static_cast<int32_t>(kc->type), 0};
     const int key32 = kc->type != DType::Int64;
     ProfScope prof("join_build_kernel", s);
-    join_build_kernel<<<grid_for(n), 256, 0, s>>>(k, n, t.slots->as<uint64_t>(), cap - 1, key32, st);
+    join_build_kernel<<<grid_for(n), 256, 0, s>>>(k, n, t.build->rows_dev(), t.slots->as<uint64_t>(), cap - 1,
+                                                 key32, st);
     after_launch("join_build_kernel");
     prof.stop(static_cast<double>(n) * dtype_width(kc->type));
   }
 }
 
 void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,
-                      BufferPtr* build_idx, int64_t* n_out, cudaStream_t s) {
+                      BufferPtr* build_idx, int64_t* n_out, cudaStream_t s, BufferPtr* count_owner,
+                      const int64_t** count_dev) {
   const int64_t n = probe.num_rows();
   if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join probe batch must have fewer than 2^31 rows");
   const auto& pc = probe.column(probe_key);
@@ -156,17 +168,29 @@ void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, 
   DevCol bkc{bk->data, nullptr, static_cast<int32_t>(bk->type), 0};
   int64_t cap = n > 0 ? n : 1;
   auto status = make_buffer(sizeof(DevStatus), s);
+  const bool defer = deferred_mode() && count_dev != nullptr;
   for (int attempt = 0; attempt < 2; ++attempt) {
     *probe_idx = make_buffer(cap * 4, s);
     *build_idx = make_buffer(cap * 4, s);
     GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
     if (n > 0 && t.build->num_rows() > 0) {
       ProfScope prof("join_probe_kernel", s);
-      join_probe_kernel<<<grid_for(n), 256, 0, s>>>(pk, n, t.slots->as<uint64_t>(), t.capacity - 1, bkc,
-                                                   key32 ? 1 : 0, (*probe_idx)->as<int32_t>(),
+      join_probe_kernel<<<grid_for(n), 256, 0, s>>>(pk, n, probe.rows_dev(), t.slots->as<uint64_t>(),
+                                                   t.capacity - 1, bkc, key32 ? 1 : 0, (*probe_idx)->as<int32_t>(),
                                                    (*build_idx)->as<int32_t>(), cap, status->as<DevStatus>());
       after_launch("join_probe_kernel");
       prof.stop(static_cast<double>(n) * dtype_width(pc->type));
+      prof.set_bytes_model(probe.rows_dev(), n, dtype_width(pc->type), &status->as<DevStatus>()->value, 8.0, status,
+                           probe.rows_owner());
+    }
+    if (defer) {
+      // The pairs fit whenever the build keys are unique; the plan's final
+      // checks re-run it with exact sizes if they did not.
+      defer_check(status, status->as<DevStatus>(), "hash join probe", cap);
+      *n_out = cap;
+      *count_dev = &status->as<DevStatus>()->value;
+      if (count_owner) *count_owner = status;
+      return;
     }
     DevStatus hs;
     GF_CUDA(cudaMemcpyAsync(&hs, status->data(), sizeof(hs), cudaMemcpyDeviceToHost, s));

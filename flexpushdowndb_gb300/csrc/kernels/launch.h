@@ -22,7 +22,20 @@ struct GatherSpec {
   const Column* src;
   const int32_t* idx;  // row ids into src
 };
-std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s);
+// With n_dev, n is a capacity and the kernels read the true count from the
+// device (deferred sizes); utf8 columns need an exact n.
+std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s,
+                                      const int64_t* n_dev = nullptr, BufferPtr n_owner = nullptr);
+
+// Copy several device byte ranges into one contiguous device buffer (one
+// CTA per range): bundles a captured plan's status blocks and result
+// columns so a single copy brings them all to the host.
+struct CopySpan {
+  const void* src;
+  int64_t bytes;
+  int64_t dst_off;
+};
+void pack_spans(const std::vector<CopySpan>& spans, void* dst, cudaStream_t s);
 
 // Exclusive prefix sum of n int32 values into n+1 int32 offsets (offsets[n] =
 // total). Returns the total (synchronizes the stream).
@@ -32,16 +45,22 @@ int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStrea
 
 struct BloomFilterDev {
   BufferPtr blocks;     // num_blocks * 8 uint32 words
-  int64_t num_blocks = 0;
-  int64_t num_keys = 0;
+  int64_t num_blocks = 0;  // exact, or the capacity when nblocks_dev is set
+  int64_t num_keys = 0;    // exact, or an upper bound when nblocks_dev is set
   int32_t num_hashes = 3;
   int32_t bits_per_key = 10;
   bool valid = true;
+  // Set when the filter was sized on the device from deferred key counts.
+  BufferPtr header;
+  const uint64_t* nblocks_dev = nullptr;
+  const int32_t* valid_dev = nullptr;
 };
 using BloomPtr = std::shared_ptr<const BloomFilterDev>;
 
+// part_rows_dev[i] (optional) is the device row count of key_parts[i] when
+// that part comes from a deferred TupleSet (its length is then a capacity).
 BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_per_key, int32_t num_hashes,
-                     cudaStream_t s);
+                     cudaStream_t s, const std::vector<const int64_t*>& part_rows_dev = {});
 
 // ------------------------------------------------------------- select.cu
 
@@ -75,9 +94,13 @@ struct JoinTable {
 void join_build_table(JoinTable& t, double load_factor, cudaStream_t s);
 
 // Probe `probe` on column `probe_key`; returns matching (probe row, build
-// row) pairs as two device int32 arrays of length *n_out.
+// row) pairs as two device int32 arrays of length *n_out. With count_dev
+// and deferred mode on, nothing waits: *n_out is the pairs' capacity (the
+// probe's row capacity, enough when build keys are unique), *count_dev the
+// device count, and an overflow is detected by the plan's final checks.
 void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,
-                      BufferPtr* build_idx, int64_t* n_out, cudaStream_t s);
+                      BufferPtr* build_idx, int64_t* n_out, cudaStream_t s, BufferPtr* count_owner = nullptr,
+                      const int64_t** count_dev = nullptr);
 
 // ------------------------------------------------------------- group.cu
 

@@ -14,11 +14,13 @@
 // and probes are evaluated in order and a later column is only loaded for the
 // rows still alive, so a selective early term saves the DRAM sectors of later
 // columns. Selected rows are ranked with a block scan plus decoupled
-// look-back, giving stable (input-order) output in a single pass; the tile's
-// selected row ids go through shared memory so every output column is written
-// with coalesced stores. Small bloom filters are staged in shared memory once
-// per CTA.
+// look-back, giving stable (input-order) output in a single pass; each thread
+// then moves its own selected rows of every projected column with 128-bit
+// loads, so a sparse tile only touches the sectors holding selected rows.
+// Small bloom filters are staged in shared memory once per CTA. Inputs whose
+// row count lives on the device (deferred sizes) are read with that count.
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <type_traits>
 
@@ -38,23 +40,26 @@ constexpr int kBloomSmemBudget = 96 * 1024;
 
 struct BloomDev {
   const uint32_t* blocks;
+  const uint64_t* nblocks_dev;  // set when the filter's size lives on the device
+  const int32_t* valid_dev;
   uint32_t num_blocks;
   int16_t col;
   int8_t num_hashes;
   int8_t valid;
-  int32_t smem_word;  // < 0: probe from global memory
-  int32_t pad;
+  int32_t smem_word;      // < 0: probe from global memory
+  int32_t smem_cap_words; // shared-memory words reserved for this filter
 };
 
 struct OutCol {
   const void* src;
   void* dst;
   int32_t width;
-  int32_t pad;
+  int32_t aligned;  // src is 16-byte aligned: 128-bit loads allowed
 };
 
 struct SelectParams {
-  int64_t n_rows;
+  int64_t n_rows;            // exact row count, or the capacity when n_dev is set
+  const int64_t* n_dev;      // device row count of a deferred input
   int64_t n_tiles;
   int32_t n_cols;
   int32_t n_probes;
@@ -191,20 +196,36 @@ __device__ __forceinline__ uint32_t leaf8(const SelectParams& p, const Leaf& L, 
   return r & need;
 }
 
+// kPred = false compiles the probe-only form (BloomFilterUse chains), which
+// needs far fewer registers than the general CNF evaluator.
+template <bool kPred>
 __global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_constant__ SelectParams p) {
   extern __shared__ __align__(16) uint32_t s_bloom[];
-  __shared__ int32_t s_rows[kSelTile];
   __shared__ int s_warp[kSelThreads / 32 + 1];
   __shared__ uint32_t s_tile;
   __shared__ uint64_t s_base;
+  __shared__ uint32_t s_nblocks[kMaxBlooms];
 
-  // Stage the small bloom filters in shared memory once per CTA.
+  // Row count: exact, or produced on the device by the previous operator.
+  const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
+  const int64_t n_tiles = (n_rows + kSelTile - 1) / kSelTile;
+
+  // Filter sizes may also live on the device (filters built from deferred
+  // inputs). Stage each filter in shared memory when it fits its slot.
+  uint32_t staged = 0, valid = 0;
+#pragma unroll 1
   for (int pi = 0; pi < p.n_probes; ++pi) {
     const BloomDev& b = p.probes[pi];
-    if (b.smem_word < 0 || !b.valid) continue;
-    const uint4* src = reinterpret_cast<const uint4*>(b.blocks);
-    uint4* dst = reinterpret_cast<uint4*>(s_bloom + b.smem_word);
-    for (uint32_t i = threadIdx.x; i < b.num_blocks * 2; i += kSelThreads) dst[i] = __ldg(src + i);
+    const uint32_t nb = b.nblocks_dev ? static_cast<uint32_t>(*b.nblocks_dev) : b.num_blocks;
+    if (threadIdx.x == 0) s_nblocks[pi] = nb;
+    const bool v = b.valid_dev ? (*b.valid_dev != 0) : (b.valid != 0);
+    if (v) valid |= 1u << pi;
+    if (v && b.smem_word >= 0 && nb * 8 <= static_cast<uint32_t>(b.smem_cap_words)) {
+      staged |= 1u << pi;
+      const uint4* src = reinterpret_cast<const uint4*>(b.blocks);
+      uint4* dst = reinterpret_cast<uint4*>(s_bloom + b.smem_word);
+      for (uint32_t i = threadIdx.x; i < nb * 2; i += kSelThreads) dst[i] = __ldg(src + i);
+    }
   }
   __syncthreads();
 
@@ -212,39 +233,42 @@ __global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_consta
     if (threadIdx.x == 0) s_tile = atomicAdd(p.ticket, 1u);
     __syncthreads();
     const int64_t tile = s_tile;
-    if (tile >= p.n_tiles) break;
+    if (tile >= n_tiles) break;
     const int64_t row0 = tile * kSelTile + static_cast<int64_t>(threadIdx.x) * kSelItems;
-    const bool full = row0 + kSelItems <= p.n_rows;
+    const bool full = row0 + kSelItems <= n_rows;
     const bool vec = full && p.aligned;
     uint32_t mask;
     if (full) {
       mask = 0xFFu;
     } else {
-      const int64_t rem = p.n_rows - row0;
+      const int64_t rem = n_rows - row0;
       mask = rem <= 0 ? 0u : ((1u << rem) - 1u);
     }
 
     // Bloom probes (the predicate-transfer chain), most selective first as
     // the caller ordered them.
+#pragma unroll 1
     for (int pi = 0; pi < p.n_probes; ++pi) {
+      if (!((valid >> pi) & 1u) || mask == 0) continue;
       const BloomDev& b = p.probes[pi];
-      if (!b.valid || mask == 0) continue;
+      const uint32_t nb = s_nblocks[pi];
       int64_t keys[8];
       load8(p.cols[b.col], row0, mask, vec, keys);
       uint32_t keep = 0;
+      const bool in_smem = (staged >> pi) & 1u;
 #pragma unroll
       for (int k = 0; k < kSelItems; ++k) {
         if (!((mask >> k) & 1u)) continue;
         const uint64_t h = hash_key(keys[k]);
-        const uint32_t blk = bloom_block_of(h, b.num_blocks);
-        const uint32_t* words = b.smem_word >= 0 ? s_bloom + b.smem_word + blk * 8 : b.blocks + static_cast<uint64_t>(blk) * 8;
+        const uint32_t blk = bloom_block_of(h, nb);
         bool ok;
-        if (b.smem_word >= 0) {
-          ok = bloom_test(words, h, b.num_hashes);
+        if (in_smem) {
+          ok = bloom_test(s_bloom + b.smem_word + blk * 8, h, b.num_hashes);
         } else {
+          const uint4* words = reinterpret_cast<const uint4*>(b.blocks + static_cast<uint64_t>(blk) * 8);
           uint32_t w[8];
-          const uint4 lo = __ldg(reinterpret_cast<const uint4*>(words));
-          const uint4 hi = __ldg(reinterpret_cast<const uint4*>(words) + 1);
+          const uint4 lo = __ldg(words);
+          const uint4 hi = __ldg(words + 1);
           w[0] = lo.x; w[1] = lo.y; w[2] = lo.z; w[3] = lo.w;
           w[4] = hi.x; w[5] = hi.y; w[6] = hi.z; w[7] = hi.w;
           ok = bloom_test(w, h, b.num_hashes);
@@ -255,12 +279,14 @@ __global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_consta
     }
 
     // Predicate in CNF.
-    for (int c = 0; c < p.prog.n_clauses; ++c) {
-      if (mask == 0) break;
-      uint32_t cm = 0;
-      for (int l = p.prog.clause_begin[c]; l < p.prog.clause_begin[c + 1]; ++l)
-        cm |= leaf8(p, p.prog.leaves[l], row0, mask & ~cm, vec);
-      mask &= cm;
+    if constexpr (kPred) {
+      for (int c = 0; c < p.prog.n_clauses; ++c) {
+        if (mask == 0) break;
+        uint32_t cm = 0;
+        for (int l = p.prog.clause_begin[c]; l < p.prog.clause_begin[c + 1]; ++l)
+          cm |= leaf8(p, p.prog.leaves[l], row0, mask & ~cm, vec);
+        mask &= cm;
+      }
     }
 
     // Rank the selected rows: block scan + decoupled look-back.
@@ -271,44 +297,75 @@ __global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_consta
       const uint64_t b = lookback_exclusive(p.tile_status, tile, static_cast<uint64_t>(tile_total), p.status);
       if (threadIdx.x == 0) s_base = b;
     }
-    {
-      int o = excl;
-#pragma unroll
-      for (int k = 0; k < kSelItems; ++k)
-        if ((mask >> k) & 1u) s_rows[o++] = static_cast<int32_t>(threadIdx.x) * kSelItems + k;
-    }
     __syncthreads();
     const int64_t base = static_cast<int64_t>(s_base);
-    const int64_t tile_row0 = tile * kSelTile;
-    for (int j = 0; j < p.n_out; ++j) {
-      const OutCol& oc = p.outs[j];
-      if (oc.width == 8) {
-        const long long* src = static_cast<const long long*>(oc.src) + tile_row0;
-        long long* dst = static_cast<long long*>(oc.dst) + base;
-        for (int i = threadIdx.x; i < tile_total; i += kSelThreads) dst[i] = __ldg(src + s_rows[i]);
-      } else {
-        const int* src = static_cast<const int*>(oc.src) + tile_row0;
-        int* dst = static_cast<int*>(oc.dst) + base;
-        for (int i = threadIdx.x; i < tile_total; i += kSelThreads) dst[i] = __ldg(src + s_rows[i]);
+    // Projection: each thread moves its own selected rows. A thread with any
+    // selected row loads its 8 rows of a column with 128-bit loads (the
+    // sectors a row-granular gather would touch anyway) and writes the
+    // selected values to consecutive output slots; threads with none load
+    // nothing, so sparse tiles skip most sectors of unselected columns.
+    if (mask != 0) {
+      const int64_t out0 = base + excl;
+#pragma unroll 1
+      for (int j = 0; j < p.n_out; ++j) {
+        const OutCol& oc = p.outs[j];
+        int64_t v[8];
+        const DevCol c{oc.src, nullptr, oc.width == 8 ? CT_I64 : CT_I32, 0};
+        load8(c, row0, mask, vec && oc.aligned, v);
+        int o = 0;
+        if (oc.width == 8) {
+          long long* dst = static_cast<long long*>(oc.dst) + out0;
+#pragma unroll
+          for (int k = 0; k < kSelItems; ++k)
+            if ((mask >> k) & 1u) dst[o++] = v[k];
+        } else {
+          int* dst = static_cast<int*>(oc.dst) + out0;
+#pragma unroll
+          for (int k = 0; k < kSelItems; ++k)
+            if ((mask >> k) & 1u) dst[o++] = static_cast<int>(v[k]);
+        }
+      }
+      if (p.out_rowids != nullptr) {
+        int o = 0;
+#pragma unroll
+        for (int k = 0; k < kSelItems; ++k)
+          if ((mask >> k) & 1u) p.out_rowids[out0 + o++] = static_cast<int32_t>(row0 + k);
       }
     }
-    if (p.out_rowids != nullptr) {
-      for (int i = threadIdx.x; i < tile_total; i += kSelThreads)
-        p.out_rowids[base + i] = static_cast<int32_t>(tile_row0 + s_rows[i]);
-    }
-    if (tile == p.n_tiles - 1 && threadIdx.x == 0) p.status->value = base + tile_total;
+    if (tile == n_tiles - 1 && threadIdx.x == 0) p.status->value = base + tile_total;
     __syncthreads();
   }
 }
 
-int g_select_blocks_per_sm = 0;
+// Resident CTAs per SM for a variant and dynamic shared-memory size, cached
+// (the occupancy query is not free and the answer never changes).
+int select_blocks_per_sm(bool with_pred, size_t dyn) {
+  static std::mutex mu;
+  static std::map<std::pair<bool, size_t>, int> cache;
+  static bool attr_set[2] = {false, false};
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(with_pred, dyn);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  const void* fn = with_pred ? reinterpret_cast<const void*>(select_kernel<true>)
+                             : reinterpret_cast<const void*>(select_kernel<false>);
+  if (!attr_set[with_pred]) {
+    GF_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kBloomSmemBudget));
+    attr_set[with_pred] = true;
+  }
+  int per_sm = 0;
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSelThreads, dyn));
+  if (per_sm < 1) per_sm = 1;
+  cache[key] = per_sm;
+  return per_sm;
+}
 
 }  // namespace
 
 TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const std::vector<BloomProbe>& probes,
                         const std::vector<std::string>& project, bool all_columns, cudaStream_t s,
                         SelectStats* stats) {
-  const int64_t n = in.num_rows();
+  const int64_t n = in.num_rows();  // exact, or the capacity of a deferred input
   if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "a TupleSet passed to select must have fewer than 2^31 rows");
   if (static_cast<int>(probes.size()) > kMaxBlooms) fail(GFPDB_EUNSUPPORTED, "too many bloom probes in one select");
 
@@ -317,6 +374,7 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   SelectParams& p = *pp;
   std::memset(&p, 0, sizeof(p));
   p.n_rows = n;
+  p.n_dev = in.rows_dev();
 
   ColumnSlots slots;
   if (pred != nullptr) {
@@ -339,6 +397,10 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     if ((reinterpret_cast<uintptr_t>(p.cols[i].data) & 15u) != 0) aligned = false;
   p.aligned = aligned ? 1 : 0;
 
+  // Shared-memory slots for the filters: an exact filter gets its whole size
+  // while the budget lasts; a filter whose size is only known on the device
+  // gets up to kDeferredBloomSlot bytes and is staged if it turns out to fit.
+  constexpr int kDeferredBloomSlot = 16 * 1024;
   int smem_words = 0;
   p.n_probes = static_cast<int32_t>(probes.size());
   for (size_t i = 0; i < probes.size(); ++i) {
@@ -347,13 +409,17 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     b.blocks = bf.blocks->as<uint32_t>();
     if (bf.num_blocks >= (int64_t{1} << 32)) fail(GFPDB_EUNSUPPORTED, "bloom filter too large");
     b.num_blocks = static_cast<uint32_t>(bf.num_blocks);
+    b.nblocks_dev = bf.nblocks_dev;
+    b.valid_dev = bf.valid_dev;
     b.col = static_cast<int16_t>(probe_slot[i]);
     b.num_hashes = static_cast<int8_t>(bf.num_hashes);
     b.valid = bf.valid ? 1 : 0;
-    const int words = static_cast<int>(bf.num_blocks * 8);
-    if (bf.valid && (smem_words + words) * 4 <= kBloomSmemBudget) {
+    int64_t words = bf.num_blocks * 8;
+    if (bf.nblocks_dev != nullptr && words * 4 > kDeferredBloomSlot) words = kDeferredBloomSlot / 4;
+    if ((bf.valid || bf.valid_dev) && (smem_words + words) * 4 <= kBloomSmemBudget) {
       b.smem_word = smem_words;
-      smem_words += words;
+      b.smem_cap_words = static_cast<int32_t>(words);
+      smem_words += static_cast<int>(words);
     } else {
       b.smem_word = -1;
     }
@@ -384,6 +450,7 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     oc.src = c->data;
     oc.dst = out_bufs[j]->data();
     oc.width = w;
+    oc.aligned = (reinterpret_cast<uintptr_t>(c->data) & 15u) == 0 ? 1 : 0;
   }
   BufferPtr rowids;
   if (need_rowids) {
@@ -391,7 +458,7 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     p.out_rowids = rowids->as<int32_t>();
   }
 
-  const int64_t n_tiles = (n + kSelTile - 1) / kSelTile;
+  const int64_t n_tiles = (n + kSelTile - 1) / kSelTile;  // upper bound
   p.n_tiles = n_tiles;
   auto scratch = make_buffer(sizeof(DevStatus) + 64 + n_tiles * 8, s);
   char* sb = scratch->as<char>();
@@ -400,41 +467,48 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   p.tile_status = reinterpret_cast<uint64_t*>(sb + sizeof(DevStatus) + 64);
   GF_CUDA(cudaMemsetAsync(sb, 0, scratch->size(), s));
 
-  int64_t count = 0;
+  // Algorithmic bytes: every evaluated column read once over all rows, the
+  // selected rows of the other projected columns read once, every projected
+  // value written once.
+  double read_all = 0, proj_read = 0, proj_write = 0;
+  for (int i = 0; i < p.n_cols; ++i) read_all += dtype_width(static_cast<DType>(p.cols[i].type));
+  for (int j = 0; j < p.n_out; ++j) {
+    proj_write += p.outs[j].width;
+    bool evaluated = false;
+    for (int i = 0; i < p.n_cols; ++i) evaluated |= p.cols[i].data == p.outs[j].src;
+    if (!evaluated) proj_read += p.outs[j].width;
+  }
   if (n_tiles > 0) {
     const size_t dyn = static_cast<size_t>(smem_words) * 4;
-    if (g_select_blocks_per_sm == 0) {
-      GF_CUDA(cudaFuncSetAttribute(select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBloomSmemBudget));
-    }
-    int per_sm = 0;
-    GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_kernel, kSelThreads, dyn));
-    if (per_sm < 1) per_sm = 1;
-    g_select_blocks_per_sm = per_sm;
+    const bool with_pred = p.prog.n_clauses > 0;
+    const int per_sm = select_blocks_per_sm(with_pred, dyn);
     int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
     if (grid > n_tiles) grid = n_tiles;
     ProfScope prof("select_kernel", s);
-    select_kernel<<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
+    if (with_pred)
+      select_kernel<true><<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
+    else
+      select_kernel<false><<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
     after_launch("select_kernel");
     prof.stop(0);
+    prof.set_bytes_model(p.n_dev, n, read_all, &p.status->value, proj_read + proj_write, scratch, in.rows_owner());
+  }
+
+  const bool defer = deferred_mode() && !need_rowids && stats == nullptr;
+  if (defer) {
+    defer_check(scratch, p.status, "select");
+    for (size_t j = 0; j < out_names.size(); ++j)
+      out_cols[j] = make_fixed_column(out_fields[j].type, n, out_bufs[j]);
+    return TupleSet::make_deferred(std::move(out_fields), std::move(out_cols), n, scratch, &p.status->value);
+  }
+  int64_t count = 0;
+  if (n_tiles > 0) {
     DevStatus hs;
     GF_CUDA(cudaMemcpyAsync(&hs, p.status, sizeof(hs), cudaMemcpyDeviceToHost, s));
     sync(s);
     raise_device_status(hs, "select");
     count = hs.value;
-    // Algorithmic bytes: every evaluated column read once over all rows, the
-    // selected rows of the other projected columns read once, every projected
-    // value written once.
-    double read_all = 0, proj_read = 0, proj_write = 0;
-    for (int i = 0; i < p.n_cols; ++i) read_all += dtype_width(static_cast<DType>(p.cols[i].type));
-    for (int j = 0; j < p.n_out; ++j) {
-      proj_write += p.outs[j].width;
-      bool evaluated = false;
-      for (int i = 0; i < p.n_cols; ++i) evaluated |= p.cols[i].data == p.outs[j].src;
-      if (!evaluated) proj_read += p.outs[j].width;
-    }
-    prof.set_bytes(static_cast<double>(n) * read_all + static_cast<double>(count) * (proj_read + proj_write));
   }
-
   for (size_t j = 0; j < out_names.size(); ++j) {
     if (out_fields[j].type == DType::Utf8) continue;
     out_cols[j] = make_fixed_column(out_fields[j].type, count, out_bufs[j]);
@@ -576,6 +650,7 @@ extern "C" int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, con
       oc.src = static_cast<const char*>(c->buffers[1]) + (c->offset + arr.offset) * dtype_width(t);
       oc.dst = out_columns[j];
       oc.width = dtype_width(t);
+      oc.aligned = (reinterpret_cast<uintptr_t>(oc.src) & 15u) == 0 ? 1 : 0;
     }
     const int64_t n_tiles = (n + kSelTile - 1) / kSelTile;
     p.n_tiles = n_tiles;
@@ -588,12 +663,9 @@ extern "C" int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, con
     GF_CUDA(cudaMemsetAsync(sb, 0, kNoAllocHeader + static_cast<size_t>(n_tiles) * 8, s));
     int64_t count = 0;
     if (n_tiles > 0) {
-      int per_sm = 0;
-      GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_kernel, kSelThreads, 0));
-      if (per_sm < 1) per_sm = 1;
-      int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
+      int64_t grid = static_cast<int64_t>(num_sms()) * select_blocks_per_sm(true, 0);
       if (grid > n_tiles) grid = n_tiles;
-      select_kernel<<<static_cast<int>(grid), kSelThreads, 0, s>>>(p);
+      select_kernel<true><<<static_cast<int>(grid), kSelThreads, 0, s>>>(p);
       after_launch("select_kernel");
       DevStatus hs;
       GF_CUDA(cudaMemcpyAsync(&hs, p.status, sizeof(hs), cudaMemcpyDeviceToHost, s));

@@ -48,6 +48,76 @@ def test_star_query_forward_only(gpu):
     assert got.table.sorted_rows() == queries.star_query_direct(tabs).sorted_rows()
 
 
+@pytest.mark.parametrize("deferred", [True, False])
+def test_star_query_deferred_and_exact_sizes(gpu, deferred):
+    tabs = workloads.star_tables(fact_rows=300_000, seed=2024)
+    p = workloads.star_plan()
+    text = p.to_json()[:-1] + f',"deferredSizes":{"true" if deferred else "false"}}}'
+    got = plan.execute(text, tabs)
+    assert got.table.sorted_rows() == queries.star_query(tabs).sorted_rows()
+
+
+def _with_options(p, **opts):
+    import json
+
+    d = json.loads(p.to_json())
+    d.update(opts)
+    return json.dumps(d)
+
+
+def test_star_query_cuda_graph_capture_and_replay(gpu):
+    tabs = workloads.star_tables(fact_rows=500_000, seed=77)
+    dev = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
+    text = _with_options(workloads.star_plan(), cudaGraph=True)
+    want = queries.star_query(tabs).sorted_rows()
+    for _ in range(4):  # capture on the first call, replays after
+        got = plan.execute(text, dev)
+        assert got.table.sorted_rows() == want
+    # other input buffers: a new capture for them
+    tabs2 = workloads.star_tables(fact_rows=500_000, seed=78)
+    dev2 = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs2.items()})
+    for _ in range(2):
+        assert plan.execute(text, dev2).table.sorted_rows() == queries.star_query(tabs2).sorted_rows()
+    # the first inputs' graph is still valid
+    assert plan.execute(text, dev).table.sorted_rows() == want
+
+
+def test_cuda_graph_with_host_inputs_and_fallback(gpu):
+    # pinned host inputs: the host-to-device copies are part of the graph
+    tabs = workloads.star_tables(fact_rows=200_000, seed=5)
+    pinned = plan.PreparedInputs(tabs, pinned=True)
+    text = _with_options(workloads.star_plan(), cudaGraph=True)
+    want = queries.star_query(tabs).sorted_rows()
+    for _ in range(3):
+        assert plan.execute(text, pinned).table.sorted_rows() == want
+    # a utf8 group key needs the host mid-plan: capture is refused and every
+    # call runs the ordinary path
+    t2 = workloads.two_table_tables(fact_rows=100_000)
+    text2 = _with_options(workloads.two_table_plan(), cudaGraph=True)
+    for _ in range(3):
+        assert plan.execute(text2, t2).table.sorted_rows() == queries.two_table_query(t2).sorted_rows()
+
+
+def test_duplicate_build_keys_rerun_with_exact_sizes(gpu):
+    # Every dim key appears twice, so each matching fact row joins two dim
+    # rows and the join output exceeds the probe side's row count: the
+    # deferred run overflows and the plan is re-run with exact sizes.
+    import numpy as np
+
+    from flexpushdowndb_gb300.tupleset import Column, Table
+    from oracle import ops as oops
+
+    tabs = workloads.two_table_tables(fact_rows=50_000, dim_rows=2_000)
+    d = tabs["dim"]
+    dup = Table([Column(c.name, c.type, np.concatenate([c.values, c.values]) if c.type != "utf8" else
+                        d[c.name] + d[c.name]) for c in d.columns])
+    tabs2 = {"fact": tabs["fact"], "dim": dup}
+    got = plan.execute(workloads.two_table_plan(), tabs2)
+    want = queries.two_table_query(tabs2)
+    assert got.table.sorted_rows() == want.sorted_rows()
+    assert sum(r[-1] for r in want.rows()) > 0
+
+
 def test_plan_errors_surface_as_error_messages(gpu):
     tabs = workloads.two_table_tables(fact_rows=1000)
     p = workloads.two_table_plan()
