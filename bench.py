@@ -296,20 +296,27 @@ def main():
             plan.execute(plain_text, dev_inputs, stream=sptr)
         plain_ms, plain_steps, _, _ = timed(plain_text, dev_inputs, args.steps)
         plain_ms = max_over_ranks(plain_ms)
-        # ---- e2e: pinned host inputs through the same C-ABI call
-        for _ in range(args.warmup):
-            plan.execute(graph_text, host_inputs, stream=sptr)
-        barrier()
-        e2e_times = []
-        h2d = d2h = 0
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            r = plan.execute(graph_text, host_inputs, stream=sptr)
-            torch.cuda.synchronize()
-            e2e_times.append(time.perf_counter() - t0)
-            h2d, d2h = r.stats["h2d_bytes"], r.stats["d2h_bytes"]
-        barrier()
-        e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times))
+        # ---- e2e: pinned host inputs through the same C-ABI call; the scans
+        # copy them with the copy engine or with SM loads over the
+        # chip-to-chip link, and the faster of the two is reported
+        e2e_modes = {}
+        for mode in ("engine", "sm"):
+            text = json.dumps(dict(plan_d, cudaGraph=True, hostCopy=mode))
+            parity = parity and plan.execute(text, host_inputs, stream=sptr).table.sorted_rows() == want
+            for _ in range(args.warmup):
+                plan.execute(text, host_inputs, stream=sptr)
+            barrier()
+            e2e_times = []
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                r = plan.execute(text, host_inputs, stream=sptr)
+                torch.cuda.synchronize()
+                e2e_times.append(time.perf_counter() - t0)
+            barrier()
+            e2e_modes[mode] = (max_over_ranks(sum(e2e_times) / len(e2e_times)), r.stats)
+        e2e_mode = min(e2e_modes, key=lambda m: e2e_modes[m][0])
+        e2e_s, e2e_stats = e2e_modes[e2e_mode]
+        h2d, d2h = e2e_stats["h2d_bytes"], e2e_stats["d2h_bytes"]
         # ---- profiled pass: every kernel launch of the plain path timed with
         # CUDA events on its stream, algorithmic bytes per launch
         _abi.check(L.gfpdb_profile_reset())
@@ -371,7 +378,8 @@ def main():
                   "latency_ms": {"p50": plat[len(plat) // 2], "p99": plat[min(len(plat) - 1, int(0.99 * len(plat)))]}},
         "parity": parity,
         "e2e": {"value": FACT_ROWS * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s},
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s, "host_copy": e2e_mode,
+                "ms_per_step_by_copy": {m: 1e3 * v[0] for m, v in e2e_modes.items()}},
         "gpu_launches": launches,
         "roofline": roofline,
         "kernels": {k: {"launches_per_step": v["launches"] / args.steps, "us_per_step": 1e3 * v["ms"] / args.steps}

@@ -217,23 +217,36 @@ class BloomFilterCreatePOp : public PhysicalOp {
 
 // BloomFilterUsePOp (fpdb-executor/src/physical/bloomfilter/BloomFilterUsePOp.cpp:71-142):
 // buffers TupleSets until the filter arrives, then filters each one.
+//
+// After pipeline fusion (fuse_bloom_chains below) one BloomFilterUsePOp may
+// carry several (column, creator) probes: it waits for every filter and then
+// applies them all in one pass over each TupleSet, in chain order.
 class BloomFilterUsePOp : public PhysicalOp {
  public:
-  BloomFilterUsePOp(std::string name, std::string column)
-      : PhysicalOp(std::move(name), "BloomFilterUsePOp"), column_(std::move(column)) {}
+  BloomFilterUsePOp(std::string name, std::vector<std::string> columns, std::vector<std::string> creators)
+      : PhysicalOp(std::move(name), "BloomFilterUsePOp"), columns_(std::move(columns)),
+        creators_(std::move(creators)), blooms_(columns_.size()) {}
 
   void onReceive(const Envelope& env) override {
     const Message& m = env.getMessage();
     if (m.type == MessageType::TUPLESET) {
-      if (bloom_) filterAndSend(m.tuples);
+      if (ready()) filterAndSend(m.tuples);
       else buffered_.push_back(m.tuples);
     } else if (m.type == MessageType::BLOOM_FILTER) {
-      bloom_ = m.bloom;
-      for (auto& t : buffered_) filterAndSend(t);
-      buffered_.clear();
+      size_t i = 0;
+      if (!creators_.empty()) {
+        auto it = std::find(creators_.begin(), creators_.end(), m.sender);
+        if (it == creators_.end()) fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name_ + "': filter from '" + m.sender + "'");
+        i = static_cast<size_t>(it - creators_.begin());
+      }
+      blooms_[i] = m.bloom;
+      if (ready()) {
+        for (auto& t : buffered_) filterAndSend(t);
+        buffered_.clear();
+      }
     } else if (m.type == MessageType::COMPLETE) {
       if (!is_producer_complete(*this)) return;
-      if (!bloom_ && !buffered_.empty())
+      if (!ready() && !buffered_.empty())
         fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name_ + "': producers completed without a bloom filter");
       ctx()->notifyComplete();
     }
@@ -241,18 +254,26 @@ class BloomFilterUsePOp : public PhysicalOp {
 
   void clear() override {
     buffered_.clear();
-    bloom_.reset();
+    for (auto& b : blooms_) b.reset();
   }
 
  private:
+  bool ready() const {
+    for (auto& b : blooms_)
+      if (!b) return false;
+    return true;
+  }
   void filterAndSend(const TupleSetPtr& ts) {
+    std::vector<BloomProbe> probes;
+    for (size_t i = 0; i < columns_.size(); ++i) probes.push_back(BloomProbe{blooms_[i], columns_[i]});
     Message out;
     out.type = MessageType::TUPLESET;
-    out.tuples = select_rows(*ts, nullptr, {BloomProbe{bloom_, column_}}, {}, true, ctx()->stream());
+    out.tuples = select_rows(*ts, nullptr, probes, {}, true, ctx()->stream());
     ctx()->tell(out);
   }
-  std::string column_;
-  BloomPtr bloom_;
+  std::vector<std::string> columns_;
+  std::vector<std::string> creators_;
+  std::vector<BloomPtr> blooms_;
   std::vector<TupleSetPtr> buffered_;
 };
 
@@ -558,7 +579,12 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
                                                 static_cast<int>(o.get_int("numHashes", 3)),
                                                 o.str_list("bloomFilterUsePOps"));
   } else if (type == "BloomFilterUsePOp") {
-    op = std::make_unique<BloomFilterUsePOp>(name, o.at("bloomFilterColumn").str());
+    std::vector<std::string> cols = o.contains("bloomFilterColumns") ? o.str_list("bloomFilterColumns")
+                                                                     : std::vector<std::string>{o.at("bloomFilterColumn").str()};
+    std::vector<std::string> creators = o.str_list("creators");
+    if (!creators.empty() && creators.size() != cols.size())
+      fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name + "': one creator per filter column");
+    op = std::make_unique<BloomFilterUsePOp>(name, cols, creators);
   } else if (type == "HashJoinArrowPOp") {
     std::string jt = o.get_str("joinType", "INNER");
     if (jt != "INNER") fail(GFPDB_EUNSUPPORTED, "join type '" + jt + "' (only INNER runs on the GPU path)");
@@ -588,7 +614,110 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
 
 }  // namespace
 
-std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream) {
+namespace {
+
+json::Value jstr(const std::string& s) {
+  json::Value v;
+  v.kind = json::Value::String;
+  v.s = s;
+  return v;
+}
+
+json::Value jlist(const std::vector<std::string>& xs) {
+  json::Value v;
+  v.kind = json::Value::Array;
+  for (auto& x : xs) v.a.push_back(jstr(x));
+  return v;
+}
+
+void jset(json::Value& o, const std::string& key, json::Value v) {
+  for (auto& kv : o.o)
+    if (kv.first == key) {
+      kv.second = std::move(v);
+      return;
+    }
+  o.o.emplace_back(key, std::move(v));
+}
+
+json::Value* jfind(json::Value& o, const std::string& key) {
+  for (auto& kv : o.o)
+    if (kv.first == key) return &kv.second;
+  return nullptr;
+}
+
+}  // namespace
+
+// Pipeline fusion: a chain of BloomFilterUsePOps in which each one's only
+// consumer is the next, and the next's only data producer is the previous,
+// becomes one BloomFilterUsePOp carrying every (column, creator) probe, so
+// the fact table is scanned once instead of once per filter. The fused
+// operator keeps the last one's name, so every reference to the chain's end
+// stays valid. Results are unchanged: a row survives the fused pass exactly
+// when it survives every filter of the chain.
+json::Value fuse_bloom_chains(const json::Value& plan) {
+  json::Value out = plan;
+  json::Value* ops_v = jfind(out, "ops");
+  if (ops_v == nullptr) return out;
+  auto& ops = ops_v->a;
+  for (;;) {
+    std::map<std::string, std::vector<std::string>> producers, creators;
+    for (auto& o : ops) {
+      for (auto& c : o.str_list("consumers")) producers[c].push_back(o.at("name").str());
+      if (o.at("type").str() == "BloomFilterCreatePOp")
+        for (auto& u : o.str_list("bloomFilterUsePOps")) creators[u].push_back(o.at("name").str());
+    }
+    auto creators_of = [&](const json::Value& u) {
+      auto c = u.str_list("creators");
+      return c.empty() ? creators[u.at("name").str()] : c;
+    };
+    auto columns_of = [&](const json::Value& u) {
+      return u.contains("bloomFilterColumns") ? u.str_list("bloomFilterColumns")
+                                              : std::vector<std::string>{u.at("bloomFilterColumn").str()};
+    };
+    int first = -1, second = -1;
+    for (size_t i = 0; i < ops.size() && first < 0; ++i) {
+      if (ops[i].at("type").str() != "BloomFilterUsePOp") continue;
+      auto cons = ops[i].str_list("consumers");
+      if (cons.size() != 1) continue;
+      for (size_t j = 0; j < ops.size(); ++j) {
+        if (j == i || ops[j].at("type").str() != "BloomFilterUsePOp" || ops[j].at("name").str() != cons[0]) continue;
+        if (producers[cons[0]] != std::vector<std::string>{ops[i].at("name").str()}) break;
+        if (creators_of(ops[i]).size() != columns_of(ops[i]).size()) break;
+        if (creators_of(ops[j]).size() != columns_of(ops[j]).size()) break;
+        first = static_cast<int>(i);
+        second = static_cast<int>(j);
+        break;
+      }
+    }
+    if (first < 0) break;
+    const std::string u1 = ops[first].at("name").str(), u2 = ops[second].at("name").str();
+    auto cols = columns_of(ops[first]);
+    auto c2 = columns_of(ops[second]);
+    cols.insert(cols.end(), c2.begin(), c2.end());
+    auto crs = creators_of(ops[first]);
+    auto r2 = creators_of(ops[second]);
+    crs.insert(crs.end(), r2.begin(), r2.end());
+    jset(ops[second], "bloomFilterColumns", jlist(cols));
+    jset(ops[second], "creators", jlist(crs));
+    for (auto& o : ops) {
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers"}) {
+        json::Value* l = jfind(o, key);
+        if (l == nullptr) continue;
+        std::vector<std::string> v = o.str_list(key), nv;
+        for (auto& x : v) {
+          const std::string y = x == u1 ? u2 : x;
+          if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
+        }
+        *l = jlist(nv);
+      }
+    }
+    ops.erase(ops.begin() + first);
+  }
+  return out;
+}
+
+std::unique_ptr<Execution> build_execution(const json::Value& plan_in, cudaStream_t stream) {
+  const json::Value plan = plan_in.get_bool("fusePipelines", true) ? fuse_bloom_chains(plan_in) : plan_in;
   auto ex = std::make_unique<Execution>(stream);
   for (auto& o : plan.at("ops").array()) ex->add(make_op(o, ex.get()));
   for (auto& o : plan.at("ops").array()) {

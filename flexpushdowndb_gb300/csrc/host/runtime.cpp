@@ -270,6 +270,12 @@ thread_local std::vector<DeferredCheck> g_checks;
 bool deferred_mode() { return g_deferred; }
 void set_deferred_mode(bool on) { g_deferred = on; }
 
+namespace {
+thread_local int g_host_copy = 0;
+}
+int host_copy_mode() { return g_host_copy; }
+void set_host_copy_mode(int mode) { g_host_copy = mode; }
+
 void defer_check(BufferPtr owner, const DevStatus* status, const char* where, int64_t capacity) {
   g_checks.push_back(DeferredCheck{std::move(owner), status, where, capacity});
 }

@@ -160,6 +160,9 @@ struct DeferredCheck {
 };
 bool deferred_mode();
 void set_deferred_mode(bool on);
+// How scans copy host inputs to the device: 0 = copy engine, 1 = SM loads.
+int host_copy_mode();
+void set_host_copy_mode(int mode);
 void defer_check(BufferPtr owner, const DevStatus* status, const char* where, int64_t capacity = 0);
 // Reads every recorded status (the stream must be synchronized). Raises the
 // first device error; returns false if some output overflowed its capacity.

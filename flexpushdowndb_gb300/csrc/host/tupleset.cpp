@@ -262,7 +262,7 @@ TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* d
       if (host || copy_device) {
         auto buf = make_buffer(n * w, s);
         if (host) {
-          memcpy_h2d(buf->data(), src, n * w, s);
+          copy_h2d(buf->data(), src, n * w, s);
         } else if (n > 0) {
           GF_CUDA(cudaMemcpyAsync(buf->data(), src, n * w, cudaMemcpyDeviceToDevice, s));
         }

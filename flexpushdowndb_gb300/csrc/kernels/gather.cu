@@ -137,6 +137,23 @@ __global__ void __launch_bounds__(256) pack_spans_kernel(const __grid_constant__
   }
 }
 
+// Host-to-device copy done by the SMs: each thread streams 16-byte words from
+// page-locked host memory (reachable from the device through its unified
+// address) into device memory, four loads in flight per thread.
+__global__ void __launch_bounds__(256) h2d_copy_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                                       int64_t n16) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+    dst[i] = a;
+    dst[i + stride] = b;
+    dst[i + 2 * stride] = c;
+    dst[i + 3 * stride] = d;
+  }
+  for (; i < n16; i += stride) dst[i] = src[i];
+}
+
 int grid_for(int64_t n, int threads) {
   int64_t blocks = (n + threads - 1) / threads;
   int64_t cap = static_cast<int64_t>(num_sms()) * 8;
@@ -146,6 +163,27 @@ int grid_for(int64_t n, int threads) {
 }
 
 }  // namespace
+
+void copy_h2d(void* dst, const void* src, int64_t bytes, cudaStream_t s) {
+  if (bytes <= 0) return;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0;
+  cudaPointerAttributes attr{};
+  const bool pinned = cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+  (void)cudaGetLastError();
+  if (host_copy_mode() != 1 || !aligned || !pinned || bytes < (int64_t{1} << 20)) {
+    memcpy_h2d(dst, src, bytes, s);
+    return;
+  }
+  const int64_t n16 = bytes / 16;
+  const int grid = num_sms() * 4;
+  h2d_copy_kernel<<<grid, 256, 0, s>>>(static_cast<const uint4*>(attr.devicePointer ? attr.devicePointer : src),
+                                       static_cast<uint4*>(dst), n16);
+  after_launch("h2d_copy_kernel");
+  const int64_t tail = bytes - n16 * 16;
+  if (tail > 0) GF_CUDA(cudaMemcpyAsync(static_cast<char*>(dst) + n16 * 16, static_cast<const char*>(src) + n16 * 16,
+                                        tail, cudaMemcpyHostToDevice, s));
+  copy_counters().h2d += bytes;
+}
 
 void pack_spans(const std::vector<CopySpan>& spans, void* dst, cudaStream_t s) {
   for (size_t at = 0; at < spans.size(); at += kPackMax) {

@@ -37,6 +37,11 @@ struct CopySpan {
 };
 void pack_spans(const std::vector<CopySpan>& spans, void* dst, cudaStream_t s);
 
+// Host-to-device copy of a scan's input: the copy engine (cudaMemcpyAsync),
+// or, with host_copy_mode() == 1 and page-locked aligned sources of at least
+// 1 MiB, a kernel whose loads read host memory over the chip-to-chip link.
+void copy_h2d(void* dst, const void* src, int64_t bytes, cudaStream_t s);
+
 // Exclusive prefix sum of n int32 values into n+1 int32 offsets (offsets[n] =
 // total). Returns the total (synchronizes the stream).
 int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);

@@ -98,6 +98,15 @@ def test_cuda_graph_with_host_inputs_and_fallback(gpu):
         assert plan.execute(text2, t2).table.sorted_rows() == queries.two_table_query(t2).sorted_rows()
 
 
+@pytest.mark.parametrize("fuse", [True, False])
+def test_bloom_chain_fusion_same_result(gpu, fuse):
+    tabs = workloads.star_tables(fact_rows=400_000, seed=99)
+    r = plan.execute(_with_options(workloads.star_plan(), fusePipelines=fuse), tabs)
+    assert r.table.sorted_rows() == queries.star_query(tabs).sorted_rows()
+    # the four forward BloomFilterUsePOps on the fact table fuse into one
+    assert r.stats["num_ops"] == (28 if fuse else 31)
+
+
 def test_duplicate_build_keys_rerun_with_exact_sizes(gpu):
     # Every dim key appears twice, so each matching fact row joins two dim
     # rows and the join output exceeds the probe side's row count: the
