@@ -300,7 +300,7 @@ def main():
         # copy them with the copy engine or with SM loads over the
         # chip-to-chip link, and the faster of the two is reported
         e2e_modes = {}
-        for mode in ("engine", "sm"):
+        for mode in ("engine", "sm", "zerocopy"):
             text = json.dumps(dict(plan_d, cudaGraph=True, hostCopy=mode))
             parity = parity and plan.execute(text, host_inputs, stream=sptr).table.sorted_rows() == want
             for _ in range(args.warmup):
@@ -314,7 +314,9 @@ def main():
                 e2e_times.append(time.perf_counter() - t0)
             barrier()
             e2e_modes[mode] = (max_over_ranks(sum(e2e_times) / len(e2e_times)), r.stats)
-        e2e_mode = min(e2e_modes, key=lambda m: e2e_modes[m][0])
+        # e2e counts only paths that copy every input across; the zero-copy
+        # scan (kernels read host columns in place) is reported beside it
+        e2e_mode = min(("engine", "sm"), key=lambda m: e2e_modes[m][0])
         e2e_s, e2e_stats = e2e_modes[e2e_mode]
         h2d, d2h = e2e_stats["h2d_bytes"], e2e_stats["d2h_bytes"]
         # ---- profiled pass: every kernel launch of the plain path timed with
@@ -380,6 +382,10 @@ def main():
         "e2e": {"value": FACT_ROWS * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s, "host_copy": e2e_mode,
                 "ms_per_step_by_copy": {m: 1e3 * v[0] for m, v in e2e_modes.items()}},
+        "e2e_zero_copy": {"value": FACT_ROWS * world / e2e_modes["zerocopy"][0], "unit": UNIT,
+                          "note": "host columns read in place over NVLink-C2C by the scan kernels; "
+                                  "only touched sectors cross the link",
+                          "ms_per_step": 1e3 * e2e_modes["zerocopy"][0]},
         "gpu_launches": launches,
         "roofline": roofline,
         "kernels": {k: {"launches_per_step": v["launches"] / args.steps, "us_per_step": 1e3 * v["ms"] / args.steps}

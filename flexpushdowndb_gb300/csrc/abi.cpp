@@ -675,7 +675,7 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
     struct CopyModeGuard {
       explicit CopyModeGuard(int m) { set_host_copy_mode(m); }
       ~CopyModeGuard() { set_host_copy_mode(0); }
-    } copy_mode(plan.get_str("hostCopy", "engine") == "sm" ? 1 : 0);
+    } copy_mode(plan.get_str("hostCopy", "engine") == "sm" ? 1 : plan.get_str("hostCopy", "engine") == "zerocopy" ? 2 : 0);
     const bool use_graph = deferred && plan.get_bool("cudaGraph", false);
     TupleSetPtr result;
     pop::ExecStats xs;

@@ -160,7 +160,8 @@ struct DeferredCheck {
 };
 bool deferred_mode();
 void set_deferred_mode(bool on);
-// How scans copy host inputs to the device: 0 = copy engine, 1 = SM loads.
+// How scans bring host inputs to the device: 0 = copy engine, 1 = SM loads,
+// 2 = no copy (kernels read page-locked host columns directly).
 int host_copy_mode();
 void set_host_copy_mode(int mode);
 void defer_check(BufferPtr owner, const DevStatus* status, const char* where, int64_t capacity = 0);

@@ -233,6 +233,17 @@ std::vector<Field> import_schema(const ArrowSchema* schema) {
   return fields;
 }
 
+// Device address of page-locked host memory (nullptr for pageable memory).
+const void* device_view_of_host(const void* p) {
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (attr.type != cudaMemoryTypeHost) return nullptr;
+  return attr.devicePointer != nullptr ? attr.devicePointer : p;
+}
+
 TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* darr, cudaStream_t s,
                             bool copy_device) {
   auto fields = import_schema(schema);
@@ -259,7 +270,13 @@ TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* d
       if (c->n_buffers != 2) fail(GFPDB_EINVAL, "fixed-width column needs 2 buffers");
       int w = dtype_width(t);
       const char* src = static_cast<const char*>(c->buffers[1]) + off * w;
-      if (host || copy_device) {
+      const void* zc = host && host_copy_mode() == 2 && !copy_device ? device_view_of_host(src) : nullptr;
+      if (zc != nullptr) {
+        // Zero-copy: kernels read the page-locked host column over the
+        // chip-to-chip link; only the sectors they touch cross it.
+        auto buf = std::make_shared<DeviceBuffer>(const_cast<void*>(zc), n * w);
+        cols.push_back(make_fixed_column(t, n, buf));
+      } else if (host || copy_device) {
         auto buf = make_buffer(n * w, s);
         if (host) {
           copy_h2d(buf->data(), src, n * w, s);

@@ -98,6 +98,17 @@ def test_cuda_graph_with_host_inputs_and_fallback(gpu):
         assert plan.execute(text2, t2).table.sorted_rows() == queries.two_table_query(t2).sorted_rows()
 
 
+@pytest.mark.parametrize("mode", ["engine", "sm", "zerocopy"])
+@pytest.mark.parametrize("graph", [False, True])
+def test_host_input_copy_modes(gpu, mode, graph):
+    tabs = workloads.star_tables(fact_rows=300_000, seed=31)
+    pinned = plan.PreparedInputs(tabs, pinned=True)
+    text = _with_options(workloads.star_plan(), hostCopy=mode, cudaGraph=graph)
+    want = queries.star_query(tabs).sorted_rows()
+    for _ in range(3 if graph else 1):
+        assert plan.execute(text, pinned).table.sorted_rows() == want
+
+
 @pytest.mark.parametrize("fuse", [True, False])
 def test_bloom_chain_fusion_same_result(gpu, fuse):
     tabs = workloads.star_tables(fact_rows=400_000, seed=99)
