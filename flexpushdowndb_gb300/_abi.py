@@ -142,6 +142,12 @@ SIGNATURES = {
         [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A), _I32, _S, _A, ctypes.POINTER(ExecStats), _P],
     ),
     "gfpdb_plan_validate": (_I32, [ctypes.c_char_p]),
+    "gfpdb_graph_cache_clear": (_I32, []),
+    "gfpdb_star_batch": (
+        _I32,
+        [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A), _I32, _I32, _S, _A,
+         ctypes.POINTER(ExecStats), _P],
+    ),
 }
 
 _lib = None

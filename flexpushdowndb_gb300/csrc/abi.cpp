@@ -189,6 +189,108 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
   return cp;
 }
 
+// ---- batched star queries: prepared batches (and their graphs), cached.
+
+struct BatchEntry {
+  StarBatch batch;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;
+  ~BatchEntry() {
+    if (exec) (void)cudaGraphExecDestroy(exec);
+  }
+};
+
+std::mutex g_batch_mu;
+std::map<std::string, std::shared_ptr<BatchEntry>> g_batches;
+
+std::shared_ptr<BatchEntry> find_batch(const std::string& key) {
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  auto it = g_batches.find(key);
+  return it == g_batches.end() ? nullptr : it->second;
+}
+
+void remember_batch(const std::string& key, std::shared_ptr<BatchEntry> be) {
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  if (g_batches.size() >= 64) g_batches.clear();  // bounded cache
+  g_batches[key] = std::move(be);
+}
+
+void clear_batches() {
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  g_batches.clear();
+}
+
+std::shared_ptr<BatchEntry> make_batch(const json::Value& spec, const std::map<std::string, TupleSetPtr>& tables,
+                                       bool use_graph, cudaStream_t s) {
+  auto be = std::make_shared<BatchEntry>();
+  StarBatchSpec& sp = be->batch.spec();
+  auto table = [&](const std::string& name) {
+    auto it = tables.find(name);
+    if (it == tables.end()) fail(GFPDB_EINVAL, "batched star query names table '" + name + "' which was not passed");
+    return it->second;
+  };
+  sp.fact_tables = spec.str_list("factTables");
+  for (auto& n : sp.fact_tables) be->batch.parts().push_back(table(n));
+  for (auto& d : spec.at("dimensions").array()) {
+    StarBatchSpec::Dim dim{d.at("table").str(), d.at("key").str(), d.at("factKey").str(), d.at("filterColumn").str()};
+    be->batch.dim_tables().push_back(table(dim.table));
+    sp.dims.push_back(dim);
+  }
+  if (spec.contains("groupBy"))
+    for (auto& g : spec.at("groupBy").array())
+      sp.group.push_back(StarBatchSpec::Group{static_cast<int>(g.at("dimension").integer()), g.at("column").str()});
+  for (auto& a : spec.at("aggregates").array()) {
+    StarBatchSpec::Agg agg;
+    const std::string f = a.at("function").str();
+    if (f == "SUM") agg.fn = AGG_SUM;
+    else if (f == "COUNT") agg.fn = AGG_COUNT_STAR;
+    else fail(GFPDB_EUNSUPPORTED, "batched star aggregates are SUM and COUNT(*)");
+    agg.name = a.at("name").str();
+    agg.columns = a.str_list("columns");
+    sp.aggs.push_back(agg);
+  }
+  for (auto& q : spec.at("queries").array()) {
+    std::vector<std::pair<int64_t, int64_t>> ranges;
+    for (auto& r : q.array()) ranges.emplace_back(r.array().at(0).integer(), r.array().at(1).integer());
+    if (ranges.size() != sp.dims.size()) fail(GFPDB_EINVAL, "each batched query needs one range per dimension");
+    sp.queries.push_back(ranges);
+  }
+  if (spec.contains("probeOrder"))
+    for (auto& o : spec.at("probeOrder").array()) sp.probe_order.push_back(static_cast<int>(o.integer()));
+  sp.load_factor = spec.get_num("loadFactor", 0.5);
+  if (!(sp.load_factor > 0 && sp.load_factor <= 0.9)) fail(GFPDB_EINVAL, "loadFactor must be in (0, 0.9]");
+  sp.items_per_thread = static_cast<int>(spec.get_int("itemsPerThread", 4));
+  sp.blocks_per_sm = static_cast<int>(spec.get_int("blocksPerSm", 4));
+  if (sp.blocks_per_sm < 1 || sp.blocks_per_sm > 16) fail(GFPDB_EINVAL, "blocksPerSm must be in [1, 16]");
+  sp.groups_hint = spec.get_int("groupsHint", 1024);
+  be->batch.prepare(s);
+  if (use_graph) {
+    // run() only clears preallocated buffers and launches kernels: capture it.
+    cudaStream_t cs = nullptr;
+    GF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    const uint64_t k0 = g_kernel_launches.load();
+    cudaGraph_t graph = nullptr;
+    bool ok = true;
+    GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+      be->batch.run(cs);
+    } catch (const std::exception&) {
+      ok = false;
+    }
+    if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) ok = false;
+    if (ok && cudaGraphInstantiate(&be->exec, graph, 0) != cudaSuccess) ok = false;
+    if (graph) (void)cudaGraphDestroy(graph);
+    (void)cudaGetLastError();
+    (void)cudaStreamDestroy(cs);
+    be->kernels = g_kernel_launches.load() - k0;
+    if (!ok && be->exec) {
+      (void)cudaGraphExecDestroy(be->exec);
+      be->exec = nullptr;
+    }
+  }
+  return be;
+}
+
 // A device copy of the first n rows of an arena-backed result (the next
 // replay reuses the arena).
 TupleSetPtr device_copy(const TupleSet& r, int64_t n, cudaStream_t s) {
@@ -720,6 +822,72 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
     export_tupleset(result, out_schema, out, result_to_host != 0, s);
     sync(s);
     fill_stats(xs.num_ops, xs.messages);
+  });
+}
+
+int32_t gfpdb_graph_cache_clear(void) {
+  return guarded([&] {
+    {
+      std::lock_guard<std::mutex> lk(g_graph_mu);
+      g_graphs.clear();
+    }
+    clear_batches();
+  });
+}
+
+int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* const* table_names,
+                         const ArrowSchema* const* schemas, const ArrowDeviceArray* const* arrays, int32_t use_graph,
+                         int32_t result_to_host, ArrowSchema* out_schema, ArrowDeviceArray* out,
+                         gfpdb_exec_stats* stats, void* stream) {
+  return guarded([&] {
+    require(spec_json != nullptr && out_schema != nullptr && out != nullptr, "null argument");
+    const auto t0 = std::chrono::steady_clock::now();
+    ensure_device();
+    cudaStream_t s = as_stream(stream);
+    const CopyCounters c0 = copy_counters();
+    const uint64_t launches0 = g_kernel_launches.load();
+    const std::string key = std::string(use_graph ? "G|" : "P|") + plan_key(spec_json, n_tables, table_names, arrays);
+    std::shared_ptr<BatchEntry> be = find_batch(key);
+    if (!be) {
+      json::Value spec;
+      try {
+        spec = json::parse(spec_json);
+      } catch (const std::exception& e) {
+        fail(GFPDB_EINVAL, e.what());
+      }
+      std::map<std::string, TupleSetPtr> tables;
+      for (int32_t i = 0; i < n_tables; ++i) {
+        require(table_names[i] != nullptr, "null table name");
+        if (arrays[i]->device_type != ARROW_DEVICE_CUDA)
+          fail(GFPDB_EINVAL, "batched star inputs must be device-resident");
+        tables[table_names[i]] = import_tupleset(schemas[i], arrays[i], s);
+      }
+      be = make_batch(spec, tables, use_graph != 0, s);
+      remember_batch(key, be);
+    }
+    if (be->exec != nullptr) {
+      GF_CUDA(cudaGraphLaunch(be->exec, s));
+      count_launch(be->kernels);
+    } else {
+      be->batch.run(s);
+    }
+    DevStatus st;
+    GF_CUDA(cudaMemcpyAsync(&st, be->batch.status(), sizeof(st), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    if (st.code == GFPDB_EINVAL && st.detail >= 100 && st.detail < 110)
+      fail(GFPDB_EINVAL, "batched star query: dimension " + std::to_string(st.detail - 100) + " repeats a key");
+    raise_device_status(st, "batched star query");
+    export_tupleset(be->batch.result_view(), out_schema, out, result_to_host != 0, s);
+    sync(s);
+    if (stats != nullptr) {
+      stats->kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
+      stats->h2d_bytes = copy_counters().h2d - c0.h2d;
+      stats->d2h_bytes = copy_counters().d2h - c0.d2h;
+      stats->num_ops = 3;
+      stats->messages = 0;
+      stats->elapsed_ns =
+          std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    }
   });
 }
 

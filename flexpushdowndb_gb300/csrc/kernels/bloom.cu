@@ -22,7 +22,7 @@ struct BloomHeader {
   int64_t num_keys;
 };
 
-constexpr int kMaxBloomParts = 64;
+constexpr int kMaxBloomParts = 256;
 
 struct BloomSizeParams {
   const int64_t* n_dev[kMaxBloomParts];

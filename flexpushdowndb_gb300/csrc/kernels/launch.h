@@ -123,6 +123,62 @@ std::shared_ptr<GroupTable> group_table_create(const std::vector<std::string>& g
 void group_table_update(GroupTable& g, const TupleSet& batch, cudaStream_t s);
 TupleSetPtr group_table_finalize(GroupTable& g, cudaStream_t s);
 
+// --------------------------------------------------------- starbatch.cu
+
+constexpr int kSBMaxDims = 8;
+constexpr int kSBMaxQueries = 64;
+constexpr int kSBMaxParts = 256;
+
+// A batch of star queries over one partitioned fact table that differ only
+// in their per-dimension filter ranges (lo <= filter column <= hi).
+struct StarBatchSpec {
+  struct Dim {
+    std::string table, key, fact_key, filter;
+  };
+  struct Group {
+    int dim;
+    std::string column;
+  };
+  struct Agg {
+    AggFn fn;  // AGG_SUM or AGG_COUNT_STAR
+    std::string name;
+    std::vector<std::string> columns;  // SUM of one fact column or of the product of two
+  };
+  std::vector<std::string> fact_tables;
+  std::vector<Dim> dims;
+  std::vector<Group> group;
+  std::vector<Agg> aggs;
+  std::vector<std::vector<std::pair<int64_t, int64_t>>> queries;  // [query][dim] = (lo, hi)
+  std::vector<int> probe_order;  // dimension probe order (most selective first)
+  double load_factor = 0.5;      // join tables
+  int items_per_thread = 4;      // fact rows per thread per tile
+  int blocks_per_sm = 4;         // persistent CTAs per SM
+  int64_t groups_hint = 1024;    // upper bound on groups per query
+};
+
+struct StarBatchState;
+
+// Preallocates every buffer in prepare(); run() only clears and fills them,
+// so it can be captured into a CUDA graph.
+class StarBatch {
+ public:
+  StarBatch();
+  ~StarBatch();
+  StarBatchSpec& spec();
+  std::vector<TupleSetPtr>& parts();       // fact partitions
+  std::vector<TupleSetPtr>& dim_tables();  // one per spec().dims
+  void prepare(cudaStream_t s);
+  void run(cudaStream_t s);
+  // (query_id, group columns..., aggregates...), row count on the device;
+  // valid after run() until the next run().
+  TupleSetPtr result_view() const;
+  const DevStatus* status() const;
+  int64_t fact_rows() const;
+
+ private:
+  std::unique_ptr<StarBatchState> st_;
+};
+
 // --------------------------------------------------------------- csv.cu
 
 struct CsvField {

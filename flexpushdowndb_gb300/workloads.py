@@ -21,7 +21,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .expression import col, eq, lt, num_lit, times
+from .expression import and_, col, eq, gte, lt, lte, num_lit, times
 from .ops import aggregate
 from .plan import Plan
 from .tupleset import Column, Table
@@ -115,24 +115,41 @@ def star_tables(fact_rows: int = 6_000_000, seed: int = 2000) -> dict[str, Table
 
 
 def star_plan(consts=STAR_DEFAULT_CONSTS, bits_per_key: int = 10, num_hashes: int = 3, chunk_rows: int = 0,
-              backward: bool = True) -> Plan:
+              backward: bool = True, ranges=None, fact_tables=("fact",), probe_order=(2, 3, 4, 1)) -> Plan:
     """Forward + backward bloom predicate transfer, then the 4-way join and
     group-by, in the shape SmallToLargePredTransOrder builds
-    (fpdb-executor/src/physical/transform/pred-trans/SmallToLargePredTransOrder.cpp:38-214)."""
+    (fpdb-executor/src/physical/transform/pred-trans/SmallToLargePredTransOrder.cpp:38-214).
+    Dimension filters are f == const, or lo <= f <= hi with `ranges`; the
+    fact table may be several partitions, one scan each (the reference's one
+    scan operator per partition, PrePToPTransformer.cpp:1078-1100)."""
     p = Plan()
     dim_tail = {}
     fwd = {}
     for i in range(1, 5):
         p.scan(f"scan_d{i}", f"d{i}", [f"d{i}_pk", f"d{i}_f", f"d{i}_g"])
         keep = [f"d{i}_pk", f"d{i}_g"] if i in (2, 4) else [f"d{i}_pk"]
-        p.filter(f"filter_d{i}", f"scan_d{i}", eq(col(f"d{i}_f"), num_lit(int(consts[i - 1]), "int32")), keep)
+        if ranges is not None:
+            lo, hi = ranges[i - 1]
+            pred = and_(gte(col(f"d{i}_f"), num_lit(int(lo), "int32")), lte(col(f"d{i}_f"), num_lit(int(hi), "int32")))
+        else:
+            pred = eq(col(f"d{i}_f"), num_lit(int(consts[i - 1]), "int32"))
+        p.filter(f"filter_d{i}", f"scan_d{i}", pred, keep)
         fwd[i] = p.bloom_create(f"bf_fwd_create_d{i}", f"filter_d{i}", f"d{i}_pk", bits_per_key, num_hashes)
         dim_tail[i] = fwd[i]
-    p.scan("scan_fact", "fact", ["fk1", "fk2", "fk3", "fk4", "qty", "price_cents", "discount"], chunk_rows=chunk_rows)
-    tail = "scan_fact"
+    fact_cols = ["fk1", "fk2", "fk3", "fk4", "qty", "price_cents", "discount"]
+    scans = [p.scan(f"scan_{t}", t, fact_cols, chunk_rows=chunk_rows) for t in fact_tables]
     # forward: the most selective filters first (1/25, 1/7, 1/7, 1/5)
-    for i in (2, 3, 4, 1):
-        tail = p.bloom_use(f"bf_fwd_use_fk{i}", tail, fwd[i], f"fk{i}")
+    first = True
+    tail = None
+    for i in probe_order:
+        name = f"bf_fwd_use_fk{i}"
+        if first:
+            tail = p.bloom_use(name, scans[0], fwd[i], f"fk{i}")
+            for sc in scans[1:]:
+                p.connect(sc, name)
+            first = False
+        else:
+            tail = p.bloom_use(name, tail, fwd[i], f"fk{i}")
     if backward:
         for i in range(1, 5):
             c = p.bloom_create(f"bf_bwd_create_fk{i}", tail, f"fk{i}", bits_per_key, num_hashes)
@@ -152,3 +169,60 @@ def star_plan(consts=STAR_DEFAULT_CONSTS, bits_per_key: int = 10, num_hashes: in
     ], groups_hint=256)
     p.collate("collate", "group")
     return p
+
+
+# -------------------------------------------------------------------- batched
+#
+# The batched form: the star query's fact table split into partitions of
+# uneven size, and query variants that differ in their dimension filter
+# ranges. Dimension filter columns are uniform over 100 values so a variant
+# selecting k values of a dimension has selectivity k% (1% to 40%).
+
+BATCH_FILTER_VALUES = 100
+
+
+def batch_partition_sizes(n_parts: int = 64, lo: int = 50_000, hi: int = 4_000_000, seed: int = 4000) -> list[int]:
+    """Partition sizes log-uniform in [lo, hi]."""
+    u = splitmix64(seed, n_parts).astype(np.float64) / float(2**64)
+    return [int(round(np.exp(np.log(lo) + x * (np.log(hi) - np.log(lo))))) for x in u]
+
+
+def batch_tables(n_parts: int = 64, sizes=None, seed: int = 4000) -> dict[str, Table]:
+    sizes = sizes or batch_partition_sizes(n_parts, seed=seed)
+    out = {}
+    for i, n in enumerate(STAR_DIM_ROWS, start=1):
+        out[f"d{i}"] = Table([
+            Column(f"d{i}_pk", "int32", np.arange(1, n + 1, dtype=np.int64)),
+            Column(f"d{i}_f", "int32", uniform(seed, 10 + i, n, 0, BATCH_FILTER_VALUES - 1)),
+            Column(f"d{i}_g", "int32", uniform(seed, 20 + i, n, 0, STAR_GROUP_VALUES[i - 1] - 1)),
+        ])
+    start = 0
+    for p, n in enumerate(sizes):
+        out[f"p{p}"] = star_fact(n, seed=seed, start=start)
+        start += n
+    return out
+
+
+def batch_queries(n_queries: int = 32, seed: int = 4100) -> list[list[tuple[int, int]]]:
+    """Per query and dimension a range [0, k - 1] with k in [1, 40]."""
+    k = uniform(seed, 1, n_queries * 4, 1, 40).reshape(n_queries, 4)
+    return [[(0, int(k[q, d]) - 1) for d in range(4)] for q in range(n_queries)]
+
+
+def star_batch_spec(fact_tables, queries, load_factor: float = 0.5, items_per_thread: int = 4,
+                    blocks_per_sm: int = 4, probe_order=(1, 2, 3, 0), groups_hint: int = 256) -> dict:
+    return {
+        "factTables": list(fact_tables),
+        "dimensions": [{"table": f"d{i}", "key": f"d{i}_pk", "factKey": f"fk{i}", "filterColumn": f"d{i}_f"}
+                       for i in range(1, 5)],
+        "groupBy": [{"dimension": 1, "column": "d2_g"}, {"dimension": 3, "column": "d4_g"}],
+        "aggregates": [{"function": "SUM", "name": "revenue", "columns": ["price_cents", "qty"]},
+                       {"function": "SUM", "name": "discount_revenue", "columns": ["price_cents", "discount"]},
+                       {"function": "COUNT", "name": "cnt"}],
+        "queries": [[list(r) for r in q] for q in queries],
+        "probeOrder": list(probe_order),
+        "loadFactor": load_factor,
+        "itemsPerThread": items_per_thread,
+        "blocksPerSm": blocks_per_sm,
+        "groupsHint": groups_hint,
+    }

@@ -295,6 +295,39 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
 /* Parse and check a plan without running it (host only, no CUDA calls). */
 int32_t gfpdb_plan_validate(const char* plan_json);
 
+/* Plans run with "cudaGraph": true and batches run with use_graph are kept,
+ * keyed by their text and input buffer addresses, so later calls replay them.
+ * They reference the caller's input buffers: clear them before freeing those
+ * buffers for good. */
+int32_t gfpdb_graph_cache_clear(void);
+
+/* ---------------------------------------------------- batched star queries */
+
+/* Run many star queries that differ only in their dimension filter ranges
+ * over one fact table split into partitions, with one launch per stage for
+ * all queries and partitions: a dimension pass builds one shared join table
+ * per dimension whose rows carry the bitmask of the queries selecting them, a
+ * persistent fact pass probes every dimension once per fact row for all
+ * queries and aggregates into per-query group tables, and a final pass
+ * compacts every query's groups. With use_graph the stages are captured once
+ * as a CUDA graph and replayed. Spec JSON:
+ *   {"factTables": ["p0", ...],
+ *    "dimensions": [{"table": "d1", "key": "d1_pk", "factKey": "fk1", "filterColumn": "d1_f"}, ...],
+ *    "groupBy": [{"dimension": 1, "column": "d2_g"}, ...],          (0 to 2)
+ *    "aggregates": [{"function": "SUM", "name": "revenue", "columns": ["price_cents", "qty"]},
+ *                   {"function": "COUNT", "name": "cnt"}],
+ *    "queries": [[[lo, hi], ...one range per dimension...], ...],   (1 to 64)
+ *    "probeOrder": [1, 2, 3, 0], "loadFactor": 0.5, "itemsPerThread": 4,
+ *    "blocksPerSm": 4, "groupsHint": 1024}
+ * The result has a query_id column, then the group columns, then the
+ * aggregates; each query's rows equal that query's single-query plan
+ * (the join / group parts of SmallToLargePredTransOrder.cpp's star plans,
+ * HashJoinArrowKernel.cpp and GroupArrowKernel.cpp semantics). */
+int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* const* table_names,
+                         const struct ArrowSchema* const* schemas, const struct ArrowDeviceArray* const* arrays,
+                         int32_t use_graph, int32_t result_to_host, struct ArrowSchema* out_schema,
+                         struct ArrowDeviceArray* out, gfpdb_exec_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,3 +69,27 @@ def star_query(tables: dict[str, Table], consts=(1, 3, 2, 5), bits_per_key: int 
 
 def star_query_direct(tables: dict[str, Table], consts=(1, 3, 2, 5)) -> Table:
     return _star_join_group(tables["fact"], _star_dims(tables, consts))
+
+
+def concat_tables(parts: list[Table]) -> Table:
+    import numpy as np
+
+    from flexpushdowndb_gb300.tupleset import Column
+
+    return Table([Column(c.name, c.type, np.concatenate([p.column(c.name).values for p in parts]))
+                  for c in parts[0].columns])
+
+
+def star_query_ranges(tables: dict[str, Table], fact_tables, ranges) -> Table:
+    """The star query with lo <= d{i}_f <= hi dimension filters over a fact
+    table given as partitions (no bloom pass: blooms never change results)."""
+    from flexpushdowndb_gb300.expression import and_, gte, lte
+
+    dims = {}
+    for i in range(1, 5):
+        keep = [f"d{i}_pk", f"d{i}_g"] if i in (2, 4) else [f"d{i}_pk"]
+        lo, hi = ranges[i - 1]
+        pred = and_(gte(col(f"d{i}_f"), num_lit(int(lo), "int32")), lte(col(f"d{i}_f"), num_lit(int(hi), "int32")))
+        dims[i] = ops.filter_table(tables[f"d{i}"], pred, keep)
+    fact = concat_tables([tables[t] for t in fact_tables])
+    return _star_join_group(fact, dims)
