@@ -148,6 +148,98 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _kernel_profile(L, _abi, fn, reps: int) -> dict:
+    """Per-kernel event timings of `reps` calls of fn (profiling on)."""
+    _abi.check(L.gfpdb_profile_reset())
+    _abi.check(L.gfpdb_profile_enable(1))
+    for _ in range(reps):
+        fn()
+    _abi.check(L.gfpdb_profile_enable(0))
+    buf = ctypes.create_string_buffer(4096)
+    _abi.check(L.gfpdb_profile_kernels(buf, 4096))
+    out = {}
+    for name in buf.value.decode().split():
+        n, t_ms, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+        _abi.check(L.gfpdb_profile_read(name.encode(), n, t_ms, by))
+        out[name] = {"launches": n.value, "ms": t_ms.value, "bytes": by.value}
+    return out
+
+
+def batched_section(args, L, sptr) -> dict:
+    """The batched form: the star query's fact table as 64 partitions of
+    log-uniform size (59,952,713 rows), 32 query variants with dimension
+    filter ranges of 1%-40% selectivity each. Batched: one gfpdb_star_batch
+    call (one launch per stage for all partitions and queries, replayed as a
+    CUDA graph). Plain: each query as its own physical plan (one scan per
+    partition), launched operator by operator; per-query graph: the same
+    plans captured and replayed one at a time. Every query's batched result
+    is compared with its plain plan's."""
+    from flexpushdowndb_gb300 import _abi, batch, plan, workloads
+    from flexpushdowndb_gb300.tupleset import DeviceTable
+
+    tabs = workloads.batch_tables()
+    parts = [f"p{i}" for i in range(64)]
+    qs = workloads.batch_queries(32)
+    nq = len(qs)
+    rows = sum(tabs[p].num_rows for p in parts)
+    dev = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
+    del tabs
+    spec = workloads.star_batch_spec(parts, qs)
+    for _ in range(args.warmup):
+        batch.star_batch(spec, dev, stream=sptr)
+    times = []
+    for _ in range(max(args.steps, 10)):
+        t0 = time.perf_counter()
+        r = batch.star_batch(spec, dev, stream=sptr)
+        times.append(time.perf_counter() - t0)
+    got = batch.split_by_query(r.table)
+    kern = _kernel_profile(L, _abi, lambda: batch.star_batch(spec, dev, use_graph=False, stream=sptr), 3)
+    # plain per-query plans, operator by operator
+    texts = [workloads.star_plan(ranges=q, fact_tables=parts).to_json() for q in qs]
+    plan.execute(texts[0], dev, stream=sptr)
+    parity = True
+    plain = []
+    for q in range(nq):
+        t0 = time.perf_counter()
+        res = plan.execute(texts[q], dev, stream=sptr)
+        plain.append(time.perf_counter() - t0)
+        parity &= res.table.sorted_rows() == got.get(q, [])
+    # per-query graphs: a few queries, each captured then replayed
+    graph = []
+    for q in range(4):
+        text = json.dumps(dict(json.loads(texts[q]), cudaGraph=True))
+        for _ in range(2):
+            plan.execute(text, dev, stream=sptr)
+        for _ in range(5):
+            t0 = time.perf_counter()
+            plan.execute(text, dev, stream=sptr)
+            graph.append(time.perf_counter() - t0)
+        batch.clear_graph_cache()
+    t_batch = statistics.median(times)
+    t_plain = sum(plain) / len(plain)
+    t_graph = statistics.median(graph)
+    lat = sorted(times)
+    fact = kern.get("sb_fact_kernel")
+    return {
+        "workload": "star query over 64 fact partitions (log-uniform 50,000-4,000,000 rows, %d in all), "
+                    "32 variants with dimension filter ranges of 1%%-40%% selectivity" % rows,
+        "fact_rows": rows, "queries": nq,
+        "queries_per_s": nq / t_batch,
+        "fact_rows_per_s": rows * nq / t_batch,
+        "ms_per_batch": 1e3 * t_batch,
+        "latency_ms": {"p50": 1e3 * lat[len(lat) // 2], "p99": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "plain_per_query": {"queries_per_s": 1 / t_plain, "ms_per_query": 1e3 * t_plain},
+        "graph_per_query": {"queries_per_s": 1 / t_graph, "ms_per_query": 1e3 * t_graph,
+                            "note": "median over 4 of the 32 queries, each captured and replayed"},
+        "speedup_vs_plain": t_plain * nq / t_batch,
+        "speedup_vs_graph_per_query": t_graph * nq / t_batch,
+        "parity_vs_plain": parity,
+        "kernels_us_per_batch": {k: 1e3 * v["ms"] / 3 for k, v in kern.items()},
+        "fact_kernel_fk_gbs": (fact["bytes"] / (fact["ms"] / 1e3) / 1e9) if fact else None,
+        "settings": {k: spec[k] for k in ("itemsPerThread", "blocksPerSm", "loadFactor")},
+    }
+
+
 def run_case(args):
     """Single-kernel cases for profiling (ncu) and kernel tuning; prints one
     JSON line with the case's own timing. `select`: the forward bloom probe of
@@ -206,6 +298,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph")
     ap.add_argument("--rows", type=int, default=FACT_ROWS)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form section")
     args = ap.parse_args()
     if args.case:
         return run_case(args)
@@ -353,6 +446,9 @@ def main():
                     "algorithmic_bytes_per_launch": k["bytes"] / max(1, k["launches"]),
                     "share_of_kernel_time": k["ms"] / gpu_ms_total if gpu_ms_total else None}
 
+    # the batched form runs after the timed region, on every rank (replicas)
+    batched = None if args.no_batched else batched_section(args, L, sptr)
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -392,6 +488,7 @@ def main():
                     for k, v in kernels.items()},
         "clocks": clocks.summary(),
         "cpu_baseline": base,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

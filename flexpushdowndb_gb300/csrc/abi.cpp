@@ -259,7 +259,7 @@ std::shared_ptr<BatchEntry> make_batch(const json::Value& spec, const std::map<s
     for (auto& o : spec.at("probeOrder").array()) sp.probe_order.push_back(static_cast<int>(o.integer()));
   sp.load_factor = spec.get_num("loadFactor", 0.5);
   if (!(sp.load_factor > 0 && sp.load_factor <= 0.9)) fail(GFPDB_EINVAL, "loadFactor must be in (0, 0.9]");
-  sp.items_per_thread = static_cast<int>(spec.get_int("itemsPerThread", 4));
+  sp.items_per_thread = static_cast<int>(spec.get_int("itemsPerThread", 2));
   sp.blocks_per_sm = static_cast<int>(spec.get_int("blocksPerSm", 4));
   if (sp.blocks_per_sm < 1 || sp.blocks_per_sm > 16) fail(GFPDB_EINVAL, "blocksPerSm must be in [1, 16]");
   sp.groups_hint = spec.get_int("groupsHint", 1024);

@@ -128,6 +128,9 @@ TupleSetPtr group_table_finalize(GroupTable& g, cudaStream_t s);
 constexpr int kSBMaxDims = 8;
 constexpr int kSBMaxQueries = 64;
 constexpr int kSBMaxParts = 256;
+constexpr int64_t kSBSmemBudget = 200 * 1024;       // staged query masks per SM
+constexpr int64_t kSBSmemPerBlockMax = 200 * 1024;  // and per block
+constexpr int64_t kSBSmemMaxDynamic = 220 * 1024;   // dynamic shared memory of one fact-stage block
 
 // A batch of star queries over one partitioned fact table that differ only
 // in their per-dimension filter ranges (lo <= filter column <= hi).
@@ -149,9 +152,9 @@ struct StarBatchSpec {
   std::vector<Group> group;
   std::vector<Agg> aggs;
   std::vector<std::vector<std::pair<int64_t, int64_t>>> queries;  // [query][dim] = (lo, hi)
-  std::vector<int> probe_order;  // dimension probe order (most selective first)
+  std::vector<int> probe_order;  // dimension probe order; empty: shared-memory dimensions, then by size
   double load_factor = 0.5;      // join tables
-  int items_per_thread = 4;      // fact rows per thread per tile
+  int items_per_thread = 2;      // fact rows per consumer thread per tile: 1, 2, 4 or 8
   int blocks_per_sm = 4;         // persistent CTAs per SM
   int64_t groups_hint = 1024;    // upper bound on groups per query
 };

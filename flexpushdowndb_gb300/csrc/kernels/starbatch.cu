@@ -33,6 +33,12 @@ namespace sb {
 
 constexpr int kSBThreads = 256;
 
+// A dimension is looked up in one of two ways, chosen on the device each run
+// from the key range of its rows: when max - min + 1 is at most the table
+// capacity (dense surrogate keys), the query mask and row of key k sit at
+// k - min in two direct arrays; otherwise in the open-addressing table.
+// Either way a fact row finds exactly the dimension rows whose key equals
+// its foreign key.
 struct SBDimDev {
   DevCol key;
   DevCol filter;
@@ -42,8 +48,15 @@ struct SBDimDev {
   uint64_t* slots;       // (tag << 32 | row), all-ones = empty
   uint64_t mask;         // capacity - 1
   uint64_t* qmask;       // per dimension row
+  uint64_t* dq;          // direct: query mask per key - min (0 = no row)
+  uint32_t* drow;        // direct: row per key - min (all-ones = no row)
+  int32_t* dg[2];        // direct: group column values per key - min
+  unsigned long long* kmin_u;  // key range, order-preserving unsigned (key ^ sign bit)
+  unsigned long long* kmax_u;
   int32_t key32;
   int32_t n_group;
+  int32_t smem_off;      // byte offset of this dimension's staged masks and group values (-1: not staged)
+  int32_t smem_cap;      // keys staged when the key range fits (a multiple of 8)
 };
 
 struct SBDimsParams {
@@ -54,6 +67,45 @@ struct SBDimsParams {
   const int64_t* ranges;  // [q][d][2] (lo, hi)
   DevStatus* st;
 };
+
+constexpr unsigned long long kSignBit = 0x8000000000000000ull;
+
+struct SBDirect {
+  int64_t kmin;
+  uint64_t range;  // 0: look up in the hash table
+};
+
+__device__ __forceinline__ SBDirect sb_direct(const SBDimDev& D) {
+  const unsigned long long lo = *reinterpret_cast<volatile unsigned long long*>(D.kmin_u);
+  const unsigned long long hi = *reinterpret_cast<volatile unsigned long long*>(D.kmax_u);
+  if (D.rows == 0 || lo > hi) return SBDirect{0, 0};
+  const uint64_t range = static_cast<uint64_t>(hi - lo) + 1;  // difference of order-preserving codes
+  if (range == 0 || range > D.mask + 1) return SBDirect{0, 0};
+  return SBDirect{static_cast<int64_t>(lo ^ kSignBit), range};
+}
+
+// Key range of every dimension: blockIdx.y is the dimension.
+__global__ void __launch_bounds__(kSBThreads) sb_range_kernel(const __grid_constant__ SBDimsParams p) {
+  const SBDimDev& D = p.dims[blockIdx.y];
+  unsigned long long lo = ~0ull, hi = 0ull;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < D.rows; r += stride) {
+    const unsigned long long u = static_cast<unsigned long long>(load_int(D.key, r)) ^ kSignBit;
+    lo = u < lo ? u : lo;
+    hi = u > hi ? u : hi;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(0xffffffffu, lo, o);
+    const unsigned long long b = __shfl_xor_sync(0xffffffffu, hi, o);
+    lo = a < lo ? a : lo;
+    hi = b > hi ? b : hi;
+  }
+  if ((threadIdx.x & 31) == 0 && lo <= hi) {
+    atomicMin(D.kmin_u, lo);
+    atomicMax(D.kmax_u, hi);
+  }
+}
 
 __global__ void __launch_bounds__(kSBThreads) sb_dims_kernel(const __grid_constant__ SBDimsParams p) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
@@ -71,6 +123,17 @@ __global__ void __launch_bounds__(kSBThreads) sb_dims_kernel(const __grid_consta
     D.qmask[r] = m;
     if (m == 0) continue;
     const int64_t k = load_int(D.key, r);
+    const SBDirect dr = sb_direct(D);
+    if (dr.range != 0) {
+      const uint64_t idx = static_cast<uint64_t>(k) - static_cast<uint64_t>(dr.kmin);  // < range by construction
+      if (atomicCAS(D.drow + idx, 0xFFFFFFFFu, static_cast<uint32_t>(r)) != 0xFFFFFFFFu) {
+        raise_status(p.st, GFPDB_EINVAL, 100 + d);  // repeated dimension key
+      } else {
+        D.dq[idx] = m;
+        for (int c = 0; c < D.n_group; ++c) D.dg[c][idx] = static_cast<int32_t>(load_int(D.group[c], r));
+      }
+      continue;
+    }
     const uint64_t h = hash_key(k);
     const uint32_t tag = D.key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
     const uint64_t packed = (static_cast<uint64_t>(tag) << 32) | static_cast<uint32_t>(r);
@@ -110,6 +173,12 @@ struct SBAgg {
   int32_t pad;
 };
 
+constexpr int kSBConsumerWarps = 8;
+constexpr int kSBFactThreads = (kSBConsumerWarps + 1) * 32;  // consumer warps + one producer warp
+constexpr int kSBStages = 2;
+constexpr int kSBMaxAggsFact = 4;  // aggregates of a batched star query
+constexpr int kSBBarBytes = 128;  // 2 * kSBStages mbarriers, padded
+
 struct SBFactParams {
   SBDimDev dims[kSBMaxDims];
   SBFactDims fd;
@@ -119,18 +188,22 @@ struct SBFactParams {
   int32_t n_queries;
   int32_t n_parts;
   int32_t n_cols;       // fact columns per partition
-  int32_t items;        // rows per thread per tile
+  int32_t items;        // rows per consumer thread per tile
   uint64_t qvalid;      // bitmask of the batch's queries
   const DevCol* part_cols;   // [part][n_cols]
-  const int64_t* tile_base;  // [n_parts + 1] first tile of each partition
+  const int64_t* tile_base;  // [n_parts + 1] first tile (kSBConsumerWarps * 32 * items rows) of each partition
   const int64_t* part_rows;  // [n_parts]
   int64_t n_tiles;
-  uint32_t* ticket;
-  uint64_t* gkeys;           // [q][gcap + 1]
-  unsigned long long* gaccs; // [q][gcap + 1][n_aggs]
-  uint64_t gmask;            // gcap - 1
-  int64_t* special;          // [q] the all-ones key has a group
-  int64_t* groups;           // [q] groups claimed
+  uint64_t* gkeys;               // [gcap] group keys, shared by every query (all-ones = empty)
+  unsigned long long* touched;   // [gcap + 1] queries with rows in each group; slot gcap: the all-ones key
+  unsigned long long* gaccs;     // [q][gcap + 1][n_aggs]
+  uint64_t gmask;                // gcap - 1
+  int32_t staged;                // foreign-key columns are 16-byte aligned: tiles arrive by bulk copy
+  int32_t stage_bytes;           // one pipeline stage: every foreign-key segment of a tile
+  int32_t seg_off[kSBMaxDims];   // byte offset of dimension d's foreign keys in a stage
+  int32_t fk_width[kSBMaxDims];  // 4 or 8
+  int32_t masks_off;             // byte offset of the staged query masks in dynamic shared memory
+  int32_t pad;
   DevStatus* st;
 };
 
@@ -150,92 +223,299 @@ __device__ __forceinline__ int64_t sb_lookup(const SBDimDev& D, int64_t k) {
   return -1;
 }
 
-__device__ __forceinline__ uint64_t sb_group_slot(const SBFactParams& p, int q, uint64_t key) {
-  uint64_t* keys = p.gkeys + static_cast<uint64_t>(q) * (p.gmask + 2);
-  if (key == kEmptySlot) {
-    if (atomicExch(reinterpret_cast<unsigned long long*>(&p.special[q]), 1ull) == 0ull)
-      atomicAdd(reinterpret_cast<unsigned long long*>(&p.groups[q]), 1ull);
-    return p.gmask + 1;
-  }
+// Slot of a group key in the table shared by all queries (gmask + 1 for the
+// all-ones key). A slot's key changes once, from empty to its final value, so
+// a cached read that sees a key can trust it; one that sees empty is settled
+// by the CAS.
+__device__ __forceinline__ uint64_t sb_group_slot(const SBFactParams& p, uint64_t key) {
+  if (key == kEmptySlot) return p.gmask + 1;
   uint64_t slot = hash_key(static_cast<int64_t>(key)) & p.gmask;
   for (uint64_t i = 0; i <= p.gmask; ++i) {
-    uint64_t s = *reinterpret_cast<volatile uint64_t*>(keys + slot);
-    if (s == kEmptySlot) {
-      s = atomicCAS(reinterpret_cast<unsigned long long*>(keys + slot), static_cast<unsigned long long>(kEmptySlot),
+    uint64_t s = p.gkeys[slot];
+    if (s == kEmptySlot)
+      s = atomicCAS(reinterpret_cast<unsigned long long*>(p.gkeys + slot), static_cast<unsigned long long>(kEmptySlot),
                     static_cast<unsigned long long>(key));
-      if (s == kEmptySlot) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&p.groups[q]), 1ull);
-        return slot;
-      }
-    }
-    if (s == key) return slot;
+    if (s == kEmptySlot || s == key) return slot;
     slot = (slot + 1) & p.gmask;
   }
   raise_status(p.st, GFPDB_ENOMEM, 120);
   return UINT64_MAX;
 }
 
-__global__ void __launch_bounds__(kSBThreads) sb_fact_kernel(const __grid_constant__ SBFactParams p) {
-  __shared__ int64_t s_tile;
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = static_cast<int64_t>(atomicAdd(p.ticket, 1u));
-    __syncthreads();
-    const int64_t tile = s_tile;
-    __syncthreads();
-    if (tile >= p.n_tiles) break;
-    int part = 0;
-    {
-      int lo = 0, hi = p.n_parts - 1;  // last partition whose first tile <= tile
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) / 2;
-        if (p.tile_base[mid] <= tile) lo = mid;
-        else hi = mid - 1;
-      }
-      part = lo;
+struct SBTile {
+  int64_t start;  // first row within the partition
+  int64_t rows;   // rows in this tile
+  int part;
+};
+
+__device__ __forceinline__ SBTile sb_tile(const SBFactParams& p, int64_t tile, int64_t tile_rows, int* part) {
+  while (*part + 1 < p.n_parts && p.tile_base[*part + 1] <= tile) ++*part;  // tiles only grow
+  SBTile t;
+  t.part = *part;
+  t.start = (tile - p.tile_base[*part]) * tile_rows;
+  const int64_t left = p.part_rows[*part] - t.start;
+  t.rows = left < tile_rows ? left : tile_rows;
+  return t;
+}
+
+// Bytes of dimension d's foreign keys that the bulk copy brings for a tile
+// (a multiple of 16; the last few rows of a partition come by plain loads).
+__device__ __forceinline__ uint32_t sb_seg_bytes(const SBFactParams& p, int d, int64_t rows) {
+  return p.staged ? static_cast<uint32_t>((rows * p.fk_width[d]) & ~int64_t{15}) : 0u;
+}
+
+// Stage 2: one persistent pass over every tile of every partition.
+// Warp kSBConsumerWarps is the producer: one lane streams each tile's
+// foreign-key columns into a kSBStages-deep ring of shared-memory stages
+// with cp.async.bulk, completing on the stage's "full" mbarrier. The other
+// warps consume: each takes 32 * ITEMS rows of the tile (lanes on
+// consecutive rows) and releases the stage on its "empty" mbarrier once it
+// has read its foreign keys, so consumer warps drift apart instead of meeting
+// at a block barrier. A consumer first applies the dimensions staged in
+// shared memory (query masks and group values by key), then issues the
+// lookups of the other dimensions one dimension ahead of their use, so their
+// memory latencies overlap. A row that survives every dimension finds its
+// group once in the table shared by all queries and adds its measures to each
+// of its queries' accumulators. Every wait is bounded: on timeout the kernel
+// records GFPDB_ETIMEDOUT and stops.
+template <int ITEMS>
+__global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_constant__ SBFactParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + kSBStages;
+  unsigned char* stages = smem + kSBBarBytes;
+  unsigned char* staged_dims = smem + p.masks_off;
+  __shared__ int64_t s_kmin[kSBMaxDims];
+  __shared__ uint64_t s_range[kSBMaxDims];
+  __shared__ int32_t s_off[kSBMaxDims];  // staged: byte offset in staged_dims, else -1
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < p.n_dims) {
+    const SBDimDev& D = p.dims[threadIdx.x];
+    const SBDirect dr = sb_direct(D);
+    s_kmin[threadIdx.x] = dr.kmin;
+    s_range[threadIdx.x] = dr.range;
+    s_off[threadIdx.x] =
+        (dr.range != 0 && D.smem_off >= 0 && dr.range <= static_cast<uint64_t>(D.smem_cap)) ? D.smem_off : -1;
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSBStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kSBConsumerWarps);
     }
-    const DevCol* cols = p.part_cols + static_cast<int64_t>(part) * p.n_cols;
-    const int64_t rows = p.part_rows[part];
-    const int64_t row0 = (tile - p.tile_base[part]) * static_cast<int64_t>(kSBThreads) * p.items;
-    for (int it = 0; it < p.items; ++it) {
-      // consecutive threads read consecutive rows: coalesced FK loads
-      const int64_t row = row0 + static_cast<int64_t>(it) * kSBThreads + threadIdx.x;
-      if (row >= rows) break;
-      uint64_t m = p.qvalid;
-      int64_t drow[kSBMaxDims];
-      for (int j = 0; j < p.n_dims && m != 0; ++j) {
+    mbar_fence_init();
+  }
+  __syncthreads();
+  for (int d = 0; d < p.n_dims; ++d) {
+    if (s_off[d] < 0) continue;
+    const SBDimDev& D = p.dims[d];
+    uint64_t* q = reinterpret_cast<uint64_t*>(staged_dims + s_off[d]);
+    for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) q[i] = __ldg(D.dq + i);
+    for (int c = 0; c < D.n_group; ++c) {
+      int32_t* g = reinterpret_cast<int32_t*>(staged_dims + s_off[d] + D.smem_cap * 8 + c * D.smem_cap * 4);
+      for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) g[i] = __ldg(D.dg[c] + i);
+    }
+  }
+  __syncthreads();  // the last block-wide barrier: roles split below
+  constexpr int64_t kTileRows = static_cast<int64_t>(kSBConsumerWarps) * 32 * ITEMS;
+  int part = 0;
+  if (warp == kSBConsumerWarps) {
+    // ---------------------------------------------------------- producer
+    if (lane != 0) return;
+    int64_t k = 0;
+    for (int64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x, ++k) {
+      const int s = static_cast<int>(k % kSBStages);
+      if (k >= kSBStages && !mbar_wait(&empty[s], static_cast<uint32_t>((k / kSBStages - 1) & 1))) {
+        raise_status(p.st, GFPDB_ETIMEDOUT, 130);
+        break;
+      }
+      const SBTile t = sb_tile(p, tile, kTileRows, &part);
+      const DevCol* cols = p.part_cols + static_cast<int64_t>(t.part) * p.n_cols;
+      uint32_t bytes = 0;
+      for (int d = 0; d < p.n_dims; ++d) bytes += sb_seg_bytes(p, d, t.rows);
+      mbar_arrive_expect_tx(&full[s], bytes);
+      for (int d = 0; d < p.n_dims; ++d) {
+        const uint32_t b = sb_seg_bytes(p, d, t.rows);
+        if (b == 0) continue;
+        const unsigned char* src =
+            static_cast<const unsigned char*>(cols[p.fd.fk_col[d]].data) + t.start * p.fk_width[d];
+        bulk_g2s(stages + static_cast<int64_t>(s) * p.stage_bytes + p.seg_off[d], src, b, &full[s]);
+      }
+    }
+    // Copies still in flight land before this CTA exits: wait for the
+    // stages issued last (consumers wait on the same phases).
+    const int64_t issued = k;
+    for (int64_t j = issued > kSBStages ? issued - kSBStages : 0; j < issued; ++j)
+      if (!mbar_wait(&full[j % kSBStages], static_cast<uint32_t>((j / kSBStages) & 1))) {
+        raise_status(p.st, GFPDB_ETIMEDOUT, 131);
+        break;
+      }
+    return;
+  }
+  // ------------------------------------------------------------ consumers
+  const int gd0 = p.fd.n_group > 0 ? p.fd.group_dim[0] : -1;
+  const int gd1 = p.fd.n_group > 1 ? p.fd.group_dim[1] : -1;
+  int64_t k = 0;
+  for (int64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x, ++k) {
+    const int s = static_cast<int>(k % kSBStages);
+    const SBTile t = sb_tile(p, tile, kTileRows, &part);
+    const DevCol* cols = p.part_cols + static_cast<int64_t>(t.part) * p.n_cols;
+    const bool ok = mbar_wait(&full[s], static_cast<uint32_t>((k / kSBStages) & 1));
+    if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform exit
+      if (lane == 0) raise_status(p.st, GFPDB_ETIMEDOUT, 132);
+      break;
+    }
+    const unsigned char* stage = stages + static_cast<int64_t>(s) * p.stage_bytes;
+    const int64_t r0 = static_cast<int64_t>(warp) * 32 * ITEMS + lane;  // row within the tile of item 0
+    // this lane's foreign key of dimension d, item i (stage or, for the
+    // last rows of a partition, global memory)
+    auto fk_of = [&](int d, int i) -> int64_t {
+      const int64_t r = r0 + i * 32;
+      const int64_t in_smem = sb_seg_bytes(p, d, t.rows) / p.fk_width[d];
+      const unsigned char* seg = stage + p.seg_off[d];
+      if (r < in_smem)
+        return p.fk_width[d] == 8 ? reinterpret_cast<const int64_t*>(seg)[r]
+                                  : static_cast<int64_t>(reinterpret_cast<const int32_t*>(seg)[r]);
+      return load_int(cols[p.fd.fk_col[d]], t.start + r);
+    };
+    uint64_t m[ITEMS];
+    uint32_t g0[ITEMS], g1[ITEMS];  // group column values
+    bool any = false;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      m[i] = r0 + i * 32 < t.rows ? p.qvalid : 0ull;
+      any |= m[i] != 0;
+      g0[i] = g1[i] = 0;
+    }
+    // (a) dimensions staged in shared memory, in probe order, early exit
+    for (int j = 0; j < p.n_dims && __any_sync(0xffffffffu, any); ++j) {
+      const int d = p.fd.order[j];
+      const int off = s_off[d];
+      if (off < 0) continue;
+      const uint64_t kmin = static_cast<uint64_t>(s_kmin[d]);
+      const uint64_t range = s_range[d];
+      const uint64_t* sq = reinterpret_cast<const uint64_t*>(staged_dims + off);
+      const int cap = p.dims[d].smem_cap;
+      const int c0 = d == gd0 ? p.fd.group_idx[0] : -1, c1 = d == gd1 ? p.fd.group_idx[1] : -1;
+      any = false;
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        if (m[i] == 0) continue;
+        const uint64_t idx = static_cast<uint64_t>(fk_of(d, i)) - kmin;
+        m[i] &= idx < range ? sq[idx] : 0ull;
+        if (m[i] != 0) {
+          if (c0 >= 0) g0[i] = reinterpret_cast<const uint32_t*>(staged_dims + off + cap * 8 + c0 * cap * 4)[idx];
+          if (c1 >= 0) g1[i] = reinterpret_cast<const uint32_t*>(staged_dims + off + cap * 8 + c1 * cap * 4)[idx];
+        }
+        any |= m[i] != 0;
+      }
+    }
+    // (b) direct dimensions in global memory: each dimension's loads are
+    // issued before the previous dimension's results are applied
+    {
+      uint64_t pq[ITEMS];
+      uint32_t pg0[ITEMS], pg1[ITEMS];
+      bool have = false, pk0 = false, pk1 = false;
+      for (int j = 0; j < p.n_dims && __any_sync(0xffffffffu, any); ++j) {
         const int d = p.fd.order[j];
-        const int64_t r = sb_lookup(p.dims[d], load_int(cols[p.fd.fk_col[d]], row));
-        drow[d] = r;
-        m &= r >= 0 ? __ldg(reinterpret_cast<const unsigned long long*>(p.dims[d].qmask + r)) : 0ull;
+        if (s_off[d] >= 0 || s_range[d] == 0) continue;
+        const SBDimDev& D = p.dims[d];
+        const uint64_t kmin = static_cast<uint64_t>(s_kmin[d]);
+        const uint64_t range = s_range[d];
+        const int c0 = d == gd0 ? p.fd.group_idx[0] : -1, c1 = d == gd1 ? p.fd.group_idx[1] : -1;
+        uint64_t cq[ITEMS];
+        uint32_t cg0[ITEMS], cg1[ITEMS];
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          cq[i] = 0;
+          cg0[i] = cg1[i] = 0;
+          if (m[i] == 0) continue;
+          const uint64_t idx = static_cast<uint64_t>(fk_of(d, i)) - kmin;
+          if (idx < range) {
+            cq[i] = __ldg(reinterpret_cast<const unsigned long long*>(D.dq + idx));
+            if (c0 >= 0) cg0[i] = static_cast<uint32_t>(__ldg(D.dg[c0] + idx));
+            if (c1 >= 0) cg1[i] = static_cast<uint32_t>(__ldg(D.dg[c1] + idx));
+          }
+        }
+        if (have) {
+          any = false;
+#pragma unroll
+          for (int i = 0; i < ITEMS; ++i) {
+            m[i] &= pq[i];
+            if (pk0) g0[i] = pg0[i];
+            if (pk1) g1[i] = pg1[i];
+            any |= m[i] != 0;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          pq[i] = cq[i];
+          pg0[i] = cg0[i];
+          pg1[i] = cg1[i];
+        }
+        pk0 = c0 >= 0;
+        pk1 = c1 >= 0;
+        have = true;
       }
-      if (m == 0) continue;
+      if (have) {
+        any = false;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+          m[i] &= pq[i];
+          if (pk0) g0[i] = pg0[i];
+          if (pk1) g1[i] = pg1[i];
+          any |= m[i] != 0;
+        }
+      }
+    }
+    // (c) dimensions looked up by hash (sparse keys)
+    for (int j = 0; j < p.n_dims && __any_sync(0xffffffffu, any); ++j) {
+      const int d = p.fd.order[j];
+      if (s_range[d] != 0) continue;
+      const SBDimDev& D = p.dims[d];
+      const int c0 = d == gd0 ? p.fd.group_idx[0] : -1, c1 = d == gd1 ? p.fd.group_idx[1] : -1;
+      any = false;
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i) {
+        if (m[i] == 0) continue;
+        const int64_t r = sb_lookup(D, fk_of(d, i));
+        m[i] &= r >= 0 ? __ldg(reinterpret_cast<const unsigned long long*>(D.qmask + r)) : 0ull;
+        if (m[i] != 0) {
+          if (c0 >= 0) g0[i] = static_cast<uint32_t>(load_int(D.group[c0], r));
+          if (c1 >= 0) g1[i] = static_cast<uint32_t>(load_int(D.group[c1], r));
+        }
+        any |= m[i] != 0;
+      }
+    }
+    // Every foreign key this warp needs from the stage has been read.
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    if (!any) continue;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      uint64_t mi = m[i];
+      if (mi == 0) continue;
+      const int64_t row = t.start + r0 + i * 32;
       uint64_t key = 0;
-      if (p.fd.n_group == 1) {
-        const SBDimDev& D = p.dims[p.fd.group_dim[0]];
-        key = static_cast<uint32_t>(load_int(D.group[p.fd.group_idx[0]], drow[p.fd.group_dim[0]]));
-      } else if (p.fd.n_group == 2) {
-        const SBDimDev& A = p.dims[p.fd.group_dim[0]];
-        const SBDimDev& B = p.dims[p.fd.group_dim[1]];
-        const uint32_t a = static_cast<uint32_t>(load_int(A.group[p.fd.group_idx[0]], drow[p.fd.group_dim[0]]));
-        const uint32_t b = static_cast<uint32_t>(load_int(B.group[p.fd.group_idx[1]], drow[p.fd.group_dim[1]]));
-        key = (static_cast<uint64_t>(a) << 32) | b;
-      }
-      unsigned long long vals[kMaxAggs];
+      if (p.fd.n_group == 1) key = g0[i];
+      else if (p.fd.n_group == 2) key = (static_cast<uint64_t>(g0[i]) << 32) | g1[i];
+      unsigned long long vals[kSBMaxAggsFact];
       for (int a = 0; a < p.n_aggs; ++a) {
         const SBAgg& g = p.aggs[a];
         if (g.fn == AGG_COUNT_STAR) {
           vals[a] = 1ull;
         } else {
-          uint64_t v = static_cast<uint64_t>(load_int(cols[g.a], row));
-          if (g.b >= 0) v *= static_cast<uint64_t>(load_int(cols[g.b], row));  // int64 wrap
-          vals[a] = v;
+          uint64_t x = static_cast<uint64_t>(load_int(cols[g.a], row));
+          if (g.b >= 0) x *= static_cast<uint64_t>(load_int(cols[g.b], row));  // int64 wrap
+          vals[a] = x;
         }
       }
-      while (m != 0) {
-        const int q = __ffsll(static_cast<long long>(m)) - 1;
-        m &= m - 1;
-        const uint64_t slot = sb_group_slot(p, q, key);
-        if (slot == UINT64_MAX) continue;
+      const uint64_t slot = sb_group_slot(p, key);
+      if (slot == UINT64_MAX) continue;
+      atomicOr(p.touched + slot, static_cast<unsigned long long>(mi));
+      while (mi != 0) {
+        const int q = __ffsll(static_cast<long long>(mi)) - 1;
+        mi &= mi - 1;
         unsigned long long* acc =
             p.gaccs + (static_cast<uint64_t>(q) * (p.gmask + 2) + slot) * static_cast<uint64_t>(p.n_aggs);
         for (int a = 0; a < p.n_aggs; ++a) atomicAdd(acc + a, vals[a]);
@@ -246,22 +526,23 @@ __global__ void __launch_bounds__(kSBThreads) sb_fact_kernel(const __grid_consta
 
 struct SBFinalParams {
   const uint64_t* gkeys;
+  const unsigned long long* touched;
   const unsigned long long* gaccs;
-  const int64_t* special;
-  uint64_t slots_per_q;  // gcap + 1
+  uint64_t slots;  // gcap + 1
   int32_t n_queries;
   int32_t n_aggs;
   int32_t n_group;
-  int32_t group_type[2];
+  int32_t pad;
   int32_t* out_q;
   void* out_g[2];
   long long* out_a[kMaxAggs];
   unsigned long long* counter;
 };
 
+// Stage 3: every (query, group) with rows becomes one output row.
 __global__ void __launch_bounds__(256) sb_final_kernel(const __grid_constant__ SBFinalParams p) {
   const int lane = threadIdx.x & 31;
-  const uint64_t total = p.slots_per_q * static_cast<uint64_t>(p.n_queries);
+  const uint64_t total = p.slots * static_cast<uint64_t>(p.n_queries);
   const uint64_t w0 = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
   for (uint64_t base = w0 * 32; base < total; base += nw * 32) {
@@ -270,15 +551,10 @@ __global__ void __launch_bounds__(256) sb_final_kernel(const __grid_constant__ S
     uint64_t key = 0;
     int q = 0;
     if (i < total) {
-      q = static_cast<int>(i / p.slots_per_q);
-      const uint64_t s = i % p.slots_per_q;
-      if (s + 1 < p.slots_per_q) {
-        key = p.gkeys[i];
-        live = key != kEmptySlot;
-      } else {
-        key = kEmptySlot;
-        live = p.special[q] != 0;
-      }
+      q = static_cast<int>(i / p.slots);
+      const uint64_t s = i % p.slots;
+      live = ((p.touched[s] >> q) & 1ull) != 0;
+      key = s + 1 < p.slots ? p.gkeys[s] : kEmptySlot;
     }
     const uint32_t bal = __ballot_sync(0xffffffffu, live);
     if (bal == 0) continue;
@@ -290,8 +566,7 @@ __global__ void __launch_bounds__(256) sb_final_kernel(const __grid_constant__ S
     const int64_t pos = static_cast<int64_t>(at) + __popc(bal & ((1u << lane) - 1u));
     p.out_q[pos] = q;
     if (p.n_group == 1) {
-      const int32_t v = static_cast<int32_t>(static_cast<uint32_t>(key));
-      static_cast<int32_t*>(p.out_g[0])[pos] = v;
+      static_cast<int32_t*>(p.out_g[0])[pos] = static_cast<int32_t>(static_cast<uint32_t>(key));
     } else if (p.n_group == 2) {
       static_cast<int32_t*>(p.out_g[0])[pos] = static_cast<int32_t>(static_cast<uint32_t>(key >> 32));
       static_cast<int32_t*>(p.out_g[1])[pos] = static_cast<int32_t>(static_cast<uint32_t>(key));
@@ -318,8 +593,10 @@ struct StarBatchState {
   std::vector<std::string> fact_cols;
   SBDimsParams dims_params;
   SBFactParams fact_params;
-  BufferPtr tables_buf, masks_buf, gkeys_buf, gaccs_buf, misc_buf, meta_buf, out_q;
+  BufferPtr tables_buf, masks_buf, dq_buf, drow_buf, dg_buf, krange_buf, gkeys_buf, touched_buf, gaccs_buf, misc_buf, meta_buf,
+      out_q;
   BufferPtr out_g[2], out_a[kMaxAggs];
+  size_t fact_smem = 0;  // staged query masks, bytes per block
   std::vector<char> host_meta;
   DType group_types[2] = {DType::Int32, DType::Int32};
   uint64_t gcap = 0;
@@ -328,6 +605,7 @@ struct StarBatchState {
 
   void prepare(cudaStream_t s);
   void run(cudaStream_t s);
+  void launch_fact(int grid, cudaStream_t s);
   TupleSetPtr result_view() const;
   const DevStatus* status() const;
 };
@@ -349,8 +627,8 @@ void StarBatchState::prepare(cudaStream_t s) {
   if (spec.queries.empty() || spec.queries.size() > static_cast<size_t>(kSBMaxQueries))
     fail(GFPDB_EUNSUPPORTED, "a batch holds 1 to 64 queries");
   if (spec.group.size() > 2) fail(GFPDB_EUNSUPPORTED, "at most two group columns in a batched star query");
-  if (spec.aggs.empty() || spec.aggs.size() > static_cast<size_t>(kMaxAggs))
-    fail(GFPDB_EUNSUPPORTED, "1 to 8 aggregates in a batched star query");
+  if (spec.aggs.empty() || spec.aggs.size() > static_cast<size_t>(kSBMaxAggsFact))
+    fail(GFPDB_EUNSUPPORTED, "1 to 4 aggregates in a batched star query");
   if (parts.empty() || parts.size() > static_cast<size_t>(kSBMaxParts))
     fail(GFPDB_EUNSUPPORTED, "a batch scans 1 to 256 fact partitions");
   const int nd = static_cast<int>(spec.dims.size());
@@ -375,8 +653,11 @@ void StarBatchState::prepare(cudaStream_t s) {
   const int nc = static_cast<int>(fact_cols.size());
   // partitions: column descriptors and tile ranges
   const int items = spec.items_per_thread;
-  if (items < 1 || items > 64) fail(GFPDB_EINVAL, "itemsPerThread must be in [1, 64]");
-  const int64_t tile_rows = static_cast<int64_t>(kSBThreads) * items;
+  if (items != 1 && items != 2 && items != 4 && items != 8)
+    fail(GFPDB_EINVAL, "itemsPerThread must be 1, 2, 4 or 8");
+  const int64_t tile_rows = static_cast<int64_t>(kSBConsumerWarps) * 32 * items;
+  std::vector<int32_t> fk_width(nd, 0);
+  bool aligned = true;
   std::vector<DevCol> hcols(parts.size() * nc);
   std::vector<int64_t> hbase(parts.size() + 1), hrows(parts.size());
   int64_t tiles = 0;
@@ -390,6 +671,14 @@ void StarBatchState::prepare(cudaStream_t s) {
         fail(GFPDB_EUNSUPPORTED, "batched star fact columns must be integer columns");
       hcols[pi * nc + c] = DevCol{col->data, nullptr, static_cast<int32_t>(col->type), 0};
     }
+    for (int d = 0; d < nd; ++d) {
+      const auto& col = t.column(fact_cols[fk_slot[d]]);
+      const int32_t w = col->type == DType::Int64 ? 8 : 4;
+      if (fk_width[d] != 0 && fk_width[d] != w)
+        fail(GFPDB_EUNSUPPORTED, "batched star partitions must agree on foreign-key column types");
+      fk_width[d] = w;
+      aligned &= reinterpret_cast<uintptr_t>(col->data) % 16 == 0;
+    }
     hbase[pi] = tiles;
     hrows[pi] = t.num_rows();
     tiles += (t.num_rows() + tile_rows - 1) / tile_rows;
@@ -397,6 +686,18 @@ void StarBatchState::prepare(cudaStream_t s) {
   }
   hbase[parts.size()] = tiles;
   n_tiles = tiles;
+  // pipeline stage: the tile's foreign keys of every dimension, one segment each
+  std::memset(&fact_params, 0, sizeof(fact_params));
+  int64_t stage_bytes = 0;
+  for (int d = 0; d < nd; ++d) {
+    fact_params.seg_off[d] = static_cast<int32_t>(stage_bytes);
+    fact_params.fk_width[d] = fk_width[d];
+    stage_bytes += tile_rows * fk_width[d];  // tile_rows is a multiple of 256: segments stay 16-byte aligned
+  }
+  fact_params.staged = aligned ? 1 : 0;
+  fact_params.stage_bytes = static_cast<int32_t>(stage_bytes);
+  const int64_t masks_off = kSBBarBytes + kSBStages * stage_bytes;
+  fact_params.masks_off = static_cast<int32_t>(masks_off);
   // dimensions
   std::memset(&dims_params, 0, sizeof(dims_params));
   int64_t base = 0;
@@ -424,7 +725,6 @@ void StarBatchState::prepare(cudaStream_t s) {
   dims_params.n_queries = nq;
   dims_params.total_rows = base;
   // group columns
-  std::memset(&fact_params, 0, sizeof(fact_params));
   fact_params.fd.n_group = static_cast<int32_t>(spec.group.size());
   for (size_t g = 0; g < spec.group.size(); ++g) {
     const int d = spec.group[g].dim;
@@ -439,9 +739,48 @@ void StarBatchState::prepare(cudaStream_t s) {
     group_types[g] = c->type;
     ++D.n_group;
   }
+  // Shared-memory staging: the smallest dimensions first, one 64-bit mask
+  // per key, within a per-block budget that leaves room for blocks_per_sm
+  // blocks on an SM.
+  std::vector<int> by_rows(nd);
+  for (int d = 0; d < nd; ++d) by_rows[d] = d;
+  std::stable_sort(by_rows.begin(), by_rows.end(),
+                   [&](int a, int b) { return dims_params.dims[a].rows < dims_params.dims[b].rows; });
+  const int64_t block_target = std::min<int64_t>(kSBSmemBudget / std::max(1, spec.blocks_per_sm), kSBSmemPerBlockMax);
+  const int64_t budget = std::max<int64_t>(0, block_target - masks_off);
+  int64_t staged = 0;  // bytes
+  for (int d = 0; d < nd; ++d) dims_params.dims[d].smem_off = -1;
+  for (int d : by_rows) {
+    SBDimDev& D = dims_params.dims[d];
+    const int64_t keys = (D.rows + 7) / 8 * 8;  // a dense key range needs one entry per row
+    const int64_t bytes = keys * (8 + 4 * D.n_group);  // query masks, then each group column
+    if (D.rows == 0 || staged + bytes > budget) continue;
+    D.smem_off = static_cast<int32_t>(staged);
+    D.smem_cap = static_cast<int32_t>(keys);
+    staged += bytes;
+  }
+  fact_smem = static_cast<size_t>(masks_off + staged);
+  if (fact_smem > static_cast<size_t>(kSBSmemMaxDynamic))
+    fail(GFPDB_EUNSUPPORTED, "itemsPerThread needs more shared memory than a block can have for these key widths");
+  // Probe order: as given (a permutation of the dimensions), else the staged
+  // dimensions, then the rest, each by row count.
+  std::vector<int> order;
+  if (!spec.probe_order.empty()) {
+    std::vector<int> seen(nd, 0);
+    if (static_cast<int>(spec.probe_order.size()) != nd) fail(GFPDB_EINVAL, "probeOrder must list every dimension once");
+    for (int d : spec.probe_order) {
+      if (d < 0 || d >= nd || seen[d]++) fail(GFPDB_EINVAL, "probeOrder must list every dimension once");
+      order.push_back(d);
+    }
+  } else {
+    for (int d : by_rows)
+      if (dims_params.dims[d].smem_off >= 0) order.push_back(d);
+    for (int d : by_rows)
+      if (dims_params.dims[d].smem_off < 0) order.push_back(d);
+  }
   for (int d = 0; d < nd; ++d) {
     fact_params.fd.fk_col[d] = fk_slot[d];
-    fact_params.fd.order[d] = d < static_cast<int>(spec.probe_order.size()) ? spec.probe_order[d] : d;
+    fact_params.fd.order[d] = order[d];
   }
   for (size_t a = 0; a < spec.aggs.size(); ++a) {
     fact_params.aggs[a].fn = spec.aggs[a].fn == AGG_COUNT_STAR ? AGG_COUNT_STAR : AGG_SUM;
@@ -458,10 +797,17 @@ void StarBatchState::prepare(cudaStream_t s) {
   const int na = static_cast<int>(spec.aggs.size());
   const int64_t gslots = static_cast<int64_t>(nq) * static_cast<int64_t>(gcap + 1);
   tables_buf = make_buffer(table_words * 8, s);
+  dq_buf = make_buffer(table_words * 8, s);
+  drow_buf = make_buffer(table_words * 4, s);
+  int64_t group_words = 0;
+  for (int d = 0; d < nd; ++d) group_words += static_cast<int64_t>(dims_params.dims[d].mask + 1) * dims_params.dims[d].n_group;
+  dg_buf = make_buffer(std::max<int64_t>(group_words, 1) * 4, s);
+  krange_buf = make_buffer(2 * kSBMaxDims * 8, s);
   masks_buf = make_buffer(std::max<int64_t>(mask_words, 1) * 8, s);
-  gkeys_buf = make_buffer(gslots * 8, s);
+  gkeys_buf = make_buffer(static_cast<int64_t>(gcap) * 8, s);
+  touched_buf = make_buffer(static_cast<int64_t>(gcap + 1) * 8, s);
   gaccs_buf = make_buffer(gslots * 8 * na, s);
-  misc_buf = make_buffer(sizeof(DevStatus) + 64 + 2 * 8 * kSBMaxQueries + 64, s);
+  misc_buf = make_buffer(sizeof(DevStatus) + 64, s);
   meta_buf = make_buffer(static_cast<int64_t>(hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8 +
                                               kSBMaxQueries * kSBMaxDims * 16),
                          s);
@@ -470,11 +816,19 @@ void StarBatchState::prepare(cudaStream_t s) {
   for (size_t g = 0; g < spec.group.size(); ++g) out_g[g] = make_buffer(out_cap * 4, s);
   for (int a = 0; a < na; ++a) out_a[a] = make_buffer(out_cap * 8, s);
   // wire pointers
-  int64_t toff = 0, moff = 0;
+  int64_t toff = 0, moff = 0, goff = 0;
   for (int d = 0; d < nd; ++d) {
     SBDimDev& D = dims_params.dims[d];
     D.slots = tables_buf->as<uint64_t>() + toff;
     D.qmask = masks_buf->as<uint64_t>() + moff;
+    D.dq = dq_buf->as<uint64_t>() + toff;
+    D.drow = drow_buf->as<uint32_t>() + toff;
+    for (int c = 0; c < D.n_group; ++c) {
+      D.dg[c] = dg_buf->as<int32_t>() + goff;
+      goff += static_cast<int64_t>(D.mask + 1);
+    }
+    D.kmin_u = krange_buf->as<unsigned long long>() + d;
+    D.kmax_u = krange_buf->as<unsigned long long>() + kSBMaxDims + d;
     toff += static_cast<int64_t>(D.mask + 1);
     moff += D.rows;
   }
@@ -513,24 +867,67 @@ void StarBatchState::prepare(cudaStream_t s) {
   fact_params.tile_base = dbase;
   fact_params.part_rows = drows;
   fact_params.n_tiles = n_tiles;
-  fact_params.ticket = reinterpret_cast<uint32_t*>(misc + sizeof(DevStatus));
   fact_params.gkeys = gkeys_buf->as<uint64_t>();
   fact_params.gaccs = gaccs_buf->as<unsigned long long>();
   fact_params.gmask = gcap - 1;
-  fact_params.special = reinterpret_cast<int64_t*>(misc + sizeof(DevStatus) + 64);
-  fact_params.groups = fact_params.special + kSBMaxQueries;
+  fact_params.touched = touched_buf->as<unsigned long long>();
   fact_params.st = st;
   for (int d = 0; d < nd; ++d) fact_params.dims[d] = dims_params.dims[d];
-  counter = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus) + 64 + 2 * 8 * kSBMaxQueries);
+  counter = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus));
+}
+
+// Launches with at most as many blocks as are resident at once: tiles are
+// striped over the grid, so a block that had to wait for a free SM would
+// finish its stripe after everyone else.
+template <int ITEMS>
+static void launch_fact_items(const SBFactParams& p, size_t smem, int grid, cudaStream_t s) {
+  // Opt in once to the largest dynamic size this engine asks for (static
+  // plus dynamic shared memory above 48 KB needs it).
+  static bool configured = false;
+  if (!configured) {
+    GF_CUDA(cudaFuncSetAttribute(sb_fact_kernel<ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(kSBSmemMaxDynamic)));
+    configured = true;
+  }
+  int per_sm = 0;
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sb_fact_kernel<ITEMS>, kSBFactThreads, smem));
+  if (per_sm < 1) fail(GFPDB_EUNSUPPORTED, "the batched fact stage does not fit on an SM with these settings");
+  const int resident = per_sm * num_sms();
+  sb_fact_kernel<ITEMS><<<grid < resident ? grid : resident, kSBFactThreads, smem, s>>>(p);
+}
+
+void StarBatchState::launch_fact(int grid, cudaStream_t s) {
+  switch (fact_params.items) {
+    case 1: launch_fact_items<1>(fact_params, fact_smem, grid, s); break;
+    case 2: launch_fact_items<2>(fact_params, fact_smem, grid, s); break;
+    case 4: launch_fact_items<4>(fact_params, fact_smem, grid, s); break;
+    default: launch_fact_items<8>(fact_params, fact_smem, grid, s); break;
+  }
 }
 
 void StarBatchState::run(cudaStream_t s) {
   // clear: join tables to empty, group keys to empty, accumulators / status / counters to zero
   GF_CUDA(cudaMemsetAsync(tables_buf->data(), 0xFF, tables_buf->size(), s));
+  GF_CUDA(cudaMemsetAsync(dq_buf->data(), 0, dq_buf->size(), s));
+  GF_CUDA(cudaMemsetAsync(drow_buf->data(), 0xFF, drow_buf->size(), s));
+  GF_CUDA(cudaMemsetAsync(krange_buf->data(), 0xFF, kSBMaxDims * 8, s));  // minima
+  GF_CUDA(cudaMemsetAsync(krange_buf->as<char>() + kSBMaxDims * 8, 0, kSBMaxDims * 8, s));  // maxima
   GF_CUDA(cudaMemsetAsync(gkeys_buf->data(), 0xFF, gkeys_buf->size(), s));
+  GF_CUDA(cudaMemsetAsync(touched_buf->data(), 0, touched_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(gaccs_buf->data(), 0, gaccs_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(misc_buf->data(), 0, misc_buf->size(), s));
   const int sms = num_sms();
+  {
+    int64_t max_rows = 1;
+    for (int d = 0; d < dims_params.n_dims; ++d) max_rows = std::max<int64_t>(max_rows, dims_params.dims[d].rows);
+    int64_t bx = (max_rows + kSBThreads - 1) / kSBThreads;
+    if (bx > 64) bx = 64;
+    ProfScope prof("sb_range_kernel", s);
+    sb_range_kernel<<<dim3(static_cast<unsigned>(bx), static_cast<unsigned>(dims_params.n_dims)), kSBThreads, 0, s>>>(
+        dims_params);
+    after_launch("sb_range_kernel");
+    prof.stop(static_cast<double>(dims_params.total_rows) * 4.0);
+  }
   {
     int64_t blocks = (dims_params.total_rows + kSBThreads - 1) / kSBThreads;
     if (blocks > sms * 8) blocks = sms * 8;
@@ -544,18 +941,21 @@ void StarBatchState::run(cudaStream_t s) {
     int64_t grid = static_cast<int64_t>(sms) * spec.blocks_per_sm;
     if (grid > n_tiles) grid = n_tiles;
     ProfScope prof("sb_fact_kernel", s);
-    sb_fact_kernel<<<static_cast<int>(grid), kSBThreads, 0, s>>>(fact_params);
+    launch_fact(static_cast<int>(grid), s);
     after_launch("sb_fact_kernel");
-    // algorithmic bytes: every foreign key of every fact row read once
-    prof.stop(static_cast<double>(fact_rows) * 4.0 * static_cast<double>(spec.dims.size()));
+    // algorithmic bytes: every foreign key of every fact row read once (the
+    // measures of the few surviving rows are not counted)
+    double fk_bytes = 0;
+    for (int d = 0; d < fact_params.n_dims; ++d) fk_bytes += fact_params.fk_width[d];
+    prof.stop(static_cast<double>(fact_rows) * fk_bytes);
   }
   {
     SBFinalParams fp;
     std::memset(&fp, 0, sizeof(fp));
     fp.gkeys = gkeys_buf->as<uint64_t>();
+    fp.touched = touched_buf->as<unsigned long long>();
     fp.gaccs = gaccs_buf->as<unsigned long long>();
-    fp.special = fact_params.special;
-    fp.slots_per_q = gcap + 1;
+    fp.slots = gcap + 1;
     fp.n_queries = static_cast<int32_t>(spec.queries.size());
     fp.n_aggs = static_cast<int32_t>(spec.aggs.size());
     fp.n_group = static_cast<int32_t>(spec.group.size());
@@ -563,11 +963,13 @@ void StarBatchState::run(cudaStream_t s) {
     for (size_t g = 0; g < spec.group.size(); ++g) fp.out_g[g] = out_g[g]->data();
     for (size_t a = 0; a < spec.aggs.size(); ++a) fp.out_a[a] = out_a[a]->as<long long>();
     fp.counter = counter;
-    const uint64_t total = fp.slots_per_q * static_cast<uint64_t>(fp.n_queries);
+    const uint64_t total = fp.slots * static_cast<uint64_t>(fp.n_queries);
     int64_t blocks = static_cast<int64_t>((total + 255) / 256);
     if (blocks > sms * 8) blocks = sms * 8;
+    ProfScope prof("sb_final_kernel", s);
     sb_final_kernel<<<static_cast<int>(blocks), 256, 0, s>>>(fp);
     after_launch("sb_final_kernel");
+    prof.stop(static_cast<double>(total) * 8.0 * (1 + fp.n_aggs));
   }
 }
 

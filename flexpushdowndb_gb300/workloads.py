@@ -181,13 +181,16 @@ def star_plan(consts=STAR_DEFAULT_CONSTS, bits_per_key: int = 10, num_hashes: in
 BATCH_FILTER_VALUES = 100
 
 
-def batch_partition_sizes(n_parts: int = 64, lo: int = 50_000, hi: int = 4_000_000, seed: int = 4000) -> list[int]:
+BATCH_SEED = 4106  # 64 partitions of 59,952,713 rows in all
+
+
+def batch_partition_sizes(n_parts: int = 64, lo: int = 50_000, hi: int = 4_000_000, seed: int = BATCH_SEED) -> list[int]:
     """Partition sizes log-uniform in [lo, hi]."""
     u = splitmix64(seed, n_parts).astype(np.float64) / float(2**64)
     return [int(round(np.exp(np.log(lo) + x * (np.log(hi) - np.log(lo))))) for x in u]
 
 
-def batch_tables(n_parts: int = 64, sizes=None, seed: int = 4000) -> dict[str, Table]:
+def batch_tables(n_parts: int = 64, sizes=None, seed: int = BATCH_SEED) -> dict[str, Table]:
     sizes = sizes or batch_partition_sizes(n_parts, seed=seed)
     out = {}
     for i, n in enumerate(STAR_DIM_ROWS, start=1):
@@ -209,9 +212,11 @@ def batch_queries(n_queries: int = 32, seed: int = 4100) -> list[list[tuple[int,
     return [[(0, int(k[q, d]) - 1) for d in range(4)] for q in range(n_queries)]
 
 
-def star_batch_spec(fact_tables, queries, load_factor: float = 0.5, items_per_thread: int = 4,
-                    blocks_per_sm: int = 4, probe_order=(1, 2, 3, 0), groups_hint: int = 256) -> dict:
-    return {
+def star_batch_spec(fact_tables, queries, load_factor: float = 0.5, items_per_thread: int = 2,
+                    blocks_per_sm: int = 4, probe_order=None, groups_hint: int = 256) -> dict:
+    """probe_order None lets the engine order the dimensions (shared-memory
+    staged ones first, then by size)."""
+    spec = {
         "factTables": list(fact_tables),
         "dimensions": [{"table": f"d{i}", "key": f"d{i}_pk", "factKey": f"fk{i}", "filterColumn": f"d{i}_f"}
                        for i in range(1, 5)],
@@ -220,9 +225,11 @@ def star_batch_spec(fact_tables, queries, load_factor: float = 0.5, items_per_th
                        {"function": "SUM", "name": "discount_revenue", "columns": ["price_cents", "discount"]},
                        {"function": "COUNT", "name": "cnt"}],
         "queries": [[list(r) for r in q] for q in queries],
-        "probeOrder": list(probe_order),
         "loadFactor": load_factor,
         "itemsPerThread": items_per_thread,
         "blocksPerSm": blocks_per_sm,
         "groupsHint": groups_hint,
     }
+    if probe_order is not None:
+        spec["probeOrder"] = list(probe_order)
+    return spec

@@ -315,11 +315,15 @@ int32_t gfpdb_graph_cache_clear(void);
  *    "dimensions": [{"table": "d1", "key": "d1_pk", "factKey": "fk1", "filterColumn": "d1_f"}, ...],
  *    "groupBy": [{"dimension": 1, "column": "d2_g"}, ...],          (0 to 2)
  *    "aggregates": [{"function": "SUM", "name": "revenue", "columns": ["price_cents", "qty"]},
- *                   {"function": "COUNT", "name": "cnt"}],
+ *                   {"function": "COUNT", "name": "cnt"}],                  (1 to 4)
  *    "queries": [[[lo, hi], ...one range per dimension...], ...],   (1 to 64)
- *    "probeOrder": [1, 2, 3, 0], "loadFactor": 0.5, "itemsPerThread": 4,
+ *    "probeOrder": [1, 2, 3, 0], "loadFactor": 0.5, "itemsPerThread": 2,
  *    "blocksPerSm": 4, "groupsHint": 1024}
- * The result has a query_id column, then the group columns, then the
+ * probeOrder (optional) lists every dimension once; without it the smallest
+ * dimensions go first. itemsPerThread is 1, 2, 4 or 8. Dimensions with
+ * dense keys (max - min + 1 within the join table's capacity) are looked up
+ * by direct address, the others by hash; the choice is made on the device
+ * each run and never changes results. The result has a query_id column, then the group columns, then the
  * aggregates; each query's rows equal that query's single-query plan
  * (the join / group parts of SmallToLargePredTransOrder.cpp's star plans,
  * HashJoinArrowKernel.cpp and GroupArrowKernel.cpp semantics). */

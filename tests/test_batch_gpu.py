@@ -44,7 +44,7 @@ def test_batch_equals_single_query_plans(gpu):
 
 
 @pytest.mark.parametrize("items,blocks,lf,order", [(1, 1, 0.25, (0, 1, 2, 3)), (8, 8, 0.9, (3, 2, 1, 0)),
-                                                   (16, 2, 0.5, (1, 2, 3, 0))])
+                                                   (2, 2, 0.5, (1, 2, 3, 0)), (4, 3, 0.5, None)])
 def test_batch_tuning_knobs_keep_results(gpu, items, blocks, lf, order):
     tabs, parts, qs = small_batch(n_parts=3, n_queries=6, seed=4020)
     dev = device(tabs)
@@ -71,3 +71,82 @@ def test_batch_rejects_repeated_dimension_keys(gpu):
     with pytest.raises(GfpdbError) as ei:
         batch.star_batch(workloads.star_batch_spec(parts, qs), device(tabs))
     assert "repeats a key" in ei.value.message
+
+
+def _rekey(tabs, parts, scale, offset, dtype):
+    """Dimension keys k -> k * scale + offset (and the foreign keys with
+    them): sparse key ranges take the hash-table lookup path."""
+    out = dict(tabs)
+    for i in range(1, 5):
+        d = tabs[f"d{i}"]
+        out[f"d{i}"] = Table([Column(c.name, dtype if c.name.endswith("_pk") else c.type,
+                                     c.values.astype(np.int64) * scale + offset if c.name.endswith("_pk") else c.values)
+                              for c in d.columns])
+    for p in parts:
+        t = tabs[p]
+        out[p] = Table([Column(c.name, dtype if c.name.startswith("fk") else c.type,
+                               c.values.astype(np.int64) * scale + offset if c.name.startswith("fk") else c.values)
+                        for c in t.columns])
+    return out
+
+
+@pytest.mark.parametrize("scale,offset,dtype", [(7919, -5_000_000, "int32"), (1 << 33, -(1 << 40), "int64"),
+                                                (1, -(1 << 31) + 10, "int32")])
+def test_batch_sparse_and_negative_keys(gpu, scale, offset, dtype):
+    tabs, parts, qs = small_batch(n_parts=3, n_queries=6, seed=4050)
+    tabs = _rekey(tabs, parts, scale, offset, dtype)
+    got = batch.split_by_query(batch.star_batch(workloads.star_batch_spec(parts, qs), device(tabs)).table)
+    for q, ranges in enumerate(qs):
+        assert got.get(q, []) == queries.star_query_ranges(tabs, parts, ranges).sorted_rows(), f"query {q}"
+
+
+@pytest.mark.parametrize("order", [(0, 1, 2), (0, 1, 2, 2), (0, 1, 2, 4)])
+def test_batch_rejects_bad_probe_order(gpu, order):
+    tabs, parts, qs = small_batch(n_parts=2, n_queries=2, seed=4060)
+    with pytest.raises(GfpdbError) as ei:
+        batch.star_batch(workloads.star_batch_spec(parts, qs, probe_order=order), device(tabs))
+    assert "probeOrder" in ei.value.message
+
+
+def test_batch_rejects_bad_items_per_thread(gpu):
+    tabs, parts, qs = small_batch(n_parts=2, n_queries=2, seed=4070)
+    with pytest.raises(GfpdbError) as ei:
+        batch.star_batch(workloads.star_batch_spec(parts, qs, items_per_thread=16), device(tabs))
+    assert "itemsPerThread" in ei.value.message
+
+
+def test_batch_tiny_and_empty_partitions(gpu):
+    """Partitions shorter than one 16-byte copy, empty ones, and tails that
+    are not a multiple of 4 rows."""
+    sizes = [0, 1, 3, 5, 0, 2049, 70_001, 2]
+    tabs = workloads.batch_tables(len(sizes), sizes=sizes, seed=4080)
+    parts = [f"p{i}" for i in range(len(sizes))]
+    qs = workloads.batch_queries(5, seed=4081) + [[(0, 99)] * 4]
+    for items in (1, 8):
+        spec = workloads.star_batch_spec(parts, qs, items_per_thread=items)
+        got = batch.split_by_query(batch.star_batch(spec, device(tabs)).table)
+        for q, ranges in enumerate(qs):
+            assert got.get(q, []) == queries.star_query_ranges(tabs, parts, ranges).sorted_rows(), f"query {q}"
+
+
+def test_batch_unaligned_columns(gpu):
+    """Foreign-key columns that do not start on a 16-byte boundary are read
+    with plain loads instead of bulk copies; results are the same."""
+    import torch
+
+    tabs, parts, qs = small_batch(n_parts=3, n_queries=4, seed=4090)
+    dev = {k: DeviceTable.from_host(v) for k, v in tabs.items()}
+    for p in parts:
+        dt = dev[p]
+        shifted = []
+        for ts in dt.tensors:
+            views = []
+            for t in ts:
+                buf = torch.empty(t.numel() + 1, dtype=t.dtype, device=t.device)
+                buf[1:] = t
+                views.append(buf[1:])
+            shifted.append(views)
+        dev[p] = DeviceTable(dt.names, dt.types, shifted, dt.num_rows)
+    got = batch.split_by_query(batch.star_batch(workloads.star_batch_spec(parts, qs), plan.PreparedInputs(dev)).table)
+    for q, ranges in enumerate(qs):
+        assert got.get(q, []) == queries.star_query_ranges(tabs, parts, ranges).sorted_rows(), f"query {q}"
