@@ -245,7 +245,9 @@ def run_case(args):
     JSON line with the case's own timing. `select`: the forward bloom probe of
     the star query (fk2 against the 1/25 dim filter) over the 6M-row fact
     table, as one BloomFilterUsePOp runs it; `select4`: all four forward
-    probes fused in one pass."""
+    probes fused in one pass; `batch`: the batched star query (32 variants)
+    over the first --parts partitions of the batched workload, stages launched
+    without a graph."""
     import torch
 
     from flexpushdowndb_gb300 import ops, workloads
@@ -254,6 +256,16 @@ def run_case(args):
     from oracle import ops as oops
 
     ops.init(0)
+    if args.case == "batch":
+        from flexpushdowndb_gb300 import batch, plan
+
+        tabs = workloads.batch_tables(args.parts)
+        parts = [f"p{i}" for i in range(args.parts)]
+        dev = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
+        spec = workloads.star_batch_spec(parts, workloads.batch_queries(32))
+        fn = lambda: batch.star_batch(spec, dev, use_graph=False).table  # noqa: E731
+        args.rows = sum(tabs[p].num_rows for p in parts)
+        return _time_case(args, fn)
     tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
     fact = DeviceTable.from_host(tabs["fact"])
     if args.case in ("plan", "plan-graph"):
@@ -277,6 +289,12 @@ def run_case(args):
         fn = lambda: ops.select(fact, blooms=blooms)  # noqa: E731
     else:
         raise SystemExit(f"unknown case {args.case}")
+    return _time_case(args, fn)
+
+
+def _time_case(args, fn):
+    import torch
+
     for _ in range(args.warmup):
         fn()
     torch.cuda.synchronize()
@@ -296,7 +314,8 @@ def main():
     ap.add_argument("--impl", default="gfpdb", choices=["gfpdb", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph")
+    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | batch")
+    ap.add_argument("--parts", type=int, default=64, help="fact partitions of the batch case")
     ap.add_argument("--rows", type=int, default=FACT_ROWS)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form section")
     args = ap.parse_args()

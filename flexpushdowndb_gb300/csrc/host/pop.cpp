@@ -54,6 +54,7 @@ void POpContext::tell(Message msg) { tell(std::move(msg), op_->consumers()); }
 
 void POpContext::tell(Message msg, const std::vector<std::string>& consumers) {
   msg.sender = op_->name();
+  exec_->stamp(msg, op_);
   for (auto& c : consumers) exec_->post(c, msg);
 }
 
@@ -71,7 +72,7 @@ void POpContext::notifyError(const std::string& error) { exec_->error(op_->name(
 
 LocalPOpDirectory& POpContext::operatorMap() { return op_->directory(); }
 
-cudaStream_t POpContext::stream() const { return exec_->stream(); }
+cudaStream_t POpContext::stream() const { return exec_->streamOf(op_); }
 
 // ------------------------------------------------------------------ ops
 
@@ -492,6 +493,104 @@ const InputTable& Execution::input(const std::string& name) const {
 
 void Execution::post(const std::string& to, Message msg) { mailbox_.emplace_back(to, std::move(msg)); }
 
+namespace {
+
+// This thread's secondary streams and events for the current device, created
+// on first use and kept (creating them is not free, and a graph capture must
+// not be the first to need one).
+struct StreamPool {
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;
+};
+
+StreamPool& stream_pool() {
+  thread_local std::map<int, StreamPool> pools;
+  int dev = 0;
+  GF_CUDA(cudaGetDevice(&dev));
+  return pools[dev];
+}
+
+cudaStream_t pooled_stream(size_t i) {
+  StreamPool& p = stream_pool();
+  while (p.streams.size() <= i) {
+    cudaStream_t s = nullptr;
+    GF_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    p.streams.push_back(s);
+  }
+  return p.streams[i];
+}
+
+cudaEvent_t pooled_event(size_t i) {
+  StreamPool& p = stream_pool();
+  while (p.events.size() <= i) {
+    cudaEvent_t e = nullptr;
+    GF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    p.events.push_back(e);
+  }
+  return p.events[i];
+}
+
+}  // namespace
+
+Execution::~Execution() = default;
+
+// Streams by position in the plan: an operator continues its first producer's
+// stream unless another consumer of that producer already did; roots and
+// branches take the next stream in turn.
+void Execution::assignStreams() {
+  streams_.assign(1, stream_);
+  op_stream_.clear();
+  if (n_streams_ <= 1) {
+    for (auto& o : ops_) op_stream_[o.get()] = 0;
+    return;
+  }
+  for (int i = 1; i < n_streams_; ++i) streams_.push_back(pooled_stream(static_cast<size_t>(i - 1)));
+  // topological order over producers
+  std::map<std::string, int> indeg;
+  for (auto& o : ops_) indeg[o->name()] = static_cast<int>(o->producers().size());
+  std::deque<PhysicalOp*> ready;
+  for (auto& o : ops_)
+    if (o->producers().empty()) ready.push_back(o.get());
+  std::set<const PhysicalOp*> continued;  // producers whose stream a consumer took
+  int next = 0;
+  auto fresh = [&]() { return next++ % n_streams_; };
+  std::set<std::string> seen;
+  while (!ready.empty()) {
+    PhysicalOp* o = ready.front();
+    ready.pop_front();
+    if (!seen.insert(o->name()).second) continue;
+    int st = -1;
+    for (auto& pn : o->producers()) {
+      const PhysicalOp* p = op(pn);
+      if (!continued.count(p)) {
+        continued.insert(p);
+        st = op_stream_[p];
+        break;
+      }
+    }
+    op_stream_[o] = st >= 0 ? st : fresh();
+    for (auto& cn : o->consumers())
+      if (--indeg[cn] == 0) ready.push_back(op(cn));
+  }
+  for (auto& o : ops_)
+    if (!op_stream_.count(o.get())) op_stream_[o.get()] = 0;  // not reached (cycles): the caller's stream
+}
+
+cudaStream_t Execution::streamOf(const PhysicalOp* op) const {
+  auto it = op_stream_.find(op);
+  return it == op_stream_.end() || streams_.empty() ? stream_ : streams_[it->second];
+}
+
+void Execution::stamp(Message& msg, const PhysicalOp* sender) {
+  if (streams_.size() <= 1) return;
+  auto it = op_stream_.find(sender);
+  msg.stream = it == op_stream_.end() ? 0 : it->second;
+  msg.ready = pooled_event(events_used_++);
+  GF_CUDA(cudaEventRecord(msg.ready, streams_[msg.stream]));
+  if (msg.tuples) retained_tuples_.push_back(msg.tuples);
+  if (msg.bloom) retained_blooms_.push_back(msg.bloom);
+}
+
 void Execution::markComplete(const std::string&) {}
 
 void Execution::error(const std::string& from, const std::string& msg) {
@@ -501,6 +600,34 @@ void Execution::error(const std::string& from, const std::string& msg) {
 TupleSetPtr Execution::execute() {
   const uint64_t launches0 = g_kernel_launches.load();
   const CopyCounters c0 = copy_counters();
+  assignStreams();
+  events_used_ = 0;
+  // Fork: every secondary stream starts after the work already on the
+  // caller's stream (and, under capture, joins the capture).
+  if (streams_.size() > 1) {
+    cudaEvent_t fork = pooled_event(events_used_++);
+    GF_CUDA(cudaEventRecord(fork, stream_));
+    for (size_t i = 1; i < streams_.size(); ++i) GF_CUDA(cudaStreamWaitEvent(streams_[i], fork, 0));
+  }
+  // Join: the caller's stream waits for every secondary stream, on every
+  // exit path (a capture cannot end with unjoined streams).
+  struct JoinGuard {
+    Execution* e;
+    ~JoinGuard() {
+      for (size_t i = 1; i < e->streams_.size(); ++i) {
+        cudaEvent_t j = nullptr;
+        try {
+          j = pooled_event(e->events_used_++);
+        } catch (...) {
+          return;
+        }
+        (void)cudaEventRecord(j, e->streams_[i]);
+        (void)cudaStreamWaitEvent(e->stream_, j, 0);
+      }
+    }
+  };
+  std::optional<JoinGuard> join_guard;
+  join_guard.emplace(JoinGuard{this});
   for (auto& o : ops_) {
     Message start;
     start.type = MessageType::START;
@@ -519,6 +646,10 @@ TupleSetPtr Execution::execute() {
     PhysicalOp* dst = op(to);
     if (dst->ctx()->isComplete()) continue;
     ++stats_.messages;
+    if (msg.ready != nullptr) {
+      const int ds = op_stream_.count(dst) ? op_stream_[dst] : 0;
+      if (ds != msg.stream) GF_CUDA(cudaStreamWaitEvent(streams_[ds], msg.ready, 0));
+    }
     if (msg.type == MessageType::COMPLETE) dst->directory().setComplete(msg.sender);
     try {
       dst->onReceive(Envelope{msg});
@@ -530,6 +661,7 @@ TupleSetPtr Execution::execute() {
     }
   }
   set_deferred_mode(false);
+  join_guard.reset();  // join the streams before anything waits on the caller's stream
   if (!error_.empty()) {
     clear_deferred_checks();
     fail(code, error_);
@@ -729,6 +861,9 @@ std::unique_ptr<Execution> build_execution(const json::Value& plan_in, cudaStrea
       }
   }
   ex->connect();
+  const int64_t streams = plan.get_int("streams", kDefaultPlanStreams);
+  if (streams < 1 || streams > 16) fail(GFPDB_EINVAL, "\"streams\" must be in [1, 16]");
+  ex->setStreams(static_cast<int>(streams));
   return ex;
 }
 

@@ -17,12 +17,18 @@
 // The CAF actor runtime (one actor per operator, serial mailboxes,
 // fpdb-executor/src/physical/POpActor.cpp:25-135) is replaced by one host
 // thread delivering messages in FIFO order while every operator enqueues its
-// device work on the execution's CUDA stream.
+// device work on its own CUDA stream. Operators on independent branches of
+// the plan (the dimension pipelines of a star query) get different streams,
+// so their kernels run concurrently; a message carries an event recorded on
+// its sender's stream, which the receiver's stream waits for. Under graph
+// capture the streams fork from and join back to the caller's stream, so the
+// captured graph has the plan's branches as parallel branches.
 #pragma once
 
 #include <deque>
 #include <map>
 #include <memory>
+#include <optional>
 #include <set>
 #include <string>
 #include <vector>
@@ -43,6 +49,8 @@ struct Message {
   TupleSetPtr tuples;   // TUPLESET
   BloomPtr bloom;       // BLOOM_FILTER
   std::string error;    // ERROR
+  cudaEvent_t ready = nullptr;  // recorded on the sender's stream after its work for this message
+  int stream = 0;               // the sender's stream index
 };
 
 // The reference wraps a message in an Envelope; here the envelope is the
@@ -73,6 +81,9 @@ class LocalPOpDirectory {
 
 class Execution;
 class PhysicalOp;
+
+// Streams a plan runs on unless its "streams" option says otherwise.
+constexpr int kDefaultPlanStreams = 4;
 
 class POpContext {
  public:
@@ -172,8 +183,24 @@ class Execution {
   cudaStream_t stream() const { return stream_; }
   ExecStats stats() const { return stats_; }
 
+  // Up to n streams (the caller's plus n - 1 of this thread's pool); 1 runs
+  // every operator on the caller's stream. Call before execute().
+  void setStreams(int n) { n_streams_ = n < 1 ? 1 : n; }
+  int streamCount() const { return static_cast<int>(streams_.size()); }
+  cudaStream_t streamOf(const PhysicalOp* op) const;
+  // Stamps an outgoing message with its sender's stream and ready event.
+  void stamp(Message& msg, const PhysicalOp* sender);
+  ~Execution();
+
  private:
+  void assignStreams();
   cudaStream_t stream_;
+  int n_streams_ = 1;
+  std::vector<cudaStream_t> streams_;           // [0] is the caller's stream
+  std::map<const PhysicalOp*, int> op_stream_;
+  size_t events_used_ = 0;  // of this thread's event pool, in this execution
+  std::vector<TupleSetPtr> retained_tuples_;   // message payloads, kept until the plan has finished
+  std::vector<BloomPtr> retained_blooms_;
   std::vector<std::unique_ptr<PhysicalOp>> ops_;
   std::map<std::string, PhysicalOp*> by_name_;
   std::deque<std::pair<std::string, Message>> mailbox_;

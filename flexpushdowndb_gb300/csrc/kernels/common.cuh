@@ -211,4 +211,41 @@ __device__ __forceinline__ int block_exclusive_sum(int x, int* total, int* s_war
   return r;
 }
 
+// Barrier over the first THREADS threads of the block only (named barrier
+// BAR_ID), for warp-specialised kernels whose other warps never join.
+template <int BAR_ID, int THREADS>
+__device__ __forceinline__ void named_sync() {
+  asm volatile("bar.sync %0, %1;" ::"n"(BAR_ID), "n"(THREADS) : "memory");
+}
+
+// block_exclusive_sum over threads [0, THREADS) synchronised by named
+// barrier BAR_ID.
+template <int BAR_ID, int THREADS>
+__device__ __forceinline__ int named_exclusive_sum(int x, int* total, int* s_warp) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int NW = THREADS / 32;
+  int incl = x;
+  for (int d = 1; d < 32; d <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  named_sync<BAR_ID, THREADS>();
+  if (warp == 0) {
+    int w = lane < NW ? s_warp[lane] : 0;
+    int wi = w;
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += y;
+    }
+    if (lane < NW) s_warp[lane] = wi - w;
+    if (lane == NW - 1) s_warp[NW] = wi;
+  }
+  named_sync<BAR_ID, THREADS>();
+  int r = incl - x + s_warp[warp];
+  *total = s_warp[NW];
+  return r;
+}
+
 }  // namespace gfpdb

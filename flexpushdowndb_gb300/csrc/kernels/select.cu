@@ -19,6 +19,7 @@
 // loads, so a sparse tile only touches the sectors holding selected rows.
 // Small bloom filters are staged in shared memory once per CTA. Inputs whose
 // row count lives on the device (deferred sizes) are read with that count.
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -360,6 +361,344 @@ int select_blocks_per_sm(bool with_pred, size_t dyn) {
   return per_sm;
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined probe-only selection (the BloomFilterUse chain over a large
+// input), in two passes. select_kernel takes a tile, then loads each probe's
+// key column only for the rows still alive, so a chain of k probes costs k
+// dependent DRAM round trips per tile behind block barriers, and its
+// single-pass ranking makes each tile wait for its predecessors.
+// Pass 1 (select_probe_kernel): one producer warp claims tiles and streams
+// the first probe's key column for the tile into a kSpStages-deep ring of
+// shared-memory stages with cp.async.bulk; the eight consumer warps run the
+// first probe over every row (filter staged in shared memory), compact the
+// survivors into per-warp row lists, run the later probes over the lists only
+// (their keys read directly for the survivors), and write the tile's
+// selected row ids, in order, to the tile's own slice of a row-id buffer plus
+// the tile's count. No tile waits for another.
+// Pass 2 (select_gather_kernel): each CTA sums the counts before its range of
+// tiles and moves each tile's selected rows of every projected column to
+// their output offsets.
+// Output order is input order, as in the single-pass kernel. All waits are
+// bounded; on timeout the call reports GFPDB_ETIMEDOUT.
+constexpr int kSpConsumerWarps = 8;
+constexpr int kSpConsumers = kSpConsumerWarps * 32;  // == kSelThreads: one 8-row group per consumer
+constexpr int kSpThreads = kSpConsumers + 32;
+constexpr int kSpStages = 4;
+constexpr int kSpHeader = 128;  // full[S], empty[S] mbarriers, then the tile of each stage
+constexpr int64_t kSpMaxDynamic = 200 * 1024;
+constexpr int64_t kSpMinRows = int64_t{1} << 20;  // below this the simple kernel's tiles all start at once
+
+static_assert(kSpConsumers == kSelThreads, "the pipelined select keeps select_kernel's tile shape");
+
+struct SpLayout {
+  int32_t key_width[kMaxBlooms];  // 4 or 8
+  int32_t stage_bytes;            // the first probe's keys of one tile
+  int32_t bloom_off;              // byte offset of the staged filter in dynamic shared memory
+};
+
+__device__ __forceinline__ uint32_t sp_seg_bytes(const SpLayout& L, int pi, int64_t rows) {
+  return static_cast<uint32_t>((rows * L.key_width[pi]) & ~int64_t{15});
+}
+
+__global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_constant__ SelectParams p,
+                                                                  const __grid_constant__ SpLayout L) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + kSpStages;
+  int64_t* stage_tile = reinterpret_cast<int64_t*>(smem + 64);
+  unsigned char* stages = smem + kSpHeader;
+  uint32_t* s_bloom = reinterpret_cast<uint32_t*>(smem + L.bloom_off);
+  __shared__ int s_wcount[kSpConsumerWarps];
+  __shared__ uint16_t s_list[kSpConsumers * kSelItems];  // per warp: surviving rows of its 256
+  __shared__ uint32_t s_nblocks[kMaxBlooms];
+  __shared__ int s_abort;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
+  const int64_t n_tiles = (n_rows + kSelTile - 1) / kSelTile;
+
+  uint32_t staged = 0, valid = 0;
+#pragma unroll 1
+  for (int pi = 0; pi < p.n_probes; ++pi) {
+    const BloomDev& b = p.probes[pi];
+    const uint32_t nb = b.nblocks_dev ? static_cast<uint32_t>(*b.nblocks_dev) : b.num_blocks;
+    if (threadIdx.x == 0) s_nblocks[pi] = nb;
+    const bool v = b.valid_dev ? (*b.valid_dev != 0) : (b.valid != 0);
+    if (v) valid |= 1u << pi;
+    if (v && b.smem_word >= 0 && nb * 8 <= static_cast<uint32_t>(b.smem_cap_words)) {
+      staged |= 1u << pi;
+      const uint4* src = reinterpret_cast<const uint4*>(b.blocks);
+      uint4* dst = reinterpret_cast<uint4*>(s_bloom + b.smem_word);
+      for (uint32_t i = threadIdx.x; i < nb * 2; i += kSpThreads) dst[i] = __ldg(src + i);
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSpStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kSpConsumerWarps);
+    }
+    mbar_fence_init();
+    s_abort = 0;
+  }
+  __syncthreads();  // the last block-wide barrier: roles split below
+
+  if (warp == kSpConsumerWarps) {
+    // ------------------------------------------------------------ producer
+    if (lane != 0) return;
+    int64_t k = 0;
+    for (;; ++k) {
+      const int s = static_cast<int>(k % kSpStages);
+      if (k >= kSpStages && !mbar_wait(&empty[s], static_cast<uint32_t>((k / kSpStages - 1) & 1))) {
+        raise_status(p.status, GFPDB_ETIMEDOUT, 140);
+        break;
+      }
+      const int64_t tile = static_cast<int64_t>(atomicAdd(p.ticket, 1u));
+      if (tile >= n_tiles) {
+        stage_tile[s] = -1;  // end of input: published by the arrive (release)
+        mbar_arrive(&full[s]);
+        ++k;
+        break;
+      }
+      stage_tile[s] = tile;
+      const int64_t start = tile * kSelTile;
+      const int64_t left = n_rows - start;
+      const int64_t rows = left < kSelTile ? left : kSelTile;
+      // only the first probe's keys: it runs on every row; later probes
+      // read the keys of the few survivors directly
+      const uint32_t bytes = sp_seg_bytes(L, 0, rows);
+      mbar_arrive_expect_tx(&full[s], bytes);
+      if (bytes != 0) {
+        const unsigned char* src =
+            static_cast<const unsigned char*>(p.cols[p.probes[0].col].data) + start * L.key_width[0];
+        bulk_g2s(stages + static_cast<int64_t>(s) * L.stage_bytes, src, bytes, &full[s]);
+      }
+    }
+    // Copies still in flight land before this CTA exits.
+    for (int64_t j = k > kSpStages ? k - kSpStages : 0; j < k; ++j)
+      if (!mbar_wait(&full[j % kSpStages], static_cast<uint32_t>((j / kSpStages) & 1))) {
+        raise_status(p.status, GFPDB_ETIMEDOUT, 141);
+        break;
+      }
+    return;
+  }
+
+  // -------------------------------------------------------------- consumers
+  for (int64_t k = 0;; ++k) {
+    const int s = static_cast<int>(k % kSpStages);
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[s], static_cast<uint32_t>((k / kSpStages) & 1)));
+    if (!ok && lane == 0) {
+      raise_status(p.status, GFPDB_ETIMEDOUT, 142);
+      s_abort = 1;
+    }
+    named_sync<1, kSpConsumers>();  // every consumer warp leaves together
+    if (s_abort != 0) break;
+    const int64_t tile = stage_tile[s];
+    if (tile < 0) break;
+    const int64_t start = tile * kSelTile;
+    const int64_t tile_rows = n_rows - start < kSelTile ? n_rows - start : kSelTile;
+    const int r_in = threadIdx.x * kSelItems;  // first row of this thread within the tile
+    const int64_t row0 = start + r_in;
+    const bool full_rows = r_in + kSelItems <= tile_rows;
+    uint32_t mask;
+    if (full_rows) {
+      mask = 0xFFu;
+    } else {
+      const int64_t rem = tile_rows - r_in;
+      mask = rem <= 0 ? 0u : ((1u << rem) - 1u);
+    }
+    const unsigned char* stage = stages + static_cast<int64_t>(s) * L.stage_bytes;
+    // key of probe pi for row r of the tile: the stage, or global memory for
+    // the last rows of the input that the 16-byte copy left out
+    auto key_at = [&](int pi, int r) -> int64_t {
+      if (pi == 0) {
+        const int w = L.key_width[0];
+        if (r < static_cast<int64_t>(sp_seg_bytes(L, 0, tile_rows) / w))
+          return w == 8 ? reinterpret_cast<const int64_t*>(stage)[r]
+                        : static_cast<int64_t>(reinterpret_cast<const int32_t*>(stage)[r]);
+      }
+      return load_int(p.cols[p.probes[pi].col], start + r);
+    };
+    auto probe_hit = [&](int pi, int64_t key) -> bool {
+      const BloomDev& b = p.probes[pi];
+      const uint64_t h = hash_key(key);
+      const uint32_t blk = bloom_block_of(h, s_nblocks[pi]);
+      if ((staged >> pi) & 1u) return bloom_test(s_bloom + b.smem_word + blk * 8, h, b.num_hashes);
+      const uint4* words = reinterpret_cast<const uint4*>(b.blocks + static_cast<uint64_t>(blk) * 8);
+      uint32_t wv[8];
+      const uint4 lo = __ldg(words);
+      const uint4 hi = __ldg(words + 1);
+      wv[0] = lo.x; wv[1] = lo.y; wv[2] = lo.z; wv[3] = lo.w;
+      wv[4] = hi.x; wv[5] = hi.y; wv[6] = hi.z; wv[7] = hi.w;
+      return bloom_test(wv, h, b.num_hashes);
+    };
+    // (1) the first probe (keys in the stage) over this thread's 8 rows
+    const int first = 0;
+    if ((valid & 1u) && mask != 0) {
+      const int w = L.key_width[0];
+      const int64_t in_smem = sp_seg_bytes(L, 0, tile_rows) / w;
+      const unsigned char* seg = stage;
+      int64_t keys[8];
+      if (r_in + kSelItems <= in_smem) {
+        if (w == 8) {
+          const longlong2* q = reinterpret_cast<const longlong2*>(seg) + r_in / 2;
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const longlong2 a = q[h];
+            keys[2 * h] = a.x;
+            keys[2 * h + 1] = a.y;
+          }
+        } else {
+          const int4* q = reinterpret_cast<const int4*>(seg) + r_in / 4;
+          const int4 a = q[0], c = q[1];
+          keys[0] = a.x; keys[1] = a.y; keys[2] = a.z; keys[3] = a.w;
+          keys[4] = c.x; keys[5] = c.y; keys[6] = c.z; keys[7] = c.w;
+        }
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < kSelItems; ++kk) keys[kk] = (mask >> kk) & 1u ? key_at(first, r_in + kk) : 0;
+      }
+      uint32_t keep = 0;
+#pragma unroll
+      for (int kk = 0; kk < kSelItems; ++kk)
+        if ((mask >> kk) & 1u) keep |= static_cast<uint32_t>(probe_hit(first, keys[kk])) << kk;
+      mask &= keep;
+    }
+    // (2) the survivors, in row order, into this warp's list
+    uint16_t* list = s_list + warp * 32 * kSelItems;
+    int n_alive;
+    {
+      const int c = __popc(mask);
+      int incl = c;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+      }
+      n_alive = __shfl_sync(0xffffffffu, incl, 31);
+      int o = incl - c;
+#pragma unroll
+      for (int kk = 0; kk < kSelItems; ++kk)
+        if ((mask >> kk) & 1u) list[o++] = static_cast<uint16_t>(r_in + kk);
+      __syncwarp();
+    }
+    // (3) the later probes over the list only: a lane loads all of its
+    // survivor's later keys at once (one memory round trip), tests them in
+    // probe order, and the list is compacted in place
+    if (p.n_probes > 1 && n_alive > 0) {
+      int m = 0;
+      for (int base = 0; base < n_alive; base += 32) {
+        const int idx = base + lane;
+        bool alive = idx < n_alive;
+        const int r = alive ? list[idx] : 0;
+        int64_t later[kMaxBlooms - 1];
+#pragma unroll
+        for (int j = 0; j < kMaxBlooms - 1; ++j) {
+          const int pi = j + 1;
+          later[j] = (alive && pi < p.n_probes && ((valid >> pi) & 1u))
+                         ? load_int(p.cols[p.probes[pi].col], start + r) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxBlooms - 1; ++j) {
+          const int pi = j + 1;
+          if (alive && pi < p.n_probes && ((valid >> pi) & 1u)) alive = probe_hit(pi, later[j]);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, alive);
+        __syncwarp();  // every lane has read its entry before any is overwritten
+        if (alive) list[m + __popc(bal & ((1u << lane) - 1u))] = static_cast<uint16_t>(r);
+        m += __popc(bal);
+        __syncwarp();
+      }
+      n_alive = m;
+    }
+    // The stage's keys are consumed: hand it back to the producer.
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(&empty[s]);
+      s_wcount[warp] = n_alive;
+    }
+    // (4) warp offsets within the tile, then the row ids in order
+    named_sync<1, kSpConsumers>();
+    int woff = 0, tile_total = 0;
+#pragma unroll
+    for (int w = 0; w < kSpConsumerWarps; ++w) {
+      const int c = s_wcount[w];
+      woff += w < warp ? c : 0;
+      tile_total += c;
+    }
+    int32_t* dst = p.out_rowids + start + woff;
+    for (int i = lane; i < n_alive; i += 32) dst[i] = static_cast<int32_t>(start + list[i]);
+    if (threadIdx.x == 0) p.tile_status[tile] = static_cast<uint64_t>(tile_total);
+  }
+}
+
+// Pass 2: each CTA takes a contiguous range of at most kSelThreads tiles,
+// sums the counts of the tiles before it, scans its own tiles' counts, then
+// moves every selected row of its range in one parallel pass (row ids in
+// order in each tile's slice of the row-id buffer) to the output. The CTA
+// holding the last tile records the total.
+__global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid_constant__ SelectParams p,
+                                                                   const int32_t* rowlist, int32_t* out_rowids) {
+  __shared__ int s_w[kSelThreads / 32 + 1];
+  __shared__ int s_pref[kSelThreads + 1];
+  const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
+  const int64_t n_tiles = (n_rows + kSelTile - 1) / kSelTile;
+  const int64_t per = (n_tiles + gridDim.x - 1) / gridDim.x;  // <= kSelThreads by the launch
+  const int64_t t0 = static_cast<int64_t>(blockIdx.x) * per;
+  if (t0 >= n_tiles) return;
+  const int64_t t1 = t0 + per < n_tiles ? t0 + per : n_tiles;
+  const int nt = static_cast<int>(t1 - t0);
+  int before = 0;
+  for (int64_t t = threadIdx.x; t < t0; t += kSelThreads) before += static_cast<int>(p.tile_status[t]);
+  const int c = threadIdx.x < nt ? static_cast<int>(p.tile_status[t0 + threadIdx.x]) : 0;
+  int before_total;
+  block_exclusive_sum<kSelThreads>(before, &before_total, s_w);
+  __syncthreads();  // s_w is reused
+  int range_total;
+  const int excl = block_exclusive_sum<kSelThreads>(c, &range_total, s_w);
+  if (threadIdx.x < nt) s_pref[threadIdx.x] = excl;
+  if (threadIdx.x == 0) s_pref[nt] = range_total;
+  __syncthreads();
+  const int64_t base = before_total;
+  for (int i = threadIdx.x; i < range_total; i += kSelThreads) {
+    int lo = 0, hi = nt - 1;  // last tile of the range whose first output is <= i
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_pref[mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    const int32_t row = rowlist[(t0 + lo) * kSelTile + (i - s_pref[lo])];
+    const int64_t o = base + i;
+    for (int j = 0; j < p.n_out; ++j) {
+      const OutCol& oc = p.outs[j];
+      if (oc.width == 8)
+        static_cast<long long*>(oc.dst)[o] = __ldg(static_cast<const long long*>(oc.src) + row);
+      else
+        static_cast<int*>(oc.dst)[o] = __ldg(static_cast<const int*>(oc.src) + row);
+    }
+    if (out_rowids != nullptr) out_rowids[o] = row;
+  }
+  if (t1 == n_tiles && threadIdx.x == 0) p.status->value = base + range_total;
+}
+
+int select_probe_blocks_per_sm(size_t dyn) {
+  static std::mutex mu;
+  static std::map<size_t, int> cache;
+  static bool attr_set = false;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dyn);
+  if (it != cache.end()) return it->second;
+  if (!attr_set) {
+    GF_CUDA(cudaFuncSetAttribute(select_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(kSpMaxDynamic)));
+    attr_set = true;
+  }
+  int per_sm = 0;
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_probe_kernel, kSpThreads, dyn));
+  cache[dyn] = per_sm;
+  return per_sm;
+}
+
 }  // namespace
 
 TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const std::vector<BloomProbe>& probes,
@@ -481,17 +820,72 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   if (n_tiles > 0) {
     const size_t dyn = static_cast<size_t>(smem_words) * 4;
     const bool with_pred = p.prog.n_clauses > 0;
-    const int per_sm = select_blocks_per_sm(with_pred, dyn);
-    int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
-    if (grid > n_tiles) grid = n_tiles;
-    ProfScope prof("select_kernel", s);
-    if (with_pred)
-      select_kernel<true><<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
-    else
-      select_kernel<false><<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
-    after_launch("select_kernel");
-    prof.stop(0);
-    prof.set_bytes_model(p.n_dev, n, read_all, &p.status->value, proj_read + proj_write, scratch, in.rows_owner());
+    // The pipelined probe-only kernel: no predicate, 16-byte aligned key
+    // columns, and an input of at least a few tiles per SM.
+    SpLayout lay{};
+    bool pipelined = !with_pred && p.n_probes > 0 && n >= kSpMinRows &&
+                     (reinterpret_cast<uintptr_t>(p.cols[p.probes[0].col].data) & 15u) == 0;
+    size_t sp_bloom = 0;
+    if (pipelined) {
+      for (int pi = 0; pi < p.n_probes; ++pi) lay.key_width[pi] = p.cols[p.probes[pi].col].type == CT_I64 ? 8 : 4;
+      lay.stage_bytes = kSelTile * lay.key_width[0];
+      lay.bloom_off = kSpHeader + kSpStages * lay.stage_bytes;
+      // only the first probe's filter is staged: the later ones see few rows
+      if (p.probes[0].smem_word >= 0) sp_bloom = static_cast<size_t>(p.probes[0].smem_cap_words) * 4;
+    }
+    int per_sm = 0;
+    const size_t sp_dyn = lay.bloom_off + sp_bloom;
+    if (pipelined) per_sm = select_probe_blocks_per_sm(sp_dyn);
+    if (pipelined && per_sm > 0) {
+      // pass 1: probes; each tile's selected row ids into its slice of rowlist
+      auto rowlist = make_buffer(n * 4, s);
+      SelectParams& p1 = *pp;
+      int32_t* utf8_rowids = p1.out_rowids;
+      std::vector<int32_t> saved_words(p1.n_probes);
+      for (int pi = 0; pi < p1.n_probes; ++pi) {
+        saved_words[pi] = p1.probes[pi].smem_word;
+        if (pi > 0) p1.probes[pi].smem_word = -1;
+      }
+      if (p1.probes[0].smem_word >= 0) p1.probes[0].smem_word = 0;
+      p1.out_rowids = rowlist->as<int32_t>();
+      {
+        int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
+        if (grid > n_tiles) grid = n_tiles;
+        ProfScope prof("select_probe_kernel", s);
+        select_probe_kernel<<<static_cast<int>(grid), kSpThreads, sp_dyn, s>>>(p1, lay);
+        after_launch("select_probe_kernel");
+        prof.stop(0);
+        // the first probe's keys over all rows (later probes' keys are read
+        // for survivors only and not counted)
+        prof.set_bytes_model(p.n_dev, n, lay.key_width[0], &p.status->value, 4.0, scratch, in.rows_owner());
+      }
+      for (int pi = 0; pi < p1.n_probes; ++pi) p1.probes[pi].smem_word = saved_words[pi];
+      p1.out_rowids = utf8_rowids;
+      {
+        // ranges of at most kSelThreads tiles, at least two CTAs per SM
+        int64_t grid = std::max<int64_t>((n_tiles + kSelThreads - 1) / kSelThreads,
+                                         std::min<int64_t>(n_tiles, static_cast<int64_t>(num_sms()) * 2));
+        ProfScope prof("select_gather_kernel", s);
+        select_gather_kernel<<<static_cast<int>(grid), kSelThreads, 0, s>>>(p1, rowlist->as<int32_t>(), utf8_rowids);
+        after_launch("select_gather_kernel");
+        prof.stop(0);
+        prof.set_bytes_model(nullptr, 0, 0, &p.status->value, 4.0 + proj_read + proj_write, scratch,
+                             in.rows_owner());
+      }  // rowlist is freed stream-ordered, after the gather
+    } else {
+      ProfScope prof("select_kernel", s);
+      per_sm = select_blocks_per_sm(with_pred, dyn);
+      int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
+      if (grid > n_tiles) grid = n_tiles;
+      if (with_pred)
+        select_kernel<true><<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
+      else
+        select_kernel<false><<<static_cast<int>(grid), kSelThreads, dyn, s>>>(p);
+      after_launch("select_kernel");
+      prof.stop(0);
+      prof.set_bytes_model(p.n_dev, n, read_all, &p.status->value, proj_read + proj_write, scratch,
+                           in.rows_owner());
+    }
   }
 
   const bool defer = deferred_mode() && !need_rowids && stats == nullptr;

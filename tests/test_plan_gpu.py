@@ -151,3 +151,25 @@ def test_plan_errors_surface_as_error_messages(gpu):
     # the device is still usable after an operator error
     ok = plan.execute(workloads.two_table_plan(), tabs)
     assert ok.table.sorted_rows() == queries.two_table_query(tabs).sorted_rows()
+
+
+@pytest.mark.parametrize("streams,graph,deferred", [(1, False, True), (4, False, True), (8, False, False),
+                                                    (4, True, True), (16, True, True), (2, False, True)])
+def test_streams_same_result(gpu, streams, graph, deferred):
+    """Operators on independent plan branches run on their own streams (and
+    as parallel graph branches); results equal the single-stream run's and
+    the oracle's, for the star query and the chunked two-table query."""
+    tabs = workloads.star_tables(fact_rows=1_500_000, seed=2300 + streams)
+    dev = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
+    text = _with_options(workloads.star_plan(), streams=streams, cudaGraph=graph, deferredSizes=deferred)
+    want = queries.star_query(tabs).sorted_rows()
+    for _ in range(3):  # with a graph: capture, then replays
+        assert plan.execute(text, dev).table.sorted_rows() == want
+    t2 = workloads.two_table_tables(fact_rows=700_000, seed=2400 + streams)
+    text2 = _with_options(workloads.two_table_plan(chunk_rows=100_000), streams=streams, cudaGraph=graph)
+    assert plan.execute(text2, t2).table.sorted_rows() == queries.two_table_query(t2).sorted_rows()
+
+
+def test_streams_option_validated(gpu):
+    with pytest.raises(GfpdbError):
+        plan.execute(_with_options(workloads.star_plan(), streams=0), workloads.star_tables(fact_rows=1000))
