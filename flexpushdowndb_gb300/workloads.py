@@ -233,3 +233,180 @@ def star_batch_spec(fact_tables, queries, load_factor: float = 0.5, items_per_th
     if probe_order is not None:
         spec["probeOrder"] = list(probe_order)
     return spec
+
+
+# ------------------------------------------------------------------------ CSV
+#
+# TPC-H-lineitem-shaped '|'-delimited text: per row 4 int32 uniform on
+# [1, 2^20], 4 decimal(15,2) uniform on [0, 100000.00] written with two
+# fractional digits, 2 dates uniform on 1992-01-01..1998-12-31 as YYYY-MM-DD,
+# and 6 strings of length uniform on [10, 40] over [A-Za-z0-9 ]. Generated
+# with vectorised digit writes, in chunks of rows, from SplitMix64 streams.
+
+LINEITEM_FIELDS = ([(f"i{k}", "int32") for k in range(1, 5)] + [(f"d{k}", "decimal(15,2)") for k in range(1, 5)]
+                   + [("t1", "date32"), ("t2", "date32")] + [(f"s{k}", "utf8") for k in range(1, 7)])
+CSV_SEED = 3000
+_ALPHABET = np.frombuffer(b"ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789 ", dtype=np.uint8)
+DATE_LO = 8035   # 1992-01-01 as days since 1970-01-01
+DATE_HI = 10591  # 1998-12-31
+
+
+def civil_from_days(z: np.ndarray):
+    """(year, month, day) of days since 1970-01-01 (H. Hinnant's
+    civil_from_days, vectorised)."""
+    z = z.astype(np.int64) + 719468
+    era = np.floor_divide(z, 146097)
+    doe = z - era * 146097
+    yoe = (doe - doe // 1460 + doe // 36524 - doe // 146096) // 365
+    y = yoe + era * 400
+    doy = doe - (365 * yoe + yoe // 4 - yoe // 100)
+    mp = (5 * doy + 2) // 153
+    d = doy - (153 * mp + 2) // 5 + 1
+    m = np.where(mp < 10, mp + 3, mp - 9)
+    return y + (m <= 2), m, d
+
+
+def _ndigits(x: np.ndarray) -> np.ndarray:
+    n = np.ones(x.shape, dtype=np.int64)
+    for k in range(1, 19):
+        n += x >= 10**k
+    return n
+
+
+def _put_uint(buf: np.ndarray, pos: np.ndarray, x: np.ndarray, nd: np.ndarray) -> None:
+    x = x.astype(np.int64)
+    for k in range(int(nd.max()) if len(nd) else 0):
+        m = nd > k
+        buf[pos[m] + nd[m] - 1 - k] = 48 + (x[m] // 10**k) % 10
+
+
+def lineitem_columns(rows: int, seed: int = CSV_SEED, start: int = 0) -> dict[str, np.ndarray]:
+    """The typed values of rows [start, start + rows) (int32 as int64, decimals
+    in cents, dates in days since the epoch; strings as (lengths, chars))."""
+    cols = {}
+    for k in range(1, 5):
+        cols[f"i{k}"] = uniform(seed, k, rows, 1, 1 << 20, start)
+    for k in range(1, 5):
+        cols[f"d{k}"] = uniform(seed, 4 + k, rows, 0, 10_000_000, start)
+    cols["t1"] = uniform(seed, 9, rows, DATE_LO, DATE_HI, start)
+    cols["t2"] = uniform(seed, 10, rows, DATE_LO, DATE_HI, start)
+    for k in range(1, 7):
+        lens = uniform(seed, 10 + k, rows, 10, 40, start)
+        # the chars of row r start at a counter position that does not depend
+        # on the chunking: 40 slots per row
+        pos = np.repeat((np.arange(rows, dtype=np.int64) + start) * 40, lens) + (
+            np.arange(int(lens.sum()), dtype=np.int64) - np.repeat(np.cumsum(lens) - lens, lens))
+        chars = _ALPHABET[_stream_at(seed * 1_000_003 + 20 + k, pos) % np.uint64(len(_ALPHABET))]
+        cols[f"s{k}"] = (lens, chars)
+    return cols
+
+
+def _stream_at(seed: int, idx: np.ndarray) -> np.ndarray:
+    """SplitMix64 outputs at arbitrary counter positions."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + (idx.astype(np.uint64) + np.uint64(1)) * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def lineitem_csv(rows: int, seed: int = CSV_SEED, chunk: int = 250_000, processes: int = 0) -> bytes:
+    """The text of `rows` lineitem-shaped rows, '|'-delimited, '\\n'-terminated.
+    Chunks are independent (counter-based streams); with processes > 1 they
+    are generated by a pool of spawned processes (never forked: the caller
+    may already hold a CUDA context)."""
+    jobs = [(min(chunk, rows - start), seed, start) for start in range(0, rows, chunk)]
+    if processes > 1 and len(jobs) > 1:
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(min(processes, len(jobs))) as pool:
+            return b"".join(pool.starmap(_lineitem_chunk, jobs))
+    return b"".join(_lineitem_chunk(*j) for j in jobs)
+
+
+def _lineitem_chunk(rows: int, seed: int, start: int) -> bytes:
+    c = lineitem_columns(rows, seed, start)
+    names = [n for n, _ in LINEITEM_FIELDS]
+    lens = []
+    for n, ty in LINEITEM_FIELDS:
+        if ty == "int32":
+            lens.append(_ndigits(c[n]))
+        elif ty.startswith("decimal"):
+            lens.append(_ndigits(c[n] // 100) + 3)
+        elif ty == "date32":
+            lens.append(np.full(rows, 10, dtype=np.int64))
+        else:
+            lens.append(c[n][0])
+    L = np.stack(lens)                          # [field, row]
+    row_len = L.sum(axis=0) + len(names)        # separators + newline
+    row_off = np.cumsum(row_len) - row_len
+    buf = np.empty(int(row_len.sum()), dtype=np.uint8)
+    off = row_off.copy()
+    for f, (n, ty) in enumerate(LINEITEM_FIELDS):
+        ln = L[f]
+        if ty == "int32":
+            _put_uint(buf, off, c[n], ln)
+        elif ty.startswith("decimal"):
+            ip = c[n] // 100
+            nd = ln - 3
+            _put_uint(buf, off, ip, nd)
+            buf[off + nd] = ord(".")
+            _put_uint(buf, off + nd + 1, c[n] % 100, np.full(rows, 2, dtype=np.int64))
+        elif ty == "date32":
+            y, m, d = civil_from_days(c[n])
+            _put_uint(buf, off, y, np.full(rows, 4, dtype=np.int64))
+            buf[off + 4] = ord("-")
+            _put_uint(buf, off + 5, m, np.full(rows, 2, dtype=np.int64))
+            buf[off + 7] = ord("-")
+            _put_uint(buf, off + 8, d, np.full(rows, 2, dtype=np.int64))
+        else:
+            lens_s, chars = c[n]
+            pos = np.repeat(off, lens_s) + (np.arange(int(lens_s.sum()), dtype=np.int64)
+                                            - np.repeat(np.cumsum(lens_s) - lens_s, lens_s))
+            buf[pos] = chars
+        buf[off + ln] = ord("|") if f + 1 < len(names) else ord("\n")
+        off = off + ln + 1
+    return buf.tobytes()
+
+
+# The scan of the CSV workload: three range predicates (one date32, one
+# decimal, one int32) with a joint selectivity of about 2%, fused with
+# sum(d2 * i2) (int64 cents) and count(*).
+CSV_T1_RANGE = (9131, 9769)       # 1995-01-01 .. 1996-09-30, ~25% of the dates
+CSV_D1_LT = 2_000_000             # d1 < 20000.00: ~20%
+CSV_I1_LT = 419_431               # i1 < 0.4 * 2^20: ~40%
+
+
+def csv_scan_predicate():
+    return and_(gte(col("t1"), num_lit(CSV_T1_RANGE[0], "date32")), lte(col("t1"), num_lit(CSV_T1_RANGE[1], "date32")),
+                lt(col("d1"), num_lit(CSV_D1_LT, "int64")), lt(col("i1"), num_lit(CSV_I1_LT, "int32")))
+
+
+# ----------------------------------------------------- high-cardinality group
+#
+# The serving form's group-by template: int64 keys drawn from n_keys distinct
+# values with Zipf(s) frequencies (rank r has weight 1/r^s), one int64 value
+# column. Ranks map to scattered int64 keys through an odd multiplier.
+
+def zipf_keys(rows: int, n_keys: int, s: float = 1.1, seed: int = 5000) -> np.ndarray:
+    ranks = np.arange(1, n_keys + 1, dtype=np.float64)
+    cdf = np.cumsum(ranks ** -s)
+    cdf /= cdf[-1]
+    u = (splitmix64(seed * 1_000_003 + 1, rows) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    r = np.minimum(np.searchsorted(cdf, u, side="right"), n_keys - 1).astype(np.uint64)
+    with np.errstate(over="ignore"):
+        return ((r + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15) >> np.uint64(1)).astype(np.int64)
+
+
+def groupby_table(rows: int, n_keys: int, s: float = 1.1, seed: int = 5000) -> Table:
+    return Table([Column("k", "int64", zipf_keys(rows, n_keys, s, seed)),
+                  Column("v", "int64", uniform(seed, 2, rows, -1_000_000, 1_000_000))])
+
+
+def groupby_plan(groups_hint: int = 0) -> Plan:
+    p = Plan()
+    p.scan("scan", "t", ["k", "v"])
+    p.group("group", "scan", ["k"], [aggregate("SUM", "s", col("v")), aggregate("COUNT", "c")],
+            groups_hint=groups_hint)
+    p.collate("collate", "group")
+    return p
