@@ -85,6 +85,26 @@ class ExecStats(ctypes.Structure):
     ]
 
 
+class RequestStats(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("batch_size", ctypes.c_int32),
+        ("submit_ns", ctypes.c_int64),
+        ("start_ns", ctypes.c_int64),
+        ("end_ns", ctypes.c_int64),
+        ("kernel_launches", ctypes.c_int64),
+        ("cache_misses", ctypes.c_int64),
+        ("worker", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "submitted", "completed", "failed", "batches", "batched_requests", "cache_hits", "cache_misses",
+        "cache_evictions", "cache_bytes", "cache_capacity", "reserved_bytes", "hbm_budget", "admission_waits")]
+
+
 class GfpdbError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"gfpdb error {code}: {message}")
@@ -143,6 +163,12 @@ SIGNATURES = {
     ),
     "gfpdb_plan_validate": (_I32, [ctypes.c_char_p]),
     "gfpdb_graph_cache_clear": (_I32, []),
+    "gfpdb_server_create": (_I32, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "gfpdb_server_register_table": (_I32, [_P, ctypes.c_char_p, _S, _A]),
+    "gfpdb_server_submit": (_I32, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "gfpdb_server_wait": (_I32, [_P, ctypes.c_uint64, _I64, _S, _A, ctypes.POINTER(RequestStats)]),
+    "gfpdb_server_get_stats": (_I32, [_P, ctypes.POINTER(ServerStats)]),
+    "gfpdb_server_destroy": (_I32, [_P]),
     "gfpdb_star_batch": (
         _I32,
         [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A), _I32, _I32, _S, _A,

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/gfpdb.h"
+#include "host/batchspec.h"
 #include "host/handles.h"
 #include "host/pop.h"
 #include "kernels/launch.h"
@@ -229,65 +230,12 @@ std::shared_ptr<BatchEntry> make_batch(const json::Value& spec, const std::map<s
     if (it == tables.end()) fail(GFPDB_EINVAL, "batched star query names table '" + name + "' which was not passed");
     return it->second;
   };
-  sp.fact_tables = spec.str_list("factTables");
+  parse_star_batch_spec(spec, sp);
+  if (sp.queries.empty()) fail(GFPDB_EINVAL, "a batched star query needs \"queries\"");
   for (auto& n : sp.fact_tables) be->batch.parts().push_back(table(n));
-  for (auto& d : spec.at("dimensions").array()) {
-    StarBatchSpec::Dim dim{d.at("table").str(), d.at("key").str(), d.at("factKey").str(), d.at("filterColumn").str()};
-    be->batch.dim_tables().push_back(table(dim.table));
-    sp.dims.push_back(dim);
-  }
-  if (spec.contains("groupBy"))
-    for (auto& g : spec.at("groupBy").array())
-      sp.group.push_back(StarBatchSpec::Group{static_cast<int>(g.at("dimension").integer()), g.at("column").str()});
-  for (auto& a : spec.at("aggregates").array()) {
-    StarBatchSpec::Agg agg;
-    const std::string f = a.at("function").str();
-    if (f == "SUM") agg.fn = AGG_SUM;
-    else if (f == "COUNT") agg.fn = AGG_COUNT_STAR;
-    else fail(GFPDB_EUNSUPPORTED, "batched star aggregates are SUM and COUNT(*)");
-    agg.name = a.at("name").str();
-    agg.columns = a.str_list("columns");
-    sp.aggs.push_back(agg);
-  }
-  for (auto& q : spec.at("queries").array()) {
-    std::vector<std::pair<int64_t, int64_t>> ranges;
-    for (auto& r : q.array()) ranges.emplace_back(r.array().at(0).integer(), r.array().at(1).integer());
-    if (ranges.size() != sp.dims.size()) fail(GFPDB_EINVAL, "each batched query needs one range per dimension");
-    sp.queries.push_back(ranges);
-  }
-  if (spec.contains("probeOrder"))
-    for (auto& o : spec.at("probeOrder").array()) sp.probe_order.push_back(static_cast<int>(o.integer()));
-  sp.load_factor = spec.get_num("loadFactor", 0.5);
-  if (!(sp.load_factor > 0 && sp.load_factor <= 0.9)) fail(GFPDB_EINVAL, "loadFactor must be in (0, 0.9]");
-  sp.items_per_thread = static_cast<int>(spec.get_int("itemsPerThread", 2));
-  sp.blocks_per_sm = static_cast<int>(spec.get_int("blocksPerSm", 4));
-  if (sp.blocks_per_sm < 1 || sp.blocks_per_sm > 16) fail(GFPDB_EINVAL, "blocksPerSm must be in [1, 16]");
-  sp.groups_hint = spec.get_int("groupsHint", 1024);
+  for (auto& d : sp.dims) be->batch.dim_tables().push_back(table(d.table));
   be->batch.prepare(s);
-  if (use_graph) {
-    // run() only clears preallocated buffers and launches kernels: capture it.
-    cudaStream_t cs = nullptr;
-    GF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    const uint64_t k0 = g_kernel_launches.load();
-    cudaGraph_t graph = nullptr;
-    bool ok = true;
-    GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    try {
-      be->batch.run(cs);
-    } catch (const std::exception&) {
-      ok = false;
-    }
-    if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) ok = false;
-    if (ok && cudaGraphInstantiate(&be->exec, graph, 0) != cudaSuccess) ok = false;
-    if (graph) (void)cudaGraphDestroy(graph);
-    (void)cudaGetLastError();
-    (void)cudaStreamDestroy(cs);
-    be->kernels = g_kernel_launches.load() - k0;
-    if (!ok && be->exec) {
-      (void)cudaGraphExecDestroy(be->exec);
-      be->exec = nullptr;
-    }
-  }
+  if (use_graph) be->exec = capture_star_batch(be->batch, &be->kernels);
   return be;
 }
 

@@ -395,8 +395,9 @@ class HashJoinArrowPOp : public PhysicalOp {
 // TupleSet as it arrives, finalise when all producers are complete.
 class GroupPOp : public PhysicalOp {
  public:
-  GroupPOp(std::string name, std::vector<std::string> group_cols, std::vector<GroupAggregate> aggs, int64_t hint)
-      : PhysicalOp(std::move(name), "GroupPOp") {
+  GroupPOp(std::string name, std::vector<std::string> group_cols, std::vector<GroupAggregate> aggs, int64_t hint,
+           std::string type = "GroupPOp")
+      : PhysicalOp(std::move(name), std::move(type)) {
     table_ = group_table_create(group_cols, aggs, hint);
   }
 
@@ -419,6 +420,49 @@ class GroupPOp : public PhysicalOp {
 
  private:
   std::shared_ptr<GroupTable> table_;
+};
+
+// Parses delimited text into a TupleSet: the CSV branch of the reference's
+// file scans (FileScanAbstractPOp::readAndSendTuples reading through
+// CSVReader::read, fpdb-tuple/src/csv/CSVReader.cpp:15-21), reading the text
+// from an input table whose first column is a single utf8 value (the file's
+// bytes) instead of a file. Only the projected fields are materialised.
+class CsvScanPOp : public PhysicalOp {
+ public:
+  CsvScanPOp(std::string name, std::string table, std::vector<CsvField> fields, std::vector<int> emit, char delim,
+             bool header)
+      : PhysicalOp(std::move(name), "CsvScanPOp"), table_(std::move(table)), fields_(std::move(fields)),
+        emit_(std::move(emit)), delim_(delim), header_(header) {}
+
+  void setExecution(Execution* e) { exec_ = e; }
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type != MessageType::START) return;
+    const InputTable& in = exec_->input(table_);
+    TupleSetPtr ts = in.device ? in.device : import_tupleset(in.schema, in.array, ctx()->stream());
+    ts = resolved(ts, ctx()->stream());
+    if (ts->num_columns() < 1 || ts->field(0).type != DType::Utf8 || ts->num_rows() != 1)
+      fail(GFPDB_EINVAL, "CsvScanPOp input '" + table_ + "' must hold the text as one utf8 value");
+    const auto& c = ts->column(0);
+    int32_t off[2];
+    GF_CUDA(cudaMemcpyAsync(off, c->offsets, sizeof(off), cudaMemcpyDeviceToHost, ctx()->stream()));
+    sync(ctx()->stream());
+    const char* text = static_cast<const char*>(c->data) + off[0];
+    Message out;
+    out.type = MessageType::TUPLESET;
+    out.tuples = csv_parse(text, off[1] - off[0], delim_, header_, fields_, emit_, ctx()->stream());
+    ctx()->tell(out);
+    ctx()->notifyComplete();
+  }
+
+ private:
+  Execution* exec_ = nullptr;
+  std::string table_;
+  std::vector<CsvField> fields_;
+  std::vector<int> emit_;
+  char delim_;
+  bool header_;
 };
 
 // CollatePOp (fpdb-executor/src/physical/collate/CollatePOp.cpp:67-150):
@@ -723,7 +767,43 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
     op = std::make_unique<HashJoinArrowPOp>(name, o.str_list("buildProducers"), o.str_list("probeProducers"),
                                             o.at("buildKey").str(), o.at("probeKey").str(),
                                             o.get_num("loadFactor", 0.5));
-  } else if (type == "GroupPOp") {
+  } else if (type == "CsvScanPOp") {
+    std::vector<CsvField> fields;
+    for (auto& f : o.at("fields").array()) {
+      CsvField cf;
+      cf.name = f.at("name").str();
+      const std::string ty = f.at("type").str();
+      if (ty.rfind("decimal", 0) == 0) {
+        const auto comma = ty.find(',');
+        if (comma == std::string::npos) fail(GFPDB_EINVAL, "decimal field types are written decimal(p,s)");
+        cf.type = DType::Int64;
+        cf.decimal = true;
+        cf.scale = std::atoi(ty.c_str() + comma + 1);
+        if (cf.scale < 0 || cf.scale > 9) fail(GFPDB_EINVAL, "decimal scale must be in [0, 9]");
+      } else {
+        cf.type = dtype_from_name(ty);
+      }
+      fields.push_back(cf);
+    }
+    std::vector<int> emit;
+    if (o.contains("columns")) {
+      for (auto& cn : o.str_list("columns")) {
+        int found = -1;
+        for (size_t i = 0; i < fields.size(); ++i)
+          if (fields[i].name == cn) found = static_cast<int>(i);
+        if (found < 0) fail(GFPDB_EINVAL, "CsvScanPOp '" + name + "': column '" + cn + "' is not a field");
+        emit.push_back(found);
+      }
+    } else {
+      for (size_t i = 0; i < fields.size(); ++i) emit.push_back(static_cast<int>(i));
+    }
+    const std::string delim = o.get_str("delimiter", ",");
+    if (delim.size() != 1) fail(GFPDB_EINVAL, "CsvScanPOp delimiter must be one byte");
+    auto cs = std::make_unique<CsvScanPOp>(name, o.at("table").str(), std::move(fields), std::move(emit), delim[0],
+                                           o.get_bool("header", false));
+    cs->setExecution(exec);
+    op = std::move(cs);
+  } else if (type == "GroupPOp" || type == "AggregatePOp") {
     std::vector<GroupAggregate> aggs;
     for (auto& a : o.at("aggregates").array()) {
       GroupAggregate g;
@@ -733,7 +813,13 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
       else if (g.fn == AGG_COUNT) g.fn = AGG_COUNT_STAR;
       aggs.push_back(g);
     }
-    op = std::make_unique<GroupPOp>(name, o.str_list("groupColumnNames"), aggs, o.get_int("groupsHint", 0));
+    if (type == "AggregatePOp") {
+      // AggregatePOp (fpdb-executor/src/physical/aggregate/AggregatePOp.cpp:57-153):
+      // the non-grouped aggregate, run as a group-by with one implicit group.
+      op = std::make_unique<GroupPOp>(name, std::vector<std::string>{}, aggs, 1, "AggregatePOp");
+    } else {
+      op = std::make_unique<GroupPOp>(name, o.str_list("groupColumnNames"), aggs, o.get_int("groupsHint", 0));
+    }
   } else if (type == "CollatePOp") {
     op = std::make_unique<CollatePOp>(name);
   } else {

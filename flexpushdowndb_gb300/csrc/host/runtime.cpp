@@ -7,6 +7,11 @@ namespace gfpdb {
 
 std::atomic<uint64_t> g_kernel_launches{0};
 
+uint64_t& thread_kernel_launches() {
+  thread_local uint64_t n = 0;
+  return n;
+}
+
 void fail(int32_t code, const std::string& msg) { throw Error(code, msg); }
 
 std::string& last_error() {

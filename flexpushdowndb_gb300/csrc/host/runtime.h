@@ -59,7 +59,13 @@ void check_cuda(cudaError_t e, const char* what);
 // Every kernel launch in the library goes through this counter so a caller
 // can tell how many device kernels a call issued.
 extern std::atomic<uint64_t> g_kernel_launches;
-inline void count_launch(uint64_t n = 1) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
+// Kernel launches of the calling thread (what one request of a worker
+// thread launched, when several threads share the GPU).
+uint64_t& thread_kernel_launches();
+inline void count_launch(uint64_t n = 1) {
+  g_kernel_launches.fetch_add(n, std::memory_order_relaxed);
+  thread_kernel_launches() += n;
+}
 // Checks the launch that was just issued and counts it.
 void after_launch(const char* kernel_name);
 

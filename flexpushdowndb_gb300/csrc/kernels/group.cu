@@ -58,6 +58,7 @@ struct GroupParams {
 };
 
 __device__ __forceinline__ uint64_t pack_key(const GroupParams& p, int64_t row) {
+  if (p.n_keys == 0) return 0;  // a non-grouped aggregate: one group
   if (p.n_keys == 1) {
     const int64_t v = load_int(p.key_cols[0], row);
     return p.key_bits[0] == 64 ? static_cast<uint64_t>(v) : static_cast<uint64_t>(static_cast<uint32_t>(v));
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(256) group_finalize_kernel(const __grid_consta
     if (p.n_keys == 1) {
       const int64_t v = p.key_bits[0] == 64 ? static_cast<int64_t>(key) : static_cast<int32_t>(static_cast<uint32_t>(key));
       store_typed(p.key_dst[0], pos, p.key_type[0], v);
-    } else {
+    } else if (p.n_keys == 2) {
       store_typed(p.key_dst[0], pos, p.key_type[0], static_cast<int32_t>(static_cast<uint32_t>(key >> 32)));
       store_typed(p.key_dst[1], pos, p.key_type[1], static_cast<int32_t>(static_cast<uint32_t>(key)));
     }
@@ -589,7 +590,6 @@ class GroupTable {
   int64_t groups_upper = 0;
 
   void compile(const TupleSet& ts) {
-    if (group_cols.empty()) fail(GFPDB_EUNSUPPORTED, "group-by without group columns (use an aggregate)");
     if (group_cols.size() > 2) fail(GFPDB_EUNSUPPORTED, "group-by over more than two key columns");
     int bits = 0;
     for (auto& g : group_cols) {

@@ -177,6 +177,12 @@ class StarBatch {
   TupleSetPtr result_view() const;
   const DevStatus* status() const;
   int64_t fact_rows() const;
+  // Replaces the query ranges (at most the prepared number of queries; the
+  // remaining slots select nothing) without preparing again.
+  void set_ranges(const std::vector<std::vector<std::pair<int64_t, int64_t>>>& q, cudaStream_t s);
+  // Device array of kSBMaxQueries + 1 offsets: query q's rows of the result
+  // are [off[q], off[q + 1]); valid after run().
+  const unsigned long long* query_offsets() const;
 
  private:
   std::unique_ptr<StarBatchState> st_;

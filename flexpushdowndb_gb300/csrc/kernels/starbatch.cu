@@ -23,6 +23,7 @@
 // keys); a repeated key is reported as an error.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "common.cuh"
 #include "launch.h"
@@ -536,34 +537,56 @@ struct SBFinalParams {
   int32_t* out_q;
   void* out_g[2];
   long long* out_a[kMaxAggs];
-  unsigned long long* counter;
+  unsigned long long* counter;   // output rows in all
+  unsigned long long* qcount;    // [kSBMaxQueries] output rows of each query
+  unsigned long long* qcursor;   // [kSBMaxQueries]
+  unsigned long long* qoff;      // [kSBMaxQueries + 1] first output row of each query
 };
 
-// Stage 3: every (query, group) with rows becomes one output row.
-__global__ void __launch_bounds__(256) sb_final_kernel(const __grid_constant__ SBFinalParams p) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t total = p.slots * static_cast<uint64_t>(p.n_queries);
-  const uint64_t w0 = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nw = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
-  for (uint64_t base = w0 * 32; base < total; base += nw * 32) {
-    const uint64_t i = base + lane;
-    bool live = false;
-    uint64_t key = 0;
-    int q = 0;
-    if (i < total) {
-      q = static_cast<int>(i / p.slots);
-      const uint64_t s = i % p.slots;
-      live = ((p.touched[s] >> q) & 1ull) != 0;
-      key = s + 1 < p.slots ? p.gkeys[s] : kEmptySlot;
+// Stage 3a: output rows of each query (groups it touched).
+__global__ void __launch_bounds__(256) sb_count_kernel(const __grid_constant__ SBFinalParams p) {
+  __shared__ unsigned int s_cnt[kSBMaxQueries];
+  for (int q = threadIdx.x; q < kSBMaxQueries; q += blockDim.x) s_cnt[q] = 0;
+  __syncthreads();
+  for (uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < p.slots;
+       s += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    unsigned long long m = p.touched[s];
+    while (m != 0) {
+      atomicAdd(&s_cnt[__ffsll(static_cast<long long>(m)) - 1], 1u);
+      m &= m - 1;
     }
-    const uint32_t bal = __ballot_sync(0xffffffffu, live);
-    if (bal == 0) continue;
-    unsigned long long at = 0;
-    const int leader = __ffs(bal) - 1;
-    if (lane == leader) at = atomicAdd(p.counter, static_cast<unsigned long long>(__popc(bal)));
-    at = __shfl_sync(0xffffffffu, at, leader);
-    if (!live) continue;
-    const int64_t pos = static_cast<int64_t>(at) + __popc(bal & ((1u << lane) - 1u));
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < kSBMaxQueries; q += blockDim.x)
+    if (s_cnt[q] != 0) atomicAdd(p.qcount + q, static_cast<unsigned long long>(s_cnt[q]));
+}
+
+// Stage 3b: every (query, group) with rows becomes one output row; each
+// query's rows are contiguous (queries in order), so a query's result is a
+// slice of the output.
+__global__ void __launch_bounds__(256) sb_final_kernel(const __grid_constant__ SBFinalParams p) {
+  __shared__ unsigned long long s_off[kSBMaxQueries];
+  if (threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    for (int q = 0; q < kSBMaxQueries; ++q) {
+      s_off[q] = acc;
+      acc += p.qcount[q];
+    }
+    if (blockIdx.x == 0) {
+      for (int q = 0; q < kSBMaxQueries; ++q) p.qoff[q] = s_off[q];
+      p.qoff[kSBMaxQueries] = acc;
+      *p.counter = acc;
+    }
+  }
+  __syncthreads();
+  const uint64_t total = p.slots * static_cast<uint64_t>(p.n_queries);
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const int q = static_cast<int>(i / p.slots);
+    const uint64_t s = i % p.slots;
+    if (((p.touched[s] >> q) & 1ull) == 0) continue;
+    const uint64_t key = s + 1 < p.slots ? p.gkeys[s] : kEmptySlot;
+    const int64_t pos = static_cast<int64_t>(s_off[q] + atomicAdd(p.qcursor + q, 1ull));
     p.out_q[pos] = q;
     if (p.n_group == 1) {
       static_cast<int32_t*>(p.out_g[0])[pos] = static_cast<int32_t>(static_cast<uint32_t>(key));
@@ -602,12 +625,17 @@ struct StarBatchState {
   uint64_t gcap = 0;
   int64_t out_cap = 0, n_tiles = 0, fact_rows = 0;
   unsigned long long* counter = nullptr;
+  unsigned long long* qcount = nullptr;
+  unsigned long long* qcursor = nullptr;
+  unsigned long long* qoff = nullptr;
+  size_t ranges_host_off = 0;  // byte offset of the query ranges in host_meta / meta_buf
 
   void prepare(cudaStream_t s);
   void run(cudaStream_t s);
   void launch_fact(int grid, cudaStream_t s);
   TupleSetPtr result_view() const;
   const DevStatus* status() const;
+  void set_ranges(const std::vector<std::vector<std::pair<int64_t, int64_t>>>& q, cudaStream_t s);
 };
 
 StarBatch::StarBatch() : st_(new StarBatchState()) {}
@@ -620,6 +648,10 @@ void StarBatch::run(cudaStream_t s) { st_->run(s); }
 TupleSetPtr StarBatch::result_view() const { return st_->result_view(); }
 const DevStatus* StarBatch::status() const { return st_->status(); }
 int64_t StarBatch::fact_rows() const { return st_->fact_rows; }
+void StarBatch::set_ranges(const std::vector<std::vector<std::pair<int64_t, int64_t>>>& q, cudaStream_t s) {
+  st_->set_ranges(q, s);
+}
+const unsigned long long* StarBatch::query_offsets() const { return st_->qoff; }
 
 void StarBatchState::prepare(cudaStream_t s) {
   if (spec.dims.empty() || spec.dims.size() > static_cast<size_t>(kSBMaxDims))
@@ -807,7 +839,8 @@ void StarBatchState::prepare(cudaStream_t s) {
   gkeys_buf = make_buffer(static_cast<int64_t>(gcap) * 8, s);
   touched_buf = make_buffer(static_cast<int64_t>(gcap + 1) * 8, s);
   gaccs_buf = make_buffer(gslots * 8 * na, s);
-  misc_buf = make_buffer(sizeof(DevStatus) + 64, s);
+  // status block, output count, then per-query counts, cursors and offsets
+  misc_buf = make_buffer(sizeof(DevStatus) + 64 + 8 * (3 * kSBMaxQueries + 1), s);
   meta_buf = make_buffer(static_cast<int64_t>(hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8 +
                                               kSBMaxQueries * kSBMaxDims * 16),
                          s);
@@ -874,6 +907,10 @@ void StarBatchState::prepare(cudaStream_t s) {
   fact_params.st = st;
   for (int d = 0; d < nd; ++d) fact_params.dims[d] = dims_params.dims[d];
   counter = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus));
+  qcount = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus) + 64);
+  qcursor = qcount + kSBMaxQueries;
+  qoff = qcursor + kSBMaxQueries;
+  ranges_host_off = hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8;
 }
 
 // Launches with at most as many blocks as are resident at once: tiles are
@@ -883,12 +920,11 @@ template <int ITEMS>
 static void launch_fact_items(const SBFactParams& p, size_t smem, int grid, cudaStream_t s) {
   // Opt in once to the largest dynamic size this engine asks for (static
   // plus dynamic shared memory above 48 KB needs it).
-  static bool configured = false;
-  if (!configured) {
+  static std::once_flag configured;
+  std::call_once(configured, [] {
     GF_CUDA(cudaFuncSetAttribute(sb_fact_kernel<ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(kSBSmemMaxDynamic)));
-    configured = true;
-  }
+  });
   int per_sm = 0;
   GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sb_fact_kernel<ITEMS>, kSBFactThreads, smem));
   if (per_sm < 1) fail(GFPDB_EUNSUPPORTED, "the batched fact stage does not fit on an SM with these settings");
@@ -963,7 +999,14 @@ void StarBatchState::run(cudaStream_t s) {
     for (size_t g = 0; g < spec.group.size(); ++g) fp.out_g[g] = out_g[g]->data();
     for (size_t a = 0; a < spec.aggs.size(); ++a) fp.out_a[a] = out_a[a]->as<long long>();
     fp.counter = counter;
+    fp.qcount = qcount;
+    fp.qcursor = qcursor;
+    fp.qoff = qoff;
     const uint64_t total = fp.slots * static_cast<uint64_t>(fp.n_queries);
+    int64_t cblocks = static_cast<int64_t>((fp.slots + 255) / 256);
+    if (cblocks > sms * 2) cblocks = sms * 2;
+    sb_count_kernel<<<static_cast<int>(cblocks), 256, 0, s>>>(fp);
+    after_launch("sb_count_kernel");
     int64_t blocks = static_cast<int64_t>((total + 255) / 256);
     if (blocks > sms * 8) blocks = sms * 8;
     ProfScope prof("sb_final_kernel", s);
@@ -971,6 +1014,23 @@ void StarBatchState::run(cudaStream_t s) {
     after_launch("sb_final_kernel");
     prof.stop(static_cast<double>(total) * 8.0 * (1 + fp.n_aggs));
   }
+}
+
+void StarBatchState::set_ranges(const std::vector<std::vector<std::pair<int64_t, int64_t>>>& q, cudaStream_t s) {
+  const int nq = static_cast<int>(spec.queries.size());
+  const int nd = static_cast<int>(spec.dims.size());
+  if (static_cast<int>(q.size()) > nq) fail(GFPDB_EINVAL, "more queries than the batch was prepared for");
+  int64_t* hr = reinterpret_cast<int64_t*>(host_meta.data() + ranges_host_off);
+  for (int i = 0; i < nq; ++i)
+    for (int d = 0; d < nd; ++d) {
+      const bool used = i < static_cast<int>(q.size());
+      if (used && static_cast<int>(q[i].size()) != nd) fail(GFPDB_EINVAL, "each query needs one range per dimension");
+      hr[(i * kSBMaxDims + d) * 2] = used ? q[i][d].first : 1;  // unused slot: the empty range [1, 0]
+      hr[(i * kSBMaxDims + d) * 2 + 1] = used ? q[i][d].second : 0;
+    }
+  GF_CUDA(cudaMemcpyAsync(meta_buf->as<char>() + ranges_host_off, host_meta.data() + ranges_host_off,
+                          static_cast<size_t>(nq) * kSBMaxDims * 16, cudaMemcpyHostToDevice, s));
+  sync(s);  // host_meta may be rewritten by the next call
 }
 
 TupleSetPtr StarBatchState::result_view() const {

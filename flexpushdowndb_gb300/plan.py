@@ -84,6 +84,22 @@ class Plan:
         self.connect(producer, name)
         return name
 
+    def aggregate(self, name: str, producer: str, aggregates: Sequence[dict]) -> str:
+        """Non-grouped aggregate (AggregatePOp)."""
+        self._add({"type": "AggregatePOp", "name": name, "aggregates": list(aggregates)})
+        self.connect(producer, name)
+        return name
+
+    def csv_scan(self, name: str, table: str, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
+                 delimiter: str = ",", header: bool = False) -> str:
+        """Parse the text held by input `table` (one utf8 value, see
+        tupleset.text_table) into the projected `columns`."""
+        op = {"type": "CsvScanPOp", "name": name, "table": table,
+              "fields": [{"name": n, "type": t} for n, t in fields], "delimiter": delimiter, "header": header}
+        if columns:
+            op["columns"] = list(columns)
+        return self._add(op)
+
     def collate(self, name: str, producer: str) -> str:
         self._add({"type": "CollatePOp", "name": name})
         self.connect(producer, name)

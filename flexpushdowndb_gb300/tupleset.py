@@ -326,3 +326,10 @@ def import_result(schema: _abi.ArrowSchema, darr: _abi.ArrowDeviceArray, release
         if schema.release:
             schema.release(ctypes.pointer(schema))
     return Table(cols)
+
+
+def text_table(text: bytes, name: str = "text") -> Table:
+    """A one-row table whose utf8 value is `text` (the input of CsvScanPOp)."""
+    if len(text) >= 2**31:
+        raise ValueError("text exceeds 2 GiB")
+    return Table([Column(name, "utf8", (np.array([0, len(text)], dtype=np.int32), np.frombuffer(text, dtype=np.uint8)))])

@@ -410,3 +410,15 @@ def groupby_plan(groups_hint: int = 0) -> Plan:
             groups_hint=groups_hint)
     p.collate("collate", "group")
     return p
+
+
+def csv_scan_plan(columns=("t1", "d1", "i1", "d2", "i2")) -> Plan:
+    """Parse the lineitem text (input "lineitem"), apply the three range
+    predicates and sum(d2 * i2), count(*)."""
+    p = Plan()
+    p.csv_scan("scan", "lineitem", LINEITEM_FIELDS, columns=list(columns), delimiter="|")
+    p.filter("filter", "scan", csv_scan_predicate(), ["d2", "i2"])
+    p.aggregate("agg", "filter", [aggregate("SUM", "sum_d2_i2", times(col("d2"), col("i2"))),
+                                  aggregate("COUNT", "cnt")])
+    p.collate("collate", "agg")
+    return p

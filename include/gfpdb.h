@@ -332,6 +332,69 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
                          int32_t use_graph, int32_t result_to_host, struct ArrowSchema* out_schema,
                          struct ArrowDeviceArray* out, gfpdb_exec_stats* stats, void* stream);
 
+/* ------------------------------------------------------------ request server */
+
+/* The serving form: a request server on one GPU with an HBM-resident column
+ * cache, admission by HBM budget, worker threads on their own CUDA streams and
+ * continuous batching of star queries. It stands where the reference's query
+ * front end meets fpdb-cache (SegmentCache, fpdb-cache/src/SegmentCache.cpp:21-75,
+ * LFU policy fpdb-cache/src/policy/LFUCachingPolicy.cpp; CacheLoadPOp,
+ * fpdb-executor/src/physical/cache/CacheLoadPOp.cpp:64-261).
+ *
+ * Config JSON (every key optional):
+ *   {"device": 0, "workers": 4, "hbmBudgetBytes": 128849018880,
+ *    "cacheBytes": 107374182400, "maxBatch": 64, "batching": true,
+ *    "planStreams": 2, "cudaGraphs": true, "admissionTimeoutMs": 120000}
+ * Requests (JSON):
+ *   {"kind": "plan", "plan": <a plan as for gfpdb_execute_plan>}
+ *   {"kind": "star", "batch": <gfpdb_star_batch spec without "queries">,
+ *    "ranges": [[lo, hi], ...one per dimension]}
+ * Star requests with the same "batch" text are batched: when a worker frees
+ * up it takes the oldest request and every queued star request of the same
+ * batch (up to maxBatch) into one run; each request's result is exactly its
+ * own rows (group columns, then aggregates). Plan requests run one per
+ * worker, concurrently across workers. A request starts when its
+ * working-memory estimate fits hbmBudgetBytes - cacheBytes next to the
+ * requests already running (one request alone always starts). */
+typedef struct gfpdb_server gfpdb_server;
+
+typedef struct gfpdb_request_stats {
+  int32_t status;        /* GFPDB_OK or the request's error code */
+  int32_t batch_size;    /* requests that shared this request's launches */
+  int64_t submit_ns;     /* steady clock: submitted, started, finished */
+  int64_t start_ns;
+  int64_t end_ns;
+  int64_t kernel_launches;
+  int64_t cache_misses;  /* columns this request loaded into HBM */
+  int32_t worker;
+  int32_t pad;
+} gfpdb_request_stats;
+
+typedef struct gfpdb_server_stats {
+  int64_t submitted, completed, failed;
+  int64_t batches, batched_requests;
+  int64_t cache_hits, cache_misses, cache_evictions;
+  int64_t cache_bytes, cache_capacity, reserved_bytes, hbm_budget;
+  int64_t admission_waits;
+} gfpdb_server_stats;
+
+int32_t gfpdb_server_create(const char* config_json, gfpdb_server** out);
+/* Register a table held in host memory (ARROW_DEVICE_CPU or
+ * ARROW_DEVICE_CUDA_HOST); its buffers must stay valid until the server is
+ * destroyed. Columns are copied to HBM on first use. */
+int32_t gfpdb_server_register_table(gfpdb_server* server, const char* name, const struct ArrowSchema* schema,
+                                    const struct ArrowDeviceArray* array);
+int32_t gfpdb_server_submit(gfpdb_server* server, const char* request_json, uint64_t* ticket);
+/* Waits for a request (timeout_ms < 0: no limit; GFPDB_ETIMEDOUT when it is
+ * not finished in time). On success the result is a host array the caller
+ * releases (out_schema / out may be NULL to drop it); a failed request returns
+ * its error. A ticket can be collected once. */
+int32_t gfpdb_server_wait(gfpdb_server* server, uint64_t ticket, int64_t timeout_ms, struct ArrowSchema* out_schema,
+                          struct ArrowDeviceArray* out, gfpdb_request_stats* stats);
+int32_t gfpdb_server_get_stats(gfpdb_server* server, gfpdb_server_stats* out);
+/* Finishes the queued requests, then frees the server. */
+int32_t gfpdb_server_destroy(gfpdb_server* server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,6 +157,10 @@ def group_by(table: Table, group_cols: list[str], aggregates: list[dict]) -> Tab
     if n == 0:
         uniq_rows: list[tuple] = []
         inv = np.zeros(0, dtype=np.int64)
+    elif not group_cols:
+        # a non-grouped aggregate (AggregatePOp): one group of every row
+        uniq_rows = [()]
+        inv = np.zeros(n, dtype=np.int64)
     else:
         tuples = list(zip(*[k.tolist() for k in keys]))
         index: dict = {}

@@ -150,3 +150,20 @@ def test_gpu_groupby_golden(gpu):
     t = workloads.groupby_table(f["rows"], f["n_keys"], seed=f["seed"])
     got = plan.execute(workloads.groupby_plan(), {"t": t}).table
     groupby_check(f, got.rows())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [False, True])
+def test_gpu_csv_scan_plan_golden(gpu, graph):
+    """CsvScanPOp -> FilterPOp -> AggregatePOp as one plan."""
+    from flexpushdowndb_gb300 import plan
+    from flexpushdowndb_gb300.tupleset import text_table
+
+    f = fixture("csv_scan_20k")
+    text = workloads.lineitem_csv(f["rows"], f["seed"])
+    p = json.loads(workloads.csv_scan_plan().to_json())
+    p["cudaGraph"] = graph
+    for _ in range(2):
+        got = plan.execute(json.dumps(p), {"lineitem": text_table(text)}).table
+        assert got.names == ["sum_d2_i2", "cnt"]
+        assert got.rows() == [(f["sum_d2_i2"], f["selected"])]

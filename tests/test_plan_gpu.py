@@ -173,3 +173,31 @@ def test_streams_same_result(gpu, streams, graph, deferred):
 def test_streams_option_validated(gpu):
     with pytest.raises(GfpdbError):
         plan.execute(_with_options(workloads.star_plan(), streams=0), workloads.star_tables(fact_rows=1000))
+
+
+def test_aggregate_pop_matches_oracle(gpu):
+    """AggregatePOp: one row of non-grouped sums/counts/min/max; no rows in
+    (every row filtered out) gives no rows out."""
+    from flexpushdowndb_gb300.expression import col, lt, num_lit, times
+    from flexpushdowndb_gb300.ops import aggregate
+    from oracle import ops as oops
+
+    tabs = workloads.two_table_tables(fact_rows=300_000, seed=2500)
+    for cut in (25, 0):
+        p = plan.Plan()
+        p.scan("scan", "fact", ["fk", "qty", "price_cents"])
+        p.filter("f", "scan", lt(col("qty"), num_lit(cut)))
+        aggs = [aggregate("SUM", "rev", times(col("price_cents"), col("qty"))), aggregate("COUNT", "n"),
+                aggregate("MIN", "lo", col("price_cents")), aggregate("MAX", "hi", col("fk"))]
+        p.aggregate("agg", "f", aggs)
+        p.collate("collate", "agg")
+        got = plan.execute(p, tabs).table
+        sel = oops.filter_table(tabs["fact"], lt(col("qty"), num_lit(cut)))
+        if sel.num_rows == 0:
+            assert got.num_rows == 0
+            continue
+        want = oops.group_by(sel, [], [{"function": "SUM", "name": "rev", "expr": times(col("price_cents"), col("qty"))},
+                                        {"function": "COUNT", "name": "n"},
+                                        {"function": "MIN", "name": "lo", "expr": col("price_cents")},
+                                        {"function": "MAX", "name": "hi", "expr": col("fk")}])
+        assert got.rows() == want.rows()
