@@ -165,7 +165,7 @@ def _kernel_profile(L, _abi, fn, reps: int) -> dict:
     return out
 
 
-def batched_section(args, L, sptr) -> dict:
+def batched_section(args, L, sptr, tabs) -> dict:
     """The batched form: the star query's fact table as 64 partitions of
     log-uniform size (59,952,713 rows), 32 query variants with dimension
     filter ranges of 1%-40% selectivity each. Batched: one gfpdb_star_batch
@@ -177,13 +177,11 @@ def batched_section(args, L, sptr) -> dict:
     from flexpushdowndb_gb300 import _abi, batch, plan, workloads
     from flexpushdowndb_gb300.tupleset import DeviceTable
 
-    tabs = workloads.batch_tables()
     parts = [f"p{i}" for i in range(64)]
     qs = workloads.batch_queries(32)
     nq = len(qs)
     rows = sum(tabs[p].num_rows for p in parts)
     dev = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
-    del tabs
     spec = workloads.star_batch_spec(parts, qs)
     for _ in range(args.warmup):
         batch.star_batch(spec, dev, stream=sptr)
@@ -237,6 +235,140 @@ def batched_section(args, L, sptr) -> dict:
         "kernels_us_per_batch": {k: 1e3 * v["ms"] / 3 for k, v in kern.items()},
         "fact_kernel_fk_gbs": (fact["bytes"] / (fact["ms"] / 1e3) / 1e9) if fact else None,
         "settings": {k: spec[k] for k in ("itemsPerThread", "blocksPerSm", "loadFactor")},
+    }
+
+
+def serving_section(args, batch_tabs) -> dict:
+    """The serving form: Poisson arrivals of a request mix, swept over
+    offered rates, through the request server (4 workers on their own
+    streams, HBM column cache, admission by HBM budget, continuous batching
+    of star queries, graphs) and through the plain path (one worker, every
+    request its own per-operator plan, one stream, no batching). Latency is
+    the server's finish - submit time. Templates: star queries with range
+    filters over the 64-partition fact table (59,952,713 rows) and over its
+    first 16 partitions; the two-table query and the star query with
+    predicate transfer at 6,000,000 fact rows; the CSV scan over 2,000,000
+    lineitem rows (484 MB of text, parsed per request); a group-by over
+    20,000,000 rows with 10,000,000 Zipf(1.1) int64 keys."""
+    import numpy as np
+
+    from flexpushdowndb_gb300 import serving, workloads
+    from flexpushdowndb_gb300.tupleset import text_table
+
+    tables = dict(batch_tabs)
+    two = workloads.two_table_tables(fact_rows=6_000_000, seed=1000)
+    tables["fact"], tables["dim"] = two["fact"], two["dim"]
+    star = workloads.star_tables(fact_rows=6_000_000, seed=2000)
+    tables["sfact"] = star["fact"]
+    for i in range(1, 5):
+        tables[f"s{i}"] = star[f"d{i}"]
+    tables["g"] = workloads.groupby_table(20_000_000, 10_000_000)
+    csv_rows = 2_000_000
+    tables["lineitem"] = text_table(workloads.lineitem_csv(csv_rows, processes=os.cpu_count() or 1))
+    from flexpushdowndb_gb300.tupleset import export_host
+
+    tables = {k: export_host(v, pinned=True) for k, v in tables.items()}  # shared by every server below
+
+    parts64 = [f"p{i}" for i in range(64)]
+    parts16 = parts64[:16]
+    tmpl = {64: serving.star_batch_template(workloads.star_batch_spec(parts64, [])),
+            16: serving.star_batch_template(workloads.star_batch_spec(parts16, []))}
+    star_plan = json.loads(workloads.star_plan().to_json())
+    for o in star_plan["ops"]:
+        if o["type"] == "TableScanPOp":
+            o["table"] = "sfact" if o["table"] == "fact" else "s" + o["table"][1:]
+    two_plan = json.loads(workloads.two_table_plan().to_json())
+    csv_plan = json.loads(workloads.csv_scan_plan().to_json())
+    g_plan = json.loads(workloads.groupby_plan(groups_hint=8_000_000).to_json())
+    g_plan["ops"][0]["table"] = "g"
+    rng = np.random.default_rng(7000)
+    qranges = workloads.batch_queries(512, seed=7100)
+
+    def request(k, plain):
+        """The k-th request of the mix, as the served form or the plain form."""
+        u = rng.random()
+        if u < 0.72:  # star range query, 64 or 16 partitions
+            n = 64 if u < 0.54 else 16
+            q = qranges[k % len(qranges)]
+            if plain:
+                p = json.loads(workloads.star_plan(ranges=q, fact_tables=parts64 if n == 64 else parts16).to_json())
+                return {"kind": "plan", "plan": p}
+            return {"kind": "star", "batch": tmpl[n], "ranges": [list(r) for r in q]}
+        if u < 0.82:
+            return {"kind": "plan", "plan": two_plan}
+        if u < 0.92:
+            return {"kind": "plan", "plan": star_plan}
+        if u < 0.96:
+            return {"kind": "plan", "plan": csv_plan}
+        return {"kind": "plan", "plan": g_plan}
+
+    rates = [10, 100, 500, 1000, 2000, 4000, 8000]
+
+    def sweep(plain):
+        sv = serving.Server(workers=1 if plain else 4, batching=not plain, cuda_graphs=not plain,
+                            plan_streams=1 if plain else 2, cache_bytes=100 << 30, hbm_budget_bytes=140 << 30)
+        try:
+            for name, t in tables.items():
+                sv.register(name, t)
+            # warm-up: every template once (loads the cache, prepares batches)
+            rng.bit_generator.state = np.random.default_rng(7000).bit_generator.state
+            warm = [request(k, plain) for k in range(40)]
+            serving.run_load(sv, warm, [0.0] * len(warm))
+            out = []
+            for rate in rates:
+                n = int(min(rate * args.serve_seconds, 4000 if not plain else 600))
+                rng.bit_generator.state = np.random.default_rng(7000 + rate).bit_generator.state
+                gaps = rng.exponential(1.0 / rate, n)
+                arrivals = list(np.cumsum(gaps) - gaps[0])
+                reqs = [request(k, plain) for k in range(n)]
+                r = serving.run_load(sv, reqs, arrivals)
+                out.append({"offered_qps": rate, "requests": n, "achieved_qps": r.achieved_qps,
+                            "p50_ms": r.percentile(50), "p99_ms": r.percentile(99), "failed": r.failed,
+                            "mean_batch": float(np.mean(r.batch_sizes)) if r.batch_sizes else 0.0})
+                if r.achieved_qps < 0.6 * rate:
+                    break  # saturated: higher rates only grow the queue
+            st = sv.stats()
+        finally:
+            sv.close()
+        return out, st
+
+    def parity_check():
+        """A sample of requests served both ways: identical results."""
+        served_sv = serving.Server(workers=4, cache_bytes=100 << 30, hbm_budget_bytes=140 << 30)
+        plain_sv = serving.Server(workers=1, batching=False, cuda_graphs=False, plan_streams=1,
+                                  cache_bytes=100 << 30, hbm_budget_bytes=140 << 30)
+        try:
+            for name, t in tables.items():
+                served_sv.register(name, t)
+                plain_sv.register(name, t)
+            ok = True
+            for k in range(24):
+                state = np.random.default_rng(9000 + k).bit_generator.state
+                rng.bit_generator.state = state
+                a = request(k, False)
+                rng.bit_generator.state = state
+                b = request(k, True)
+                ta, tb = served_sv.submit(a), plain_sv.submit(b)
+                ok &= served_sv.wait(ta)[0].sorted_rows() == plain_sv.wait(tb)[0].sorted_rows()
+            return ok
+        finally:
+            served_sv.close()
+            plain_sv.close()
+
+    served, st_served = sweep(False)
+    plain, _ = sweep(True)
+    parity = parity_check()
+    return {
+        "workload": "Poisson arrivals; mix: 54% star range queries over 59,952,713 fact rows (64 partitions), "
+                    "18% over 16 partitions, 10% two-table query (6M fact), 10% star query with bloom transfer "
+                    "(6M fact), 4% CSV scan (2M lineitem rows of text, parsed per request), 4% group-by "
+                    "(20M rows, 10M Zipf(1.1) int64 keys)",
+        "served": served, "plain": plain, "parity_served_vs_plain": parity,
+        "server": {"workers": 4, "cache_bytes": 100 << 30, "hbm_budget_bytes": 140 << 30,
+                   "cache_hits": st_served["cache_hits"], "cache_misses": st_served["cache_misses"],
+                   "batches": st_served["batches"], "batched_requests": st_served["batched_requests"],
+                   "admission_waits": st_served["admission_waits"]},
+        "plain_path": "1 worker, every request its own per-operator plan on one stream, no batching, no graphs",
     }
 
 
@@ -318,6 +450,8 @@ def main():
     ap.add_argument("--parts", type=int, default=64, help="fact partitions of the batch case")
     ap.add_argument("--rows", type=int, default=FACT_ROWS)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form section")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-form section")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per offered rate")
     args = ap.parse_args()
     if args.case:
         return run_case(args)
@@ -479,7 +613,9 @@ def main():
     roofline_fact = roofline_of(fact_scan) if fact_scan else None
 
     # the batched form runs after the timed region, on every rank (replicas)
-    batched = None if args.no_batched else batched_section(args, L, sptr)
+    batch_tabs = None if (args.no_batched and args.no_serving) else workloads.batch_tables()
+    batched = None if args.no_batched else batched_section(args, L, sptr, batch_tabs)
+    serving = None if args.no_serving else serving_section(args, batch_tabs)
 
     if rank != 0:
         if dist is not None:
@@ -522,6 +658,7 @@ def main():
         "clocks": clocks.summary(),
         "cpu_baseline": base,
         "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -16,7 +16,7 @@ import time
 from dataclasses import dataclass
 
 from . import _abi
-from .tupleset import Table, export_host, import_result, new_output
+from .tupleset import Exported, Table, export_host, import_result, new_output
 
 
 class Server:
@@ -30,8 +30,11 @@ class Server:
         _abi.check(_abi.lib().gfpdb_server_create(json.dumps(cfg).encode(), ctypes.byref(self._h)))
         self._keep = []  # exported host tables: their buffers must outlive the server
 
-    def register(self, name: str, table: Table, pinned: bool = True) -> None:
-        ex = export_host(table, pinned=pinned)
+    def register(self, name: str, table, pinned: bool = True) -> None:
+        """Register a host Table (exported here, page-locked unless pinned is
+        False) or an already exported one (tupleset.export_host), which
+        several servers may share."""
+        ex = table if isinstance(table, Exported) else export_host(table, pinned=pinned)
         self._keep.append(ex)
         _abi.check(_abi.lib().gfpdb_server_register_table(self._h, name.encode(), ex.schema_ptr, ex.array_ptr))
 
