@@ -148,6 +148,14 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _nth_newline(text: bytes, n: int) -> int:
+    """Byte offset just past the n-th newline (the end of the first n rows)."""
+    import numpy as np
+
+    nl = np.flatnonzero(np.frombuffer(text, dtype=np.uint8) == 10)
+    return int(nl[n - 1]) + 1
+
+
 def _kernel_profile(L, _abi, fn, reps: int) -> dict:
     """Per-kernel event timings of `reps` calls of fn (profiling on)."""
     _abi.check(L.gfpdb_profile_reset())
@@ -246,7 +254,75 @@ def batched_section(args, L, sptr, tabs) -> dict:
     }
 
 
-def serving_section(args, batch_tabs) -> dict:
+def csv_section(args, L, text: bytes, rows: int) -> dict:
+    """The CSV form: 6,000,000 lineitem-shaped rows of '|'-delimited text
+    (16 fields: 4 int32, 4 decimal(15,2), 2 dates, 6 strings of 10-40
+    characters). Ingest: every field parsed into Arrow columns (int32, int64
+    cents, date32, utf8) from device-resident text, timed by CUDA events
+    around the parse kernels. Scan: the CsvScanPOp -> FilterPOp (three range
+    predicates, ~2% selected) -> AggregatePOp (sum(d2 * i2), count) plan,
+    from device-resident text and, end to end, from page-locked host text
+    (the text's host-to-device copy inside the timed region). The CPU
+    baseline parses the same text with the C restatement on every host
+    thread."""
+    from flexpushdowndb_gb300 import _abi, ops, plan, workloads
+    from flexpushdowndb_gb300.tupleset import DeviceTable, export_host, text_table
+    from oracle import cbaseline
+
+    tt = text_table(text, "text")
+    dev = DeviceTable.from_host(tt)
+    text_ptr = dev.tensors[0][1].data_ptr()
+
+    def ingest():
+        return ops.csv_read(len(text), workloads.LINEITEM_FIELDS, delimiter="|", device_ptr=text_ptr, to_host=False)
+
+    assert ingest() == rows
+    kern = _kernel_profile(L, _abi, ingest, 3)
+    csv_ms = sum(v["ms"] for v in kern.values()) / 3  # every kernel of the parse
+    t_ingest = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ingest()
+        t_ingest.append(time.perf_counter() - t0)
+    scan_text = workloads.csv_scan_plan().to_json()
+    dev_in = plan.PreparedInputs({"lineitem": dev})
+    host_in = plan.PreparedInputs({"lineitem": export_host(tt, pinned=True)})
+    got = plan.execute(scan_text, dev_in).table.rows()
+    for _ in range(2):
+        plan.execute(scan_text, dev_in)
+    t_scan, t_e2e = [], []
+    for _ in range(max(args.steps // 2, 5)):
+        t0 = time.perf_counter()
+        plan.execute(scan_text, dev_in)
+        t_scan.append(time.perf_counter() - t0)
+    plan.execute(scan_text, host_in)
+    for _ in range(5):
+        t0 = time.perf_counter()
+        plan.execute(scan_text, host_in)
+        t_e2e.append(time.perf_counter() - t0)
+    threads = os.cpu_count() or 1
+    cpu_t = []
+    cpu = None
+    t_end = time.perf_counter() + min(args.cpu_seconds, 10.0)
+    while not cpu_t or (time.perf_counter() < t_end and len(cpu_t) < 20):
+        t0 = time.perf_counter()
+        cpu = cbaseline.csv_scan(text, workloads.CSV_T1_RANGE, workloads.CSV_D1_LT, workloads.CSV_I1_LT, threads)
+        cpu_t.append(time.perf_counter() - t0)
+    ti, ts, te, tc = (statistics.median(x) for x in (t_ingest, t_scan, t_e2e, cpu_t))
+    return {
+        "workload": "%d lineitem-shaped rows, %d bytes of '|'-delimited text (16 fields)" % (rows, len(text)),
+        "ingest": {"rows_per_s": rows / (csv_ms / 1e3), "text_gbs": len(text) / (csv_ms / 1e3) / 1e9,
+                   "kernel_ms": csv_ms, "call_ms": 1e3 * ti,
+                   "kernels_ms": {k: v["ms"] / 3 for k, v in kern.items()}},
+        "scan": {"rows_per_s": rows / ts, "ms": 1e3 * ts, "result": got},
+        "scan_e2e": {"rows_per_s": rows / te, "ms": 1e3 * te, "h2d_bytes_per_step": len(text) + 8},
+        "cpu_baseline": {"rows_per_s": rows / tc, "ms": 1e3 * tc, "cores": threads, "kind": "port",
+                         "sample": f"the full {rows}-row scan, {len(cpu_t)} runs"},
+        "parity_vs_cpu": got == [tuple(cpu)] if cpu[1] else got == [],
+    }
+
+
+def serving_section(args, batch_tabs, csv_text_2m) -> dict:
     """The serving form: Poisson arrivals of a request mix, swept over
     offered rates, through the request server (4 workers on their own
     streams, HBM column cache, admission by HBM budget, continuous batching
@@ -271,8 +347,7 @@ def serving_section(args, batch_tabs) -> dict:
     for i in range(1, 5):
         tables[f"s{i}"] = star[f"d{i}"]
     tables["g"] = workloads.groupby_table(20_000_000, 10_000_000)
-    csv_rows = 2_000_000
-    tables["lineitem"] = text_table(workloads.lineitem_csv(csv_rows, processes=os.cpu_count() or 1))
+    tables["lineitem"] = text_table(csv_text_2m)
     from flexpushdowndb_gb300.tupleset import export_host
 
     tables = {k: export_host(v, pinned=True) for k, v in tables.items()}  # shared by every server below
@@ -459,6 +534,7 @@ def main():
     ap.add_argument("--rows", type=int, default=FACT_ROWS)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form section")
+    ap.add_argument("--no-csv", action="store_true", help="skip the CSV-form section")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per offered rate")
     args = ap.parse_args()
     if args.case:
@@ -628,7 +704,12 @@ def main():
     autotune_plan = autotune.tune_star_plan(plan_d, dev_inputs, cache=None)
     batch_tabs = None if (args.no_batched and args.no_serving) else workloads.batch_tables()
     batched = None if args.no_batched else batched_section(args, L, sptr, batch_tabs)
-    serving = None if args.no_serving else serving_section(args, batch_tabs)
+    csv_text = None if (args.no_csv and args.no_serving) else workloads.lineitem_csv(
+        6_000_000, processes=os.cpu_count() or 1)
+    csv = None if args.no_csv else csv_section(args, L, csv_text, 6_000_000)
+    # the serving form's CSV template reads the first 2,000,000 rows
+    cut = None if csv_text is None else _nth_newline(csv_text, 2_000_000)
+    serving = None if args.no_serving else serving_section(args, batch_tabs, csv_text[:cut])
 
     if rank != 0:
         if dist is not None:
@@ -671,6 +752,7 @@ def main():
         "clocks": clocks.summary(),
         "cpu_baseline": base,
         "autotune_star_plan": autotune_plan,
+        "csv": csv,
         "batched": batched,
         "serving": serving,
     }

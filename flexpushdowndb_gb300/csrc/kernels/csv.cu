@@ -298,8 +298,10 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   auto tile_off = make_buffer((n_tiles + 1) * 4, s);
   int64_t newlines = 0;
   if (n_tiles > 0) {
+    ProfScope prof("csv_newline_count_kernel", s);
     csv_newline_count_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(text, n_bytes, counts->as<int32_t>());
     after_launch("csv_newline_count_kernel");
+    prof.stop(static_cast<double>(n_bytes));
     newlines = exclusive_scan_i32(counts->as<int32_t>(), tile_off->as<int32_t>(), n_tiles, s);
   }
   // Last line without a trailing newline still counts as a row.
@@ -314,9 +316,11 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   auto starts = make_buffer((lines + 2) * 8, s);
   GF_CUDA(cudaMemsetAsync(starts->data(), 0, 8, s));
   if (n_tiles > 0) {
+    ProfScope prof("csv_row_starts_kernel", s);
     csv_row_starts_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(text, n_bytes, tile_off->as<int32_t>(),
                                                                            starts->as<int64_t>() + 1);
     after_launch("csv_row_starts_kernel");
+    prof.stop(static_cast<double>(n_bytes) + 8.0 * static_cast<double>(newlines));
   }
   if (last != '\n') {
     csv_tail_kernel<<<1, 1, 0, s>>>(starts->as<int64_t>(), lines, n_bytes + 1);
@@ -391,9 +395,11 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
     if (n_rows > 0 && total > 0) {
       int64_t blocks = (n_rows * 32 + 255) / 256;
       int64_t cap = static_cast<int64_t>(num_sms()) * 16;
+      ProfScope prof("csv_copy_strings_kernel", s);
       csv_copy_strings_kernel<<<static_cast<int>(blocks < cap ? blocks : cap), 256, 0, s>>>(
           text, sstart[k]->as<int64_t>(), offs->as<int32_t>(), bytes->as<uint8_t>(), n_rows);
       after_launch("csv_copy_strings_kernel");
+      prof.stop(2.0 * static_cast<double>(total) + 12.0 * static_cast<double>(n_rows));
     }
     cols.push_back(make_utf8_column(n_rows, offs, bytes));
   }

@@ -187,11 +187,14 @@ class Group:
             self._h = ctypes.c_void_p()
 
 
-def csv_read(text: bytes | np.ndarray, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
-             delimiter: str = ",", has_header: bool = False, device_ptr: int | None = None, stream=None) -> Table:
+def csv_read(text: bytes | np.ndarray | int, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
+             delimiter: str = ",", has_header: bool = False, device_ptr: int | None = None, stream=None,
+             to_host: bool = True):
     """Parse delimited text (CSVReader::read). ``fields`` lists (name, type)
     for every field of a line; a type "decimal(p,s)" parses into int64
-    scaled by 10^s."""
+    scaled by 10^s. With device_ptr, `text` is the byte count of device text.
+    With to_host False the parsed columns stay on the device and are
+    released; the row count is returned (for timing the ingest alone)."""
     schema_children = []
     for name, ty in fields:
         if ty.startswith("decimal"):
@@ -229,4 +232,8 @@ def csv_read(text: bytes | np.ndarray, fields: Sequence[tuple[str, str]], column
         nbytes, ptr, dev_type = buf.nbytes, buf.ctypes.data, _abi.ARROW_DEVICE_CPU
     _abi.check(_abi.lib().gfpdb_csv_read(ptr, nbytes, dev_type, delimiter.encode(), 1 if has_header else 0,
                                          ctypes.byref(sch), names, n, ctypes.byref(s), ctypes.byref(a), stream))
+    if not to_host:
+        from .tupleset import release_result
+
+        return release_result(s, a)
     return import_result(s, a)

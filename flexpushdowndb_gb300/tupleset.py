@@ -280,6 +280,16 @@ def new_output() -> tuple[_abi.ArrowSchema, _abi.ArrowDeviceArray]:
     return _abi.ArrowSchema(), _abi.ArrowDeviceArray()
 
 
+def release_result(schema: _abi.ArrowSchema, darr: _abi.ArrowDeviceArray) -> int:
+    """Release an exported TupleSet without copying it; returns its rows."""
+    n = darr.array.length
+    if darr.array.release:
+        darr.array.release(ctypes.pointer(darr.array))
+    if schema.release:
+        schema.release(ctypes.pointer(schema))
+    return n
+
+
 def import_result(schema: _abi.ArrowSchema, darr: _abi.ArrowDeviceArray, release: bool = True) -> Table:
     """Copy an exported TupleSet (device or host) into a host Table and
     release the library's structures."""

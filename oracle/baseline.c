@@ -258,3 +258,117 @@ int64_t orc_star_query(const orc_star_fact* fact, const orc_star_dim* dims, cons
   free(rows);
   return ng;
 }
+
+/*
+ * CPU restatement of the CSV scan workload (lineitem-shaped '|'-delimited
+ * text): parse the projected fields of each line the way CSVReader's parser
+ * does (fpdb-tuple/src/csv/CSVToArrowSIMDChunkParser.cpp:183-374: split on
+ * the delimiter, then convert each projected field), keep the rows with
+ * t_lo <= t1 <= t_hi, d1 < d1_lt and i1 < i1_lt, and sum d2 * i2 (decimals as
+ * int64 cents, dates as days since 1970-01-01). The text is split into
+ * `threads` line-aligned ranges.
+ */
+typedef struct {
+  const char* b;
+  const char* e;
+  int64_t t_lo, t_hi, d1_lt, i1_lt;
+  int64_t sum, cnt;
+} csv_job;
+
+static int64_t csv_int(const char* p, const char* e) {
+  int neg = 0;
+  if (p < e && (*p == '-' || *p == '+')) neg = *p++ == '-';
+  int64_t v = 0;
+  while (p < e && *p >= '0' && *p <= '9') v = v * 10 + (*p++ - '0');
+  return neg ? -v : v;
+}
+
+static int64_t csv_cents(const char* p, const char* e) {
+  int neg = 0;
+  if (p < e && (*p == '-' || *p == '+')) neg = *p++ == '-';
+  int64_t v = 0;
+  while (p < e && *p >= '0' && *p <= '9') v = v * 10 + (*p++ - '0');
+  int64_t f = 0, k = 0;
+  if (p < e && *p == '.') {
+    ++p;
+    while (p < e && k < 2 && *p >= '0' && *p <= '9') {
+      f = f * 10 + (*p++ - '0');
+      ++k;
+    }
+  }
+  while (k < 2) {
+    f *= 10;
+    ++k;
+  }
+  v = v * 100 + f;
+  return neg ? -v : v;
+}
+
+/* days since 1970-01-01 (H. Hinnant's days_from_civil) */
+static int64_t csv_days(const char* p) {
+  int64_t y = csv_int(p, p + 4), m = csv_int(p + 5, p + 7), d = csv_int(p + 8, p + 10);
+  y -= m <= 2;
+  const int64_t era = (y >= 0 ? y : y - 399) / 400;
+  const int64_t yoe = y - era * 400;
+  const int64_t doy = (153 * (m > 2 ? m - 3 : m + 9) + 2) / 5 + d - 1;
+  const int64_t doe = yoe * 365 + yoe / 4 - yoe / 100 + doy;
+  return era * 146097 + doe - 719468;
+}
+
+static void* csv_range(void* arg) {
+  csv_job* j = (csv_job*)arg;
+  const char* p = j->b;
+  while (p < j->e) {
+    const char* f[17];
+    int nf = 0;
+    f[nf++] = p;
+    while (p < j->e && *p != '\n') {
+      if (*p == '|' && nf < 17) f[nf++] = p + 1;
+      ++p;
+    }
+    const char* eol = p;
+    if (p < j->e) ++p;  /* past '\n' */
+    if (nf < 16) continue;
+    const int64_t i1 = csv_int(f[0], f[1] - 1), i2 = csv_int(f[1], f[2] - 1);
+    const int64_t d1 = csv_cents(f[4], f[5] - 1), d2 = csv_cents(f[5], f[6] - 1);
+    const int64_t t1 = csv_days(f[8]);
+    (void)eol;
+    if (t1 >= j->t_lo && t1 <= j->t_hi && d1 < j->d1_lt && i1 < j->i1_lt) {
+      j->sum = (int64_t)((uint64_t)j->sum + (uint64_t)d2 * (uint64_t)i2);
+      j->cnt += 1;
+    }
+  }
+  return NULL;
+}
+
+int64_t orc_csv_scan(const char* text, int64_t n, int64_t t_lo, int64_t t_hi, int64_t d1_lt, int64_t i1_lt,
+                     int threads, int64_t* sum_out) {
+  if (threads < 1) threads = 1;
+  csv_job* jobs = (csv_job*)calloc((size_t)threads, sizeof(csv_job));
+  pthread_t* tids = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+  const char* end = text + n;
+  const char* at = text;
+  for (int t = 0; t < threads; ++t) {
+    const char* e = t == threads - 1 ? end : text + (n / threads) * (t + 1);
+    if (e < at) e = at;
+    while (e < end && e > text && e[-1] != '\n') ++e; /* line-aligned */
+    jobs[t].b = at;
+    jobs[t].e = e;
+    jobs[t].t_lo = t_lo;
+    jobs[t].t_hi = t_hi;
+    jobs[t].d1_lt = d1_lt;
+    jobs[t].i1_lt = i1_lt;
+    at = e;
+  }
+  for (int t = 0; t < threads; ++t) pthread_create(&tids[t], NULL, csv_range, &jobs[t]);
+  int64_t sum = 0, cnt = 0;
+  for (int t = 0; t < threads; ++t) {
+    pthread_join(tids[t], NULL);
+    sum = (int64_t)((uint64_t)sum + (uint64_t)jobs[t].sum);
+    cnt += jobs[t].cnt;
+  }
+  free(jobs);
+  free(tids);
+  *sum_out = sum;
+  return cnt;
+}

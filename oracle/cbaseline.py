@@ -83,3 +83,16 @@ def star_query(inputs: StarInputs, consts=(1, 3, 2, 5), bits: int = 10, nh: int 
     return Table([Column("d2_g", "int32", g2[:n]), Column("d4_g", "int32", g4[:n]),
                   Column("revenue", "int64", rev[:n]), Column("discount_revenue", "int64", drev[:n]),
                   Column("cnt", "int64", cnt[:n])])
+
+
+def csv_scan(text: bytes, t_range, d1_lt: int, i1_lt: int, threads: int | None = None) -> tuple[int, int]:
+    """(sum(d2 * i2), count) of the CSV scan workload, parsed by the C
+    restatement on `threads` host threads."""
+    threads = threads or os.cpu_count() or 1
+    L = lib()
+    L.orc_csv_scan.restype = ctypes.c_int64
+    s = ctypes.c_int64()
+    buf = ctypes.c_char_p(text)
+    n = L.orc_csv_scan(buf, ctypes.c_int64(len(text)), ctypes.c_int64(t_range[0]), ctypes.c_int64(t_range[1]),
+                       ctypes.c_int64(d1_lt), ctypes.c_int64(i1_lt), ctypes.c_int(threads), ctypes.byref(s))
+    return s.value, n

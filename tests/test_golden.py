@@ -167,3 +167,17 @@ def test_gpu_csv_scan_plan_golden(gpu, graph):
         got = plan.execute(json.dumps(p), {"lineitem": text_table(text)}).table
         assert got.names == ["sum_d2_i2", "cnt"]
         assert got.rows() == [(f["sum_d2_i2"], f["selected"])]
+
+
+def test_c_baselines_golden():
+    """The timed CPU baselines (oracle/baseline.c) reproduce the fixtures."""
+    from oracle import cbaseline
+
+    f = fixture("csv_scan_20k")
+    text = workloads.lineitem_csv(f["rows"], f["seed"])
+    s, n = cbaseline.csv_scan(text, workloads.CSV_T1_RANGE, workloads.CSV_D1_LT, workloads.CSV_I1_LT, threads=3)
+    assert (s, n) == (f["sum_d2_i2"], f["selected"])
+    f = fixture("star_120k")
+    tabs = workloads.star_tables(fact_rows=f["fact_rows"], seed=f["seed"])
+    got = cbaseline.star_query(cbaseline.StarInputs(tabs), consts=tuple(f["consts"]), threads=3)
+    assert got.sorted_rows() == rows(f["rows"])
