@@ -1,0 +1,60 @@
+"""The multi-rank path on CPU: two gloo ranks, each computing the star
+query over its own fact partitions (with the oracle, standing in for its
+GPU), merge their partial group tables; the merge equals the query over all
+partitions. Also the merge alone, with int64 wrap-around."""
+
+import os
+import socket
+
+import pytest
+
+from flexpushdowndb_gb300 import distributed, workloads
+from flexpushdowndb_gb300.tupleset import Column, Table
+
+
+def test_merge_partials_wraps_and_groups():
+    a = Table([Column("g", "int32", [1, 2]), Column("s", "int64", [2**62, 5]), Column("c", "int64", [1, 1])])
+    b = Table([Column("g", "int32", [2, 1]), Column("s", "int64", [7, 2**62]), Column("c", "int64", [2, 3])])
+    m = distributed.merge_partials([a, b, Table([])], ["g"], ["s", "c"])
+    got = dict((r[0], r[1:]) for r in m.rows())
+    assert got[1] == (-(2**63), 4)  # 2^62 + 2^62 wraps to -2^63
+    assert got[2] == (12, 3)
+
+
+def test_rank_partitions_cover_all():
+    parts = [distributed.rank_partitions(10, r, 3) for r in range(3)]
+    assert sorted(sum(parts, [])) == list(range(10))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_path):
+    import torch.distributed as dist
+
+    from oracle import queries
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sizes = workloads.batch_partition_sizes(6, lo=2_000, hi=40_000, seed=9100)
+    tabs = workloads.batch_tables(6, sizes=sizes, seed=9100)
+    ranges = [(0, 39), (0, 24), (3, 50), (0, 99)]
+    mine = [f"p{i}" for i in distributed.rank_partitions(6, rank, world)]
+    partial = queries.star_query_ranges(tabs, mine, ranges)
+    merged = distributed.gather_and_merge(partial, ["d2_g", "d4_g"], ["revenue", "discount_revenue", "cnt"])
+    if rank == 0:
+        want = queries.star_query_ranges(tabs, [f"p{i}" for i in range(6)], ranges)
+        with open(out_path, "w") as f:
+            f.write("ok" if merged.sorted_rows() == want.sorted_rows() else "mismatch")
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_merge_star_partials(tmp_path):
+    torch_mp = pytest.importorskip("torch.multiprocessing")
+    out = tmp_path / "result.txt"
+    torch_mp.spawn(_rank_main, args=(2, _free_port(), str(out)), nprocs=2, join=True)
+    assert out.read_text() == "ok"
