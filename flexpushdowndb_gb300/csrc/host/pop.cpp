@@ -337,18 +337,55 @@ class HashJoinArrowPOp : public PhysicalOp {
 
   void probe(const TupleSetPtr& ts) {
     const int pk = ts->require_column(probe_key_);
-    BufferPtr pidx, bidx, count_owner;
-    const int64_t* count_dev = nullptr;
-    int64_t n = 0;
-    join_probe_pairs(table_, *ts, pk, &pidx, &bidx, &n, ctx()->stream(), &count_owner, &count_dev);
-    // Output: probe fields then build fields (HashJoinArrowKernel.cpp:148-162),
-    // each filtered to the needed columns.
-    std::vector<GatherSpec> specs;
-    std::vector<Field> fields;
     auto needed = [&](const std::string& c) {
       return projectColumnNames_.empty() ||
              std::find(projectColumnNames_.begin(), projectColumnNames_.end(), c) != projectColumnNames_.end();
     };
+    // Output: probe fields then build fields (HashJoinArrowKernel.cpp:148-162),
+    // each filtered to the needed columns.
+    {
+      std::vector<Field> fields;
+      std::vector<int> pcols, bcols;
+      bool fixed = true;
+      for (int i = 0; i < ts->num_columns(); ++i)
+        if (needed(ts->field(i).name)) {
+          fields.push_back(ts->field(i));
+          pcols.push_back(i);
+          fixed &= ts->field(i).type != DType::Utf8;
+        }
+      const TupleSet& b = *table_.build;
+      for (int i = 0; i < b.num_columns(); ++i)
+        if (needed(b.field(i).name)) {
+          for (auto& f : fields)
+            if (f.name == b.field(i).name)
+              fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': column '" + f.name + "' is on both sides");
+          fields.push_back(b.field(i));
+          bcols.push_back(i);
+          fixed &= b.field(i).type != DType::Utf8;
+        }
+      if (fixed) {
+        // fixed-width outputs: probe and materialise in one kernel
+        BufferPtr count_owner;
+        const int64_t* count_dev = nullptr;
+        int64_t n = 0;
+        auto cols = join_probe_materialize(table_, *ts, pk, pcols, bcols, &n, ctx()->stream(), &count_owner,
+                                           &count_dev);
+        Message out;
+        out.type = MessageType::TUPLESET;
+        if (count_dev != nullptr)
+          out.tuples = TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev);
+        else
+          out.tuples = TupleSet::make(std::move(fields), std::move(cols), n);
+        ctx()->tell(out);
+        return;
+      }
+    }
+    BufferPtr pidx, bidx, count_owner;
+    const int64_t* count_dev = nullptr;
+    int64_t n = 0;
+    join_probe_pairs(table_, *ts, pk, &pidx, &bidx, &n, ctx()->stream(), &count_owner, &count_dev);
+    std::vector<GatherSpec> specs;
+    std::vector<Field> fields;
     for (int i = 0; i < ts->num_columns(); ++i)
       if (needed(ts->field(i).name)) {
         fields.push_back(ts->field(i));

@@ -115,6 +115,86 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Probe and materialise in one pass: every match writes its output row
+// directly (probe columns from the probe row, build columns from the build
+// row) at a position claimed with one warp-aggregated atomic, so no pair
+// buffer and no separate gather launch are needed. Fixed-width columns only.
+constexpr int kJoinOutMax = 24;
+
+struct JoinEmitParams {
+  DevCol pkey;
+  DevCol bkey;
+  int64_t n_cap;
+  const int64_t* n_dev;
+  const uint64_t* slots;
+  uint64_t mask;
+  int64_t cap;
+  DevStatus* st;
+  int32_t key32;
+  int32_t n_out;
+  const void* src[kJoinOutMax];
+  void* dst[kJoinOutMax];
+  int32_t width[kJoinOutMax];
+  int32_t from_build[kJoinOutMax];
+};
+
+__global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_constant__ JoinEmitParams p) {
+  const int64_t n = clamp_rows(p.n_dev, p.n_cap);
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(&p.st->value);
+  for (int64_t base = warp_global * 32; base < n; base += n_warps * 32) {
+    const int64_t r = base + lane;
+    bool active = r < n;
+    int64_t k = 0;
+    uint32_t tag = 0;
+    uint64_t slot = 0;
+    if (active) {
+      k = load_int(p.pkey, r);
+      const uint64_t h = hash_key(k);
+      tag = p.key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
+      slot = h & p.mask;
+    }
+    uint64_t steps = 0;
+    while (__any_sync(0xffffffffu, active)) {
+      bool emit = false;
+      int32_t brow = 0;
+      if (active) {
+        const uint64_t s = __ldg(reinterpret_cast<const unsigned long long*>(p.slots + slot));
+        if (s == kEmptySlot || ++steps > p.mask + 1) {
+          active = false;
+        } else {
+          if (static_cast<uint32_t>(s >> 32) == tag) {
+            brow = static_cast<int32_t>(static_cast<uint32_t>(s));
+            emit = p.key32 ? true : (load_int(p.bkey, brow) == k);
+          }
+          slot = (slot + 1) & p.mask;
+        }
+      }
+      const uint32_t em = __ballot_sync(0xffffffffu, emit);
+      if (em != 0) {
+        unsigned long long at = 0;
+        const int leader = __ffs(em) - 1;
+        if (lane == leader) at = atomicAdd(cursor, static_cast<unsigned long long>(__popc(em)));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (emit) {
+          const int64_t pos = static_cast<int64_t>(at) + __popc(em & ((1u << lane) - 1u));
+          if (pos < p.cap) {
+            for (int c = 0; c < p.n_out; ++c) {
+              const int64_t from = p.from_build[c] ? brow : r;
+              if (p.width[c] == 8)
+                static_cast<long long*>(p.dst[c])[pos] = __ldg(static_cast<const long long*>(p.src[c]) + from);
+              else
+                static_cast<int*>(p.dst[c])[pos] = __ldg(static_cast<const int*>(p.src[c]) + from);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 int grid_for(int64_t n) {
   int64_t blocks = (n + 255) / 256;
   int64_t cap = static_cast<int64_t>(num_sms()) * 8;
@@ -146,6 +226,89 @@ void join_build_table(JoinTable& t, double load_factor, cudaStream_t s) {
     after_launch("join_build_kernel");
     prof.stop(static_cast<double>(n) * dtype_width(kc->type));
   }
+}
+
+std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet& probe, int probe_key,
+                                              const std::vector<int>& probe_cols, const std::vector<int>& build_cols,
+                                              int64_t* n_out, cudaStream_t s, BufferPtr* count_owner,
+                                              const int64_t** count_dev) {
+  const int64_t n = probe.num_rows();
+  if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join probe batch must have fewer than 2^31 rows");
+  const auto& pc = probe.column(probe_key);
+  if (pc->type == DType::Utf8 || pc->type == DType::Float64)
+    fail(GFPDB_EUNSUPPORTED, "hash join keys must be integer columns");
+  const bool key32 = t.key_type != DType::Int64 && pc->type != DType::Int64;
+  if (!key32 && t.key_type != DType::Int64)
+    fail(GFPDB_EUNSUPPORTED, "int64 probe key against an int32 build key");
+  if (probe_cols.size() + build_cols.size() > static_cast<size_t>(kJoinOutMax))
+    fail(GFPDB_EUNSUPPORTED, "too many hash join output columns");
+  const auto& bk = t.build->column(t.key_col);
+  JoinEmitParams p{};
+  p.pkey = DevCol{pc->data, nullptr, static_cast<int32_t>(pc->type), 0};
+  p.bkey = DevCol{bk->data, nullptr, static_cast<int32_t>(bk->type), 0};
+  p.n_cap = n;
+  p.n_dev = probe.rows_dev();
+  p.slots = t.slots->as<uint64_t>();
+  p.mask = t.capacity - 1;
+  p.key32 = key32 ? 1 : 0;
+  std::vector<const Column*> srcs;
+  std::vector<int> from_build;
+  for (int c : probe_cols) {
+    srcs.push_back(probe.column(c).get());
+    from_build.push_back(0);
+  }
+  for (int c : build_cols) {
+    srcs.push_back(t.build->column(c).get());
+    from_build.push_back(1);
+  }
+  p.n_out = static_cast<int32_t>(srcs.size());
+  auto status = make_buffer(sizeof(DevStatus), s);
+  const bool defer = deferred_mode() && count_dev != nullptr;
+  int64_t cap = n > 0 ? n : 1;
+  std::vector<BufferPtr> bufs(srcs.size());
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    for (size_t c = 0; c < srcs.size(); ++c) {
+      if (srcs[c]->type == DType::Utf8) fail(GFPDB_EUNSUPPORTED, "utf8 output in the fused join");
+      const int w = dtype_width(srcs[c]->type);
+      bufs[c] = make_buffer(cap * w, s);
+      p.src[c] = srcs[c]->data;
+      p.dst[c] = bufs[c]->data();
+      p.width[c] = w;
+      p.from_build[c] = from_build[c];
+    }
+    p.cap = cap;
+    p.st = status->as<DevStatus>();
+    GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    if (n > 0 && t.build->num_rows() > 0) {
+      ProfScope prof("join_probe_emit_kernel", s);
+      join_probe_emit_kernel<<<grid_for(n), 256, 0, s>>>(p);
+      after_launch("join_probe_emit_kernel");
+      prof.stop(0);
+      double w_out = 0;
+      for (size_t c = 0; c < srcs.size(); ++c) w_out += 2.0 * p.width[c];
+      prof.set_bytes_model(probe.rows_dev(), n, dtype_width(pc->type), &status->as<DevStatus>()->value, w_out, status,
+                           probe.rows_owner());
+    }
+    if (defer) {
+      defer_check(status, status->as<DevStatus>(), "hash join probe", cap);
+      *n_out = cap;
+      *count_dev = &status->as<DevStatus>()->value;
+      if (count_owner) *count_owner = status;
+      break;
+    }
+    DevStatus hs;
+    GF_CUDA(cudaMemcpyAsync(&hs, status->data(), sizeof(hs), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    raise_device_status(hs, "hash join probe");
+    if (hs.value <= cap) {
+      *n_out = hs.value;
+      break;
+    }
+    cap = hs.value;  // more matches than probe rows (repeated build keys): once more, exactly sized
+  }
+  std::vector<ColumnPtr> cols;
+  for (size_t c = 0; c < srcs.size(); ++c) cols.push_back(make_fixed_column(srcs[c]->type, *n_out, bufs[c]));
+  return cols;
 }
 
 void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,

@@ -103,6 +103,15 @@ void join_build_table(JoinTable& t, double load_factor, cudaStream_t s);
 // and deferred mode on, nothing waits: *n_out is the pairs' capacity (the
 // probe's row capacity, enough when build keys are unique), *count_dev the
 // device count, and an overflow is detected by the plan's final checks.
+// Probe and materialise fixed-width output columns in one pass: probe
+// columns `probe_cols` (indexes into probe) then build columns `build_cols`
+// (indexes into t.build). In deferred mode (count_dev given) the row count
+// stays on the device; an overflow (repeated build keys) is reported by the
+// deferred checks.
+std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet& probe, int probe_key,
+                                              const std::vector<int>& probe_cols, const std::vector<int>& build_cols,
+                                              int64_t* n_out, cudaStream_t s, BufferPtr* count_owner = nullptr,
+                                              const int64_t** count_dev = nullptr);
 void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,
                       BufferPtr* build_idx, int64_t* n_out, cudaStream_t s, BufferPtr* count_owner = nullptr,
                       const int64_t** count_dev = nullptr);

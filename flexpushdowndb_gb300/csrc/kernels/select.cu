@@ -396,6 +396,38 @@ struct SpLayout {
   int32_t bloom_off;              // byte offset of the staged filter in dynamic shared memory
 };
 
+// Bloom test of 8 keys against one filter with NH hashes: bit positions
+// from the low 32 bits of each key's hash (bloom.cuh). `blocks` is the
+// filter in shared memory (in_smem) or global memory.
+template <int NH>
+__device__ __forceinline__ uint32_t probe8(const uint32_t* blocks, bool in_smem, uint32_t nb, const int64_t keys[8],
+                                           uint32_t mask) {
+  uint32_t keep = 0;
+#pragma unroll
+  for (int kk = 0; kk < kSelItems; ++kk) {
+    if (!((mask >> kk) & 1u)) continue;
+    const uint64_t h = hash_key(keys[kk]);
+    const uint32_t* blk = blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8;
+    const uint32_t lo = static_cast<uint32_t>(h);
+    bool ok = true;
+    if (in_smem) {
+#pragma unroll
+      for (int i = 0; i < NH; ++i) {
+        const uint32_t b = (lo >> (8 * i)) & 0xFFu;
+        ok &= (blk[b >> 5] >> (b & 31)) & 1u;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NH; ++i) {
+        const uint32_t b = (lo >> (8 * i)) & 0xFFu;
+        ok &= (__ldg(blk + (b >> 5)) >> (b & 31)) & 1u;
+      }
+    }
+    keep |= static_cast<uint32_t>(ok) << kk;
+  }
+  return keep;
+}
+
 __device__ __forceinline__ uint32_t sp_seg_bytes(const SpLayout& L, int pi, int64_t rows) {
   return static_cast<uint32_t>((rows * L.key_width[pi]) & ~int64_t{15});
 }
@@ -558,10 +590,17 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
 #pragma unroll
         for (int kk = 0; kk < kSelItems; ++kk) keys[kk] = (mask >> kk) & 1u ? key_at(first, r_in + kk) : 0;
       }
-      uint32_t keep = 0;
-#pragma unroll
-      for (int kk = 0; kk < kSelItems; ++kk)
-        if ((mask >> kk) & 1u) keep |= static_cast<uint32_t>(probe_hit(first, keys[kk])) << kk;
+      // the first probe's filter parameters, read once per tile
+      const BloomDev& b0 = p.probes[0];
+      const uint32_t nb0 = s_nblocks[0];
+      const uint32_t* blocks0 = (staged & 1u) ? s_bloom + b0.smem_word : b0.blocks;
+      uint32_t keep;
+      switch (b0.num_hashes) {
+        case 1: keep = probe8<1>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
+        case 2: keep = probe8<2>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
+        case 3: keep = probe8<3>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
+        default: keep = probe8<4>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
+      }
       mask &= keep;
     }
     // (2) the survivors, in row order, into this warp's list
