@@ -322,6 +322,57 @@ def csv_section(args, L, text: bytes, rows: int) -> dict:
     }
 
 
+def micro_section() -> dict:
+    """Operator micro-benchmarks in the reference's shapes
+    (fpdb-executor/bench/BloomFilterBenchmark.cpp:91-127,
+    HashJoinBenchmark.cpp:99-131): tables of 10 int64 columns; bloom create
+    over R rows with keys uniform on [0, 2R]; bloom use of R rows (keys
+    uniform on [0, 2000]) against a filter of 10,000 keys uniform on
+    [0, 1000]; hash join of L build x R probe rows on the first column (keys
+    uniform on [0, 2R]) keeping three probe and two build columns. Device-resident inputs; median wall time per call
+    of the C ABI (every call synchronizes its stream)."""
+    import numpy as np
+
+    from flexpushdowndb_gb300 import ops
+    from flexpushdowndb_gb300.tupleset import Column, DeviceTable, Table
+
+    rng = np.random.default_rng(11000)
+
+    def table(rows, hi, prefix="c"):
+        cols = [Column(f"{prefix}_0", "int64", rng.integers(0, hi + 1, rows))]
+        cols += [Column(f"{prefix}_{i}", "int64", rng.integers(0, 1 << 40, rows)) for i in range(1, 10)]
+        return DeviceTable.from_host(Table(cols))
+
+    def med(fn, reps=20):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return 1e6 * statistics.median(ts)
+
+    out = {"bloom_create_us": {}, "bloom_use_us": {}, "hash_join_us": {}}
+    for r in (10, 100, 1000, 10_000, 100_000, 1_000_000):
+        t = table(r, 2 * r)
+        out["bloom_create_us"][str(r)] = med(lambda: ops.BloomFilter([t], "c_0"))
+    bf = ops.BloomFilter([table(10_000, 1000)], "c_0")
+    for r in (10, 100, 1000, 10_000, 100_000, 1_000_000):
+        t = table(r, 2000)
+        out["bloom_use_us"][str(r)] = med(lambda: bf.use(t, "c_0"))
+    for left, right in ((10, 100), (10, 1000), (10, 10_000), (100, 1000), (100, 10_000), (1000, 10_000)):
+        lt, rt = table(left, 2 * right, "b"), table(right, 2 * right)
+
+        def join():
+            j = ops.HashJoin("b_0", "c_0", ["c_0", "c_1", "c_2", "b_1", "b_2"])
+            j.put_build(lt)
+            j.finalize_build()
+            return j.probe(rt)
+
+        out["hash_join_us"][f"{left}x{right}"] = med(join)
+    return out
+
+
 def serving_section(args, batch_tabs, csv_text_2m) -> dict:
     """The serving form: Poisson arrivals of a request mix, swept over
     offered rates, through the request server (4 workers on their own
@@ -535,6 +586,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form section")
     ap.add_argument("--no-csv", action="store_true", help="skip the CSV-form section")
+    ap.add_argument("--no-micro", action="store_true", help="skip the operator micro-benchmarks")
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per offered rate")
     args = ap.parse_args()
     if args.case:
@@ -707,6 +759,7 @@ def main():
     csv_text = None if (args.no_csv and args.no_serving) else workloads.lineitem_csv(
         6_000_000, processes=os.cpu_count() or 1)
     csv = None if args.no_csv else csv_section(args, L, csv_text, 6_000_000)
+    micro = None if args.no_micro else micro_section()
     # the serving form's CSV template reads the first 2,000,000 rows
     cut = None if csv_text is None else _nth_newline(csv_text, 2_000_000)
     serving = None if args.no_serving else serving_section(args, batch_tabs, csv_text[:cut])
@@ -719,6 +772,13 @@ def main():
     if world == 1 and not args.no_cpu_baseline:
         b = cpu_baseline(tables, 3, 1, budget_s=args.cpu_seconds)
         base = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # the same C port on one thread (SURVEY: "1 thread and all cores")
+        from oracle import cbaseline
+
+        inp = cbaseline.StarInputs(tables)
+        t0 = time.perf_counter()
+        cbaseline.star_query(inp, threads=1)
+        base["one_thread_value"] = FACT_ROWS / (time.perf_counter() - t0)
     lat = sorted(per_step)
     plat = sorted(plain_steps)
     line = {
@@ -753,6 +813,7 @@ def main():
         "cpu_baseline": base,
         "autotune_star_plan": autotune_plan,
         "csv": csv,
+        "micro": micro,
         "batched": batched,
         "serving": serving,
     }

@@ -16,12 +16,18 @@
 // (days since 1970-01-01 by Howard Hinnant's public-domain days_from_civil
 // algorithm), and utf8 (bytes copied as they are).
 //
-// Kernels: (1) newline count per 64 KiB tile, (2) prefix sum, (3) row start
-// offsets, written in input order with one block scan per 4 KiB step,
-// (4) per block of 256 rows: each thread splits its row into field offsets in
-// shared memory, then the block converts fields column by column so output
-// stores are coalesced; utf8 fields record their length and start, and
-// (5) after a prefix sum of the lengths, a copy kernel moves the bytes.
+// Kernels: the text is cut into 16 KiB tiles of 256 threads x 64 bytes (read
+// with 128-bit loads). A separator is a delimiter or a newline; in a
+// well-formed text every row has n_fields separators, so the field that ends
+// at the g-th separator of the text is row g / n_fields, field g % n_fields.
+// (1) csv_index_kernel: per tile, the separator count and the position of its
+// last separator; (2) csv_tile_scan_kernel: each tile's first separator
+// ordinal and the position of the separator before it; (3) csv_fields_kernel:
+// every thread finds the separators of its 64 bytes, ranks them with block
+// scans, and converts the field ending at each one (a newline at any
+// position but the last field of a row marks the row malformed); utf8 fields
+// record their length and start, and (4) after a prefix sum of the lengths a
+// copy kernel moves the bytes.
 #include <cstring>
 
 #include "common.cuh"
@@ -32,61 +38,139 @@ namespace gfpdb {
 namespace {
 
 constexpr int kCsvThreads = 256;
-constexpr int kCsvTileBytes = 65536;
-constexpr int kStepBytes = kCsvThreads * 16;
+constexpr int kCsvChunk = 64;                               // bytes per thread
+constexpr int kCsvTile = kCsvThreads * kCsvChunk;           // bytes per tile
+constexpr int kCsvScanThreads = 1024;
 
-__global__ void __launch_bounds__(kCsvThreads)
-    csv_newline_count_kernel(const uint8_t* __restrict__ text, int64_t n, int32_t* __restrict__ counts) {
-  const int64_t base = static_cast<int64_t>(blockIdx.x) * kCsvTileBytes;
-  int c = 0;
-  for (int step = 0; step < kCsvTileBytes / kStepBytes; ++step) {
-    const int64_t at = base + static_cast<int64_t>(step) * kStepBytes + threadIdx.x * 16;
-    if (at + 16 <= n) {
-      const uint4 v = __ldg(reinterpret_cast<const uint4*>(text + at));
-      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+// Block-wide exclusive scan of one int64 per thread under `op` (sum or max)
+// with identity `id`; *total gets the reduction over the block.
+template <int NT, typename Op>
+__device__ __forceinline__ int64_t block_scan64(int64_t x, int64_t id, Op op, int64_t* total, int64_t* s_w) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = NT / 32;
+  int64_t incl = x;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        // bytes equal to '\n' (0x0A): classic has-zero-byte test on w ^ 0x0A0A0A0A
-        const uint32_t x = w[k] ^ 0x0A0A0A0Au;
-        const uint32_t z = (x - 0x01010101u) & ~x & 0x80808080u;
-        // The test can flag a 0x0B byte right after a real match; count exactly instead.
-        if (z != 0) {
-#pragma unroll
-          for (int b = 0; b < 4; ++b) c += ((w[k] >> (8 * b)) & 0xFFu) == 0x0Au;
-        }
-      }
-    } else {
-      for (int64_t i = at; i < at + 16 && i < n; ++i) c += text[i] == '\n';
-    }
+  for (int d = 1; d < 32; d <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl = op(incl, y);
   }
-  __shared__ int s_warp[kCsvThreads / 32 + 1];
-  int total;
-  (void)block_exclusive_sum<kCsvThreads>(c, &total, s_warp);
-  if (threadIdx.x == 0) counts[blockIdx.x] = total;
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int64_t w = lane < NW ? s_w[lane] : id;
+    int64_t wi = w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi = op(wi, y);
+    }
+    const int64_t prev_w = __shfl_up_sync(0xffffffffu, wi, 1);  // every lane takes part
+    if (lane < NW) s_w[NW + 1 + lane] = lane == 0 ? id : prev_w;
+    if (lane == NW - 1) s_w[NW] = wi;
+  }
+  __syncthreads();
+  const int64_t up = __shfl_up_sync(0xffffffffu, incl, 1);  // every lane takes part
+  const int64_t excl_in_warp = lane == 0 ? id : up;
+  const int64_t r = op(s_w[NW + 1 + warp], excl_in_warp);
+  *total = s_w[NW];
+  __syncthreads();  // s_w is reused by the next scan
+  return r;
 }
 
-// Writes the byte offset just after each '\n' (the start of the next row).
-__global__ void __launch_bounds__(kCsvThreads)
-    csv_row_starts_kernel(const uint8_t* __restrict__ text, int64_t n, const int32_t* __restrict__ tile_offsets,
-                          int64_t* __restrict__ starts) {
-  __shared__ int s_warp[kCsvThreads / 32 + 1];
-  const int64_t base = static_cast<int64_t>(blockIdx.x) * kCsvTileBytes;
-  int64_t run = tile_offsets[blockIdx.x];
-  for (int step = 0; step < kCsvTileBytes / kStepBytes; ++step) {
-    const int64_t at = base + static_cast<int64_t>(step) * kStepBytes + threadIdx.x * 16;
-    uint32_t mask = 0;
-    for (int b = 0; b < 16; ++b)
-      if (at + b < n && text[at + b] == '\n') mask |= 1u << b;
-    int total;
-    const int excl = block_exclusive_sum<kCsvThreads>(__popc(mask), &total, s_warp);
-    int64_t o = run + excl;
-    while (mask) {
-      const int b = __ffs(mask) - 1;
-      mask &= mask - 1;
-      starts[o++] = at + b + 1;
+struct SumOp {
+  __device__ int64_t operator()(int64_t a, int64_t b) const { return a + b; }
+};
+struct MaxOp {
+  __device__ int64_t operator()(int64_t a, int64_t b) const { return a > b ? a : b; }
+};
+
+// The 64 bytes of this thread's chunk (zeros past the end of the text).
+__device__ __forceinline__ void load_chunk(const uint8_t* text, int64_t n, int64_t at, uint32_t w[16]) {
+  if (at + kCsvChunk <= n) {
+    const uint4* q = reinterpret_cast<const uint4*>(text + at);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint4 v = __ldg(q + k);
+      w[4 * k] = v.x;
+      w[4 * k + 1] = v.y;
+      w[4 * k + 2] = v.z;
+      w[4 * k + 3] = v.w;
     }
-    run += total;
-    __syncthreads();
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) w[k] = 0;
+    for (int64_t i = at; i < n && i < at + kCsvChunk; ++i)
+      w[(i - at) >> 2] |= static_cast<uint32_t>(text[i]) << (8 * ((i - at) & 3));
+  }
+}
+
+// Bit i set when byte i of the chunk is a separator (delimiter or newline).
+__device__ __forceinline__ uint64_t separator_mask(const uint32_t w[16], uint8_t delim, uint64_t* nl_mask) {
+  uint64_t m = 0, nl = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const uint32_t c = (w[k] >> (8 * b)) & 0xFFu;
+      const uint64_t bit = uint64_t{1} << (4 * k + b);
+      if (c == delim) m |= bit;
+      if (c == '\n') {
+        m |= bit;
+        nl |= bit;
+      }
+    }
+  }
+  *nl_mask = nl;
+  return m;
+}
+
+// (1) per tile: separators, and the position of the last one (-1: none)
+__global__ void __launch_bounds__(kCsvThreads)
+    csv_index_kernel(const uint8_t* __restrict__ text, int64_t n, uint8_t delim, int64_t* __restrict__ tile_count,
+                     int64_t* __restrict__ tile_last) {
+  __shared__ int64_t s_w[2 * (kCsvThreads / 32) + 2];
+  const int64_t at = static_cast<int64_t>(blockIdx.x) * kCsvTile + static_cast<int64_t>(threadIdx.x) * kCsvChunk;
+  uint32_t w[16];
+  load_chunk(text, n, at, w);
+  uint64_t nl;
+  uint64_t m = separator_mask(w, delim, &nl);
+  if (at + kCsvChunk > n) m &= n > at ? (~uint64_t{0} >> (64 - (n - at))) : 0;  // bytes past the end are zero anyway
+  const int64_t cnt = __popcll(m);
+  const int64_t last = m ? at + 63 - __clzll(static_cast<long long>(m)) : -1;
+  int64_t total_cnt, max_last;
+  (void)block_scan64<kCsvThreads>(cnt, 0, SumOp{}, &total_cnt, s_w);
+  (void)block_scan64<kCsvThreads>(last, -1, MaxOp{}, &max_last, s_w);
+  if (threadIdx.x == 0) {
+    tile_count[blockIdx.x] = total_cnt;
+    tile_last[blockIdx.x] = max_last;
+  }
+}
+
+// (2) one CTA: exclusive sum of the tile counts (in place), exclusive max of
+// the tiles' last separators (in place), the total into out[0] and the last
+// byte of the text into out[1].
+__global__ void __launch_bounds__(kCsvScanThreads)
+    csv_tile_scan_kernel(int64_t* __restrict__ tile_count, int64_t* __restrict__ tile_last, int64_t n_tiles,
+                         const uint8_t* __restrict__ text, int64_t n, int64_t* __restrict__ out) {
+  __shared__ int64_t s_w[2 * (kCsvScanThreads / 32) + 2];
+  int64_t carry_sum = 0, carry_max = -1;
+  for (int64_t base = 0; base < n_tiles; base += kCsvScanThreads) {
+    const int64_t t = base + threadIdx.x;
+    const int64_t c = t < n_tiles ? tile_count[t] : 0;
+    const int64_t l = t < n_tiles ? tile_last[t] : -1;
+    int64_t tot_c, tot_l;
+    const int64_t ec = block_scan64<kCsvScanThreads>(c, 0, SumOp{}, &tot_c, s_w);
+    const int64_t el = block_scan64<kCsvScanThreads>(l, -1, MaxOp{}, &tot_l, s_w);
+    if (t < n_tiles) {
+      tile_count[t] = carry_sum + ec;
+      tile_last[t] = carry_max > el ? carry_max : el;
+    }
+    carry_sum += tot_c;
+    carry_max = carry_max > tot_l ? carry_max : tot_l;
+  }
+  if (threadIdx.x == 0) {
+    out[0] = carry_sum;
+    out[1] = n > 0 ? text[n - 1] : '\n';
   }
 }
 
@@ -102,23 +186,28 @@ __device__ __forceinline__ int32_t days_from_civil(int32_t y, uint32_t m, uint32
 struct CsvOut {
   void* data;         // fixed-width output, or utf8 lengths (int32)
   int64_t* str_start; // utf8: absolute start offset of each field
-  int32_t field;      // field index in the line
   int32_t type;       // ColTypeCode
   int32_t decimal;    // 1: decimal text -> scaled int64
   int32_t scale;
+  int32_t pad;
 };
 
 constexpr int kCsvMaxOut = 32;
+constexpr int kCsvMaxFields = 256;
 
 struct CsvParams {
   const uint8_t* text;
-  const int64_t* starts;  // n_rows + 1 row starts (last = end of text + 1)
-  int64_t n_rows;
+  int64_t n;                   // text bytes
+  const int64_t* tile_base;    // first separator ordinal of each tile
+  const int64_t* tile_prev;    // position of the separator before each tile (-1: none)
+  int64_t n_rows;              // data rows (after the header)
   int32_t n_fields;
-  int32_t n_out;
+  int32_t header;              // 1: the first row is skipped
+  int32_t virtual_end;         // 1: the text does not end with '\n' (a newline is implied at n)
   uint8_t delim;
-  uint8_t pad[7];
+  uint8_t pad[3];
   DevStatus* st;
+  int16_t slot[kCsvMaxFields]; // output slot of each field (-1: not emitted)
   CsvOut out[kCsvMaxOut];
 };
 
@@ -203,83 +292,114 @@ __device__ __forceinline__ bool parse_date(const uint8_t* t, int64_t b, int64_t 
   return true;
 }
 
-__global__ void __launch_bounds__(kCsvThreads) csv_convert_kernel(const __grid_constant__ CsvParams p) {
-  extern __shared__ int32_t s_fs[];  // [kCsvThreads][n_fields + 1] field starts relative to the row start
-  const int F = p.n_fields;
-  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * kCsvThreads;
-  const int lr = threadIdx.x;
-  const int64_t row = row0 + lr;
-  // Phase A: split my row.
-  if (row < p.n_rows) {
-    const int64_t b = p.starts[row];
-    int64_t e = p.starts[row + 1] - 1;  // exclusive of the '\n'
-    if (e > b && p.text[e - 1] == '\r') --e;
-    int32_t* fs = s_fs + lr * (F + 1);
-    fs[0] = 0;
-    int k = 1;
-    for (int64_t i = b; i < e; ++i) {
-      if (p.text[i] == p.delim) {
-        if (k < F) fs[k] = static_cast<int32_t>(i + 1 - b);
-        ++k;
-      }
-    }
-    fs[F] = static_cast<int32_t>(e + 1 - b);
-    // A short row leaves its missing fields empty (start = end of row), so
-    // phase B never reads outside the row; the row is reported as malformed.
-    for (int j = k; j < F; ++j) fs[j] = fs[F];
-    if (k != F) raise_status(p.st, GFPDB_EINVAL, static_cast<int32_t>(row < INT32_MAX ? row : INT32_MAX));
+__device__ __forceinline__ void csv_malformed(DevStatus* st, int64_t row) {
+  raise_status(st, GFPDB_EINVAL, static_cast<int32_t>(row < 0 ? 0 : (row < INT32_MAX ? row : INT32_MAX)));
+}
+
+// (3) every field, by the separator that ends it
+__global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_constant__ CsvParams p) {
+  __shared__ int64_t s_w[2 * (kCsvThreads / 32) + 2];
+  const int64_t at = static_cast<int64_t>(blockIdx.x) * kCsvTile + static_cast<int64_t>(threadIdx.x) * kCsvChunk;
+  uint32_t w[16];
+  load_chunk(p.text, p.n, at, w);
+  uint64_t nl;
+  uint64_t m = separator_mask(w, p.delim, &nl);
+  if (at + kCsvChunk > p.n) {
+    const uint64_t valid = p.n > at ? (~uint64_t{0} >> (64 - (p.n - at))) : 0;
+    m &= valid;
+    nl &= valid;
   }
-  __syncthreads();
-  // Phase B: convert, one emitted column at a time across the block's rows.
-  const int64_t rows_here = p.n_rows - row0 < kCsvThreads ? p.n_rows - row0 : kCsvThreads;
-  for (int task = threadIdx.x; task < p.n_out * kCsvThreads; task += kCsvThreads) {
-    const int oc = task / kCsvThreads;
-    const int r = task % kCsvThreads;
-    if (r >= rows_here) continue;
-    const CsvOut& o = p.out[oc];
-    const int32_t* fs = s_fs + r * (F + 1);
-    const int64_t rb = p.starts[row0 + r];
-    int64_t b = rb + fs[o.field];
-    int64_t e = rb + fs[o.field + 1] - 1;
-    if (e < b) e = b;
+  // the implied newline after an unterminated last line belongs to the chunk
+  // holding the last byte
+  const bool has_end = p.virtual_end && p.n > at && p.n <= at + kCsvChunk;
+  const int64_t cnt = __popcll(m) + (has_end ? 1 : 0);
+  const int64_t last = has_end ? p.n : (m ? at + 63 - __clzll(static_cast<long long>(m)) : -1);
+  int64_t tot;
+  const int64_t first = p.tile_base[blockIdx.x] + block_scan64<kCsvThreads>(cnt, 0, SumOp{}, &tot, s_w);
+  const int64_t before = block_scan64<kCsvThreads>(last, -1, MaxOp{}, &tot, s_w);
+  int64_t prev = p.tile_prev[blockIdx.x] > before ? p.tile_prev[blockIdx.x] : before;
+  const int F = p.n_fields;
+  int64_t g = first;
+  for (int k = 0; k < static_cast<int>(cnt); ++k, ++g) {
+    int64_t pos;
+    bool is_nl;
+    if (m != 0) {
+      const int bit = __ffsll(static_cast<long long>(m)) - 1;
+      m &= m - 1;
+      pos = at + bit;
+      is_nl = (nl >> bit) & 1u;
+    } else {  // the implied newline
+      pos = p.n;
+      is_nl = true;
+    }
+    int64_t b = prev + 1, e = pos;
+    prev = pos;
+    const int col = static_cast<int>(g % F);
+    const int64_t row = g / F - p.header;
+    if (is_nl != (col == F - 1)) {
+      csv_malformed(p.st, row);
+      continue;
+    }
+    if (row < 0 || row >= p.n_rows) continue;
+    const int sl = p.slot[col];
+    if (sl < 0) continue;
+    if (is_nl && e > b && p.text[e - 1] == '\r') --e;
     trim_quotes(p.text, b, e);
-    const int64_t orow = row0 + r;
+    const CsvOut& o = p.out[sl];
     bool ok = true;
     if (o.type == CT_UTF8) {
-      static_cast<int32_t*>(o.data)[orow] = static_cast<int32_t>(e - b);
-      o.str_start[orow] = b;
+      static_cast<int32_t*>(o.data)[row] = static_cast<int32_t>(e - b);
+      o.str_start[row] = b;
     } else if (o.type == CT_DATE32) {
       int32_t v = 0;
       ok = parse_date(p.text, b, e, &v);
-      static_cast<int32_t*>(o.data)[orow] = v;
+      static_cast<int32_t*>(o.data)[row] = v;
     } else {
       int64_t v = 0;
       ok = o.decimal ? parse_decimal(p.text, b, e, o.scale, &v) : parse_int(p.text, b, e, &v);
       if (o.type == CT_I32) {
         if (v < INT32_MIN || v > INT32_MAX) ok = false;
-        static_cast<int32_t*>(o.data)[orow] = static_cast<int32_t>(v);
+        static_cast<int32_t*>(o.data)[row] = static_cast<int32_t>(v);
       } else {
-        static_cast<int64_t*>(o.data)[orow] = v;
+        static_cast<int64_t*>(o.data)[row] = v;
       }
     }
-    if (!ok) raise_status(p.st, GFPDB_EINVAL, static_cast<int32_t>(orow < INT32_MAX ? orow : INT32_MAX));
+    if (!ok) csv_malformed(p.st, row);
   }
 }
 
-__global__ void csv_copy_strings_kernel(const uint8_t* __restrict__ text, const int64_t* __restrict__ str_start,
-                                        const int32_t* __restrict__ offs, uint8_t* __restrict__ out, int64_t n) {
-  // one warp per row: lanes copy consecutive bytes
-  const int lane = threadIdx.x & 31;
-  const int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+// (4) utf8 bytes: each warp takes 32 consecutive rows, whose output bytes are
+// one contiguous range, and moves that range with lane-consecutive (coalesced)
+// stores; each lane finds the row of its byte by advancing a cursor over the
+// 33 offsets in shared memory (output positions only grow).
+constexpr int kCopyThreads = 256;
+
+__global__ void __launch_bounds__(kCopyThreads)
+    csv_copy_strings_kernel(const uint8_t* __restrict__ text, const int64_t* __restrict__ str_start,
+                            const int32_t* __restrict__ offs, uint8_t* __restrict__ out, int64_t n) {
+  __shared__ int32_t s_off[kCopyThreads / 32][33];
+  __shared__ int64_t s_src[kCopyThreads / 32][32];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int64_t n_groups = (n + 31) / 32;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-  for (int64_t r = w; r < n; r += nw) {
-    const int64_t s = str_start[r];
-    const int32_t o = offs[r], len = offs[r + 1] - o;
-    for (int32_t k = lane; k < len; k += 32) out[o + k] = text[s + k];
+  for (int64_t g = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; g < n_groups; g += nw) {
+    const int64_t r0 = g * 32;
+    const int nr = static_cast<int>(n - r0 < 32 ? n - r0 : 32);
+    if (lane < nr) {
+      s_off[wi][lane] = offs[r0 + lane];
+      s_src[wi][lane] = str_start[r0 + lane];
+    }
+    if (lane == 0) s_off[wi][nr] = offs[r0 + nr];
+    __syncwarp();
+    const int32_t o0 = s_off[wi][0], o1 = s_off[wi][nr];
+    int row = 0;
+    for (int32_t q = o0 + lane; q < o1; q += 32) {
+      while (s_off[wi][row + 1] <= q) ++row;  // bounded: q < o1 = s_off[nr]
+      out[q] = text[s_src[wi][row] + (q - s_off[wi][row])];
+    }
+    __syncwarp();  // the shared offsets are rewritten by the next group
   }
 }
-
-__global__ void csv_tail_kernel(int64_t* starts, int64_t at, int64_t value) { starts[at] = value; }
 
 }  // namespace
 
@@ -292,45 +412,38 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   const uint8_t* text = reinterpret_cast<const uint8_t*>(device_text);
   if ((reinterpret_cast<uintptr_t>(text) & 15u) != 0) fail(GFPDB_EINVAL, "CSV text must be 16-byte aligned");
 
-  // (1)-(3): row starts
-  const int64_t n_tiles = n_bytes > 0 ? (n_bytes + kCsvTileBytes - 1) / kCsvTileBytes : 0;
-  auto counts = make_buffer((n_tiles + 1) * 4, s);
-  auto tile_off = make_buffer((n_tiles + 1) * 4, s);
-  int64_t newlines = 0;
+  if (static_cast<int>(fields.size()) > kCsvMaxFields) fail(GFPDB_EUNSUPPORTED, "too many CSV fields per line");
+  const int F = static_cast<int>(fields.size());
+  // (1)-(2): separators per tile, their scans, the total
+  const int64_t n_tiles = n_bytes > 0 ? (n_bytes + kCsvTile - 1) / kCsvTile : 0;
+  auto tiles = make_buffer(std::max<int64_t>(n_tiles, 1) * 16 + 16, s);
+  int64_t* tile_count = tiles->as<int64_t>();
+  int64_t* tile_last = tile_count + std::max<int64_t>(n_tiles, 1);
+  int64_t* tot = tile_last + std::max<int64_t>(n_tiles, 1);
+  int64_t host_tot[2] = {0, '\n'};
   if (n_tiles > 0) {
-    ProfScope prof("csv_newline_count_kernel", s);
-    csv_newline_count_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(text, n_bytes, counts->as<int32_t>());
-    after_launch("csv_newline_count_kernel");
-    prof.stop(static_cast<double>(n_bytes));
-    newlines = exclusive_scan_i32(counts->as<int32_t>(), tile_off->as<int32_t>(), n_tiles, s);
-  }
-  // Last line without a trailing newline still counts as a row.
-  char last = '\n';
-  if (n_bytes > 0) {
-    GF_CUDA(cudaMemcpyAsync(&last, device_text + n_bytes - 1, 1, cudaMemcpyDeviceToHost, s));
+    if (n_tiles >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "CSV text too large");
+    {
+      ProfScope prof("csv_index_kernel", s);
+      csv_index_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(text, n_bytes, static_cast<uint8_t>(delimiter),
+                                                                        tile_count, tile_last);
+      after_launch("csv_index_kernel");
+      prof.stop(static_cast<double>(n_bytes));
+    }
+    csv_tile_scan_kernel<<<1, kCsvScanThreads, 0, s>>>(tile_count, tile_last, n_tiles, text, n_bytes, tot);
+    after_launch("csv_tile_scan_kernel");
+    GF_CUDA(cudaMemcpyAsync(host_tot, tot, sizeof(host_tot), cudaMemcpyDeviceToHost, s));
     sync(s);
   }
-  const int64_t lines = newlines + (last != '\n' ? 1 : 0);
-  // starts[0] = 0, starts[1 + k] = after the k-th newline; an extra entry
-  // closes an unterminated last line.
-  auto starts = make_buffer((lines + 2) * 8, s);
-  GF_CUDA(cudaMemsetAsync(starts->data(), 0, 8, s));
-  if (n_tiles > 0) {
-    ProfScope prof("csv_row_starts_kernel", s);
-    csv_row_starts_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(text, n_bytes, tile_off->as<int32_t>(),
-                                                                           starts->as<int64_t>() + 1);
-    after_launch("csv_row_starts_kernel");
-    prof.stop(static_cast<double>(n_bytes) + 8.0 * static_cast<double>(newlines));
-  }
-  if (last != '\n') {
-    csv_tail_kernel<<<1, 1, 0, s>>>(starts->as<int64_t>(), lines, n_bytes + 1);
-    after_launch("csv_tail_kernel");
-  }
+  const bool virtual_end = n_bytes > 0 && host_tot[1] != '\n';
+  const int64_t seps = host_tot[0] + (virtual_end ? 1 : 0);
+  if (seps % F != 0)
+    fail(GFPDB_EINVAL, "malformed CSV field or wrong field count near data row " + std::to_string(seps / F));
+  const int64_t lines = seps / F;
   const int64_t skip = has_header && lines > 0 ? 1 : 0;
   const int64_t n_rows = lines - skip;
-  const int64_t* row_starts = starts->as<int64_t>() + skip;
 
-  // (4) convert
+  // (3) fields
   std::vector<Field> out_fields;
   std::vector<BufferPtr> bufs(emit.size()), sstart(emit.size());
   CsvParams* pp = new CsvParams;
@@ -338,19 +451,24 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   CsvParams& p = *pp;
   std::memset(&p, 0, sizeof(p));
   p.text = text;
-  p.starts = row_starts;
+  p.n = n_bytes;
+  p.tile_base = tile_count;
+  p.tile_prev = tile_last;
   p.n_rows = n_rows;
-  p.n_fields = static_cast<int32_t>(fields.size());
-  p.n_out = static_cast<int32_t>(emit.size());
+  p.n_fields = F;
+  p.header = static_cast<int32_t>(skip);
+  p.virtual_end = virtual_end ? 1 : 0;
   p.delim = static_cast<uint8_t>(delimiter);
+  for (int i = 0; i < kCsvMaxFields; ++i) p.slot[i] = -1;
   auto status = make_buffer(sizeof(DevStatus), s);
   GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
   p.st = status->as<DevStatus>();
   for (size_t k = 0; k < emit.size(); ++k) {
     const CsvField& f = fields[emit[k]];
+    if (p.slot[emit[k]] >= 0) fail(GFPDB_EINVAL, "CSV column '" + f.name + "' projected twice");
+    p.slot[emit[k]] = static_cast<int16_t>(k);
     out_fields.push_back(Field{f.name, f.type});
     CsvOut& o = p.out[k];
-    o.field = emit[k];
     o.type = static_cast<int32_t>(f.type);
     o.decimal = f.decimal ? 1 : 0;
     o.scale = f.scale;
@@ -363,14 +481,10 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
     }
     o.data = bufs[k]->data();
   }
-  if (n_rows > 0) {
-    const size_t dyn = static_cast<size_t>(kCsvThreads) * (fields.size() + 1) * 4;
-    if (dyn > 48 * 1024) GF_CUDA(cudaFuncSetAttribute(csv_convert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    const int64_t blocks = (n_rows + kCsvThreads - 1) / kCsvThreads;
-    if (blocks > INT32_MAX) fail(GFPDB_EUNSUPPORTED, "too many CSV rows");
-    ProfScope prof("csv_convert_kernel", s);
-    csv_convert_kernel<<<static_cast<int>(blocks), kCsvThreads, dyn, s>>>(p);
-    after_launch("csv_convert_kernel");
+  if (n_tiles > 0) {
+    ProfScope prof("csv_fields_kernel", s);
+    csv_fields_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(p);
+    after_launch("csv_fields_kernel");
     double out_w = 0;
     for (auto& f : out_fields) out_w += f.type == DType::Utf8 ? 12 : dtype_width(f.type);
     prof.stop(static_cast<double>(n_bytes) + static_cast<double>(n_rows) * out_w);
@@ -393,10 +507,11 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
     const int64_t total = exclusive_scan_i32(bufs[k]->as<int32_t>(), offs->as<int32_t>(), n_rows, s);
     auto bytes = make_buffer(total, s);
     if (n_rows > 0 && total > 0) {
-      int64_t blocks = (n_rows * 32 + 255) / 256;
+      const int64_t groups = (n_rows + 31) / 32;
+      int64_t blocks = (groups + kCopyThreads / 32 - 1) / (kCopyThreads / 32);
       int64_t cap = static_cast<int64_t>(num_sms()) * 16;
       ProfScope prof("csv_copy_strings_kernel", s);
-      csv_copy_strings_kernel<<<static_cast<int>(blocks < cap ? blocks : cap), 256, 0, s>>>(
+      csv_copy_strings_kernel<<<static_cast<int>(blocks < cap ? blocks : cap), kCopyThreads, 0, s>>>(
           text, sstart[k]->as<int64_t>(), offs->as<int32_t>(), bytes->as<uint8_t>(), n_rows);
       after_launch("csv_copy_strings_kernel");
       prof.stop(2.0 * static_cast<double>(total) + 12.0 * static_cast<double>(n_rows));

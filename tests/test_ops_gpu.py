@@ -309,3 +309,60 @@ def test_select_probe_pipeline_unaligned_columns(gpu):
         shifted.append(views)
     got = ops.select(DeviceTable(dt.names, dt.types, shifted, dt.num_rows), None, blooms)
     assert got.rows() == seq.rows()
+
+
+def test_csv_lineitem_exact_values(gpu):
+    """The lineitem text (fields up to 40 bytes, rows crossing 64-byte thread
+    chunks and 16 KiB tiles) parses into exactly the values it was written
+    from, every column."""
+    rows = 120_000
+    text = workloads.lineitem_csv(rows, seed=3300)
+    got = ops.csv_read(text, workloads.LINEITEM_FIELDS, delimiter="|")
+    want = workloads.lineitem_columns(rows, seed=3300)
+    assert got.num_rows == rows
+    for name, ty in workloads.LINEITEM_FIELDS:
+        if ty == "utf8":
+            lens, chars = want[name]
+            offs, data = got.column(name).values
+            assert np.array_equal(np.diff(offs), lens), name
+            assert np.array_equal(data, chars), name
+        else:
+            assert np.array_equal(np.asarray(got[name], dtype=np.int64), want[name]), name
+
+
+def test_csv_long_fields_span_tiles(gpu):
+    """Fields longer than a thread's 64 bytes and a tile's 16 KiB."""
+    rng = np.random.default_rng(3400)
+    lines, vals = [], []
+    for r in range(50):
+        s = "x" * int(rng.integers(0, 40_000))
+        lines.append(f"{r}|{s}|{-r * 7}")
+        vals.append((r, s, -r * 7))
+    text = ("\n".join(lines) + "\n").encode()
+    got = ops.csv_read(text, [("a", "int32"), ("s", "utf8"), ("b", "int64")], delimiter="|")
+    assert got.rows() == vals
+
+
+def test_csv_malformed_row_in_large_text(gpu):
+    from flexpushdowndb_gb300 import GfpdbError
+
+    text = bytearray(workloads.lineitem_csv(20_000, seed=3500))
+    # an extra field in row 12,345 (and one fewer in the next row: the
+    # separator total stays a multiple of the field count)
+    nl = [i for i, c in enumerate(text) if c == 10]
+    text[nl[12_344] - 1 : nl[12_344] - 1] = b"|"
+    end = nl[12_345] + 1
+    cut = text.index(b"|", end)
+    del text[cut]
+    with pytest.raises(GfpdbError) as ei:
+        ops.csv_read(bytes(text), workloads.LINEITEM_FIELDS, delimiter="|")
+    assert "malformed" in ei.value.message
+    with pytest.raises(GfpdbError):
+        ops.csv_read(b"1|2\n3\n", [("a", "int32"), ("b", "int32")], delimiter="|")
+
+
+def test_csv_empty_and_utf8_only(gpu):
+    got = ops.csv_read(b"", [("a", "int32")], delimiter="|")
+    assert got.num_rows == 0
+    got = ops.csv_read(b"||\n|x|\n", [("a", "utf8"), ("b", "utf8"), ("c", "utf8")], delimiter="|")
+    assert got.rows() == [("", "", ""), ("", "x", "")]
