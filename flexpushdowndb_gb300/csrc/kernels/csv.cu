@@ -96,11 +96,15 @@ __device__ __forceinline__ void load_chunk(const uint8_t* text, int64_t n, int64
       w[4 * k + 2] = v.z;
       w[4 * k + 3] = v.w;
     }
-  } else {
+  } else {  // the last chunk: byte loads, indexes fixed at compile time so w stays in registers
 #pragma unroll
-    for (int k = 0; k < 16; ++k) w[k] = 0;
-    for (int64_t i = at; i < n && i < at + kCsvChunk; ++i)
-      w[(i - at) >> 2] |= static_cast<uint32_t>(text[i]) << (8 * ((i - at) & 3));
+    for (int k = 0; k < 16; ++k) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (at + 4 * k + b < n) v |= static_cast<uint32_t>(text[at + 4 * k + b]) << (8 * b);
+      w[k] = v;
+    }
   }
 }
 
@@ -296,10 +300,50 @@ __device__ __forceinline__ void csv_malformed(DevStatus* st, int64_t row) {
   raise_status(st, GFPDB_EINVAL, static_cast<int32_t>(row < 0 ? 0 : (row < INT32_MAX ? row : INT32_MAX)));
 }
 
-// (3) every field, by the separator that ends it
+// Converts one field, bytes [b, e) of t (t is the text or a shared-memory copy
+// of part of it; `shift` turns an index of t into a text offset) into output
+// slot sl at `row`.
+__device__ __forceinline__ void convert_field(const CsvParams& p, int sl, int64_t row, const uint8_t* t, int64_t b,
+                                              int64_t e, int64_t shift, bool is_nl) {
+  if (is_nl && e > b && t[e - 1] == '\r') --e;
+  trim_quotes(t, b, e);
+  const CsvOut& o = p.out[sl];
+  bool ok = true;
+  if (o.type == CT_UTF8) {
+    static_cast<int32_t*>(o.data)[row] = static_cast<int32_t>(e - b);
+    o.str_start[row] = b + shift;
+  } else if (o.type == CT_DATE32) {
+    int32_t v = 0;
+    ok = parse_date(t, b, e, &v);
+    static_cast<int32_t*>(o.data)[row] = v;
+  } else {
+    int64_t v = 0;
+    ok = o.decimal ? parse_decimal(t, b, e, o.scale, &v) : parse_int(t, b, e, &v);
+    if (o.type == CT_I32) {
+      if (v < INT32_MIN || v > INT32_MAX) ok = false;
+      static_cast<int32_t*>(o.data)[row] = static_cast<int32_t>(v);
+    } else {
+      static_cast<int64_t*>(o.data)[row] = v;
+    }
+  }
+  if (!ok) csv_malformed(p.st, row);
+}
+
+// Separators of one tile kept in shared memory; a tile with more (fields of
+// about 4 bytes on average) is converted by the thread-per-chunk loop instead.
+constexpr int kCsvSepCap = 4096;
+constexpr int kCsvPosSlots = kCsvSepCap + 2 * kCsvMaxFields;
+
+// (3) every field, by the separator that ends it. The tile's text and its
+// separator positions go to shared memory, the positions stored by (field,
+// row) so that consecutive threads convert one field of consecutive rows: the
+// same conversion in every lane and coalesced stores into the column.
 __global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_constant__ CsvParams p) {
   __shared__ int64_t s_w[2 * (kCsvThreads / 32) + 2];
-  const int64_t at = static_cast<int64_t>(blockIdx.x) * kCsvTile + static_cast<int64_t>(threadIdx.x) * kCsvChunk;
+  __shared__ __align__(16) uint32_t s_text[kCsvTile / 4];
+  __shared__ int32_t s_pos[kCsvPosSlots];  // tile-relative position | (newline ? 1 << 31 : 0)
+  const int64_t tile0 = static_cast<int64_t>(blockIdx.x) * kCsvTile;
+  const int64_t at = tile0 + static_cast<int64_t>(threadIdx.x) * kCsvChunk;
   uint32_t w[16];
   load_chunk(p.text, p.n, at, w);
   uint64_t nl;
@@ -312,90 +356,178 @@ __global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_co
   // the implied newline after an unterminated last line belongs to the chunk
   // holding the last byte
   const bool has_end = p.virtual_end && p.n > at && p.n <= at + kCsvChunk;
-  const int64_t cnt = __popcll(m) + (has_end ? 1 : 0);
+  const int cnt = __popcll(m) + (has_end ? 1 : 0);
   const int64_t last = has_end ? p.n : (m ? at + 63 - __clzll(static_cast<long long>(m)) : -1);
-  int64_t tot;
-  const int64_t first = p.tile_base[blockIdx.x] + block_scan64<kCsvThreads>(cnt, 0, SumOp{}, &tot, s_w);
-  const int64_t before = block_scan64<kCsvThreads>(last, -1, MaxOp{}, &tot, s_w);
-  int64_t prev = p.tile_prev[blockIdx.x] > before ? p.tile_prev[blockIdx.x] : before;
+  int64_t tot, unused;
+  const int64_t g0 = p.tile_base[blockIdx.x];
+  const int64_t first = g0 + block_scan64<kCsvThreads>(cnt, 0, SumOp{}, &tot, s_w);
+  const int64_t before = block_scan64<kCsvThreads>(last, -1, MaxOp{}, &unused, s_w);
+  const int64_t tile_prev = p.tile_prev[blockIdx.x];
   const int F = p.n_fields;
-  int64_t g = first;
-  for (int k = 0; k < static_cast<int>(cnt); ++k, ++g) {
-    int64_t pos;
-    bool is_nl;
-    if (m != 0) {
-      const int bit = __ffsll(static_cast<long long>(m)) - 1;
-      m &= m - 1;
-      pos = at + bit;
-      is_nl = (nl >> bit) & 1u;
-    } else {  // the implied newline
-      pos = p.n;
-      is_nl = true;
+
+  if (tot > kCsvSepCap) {  // uniform over the block
+    int64_t prev = tile_prev > before ? tile_prev : before;
+    int64_t g = first;
+    for (int k = 0; k < cnt; ++k, ++g) {
+      int64_t pos;
+      bool is_nl;
+      if (m != 0) {
+        const int bit = __ffsll(static_cast<long long>(m)) - 1;
+        m &= m - 1;
+        pos = at + bit;
+        is_nl = (nl >> bit) & 1u;
+      } else {  // the implied newline
+        pos = p.n;
+        is_nl = true;
+      }
+      const int64_t b = prev + 1;
+      prev = pos;
+      const int col = static_cast<int>(g % F);
+      const int64_t row = g / F - p.header;
+      if (is_nl != (col == F - 1)) {
+        csv_malformed(p.st, row);
+        continue;
+      }
+      if (row < 0 || row >= p.n_rows) continue;
+      const int sl = p.slot[col];
+      if (sl >= 0) convert_field(p, sl, row, p.text, b, pos, 0, is_nl);
     }
-    int64_t b = prev + 1, e = pos;
-    prev = pos;
-    const int col = static_cast<int>(g % F);
-    const int64_t row = g / F - p.header;
-    if (is_nl != (col == F - 1)) {
+    return;
+  }
+
+  {
+    uint4* dst = reinterpret_cast<uint4*>(s_text) + threadIdx.x * (kCsvChunk / 16);
+#pragma unroll
+    for (int k = 0; k < kCsvChunk / 16; ++k) dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+  }
+  const int64_t row0 = g0 / F;
+  const int RS = kCsvSepCap / F + 2;  // rows per field in s_pos; F * RS <= kCsvPosSlots
+  if (cnt > 0) {
+    const int64_t q = first / F;
+    int c = static_cast<int>(first - q * F);
+    int r = static_cast<int>(q - row0);
+    for (int k = 0; k < cnt; ++k) {
+      int32_t rel;
+      bool is_nl;
+      if (m != 0) {
+        const int bit = __ffsll(static_cast<long long>(m)) - 1;
+        m &= m - 1;
+        rel = static_cast<int32_t>(at - tile0) + bit;
+        is_nl = (nl >> bit) & 1u;
+      } else {
+        rel = static_cast<int32_t>(p.n - tile0);
+        is_nl = true;
+      }
+      s_pos[c * RS + r] = rel | (is_nl ? INT32_MIN : 0);
+      if (++c == F) {
+        c = 0;
+        ++r;
+      }
+    }
+  }
+  __syncthreads();
+  if (tot == 0) return;
+  const int64_t g_end = g0 + tot;
+  const int R = static_cast<int>((g_end - 1) / F - row0 + 1);
+  const int items = F * R;
+  const uint8_t* st = reinterpret_cast<const uint8_t*>(s_text);
+  for (int i = threadIdx.x; i < items; i += kCsvThreads) {
+    const int c = i / R, r = i - c * R;
+    const int64_t g = (row0 + r) * F + c;
+    if (g < g0 || g >= g_end) continue;
+    const int32_t pe = s_pos[c * RS + r];
+    const bool is_nl = pe < 0;
+    const int64_t row = row0 + r - p.header;
+    if (is_nl != (c == F - 1)) {
       csv_malformed(p.st, row);
       continue;
     }
     if (row < 0 || row >= p.n_rows) continue;
-    const int sl = p.slot[col];
+    const int sl = p.slot[c];
     if (sl < 0) continue;
-    if (is_nl && e > b && p.text[e - 1] == '\r') --e;
-    trim_quotes(p.text, b, e);
-    const CsvOut& o = p.out[sl];
-    bool ok = true;
-    if (o.type == CT_UTF8) {
-      static_cast<int32_t*>(o.data)[row] = static_cast<int32_t>(e - b);
-      o.str_start[row] = b;
-    } else if (o.type == CT_DATE32) {
-      int32_t v = 0;
-      ok = parse_date(p.text, b, e, &v);
-      static_cast<int32_t*>(o.data)[row] = v;
+    const int64_t e = pe & INT32_MAX;
+    if (g == g0) {  // the field may start before the tile
+      const int64_t b = tile_prev + 1;
+      if (b >= tile0)
+        convert_field(p, sl, row, st, b - tile0, e, tile0, is_nl);
+      else
+        convert_field(p, sl, row, p.text, b, tile0 + e, 0, is_nl);
     } else {
-      int64_t v = 0;
-      ok = o.decimal ? parse_decimal(p.text, b, e, o.scale, &v) : parse_int(p.text, b, e, &v);
-      if (o.type == CT_I32) {
-        if (v < INT32_MIN || v > INT32_MAX) ok = false;
-        static_cast<int32_t*>(o.data)[row] = static_cast<int32_t>(v);
-      } else {
-        static_cast<int64_t*>(o.data)[row] = v;
-      }
+      const int32_t pb = c > 0 ? s_pos[(c - 1) * RS + r] : s_pos[(F - 1) * RS + r - 1];
+      convert_field(p, sl, row, st, (pb & INT32_MAX) + 1, e, tile0, is_nl);
     }
-    if (!ok) csv_malformed(p.st, row);
   }
 }
 
 // (4) utf8 bytes: each warp takes 32 consecutive rows, whose output bytes are
-// one contiguous range, and moves that range with lane-consecutive (coalesced)
-// stores; each lane finds the row of its byte by advancing a cursor over the
-// 33 offsets in shared memory (output positions only grow).
+// one contiguous range, and writes it as whole 32-bit words (four per lane in
+// flight), with byte stores for the partial words at its two ends. A lane
+// finds the row of an output byte with a cursor over the 33 offsets in shared
+// memory (its output positions only grow).
 constexpr int kCopyThreads = 256;
+constexpr int kCopyUnroll = 4;
 
 __global__ void __launch_bounds__(kCopyThreads)
     csv_copy_strings_kernel(const uint8_t* __restrict__ text, const int64_t* __restrict__ str_start,
                             const int32_t* __restrict__ offs, uint8_t* __restrict__ out, int64_t n) {
   __shared__ int32_t s_off[kCopyThreads / 32][33];
-  __shared__ int64_t s_src[kCopyThreads / 32][32];
+  __shared__ int64_t s_delta[kCopyThreads / 32][32];  // text offset - output offset, per row
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int32_t* off = s_off[wi];
+  const int64_t* delta = s_delta[wi];
   const int64_t n_groups = (n + 31) / 32;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t g = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; g < n_groups; g += nw) {
     const int64_t r0 = g * 32;
     const int nr = static_cast<int>(n - r0 < 32 ? n - r0 : 32);
     if (lane < nr) {
-      s_off[wi][lane] = offs[r0 + lane];
-      s_src[wi][lane] = str_start[r0 + lane];
+      const int32_t o = offs[r0 + lane];
+      s_off[wi][lane] = o;
+      s_delta[wi][lane] = str_start[r0 + lane] - o;
     }
     if (lane == 0) s_off[wi][nr] = offs[r0 + nr];
     __syncwarp();
-    const int32_t o0 = s_off[wi][0], o1 = s_off[wi][nr];
+    const int32_t o0 = off[0], o1 = off[nr];
+    const int32_t w0 = (o0 + 3) >> 2, w1 = o1 >> 2;  // whole output words [w0, w1)
+    {
+      // partial words: bytes [o0, min(4 w0, o1)) and [max(4 w1, 4 w0), o1), three at most each
+      const int32_t head_end = 4 * w0 < o1 ? 4 * w0 : o1;
+      const int32_t tail_beg = 4 * w1 > 4 * w0 ? 4 * w1 : 4 * w0;
+      int32_t q = -1;
+      if (lane < 4 && o0 + lane < head_end) q = o0 + lane;
+      if (lane >= 4 && lane < 8 && tail_beg + lane - 4 < o1) q = tail_beg + lane - 4;
+      if (q >= 0) {
+        int row = 0;
+        while (off[row + 1] <= q) ++row;  // bounded: q < o1 = off[nr]
+        out[q] = text[delta[row] + q];
+      }
+    }
     int row = 0;
-    for (int32_t q = o0 + lane; q < o1; q += 32) {
-      while (s_off[wi][row + 1] <= q) ++row;  // bounded: q < o1 = s_off[nr]
-      out[q] = text[s_src[wi][row] + (q - s_off[wi][row])];
+    int32_t row_end = off[1];
+    int64_t d = delta[0];
+    for (int32_t wd = w0 + lane; wd < w1; wd += 32 * kCopyUnroll) {
+      uint32_t v[kCopyUnroll];
+#pragma unroll
+      for (int u = 0; u < kCopyUnroll; ++u) {
+        const int32_t word = wd + 32 * u;
+        uint32_t x = 0;
+        if (word < w1) {
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int32_t q = 4 * word + b;
+            while (q >= row_end) {  // bounded: q < o1 = off[nr]
+              ++row;
+              row_end = off[row + 1];
+              d = delta[row];
+            }
+            x |= static_cast<uint32_t>(text[d + q]) << (8 * b);
+          }
+        }
+        v[u] = x;
+      }
+#pragma unroll
+      for (int u = 0; u < kCopyUnroll; ++u)
+        if (wd + 32 * u < w1) reinterpret_cast<uint32_t*>(out)[wd + 32 * u] = v[u];
     }
     __syncwarp();  // the shared offsets are rewritten by the next group
   }

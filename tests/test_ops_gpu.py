@@ -366,3 +366,38 @@ def test_csv_empty_and_utf8_only(gpu):
     assert got.num_rows == 0
     got = ops.csv_read(b"||\n|x|\n", [("a", "utf8"), ("b", "utf8"), ("c", "utf8")], delimiter="|")
     assert got.rows() == [("", "", ""), ("", "x", "")]
+
+
+def test_csv_dense_and_sparse_tiles(gpu):
+    """Tiles with more separators than a tile stages in shared memory (fields
+    of one or two bytes) next to tiles of long fields; empty fields, quotes
+    and CRLF in both."""
+    rng = np.random.default_rng(3600)
+    fields = [("a", "int32"), ("b", "int64"), ("s", "utf8")]
+    lines = ["a|b|s"]
+    for blk in range(12):
+        if blk % 2 == 0:
+            for r in range(int(rng.integers(2000, 9000))):
+                lines.append(f"{r % 10}|{r % 7}|{'' if r % 3 else chr(97 + r % 26)}")
+        else:
+            for r in range(int(rng.integers(100, 600))):
+                s = "".join(chr(65 + int(x)) for x in rng.integers(0, 26, int(rng.integers(0, 90))))
+                lines.append(f"{int(rng.integers(-2**31, 2**31))}|{int(rng.integers(-2**62, 2**62))}|"
+                             f"{chr(34) + s + chr(34) if r % 4 == 0 else s}")
+    text = ("\r\n".join(lines) + "\r\n").encode()
+    got = ops.csv_read(text, fields, delimiter="|", has_header=True)
+    want = oops.csv_parse(text, fields, delimiter="|", has_header=True)
+    assert got.num_rows == len(lines) - 1
+    assert got.rows() == want.rows()
+    got = ops.csv_read(text, fields, columns=["s", "a"], delimiter="|", has_header=True)
+    assert got.rows() == oops.csv_parse(text, fields, columns=["s", "a"], delimiter="|", has_header=True).rows()
+
+    from flexpushdowndb_gb300 import GfpdbError
+
+    bad = bytearray(text)
+    cut = len(lines[0]) + 2 + 6 * 1000  # inside the first dense block: "x|y|" at a row's start
+    row_start = bad.index(b"\n", cut) + 1
+    bad[row_start:row_start + 1] = b"x"  # an int32 field that is not a number
+    with pytest.raises(GfpdbError) as ei:
+        ops.csv_read(bytes(bad), fields, delimiter="|", has_header=True)
+    assert "malformed" in ei.value.message
