@@ -82,6 +82,7 @@ class ExecStats(ctypes.Structure):
         ("d2h_bytes", ctypes.c_int64),
         ("num_ops", ctypes.c_int64),
         ("messages", ctypes.c_int64),
+        ("device_ns", ctypes.c_int64),
     ]
 
 

@@ -57,7 +57,10 @@ struct CapturedPlan {
   uint64_t kernels = 0;
   int64_t num_ops = 0, messages = 0, h2d = 0;
   bool capturable = true;
+  cudaEvent_t ev[2] = {nullptr, nullptr};  // around a replay: its device time
   ~CapturedPlan() {
+    for (auto e : ev)
+      if (e) (void)cudaEventDestroy(e);
     if (exec) (void)cudaGraphExecDestroy(exec);
     if (epilogue) (void)cudaGraphExecDestroy(epilogue);
     if (pinned) (void)cudaFreeHost(pinned);
@@ -261,11 +264,21 @@ TupleSetPtr device_copy(const TupleSet& r, int64_t n, cudaStream_t s) {
 
 // Replay a captured plan. Returns false when a deferred output overflowed
 // (the caller then runs the plan with exact sizes).
-bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowDeviceArray* out, cudaStream_t s) {
+bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowDeviceArray* out, cudaStream_t s,
+                 int64_t* device_ns) {
+  if (cp.ev[0] == nullptr) {
+    GF_CUDA(cudaEventCreate(&cp.ev[0]));
+    GF_CUDA(cudaEventCreate(&cp.ev[1]));
+  }
+  GF_CUDA(cudaEventRecord(cp.ev[0], s));
   GF_CUDA(cudaGraphLaunch(cp.exec, s));
   GF_CUDA(cudaGraphLaunch(cp.epilogue, s));
+  GF_CUDA(cudaEventRecord(cp.ev[1], s));
   count_launch(cp.kernels);
   sync(s);
+  float ms = 0;
+  GF_CUDA(cudaEventElapsedTime(&ms, cp.ev[0], cp.ev[1]));
+  *device_ns = static_cast<int64_t>(static_cast<double>(ms) * 1e6);
   copy_counters().h2d += cp.h2d;
   copy_counters().d2h += cp.pinned_bytes;
   bool fits = true;
@@ -679,6 +692,7 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
     const uint64_t launches0 = g_kernel_launches.load();
     auto fill_stats = [&](int64_t num_ops, int64_t messages) {
       if (stats == nullptr) return;
+      stats->device_ns = 0;
       stats->kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
       stats->h2d_bytes = copy_counters().h2d - c0.h2d;
       stats->d2h_bytes = copy_counters().d2h - c0.d2h;
@@ -698,8 +712,10 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
         auto it = g_graphs.find(key);
         if (it != g_graphs.end()) cp = it->second;
       }
-      if (cp && cp->capturable && replay_plan(*cp, result_to_host != 0, out_schema, out, s)) {
+      int64_t device_ns = 0;
+      if (cp && cp->capturable && replay_plan(*cp, result_to_host != 0, out_schema, out, s, &device_ns)) {
         fill_stats(cp->num_ops, cp->messages);
+        if (stats != nullptr) stats->device_ns = device_ns;
         return;
       }
     }
@@ -833,6 +849,7 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
       stats->d2h_bytes = copy_counters().d2h - c0.d2h;
       stats->num_ops = 3;
       stats->messages = 0;
+      stats->device_ns = 0;
       stats->elapsed_ns =
           std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
     }

@@ -738,6 +738,268 @@ int select_probe_blocks_per_sm(size_t dyn) {
   return per_sm;
 }
 
+// ---------------------------------------------------------------------------
+// Compact selection for small inputs (dimension tables, small partitions).
+// A launch over a few thousand rows is bound by instruction fetch and by the
+// chain of dependent global accesses, not by bytes, so this kernel keeps its
+// code and its parameter block small: leaves are (integer column op integer
+// literal) with the comparison reduced to a 4-bit truth table over
+// (value < literal, value == literal), filters are probed in global memory
+// (they sit in L2) and a CTA whose grid covers every tile takes one ticket.
+constexpr int kLiteThreads = 256;
+constexpr int kLiteItems = 4;
+constexpr int kLiteTile = kLiteThreads * kLiteItems;
+constexpr int kLiteMaxLeaves = 8;
+constexpr int kLiteMaxOut = 12;
+constexpr int64_t kLiteMaxRows = int64_t{1} << 18;
+
+struct LiteLeaf {
+  const void* col;
+  int64_t lit;
+  int8_t wide;          // 1: int64 column; 0: int32 / date32
+  int8_t truth;         // bit (2 * (v < lit) + (v == lit)) set when the leaf holds
+  int8_t clause_start;  // 1: first leaf of its clause
+  int8_t pad[5];
+};
+
+struct LiteProbe {
+  const uint32_t* blocks;
+  const uint64_t* nblocks_dev;
+  const int32_t* valid_dev;
+  const void* key;
+  uint32_t num_blocks;
+  int8_t wide;
+  int8_t num_hashes;
+  int8_t valid;
+  int8_t pad;
+};
+
+struct LiteOut {
+  const void* src;
+  void* dst;
+  int32_t width;
+  int32_t pad;
+};
+
+struct LiteParams {
+  int64_t n_rows;
+  const int64_t* n_dev;
+  int32_t n_leaves;
+  int32_t n_probes;
+  int32_t n_out;
+  int32_t pad;
+  LiteLeaf leaves[kLiteMaxLeaves];
+  LiteProbe probes[kMaxBlooms];
+  LiteOut outs[kLiteMaxOut];
+  int32_t* out_rowids;
+  uint64_t* tile_status;
+  uint32_t* ticket;
+  DevStatus* status;
+};
+
+// Rows [row0, row0 + 4) of an integer column; full: all four exist (and the
+// column is 16-byte aligned), else only the rows in `mask` are read.
+__device__ __forceinline__ void lite_load4(const void* col, bool wide, int64_t row0, uint32_t mask, bool full,
+                                           int64_t v[kLiteItems]) {
+  if (wide) {
+    const long long* q = static_cast<const long long*>(col) + row0;
+    if (full) {
+      const longlong2 a = __ldg(reinterpret_cast<const longlong2*>(q));
+      const longlong2 b = __ldg(reinterpret_cast<const longlong2*>(q) + 1);
+      v[0] = a.x;
+      v[1] = a.y;
+      v[2] = b.x;
+      v[3] = b.y;
+    } else {
+#pragma unroll
+      for (int k = 0; k < kLiteItems; ++k) v[k] = ((mask >> k) & 1u) ? __ldg(q + k) : 0;
+    }
+  } else {
+    const int* q = static_cast<const int*>(col) + row0;
+    if (full) {
+      const int4 a = __ldg(reinterpret_cast<const int4*>(q));
+      v[0] = a.x;
+      v[1] = a.y;
+      v[2] = a.z;
+      v[3] = a.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < kLiteItems; ++k) v[k] = ((mask >> k) & 1u) ? __ldg(q + k) : 0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kLiteThreads) select_lite_kernel(const __grid_constant__ LiteParams p) {
+  __shared__ int s_warp[kLiteThreads / 32 + 1];
+  __shared__ uint32_t s_tile;
+  __shared__ uint64_t s_base;
+  const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
+  const int64_t n_tiles = (n_rows + kLiteTile - 1) / kLiteTile;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(p.ticket, 1u);
+    __syncthreads();
+    const int64_t tile = s_tile;
+    if (tile >= n_tiles) break;
+    const int64_t row0 = tile * kLiteTile + static_cast<int64_t>(threadIdx.x) * kLiteItems;
+    const int64_t rem = n_rows - row0;
+    const bool full = rem >= kLiteItems;
+    uint32_t mask = full ? 0xFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
+
+    // predicate: AND over clauses of OR over their leaves
+    if (p.n_leaves > 0 && mask != 0) {
+      uint32_t all = mask, any = 0;
+#pragma unroll 1
+      for (int l = 0; l < p.n_leaves; ++l) {
+        const LiteLeaf& L = p.leaves[l];
+        if (L.clause_start && l > 0) {
+          all &= any;
+          any = 0;
+        }
+        int64_t v[kLiteItems];
+        lite_load4(L.col, L.wide, row0, mask, full, v);
+#pragma unroll
+        for (int k = 0; k < kLiteItems; ++k) {
+          const uint32_t idx = (static_cast<uint32_t>(v[k] < L.lit) << 1) | static_cast<uint32_t>(v[k] == L.lit);
+          any |= ((static_cast<uint32_t>(L.truth) >> idx) & 1u) << k;
+        }
+      }
+      mask = all & any;
+    }
+
+    // bloom probes
+#pragma unroll 1
+    for (int pi = 0; pi < p.n_probes; ++pi) {
+      const LiteProbe& pr = p.probes[pi];
+      const bool valid = pr.valid_dev ? (*pr.valid_dev != 0) : (pr.valid != 0);
+      if (!valid || mask == 0) continue;
+      const uint32_t nb = pr.nblocks_dev ? static_cast<uint32_t>(*pr.nblocks_dev) : pr.num_blocks;
+      int64_t keys[kLiteItems];
+      lite_load4(pr.key, pr.wide, row0, mask, full, keys);
+      uint32_t keep = 0;
+#pragma unroll
+      for (int k = 0; k < kLiteItems; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const uint64_t h = hash_key(keys[k]);
+        const uint4* words = reinterpret_cast<const uint4*>(pr.blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8);
+        const uint4 lo = __ldg(words);
+        const uint4 hi = __ldg(words + 1);
+        const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+        keep |= static_cast<uint32_t>(bloom_test(w, h, pr.num_hashes)) << k;
+      }
+      mask &= keep;
+    }
+
+    // rank (block scan + decoupled look-back), then move the selected rows
+    const int cnt = __popc(mask);
+    int tile_total;
+    const int excl = block_exclusive_sum<kLiteThreads>(cnt, &tile_total, s_warp);
+    if (threadIdx.x < 32) {
+      const uint64_t b = lookback_exclusive(p.tile_status, tile, static_cast<uint64_t>(tile_total), p.status);
+      if (threadIdx.x == 0) s_base = b;
+    }
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(s_base);
+    if (mask != 0) {
+      const int64_t out0 = base + excl;
+#pragma unroll 1
+      for (int j = 0; j < p.n_out; ++j) {
+        const LiteOut& oc = p.outs[j];
+        int o = 0;
+        if (oc.width == 8) {
+#pragma unroll
+          for (int k = 0; k < kLiteItems; ++k)
+            if ((mask >> k) & 1u)
+              static_cast<long long*>(oc.dst)[out0 + o++] = __ldg(static_cast<const long long*>(oc.src) + row0 + k);
+        } else {
+#pragma unroll
+          for (int k = 0; k < kLiteItems; ++k)
+            if ((mask >> k) & 1u) static_cast<int*>(oc.dst)[out0 + o++] = __ldg(static_cast<const int*>(oc.src) + row0 + k);
+        }
+      }
+      if (p.out_rowids != nullptr) {
+        int o = 0;
+#pragma unroll
+        for (int k = 0; k < kLiteItems; ++k)
+          if ((mask >> k) & 1u) p.out_rowids[out0 + o++] = static_cast<int32_t>(row0 + k);
+      }
+    }
+    if (tile == n_tiles - 1 && threadIdx.x == 0) p.status->value = base + tile_total;
+    if (static_cast<int64_t>(gridDim.x) >= n_tiles) break;  // every tile was claimed by the first tickets
+    __syncthreads();
+  }
+}
+
+// The compact kernel's parameters for a select, or false when the select
+// needs the general kernel (a leaf that is not integer column vs integer
+// literal, an empty clause, too many leaves or outputs, or a column that is
+// not 16-byte aligned).
+bool lite_params(const SelectParams& p, LiteParams& lp) {
+  std::memset(&lp, 0, sizeof(lp));
+  auto aligned = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  // truth tables over (lt, eq) for LO_LT, LO_LE, LO_GT, LO_GE, LO_EQ, LO_NE
+  static const int8_t kTruth[6] = {4, 6, 1, 3, 2, 5};
+  static const int8_t kMirror[6] = {LO_GT, LO_GE, LO_LT, LO_LE, LO_EQ, LO_NE};
+  const Program& g = p.prog;
+  for (int c = 0; c < g.n_clauses; ++c) {
+    if (g.clause_begin[c] >= g.clause_begin[c + 1]) return false;
+    for (int l = g.clause_begin[c]; l < g.clause_begin[c + 1]; ++l) {
+      const Leaf& L = g.leaves[l];
+      if (L.op < LO_LT || L.op > LO_NE || L.cmp_vt != VT_I64) return false;
+      Operand a = L.lhs, b = L.rhs;
+      int op = L.op;
+      if (a.kind == OPND_LIT && b.kind == OPND_COL) {
+        std::swap(a, b);
+        op = kMirror[op];
+      }
+      if (a.kind != OPND_COL || b.kind != OPND_LIT || b.vt != VT_I64) return false;
+      const DevCol& dc = p.cols[a.col];
+      if ((dc.type != CT_I32 && dc.type != CT_I64 && dc.type != CT_DATE32) || !aligned(dc.data)) return false;
+      if (lp.n_leaves == kLiteMaxLeaves) return false;
+      LiteLeaf& o = lp.leaves[lp.n_leaves++];
+      o.col = dc.data;
+      o.lit = b.lit.i;
+      o.wide = dc.type == CT_I64 ? 1 : 0;
+      o.truth = kTruth[op];
+      o.clause_start = l == g.clause_begin[c] ? 1 : 0;
+    }
+  }
+  lp.n_probes = p.n_probes;
+  for (int pi = 0; pi < p.n_probes; ++pi) {
+    const BloomDev& b = p.probes[pi];
+    const DevCol& dc = p.cols[b.col];
+    if (!aligned(dc.data)) return false;
+    LiteProbe& o = lp.probes[pi];
+    o.blocks = b.blocks;
+    o.nblocks_dev = b.nblocks_dev;
+    o.valid_dev = b.valid_dev;
+    o.key = dc.data;
+    o.num_blocks = b.num_blocks;
+    o.wide = dc.type == CT_I64 ? 1 : 0;
+    o.num_hashes = b.num_hashes;
+    o.valid = b.valid;
+  }
+  if (p.n_out > kLiteMaxOut) return false;
+  lp.n_out = p.n_out;
+  for (int j = 0; j < p.n_out; ++j) {
+    lp.outs[j].src = p.outs[j].src;
+    lp.outs[j].dst = p.outs[j].dst;
+    lp.outs[j].width = p.outs[j].width;
+  }
+  lp.n_rows = p.n_rows;
+  lp.n_dev = p.n_dev;
+  lp.out_rowids = p.out_rowids;
+  return true;
+}
+
+int select_lite_blocks_per_sm() {
+  static const int per_sm = [] {
+    int v = 0;
+    GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, select_lite_kernel, kLiteThreads, 0));
+    return v < 1 ? 1 : v;
+  }();
+  return per_sm;
+}
+
 }  // namespace
 
 TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const std::vector<BloomProbe>& probes,
@@ -836,7 +1098,11 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     p.out_rowids = rowids->as<int32_t>();
   }
 
-  const int64_t n_tiles = (n + kSelTile - 1) / kSelTile;  // upper bound
+  // small inputs of the simple shapes take the compact kernel (its tiles are
+  // smaller, so the tile-status array is sized for them)
+  LiteParams lp;
+  const bool lite = n <= kLiteMaxRows && lite_params(p, lp);
+  const int64_t n_tiles = lite ? (n + kLiteTile - 1) / kLiteTile : (n + kSelTile - 1) / kSelTile;  // upper bound
   p.n_tiles = n_tiles;
   auto scratch = make_buffer(sizeof(DevStatus) + 64 + n_tiles * 8, s);
   char* sb = scratch->as<char>();
@@ -856,7 +1122,17 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     for (int i = 0; i < p.n_cols; ++i) evaluated |= p.cols[i].data == p.outs[j].src;
     if (!evaluated) proj_read += p.outs[j].width;
   }
-  if (n_tiles > 0) {
+  if (n_tiles > 0 && lite) {
+    lp.tile_status = p.tile_status;
+    lp.ticket = p.ticket;
+    lp.status = p.status;
+    const int64_t cap = static_cast<int64_t>(num_sms()) * select_lite_blocks_per_sm();
+    ProfScope prof("select_lite_kernel", s);
+    select_lite_kernel<<<static_cast<int>(n_tiles < cap ? n_tiles : cap), kLiteThreads, 0, s>>>(lp);
+    after_launch("select_lite_kernel");
+    prof.stop(0);
+    prof.set_bytes_model(p.n_dev, n, read_all, &p.status->value, proj_read + proj_write, scratch, in.rows_owner());
+  } else if (n_tiles > 0) {
     const size_t dyn = static_cast<size_t>(smem_words) * 4;
     const bool with_pred = p.prog.n_clauses > 0;
     // The pipelined probe-only kernel: no predicate, 16-byte aligned key

@@ -275,6 +275,9 @@ typedef struct gfpdb_exec_stats {
   int64_t d2h_bytes;         /* device->host bytes copied by this call */
   int64_t num_ops;           /* physical operators in the plan */
   int64_t messages;          /* messages delivered between operators */
+  int64_t device_ns;         /* replay of a captured plan: device time from the
+                                start of the plan graph to the end of its result
+                                copy (CUDA events); 0 for other runs */
 } gfpdb_exec_stats;
 
 /* Run a physical plan of the reference's operators (TableScanPOp, FilterPOp,

@@ -401,3 +401,44 @@ def test_csv_dense_and_sparse_tiles(gpu):
     with pytest.raises(GfpdbError) as ei:
         ops.csv_read(bytes(bad), fields, delimiter="|", has_header=True)
     assert "malformed" in ei.value.message
+
+
+LITE_PREDICATES = [
+    gt(num_lit(5), col("k")),  # literal on the left
+    lte(num_lit(-3, "int64"), col("i64")),
+    and_(gte(col("d"), num_lit(9000, "date32")), neq(col("k"), num_lit(4)), lte(col("i32"), num_lit(0))),
+    or_(*[eq(col("k"), num_lit(v)) for v in range(8)]),  # eight leaves in one clause
+    or_(*[eq(col("k"), num_lit(v)) for v in range(9)]),  # nine: beyond the compact kernel's leaves
+    and_(or_(lt(col("i32"), num_lit(-500)), gt(col("i64"), num_lit(0, "int64"))), eq(col("k"), num_lit(1))),
+]
+
+
+@pytest.mark.parametrize("pi", range(len(LITE_PREDICATES)))
+@pytest.mark.parametrize("n", [3, 1023, 1024, 1025, 262_143, 262_144, 262_145])
+def test_filter_small_input_shapes(gpu, pi, n):
+    """Inputs up to 2^18 rows with integer column-vs-literal predicates (the
+    compact selection kernel) and just past it (the general kernel), at tile
+    edges, with utf8 and float outputs moved as well."""
+    t = rand_table(n, seed=7 * n + pi)
+    pred = LITE_PREDICATES[pi]
+    got = ops.Filter(pred, t).evaluate(t)
+    assert got.rows() == oops.filter_table(t, pred).rows()
+
+
+@pytest.mark.parametrize("n", [1, 777, 4096, 200_000])
+def test_small_select_with_probes_and_predicate(gpu, n):
+    """Bloom probes on int32 and int64 keys together with a predicate, over
+    small inputs."""
+    rng = np.random.default_rng(n)
+    t = Table([Column("a", "int32", rng.integers(0, 5000, n)), Column("b", "int64", rng.integers(-10**9, 10**9, n)),
+               Column("c", "int32", rng.integers(0, 100, n)), Column("s", "utf8", [f"v{x}" for x in range(n)])])
+    ka = rng.choice(5000, 700, replace=False).astype(np.int64)
+    kb = np.asarray(t["b"], dtype=np.int64)[rng.random(n) < 0.5]
+    ta = Table([Column("a", "int32", ka)])
+    tb = Table([Column("b", "int64", kb)])
+    blooms = [(ops.BloomFilter([ta], "a"), "a"), (ops.BloomFilter([tb], "b", 12, 4), "b")]
+    pred = and_(lt(col("c"), num_lit(60)), neq(col("c"), num_lit(7)))
+    got = ops.select(DeviceTable.from_host(t), ops.Filter(pred, t), blooms)
+    want = oops.bloom_use(oops.bloom_use(oops.filter_table(t, pred), oops.bloom_words(ka), "a"),
+                          oops.bloom_words(kb, 12, 4), "b", 4)
+    assert got.rows() == want.rows()
