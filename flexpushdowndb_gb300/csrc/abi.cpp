@@ -135,7 +135,7 @@ struct ArenaGuard {
 };
 
 std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::map<std::string, pop::InputTable>& inputs,
-                                           int64_t arena_bytes) {
+                                           int64_t arena_bytes, const int64_t fill_bytes[2]) {
   auto cp = std::make_shared<CapturedPlan>();
   cudaStream_t cs = nullptr;
   GF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -150,10 +150,24 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
   const int64_t h2d0 = copy_counters().h2d;
   cudaGraph_t graph = nullptr;
   bool ok = true;
+  // The buffers the operators want pre-filled (sized by the ordinary run,
+  // with room to spare) come from two regions that the graph fills first.
+  FillPool pool;
+  for (int k = 0; k < 2; ++k) {
+    if (fill_bytes[k] <= 0) continue;
+    pool.size[k] = fill_bytes[k] + fill_bytes[k] / 4 + 4096;
+    pool.base[k] = static_cast<char*>(cp->arena->take(pool.size[k]));
+  }
   {
     ArenaGuard ag(cp->arena.get());
+    struct PoolGuard {
+      explicit PoolGuard(FillPool* p) { set_thread_fill_pool(p); }
+      ~PoolGuard() { set_thread_fill_pool(nullptr); }
+    } pg(&pool);
     GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
+      for (int k = 0; k < 2; ++k)
+        if (pool.size[k] > 0) GF_CUDA(cudaMemsetAsync(pool.base[k], k == 0 ? 0 : 0xFF, pool.size[k], cs));
       auto ex = pop::build_execution(plan, cs);
       ex->setInputs(inputs);
       ex->setDeferred(true);
@@ -775,10 +789,16 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
       // memory the plan needs), then the capture; a replay that overflowed
       // lands here too and gets the exact re-run.
       const int64_t a0 = thread_alloc_bytes();
+      int64_t f0[2], f1[2];
+      thread_filled_bytes(f0);
       result = run();
       if (!cp) {
         const int64_t bytes = thread_alloc_bytes() - a0;
-        cp = capture_plan(plan, inputs, bytes + bytes / 4 + (int64_t{1} << 20));
+        thread_filled_bytes(f1);
+        const int64_t fills[2] = {f1[0] - f0[0], f1[1] - f0[1]};
+        // the arena also holds the fill regions' spare room
+        const int64_t spare = (fills[0] + fills[1]) / 4 + 8192;
+        cp = capture_plan(plan, inputs, bytes + bytes / 4 + spare + (int64_t{1} << 20), fills);
         std::lock_guard<std::mutex> lk(g_graph_mu);
         g_graphs[key] = cp;
       }

@@ -102,6 +102,34 @@ thread_local int64_t g_thread_alloc = 0;
 void set_thread_arena(Arena* a) { g_thread_arena = a; }
 int64_t thread_alloc_bytes() { return g_thread_alloc; }
 
+namespace {
+thread_local FillPool* g_fill_pool = nullptr;
+thread_local int64_t g_filled[2] = {0, 0};
+}  // namespace
+
+void set_thread_fill_pool(FillPool* p) { g_fill_pool = p; }
+
+void thread_filled_bytes(int64_t out[2]) {
+  out[0] = g_filled[0];
+  out[1] = g_filled[1];
+}
+
+BufferPtr make_filled(int64_t bytes, int value, cudaStream_t s) {
+  if (value != 0 && value != 0xFF) fail(GFPDB_EINVAL, "make_filled takes the byte values 0 and 0xFF");
+  const int k = value == 0 ? 0 : 1;
+  const int64_t n = ((bytes > 16 ? bytes : 16) + 255) / 256 * 256;
+  g_filled[k] += n;
+  FillPool* fp = g_fill_pool;
+  if (fp != nullptr && fp->used[k] + n <= fp->size[k]) {
+    char* p = fp->base[k] + fp->used[k];
+    fp->used[k] += n;
+    return std::make_shared<DeviceBuffer>(p, bytes);
+  }
+  auto b = make_buffer(bytes, s);
+  if (bytes > 0) GF_CUDA(cudaMemsetAsync(b->data(), value, static_cast<size_t>(bytes), s));
+  return b;
+}
+
 Arena::Arena(int64_t bytes, cudaStream_t s) : size_(bytes) {
   Arena* saved = g_thread_arena;
   g_thread_arena = nullptr;  // the arena's own memory comes from the pool

@@ -131,6 +131,25 @@ class Arena {
 };
 // Activate `a` for this thread (nullptr deactivates).
 void set_thread_arena(Arena* a);
+
+// Buffers that must start out filled with one byte value, 0 or 0xFF (status
+// blocks, tickets, tile states, hash-table slots, filter words). Normally an
+// allocation and a memset on the stream. While a fill pool is active on the
+// thread (a plan being captured into a CUDA graph) they are carved from the
+// pool's region for that value, which the graph fills with one memset at its
+// start, so the plan's operators add no memset nodes of their own.
+BufferPtr make_filled(int64_t bytes, int value, cudaStream_t s);
+
+struct FillPool {
+  char* base[2] = {nullptr, nullptr};  // [0]: zeros, [1]: 0xFF bytes
+  int64_t size[2] = {0, 0};
+  int64_t used[2] = {0, 0};
+};
+// Activate `p` for this thread (nullptr deactivates).
+void set_thread_fill_pool(FillPool* p);
+// Bytes this thread has asked make_filled for, per value (zeros, 0xFF),
+// each request rounded up to 256.
+void thread_filled_bytes(int64_t out[2]);
 // Bytes this thread has allocated through DeviceBuffer (rounded to 256).
 int64_t thread_alloc_bytes();
 

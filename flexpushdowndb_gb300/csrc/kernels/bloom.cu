@@ -100,8 +100,7 @@ BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_p
   int64_t nb = (n_alloc * bits_per_key + 255) / 256;
   if (nb < 1) nb = 1;
   bf->num_blocks = nb;  // exact size, or the capacity of a device-sized filter
-  bf->blocks = make_buffer(nb * 32, s);
-  GF_CUDA(cudaMemsetAsync(bf->blocks->data(), 0, nb * 32, s));
+  bf->blocks = make_filled(nb * 32, 0, s);
   BloomSizeParams sp{};
   if (deferred) {
     if (key_parts.size() > static_cast<size_t>(kMaxBloomParts))

@@ -592,8 +592,7 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   p.virtual_end = virtual_end ? 1 : 0;
   p.delim = static_cast<uint8_t>(delimiter);
   for (int i = 0; i < kCsvMaxFields; ++i) p.slot[i] = -1;
-  auto status = make_buffer(sizeof(DevStatus), s);
-  GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+  auto status = make_filled(sizeof(DevStatus), 0, s);
   p.st = status->as<DevStatus>();
   for (size_t k = 0; k < emit.size(); ++k) {
     const CsvField& f = fields[emit[k]];

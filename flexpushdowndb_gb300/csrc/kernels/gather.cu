@@ -204,12 +204,11 @@ int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStrea
   }
   const int64_t n_tiles = (n + kScanTile - 1) / kScanTile;
   // scratch: status block, ticket, tile words
-  auto scratch = make_buffer(sizeof(DevStatus) + 64 + n_tiles * 8, s);
+  auto scratch = make_filled(sizeof(DevStatus) + 64 + n_tiles * 8, 0, s);
   char* base = scratch->as<char>();
   DevStatus* st = reinterpret_cast<DevStatus*>(base);
   uint32_t* ticket = reinterpret_cast<uint32_t*>(base + sizeof(DevStatus));
   uint64_t* tiles = reinterpret_cast<uint64_t*>(base + sizeof(DevStatus) + 64);
-  GF_CUDA(cudaMemsetAsync(base, 0, scratch->size(), s));
   int grid = static_cast<int>(n_tiles < num_sms() * 4 ? n_tiles : num_sms() * 4);
   scan_i32_kernel<<<grid, kScanThreads, 0, s>>>(in, out, n, n_tiles, tiles, ticket, st);
   after_launch("scan_i32_kernel");

@@ -475,10 +475,7 @@ class StringDict {
   }
 
   void ensure(int64_t more_codes, int64_t more_bytes, cudaStream_t s) {
-    if (!status) {
-      status = make_buffer(sizeof(DevStatus), s);
-      GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
-    }
+    if (!status) status = make_filled(sizeof(DevStatus), 0, s);
     int64_t codes_real = 0, bytes_real = 0;
     const bool grow_slots = static_cast<uint64_t>(2 * (codes_upper + more_codes)) > cap;
     const bool grow_codes = codes_upper + more_codes > code_cap;
@@ -514,10 +511,8 @@ class StringDict {
     }
     uint64_t want = next_pow2(static_cast<uint64_t>(2 * need_codes < 1024 ? 1024 : 2 * need_codes));
     if (want > cap) {
-      slot_hash = make_buffer(static_cast<int64_t>(want) * 8, s);
-      slot_code = make_buffer(static_cast<int64_t>(want) * 4, s);
-      GF_CUDA(cudaMemsetAsync(slot_hash->data(), 0xFF, want * 8, s));
-      GF_CUDA(cudaMemsetAsync(slot_code->data(), 0, want * 4, s));
+      slot_hash = make_filled(static_cast<int64_t>(want) * 8, 0xFF, s);
+      slot_code = make_filled(static_cast<int64_t>(want) * 4, 0, s);
       cap = want;
       if (codes_real > 0) {
         dict_rehash_kernel<<<grid_for(codes_real), 256, 0, s>>>(dev(), codes_real);
@@ -667,10 +662,7 @@ class GroupTable {
     group_init_kernel<<<grid_for(static_cast<int64_t>(new_cap + 1)), 256, 0, s>>>(
         nk->as<uint64_t>(), na_buf->as<unsigned long long>(), new_cap + 1, na, kinds);
     after_launch("group_init_kernel");
-    if (!status) {
-      status = make_buffer(sizeof(DevStatus), s);
-      GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
-    }
+    if (!status) status = make_filled(sizeof(DevStatus), 0, s);
     if (cap > 0) {
       group_rehash_kernel<<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(
           keys->as<uint64_t>(), accbuf->as<unsigned long long>(), cap, nk->as<uint64_t>(),
@@ -810,8 +802,7 @@ class GroupTable {
       fp.outs[j] = outs[j];
       fp.outs[j].dst = agg_out[j]->data();
     }
-    auto counter = make_buffer(8, s);
-    GF_CUDA(cudaMemsetAsync(counter->data(), 0, 8, s));
+    auto counter = make_filled(8, 0, s);
     fp.counter = counter->as<unsigned long long>();
     group_finalize_kernel<<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(fp);
     after_launch("group_finalize_kernel");

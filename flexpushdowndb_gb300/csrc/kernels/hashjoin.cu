@@ -211,10 +211,9 @@ void join_build_table(JoinTable& t, double load_factor, cudaStream_t s) {
   uint64_t cap = 64;
   while (static_cast<double>(cap) * load_factor < static_cast<double>(n)) cap <<= 1;
   t.capacity = cap;
-  t.slots = make_buffer(static_cast<int64_t>(cap) * 8 + sizeof(DevStatus), s);
-  GF_CUDA(cudaMemsetAsync(t.slots->data(), 0xFF, cap * 8, s));
-  DevStatus* st = reinterpret_cast<DevStatus*>(t.slots->as<char>() + cap * 8);
-  GF_CUDA(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
+  t.slots = make_filled(static_cast<int64_t>(cap) * 8, 0xFF, s);
+  t.status = make_filled(sizeof(DevStatus), 0, s);
+  DevStatus* st = t.status->as<DevStatus>();
   const auto& kc = t.build->column(t.key_col);
   t.key_type = kc->type;
   if (n > 0) {
@@ -262,7 +261,7 @@ std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet
     from_build.push_back(1);
   }
   p.n_out = static_cast<int32_t>(srcs.size());
-  auto status = make_buffer(sizeof(DevStatus), s);
+  auto status = make_filled(sizeof(DevStatus), 0, s);
   const bool defer = deferred_mode() && count_dev != nullptr;
   int64_t cap = n > 0 ? n : 1;
   std::vector<BufferPtr> bufs(srcs.size());
@@ -278,7 +277,7 @@ std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet
     }
     p.cap = cap;
     p.st = status->as<DevStatus>();
-    GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    if (attempt > 0) GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
     if (n > 0 && t.build->num_rows() > 0) {
       ProfScope prof("join_probe_emit_kernel", s);
       join_probe_emit_kernel<<<grid_for(n), 256, 0, s>>>(p);
@@ -330,12 +329,12 @@ void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, 
   DevCol pk{pc->data, nullptr, static_cast<int32_t>(pc->type), 0};
   DevCol bkc{bk->data, nullptr, static_cast<int32_t>(bk->type), 0};
   int64_t cap = n > 0 ? n : 1;
-  auto status = make_buffer(sizeof(DevStatus), s);
+  auto status = make_filled(sizeof(DevStatus), 0, s);
   const bool defer = deferred_mode() && count_dev != nullptr;
   for (int attempt = 0; attempt < 2; ++attempt) {
     *probe_idx = make_buffer(cap * 4, s);
     *build_idx = make_buffer(cap * 4, s);
-    GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    if (attempt > 0) GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
     if (n > 0 && t.build->num_rows() > 0) {
       ProfScope prof("join_probe_kernel", s);
       join_probe_kernel<<<grid_for(n), 256, 0, s>>>(pk, n, probe.rows_dev(), t.slots->as<uint64_t>(),

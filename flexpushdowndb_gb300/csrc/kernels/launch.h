@@ -89,6 +89,7 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
 
 struct JoinTable {
   BufferPtr slots;          // capacity uint64 (tag << 32 | build row)
+  BufferPtr status;         // build diagnostics: longest probe run, duplicate keys
   uint64_t capacity = 0;    // power of two
   TupleSetPtr build;        // concatenated build side
   int key_col = -1;

@@ -1104,12 +1104,11 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   const bool lite = n <= kLiteMaxRows && lite_params(p, lp);
   const int64_t n_tiles = lite ? (n + kLiteTile - 1) / kLiteTile : (n + kSelTile - 1) / kSelTile;  // upper bound
   p.n_tiles = n_tiles;
-  auto scratch = make_buffer(sizeof(DevStatus) + 64 + n_tiles * 8, s);
+  auto scratch = make_filled(sizeof(DevStatus) + 64 + n_tiles * 8, 0, s);
   char* sb = scratch->as<char>();
   p.status = reinterpret_cast<DevStatus*>(sb);
   p.ticket = reinterpret_cast<uint32_t*>(sb + sizeof(DevStatus));
   p.tile_status = reinterpret_cast<uint64_t*>(sb + sizeof(DevStatus) + 64);
-  GF_CUDA(cudaMemsetAsync(sb, 0, scratch->size(), s));
 
   // Algorithmic bytes: every evaluated column read once over all rows, the
   // selected rows of the other projected columns read once, every projected
