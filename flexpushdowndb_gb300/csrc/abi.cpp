@@ -43,9 +43,9 @@ void require(bool cond, const char* what) {
 struct CapturedPlan {
   std::unique_ptr<Arena> arena;
   cudaGraphExec_t exec = nullptr;
-  // Epilogue graph: packs every status block and the result (row count and
-  // columns) into one arena buffer and copies it to pinned host memory.
-  cudaGraphExec_t epilogue = nullptr;
+  // The graph ends with one kernel that packs every status block and the
+  // result (row count and columns) straight into this page-locked buffer,
+  // which the device reaches through unified addressing.
   char* pinned = nullptr;
   int64_t pinned_bytes = 0;
   std::vector<int64_t> status_off;
@@ -62,13 +62,13 @@ struct CapturedPlan {
     for (auto e : ev)
       if (e) (void)cudaEventDestroy(e);
     if (exec) (void)cudaGraphExecDestroy(exec);
-    if (epilogue) (void)cudaGraphExecDestroy(epilogue);
     if (pinned) (void)cudaFreeHost(pinned);
   }
 };
 
-// Capture the epilogue of a captured plan (see CapturedPlan::epilogue).
-bool capture_epilogue(CapturedPlan& cp, cudaStream_t cs) {
+// The end of a captured plan, issued on the capturing stream: one pack of
+// every status block and of the result into the page-locked buffer.
+void capture_epilogue(CapturedPlan& cp, cudaStream_t cs) {
   std::vector<CopySpan> spans;
   int64_t off = 0;
   auto add = [&](const void* src, int64_t bytes) {
@@ -85,7 +85,7 @@ bool capture_epilogue(CapturedPlan& cp, cudaStream_t cs) {
   for (int i = 0; i < r.num_columns(); ++i) {
     const auto& c = r.column(i);
     if (c->type == DType::Utf8) {
-      if (!c->data_buf) return false;
+      if (!c->data_buf) fail(GFPDB_EUNSUPPORTED, "captured plan result without its own string buffer");
       const int64_t o1 = add(c->offsets, (cap + 1) * 4);
       const int64_t o2 = add(c->data, c->data_buf->size());
       cp.col_off.push_back({o1, o2});
@@ -94,22 +94,14 @@ bool capture_epilogue(CapturedPlan& cp, cudaStream_t cs) {
     }
   }
   cp.pinned_bytes = off > 0 ? off : 256;
-  GF_CUDA(cudaMallocHost(reinterpret_cast<void**>(&cp.pinned), cp.pinned_bytes));
-  void* dev = cp.arena->take(cp.pinned_bytes);
-  cudaGraph_t graph = nullptr;
-  bool ok = true;
-  GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-  try {
-    pack_spans(spans, dev, cs);
-    GF_CUDA(cudaMemcpyAsync(cp.pinned, dev, cp.pinned_bytes, cudaMemcpyDeviceToHost, cs));
-  } catch (const std::exception&) {
-    ok = false;
-  }
-  if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) ok = false;
-  if (ok && cudaGraphInstantiate(&cp.epilogue, graph, 0) != cudaSuccess) ok = false;
-  if (graph) (void)cudaGraphDestroy(graph);
-  (void)cudaGetLastError();
-  return ok;
+  // page-locked allocation is not a stream operation: allowed mid-capture
+  // under the relaxed mode
+  cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+  GF_CUDA(cudaThreadExchangeStreamCaptureMode(&mode));
+  const cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&cp.pinned), cp.pinned_bytes);
+  GF_CUDA(cudaThreadExchangeStreamCaptureMode(&mode));
+  GF_CUDA(e);
+  pack_spans(spans, cp.pinned, cs);
 }
 
 std::mutex g_graph_mu;
@@ -135,7 +127,7 @@ struct ArenaGuard {
 };
 
 std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::map<std::string, pop::InputTable>& inputs,
-                                           int64_t arena_bytes, const int64_t fill_bytes[2]) {
+                                           int64_t arena_bytes, const int64_t fill_bytes[2][2]) {
   auto cp = std::make_shared<CapturedPlan>();
   cudaStream_t cs = nullptr;
   GF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -151,13 +143,29 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
   cudaGraph_t graph = nullptr;
   bool ok = true;
   // The buffers the operators want pre-filled (sized by the ordinary run,
-  // with room to spare) come from two regions that the graph fills first.
+  // with room to spare) come from regions that the graph fills first: the
+  // small ones on the capturing stream, the large ones on a side stream.
   FillPool pool;
-  for (int k = 0; k < 2; ++k) {
-    if (fill_bytes[k] <= 0) continue;
-    pool.size[k] = fill_bytes[k] + fill_bytes[k] / 4 + 4096;
-    pool.base[k] = static_cast<char*>(cp->arena->take(pool.size[k]));
-  }
+  for (int t = 0; t < 2; ++t)
+    for (int k = 0; k < 2; ++k) {
+      if (fill_bytes[t][k] <= 0) continue;
+      pool.size[t][k] = fill_bytes[t][k] + fill_bytes[t][k] / 4 + 4096;
+      pool.base[t][k] = static_cast<char*>(cp->arena->take(pool.size[t][k]));
+    }
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr;
+  GF_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  GF_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  GF_CUDA(cudaEventCreateWithFlags(&pool.large_ready, cudaEventDisableTiming));
+  struct SideGuard {
+    cudaStream_t s;
+    cudaEvent_t a, b;
+    ~SideGuard() {
+      (void)cudaEventDestroy(a);
+      (void)cudaEventDestroy(b);
+      (void)cudaStreamDestroy(s);
+    }
+  } side_guard{side, fork, pool.large_ready};
   {
     ArenaGuard ag(cp->arena.get());
     struct PoolGuard {
@@ -167,7 +175,12 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
     GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
       for (int k = 0; k < 2; ++k)
-        if (pool.size[k] > 0) GF_CUDA(cudaMemsetAsync(pool.base[k], k == 0 ? 0 : 0xFF, pool.size[k], cs));
+        if (pool.size[0][k] > 0) GF_CUDA(cudaMemsetAsync(pool.base[0][k], k == 0 ? 0 : 0xFF, pool.size[0][k], cs));
+      GF_CUDA(cudaEventRecord(fork, cs));
+      GF_CUDA(cudaStreamWaitEvent(side, fork, 0));
+      for (int k = 0; k < 2; ++k)
+        if (pool.size[1][k] > 0) GF_CUDA(cudaMemsetAsync(pool.base[1][k], k == 0 ? 0 : 0xFF, pool.size[1][k], side));
+      GF_CUDA(cudaEventRecord(pool.large_ready, side));
       auto ex = pop::build_execution(plan, cs);
       ex->setInputs(inputs);
       ex->setDeferred(true);
@@ -176,6 +189,8 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
       cp->checks = ex->takeCapturedChecks();
       cp->num_ops = ex->stats().num_ops;
       cp->messages = ex->stats().messages;
+      capture_epilogue(*cp, cs);
+      GF_CUDA(cudaStreamWaitEvent(cs, pool.large_ready, 0));  // the side stream rejoins
     } catch (const std::exception&) {
       ok = false;  // something in the plan needs the host mid-run
     }
@@ -187,19 +202,8 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
   if (graph != nullptr) (void)cudaGraphDestroy(graph);
   (void)cudaGetLastError();
   cp->h2d = copy_counters().h2d - h2d0;
-  if (ok) {
-    try {
-      ok = capture_epilogue(*cp, cs);
-    } catch (const std::exception&) {
-      ok = false;
-    }
-  }
   cp->kernels = g_kernel_launches.load() - k0;
   if (!ok) {
-    if (cp->epilogue) {
-      (void)cudaGraphExecDestroy(cp->epilogue);
-      cp->epilogue = nullptr;
-    }
     cp->capturable = false;
     cp->result.reset();
     cp->checks.clear();
@@ -286,7 +290,6 @@ bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowD
   }
   GF_CUDA(cudaEventRecord(cp.ev[0], s));
   GF_CUDA(cudaGraphLaunch(cp.exec, s));
-  GF_CUDA(cudaGraphLaunch(cp.epilogue, s));
   GF_CUDA(cudaEventRecord(cp.ev[1], s));
   count_launch(cp.kernels);
   sync(s);
@@ -569,8 +572,7 @@ int32_t gfpdb_hashjoin_info(const gfpdb_hashjoin* join, int64_t* build_rows, int
       *max_probe = 0;
       if (join->built) {
         DevStatus st;
-        GF_CUDA(cudaMemcpy(&st, join->table.slots->as<char>() + join->table.capacity * 8, sizeof(st),
-                           cudaMemcpyDeviceToHost));
+        GF_CUDA(cudaMemcpy(&st, join->table.status->data(), sizeof(st), cudaMemcpyDeviceToHost));
         *max_probe = st.aux[0];
       }
     }
@@ -789,15 +791,18 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
       // memory the plan needs), then the capture; a replay that overflowed
       // lands here too and gets the exact re-run.
       const int64_t a0 = thread_alloc_bytes();
-      int64_t f0[2], f1[2];
+      int64_t f0[2][2], f1[2][2];
       thread_filled_bytes(f0);
       result = run();
       if (!cp) {
         const int64_t bytes = thread_alloc_bytes() - a0;
         thread_filled_bytes(f1);
-        const int64_t fills[2] = {f1[0] - f0[0], f1[1] - f0[1]};
-        // the arena also holds the fill regions' spare room
-        const int64_t spare = (fills[0] + fills[1]) / 4 + 8192;
+        int64_t fills[2][2], spare = 0;
+        for (int t = 0; t < 2; ++t)
+          for (int k = 0; k < 2; ++k) {
+            fills[t][k] = f1[t][k] - f0[t][k];
+            spare += fills[t][k] / 4 + 4096;  // the arena also holds the fill regions' spare room
+          }
         cp = capture_plan(plan, inputs, bytes + bytes / 4 + spare + (int64_t{1} << 20), fills);
         std::lock_guard<std::mutex> lk(g_graph_mu);
         g_graphs[key] = cp;

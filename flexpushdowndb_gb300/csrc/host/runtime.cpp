@@ -104,25 +104,27 @@ int64_t thread_alloc_bytes() { return g_thread_alloc; }
 
 namespace {
 thread_local FillPool* g_fill_pool = nullptr;
-thread_local int64_t g_filled[2] = {0, 0};
+thread_local int64_t g_filled[2][2] = {{0, 0}, {0, 0}};
 }  // namespace
 
 void set_thread_fill_pool(FillPool* p) { g_fill_pool = p; }
 
-void thread_filled_bytes(int64_t out[2]) {
-  out[0] = g_filled[0];
-  out[1] = g_filled[1];
+void thread_filled_bytes(int64_t out[2][2]) {
+  for (int t = 0; t < 2; ++t)
+    for (int k = 0; k < 2; ++k) out[t][k] = g_filled[t][k];
 }
 
 BufferPtr make_filled(int64_t bytes, int value, cudaStream_t s) {
   if (value != 0 && value != 0xFF) fail(GFPDB_EINVAL, "make_filled takes the byte values 0 and 0xFF");
   const int k = value == 0 ? 0 : 1;
+  const int t = bytes >= kFillLargeBytes ? 1 : 0;
   const int64_t n = ((bytes > 16 ? bytes : 16) + 255) / 256 * 256;
-  g_filled[k] += n;
+  g_filled[t][k] += n;
   FillPool* fp = g_fill_pool;
-  if (fp != nullptr && fp->used[k] + n <= fp->size[k]) {
-    char* p = fp->base[k] + fp->used[k];
-    fp->used[k] += n;
+  if (fp != nullptr && fp->used[t][k] + n <= fp->size[t][k]) {
+    char* p = fp->base[t][k] + fp->used[t][k];
+    fp->used[t][k] += n;
+    if (t == 1) GF_CUDA(cudaStreamWaitEvent(s, fp->large_ready, 0));
     return std::make_shared<DeviceBuffer>(p, bytes);
   }
   auto b = make_buffer(bytes, s);

@@ -136,20 +136,27 @@ void set_thread_arena(Arena* a);
 // blocks, tickets, tile states, hash-table slots, filter words). Normally an
 // allocation and a memset on the stream. While a fill pool is active on the
 // thread (a plan being captured into a CUDA graph) they are carved from the
-// pool's region for that value, which the graph fills with one memset at its
-// start, so the plan's operators add no memset nodes of their own.
+// pool's region for that value and size class, which the graph fills with one
+// memset at its start, so the plan's operators add no memset nodes of their
+// own. Small buffers come from regions filled on the capturing stream before
+// anything else; large ones (capacity-sized tables and filters) from regions
+// filled on a side stream, overlapping the plan's first operators, and a
+// stream that takes one waits for that fill.
 BufferPtr make_filled(int64_t bytes, int value, cudaStream_t s);
 
+constexpr int64_t kFillLargeBytes = 64 * 1024;
+
 struct FillPool {
-  char* base[2] = {nullptr, nullptr};  // [0]: zeros, [1]: 0xFF bytes
-  int64_t size[2] = {0, 0};
-  int64_t used[2] = {0, 0};
+  char* base[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [small, large][zeros, 0xFF]
+  int64_t size[2][2] = {{0, 0}, {0, 0}};
+  int64_t used[2][2] = {{0, 0}, {0, 0}};
+  cudaEvent_t large_ready = nullptr;  // recorded after the large regions are filled
 };
 // Activate `p` for this thread (nullptr deactivates).
 void set_thread_fill_pool(FillPool* p);
-// Bytes this thread has asked make_filled for, per value (zeros, 0xFF),
-// each request rounded up to 256.
-void thread_filled_bytes(int64_t out[2]);
+// Bytes this thread has asked make_filled for, per size class and value
+// ([small, large][zeros, 0xFF]), each request rounded up to 256.
+void thread_filled_bytes(int64_t out[2][2]);
 // Bytes this thread has allocated through DeviceBuffer (rounded to 256).
 int64_t thread_alloc_bytes();
 

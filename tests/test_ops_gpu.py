@@ -442,3 +442,17 @@ def test_small_select_with_probes_and_predicate(gpu, n):
     want = oops.bloom_use(oops.bloom_use(oops.filter_table(t, pred), oops.bloom_words(ka), "a"),
                           oops.bloom_words(kb, 12, 4), "b", 4)
     assert got.rows() == want.rows()
+
+
+def test_join_info_after_build(gpu):
+    """Build-side statistics: rows, table capacity (power of two at load
+    factor 0.5) and the longest probe run the build recorded."""
+    keys = np.arange(10_000, dtype=np.int64) * 3
+    build = Table([Column("pk", "int32", keys), Column("v", "int32", np.arange(10_000))])
+    j = ops.HashJoin("pk", "fk")
+    j.put_build(build)
+    j.finalize_build()
+    info = j.info()
+    assert info["build_rows"] == 10_000
+    assert info["capacity"] == 32_768
+    assert 0 <= info["max_probe"] < 64  # linear probing at load 0.31
