@@ -174,12 +174,14 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
     } pg(&pool);
     GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
-      for (int k = 0; k < 2; ++k)
-        if (pool.size[0][k] > 0) GF_CUDA(cudaMemsetAsync(pool.base[0][k], k == 0 ? 0 : 0xFF, pool.size[0][k], cs));
+      // one fill kernel per size class (kernel nodes follow each other more
+      // closely than memset nodes)
+      const FillSpan small[2] = {{pool.base[0][0], pool.size[0][0], 0, 0}, {pool.base[0][1], pool.size[0][1], 0xFF, 0}};
+      const FillSpan large[2] = {{pool.base[1][0], pool.size[1][0], 0, 0}, {pool.base[1][1], pool.size[1][1], 0xFF, 0}};
+      fill_regions(small, 2, cs);
       GF_CUDA(cudaEventRecord(fork, cs));
       GF_CUDA(cudaStreamWaitEvent(side, fork, 0));
-      for (int k = 0; k < 2; ++k)
-        if (pool.size[1][k] > 0) GF_CUDA(cudaMemsetAsync(pool.base[1][k], k == 0 ? 0 : 0xFF, pool.size[1][k], side));
+      fill_regions(large, 2, side);
       GF_CUDA(cudaEventRecord(pool.large_ready, side));
       auto ex = pop::build_execution(plan, cs);
       ex->setInputs(inputs);

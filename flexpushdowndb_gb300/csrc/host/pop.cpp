@@ -643,6 +643,8 @@ void Execution::assignStreams() {
     int st = -1;
     for (auto& pn : o->producers()) {
       const PhysicalOp* p = op(pn);
+      // filter builds along a chain of BloomFilterCreatePOps run side by side
+      if (p->getTypeString() == "BloomFilterCreatePOp" && o->getTypeString() == "BloomFilterCreatePOp") continue;
       if (!continued.count(p)) {
         continued.insert(p);
         st = op_stream_[p];
@@ -664,6 +666,12 @@ cudaStream_t Execution::streamOf(const PhysicalOp* op) const {
 
 void Execution::stamp(Message& msg, const PhysicalOp* sender) {
   if (streams_.size() <= 1) return;
+  // A COMPLETE carries no device dependency: every TUPLESET and BLOOM_FILTER
+  // before it was waited for on arrival, and ordering work after the
+  // sender's own later kernels would only serialise independent operators
+  // (a chain of BloomFilterCreatePOps, each forwarding its input, would
+  // build its filters one after another).
+  if (msg.type == MessageType::COMPLETE) return;
   auto it = op_stream_.find(sender);
   msg.stream = it == op_stream_.end() ? 0 : it->second;
   msg.ready = pooled_event(events_used_++);

@@ -37,6 +37,16 @@ struct CopySpan {
 };
 void pack_spans(const std::vector<CopySpan>& spans, void* dst, cudaStream_t s);
 
+// Fill up to two regions (16-byte aligned, sizes multiples of 16) with one
+// byte value each, in one kernel launch.
+struct FillSpan {
+  void* dst;
+  int64_t bytes;
+  int32_t value;
+  int32_t pad;
+};
+void fill_regions(const FillSpan* spans, int n, cudaStream_t s);
+
 // Host-to-device copy of a scan's input: the copy engine (cudaMemcpyAsync),
 // or, with host_copy_mode() == 1 and page-locked aligned sources of at least
 // 1 MiB, a kernel whose loads read host memory over the chip-to-chip link.
