@@ -396,36 +396,40 @@ struct SpLayout {
   int32_t bloom_off;              // byte offset of the staged filter in dynamic shared memory
 };
 
-// Bloom test of 8 keys against one filter with NH hashes: bit positions
-// from the low 32 bits of each key's hash (bloom.cuh). `blocks` is the
-// filter in shared memory (in_smem) or global memory.
-template <int NH>
-__device__ __forceinline__ uint32_t probe8(const uint32_t* blocks, bool in_smem, uint32_t nb, const int64_t keys[8],
-                                           uint32_t mask) {
+// The first probe over a thread's 8 rows: the bloom test of each key with NH
+// hashes, bit positions from the low 32 bits of the key's hash (bloom.cuh).
+// IN_SMEM: the filter sits in shared memory (the pointer derives from the
+// kernel's shared array, so the tests compile to shared-memory loads); else
+// it is read through L1/L2.
+template <bool IN_SMEM, int NH>
+__device__ __forceinline__ uint32_t probe8(const uint32_t* blocks, uint32_t nb, const int64_t keys[8], uint32_t mask) {
   uint32_t keep = 0;
 #pragma unroll
   for (int kk = 0; kk < kSelItems; ++kk) {
-    if (!((mask >> kk) & 1u)) continue;
     const uint64_t h = hash_key(keys[kk]);
     const uint32_t* blk = blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8;
     const uint32_t lo = static_cast<uint32_t>(h);
-    bool ok = true;
-    if (in_smem) {
+    uint32_t ok = 1u;
 #pragma unroll
-      for (int i = 0; i < NH; ++i) {
-        const uint32_t b = (lo >> (8 * i)) & 0xFFu;
-        ok &= (blk[b >> 5] >> (b & 31)) & 1u;
-      }
-    } else {
-#pragma unroll
-      for (int i = 0; i < NH; ++i) {
-        const uint32_t b = (lo >> (8 * i)) & 0xFFu;
-        ok &= (__ldg(blk + (b >> 5)) >> (b & 31)) & 1u;
-      }
+    for (int i = 0; i < NH; ++i) {
+      const uint32_t b = (lo >> (8 * i)) & 0xFFu;
+      const uint32_t w = IN_SMEM ? blk[b >> 5] : __ldg(blk + (b >> 5));
+      ok &= w >> (b & 31);
     }
-    keep |= static_cast<uint32_t>(ok) << kk;
+    keep |= (ok & 1u) << kk;
   }
-  return keep;
+  return keep & mask;
+}
+
+template <bool IN_SMEM>
+__device__ __forceinline__ uint32_t probe8_first(const uint32_t* blocks, uint32_t nb, int num_hashes,
+                                                 const int64_t keys[8], uint32_t mask) {
+  switch (num_hashes) {
+    case 1: return probe8<IN_SMEM, 1>(blocks, nb, keys, mask);
+    case 2: return probe8<IN_SMEM, 2>(blocks, nb, keys, mask);
+    case 3: return probe8<IN_SMEM, 3>(blocks, nb, keys, mask);
+    default: return probe8<IN_SMEM, 4>(blocks, nb, keys, mask);
+  }
 }
 
 __device__ __forceinline__ uint32_t sp_seg_bytes(const SpLayout& L, int pi, int64_t rows) {
@@ -440,8 +444,9 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
   int64_t* stage_tile = reinterpret_cast<int64_t*>(smem + 64);
   unsigned char* stages = smem + kSpHeader;
   uint32_t* s_bloom = reinterpret_cast<uint32_t*>(smem + L.bloom_off);
-  __shared__ int s_wcount[kSpConsumerWarps];
-  __shared__ uint16_t s_list[kSpConsumers * kSelItems];  // per warp: surviving rows of its 256
+  __shared__ int s_scan_a[kSpConsumerWarps + 1];
+  __shared__ int s_scan_b[kSpConsumerWarps + 1];
+  __shared__ uint16_t s_list[kSelTile];  // the tile's surviving rows, in row order
   __shared__ uint32_t s_nblocks[kMaxBlooms];
   __shared__ int s_abort;
   const int warp = threadIdx.x >> 5;
@@ -530,7 +535,6 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
     const int64_t start = tile * kSelTile;
     const int64_t tile_rows = n_rows - start < kSelTile ? n_rows - start : kSelTile;
     const int r_in = threadIdx.x * kSelItems;  // first row of this thread within the tile
-    const int64_t row0 = start + r_in;
     const bool full_rows = r_in + kSelItems <= tile_rows;
     uint32_t mask;
     if (full_rows) {
@@ -593,43 +597,31 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
       // the first probe's filter parameters, read once per tile
       const BloomDev& b0 = p.probes[0];
       const uint32_t nb0 = s_nblocks[0];
-      const uint32_t* blocks0 = (staged & 1u) ? s_bloom + b0.smem_word : b0.blocks;
-      uint32_t keep;
-      switch (b0.num_hashes) {
-        case 1: keep = probe8<1>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
-        case 2: keep = probe8<2>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
-        case 3: keep = probe8<3>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
-        default: keep = probe8<4>(blocks0, (staged & 1u) != 0, nb0, keys, mask); break;
-      }
+      const uint32_t keep = (staged & 1u) ? probe8_first<true>(s_bloom + b0.smem_word, nb0, b0.num_hashes, keys, mask)
+                                          : probe8_first<false>(b0.blocks, nb0, b0.num_hashes, keys, mask);
       mask &= keep;
     }
-    // (2) the survivors, in row order, into this warp's list
-    uint16_t* list = s_list + warp * 32 * kSelItems;
+    // (2) the survivors, in row order, into the tile's list (one list for
+    // the CTA, so the later probes keep whole warps busy)
     int n_alive;
     {
-      const int c = __popc(mask);
-      int incl = c;
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-      }
-      n_alive = __shfl_sync(0xffffffffu, incl, 31);
-      int o = incl - c;
+      int o = named_exclusive_sum<1, kSpConsumers>(__popc(mask), &n_alive, s_scan_a);
 #pragma unroll
       for (int kk = 0; kk < kSelItems; ++kk)
-        if ((mask >> kk) & 1u) list[o++] = static_cast<uint16_t>(r_in + kk);
-      __syncwarp();
+        if ((mask >> kk) & 1u) s_list[o++] = static_cast<uint16_t>(r_in + kk);
     }
-    // (3) the later probes over the list only: a lane loads all of its
-    // survivor's later keys at once (one memory round trip), tests them in
-    // probe order, and the list is compacted in place
+    named_sync<1, kSpConsumers>();  // the list is complete; every thread is past its stage reads
+    if (lane == 0) mbar_arrive(&empty[s]);  // hand the stage back to the producer
+    // (3) the later probes over the list: a thread loads all of its row's
+    // later keys at once (one memory round trip), tests them in probe order,
+    // and the list is compacted in place, order kept (a compacted position
+    // never passes the position it was read from)
     if (p.n_probes > 1 && n_alive > 0) {
       int m = 0;
-      for (int base = 0; base < n_alive; base += 32) {
-        const int idx = base + lane;
+      for (int base = 0; base < n_alive; base += kSpConsumers) {
+        const int idx = base + static_cast<int>(threadIdx.x);
         bool alive = idx < n_alive;
-        const int r = alive ? list[idx] : 0;
+        const int r = alive ? s_list[idx] : 0;
         int64_t later[kMaxBlooms - 1];
 #pragma unroll
         for (int j = 0; j < kMaxBlooms - 1; ++j) {
@@ -642,32 +634,19 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
           const int pi = j + 1;
           if (alive && pi < p.n_probes && ((valid >> pi) & 1u)) alive = probe_hit(pi, later[j]);
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, alive);
-        __syncwarp();  // every lane has read its entry before any is overwritten
-        if (alive) list[m + __popc(bal & ((1u << lane) - 1u))] = static_cast<uint16_t>(r);
-        m += __popc(bal);
-        __syncwarp();
+        int kept;
+        const int pos = named_exclusive_sum<1, kSpConsumers>(alive ? 1 : 0, &kept, s_scan_b);
+        if (alive) s_list[m + pos] = static_cast<uint16_t>(r);
+        m += kept;
+        named_sync<1, kSpConsumers>();  // writes land before the next round reads; s_scan_b is free again
       }
       n_alive = m;
     }
-    // The stage's keys are consumed: hand it back to the producer.
-    __syncwarp();
-    if (lane == 0) {
-      mbar_arrive(&empty[s]);
-      s_wcount[warp] = n_alive;
-    }
-    // (4) warp offsets within the tile, then the row ids in order
-    named_sync<1, kSpConsumers>();
-    int woff = 0, tile_total = 0;
-#pragma unroll
-    for (int w = 0; w < kSpConsumerWarps; ++w) {
-      const int c = s_wcount[w];
-      woff += w < warp ? c : 0;
-      tile_total += c;
-    }
-    int32_t* dst = p.out_rowids + start + woff;
-    for (int i = lane; i < n_alive; i += 32) dst[i] = static_cast<int32_t>(start + list[i]);
-    if (threadIdx.x == 0) p.tile_status[tile] = static_cast<uint64_t>(tile_total);
+    // (4) the row ids in order into the tile's slice of the row list
+    int32_t* dst = p.out_rowids + start;
+    for (int i = static_cast<int>(threadIdx.x); i < n_alive; i += kSpConsumers)
+      dst[i] = static_cast<int32_t>(start + s_list[i]);
+    if (threadIdx.x == 0) p.tile_status[tile] = static_cast<uint64_t>(n_alive);
   }
 }
 
