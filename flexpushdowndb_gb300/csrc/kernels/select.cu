@@ -362,39 +362,26 @@ int select_blocks_per_sm(bool with_pred, size_t dyn) {
 }
 
 // ---------------------------------------------------------------------------
-// Pipelined probe-only selection (the BloomFilterUse chain over a large
-// input), in two passes. select_kernel takes a tile, then loads each probe's
-// key column only for the rows still alive, so a chain of k probes costs k
-// dependent DRAM round trips per tile behind block barriers, and its
-// single-pass ranking makes each tile wait for its predecessors.
-// Pass 1 (select_probe_kernel): one producer warp claims tiles and streams
-// the first probe's key column for the tile into a kSpStages-deep ring of
-// shared-memory stages with cp.async.bulk; the eight consumer warps run the
-// first probe over every row (filter staged in shared memory), compact the
-// survivors into per-warp row lists, run the later probes over the lists only
-// (their keys read directly for the survivors), and write the tile's
-// selected row ids, in order, to the tile's own slice of a row-id buffer plus
-// the tile's count. No tile waits for another.
+// Probe-only selection over a large input (the BloomFilterUse chain over the
+// fact table), in two passes.
+// Pass 1 (select_probe_kernel): warps work on their own 256-row slices of the
+// input (32 lanes x 8 rows), taken by a fixed stride, with no barrier
+// between warps: a lane loads its 8 keys of the first probe with 16-byte
+// loads, tests them against the first filter (staged in shared memory once
+// per CTA), the warp compacts its survivors with a ballot scan into its own
+// row list, tests the later probes over that list only (their keys read
+// directly for the survivors, all of a row's keys in one memory round trip),
+// and writes the slice's selected row ids, in order, into the slice's part of
+// a row-id buffer, with the slice's count. A warp waiting on memory for its
+// later probes holds up no other warp.
 // Pass 2 (select_gather_kernel): each CTA sums the counts before its range of
-// tiles and moves each tile's selected rows of every projected column to
+// slices and moves each slice's selected rows of every projected column to
 // their output offsets.
-// Output order is input order, as in the single-pass kernel. All waits are
-// bounded; on timeout the call reports GFPDB_ETIMEDOUT.
-constexpr int kSpConsumerWarps = 8;
-constexpr int kSpConsumers = kSpConsumerWarps * 32;  // == kSelThreads: one 8-row group per consumer
-constexpr int kSpThreads = kSpConsumers + 32;
-constexpr int kSpStages = 4;
-constexpr int kSpHeader = 128;  // full[S], empty[S] mbarriers, then the tile of each stage
-constexpr int64_t kSpMaxDynamic = 200 * 1024;
-constexpr int64_t kSpMinRows = int64_t{1} << 20;  // below this the simple kernel's tiles all start at once
-
-static_assert(kSpConsumers == kSelThreads, "the pipelined select keeps select_kernel's tile shape");
-
-struct SpLayout {
-  int32_t key_width[kMaxBlooms];  // 4 or 8
-  int32_t stage_bytes;            // the first probe's keys of one tile
-  int32_t bloom_off;              // byte offset of the staged filter in dynamic shared memory
-};
+// Output order is input order, as in the single-pass kernel.
+constexpr int kPwThreads = 256;                 // 8 warps
+constexpr int kPwRows = 32 * kSelItems;         // rows per warp slice
+constexpr int64_t kSpMinRows = int64_t{1} << 20;  // below this select_kernel's tiles all start at once
+constexpr int64_t kSpMaxDynamic = 96 * 1024;    // the first filter in shared memory
 
 // The first probe over a thread's 8 rows: the bloom test of each key with NH
 // hashes, bit positions from the low 32 bits of the key's hash (bloom.cuh).
@@ -432,30 +419,18 @@ __device__ __forceinline__ uint32_t probe8_first(const uint32_t* blocks, uint32_
   }
 }
 
-__device__ __forceinline__ uint32_t sp_seg_bytes(const SpLayout& L, int pi, int64_t rows) {
-  return static_cast<uint32_t>((rows * L.key_width[pi]) & ~int64_t{15});
-}
-
-__global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_constant__ SelectParams p,
-                                                                  const __grid_constant__ SpLayout L) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* empty = full + kSpStages;
-  int64_t* stage_tile = reinterpret_cast<int64_t*>(smem + 64);
-  unsigned char* stages = smem + kSpHeader;
-  uint32_t* s_bloom = reinterpret_cast<uint32_t*>(smem + L.bloom_off);
-  __shared__ int s_scan_a[kSpConsumerWarps + 1];
-  __shared__ int s_scan_b[kSpConsumerWarps + 1];
-  __shared__ uint16_t s_list[kSelTile];  // the tile's surviving rows, in row order
+__global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_constant__ SelectParams p,
+                                                                  int32_t* __restrict__ rowlist) {
+  extern __shared__ __align__(16) uint32_t s_filter[];  // the first probe's filter, when staged
+  __shared__ uint16_t s_list[kPwThreads / 32][kPwRows];  // per warp: its slice's survivors
   __shared__ uint32_t s_nblocks[kMaxBlooms];
-  __shared__ int s_abort;
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-
   const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
-  const int64_t n_tiles = (n_rows + kSelTile - 1) / kSelTile;
+  const int64_t n_slices = (n_rows + kPwRows - 1) / kPwRows;
 
-  uint32_t staged = 0, valid = 0;
+  uint32_t valid = 0;
+  bool staged = false;
 #pragma unroll 1
   for (int pi = 0; pi < p.n_probes; ++pi) {
     const BloomDev& b = p.probes[pi];
@@ -463,165 +438,66 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
     if (threadIdx.x == 0) s_nblocks[pi] = nb;
     const bool v = b.valid_dev ? (*b.valid_dev != 0) : (b.valid != 0);
     if (v) valid |= 1u << pi;
-    if (v && b.smem_word >= 0 && nb * 8 <= static_cast<uint32_t>(b.smem_cap_words)) {
-      staged |= 1u << pi;
+    if (pi == 0 && v && b.smem_word >= 0 && nb * 8 <= static_cast<uint32_t>(b.smem_cap_words)) {
+      staged = true;
       const uint4* src = reinterpret_cast<const uint4*>(b.blocks);
-      uint4* dst = reinterpret_cast<uint4*>(s_bloom + b.smem_word);
-      for (uint32_t i = threadIdx.x; i < nb * 2; i += kSpThreads) dst[i] = __ldg(src + i);
+      uint4* dst = reinterpret_cast<uint4*>(s_filter);
+      for (uint32_t i = threadIdx.x; i < nb * 2; i += kPwThreads) dst[i] = __ldg(src + i);
     }
   }
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kSpStages; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kSpConsumerWarps);
-    }
-    mbar_fence_init();
-    s_abort = 0;
-  }
-  __syncthreads();  // the last block-wide barrier: roles split below
+  __syncthreads();  // the only block-wide barrier: warps are independent below
 
-  if (warp == kSpConsumerWarps) {
-    // ------------------------------------------------------------ producer
-    if (lane != 0) return;
-    int64_t k = 0;
-    for (;; ++k) {
-      const int s = static_cast<int>(k % kSpStages);
-      if (k >= kSpStages && !mbar_wait(&empty[s], static_cast<uint32_t>((k / kSpStages - 1) & 1))) {
-        raise_status(p.status, GFPDB_ETIMEDOUT, 140);
-        break;
-      }
-      const int64_t tile = static_cast<int64_t>(atomicAdd(p.ticket, 1u));
-      if (tile >= n_tiles) {
-        stage_tile[s] = -1;  // end of input: published by the arrive (release)
-        mbar_arrive(&full[s]);
-        ++k;
-        break;
-      }
-      stage_tile[s] = tile;
-      const int64_t start = tile * kSelTile;
-      const int64_t left = n_rows - start;
-      const int64_t rows = left < kSelTile ? left : kSelTile;
-      // only the first probe's keys: it runs on every row; later probes
-      // read the keys of the few survivors directly
-      const uint32_t bytes = sp_seg_bytes(L, 0, rows);
-      mbar_arrive_expect_tx(&full[s], bytes);
-      if (bytes != 0) {
-        const unsigned char* src =
-            static_cast<const unsigned char*>(p.cols[p.probes[0].col].data) + start * L.key_width[0];
-        bulk_g2s(stages + static_cast<int64_t>(s) * L.stage_bytes, src, bytes, &full[s]);
-      }
-    }
-    // Copies still in flight land before this CTA exits.
-    for (int64_t j = k > kSpStages ? k - kSpStages : 0; j < k; ++j)
-      if (!mbar_wait(&full[j % kSpStages], static_cast<uint32_t>((j / kSpStages) & 1))) {
-        raise_status(p.status, GFPDB_ETIMEDOUT, 141);
-        break;
-      }
-    return;
-  }
-
-  // -------------------------------------------------------------- consumers
-  for (int64_t k = 0;; ++k) {
-    const int s = static_cast<int>(k % kSpStages);
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[s], static_cast<uint32_t>((k / kSpStages) & 1)));
-    if (!ok && lane == 0) {
-      raise_status(p.status, GFPDB_ETIMEDOUT, 142);
-      s_abort = 1;
-    }
-    named_sync<1, kSpConsumers>();  // every consumer warp leaves together
-    if (s_abort != 0) break;
-    const int64_t tile = stage_tile[s];
-    if (tile < 0) break;
-    const int64_t start = tile * kSelTile;
-    const int64_t tile_rows = n_rows - start < kSelTile ? n_rows - start : kSelTile;
-    const int r_in = threadIdx.x * kSelItems;  // first row of this thread within the tile
-    const bool full_rows = r_in + kSelItems <= tile_rows;
-    uint32_t mask;
-    if (full_rows) {
-      mask = 0xFFu;
-    } else {
-      const int64_t rem = tile_rows - r_in;
-      mask = rem <= 0 ? 0u : ((1u << rem) - 1u);
-    }
-    const unsigned char* stage = stages + static_cast<int64_t>(s) * L.stage_bytes;
-    // key of probe pi for row r of the tile: the stage, or global memory for
-    // the last rows of the input that the 16-byte copy left out
-    auto key_at = [&](int pi, int r) -> int64_t {
-      if (pi == 0) {
-        const int w = L.key_width[0];
-        if (r < static_cast<int64_t>(sp_seg_bytes(L, 0, tile_rows) / w))
-          return w == 8 ? reinterpret_cast<const int64_t*>(stage)[r]
-                        : static_cast<int64_t>(reinterpret_cast<const int32_t*>(stage)[r]);
-      }
-      return load_int(p.cols[p.probes[pi].col], start + r);
-    };
-    auto probe_hit = [&](int pi, int64_t key) -> bool {
-      const BloomDev& b = p.probes[pi];
-      const uint64_t h = hash_key(key);
-      const uint32_t blk = bloom_block_of(h, s_nblocks[pi]);
-      if ((staged >> pi) & 1u) return bloom_test(s_bloom + b.smem_word + blk * 8, h, b.num_hashes);
-      const uint4* words = reinterpret_cast<const uint4*>(b.blocks + static_cast<uint64_t>(blk) * 8);
-      uint32_t wv[8];
-      const uint4 lo = __ldg(words);
-      const uint4 hi = __ldg(words + 1);
-      wv[0] = lo.x; wv[1] = lo.y; wv[2] = lo.z; wv[3] = lo.w;
-      wv[4] = hi.x; wv[5] = hi.y; wv[6] = hi.z; wv[7] = hi.w;
-      return bloom_test(wv, h, b.num_hashes);
-    };
-    // (1) the first probe (keys in the stage) over this thread's 8 rows
-    const int first = 0;
+  const BloomDev& b0 = p.probes[0];
+  const uint32_t nb0 = s_nblocks[0];
+  const DevCol& kc0 = p.cols[b0.col];
+  const bool vec0 = (reinterpret_cast<uintptr_t>(kc0.data) & 15u) == 0;
+  uint16_t* list = s_list[warp];
+  const uint32_t lane_lt = (1u << lane) - 1u;
+  const int64_t n_warps = static_cast<int64_t>(gridDim.x) * (kPwThreads / 32);
+  for (int64_t sl = static_cast<int64_t>(blockIdx.x) * (kPwThreads / 32) + warp; sl < n_slices; sl += n_warps) {
+    const int64_t start = sl * kPwRows;
+    const int r_in = lane * kSelItems;
+    const int64_t row0 = start + r_in;
+    const int64_t rem = n_rows - row0;
+    const bool full = rem >= kSelItems;
+    uint32_t mask = full ? 0xFFu : (rem <= 0 ? 0u : ((1u << rem) - 1u));
+    // (1) the first probe over this lane's 8 rows
     if ((valid & 1u) && mask != 0) {
-      const int w = L.key_width[0];
-      const int64_t in_smem = sp_seg_bytes(L, 0, tile_rows) / w;
-      const unsigned char* seg = stage;
-      int64_t keys[8];
-      if (r_in + kSelItems <= in_smem) {
-        if (w == 8) {
-          const longlong2* q = reinterpret_cast<const longlong2*>(seg) + r_in / 2;
+      int64_t keys[kSelItems];
+      load8(kc0, row0, mask, full && vec0, keys);
+      if (!full) {
 #pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const longlong2 a = q[h];
-            keys[2 * h] = a.x;
-            keys[2 * h + 1] = a.y;
-          }
-        } else {
-          const int4* q = reinterpret_cast<const int4*>(seg) + r_in / 4;
-          const int4 a = q[0], c = q[1];
-          keys[0] = a.x; keys[1] = a.y; keys[2] = a.z; keys[3] = a.w;
-          keys[4] = c.x; keys[5] = c.y; keys[6] = c.z; keys[7] = c.w;
-        }
-      } else {
-#pragma unroll
-        for (int kk = 0; kk < kSelItems; ++kk) keys[kk] = (mask >> kk) & 1u ? key_at(first, r_in + kk) : 0;
+        for (int kk = 0; kk < kSelItems; ++kk)
+          if (!((mask >> kk) & 1u)) keys[kk] = 0;  // a defined key for the rows past the end (masked below)
       }
-      // the first probe's filter parameters, read once per tile
-      const BloomDev& b0 = p.probes[0];
-      const uint32_t nb0 = s_nblocks[0];
-      const uint32_t keep = (staged & 1u) ? probe8_first<true>(s_bloom + b0.smem_word, nb0, b0.num_hashes, keys, mask)
-                                          : probe8_first<false>(b0.blocks, nb0, b0.num_hashes, keys, mask);
-      mask &= keep;
+      mask &= staged ? probe8_first<true>(s_filter, nb0, b0.num_hashes, keys, mask)
+                     : probe8_first<false>(b0.blocks, nb0, b0.num_hashes, keys, mask);
     }
-    // (2) the survivors, in row order, into the tile's list (one list for
-    // the CTA, so the later probes keep whole warps busy)
+    // (2) the survivors, in row order, into the warp's list
     int n_alive;
     {
-      int o = named_exclusive_sum<1, kSpConsumers>(__popc(mask), &n_alive, s_scan_a);
+      const int c = __popc(mask);
+      int incl = c;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+      }
+      n_alive = __shfl_sync(0xffffffffu, incl, 31);
+      int o = incl - c;
 #pragma unroll
       for (int kk = 0; kk < kSelItems; ++kk)
-        if ((mask >> kk) & 1u) s_list[o++] = static_cast<uint16_t>(r_in + kk);
+        if ((mask >> kk) & 1u) list[o++] = static_cast<uint16_t>(r_in + kk);
+      __syncwarp();
     }
-    named_sync<1, kSpConsumers>();  // the list is complete; every thread is past its stage reads
-    if (lane == 0) mbar_arrive(&empty[s]);  // hand the stage back to the producer
-    // (3) the later probes over the list: a thread loads all of its row's
-    // later keys at once (one memory round trip), tests them in probe order,
-    // and the list is compacted in place, order kept (a compacted position
-    // never passes the position it was read from)
+    // (3) the later probes over the list, compacted in place (order kept: a
+    // compacted position never passes the position it was read from)
     if (p.n_probes > 1 && n_alive > 0) {
       int m = 0;
-      for (int base = 0; base < n_alive; base += kSpConsumers) {
-        const int idx = base + static_cast<int>(threadIdx.x);
+      for (int base = 0; base < n_alive; base += 32) {
+        const int idx = base + lane;
         bool alive = idx < n_alive;
-        const int r = alive ? s_list[idx] : 0;
+        const int r = alive ? list[idx] : 0;
         int64_t later[kMaxBlooms - 1];
 #pragma unroll
         for (int j = 0; j < kMaxBlooms - 1; ++j) {
@@ -632,35 +508,44 @@ __global__ void __launch_bounds__(kSpThreads) select_probe_kernel(const __grid_c
 #pragma unroll
         for (int j = 0; j < kMaxBlooms - 1; ++j) {
           const int pi = j + 1;
-          if (alive && pi < p.n_probes && ((valid >> pi) & 1u)) alive = probe_hit(pi, later[j]);
+          if (alive && pi < p.n_probes && ((valid >> pi) & 1u)) {
+            const BloomDev& b = p.probes[pi];
+            const uint64_t h = hash_key(later[j]);
+            const uint4* words =
+                reinterpret_cast<const uint4*>(b.blocks + static_cast<uint64_t>(bloom_block_of(h, s_nblocks[pi])) * 8);
+            const uint4 lo = __ldg(words);
+            const uint4 hi = __ldg(words + 1);
+            const uint32_t wv[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+            alive = bloom_test(wv, h, b.num_hashes);
+          }
         }
-        int kept;
-        const int pos = named_exclusive_sum<1, kSpConsumers>(alive ? 1 : 0, &kept, s_scan_b);
-        if (alive) s_list[m + pos] = static_cast<uint16_t>(r);
-        m += kept;
-        named_sync<1, kSpConsumers>();  // writes land before the next round reads; s_scan_b is free again
+        const uint32_t bal = __ballot_sync(0xffffffffu, alive);
+        __syncwarp();  // every lane has read its entry before any is overwritten
+        if (alive) list[m + __popc(bal & lane_lt)] = static_cast<uint16_t>(r);
+        m += __popc(bal);
+        __syncwarp();
       }
       n_alive = m;
     }
-    // (4) the row ids in order into the tile's slice of the row list
-    int32_t* dst = p.out_rowids + start;
-    for (int i = static_cast<int>(threadIdx.x); i < n_alive; i += kSpConsumers)
-      dst[i] = static_cast<int32_t>(start + s_list[i]);
-    if (threadIdx.x == 0) p.tile_status[tile] = static_cast<uint64_t>(n_alive);
+    // (4) the slice's row ids, in order, into its part of the row list
+    int32_t* dst = rowlist + start;
+    for (int i = lane; i < n_alive; i += 32) dst[i] = static_cast<int32_t>(start + list[i]);
+    if (lane == 0) p.tile_status[sl] = static_cast<uint64_t>(n_alive);
+    __syncwarp();  // the list is rewritten by the warp's next slice
   }
 }
 
-// Pass 2: each CTA takes a contiguous range of at most kSelThreads tiles,
-// sums the counts of the tiles before it, scans its own tiles' counts, then
+// Pass 2: each CTA takes a contiguous range of at most kSelThreads slices,
+// sums the counts of the slices before it, scans its own slices' counts, then
 // moves every selected row of its range in one parallel pass (row ids in
-// order in each tile's slice of the row-id buffer) to the output. The CTA
-// holding the last tile records the total.
+// order in each slice's part of the row-id buffer) to the output. The CTA
+// holding the last slice records the total.
 __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid_constant__ SelectParams p,
                                                                    const int32_t* rowlist, int32_t* out_rowids) {
   __shared__ int s_w[kSelThreads / 32 + 1];
   __shared__ int s_pref[kSelThreads + 1];
   const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
-  const int64_t n_tiles = (n_rows + kSelTile - 1) / kSelTile;
+  const int64_t n_tiles = (n_rows + kPwRows - 1) / kPwRows;
   const int64_t per = (n_tiles + gridDim.x - 1) / gridDim.x;  // <= kSelThreads by the launch
   const int64_t t0 = static_cast<int64_t>(blockIdx.x) * per;
   if (t0 >= n_tiles) return;
@@ -685,7 +570,7 @@ __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid
       if (s_pref[mid] <= i) lo = mid;
       else hi = mid - 1;
     }
-    const int32_t row = rowlist[(t0 + lo) * kSelTile + (i - s_pref[lo])];
+    const int32_t row = rowlist[(t0 + lo) * kPwRows + (i - s_pref[lo])];
     const int64_t o = base + i;
     for (int j = 0; j < p.n_out; ++j) {
       const OutCol& oc = p.outs[j];
@@ -712,7 +597,7 @@ int select_probe_blocks_per_sm(size_t dyn) {
     attr_set = true;
   }
   int per_sm = 0;
-  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_probe_kernel, kSpThreads, dyn));
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_probe_kernel, kPwThreads, dyn));
   cache[dyn] = per_sm;
   return per_sm;
 }
@@ -1081,7 +966,11 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   // smaller, so the tile-status array is sized for them)
   LiteParams lp;
   const bool lite = n <= kLiteMaxRows && lite_params(p, lp);
-  const int64_t n_tiles = lite ? (n + kLiteTile - 1) / kLiteTile : (n + kSelTile - 1) / kSelTile;  // upper bound
+  // probe-only selections over large inputs take the two-pass kernels (their
+  // unit is a warp's 256-row slice)
+  const bool two_pass = !lite && p.prog.n_clauses == 0 && p.n_probes > 0 && n >= kSpMinRows;
+  const int64_t unit = lite ? kLiteTile : two_pass ? kPwRows : kSelTile;
+  const int64_t n_tiles = (n + unit - 1) / unit;  // upper bound
   p.n_tiles = n_tiles;
   auto scratch = make_filled(sizeof(DevStatus) + 64 + n_tiles * 8, 0, s);
   char* sb = scratch->as<char>();
@@ -1110,62 +999,38 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     after_launch("select_lite_kernel");
     prof.stop(0);
     prof.set_bytes_model(p.n_dev, n, read_all, &p.status->value, proj_read + proj_write, scratch, in.rows_owner());
+  } else if (n_tiles > 0 && two_pass) {
+    // pass 1: probes; each slice's selected row ids into its part of rowlist
+    const size_t dyn = p.probes[0].smem_word >= 0 ? static_cast<size_t>(p.probes[0].smem_cap_words) * 4 : 0;
+    const int per_sm = select_probe_blocks_per_sm(dyn);
+    auto rowlist = make_buffer(n * 4, s);
+    {
+      const int64_t want = (n_tiles + kPwThreads / 32 - 1) / (kPwThreads / 32);
+      const int64_t cap = static_cast<int64_t>(num_sms()) * (per_sm > 0 ? per_sm : 1);
+      ProfScope prof("select_probe_kernel", s);
+      select_probe_kernel<<<static_cast<int>(want < cap ? want : cap), kPwThreads, dyn, s>>>(p, rowlist->as<int32_t>());
+      after_launch("select_probe_kernel");
+      prof.stop(0);
+      // the first probe's keys over all rows (later probes' keys are read
+      // for survivors only and not counted)
+      prof.set_bytes_model(p.n_dev, n, p.cols[p.probes[0].col].type == CT_I64 ? 8 : 4, &p.status->value, 4.0, scratch,
+                           in.rows_owner());
+    }
+    {
+      // ranges of at most kSelThreads slices, at least two CTAs per SM
+      int64_t grid = std::max<int64_t>((n_tiles + kSelThreads - 1) / kSelThreads,
+                                       std::min<int64_t>(n_tiles, static_cast<int64_t>(num_sms()) * 2));
+      ProfScope prof("select_gather_kernel", s);
+      select_gather_kernel<<<static_cast<int>(grid), kSelThreads, 0, s>>>(p, rowlist->as<int32_t>(), p.out_rowids);
+      after_launch("select_gather_kernel");
+      prof.stop(0);
+      prof.set_bytes_model(nullptr, 0, 0, &p.status->value, 4.0 + proj_read + proj_write, scratch, in.rows_owner());
+    }  // rowlist is freed stream-ordered, after the gather
   } else if (n_tiles > 0) {
     const size_t dyn = static_cast<size_t>(smem_words) * 4;
     const bool with_pred = p.prog.n_clauses > 0;
-    // The pipelined probe-only kernel: no predicate, 16-byte aligned key
-    // columns, and an input of at least a few tiles per SM.
-    SpLayout lay{};
-    bool pipelined = !with_pred && p.n_probes > 0 && n >= kSpMinRows &&
-                     (reinterpret_cast<uintptr_t>(p.cols[p.probes[0].col].data) & 15u) == 0;
-    size_t sp_bloom = 0;
-    if (pipelined) {
-      for (int pi = 0; pi < p.n_probes; ++pi) lay.key_width[pi] = p.cols[p.probes[pi].col].type == CT_I64 ? 8 : 4;
-      lay.stage_bytes = kSelTile * lay.key_width[0];
-      lay.bloom_off = kSpHeader + kSpStages * lay.stage_bytes;
-      // only the first probe's filter is staged: the later ones see few rows
-      if (p.probes[0].smem_word >= 0) sp_bloom = static_cast<size_t>(p.probes[0].smem_cap_words) * 4;
-    }
-    int per_sm = 0;
-    const size_t sp_dyn = lay.bloom_off + sp_bloom;
-    if (pipelined) per_sm = select_probe_blocks_per_sm(sp_dyn);
-    if (pipelined && per_sm > 0) {
-      // pass 1: probes; each tile's selected row ids into its slice of rowlist
-      auto rowlist = make_buffer(n * 4, s);
-      SelectParams& p1 = *pp;
-      int32_t* utf8_rowids = p1.out_rowids;
-      std::vector<int32_t> saved_words(p1.n_probes);
-      for (int pi = 0; pi < p1.n_probes; ++pi) {
-        saved_words[pi] = p1.probes[pi].smem_word;
-        if (pi > 0) p1.probes[pi].smem_word = -1;
-      }
-      if (p1.probes[0].smem_word >= 0) p1.probes[0].smem_word = 0;
-      p1.out_rowids = rowlist->as<int32_t>();
-      {
-        int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;
-        if (grid > n_tiles) grid = n_tiles;
-        ProfScope prof("select_probe_kernel", s);
-        select_probe_kernel<<<static_cast<int>(grid), kSpThreads, sp_dyn, s>>>(p1, lay);
-        after_launch("select_probe_kernel");
-        prof.stop(0);
-        // the first probe's keys over all rows (later probes' keys are read
-        // for survivors only and not counted)
-        prof.set_bytes_model(p.n_dev, n, lay.key_width[0], &p.status->value, 4.0, scratch, in.rows_owner());
-      }
-      for (int pi = 0; pi < p1.n_probes; ++pi) p1.probes[pi].smem_word = saved_words[pi];
-      p1.out_rowids = utf8_rowids;
-      {
-        // ranges of at most kSelThreads tiles, at least two CTAs per SM
-        int64_t grid = std::max<int64_t>((n_tiles + kSelThreads - 1) / kSelThreads,
-                                         std::min<int64_t>(n_tiles, static_cast<int64_t>(num_sms()) * 2));
-        ProfScope prof("select_gather_kernel", s);
-        select_gather_kernel<<<static_cast<int>(grid), kSelThreads, 0, s>>>(p1, rowlist->as<int32_t>(), utf8_rowids);
-        after_launch("select_gather_kernel");
-        prof.stop(0);
-        prof.set_bytes_model(nullptr, 0, 0, &p.status->value, 4.0 + proj_read + proj_write, scratch,
-                             in.rows_owner());
-      }  // rowlist is freed stream-ordered, after the gather
-    } else {
+    {
+      int per_sm = 0;
       ProfScope prof("select_kernel", s);
       per_sm = select_blocks_per_sm(with_pred, dyn);
       int64_t grid = static_cast<int64_t>(num_sms()) * per_sm;

@@ -280,9 +280,9 @@ def _probe_case(fact_rows, key_type, seed):
 @pytest.mark.parametrize("fact_rows,key_type,n_probes", [(1 << 20, "int32", 4), ((1 << 20) + 13, "int32", 1),
                                                          (3_000_001, "int64", 4), (2_500_007, "int32", 2)])
 def test_select_probe_pipeline_large(gpu, fact_rows, key_type, n_probes):
-    """Inputs of a million rows and more take the pipelined probe-only
-    kernel (bulk-copied key tiles); output rows and their order match the
-    oracle's sequential bloom uses, including a ragged last tile."""
+    """Inputs of a million rows and more take the two-pass probe-only
+    kernels (warp slices of 256 rows); output rows and their order match the
+    oracle's sequential bloom uses, including a ragged last slice."""
     fact, blooms, _ = _probe_case(fact_rows, key_type, 2100 + n_probes)
     want = fact
     for bf, c in blooms[:n_probes]:
@@ -293,8 +293,8 @@ def test_select_probe_pipeline_large(gpu, fact_rows, key_type, n_probes):
 
 
 def test_select_probe_pipeline_unaligned_columns(gpu):
-    """Key columns that do not start on a 16-byte boundary fall back to the
-    simple kernel; results are the same."""
+    """Key columns that do not start on a 16-byte boundary are read with
+    scalar loads; results are the same."""
     import torch
 
     fact, blooms, seq = _probe_case((1 << 20) + 5, "int32", 2200)
@@ -456,3 +456,18 @@ def test_join_info_after_build(gpu):
     assert info["build_rows"] == 10_000
     assert info["capacity"] == 32_768
     assert 0 <= info["max_probe"] < 64  # linear probing at load 0.31
+
+
+def test_select_probe_first_filter_in_global_memory(gpu):
+    """A first filter too large for shared memory (200,000 keys at 16 bits
+    per key) is probed through L1/L2; results match the oracle."""
+    fact, _, _ = _probe_case(1_200_000, "int32", 2300)
+    tabs = workloads.star_tables(fact_rows=10, seed=2300)
+    big = tabs["d2"]
+    bf = ops.BloomFilter([big], "d2_pk", 16, 3)
+    assert bf.info()["num_blocks"] * 32 > 96 * 1024
+    d3 = oops.filter_table(tabs["d3"], eq(col("d3_f"), num_lit(2)))
+    blooms = [(bf, "fk2"), (ops.BloomFilter([d3], "d3_pk"), "fk3")]
+    want = oops.bloom_use(oops.bloom_use(fact, bf.words(), "fk2"), oops.bloom_words(d3["d3_pk"]), "fk3")
+    got = ops.select(DeviceTable.from_host(fact), None, blooms)
+    assert got.rows() == want.rows()
