@@ -74,6 +74,10 @@ LocalPOpDirectory& POpContext::operatorMap() { return op_->directory(); }
 
 cudaStream_t POpContext::stream() const { return exec_->streamOf(op_); }
 
+cudaStream_t POpContext::sideStream(int k) const { return exec_->sideStreamOf(op_, k); }
+
+void POpContext::streamWait(cudaStream_t waiter, cudaStream_t on) { exec_->streamWait(waiter, on); }
+
 // ------------------------------------------------------------------ ops
 
 namespace {
@@ -278,6 +282,85 @@ class BloomFilterUsePOp : public PhysicalOp {
   std::vector<TupleSetPtr> buffered_;
 };
 
+// One hash join's probe of one TupleSet (the output: probe fields then build
+// fields, HashJoinArrowKernel.cpp:148-162, each kept when projected).
+TupleSetPtr probe_join(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
+                       const std::string& probe_key, const TupleSetPtr& ts, cudaStream_t stream) {
+  const int pk = ts->require_column(probe_key);
+  auto needed = [&](const std::string& c) {
+    return proj.empty() ||
+           std::find(proj.begin(), proj.end(), c) != proj.end();
+  };
+  // Output: probe fields then build fields (HashJoinArrowKernel.cpp:148-162),
+  // each filtered to the needed columns.
+  {
+    std::vector<Field> fields;
+    std::vector<int> pcols, bcols;
+    bool fixed = true;
+    for (int i = 0; i < ts->num_columns(); ++i)
+      if (needed(ts->field(i).name)) {
+        fields.push_back(ts->field(i));
+        pcols.push_back(i);
+        fixed &= ts->field(i).type != DType::Utf8;
+      }
+    const TupleSet& b = *table.build;
+    for (int i = 0; i < b.num_columns(); ++i)
+      if (needed(b.field(i).name)) {
+        for (auto& f : fields)
+          if (f.name == b.field(i).name)
+            fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + join_name + "': column '" + f.name + "' is on both sides");
+        fields.push_back(b.field(i));
+        bcols.push_back(i);
+        fixed &= b.field(i).type != DType::Utf8;
+      }
+    if (fixed) {
+      // fixed-width outputs: probe and materialise in one kernel
+      BufferPtr count_owner;
+      const int64_t* count_dev = nullptr;
+      int64_t n = 0;
+      auto cols = join_probe_materialize(table, *ts, pk, pcols, bcols, &n, stream, &count_owner,
+                                         &count_dev);
+      if (count_dev != nullptr)
+        return TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev);
+      return TupleSet::make(std::move(fields), std::move(cols), n);
+    }
+  }
+  BufferPtr pidx, bidx, count_owner;
+  const int64_t* count_dev = nullptr;
+  int64_t n = 0;
+  join_probe_pairs(table, *ts, pk, &pidx, &bidx, &n, stream, &count_owner, &count_dev);
+  std::vector<GatherSpec> specs;
+  std::vector<Field> fields;
+  for (int i = 0; i < ts->num_columns(); ++i)
+    if (needed(ts->field(i).name)) {
+      fields.push_back(ts->field(i));
+      specs.push_back(GatherSpec{ts->column(i).get(), pidx->as<int32_t>()});
+    }
+  const TupleSet& b = *table.build;
+  for (int i = 0; i < b.num_columns(); ++i)
+    if (needed(b.field(i).name)) {
+      for (auto& f : fields)
+        if (f.name == b.field(i).name)
+          fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + join_name + "': column '" + f.name + "' is on both sides");
+      fields.push_back(b.field(i));
+      specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
+    }
+  bool utf8 = false;
+  for (auto& f : fields) utf8 |= f.type == DType::Utf8;
+  if (count_dev != nullptr && utf8) {
+    // utf8 outputs are sized from the exact pair count
+    int64_t exact = 0;
+    GF_CUDA(cudaMemcpyAsync(&exact, count_dev, sizeof(exact), cudaMemcpyDeviceToHost, stream));
+    sync(stream);
+    n = exact < n ? exact : n;
+    count_dev = nullptr;
+  }
+  auto cols = gather_columns(specs, n, stream, count_dev, count_owner);
+  if (count_dev != nullptr)
+    return TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev);
+  return TupleSet::make(std::move(fields), std::move(cols), n);
+}
+
 // HashJoinArrowPOp (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowPOp.cpp:85-153):
 // routes TupleSets by sender to the build or probe side, builds the table
 // once every build producer is complete, probes as probe input arrives.
@@ -336,87 +419,9 @@ class HashJoinArrowPOp : public PhysicalOp {
   }
 
   void probe(const TupleSetPtr& ts) {
-    const int pk = ts->require_column(probe_key_);
-    auto needed = [&](const std::string& c) {
-      return projectColumnNames_.empty() ||
-             std::find(projectColumnNames_.begin(), projectColumnNames_.end(), c) != projectColumnNames_.end();
-    };
-    // Output: probe fields then build fields (HashJoinArrowKernel.cpp:148-162),
-    // each filtered to the needed columns.
-    {
-      std::vector<Field> fields;
-      std::vector<int> pcols, bcols;
-      bool fixed = true;
-      for (int i = 0; i < ts->num_columns(); ++i)
-        if (needed(ts->field(i).name)) {
-          fields.push_back(ts->field(i));
-          pcols.push_back(i);
-          fixed &= ts->field(i).type != DType::Utf8;
-        }
-      const TupleSet& b = *table_.build;
-      for (int i = 0; i < b.num_columns(); ++i)
-        if (needed(b.field(i).name)) {
-          for (auto& f : fields)
-            if (f.name == b.field(i).name)
-              fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': column '" + f.name + "' is on both sides");
-          fields.push_back(b.field(i));
-          bcols.push_back(i);
-          fixed &= b.field(i).type != DType::Utf8;
-        }
-      if (fixed) {
-        // fixed-width outputs: probe and materialise in one kernel
-        BufferPtr count_owner;
-        const int64_t* count_dev = nullptr;
-        int64_t n = 0;
-        auto cols = join_probe_materialize(table_, *ts, pk, pcols, bcols, &n, ctx()->stream(), &count_owner,
-                                           &count_dev);
-        Message out;
-        out.type = MessageType::TUPLESET;
-        if (count_dev != nullptr)
-          out.tuples = TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev);
-        else
-          out.tuples = TupleSet::make(std::move(fields), std::move(cols), n);
-        ctx()->tell(out);
-        return;
-      }
-    }
-    BufferPtr pidx, bidx, count_owner;
-    const int64_t* count_dev = nullptr;
-    int64_t n = 0;
-    join_probe_pairs(table_, *ts, pk, &pidx, &bidx, &n, ctx()->stream(), &count_owner, &count_dev);
-    std::vector<GatherSpec> specs;
-    std::vector<Field> fields;
-    for (int i = 0; i < ts->num_columns(); ++i)
-      if (needed(ts->field(i).name)) {
-        fields.push_back(ts->field(i));
-        specs.push_back(GatherSpec{ts->column(i).get(), pidx->as<int32_t>()});
-      }
-    const TupleSet& b = *table_.build;
-    for (int i = 0; i < b.num_columns(); ++i)
-      if (needed(b.field(i).name)) {
-        for (auto& f : fields)
-          if (f.name == b.field(i).name)
-            fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': column '" + f.name + "' is on both sides");
-        fields.push_back(b.field(i));
-        specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
-      }
-    bool utf8 = false;
-    for (auto& f : fields) utf8 |= f.type == DType::Utf8;
     Message out;
     out.type = MessageType::TUPLESET;
-    if (count_dev != nullptr && utf8) {
-      // utf8 outputs are sized from the exact pair count
-      int64_t exact = 0;
-      GF_CUDA(cudaMemcpyAsync(&exact, count_dev, sizeof(exact), cudaMemcpyDeviceToHost, ctx()->stream()));
-      sync(ctx()->stream());
-      n = exact < n ? exact : n;
-      count_dev = nullptr;
-    }
-    auto cols = gather_columns(specs, n, ctx()->stream(), count_dev, count_owner);
-    if (count_dev != nullptr)
-      out.tuples = TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev);
-    else
-      out.tuples = TupleSet::make(std::move(fields), std::move(cols), n);
+    out.tuples = probe_join(name_, table_, projectColumnNames_, probe_key_, ts, ctx()->stream());
     ctx()->tell(out);
   }
 
@@ -426,6 +431,179 @@ class HashJoinArrowPOp : public PhysicalOp {
   std::vector<TupleSetPtr> build_, probe_buffer_;
   JoinTable table_;
   bool built_ = false;
+};
+
+// HashJoinChainPOp: a chain of HashJoinArrowPOps in which each join's only
+// consumer is the next join and is its probe side (the star join: fact rows
+// probing one dimension after another), produced by the plan's pipeline
+// fusion (fuse_join_chains). Every join's table is built as its build side
+// completes, as HashJoinArrowPOp does; each probe TupleSet then goes through
+// all the joins in one kernel (join_chain_materialize) that writes only the
+// last join's output columns, instead of one probe launch and one
+// intermediate TupleSet per join. Column selection, names and errors are the
+// unfused chain's; outputs with utf8 columns take the joins one at a time.
+struct ChainJoinSpec {
+  std::string name;
+  std::vector<std::string> build_producers;
+  std::string build_key, probe_key;
+  double load_factor = 0.5;
+  std::vector<std::string> proj;
+};
+
+class HashJoinChainPOp : public PhysicalOp {
+ public:
+  HashJoinChainPOp(std::string name, std::vector<ChainJoinSpec> joins)
+      : PhysicalOp(std::move(name), "HashJoinChainPOp"), joins_(std::move(joins)), build_(joins_.size()),
+        tables_(joins_.size()), built_(joins_.size(), false) {
+    if (joins_.empty() || static_cast<int>(joins_.size()) > kJoinChainMax)
+      fail(GFPDB_EINVAL, "HashJoinChainPOp '" + name_ + "': 1 to 6 joins");
+  }
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      bool build = false;
+      for (size_t l = 0; l < joins_.size(); ++l) {
+        const auto& bp = joins_[l].build_producers;
+        if (std::find(bp.begin(), bp.end(), m.sender) == bp.end()) continue;
+        if (built_[l])
+          fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + joins_[l].name + "': build input after the table was built");
+        build_[l].push_back(m.tuples);
+        build = true;
+      }
+      if (build) return;
+      if (allBuilt()) process(m.tuples);
+      else probe_buffer_.push_back(m.tuples);
+    } else if (m.type == MessageType::COMPLETE) {
+      auto& dir = ctx()->operatorMap();
+      for (size_t l = 0; l < joins_.size(); ++l) {
+        if (built_[l]) continue;
+        bool done = true;
+        for (auto& b : joins_[l].build_producers) done &= dir.isComplete(b);
+        if (done) finalizeBuild(l);
+      }
+      if (is_producer_complete(*this))
+        for (size_t l = 0; l < joins_.size(); ++l)
+          if (!built_[l]) finalizeBuild(l);
+      if (allBuilt()) {
+        for (auto& t : probe_buffer_) process(t);
+        probe_buffer_.clear();
+      }
+      if (is_producer_complete(*this)) {
+        joinBuilds();
+        // The tables were allocated on the build streams and are freed there
+        // when this operator clears: those frees must follow every probe
+        // issued on this operator's stream.
+        for (cudaStream_t bs : used_streams_) ctx()->streamWait(bs, ctx()->stream());
+        used_streams_.clear();
+        ctx()->notifyComplete();
+      }
+    }
+  }
+
+  void clear() override {
+    build_streams_.clear();
+    used_streams_.clear();
+    for (auto& b : build_) b.clear();
+    probe_buffer_.clear();
+    for (auto& t : tables_) t = JoinTable{};
+  }
+
+ private:
+  bool allBuilt() const { return std::all_of(built_.begin(), built_.end(), [](bool b) { return b; }); }
+
+  // Each join's table is built on a stream of its own (its inputs were
+  // waited for on this operator's stream, which the build stream joins
+  // first); the operator's stream waits for every build just before the
+  // first probe, so the builds run side by side.
+  void finalizeBuild(size_t l) {
+    const auto& J = joins_[l];
+    if (build_[l].empty()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + J.name + "': no build-side input");
+    cudaStream_t bs = ctx()->sideStream(static_cast<int>(l));
+    ctx()->streamWait(bs, ctx()->stream());
+    tables_[l].build = TupleSet::concatenate(build_[l], bs);
+    tables_[l].key_col = tables_[l].build->require_column(J.build_key);
+    join_build_table(tables_[l], J.load_factor, bs);
+    build_streams_.push_back(bs);
+    if (std::find(used_streams_.begin(), used_streams_.end(), bs) == used_streams_.end()) used_streams_.push_back(bs);
+    build_[l].clear();
+    built_[l] = true;
+  }
+
+  void joinBuilds() {
+    for (cudaStream_t bs : build_streams_) ctx()->streamWait(ctx()->stream(), bs);
+    build_streams_.clear();
+  }
+
+  void process(const TupleSetPtr& ts) {
+    joinBuilds();
+    // Follow the columns through the chain by name, as the joins one at a
+    // time would see them: (source, column) of every join's probe key and of
+    // the last join's outputs.
+    struct Col {
+      Field f;
+      ChainRef ref;
+    };
+    std::vector<Col> cur;
+    for (int i = 0; i < ts->num_columns(); ++i) cur.push_back(Col{ts->field(i), ChainRef{0, i}});
+    std::vector<ChainRef> keys;
+    for (size_t l = 0; l < joins_.size(); ++l) {
+      const auto& J = joins_[l];
+      auto k = std::find_if(cur.begin(), cur.end(), [&](const Col& c) { return c.f.name == J.probe_key; });
+      if (k == cur.end()) fail(GFPDB_EINVAL, "column '" + J.probe_key + "' not found in TupleSet");
+      keys.push_back(k->ref);
+      auto needed = [&](const std::string& c) {
+        return J.proj.empty() || std::find(J.proj.begin(), J.proj.end(), c) != J.proj.end();
+      };
+      std::vector<Col> next;
+      for (auto& c : cur)
+        if (needed(c.f.name)) next.push_back(c);
+      const TupleSet& b = *tables_[l].build;
+      for (int i = 0; i < b.num_columns(); ++i) {
+        if (!needed(b.field(i).name)) continue;
+        for (auto& c : next)
+          if (c.f.name == b.field(i).name)
+            fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + J.name + "': column '" + c.f.name + "' is on both sides");
+        next.push_back(Col{b.field(i), ChainRef{static_cast<int>(l) + 1, i}});
+      }
+      cur = std::move(next);
+    }
+    bool fixed = true;
+    for (auto& c : cur) fixed &= c.f.type != DType::Utf8;
+    Message out;
+    out.type = MessageType::TUPLESET;
+    if (fixed) {
+      std::vector<const JoinTable*> tabs;
+      for (auto& t : tables_) tabs.push_back(&t);
+      std::vector<ChainRef> outs;
+      std::vector<Field> fields;
+      for (auto& c : cur) {
+        outs.push_back(c.ref);
+        fields.push_back(c.f);
+      }
+      BufferPtr count_owner;
+      const int64_t* count_dev = nullptr;
+      int64_t n = 0;
+      auto cols = join_chain_materialize(tabs, *ts, keys, outs, &n, ctx()->stream(), &count_owner, &count_dev);
+      out.tuples = count_dev != nullptr
+                       ? TupleSet::make_deferred(std::move(fields), std::move(cols), n, count_owner, count_dev)
+                       : TupleSet::make(std::move(fields), std::move(cols), n);
+    } else {
+      TupleSetPtr t = ts;
+      for (size_t l = 0; l < joins_.size(); ++l)
+        t = probe_join(joins_[l].name, tables_[l], joins_[l].proj, joins_[l].probe_key, t, ctx()->stream());
+      out.tuples = t;
+    }
+    ctx()->tell(out);
+  }
+
+  std::vector<ChainJoinSpec> joins_;
+  std::vector<std::vector<TupleSetPtr>> build_;
+  std::vector<JoinTable> tables_;
+  std::vector<bool> built_;
+  std::vector<TupleSetPtr> probe_buffer_;
+  std::vector<cudaStream_t> build_streams_;  // builds the operator's stream has not yet waited for
+  std::vector<cudaStream_t> used_streams_;   // every stream a table was built on
 };
 
 // GroupPOp (fpdb-executor/src/physical/group/GroupPOp.cpp:14-85): group each
@@ -664,6 +842,20 @@ cudaStream_t Execution::streamOf(const PhysicalOp* op) const {
   return it == op_stream_.end() || streams_.empty() ? stream_ : streams_[it->second];
 }
 
+cudaStream_t Execution::sideStreamOf(const PhysicalOp* op, int k) const {
+  if (streams_.size() <= 1) return streamOf(op);
+  auto it = op_stream_.find(op);
+  const int own = it == op_stream_.end() ? 0 : it->second;
+  return streams_[static_cast<size_t>(own + 1 + k) % streams_.size()];
+}
+
+void Execution::streamWait(cudaStream_t waiter, cudaStream_t on) {
+  if (waiter == on) return;
+  cudaEvent_t e = pooled_event(events_used_++);
+  GF_CUDA(cudaEventRecord(e, on));
+  GF_CUDA(cudaStreamWaitEvent(waiter, e, 0));
+}
+
 void Execution::stamp(Message& msg, const PhysicalOp* sender) {
   if (streams_.size() <= 1) return;
   // A COMPLETE carries no device dependency: every TUPLESET and BLOOM_FILTER
@@ -753,6 +945,11 @@ TupleSetPtr Execution::execute() {
   join_guard.reset();  // join the streams before anything waits on the caller's stream
   if (!error_.empty()) {
     clear_deferred_checks();
+    // Operators free their buffers on their own streams when the execution
+    // goes away; on this path some were not ordered after the work that
+    // uses them, so let everything issued finish first (nothing is freed
+    // under capture: the graph's memory is an arena).
+    if (!capturing_) (void)cudaStreamSynchronize(stream_);
     fail(code, error_);
   }
   if (capturing_) {
@@ -812,6 +1009,21 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
     op = std::make_unique<HashJoinArrowPOp>(name, o.str_list("buildProducers"), o.str_list("probeProducers"),
                                             o.at("buildKey").str(), o.at("probeKey").str(),
                                             o.get_num("loadFactor", 0.5));
+  } else if (type == "HashJoinChainPOp") {
+    std::vector<ChainJoinSpec> joins;
+    for (auto& j : o.at("joins").array()) {
+      std::string jt = j.get_str("joinType", "INNER");
+      if (jt != "INNER") fail(GFPDB_EUNSUPPORTED, "join type '" + jt + "' (only INNER runs on the GPU path)");
+      ChainJoinSpec c;
+      c.name = j.get_str("name", name);
+      c.build_producers = j.str_list("buildProducers");
+      c.build_key = j.at("buildKey").str();
+      c.probe_key = j.at("probeKey").str();
+      c.load_factor = j.get_num("loadFactor", 0.5);
+      c.proj = j.str_list("projectColumnNames");
+      joins.push_back(std::move(c));
+    }
+    op = std::make_unique<HashJoinChainPOp>(name, std::move(joins));
   } else if (type == "CsvScanPOp") {
     std::vector<CsvField> fields;
     for (auto& f : o.at("fields").array()) {
@@ -979,8 +1191,103 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
   return out;
 }
 
+// Pipeline fusion: a chain of inner HashJoinArrowPOps in which each join's
+// only consumer is the next join, which takes it as its only probe producer,
+// becomes one HashJoinChainPOp (the joins in order, each with its build
+// producers, keys, load factor and projection). The fused operator keeps the
+// last join's name, so every reference to the chain's end stays valid, and
+// every producer that sent to an earlier join now sends to it. Results are
+// unchanged: the fused operator builds the same tables and emits the last
+// join's rows.
+json::Value fuse_join_chains(const json::Value& plan) {
+  json::Value out = plan;
+  json::Value* ops_v = jfind(out, "ops");
+  if (ops_v == nullptr) return out;
+  auto& ops = ops_v->a;
+  auto is_join = [](const json::Value& o) {
+    return o.at("type").str() == "HashJoinArrowPOp" && o.get_str("joinType", "INNER") == "INNER";
+  };
+  auto index_of = [&](const std::string& name) {
+    for (size_t i = 0; i < ops.size(); ++i)
+      if (ops[i].at("name").str() == name) return static_cast<int>(i);
+    return -1;
+  };
+  // the join that follows ops[i] in a chain, or -1
+  auto next_of = [&](size_t i) {
+    if (!is_join(ops[i])) return -1;
+    auto cons = ops[i].str_list("consumers");
+    if (cons.size() != 1) return -1;
+    const int j = index_of(cons[0]);
+    if (j < 0 || !is_join(ops[j])) return -1;
+    if (ops[j].str_list("probeProducers") != std::vector<std::string>{ops[i].at("name").str()}) return -1;
+    auto bp = ops[j].str_list("buildProducers");
+    if (std::find(bp.begin(), bp.end(), ops[i].at("name").str()) != bp.end()) return -1;
+    return j;
+  };
+  for (;;) {
+    // the first join of a chain: a join no other join feeds as its chain successor
+    int head = -1;
+    for (size_t i = 0; i < ops.size() && head < 0; ++i) {
+      if (next_of(i) < 0) continue;
+      bool fed = false;
+      for (size_t k = 0; k < ops.size(); ++k) fed |= next_of(k) == static_cast<int>(i);
+      if (!fed) head = static_cast<int>(i);
+    }
+    if (head < 0) break;
+    std::vector<int> chain{head};
+    while (static_cast<int>(chain.size()) < kJoinChainMax) {
+      const int j = next_of(static_cast<size_t>(chain.back()));
+      if (j < 0) break;
+      chain.push_back(j);
+    }
+    if (chain.size() < 2) break;
+    json::Value fused;
+    fused.kind = json::Value::Object;
+    jset(fused, "type", jstr("HashJoinChainPOp"));
+    jset(fused, "name", ops[chain.back()].at("name"));
+    json::Value joins;
+    joins.kind = json::Value::Array;
+    std::set<std::string> absorbed;
+    for (int i : chain) {
+      const json::Value& o = ops[i];
+      json::Value j;
+      j.kind = json::Value::Object;
+      for (const char* k : {"name", "buildProducers", "buildKey", "probeKey", "loadFactor", "projectColumnNames", "joinType"})
+        if (o.contains(k)) jset(j, k, o.at(k));
+      joins.a.push_back(j);
+      absorbed.insert(o.at("name").str());
+    }
+    jset(fused, "joins", joins);
+    jset(fused, "probeProducers", ops[chain.front()].at("probeProducers"));
+    jset(fused, "consumers", jlist(ops[chain.back()].str_list("consumers")));
+    const std::string last = ops[chain.back()].at("name").str();
+    std::vector<json::Value> kept;
+    for (size_t i = 0; i < ops.size(); ++i) {
+      if (absorbed.count(ops[i].at("name").str())) {
+        if (static_cast<int>(i) == chain.back()) kept.push_back(fused);
+        continue;
+      }
+      json::Value o = ops[i];
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers"}) {
+        json::Value* l = jfind(o, key);
+        if (l == nullptr) continue;
+        std::vector<std::string> v = o.str_list(key), nv;
+        for (auto& x : v) {
+          const std::string y = absorbed.count(x) ? last : x;
+          if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
+        }
+        *l = jlist(nv);
+      }
+      kept.push_back(o);
+    }
+    ops = kept;
+  }
+  return out;
+}
+
 std::unique_ptr<Execution> build_execution(const json::Value& plan_in, cudaStream_t stream) {
-  const json::Value plan = plan_in.get_bool("fusePipelines", true) ? fuse_bloom_chains(plan_in) : plan_in;
+  const bool fuse = plan_in.get_bool("fusePipelines", true);
+  const json::Value plan = fuse ? fuse_join_chains(fuse_bloom_chains(plan_in)) : plan_in;
   auto ex = std::make_unique<Execution>(stream);
   for (auto& o : plan.at("ops").array()) ex->add(make_op(o, ex.get()));
   for (auto& o : plan.at("ops").array()) {

@@ -95,6 +95,12 @@ class POpContext {
   void notifyError(const std::string& error);
   LocalPOpDirectory& operatorMap();
   cudaStream_t stream() const;
+  // Another stream of the execution (the k-th after this operator's, round
+  // robin; the operator's own when the plan runs on one stream), for work an
+  // operator runs beside its own.
+  cudaStream_t sideStream(int k) const;
+  // Makes `waiter` wait for the work issued so far on `on` (an event).
+  void streamWait(cudaStream_t waiter, cudaStream_t on);
   bool isComplete() const { return complete_; }
 
  private:
@@ -188,6 +194,8 @@ class Execution {
   void setStreams(int n) { n_streams_ = n < 1 ? 1 : n; }
   int streamCount() const { return static_cast<int>(streams_.size()); }
   cudaStream_t streamOf(const PhysicalOp* op) const;
+  cudaStream_t sideStreamOf(const PhysicalOp* op, int k) const;
+  void streamWait(cudaStream_t waiter, cudaStream_t on);
   // Stamps an outgoing message with its sender's stream and ready event.
   void stamp(Message& msg, const PhysicalOp* sender);
   ~Execution();

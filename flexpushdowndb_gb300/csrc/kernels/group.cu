@@ -29,6 +29,7 @@ namespace gfpdb {
 namespace {
 
 constexpr int kGroupThreads = 256;
+constexpr int kGroupSmemSlotsMax = 1024;  // slots of a CTA's shared-memory table
 constexpr uint32_t kDictSpinLimit = 1u << 20;
 
 struct AccDev {
@@ -140,6 +141,8 @@ __device__ __forceinline__ unsigned long long row_value(const GroupParams& p, co
 
 __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __grid_constant__ GroupParams p) {
   extern __shared__ unsigned long long s_mem[];
+  __shared__ uint16_t s_occ[kGroupSmemSlotsMax];  // the occupied slots, listed for the merge
+  __shared__ int s_scan[kGroupThreads / 32 + 1];
   uint64_t* s_keys = reinterpret_cast<uint64_t*>(s_mem);
   unsigned long long* s_acc = s_mem + p.sm_slots;
   const int sm_mask = p.sm_slots - 1;
@@ -185,11 +188,21 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
     }
   }
   if (p.use_smem) {
+    // Merge into the global table: the occupied slots are listed first (a
+    // block scan), so each thread merges about one group, and every group's
+    // global insert and atomics run in the same round instead of one after
+    // another on the threads that hold several.
     __syncthreads();
-    for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads) {
-      const uint64_t key = s_keys[i];
-      if (key == kEmptySlot) continue;
-      const uint64_t g = global_slot(p, key);
+    int c = 0;
+    for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads) c += s_keys[i] != kEmptySlot ? 1 : 0;
+    int occupied;
+    int o = block_exclusive_sum<kGroupThreads>(c, &occupied, s_scan);
+    for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads)
+      if (s_keys[i] != kEmptySlot) s_occ[o++] = static_cast<uint16_t>(i);
+    __syncthreads();
+    for (int j = threadIdx.x; j < occupied; j += kGroupThreads) {
+      const int i = s_occ[j];
+      const uint64_t g = global_slot(p, s_keys[i]);
       if (g == UINT64_MAX) continue;
       for (int a = 0; a < p.n_acc; ++a) acc_combine(p.accs + g * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, s_acc[i * p.n_acc + a]);
     }
@@ -735,8 +748,10 @@ class GroupTable {
     p.st = status->as<DevStatus>();
     // Shared-memory pre-aggregation unless the caller expects many groups.
     const int per_slot = 8 + 8 * p.n_acc;
-    int sm_slots = 1024;
-    while (sm_slots * per_slot > 48 * 1024) sm_slots >>= 1;
+    int sm_slots = kGroupSmemSlotsMax;
+    // dynamic plus static shared memory stays within the 48 KB a launch
+    // gets without opting in to more
+    while (sm_slots * per_slot > 44 * 1024) sm_slots >>= 1;
     p.use_smem = (hint == 0 || hint <= 4096) ? 1 : 0;
     p.sm_slots = sm_slots;
     const size_t dyn = p.use_smem ? static_cast<size_t>(sm_slots) * per_slot : 0;

@@ -195,6 +195,112 @@ __global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_const
   }
 }
 
+// A chain of joins in one pass. Each lane walks its input row through the
+// levels like a depth-first search: at its current level it reads one slot
+// per step; a match at an inner level moves it to the next level (whose key
+// comes from the input row or an earlier match), a match at the last level
+// emits an output row, and the end of a run returns it to the level before,
+// whose run it continues. The warp steps together so that emitted rows still
+// take their output positions with one atomic per warp and step.
+struct ChainLevel {
+  const uint64_t* slots;
+  uint64_t mask;
+  DevCol bkey;         // the level's build key column (confirms 64-bit keys)
+  const void* key;     // the level's probe key column
+  int32_t key_src;     // 0: the input row; l + 1: the build row matched at level l
+  int32_t key_wide;    // 1: int64 probe key column
+  int32_t key32;       // 1: the slot tag is the key itself
+  int32_t pad;
+};
+
+struct ChainParams {
+  int64_t n_cap;
+  const int64_t* n_dev;
+  int32_t n_levels;
+  int32_t n_out;
+  int64_t cap;
+  DevStatus* st;
+  ChainLevel lv[kJoinChainMax];
+  const void* src[kJoinOutMax];
+  void* dst[kJoinOutMax];
+  int32_t width[kJoinOutMax];
+  int32_t from[kJoinOutMax];  // 0: the input row; l + 1: the build row of level l
+};
+
+__global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__ ChainParams p) {
+  const int64_t n = clamp_rows(p.n_dev, p.n_cap);
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(&p.st->value);
+  for (int64_t base = warp_global * 32; base < n; base += n_warps * 32) {
+    const int64_t r = base + lane;
+    bool active = r < n;
+    int64_t rows[kJoinChainMax + 1];
+    uint64_t slot[kJoinChainMax], steps[kJoinChainMax];
+    int64_t key[kJoinChainMax];
+    uint32_t tag[kJoinChainMax];
+    int lvl = 0;
+    rows[0] = r;
+    auto start_level = [&](int l) {
+      const ChainLevel& L = p.lv[l];
+      const int64_t kr = rows[L.key_src];
+      const int64_t k = L.key_wide ? static_cast<int64_t>(__ldg(static_cast<const long long*>(L.key) + kr))
+                                   : static_cast<int64_t>(__ldg(static_cast<const int*>(L.key) + kr));
+      const uint64_t h = hash_key(k);
+      key[l] = k;
+      tag[l] = L.key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
+      slot[l] = h & L.mask;
+      steps[l] = 0;
+    };
+    if (active) start_level(0);
+    while (__any_sync(0xffffffffu, active)) {
+      bool emit = false;
+      if (active) {
+        const ChainLevel& L = p.lv[lvl];
+        const uint64_t sv = __ldg(reinterpret_cast<const unsigned long long*>(L.slots + slot[lvl]));
+        if (sv == kEmptySlot || ++steps[lvl] > L.mask + 1) {
+          if (lvl == 0) active = false;  // the input row is done
+          else --lvl;                    // back to the previous level's run
+        } else {
+          slot[lvl] = (slot[lvl] + 1) & L.mask;
+          if (static_cast<uint32_t>(sv >> 32) == tag[lvl]) {
+            const int32_t brow = static_cast<int32_t>(static_cast<uint32_t>(sv));
+            if (L.key32 || load_int(L.bkey, brow) == key[lvl]) {
+              rows[lvl + 1] = brow;
+              if (lvl == p.n_levels - 1) {
+                emit = true;  // and the last level's run continues next step
+              } else {
+                ++lvl;
+                start_level(lvl);
+              }
+            }
+          }
+        }
+      }
+      const uint32_t em = __ballot_sync(0xffffffffu, emit);
+      if (em != 0) {
+        unsigned long long at = 0;
+        const int leader = __ffs(em) - 1;
+        if (lane == leader) at = atomicAdd(cursor, static_cast<unsigned long long>(__popc(em)));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (emit) {
+          const int64_t pos = static_cast<int64_t>(at) + __popc(em & ((1u << lane) - 1u));
+          if (pos < p.cap) {
+            for (int c = 0; c < p.n_out; ++c) {
+              const int64_t from = rows[p.from[c]];
+              if (p.width[c] == 8)
+                static_cast<long long*>(p.dst[c])[pos] = __ldg(static_cast<const long long*>(p.src[c]) + from);
+              else
+                static_cast<int*>(p.dst[c])[pos] = __ldg(static_cast<const int*>(p.src[c]) + from);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 int grid_for(int64_t n) {
   int64_t blocks = (n + 255) / 256;
   int64_t cap = static_cast<int64_t>(num_sms()) * 8;
@@ -304,6 +410,98 @@ std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet
       break;
     }
     cap = hs.value;  // more matches than probe rows (repeated build keys): once more, exactly sized
+  }
+  std::vector<ColumnPtr> cols;
+  for (size_t c = 0; c < srcs.size(); ++c) cols.push_back(make_fixed_column(srcs[c]->type, *n_out, bufs[c]));
+  return cols;
+}
+
+std::vector<ColumnPtr> join_chain_materialize(const std::vector<const JoinTable*>& tables, const TupleSet& probe,
+                                              const std::vector<ChainRef>& keys, const std::vector<ChainRef>& outs,
+                                              int64_t* n_out, cudaStream_t s, BufferPtr* count_owner,
+                                              const int64_t** count_dev) {
+  const int L = static_cast<int>(tables.size());
+  if (L < 1 || L > kJoinChainMax) fail(GFPDB_EUNSUPPORTED, "a join chain has 1 to 6 joins");
+  if (static_cast<int>(keys.size()) != L) fail(GFPDB_EINVAL, "a join chain needs one probe key per join");
+  if (outs.size() > static_cast<size_t>(kJoinOutMax)) fail(GFPDB_EUNSUPPORTED, "too many hash join output columns");
+  const int64_t n = probe.num_rows();
+  if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join probe batch must have fewer than 2^31 rows");
+  auto source = [&](int src) -> const TupleSet& { return src == 0 ? probe : *tables[src - 1]->build; };
+  ChainParams p{};
+  p.n_cap = n;
+  p.n_dev = probe.rows_dev();
+  p.n_levels = L;
+  bool empty_build = false;
+  for (int l = 0; l < L; ++l) {
+    const JoinTable& t = *tables[l];
+    if (keys[l].src < 0 || keys[l].src > l) fail(GFPDB_EINVAL, "a join chain key comes from the input or an earlier join");
+    const auto& kc = source(keys[l].src).column(keys[l].col);
+    if (kc->type == DType::Utf8 || kc->type == DType::Float64)
+      fail(GFPDB_EUNSUPPORTED, "hash join keys must be integer columns");
+    const bool key32 = t.key_type != DType::Int64 && kc->type != DType::Int64;
+    if (!key32 && t.key_type != DType::Int64)
+      fail(GFPDB_EUNSUPPORTED, "int64 probe key against an int32 build key");
+    const auto& bk = t.build->column(t.key_col);
+    ChainLevel& lv = p.lv[l];
+    lv.slots = t.slots->as<uint64_t>();
+    lv.mask = t.capacity - 1;
+    lv.bkey = DevCol{bk->data, nullptr, static_cast<int32_t>(bk->type), 0};
+    lv.key = kc->data;
+    lv.key_src = keys[l].src;
+    lv.key_wide = kc->type == DType::Int64 ? 1 : 0;
+    lv.key32 = key32 ? 1 : 0;
+    empty_build |= t.build->num_rows() == 0;
+  }
+  std::vector<const Column*> srcs;
+  for (auto& o : outs) {
+    if (o.src < 0 || o.src > L) fail(GFPDB_EINVAL, "a join chain output comes from the input or one of its joins");
+    const Column* c = source(o.src).column(o.col).get();
+    if (c->type == DType::Utf8) fail(GFPDB_EUNSUPPORTED, "utf8 output in the fused join");
+    srcs.push_back(c);
+  }
+  p.n_out = static_cast<int32_t>(srcs.size());
+  auto status = make_filled(sizeof(DevStatus), 0, s);
+  const bool defer = deferred_mode() && count_dev != nullptr;
+  int64_t cap = n > 0 ? n : 1;
+  std::vector<BufferPtr> bufs(srcs.size());
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    for (size_t c = 0; c < srcs.size(); ++c) {
+      const int w = dtype_width(srcs[c]->type);
+      bufs[c] = make_buffer(cap * w, s);
+      p.src[c] = srcs[c]->data;
+      p.dst[c] = bufs[c]->data();
+      p.width[c] = w;
+      p.from[c] = outs[c].src;
+    }
+    p.cap = cap;
+    p.st = status->as<DevStatus>();
+    if (attempt > 0) GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
+    if (n > 0 && !empty_build) {
+      ProfScope prof("join_chain_kernel", s);
+      join_chain_kernel<<<grid_for(n), 256, 0, s>>>(p);
+      after_launch("join_chain_kernel");
+      prof.stop(0);
+      double w_out = 0;
+      for (size_t c = 0; c < srcs.size(); ++c) w_out += 2.0 * p.width[c];
+      prof.set_bytes_model(probe.rows_dev(), n, dtype_width(source(keys[0].src).column(keys[0].col)->type),
+                           &status->as<DevStatus>()->value, w_out, status, probe.rows_owner());
+    }
+    if (defer) {
+      defer_check(status, status->as<DevStatus>(), "hash join chain probe", cap);
+      *n_out = cap;
+      *count_dev = &status->as<DevStatus>()->value;
+      if (count_owner) *count_owner = status;
+      break;
+    }
+    DevStatus hs;
+    GF_CUDA(cudaMemcpyAsync(&hs, status->data(), sizeof(hs), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    raise_device_status(hs, "hash join chain probe");
+    if (hs.value <= cap) {
+      *n_out = hs.value;
+      break;
+    }
+    cap = hs.value;  // more combinations than input rows (repeated build keys): once more, exactly sized
   }
   std::vector<ColumnPtr> cols;
   for (size_t c = 0; c < srcs.size(); ++c) cols.push_back(make_fixed_column(srcs[c]->type, *n_out, bufs[c]));

@@ -127,6 +127,21 @@ void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, 
                       BufferPtr* build_idx, int64_t* n_out, cudaStream_t s, BufferPtr* count_owner = nullptr,
                       const int64_t** count_dev = nullptr);
 
+// A chain of inner joins probed in one pass: level l probes tables[l] with a
+// key column taken from the input row (source 0) or from the build row that
+// an earlier level k matched (source k + 1), and every combination of
+// matches writes one output row. Fixed-width columns only. Output and
+// capacity rules as join_probe_materialize (capacity: the input's rows).
+struct ChainRef {
+  int src;  // 0: the input; l + 1: tables[l]->build
+  int col;  // column index in that TupleSet
+};
+constexpr int kJoinChainMax = 6;
+std::vector<ColumnPtr> join_chain_materialize(const std::vector<const JoinTable*>& tables, const TupleSet& probe,
+                                              const std::vector<ChainRef>& keys, const std::vector<ChainRef>& outs,
+                                              int64_t* n_out, cudaStream_t s, BufferPtr* count_owner = nullptr,
+                                              const int64_t** count_dev = nullptr);
+
 // ------------------------------------------------------------- group.cu
 
 struct GroupAggregate {

@@ -3,6 +3,8 @@ bit-exact against the oracle: the two-table query and the star query with
 forward + backward bloom predicate transfer, from host and device inputs,
 whole and chunked into many TupleSets."""
 
+import json
+
 import pytest
 
 from flexpushdowndb_gb300 import GfpdbError, plan, workloads
@@ -114,8 +116,9 @@ def test_bloom_chain_fusion_same_result(gpu, fuse):
     tabs = workloads.star_tables(fact_rows=400_000, seed=99)
     r = plan.execute(_with_options(workloads.star_plan(), fusePipelines=fuse), tabs)
     assert r.table.sorted_rows() == queries.star_query(tabs).sorted_rows()
-    # the four forward BloomFilterUsePOps on the fact table fuse into one
-    assert r.stats["num_ops"] == (28 if fuse else 31)
+    # the four forward BloomFilterUsePOps on the fact table fuse into one,
+    # the four joins into one chain
+    assert r.stats["num_ops"] == (25 if fuse else 31)
 
 
 def test_duplicate_build_keys_rerun_with_exact_sizes(gpu):
@@ -201,3 +204,64 @@ def test_aggregate_pop_matches_oracle(gpu):
                                         {"function": "MIN", "name": "lo", "expr": col("price_cents")},
                                         {"function": "MAX", "name": "hi", "expr": col("fk")}])
         assert got.rows() == want.rows()
+
+
+def _snowflake_tables(n_fact, seed, dup):
+    """fact -> a (on fk_a) -> b (on a_link, a column of a's rows); a and b
+    keys repeated `dup` times."""
+    import numpy as np
+
+    from flexpushdowndb_gb300.tupleset import Column, Table
+
+    rng = np.random.default_rng(seed)
+    na, nb = 3_000, 500
+    a_keys = np.repeat(np.arange(na, dtype=np.int64), dup)
+    b_keys = np.repeat(np.arange(nb, dtype=np.int64) * 7, dup)
+    fact = Table([Column("fk_a", "int32", rng.integers(-10, na + 10, n_fact)),
+                  Column("v", "int64", rng.integers(-10**12, 10**12, n_fact)),
+                  Column("w", "int32", rng.integers(0, 100, n_fact))])
+    a = Table([Column("a_pk", "int32", a_keys), Column("a_link", "int64", rng.integers(0, nb, len(a_keys)) * 7),
+               Column("a_x", "int32", rng.integers(0, 1000, len(a_keys))),
+               Column("a_s", "utf8", [f"s{int(x) % 17}" for x in a_keys])])
+    b = Table([Column("b_pk", "int64", b_keys), Column("b_y", "int64", rng.integers(-50, 50, len(b_keys)))])
+    return {"fact": fact, "a": a, "b": b}
+
+
+def _snowflake_plan(project_utf8, fuse):
+    p = plan.Plan()
+    p.scan("scan_a", "a", ["a_pk", "a_link", "a_x", "a_s"])
+    p.scan("scan_b", "b", ["b_pk", "b_y"])
+    p.scan("scan_fact", "fact", ["fk_a", "v", "w"])
+    p.hash_join("join_a", "scan_a", "scan_fact", "a_pk", "fk_a",
+                ["v", "w", "a_link", "a_x"] + (["a_s"] if project_utf8 else []))
+    p.hash_join("join_b", "scan_b", "join_a", "b_pk", "a_link", ["v", "a_x", "b_y", "w"] + (["a_s"] if project_utf8 else []))
+    p.collate("collate", "join_b")
+    d = json.loads(p.to_json())
+    d["fusePipelines"] = fuse
+    return json.dumps(d)
+
+
+@pytest.mark.parametrize("dup", [1, 3])
+@pytest.mark.parametrize("project_utf8", [False, True])
+@pytest.mark.parametrize("graph", [False, True])
+def test_join_chain_snowflake_duplicates(gpu, dup, project_utf8, graph):
+    """A join chain whose second key comes from the first join's build rows
+    (int64 key against an int64 build key), with repeated build keys (more
+    output rows than input rows: the deferred run overflows and is re-run
+    exactly) and with a utf8 output (the chain then runs join by join):
+    fused and unfused plans match the oracle."""
+    from oracle import ops as oops
+
+    tabs = _snowflake_tables(40_000, 3000 + dup, dup)
+    j1 = oops.hash_join(tabs["a"], tabs["fact"], "a_pk", "fk_a",
+                        ["v", "w", "a_link", "a_x"] + (["a_s"] if project_utf8 else []))
+    want = oops.hash_join(tabs["b"], j1, "b_pk", "a_link", ["v", "a_x", "b_y", "w"] + (["a_s"] if project_utf8 else []))
+    for fuse in (True, False):
+        text = _snowflake_plan(project_utf8, fuse)
+        if graph:
+            text = json.dumps(dict(json.loads(text), cudaGraph=True))
+        for _ in range(2 if graph else 1):
+            r = plan.execute(text, tabs)
+            assert r.table.names == want.names
+            assert r.table.sorted_rows() == want.sorted_rows()
+        assert r.stats["num_ops"] == (5 if fuse else 6)
