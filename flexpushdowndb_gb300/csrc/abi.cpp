@@ -294,7 +294,21 @@ bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowD
   GF_CUDA(cudaGraphLaunch(cp.exec, s));
   GF_CUDA(cudaEventRecord(cp.ev[1], s));
   count_launch(cp.kernels);
-  sync(s);
+  // A replay is short: poll its end instead of sleeping in a blocking wait,
+  // which would add the thread's wake-up to every query; after about two
+  // milliseconds fall back to the blocking wait.
+  {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+      const cudaError_t q = cudaEventQuery(cp.ev[1]);
+      if (q == cudaSuccess) break;
+      if (q != cudaErrorNotReady) GF_CUDA(q);
+      if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(2000)) {
+        sync(s);
+        break;
+      }
+    }
+  }
   float ms = 0;
   GF_CUDA(cudaEventElapsedTime(&ms, cp.ev[0], cp.ev[1]));
   *device_ns = static_cast<int64_t>(static_cast<double>(ms) * 1e6);
@@ -341,6 +355,43 @@ int32_t gfpdb_device_init(int32_t device) {
 }
 
 uint64_t gfpdb_kernel_launch_count(void) { return g_kernel_launches.load(); }
+
+int32_t gfpdb_result_layout(const ArrowSchema* schema, const ArrowDeviceArray* array, int32_t max_columns,
+                            int64_t* n_rows, int32_t* n_columns, int32_t* device_type, char* names,
+                            int64_t names_capacity, const void** values, const void** offsets) {
+  return guarded([&] {
+    require(schema != nullptr && array != nullptr && n_rows != nullptr && n_columns != nullptr &&
+                device_type != nullptr && names != nullptr && values != nullptr && offsets != nullptr,
+            "null argument");
+    const ArrowArray& a = array->array;
+    require(schema->n_children == a.n_children, "schema and array disagree on the column count");
+    require(a.n_children <= max_columns, "more columns than max_columns");
+    *n_rows = a.length;
+    *n_columns = static_cast<int32_t>(a.n_children);
+    *device_type = array->device_type;
+    int64_t at = 0;
+    auto put = [&](const char* s) {
+      const int64_t len = static_cast<int64_t>(std::strlen(s)) + 1;
+      require(at + len <= names_capacity, "column names exceed names_capacity");
+      std::memcpy(names + at, s, static_cast<size_t>(len));
+      at += len;
+    };
+    for (int64_t i = 0; i < a.n_children; ++i) {
+      const ArrowSchema* cs = schema->children[i];
+      const ArrowArray* ca = a.children[i];
+      put(cs->name != nullptr ? cs->name : "");
+      put(cs->format);
+      const bool utf8 = std::strcmp(cs->format, "u") == 0;
+      values[i] = ca->buffers[utf8 ? 2 : 1];
+      offsets[i] = utf8 ? ca->buffers[1] : nullptr;
+    }
+  });
+}
+
+void gfpdb_result_release(ArrowSchema* schema, ArrowDeviceArray* array) {
+  if (array != nullptr && array->array.release != nullptr) array->array.release(&array->array);
+  if (schema != nullptr && schema->release != nullptr) schema->release(schema);
+}
 
 int32_t gfpdb_memcpy(void* dst, const void* src, int64_t n_bytes, int32_t kind, void* stream) {
   return guarded([&] {

@@ -16,7 +16,7 @@ from typing import Sequence
 
 from . import _abi
 from .expression import Expr
-from .tupleset import DeviceTable, Exported, Table, export_host, import_result, new_output
+from .tupleset import DeviceTable, Exported, ResultReader, Table, export_host, import_result, new_output
 
 
 class Plan:
@@ -137,6 +137,31 @@ class PreparedInputs:
         self.c_names = _abi.cstr_array(self.names)
         self.c_schemas = (ctypes.POINTER(_abi.ArrowSchema) * max(1, n))(*[e.schema_ptr for e in self.exported])
         self.c_arrays = (ctypes.POINTER(_abi.ArrowDeviceArray) * max(1, n))(*[e.array_ptr for e in self.exported])
+
+
+class PreparedPlan:
+    """A plan bound to its inputs once: the encoded plan text, the exported
+    inputs and the call's argument structures are made here and reused, so
+    execute() does the least host work per call (a loop that runs one query
+    many times, as a serving loop or a benchmark does)."""
+
+    def __init__(self, plan: Plan | str, tables: dict | PreparedInputs, result_to_host: bool = True, stream=None):
+        self.text = (plan.to_json() if isinstance(plan, Plan) else plan).encode()
+        self.inputs = tables if isinstance(tables, PreparedInputs) else PreparedInputs(tables)
+        self.result_to_host = 1 if result_to_host else 0
+        self.stream = stream
+        self._stats = _abi.ExecStats()
+        self._fn = _abi.lib().gfpdb_execute_plan
+        self._reader = ResultReader()
+        self._s, self._a = new_output()  # reused: the reader releases them after every call
+        inp = self.inputs
+        self._args = (self.text, len(inp.names), inp.c_names, inp.c_schemas, inp.c_arrays, self.result_to_host,
+                      ctypes.byref(self._s), ctypes.byref(self._a), ctypes.byref(self._stats), stream)
+
+    def execute(self) -> Result:
+        _abi.check(self._fn(*self._args))
+        table = self._reader.read(self._s, self._a)
+        return Result(table, {k: getattr(self._stats, k) for k, _ in _abi.ExecStats._fields_})
 
 
 def execute(plan: Plan | str, tables: dict | PreparedInputs, result_to_host: bool = True, stream=None,

@@ -338,6 +338,63 @@ def import_result(schema: _abi.ArrowSchema, darr: _abi.ArrowDeviceArray, release
     return Table(cols)
 
 
+class ResultReader:
+    """Copies exported TupleSets into host Tables with one layout call and one
+    release call into the library (instead of walking the Arrow structures
+    field by field through ctypes), reusing its argument buffers: the import
+    for a loop that reads many results."""
+
+    MAX_COLUMNS = 256
+    NAMES_BYTES = 1 << 16
+
+    def __init__(self):
+        L = _abi.lib()
+        self._layout = L.gfpdb_result_layout
+        self._release = L.gfpdb_result_release
+        self._memcpy = L.gfpdb_memcpy
+        self._n, self._nc, self._dev = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()
+        self._refs = (ctypes.byref(self._n), ctypes.byref(self._nc), ctypes.byref(self._dev))
+        self._names = ctypes.create_string_buffer(self.NAMES_BYTES)
+        self._vals = (ctypes.c_void_p * self.MAX_COLUMNS)()
+        self._offs = (ctypes.c_void_p * self.MAX_COLUMNS)()
+
+    def _copy(self, dst: np.ndarray, src: int, nbytes: int, on_device: bool) -> None:
+        if nbytes == 0:
+            return
+        if on_device:
+            _abi.check(self._memcpy(dst.ctypes.data, src, nbytes, 2, None))
+        else:
+            ctypes.memmove(dst.ctypes.data, src, nbytes)
+
+    def read(self, schema: _abi.ArrowSchema, darr: _abi.ArrowDeviceArray) -> Table:
+        sref, aref = ctypes.byref(schema), ctypes.byref(darr)
+        try:
+            _abi.check(self._layout(sref, aref, self.MAX_COLUMNS, *self._refs, self._names, self.NAMES_BYTES,
+                                    self._vals, self._offs))
+            n, nc = self._n.value, self._nc.value
+            on_device = self._dev.value == _abi.ARROW_DEVICE_CUDA
+            parts = self._names.raw.split(b"\0", 2 * nc)
+            cols = []
+            for i in range(nc):
+                ty = TYPES[parts[2 * i + 1]]
+                if ty == "utf8":
+                    offs = np.empty(n + 1, dtype=np.int32)
+                    self._copy(offs, self._offs[i], (n + 1) * 4, on_device)
+                    base = int(offs[0])
+                    data = np.empty(int(offs[-1]) - base, dtype=np.uint8)
+                    self._copy(data, self._vals[i] + base, data.nbytes, on_device)
+                    values = ((offs - base).astype(np.int32), data)
+                else:
+                    values = np.empty(n, dtype=NP_TYPES[ty])
+                    self._copy(values, self._vals[i], values.nbytes, on_device)
+                c = Column.__new__(Column)  # the values already have the column's dtype and layout
+                c.name, c.type, c.values = parts[2 * i].decode(), ty, values
+                cols.append(c)
+            return Table(cols)
+        finally:
+            self._release(sref, aref)
+
+
 def text_table(text: bytes, name: str = "text") -> Table:
     """A one-row table whose utf8 value is `text` (the input of CsvScanPOp)."""
     if len(text) >= 2**31:

@@ -75,6 +75,21 @@ uint64_t gfpdb_kernel_launch_count(void);
  * 3 = device->device). Synchronous when stream is NULL. */
 int32_t gfpdb_memcpy(void* dst, const void* src, int64_t n_bytes, int32_t kind, void* stream);
 
+/* The layout of an exported TupleSet (an output of this library), for a
+ * caller that copies it out in one pass: its row count, where its buffers
+ * live (ARROW_DEVICE_CPU or ARROW_DEVICE_CUDA), and per column its name and
+ * Arrow format string, written into `names` as "name\0format\0" pairs, its
+ * values buffer and, for utf8, its offsets buffer (NULL otherwise). Fails
+ * with GFPDB_EINVAL when the TupleSet has more than max_columns columns or
+ * the names do not fit names_capacity bytes. */
+int32_t gfpdb_result_layout(const struct ArrowSchema* schema, const struct ArrowDeviceArray* array,
+                            int32_t max_columns, int64_t* n_rows, int32_t* n_columns, int32_t* device_type,
+                            char* names, int64_t names_capacity, const void** values, const void** offsets);
+
+/* Releases both structures of an exported TupleSet (either may already be
+ * released or NULL). */
+void gfpdb_result_release(struct ArrowSchema* schema, struct ArrowDeviceArray* array);
+
 /* Page-locked host allocation, so that host inputs can be copied at full
  * link bandwidth. */
 int32_t gfpdb_host_alloc(void** ptr, int64_t n_bytes);

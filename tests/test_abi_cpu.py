@@ -117,3 +117,31 @@ def test_export_host_roundtrip_structure():
     assert ex.schema.n_children == 4
     assert ex.array.array.length == 3
     assert ex.schema.children[2].contents.format == b"u"
+
+
+def test_result_layout_of_an_exported_table():
+    """gfpdb_result_layout reads any exported TupleSet's structure (host
+    memory here): rows, names and formats, buffer pointers."""
+    t = small_table()
+    ex = export_host(t)
+    L = _abi.lib()
+    n, nc, dev = ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()
+    names = ctypes.create_string_buffer(4096)
+    vals, offs = (ctypes.c_void_p * 8)(), (ctypes.c_void_p * 8)()
+    _abi.check(L.gfpdb_result_layout(ex.schema_ptr, ex.array_ptr, 8, ctypes.byref(n), ctypes.byref(nc),
+                                     ctypes.byref(dev), names, 4096, vals, offs))
+    assert (n.value, nc.value, dev.value) == (3, 4, _abi.ARROW_DEVICE_CPU)
+    parts = names.raw.split(b"\0")[: 2 * nc.value]
+    assert parts[0::2] == [c.name.encode() for c in t.columns]
+    assert parts[1::2] == [ex.schema.children[i].contents.format for i in range(4)]
+    for i in range(4):
+        ca = ex.array.array.children[i].contents
+        if parts[2 * i + 1] == b"u":
+            assert (vals[i], offs[i]) == (ca.buffers[2], ca.buffers[1])
+        else:
+            assert vals[i] == ca.buffers[1] and offs[i] is None
+    # too few columns allowed, or too little room for the names
+    assert L.gfpdb_result_layout(ex.schema_ptr, ex.array_ptr, 3, ctypes.byref(n), ctypes.byref(nc),
+                                 ctypes.byref(dev), names, 4096, vals, offs) == _abi.GFPDB_EINVAL
+    assert L.gfpdb_result_layout(ex.schema_ptr, ex.array_ptr, 8, ctypes.byref(n), ctypes.byref(nc),
+                                 ctypes.byref(dev), names, 4, vals, offs) == _abi.GFPDB_EINVAL

@@ -265,3 +265,20 @@ def test_join_chain_snowflake_duplicates(gpu, dup, project_utf8, graph):
             assert r.table.names == want.names
             assert r.table.sorted_rows() == want.sorted_rows()
         assert r.stats["num_ops"] == (5 if fuse else 6)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_prepared_plan_matches_execute(gpu, graph):
+    """PreparedPlan (bound inputs, one-call result import) returns what
+    plan.execute returns, call after call, with host and device results of
+    fixed-width and utf8 columns."""
+    tabs = workloads.two_table_tables(fact_rows=200_000)
+    text = _with_options(workloads.two_table_plan(), cudaGraph=graph)
+    want = plan.execute(text, tabs).table
+    pp = plan.PreparedPlan(text, plan.PreparedInputs(tabs))
+    for _ in range(3):
+        got = pp.execute().table
+        assert got.names == want.names
+        assert got.sorted_rows() == want.sorted_rows()
+    dev = plan.PreparedPlan(text, plan.PreparedInputs(tabs), result_to_host=False)
+    assert dev.execute().table.sorted_rows() == want.sorted_rows()
