@@ -534,6 +534,8 @@ def run_case(args):
         return _time_case(args, fn)
     tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
     fact = DeviceTable.from_host(tabs["fact"])
+    if args.case == "plan-timeline":
+        return _plan_timeline(args, tabs)
     if args.case in ("plan", "plan-graph"):
         from flexpushdowndb_gb300 import plan
 
@@ -558,6 +560,50 @@ def run_case(args):
     return _time_case(args, fn)
 
 
+def _plan_timeline(args, tabs):
+    """Kernel timeline of one replay of the captured star plan (CUPTI kernel
+    records through torch.profiler): per kernel its start and end relative
+    to the replay's first kernel and its duration. Prints one JSON line per
+    kernel, then a summary line."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+
+    from flexpushdowndb_gb300 import plan, workloads
+    from flexpushdowndb_gb300.tupleset import DeviceTable
+
+    d = json.loads(workloads.star_plan().to_json())
+    d.update({"cudaGraph": True, "streams": args.streams})
+    pp = plan.PreparedPlan(json.dumps(d), plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()}))
+    for _ in range(max(3, args.warmup)):
+        pp.execute()
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]):  # the first session of a process records nothing
+        torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        for _ in range(3):
+            r = pp.execute()
+        torch.cuda.synchronize()
+    evs = [e for e in prof.events() if e.device_type == torch.autograd.DeviceType.CUDA]
+    evs.sort(key=lambda e: e.time_range.start)
+    # the last replay: kernels after the last gap of more than 20 us
+    steps, cur = [], []
+    for e in evs:
+        if cur and e.time_range.start - max(x.time_range.end for x in cur) > 20:
+            steps.append(cur)
+            cur = []
+        cur.append(e)
+    steps.append(cur)
+    last = steps[-1]
+    t0 = last[0].time_range.start
+    for e in last:
+        print(json.dumps({"kernel": e.name.split("(")[0].replace("gfpdb::", "").replace("(anonymous namespace)::", ""),
+                          "start_us": round(e.time_range.start - t0, 1), "end_us": round(e.time_range.end - t0, 1),
+                          "us": round(e.time_range.end - e.time_range.start, 1)}))
+    print(json.dumps({"case": "plan-timeline", "streams": args.streams, "kernels": len(last),
+                      "span_us": round(max(e.time_range.end for e in last) - t0, 1),
+                      "device_ms_reported": r.stats["device_ns"] / 1e6}))
+
+
 def _time_case(args, fn):
     import torch
 
@@ -580,9 +626,10 @@ def main():
     ap.add_argument("--impl", default="gfpdb", choices=["gfpdb", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | batch")
+    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | plan-timeline | batch")
     ap.add_argument("--parts", type=int, default=64, help="fact partitions of the batch case")
     ap.add_argument("--rows", type=int, default=FACT_ROWS)
+    ap.add_argument("--streams", type=int, default=4, help="plan streams for --case plan-timeline")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form section")
     ap.add_argument("--no-csv", action="store_true", help="skip the CSV-form section")

@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_c
     // (4) the slice's row ids, in order, into its part of the row list
     int32_t* dst = rowlist + start;
     for (int i = lane; i < n_alive; i += 32) dst[i] = static_cast<int32_t>(start + list[i]);
-    if (lane == 0) p.tile_status[sl] = static_cast<uint64_t>(n_alive);
+    if (lane == 0) reinterpret_cast<uint32_t*>(p.tile_status)[sl] = static_cast<uint32_t>(n_alive);
     __syncwarp();  // the list is rewritten by the warp's next slice
   }
 }
@@ -551,9 +551,26 @@ __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid
   if (t0 >= n_tiles) return;
   const int64_t t1 = t0 + per < n_tiles ? t0 + per : n_tiles;
   const int nt = static_cast<int>(t1 - t0);
+  // the slices' counts are uint32 (written by select_probe_kernel); the
+  // counts before this range are summed with 16-byte loads, four in flight
+  const uint32_t* counts = reinterpret_cast<const uint32_t*>(p.tile_status);
   int before = 0;
-  for (int64_t t = threadIdx.x; t < t0; t += kSelThreads) before += static_cast<int>(p.tile_status[t]);
-  const int c = threadIdx.x < nt ? static_cast<int>(p.tile_status[t0 + threadIdx.x]) : 0;
+  {
+    const uint4* c4 = reinterpret_cast<const uint4*>(counts);  // 16-byte aligned: tile_status is
+    const int64_t q4 = t0 / 4;
+    int64_t q = threadIdx.x;
+    for (; q + 3 * kSelThreads < q4; q += 4 * kSelThreads) {
+      const uint4 a = c4[q], b = c4[q + kSelThreads], c = c4[q + 2 * kSelThreads], d = c4[q + 3 * kSelThreads];
+      before += static_cast<int>(a.x + a.y + a.z + a.w + b.x + b.y + b.z + b.w + c.x + c.y + c.z + c.w + d.x + d.y +
+                                 d.z + d.w);
+    }
+    for (; q < q4; q += kSelThreads) {
+      const uint4 a = c4[q];
+      before += static_cast<int>(a.x + a.y + a.z + a.w);
+    }
+    for (int64_t t = q4 * 4 + threadIdx.x; t < t0; t += kSelThreads) before += static_cast<int>(counts[t]);
+  }
+  const int c = threadIdx.x < nt ? static_cast<int>(counts[t0 + threadIdx.x]) : 0;
   int before_total;
   block_exclusive_sum<kSelThreads>(before, &before_total, s_w);
   __syncthreads();  // s_w is reused
