@@ -596,7 +596,8 @@ def _plan_timeline(args, tabs):
     last = steps[-1]
     t0 = last[0].time_range.start
     for e in last:
-        print(json.dumps({"kernel": e.name.split("(")[0].replace("gfpdb::", "").replace("(anonymous namespace)::", ""),
+        name = e.name.replace("(anonymous namespace)::", "").replace("gfpdb::", "").replace("void ", "")
+        print(json.dumps({"kernel": name.split("(")[0].split("<")[0],
                           "start_us": round(e.time_range.start - t0, 1), "end_us": round(e.time_range.end - t0, 1),
                           "us": round(e.time_range.end - e.time_range.start, 1)}))
     print(json.dumps({"case": "plan-timeline", "streams": args.streams, "kernels": len(last),
