@@ -127,7 +127,7 @@ BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_p
     DevCol k{c->data, nullptr, static_cast<int32_t>(c->type), 0};
     const int64_t* n_dev = i < part_rows_dev.size() ? part_rows_dev[i] : nullptr;
     int64_t blocks = (c->length + 255) / 256;
-    int64_t cap = static_cast<int64_t>(num_sms()) * 8;
+    int64_t cap = static_cast<int64_t>(num_sms()) * 4;  // grid-stride: four CTAs per SM keep the atomics busy
     ProfScope prof("bloom_build_kernel", s);
     if (blocks < 1) blocks = 1;
     bloom_build_kernel<<<static_cast<int>(blocks < cap ? blocks : cap), 256, 0, s>>>(

@@ -301,9 +301,12 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
   }
 }
 
+// Grid-stride launches: four CTAs per SM keep the atomics and probes busy,
+// and a launch sized for a large row capacity of which few rows arrive
+// (deferred inputs) dispatches fewer empty CTAs.
 int grid_for(int64_t n) {
   int64_t blocks = (n + 255) / 256;
-  int64_t cap = static_cast<int64_t>(num_sms()) * 8;
+  int64_t cap = static_cast<int64_t>(num_sms()) * 4;
   if (blocks > cap) blocks = cap;
   return static_cast<int>(blocks < 1 ? 1 : blocks);
 }
