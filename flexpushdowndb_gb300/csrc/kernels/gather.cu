@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256) fill_regions_kernel(const __grid_constant
 
 }  // namespace
 
-void fill_regions(const FillSpan* spans, int n, cudaStream_t s) {
+void fill_regions(const FillSpan* spans, int n, cudaStream_t s, int max_blocks) {
   FillParams p{};
   int64_t total = 0;
   for (int i = 0; i < n; ++i) {
@@ -242,7 +242,7 @@ void fill_regions(const FillSpan* spans, int n, cudaStream_t s) {
   }
   if (p.n == 0) return;
   int64_t blocks = (total + 255) / 256;
-  const int64_t cap = static_cast<int64_t>(num_sms()) * 4;
+  const int64_t cap = max_blocks > 0 ? max_blocks : static_cast<int64_t>(num_sms()) * 4;
   if (blocks > cap) blocks = cap;
   fill_regions_kernel<<<static_cast<int>(blocks < 1 ? 1 : blocks), 256, 0, s>>>(p);
   after_launch("fill_regions_kernel");

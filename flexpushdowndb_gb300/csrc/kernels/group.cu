@@ -665,16 +665,29 @@ class GroupTable {
 
   void init_table(uint64_t new_cap, cudaStream_t s) {
     const int na = static_cast<int>(accs.size());
-    auto nk = make_buffer(static_cast<int64_t>(new_cap + 1) * 8, s);
-    auto na_buf = make_buffer(static_cast<int64_t>(new_cap + 1) * 8 * (na > 0 ? na : 1), s);
-    AccKinds kinds{};
-    for (int a = 0; a < na; ++a) {
-      kinds.fn[a] = accs[a].fn;
-      kinds.vt[a] = accs[a].vt;
+    // Empty keys are all-ones and sum / count accumulators start at zero, so
+    // without MIN / MAX the table comes pre-filled (no init kernel; inside a
+    // captured plan from the graph's fill regions).
+    bool zero_init = true;
+    for (int a = 0; a < na; ++a) zero_init &= accs[a].fn != AGG_MIN && accs[a].fn != AGG_MAX;
+    const int64_t key_bytes = static_cast<int64_t>(new_cap + 1) * 8;
+    const int64_t acc_bytes = static_cast<int64_t>(new_cap + 1) * 8 * (na > 0 ? na : 1);
+    BufferPtr nk, na_buf;
+    if (zero_init) {
+      nk = make_filled(key_bytes, 0xFF, s);
+      na_buf = make_filled(acc_bytes, 0, s);
+    } else {
+      nk = make_buffer(key_bytes, s);
+      na_buf = make_buffer(acc_bytes, s);
+      AccKinds kinds{};
+      for (int a = 0; a < na; ++a) {
+        kinds.fn[a] = accs[a].fn;
+        kinds.vt[a] = accs[a].vt;
+      }
+      group_init_kernel<<<grid_for(static_cast<int64_t>(new_cap + 1)), 256, 0, s>>>(
+          nk->as<uint64_t>(), na_buf->as<unsigned long long>(), new_cap + 1, na, kinds);
+      after_launch("group_init_kernel");
     }
-    group_init_kernel<<<grid_for(static_cast<int64_t>(new_cap + 1)), 256, 0, s>>>(
-        nk->as<uint64_t>(), na_buf->as<unsigned long long>(), new_cap + 1, na, kinds);
-    after_launch("group_init_kernel");
     if (!status) status = make_filled(sizeof(DevStatus), 0, s);
     if (cap > 0) {
       group_rehash_kernel<<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(

@@ -45,7 +45,9 @@ struct FillSpan {
   int32_t value;
   int32_t pad;
 };
-void fill_regions(const FillSpan* spans, int n, cudaStream_t s);
+// max_blocks > 0 caps the grid (a fill with time to spare can run on a few
+// SMs beside other work).
+void fill_regions(const FillSpan* spans, int n, cudaStream_t s, int max_blocks = 0);
 
 // Host-to-device copy of a scan's input: the copy engine (cudaMemcpyAsync),
 // or, with host_copy_mode() == 1 and page-locked aligned sources of at least
