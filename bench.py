@@ -532,6 +532,8 @@ def run_case(args):
         fn = lambda: batch.star_batch(spec, dev, use_graph=False).table  # noqa: E731
         args.rows = sum(tabs[p].num_rows for p in parts)
         return _time_case(args, fn)
+    if args.case in ("join", "group", "csv"):
+        return _operator_case(args)
     tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
     fact = DeviceTable.from_host(tabs["fact"])
     if args.case == "plan-timeline":
@@ -557,6 +559,54 @@ def run_case(args):
         fn = lambda: ops.select(fact, blooms=blooms)  # noqa: E731
     else:
         raise SystemExit(f"unknown case {args.case}")
+    return _time_case(args, fn)
+
+
+def _operator_case(args):
+    """Single operators at sizes past the L2, for their ncu captures:
+    `join`: args.rows probe rows (int32 keys uniform over the build keys and
+    10% more, two payload columns) against args.rows / 10 unique build keys,
+    fixed-width outputs (one probe-and-materialise kernel); `group`: args.rows
+    rows of Zipf(1.1) int64 keys over args.rows / 2 keys, sum and count;
+    `csv`: the lineitem text of args.rows rows parsed on the device."""
+    import numpy as np
+
+    from flexpushdowndb_gb300 import ops, workloads
+    from flexpushdowndb_gb300.expression import col
+    from flexpushdowndb_gb300.tupleset import Column, DeviceTable, Table
+
+    ops.init(0)
+    n = args.rows
+    rng = np.random.default_rng(7000)
+    if args.case == "join":
+        nb = max(1, n // 10)
+        build = Table([Column("pk", "int32", rng.permutation(nb)), Column("bv", "int64", rng.integers(0, 10**9, nb))])
+        probe = DeviceTable.from_host(Table([Column("fk", "int32", rng.integers(0, nb + nb // 10, n)),
+                                             Column("pv", "int32", rng.integers(0, 100, n))]))
+        j = ops.HashJoin("pk", "fk")
+        j.put_build(DeviceTable.from_host(build))
+        j.finalize_build()
+        fn = lambda: j.probe(probe)  # noqa: E731
+    elif args.case == "group":
+        t = DeviceTable.from_host(workloads.groupby_table(n, max(1, n // 2)))
+        aggs = [ops.aggregate("SUM", "s", col("v")), ops.aggregate("COUNT", "c")]
+
+        def fn():
+            g = ops.Group(["k"], aggs)
+            g.group(t)
+            return g.finalise()
+    else:
+        import torch
+
+        text = workloads.lineitem_csv(n)
+        dev = torch.frombuffer(bytearray(text), dtype=torch.uint8).cuda()
+
+        class _Rows:
+            def __init__(self, k):
+                self.num_rows = k
+
+        fn = lambda: _Rows(ops.csv_read(len(text), workloads.LINEITEM_FIELDS, delimiter="|",  # noqa: E731
+                                        device_ptr=dev.data_ptr(), to_host=False))
     return _time_case(args, fn)
 
 
@@ -627,7 +677,7 @@ def main():
     ap.add_argument("--impl", default="gfpdb", choices=["gfpdb", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | plan-timeline | batch")
+    ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | plan-timeline | batch | join | group | csv")
     ap.add_argument("--parts", type=int, default=64, help="fact partitions of the batch case")
     ap.add_argument("--rows", type=int, default=FACT_ROWS)
     ap.add_argument("--streams", type=int, default=4, help="plan streams for --case plan-timeline")

@@ -30,6 +30,7 @@ namespace {
 
 constexpr int kGroupThreads = 256;
 constexpr int kGroupSmemSlotsMax = 1024;  // slots of a CTA's shared-memory table
+constexpr int kGroupSmemProbes = 4;       // shared-memory slots a row tries before the global table
 constexpr uint32_t kDictSpinLimit = 1u << 20;
 
 struct AccDev {
@@ -162,8 +163,12 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
     const uint64_t key = pack_key(p, r);
     int found = -1;
     if (p.use_smem && key != kEmptySlot) {
+      // A short probe run: with few groups the table is sparse and a key is
+      // found or placed in a step or two; with many groups (high-cardinality
+      // keys) the table is soon full and a longer run only delays the row's
+      // trip to the global table.
       int slot = static_cast<int>(hash_key(static_cast<int64_t>(key)) & sm_mask);
-      for (int i = 0; i < 16; ++i) {
+      for (int i = 0; i < kGroupSmemProbes; ++i) {
         uint64_t s = *reinterpret_cast<volatile uint64_t*>(s_keys + slot);
         if (s == kEmptySlot) {
           s = atomicCAS(reinterpret_cast<unsigned long long*>(s_keys + slot),
