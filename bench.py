@@ -532,7 +532,7 @@ def run_case(args):
         fn = lambda: batch.star_batch(spec, dev, use_graph=False).table  # noqa: E731
         args.rows = sum(tabs[p].num_rows for p in parts)
         return _time_case(args, fn)
-    if args.case in ("join", "group", "csv"):
+    if args.case in ("join", "group", "csv", "filter"):
         return _operator_case(args)
     tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
     fact = DeviceTable.from_host(tabs["fact"])
@@ -568,7 +568,10 @@ def _operator_case(args):
     10% more, two payload columns) against args.rows / 10 unique build keys,
     fixed-width outputs (one probe-and-materialise kernel); `group`: args.rows
     rows of Zipf(1.1) int64 keys over args.rows / 2 keys, sum and count;
-    `csv`: the lineitem text of args.rows rows parsed on the device."""
+    `csv`: the lineitem text of args.rows rows parsed on the device;
+    `filter`: a two-comparison range conjunction (~2% of rows) over an int32
+    and an int64 column of args.rows rows, projecting an int32 and an int64
+    column; prints the kernel's algorithmic GB/s beside the call time."""
     import numpy as np
 
     from flexpushdowndb_gb300 import ops, workloads
@@ -595,6 +598,25 @@ def _operator_case(args):
             g = ops.Group(["k"], aggs)
             g.group(t)
             return g.finalise()
+    elif args.case == "filter":
+        from flexpushdowndb_gb300.expression import and_, gte, lt, num_lit
+
+        t = Table([Column("a", "int32", rng.integers(0, 1000, n)), Column("b", "int64", rng.integers(0, 10**9, n)),
+                   Column("c", "int32", rng.integers(0, 100, n)), Column("d", "int64", rng.integers(0, 10**12, n))])
+        dt = DeviceTable.from_host(t)
+        pred = and_(lt(col("a"), num_lit(100)), gte(col("b"), num_lit(800_000_000, "int64")))
+        f = ops.Filter(pred, t)
+        fn = lambda: f.evaluate(dt, project=["c", "d"])  # noqa: E731
+        out = fn()
+        sel = out.num_rows
+        for _ in range(max(3, args.warmup)):
+            fn()
+        ms = _kernel_ms(lambda: f.evaluate(dt, project=["c", "d"]),
+                        ("select_kernel", "select_probe_kernel", "select_gather_kernel"), args.steps)
+        algo = n * 12 + sel * 24  # a, b over every row; c, d read and written for the selected rows
+        print(json.dumps({"case": "filter", "rows": n, "selected": sel, "kernel_ms": ms,
+                          "algorithmic_gbs": algo / (ms * 1e6)}))
+        return
     else:
         import torch
 
@@ -608,6 +630,15 @@ def _operator_case(args):
         fn = lambda: _Rows(ops.csv_read(len(text), workloads.LINEITEM_FIELDS, delimiter="|",  # noqa: E731
                                         device_ptr=dev.data_ptr(), to_host=False))
     return _time_case(args, fn)
+
+
+def _kernel_ms(fn, names, reps):
+    """Mean device time (CUDA events around each launch) of the named
+    kernels per call of fn."""
+    from flexpushdowndb_gb300 import _abi
+
+    prof = _kernel_profile(_abi.lib(), _abi, fn, reps)
+    return sum(v["ms"] for k, v in prof.items() if k in names) / reps
 
 
 def _plan_timeline(args, tabs):

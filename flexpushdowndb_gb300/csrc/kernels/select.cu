@@ -361,6 +361,59 @@ int select_blocks_per_sm(bool with_pred, size_t dyn) {
   return per_sm;
 }
 
+// A predicate leaf of the simple form: an integer column against an integer
+// literal, the comparison reduced to a 4-bit truth table over
+// (value < literal, value == literal). The compact and the two-pass
+// selections evaluate a CNF of such leaves.
+constexpr int kSimpleMaxLeaves = 8;
+
+struct SimpleLeaf {
+  const void* col;
+  int64_t lit;
+  int8_t wide;          // 1: int64 column; 0: int32 / date32
+  int8_t truth;         // bit (2 * (v < lit) + (v == lit)) set when the leaf holds
+  int8_t clause_start;  // 1: first leaf of its clause
+  int8_t pad[5];
+};
+
+// The predicate of p as simple leaves in clause order, or false when a leaf
+// has another form, a clause is empty, there are more than max leaves, or a
+// leaf's column is not 16-byte aligned.
+bool simple_leaves(const SelectParams& p, SimpleLeaf* out, int max, int* n_out) {
+  auto aligned = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  // truth tables over (lt, eq) for LO_LT, LO_LE, LO_GT, LO_GE, LO_EQ, LO_NE
+  static const int8_t kTruth[6] = {4, 6, 1, 3, 2, 5};
+  static const int8_t kMirror[6] = {LO_GT, LO_GE, LO_LT, LO_LE, LO_EQ, LO_NE};
+  const Program& g = p.prog;
+  int n = 0;
+  for (int c = 0; c < g.n_clauses; ++c) {
+    if (g.clause_begin[c] >= g.clause_begin[c + 1]) return false;
+    for (int l = g.clause_begin[c]; l < g.clause_begin[c + 1]; ++l) {
+      const Leaf& L = g.leaves[l];
+      if (L.op < LO_LT || L.op > LO_NE || L.cmp_vt != VT_I64) return false;
+      Operand a = L.lhs, b = L.rhs;
+      int op = L.op;
+      if (a.kind == OPND_LIT && b.kind == OPND_COL) {
+        std::swap(a, b);
+        op = kMirror[op];
+      }
+      if (a.kind != OPND_COL || b.kind != OPND_LIT || b.vt != VT_I64) return false;
+      const DevCol& dc = p.cols[a.col];
+      if ((dc.type != CT_I32 && dc.type != CT_I64 && dc.type != CT_DATE32) || !aligned(dc.data)) return false;
+      if (n == max) return false;
+      SimpleLeaf& o = out[n++];
+      o = SimpleLeaf{};
+      o.col = dc.data;
+      o.lit = b.lit.i;
+      o.wide = dc.type == CT_I64 ? 1 : 0;
+      o.truth = kTruth[op];
+      o.clause_start = l == g.clause_begin[c] ? 1 : 0;
+    }
+  }
+  *n_out = n;
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // Probe-only selection over a large input (the BloomFilterUse chain over the
 // fact table), in two passes.
@@ -419,7 +472,17 @@ __device__ __forceinline__ uint32_t probe8_first(const uint32_t* blocks, uint32_
   }
 }
 
+// The predicate of a two-pass selection (simple leaves, AND of ORs).
+struct StreamPred {
+  int32_t n_leaves;
+  int32_t pad;
+  SimpleLeaf leaves[kSimpleMaxLeaves];
+};
+
+// kPred = false compiles the probe-only form, which needs fewer registers.
+template <bool kPred>
 __global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_constant__ SelectParams p,
+                                                                  const __grid_constant__ StreamPred sp,
                                                                   int32_t* __restrict__ rowlist) {
   extern __shared__ __align__(16) uint32_t s_filter[];  // the first probe's filter, when staged
   __shared__ uint16_t s_list[kPwThreads / 32][kPwRows];  // per warp: its slice's survivors
@@ -461,6 +524,26 @@ __global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_c
     const int64_t rem = n_rows - row0;
     const bool full = rem >= kSelItems;
     uint32_t mask = full ? 0xFFu : (rem <= 0 ? 0u : ((1u << rem) - 1u));
+    // (0) the predicate over this lane's 8 rows (16-byte loads when full)
+    if (kPred && mask != 0) {
+      uint32_t all = mask, any = 0;
+#pragma unroll 1
+      for (int l = 0; l < sp.n_leaves; ++l) {
+        const SimpleLeaf& L = sp.leaves[l];
+        if (L.clause_start && l > 0) {
+          all &= any;
+          any = 0;
+        }
+        int64_t v[kSelItems];
+        load8(DevCol{L.col, nullptr, L.wide ? CT_I64 : CT_I32, 0}, row0, mask, full, v);
+#pragma unroll
+        for (int kk = 0; kk < kSelItems; ++kk) {
+          const uint32_t idx = (static_cast<uint32_t>(v[kk] < L.lit) << 1) | static_cast<uint32_t>(v[kk] == L.lit);
+          any |= ((static_cast<uint32_t>(L.truth) >> idx) & 1u) << kk;
+        }
+      }
+      mask = all & any;
+    }
     // (1) the first probe over this lane's 8 rows
     if ((valid & 1u) && mask != 0) {
       int64_t keys[kSelItems];
@@ -601,21 +684,23 @@ __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid
   if (t1 == n_tiles && threadIdx.x == 0) p.status->value = base + range_total;
 }
 
-int select_probe_blocks_per_sm(size_t dyn) {
+int select_probe_blocks_per_sm(bool with_pred, size_t dyn) {
   static std::mutex mu;
-  static std::map<size_t, int> cache;
-  static bool attr_set = false;
+  static std::map<std::pair<bool, size_t>, int> cache;
+  static bool attr_set[2] = {false, false};
   std::lock_guard<std::mutex> lk(mu);
-  auto it = cache.find(dyn);
+  const auto key = std::make_pair(with_pred, dyn);
+  auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  if (!attr_set) {
-    GF_CUDA(cudaFuncSetAttribute(select_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(kSpMaxDynamic)));
-    attr_set = true;
+  const void* fn = with_pred ? reinterpret_cast<const void*>(select_probe_kernel<true>)
+                             : reinterpret_cast<const void*>(select_probe_kernel<false>);
+  if (!attr_set[with_pred]) {
+    GF_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSpMaxDynamic)));
+    attr_set[with_pred] = true;
   }
   int per_sm = 0;
-  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, select_probe_kernel, kPwThreads, dyn));
-  cache[dyn] = per_sm;
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPwThreads, dyn));
+  cache[key] = per_sm;
   return per_sm;
 }
 
@@ -633,15 +718,6 @@ constexpr int kLiteTile = kLiteThreads * kLiteItems;
 constexpr int kLiteMaxLeaves = 8;
 constexpr int kLiteMaxOut = 12;
 constexpr int64_t kLiteMaxRows = int64_t{1} << 18;
-
-struct LiteLeaf {
-  const void* col;
-  int64_t lit;
-  int8_t wide;          // 1: int64 column; 0: int32 / date32
-  int8_t truth;         // bit (2 * (v < lit) + (v == lit)) set when the leaf holds
-  int8_t clause_start;  // 1: first leaf of its clause
-  int8_t pad[5];
-};
 
 struct LiteProbe {
   const uint32_t* blocks;
@@ -669,7 +745,7 @@ struct LiteParams {
   int32_t n_probes;
   int32_t n_out;
   int32_t pad;
-  LiteLeaf leaves[kLiteMaxLeaves];
+  SimpleLeaf leaves[kLiteMaxLeaves];
   LiteProbe probes[kMaxBlooms];
   LiteOut outs[kLiteMaxOut];
   int32_t* out_rowids;
@@ -731,7 +807,7 @@ __global__ void __launch_bounds__(kLiteThreads) select_lite_kernel(const __grid_
       uint32_t all = mask, any = 0;
 #pragma unroll 1
       for (int l = 0; l < p.n_leaves; ++l) {
-        const LiteLeaf& L = p.leaves[l];
+        const SimpleLeaf& L = p.leaves[l];
         if (L.clause_start && l > 0) {
           all &= any;
           any = 0;
@@ -817,33 +893,7 @@ __global__ void __launch_bounds__(kLiteThreads) select_lite_kernel(const __grid_
 bool lite_params(const SelectParams& p, LiteParams& lp) {
   std::memset(&lp, 0, sizeof(lp));
   auto aligned = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
-  // truth tables over (lt, eq) for LO_LT, LO_LE, LO_GT, LO_GE, LO_EQ, LO_NE
-  static const int8_t kTruth[6] = {4, 6, 1, 3, 2, 5};
-  static const int8_t kMirror[6] = {LO_GT, LO_GE, LO_LT, LO_LE, LO_EQ, LO_NE};
-  const Program& g = p.prog;
-  for (int c = 0; c < g.n_clauses; ++c) {
-    if (g.clause_begin[c] >= g.clause_begin[c + 1]) return false;
-    for (int l = g.clause_begin[c]; l < g.clause_begin[c + 1]; ++l) {
-      const Leaf& L = g.leaves[l];
-      if (L.op < LO_LT || L.op > LO_NE || L.cmp_vt != VT_I64) return false;
-      Operand a = L.lhs, b = L.rhs;
-      int op = L.op;
-      if (a.kind == OPND_LIT && b.kind == OPND_COL) {
-        std::swap(a, b);
-        op = kMirror[op];
-      }
-      if (a.kind != OPND_COL || b.kind != OPND_LIT || b.vt != VT_I64) return false;
-      const DevCol& dc = p.cols[a.col];
-      if ((dc.type != CT_I32 && dc.type != CT_I64 && dc.type != CT_DATE32) || !aligned(dc.data)) return false;
-      if (lp.n_leaves == kLiteMaxLeaves) return false;
-      LiteLeaf& o = lp.leaves[lp.n_leaves++];
-      o.col = dc.data;
-      o.lit = b.lit.i;
-      o.wide = dc.type == CT_I64 ? 1 : 0;
-      o.truth = kTruth[op];
-      o.clause_start = l == g.clause_begin[c] ? 1 : 0;
-    }
-  }
+  if (!simple_leaves(p, lp.leaves, kLiteMaxLeaves, &lp.n_leaves)) return false;
   lp.n_probes = p.n_probes;
   for (int pi = 0; pi < p.n_probes; ++pi) {
     const BloomDev& b = p.probes[pi];
@@ -985,7 +1035,10 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   const bool lite = n <= kLiteMaxRows && lite_params(p, lp);
   // probe-only selections over large inputs take the two-pass kernels (their
   // unit is a warp's 256-row slice)
-  const bool two_pass = !lite && p.prog.n_clauses == 0 && p.n_probes > 0 && n >= kSpMinRows;
+  // (probe chains, and predicates of simple leaves, with or without probes)
+  StreamPred spred{};
+  const bool two_pass = !lite && n >= kSpMinRows && simple_leaves(p, spred.leaves, kSimpleMaxLeaves, &spred.n_leaves) &&
+                        (p.n_probes > 0 || spred.n_leaves > 0);
   const int64_t unit = lite ? kLiteTile : two_pass ? kPwRows : kSelTile;
   const int64_t n_tiles = (n + unit - 1) / unit;  // upper bound
   p.n_tiles = n_tiles;
@@ -1019,19 +1072,30 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
   } else if (n_tiles > 0 && two_pass) {
     // pass 1: probes; each slice's selected row ids into its part of rowlist
     const size_t dyn = p.probes[0].smem_word >= 0 ? static_cast<size_t>(p.probes[0].smem_cap_words) * 4 : 0;
-    const int per_sm = select_probe_blocks_per_sm(dyn);
+    const bool with_pred = spred.n_leaves > 0;
+    const int per_sm = select_probe_blocks_per_sm(with_pred, dyn);
     auto rowlist = make_buffer(n * 4, s);
     {
       const int64_t want = (n_tiles + kPwThreads / 32 - 1) / (kPwThreads / 32);
       const int64_t cap = static_cast<int64_t>(num_sms()) * (per_sm > 0 ? per_sm : 1);
       ProfScope prof("select_probe_kernel", s);
-      select_probe_kernel<<<static_cast<int>(want < cap ? want : cap), kPwThreads, dyn, s>>>(p, rowlist->as<int32_t>());
+      const int grid = static_cast<int>(want < cap ? want : cap);
+      if (with_pred)
+        select_probe_kernel<true><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>());
+      else
+        select_probe_kernel<false><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>());
       after_launch("select_probe_kernel");
       prof.stop(0);
-      // the first probe's keys over all rows (later probes' keys are read
-      // for survivors only and not counted)
-      prof.set_bytes_model(p.n_dev, n, p.cols[p.probes[0].col].type == CT_I64 ? 8 : 4, &p.status->value, 4.0, scratch,
-                           in.rows_owner());
+      // the predicate's columns and the first probe's keys over all rows
+      // (later probes' keys are read for survivors only and not counted)
+      double per_row = 0;
+      for (int l = 0; l < spred.n_leaves; ++l) {
+        bool seen = false;
+        for (int m = 0; m < l; ++m) seen |= spred.leaves[m].col == spred.leaves[l].col;
+        if (!seen) per_row += spred.leaves[l].wide ? 8 : 4;
+      }
+      if (p.n_probes > 0) per_row += p.cols[p.probes[0].col].type == CT_I64 ? 8 : 4;
+      prof.set_bytes_model(p.n_dev, n, per_row, &p.status->value, 4.0, scratch, in.rows_owner());
     }
     {
       // ranges of at most kSelThreads slices, at least two CTAs per SM

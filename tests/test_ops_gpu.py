@@ -471,3 +471,24 @@ def test_select_probe_first_filter_in_global_memory(gpu):
     want = oops.bloom_use(oops.bloom_use(fact, bf.words(), "fk2"), oops.bloom_words(d3["d3_pk"]), "fk3")
     got = ops.select(DeviceTable.from_host(fact), None, blooms)
     assert got.rows() == want.rows()
+
+
+@pytest.mark.parametrize("pi", [0, 2, 3, 5])
+def test_filter_large_simple_predicates(gpu, pi):
+    """A million rows and more with an integer column-vs-literal predicate
+    take the two-pass kernels (warp slices, then the gather), utf8 and float
+    outputs included; rows and order match the oracle."""
+    n = (1 << 20) + 4097
+    t = rand_table(n, seed=300 + pi)
+    pred = LITE_PREDICATES[pi]
+    got = ops.Filter(pred, t).evaluate(DeviceTable.from_host(t))
+    assert got.rows() == oops.filter_table(t, pred).rows()
+
+
+def test_select_large_predicate_with_probes(gpu):
+    """A predicate and a chain of bloom probes over 1.2 million rows in one
+    two-pass selection."""
+    fact, blooms, seq = _probe_case(1_200_003, "int32", 2400)
+    pred = and_(gt(col("qty"), num_lit(10)), lte(num_lit(3), col("discount")))
+    got = ops.select(DeviceTable.from_host(fact), ops.Filter(pred, fact), blooms)
+    assert got.rows() == oops.filter_table(seq, pred).rows()
