@@ -618,70 +618,63 @@ __global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_c
   }
 }
 
-// Pass 2: each CTA takes a contiguous range of at most kSelThreads slices,
-// sums the counts of the slices before it, scans its own slices' counts, then
-// moves every selected row of its range in one parallel pass (row ids in
-// order in each slice's part of the row-id buffer) to the output. The CTA
-// holding the last slice records the total.
+// Pass 2: ranges of kSelThreads consecutive slices, taken in ticket order.
+// A CTA scans its range's slice counts, learns the rows of all earlier
+// ranges by decoupled look-back over their published totals (single pass,
+// linear in the slices), then moves every selected row of its range in one
+// parallel pass (row ids in order in each slice's part of the row-id buffer)
+// to the output. The CTA holding the last range records the total.
 __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid_constant__ SelectParams p,
-                                                                   const int32_t* rowlist, int32_t* out_rowids) {
+                                                                   const int32_t* rowlist, int32_t* out_rowids,
+                                                                   uint64_t* range_status, uint32_t* range_ticket) {
   __shared__ int s_w[kSelThreads / 32 + 1];
   __shared__ int s_pref[kSelThreads + 1];
+  __shared__ uint32_t s_range;
+  __shared__ uint64_t s_base;
   const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
   const int64_t n_tiles = (n_rows + kPwRows - 1) / kPwRows;
-  const int64_t per = (n_tiles + gridDim.x - 1) / gridDim.x;  // <= kSelThreads by the launch
-  const int64_t t0 = static_cast<int64_t>(blockIdx.x) * per;
-  if (t0 >= n_tiles) return;
-  const int64_t t1 = t0 + per < n_tiles ? t0 + per : n_tiles;
-  const int nt = static_cast<int>(t1 - t0);
-  // the slices' counts are uint32 (written by select_probe_kernel); the
-  // counts before this range are summed with 16-byte loads, four in flight
-  const uint32_t* counts = reinterpret_cast<const uint32_t*>(p.tile_status);
-  int before = 0;
-  {
-    const uint4* c4 = reinterpret_cast<const uint4*>(counts);  // 16-byte aligned: tile_status is
-    const int64_t q4 = t0 / 4;
-    int64_t q = threadIdx.x;
-    for (; q + 3 * kSelThreads < q4; q += 4 * kSelThreads) {
-      const uint4 a = c4[q], b = c4[q + kSelThreads], c = c4[q + 2 * kSelThreads], d = c4[q + 3 * kSelThreads];
-      before += static_cast<int>(a.x + a.y + a.z + a.w + b.x + b.y + b.z + b.w + c.x + c.y + c.z + c.w + d.x + d.y +
-                                 d.z + d.w);
+  const int64_t n_ranges = (n_tiles + kSelThreads - 1) / kSelThreads;
+  const uint32_t* counts = reinterpret_cast<const uint32_t*>(p.tile_status);  // uint32, from select_probe_kernel
+  for (;;) {
+    if (threadIdx.x == 0) s_range = atomicAdd(range_ticket, 1u);
+    __syncthreads();
+    const int64_t r = s_range;
+    if (r >= n_ranges) break;
+    const int64_t t0 = r * kSelThreads;
+    const int64_t t1 = t0 + kSelThreads < n_tiles ? t0 + kSelThreads : n_tiles;
+    const int nt = static_cast<int>(t1 - t0);
+    const int c = threadIdx.x < nt ? static_cast<int>(counts[t0 + threadIdx.x]) : 0;
+    int range_total;
+    const int excl = block_exclusive_sum<kSelThreads>(c, &range_total, s_w);
+    if (threadIdx.x < nt) s_pref[threadIdx.x] = excl;
+    if (threadIdx.x == 0) s_pref[nt] = range_total;
+    if (threadIdx.x < 32) {
+      const uint64_t b = lookback_exclusive(range_status, r, static_cast<uint64_t>(range_total), p.status);
+      if (threadIdx.x == 0) s_base = b;
     }
-    for (; q < q4; q += kSelThreads) {
-      const uint4 a = c4[q];
-      before += static_cast<int>(a.x + a.y + a.z + a.w);
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(s_base);
+    for (int i = threadIdx.x; i < range_total; i += kSelThreads) {
+      int lo = 0, hi = nt - 1;  // last slice of the range whose first output is <= i
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pref[mid] <= i) lo = mid;
+        else hi = mid - 1;
+      }
+      const int32_t row = rowlist[(t0 + lo) * kPwRows + (i - s_pref[lo])];
+      const int64_t o = base + i;
+      for (int j = 0; j < p.n_out; ++j) {
+        const OutCol& oc = p.outs[j];
+        if (oc.width == 8)
+          static_cast<long long*>(oc.dst)[o] = __ldg(static_cast<const long long*>(oc.src) + row);
+        else
+          static_cast<int*>(oc.dst)[o] = __ldg(static_cast<const int*>(oc.src) + row);
+      }
+      if (out_rowids != nullptr) out_rowids[o] = row;
     }
-    for (int64_t t = q4 * 4 + threadIdx.x; t < t0; t += kSelThreads) before += static_cast<int>(counts[t]);
+    if (r == n_ranges - 1 && threadIdx.x == 0) p.status->value = base + range_total;
+    __syncthreads();  // s_pref, s_w and s_range are rewritten for the next range
   }
-  const int c = threadIdx.x < nt ? static_cast<int>(counts[t0 + threadIdx.x]) : 0;
-  int before_total;
-  block_exclusive_sum<kSelThreads>(before, &before_total, s_w);
-  __syncthreads();  // s_w is reused
-  int range_total;
-  const int excl = block_exclusive_sum<kSelThreads>(c, &range_total, s_w);
-  if (threadIdx.x < nt) s_pref[threadIdx.x] = excl;
-  if (threadIdx.x == 0) s_pref[nt] = range_total;
-  __syncthreads();
-  const int64_t base = before_total;
-  for (int i = threadIdx.x; i < range_total; i += kSelThreads) {
-    int lo = 0, hi = nt - 1;  // last tile of the range whose first output is <= i
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (s_pref[mid] <= i) lo = mid;
-      else hi = mid - 1;
-    }
-    const int32_t row = rowlist[(t0 + lo) * kPwRows + (i - s_pref[lo])];
-    const int64_t o = base + i;
-    for (int j = 0; j < p.n_out; ++j) {
-      const OutCol& oc = p.outs[j];
-      if (oc.width == 8)
-        static_cast<long long*>(oc.dst)[o] = __ldg(static_cast<const long long*>(oc.src) + row);
-      else
-        static_cast<int*>(oc.dst)[o] = __ldg(static_cast<const int*>(oc.src) + row);
-    }
-    if (out_rowids != nullptr) out_rowids[o] = row;
-  }
-  if (t1 == n_tiles && threadIdx.x == 0) p.status->value = base + range_total;
 }
 
 int select_probe_blocks_per_sm(bool with_pred, size_t dyn) {
@@ -1098,11 +1091,14 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
       prof.set_bytes_model(p.n_dev, n, per_row, &p.status->value, 4.0, scratch, in.rows_owner());
     }
     {
-      // ranges of at most kSelThreads slices, at least two CTAs per SM
-      int64_t grid = std::max<int64_t>((n_tiles + kSelThreads - 1) / kSelThreads,
-                                       std::min<int64_t>(n_tiles, static_cast<int64_t>(num_sms()) * 2));
+      // ranges of kSelThreads slices in ticket order, at most four CTAs per SM
+      const int64_t n_ranges = (n_tiles + kSelThreads - 1) / kSelThreads;
+      auto range_scratch = make_filled(64 + n_ranges * 8, 0, s);  // ticket line, then one status word per range
+      const int64_t cap = static_cast<int64_t>(num_sms()) * 4;
       ProfScope prof("select_gather_kernel", s);
-      select_gather_kernel<<<static_cast<int>(grid), kSelThreads, 0, s>>>(p, rowlist->as<int32_t>(), p.out_rowids);
+      select_gather_kernel<<<static_cast<int>(n_ranges < cap ? n_ranges : cap), kSelThreads, 0, s>>>(
+          p, rowlist->as<int32_t>(), p.out_rowids, reinterpret_cast<uint64_t*>(range_scratch->as<char>() + 64),
+          range_scratch->as<uint32_t>());
       after_launch("select_gather_kernel");
       prof.stop(0);
       prof.set_bytes_model(nullptr, 0, 0, &p.status->value, 4.0 + proj_read + proj_write, scratch, in.rows_owner());
