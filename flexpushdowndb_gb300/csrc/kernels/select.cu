@@ -432,6 +432,7 @@ bool simple_leaves(const SelectParams& p, SimpleLeaf* out, int max, int* n_out) 
 // their output offsets.
 // Output order is input order, as in the single-pass kernel.
 constexpr int kPwThreads = 256;                 // 8 warps
+constexpr int kGatherSlices = kSelThreads;     // slices per range of the gather pass (one per thread)
 constexpr int kPwRows = 32 * kSelItems;         // rows per warp slice
 constexpr int64_t kSpMinRows = int64_t{1} << 20;  // below this select_kernel's tiles all start at once
 constexpr int64_t kSpMaxDynamic = 96 * 1024;    // the first filter in shared memory
@@ -481,9 +482,10 @@ struct StreamPred {
 
 // kPred = false compiles the probe-only form, which needs fewer registers.
 template <bool kPred>
-__global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_constant__ SelectParams p,
+__global__ void __launch_bounds__(kPwThreads, kPred ? 4 : 5) select_probe_kernel(const __grid_constant__ SelectParams p,
                                                                   const __grid_constant__ StreamPred sp,
-                                                                  int32_t* __restrict__ rowlist) {
+                                                                  int32_t* __restrict__ rowlist,
+                                                                  unsigned int* __restrict__ range_totals) {
   extern __shared__ __align__(16) uint32_t s_filter[];  // the first probe's filter, when staged
   __shared__ uint16_t s_list[kPwThreads / 32][kPwRows];  // per warp: its slice's survivors
   __shared__ uint32_t s_nblocks[kMaxBlooms];
@@ -613,47 +615,45 @@ __global__ void __launch_bounds__(kPwThreads) select_probe_kernel(const __grid_c
     // (4) the slice's row ids, in order, into its part of the row list
     int32_t* dst = rowlist + start;
     for (int i = lane; i < n_alive; i += 32) dst[i] = static_cast<int32_t>(start + list[i]);
-    if (lane == 0) reinterpret_cast<uint32_t*>(p.tile_status)[sl] = static_cast<uint32_t>(n_alive);
+    if (lane == 0) {
+      reinterpret_cast<uint32_t*>(p.tile_status)[sl] = static_cast<uint32_t>(n_alive);
+      if (n_alive > 0) atomicAdd(range_totals + sl / kGatherSlices, static_cast<unsigned int>(n_alive));
+    }
     __syncwarp();  // the list is rewritten by the warp's next slice
   }
 }
 
-// Pass 2: ranges of kSelThreads consecutive slices, taken in ticket order.
-// A CTA scans its range's slice counts, learns the rows of all earlier
-// ranges by decoupled look-back over their published totals (single pass,
-// linear in the slices), then moves every selected row of its range in one
+// Pass 2: ranges of kGatherSlices consecutive slices. Pass 1 also added
+// each slice's count into its range's total, so a CTA learns the rows of all
+// earlier ranges by summing their totals (no ordering between CTAs), scans
+// its own slices' counts, then moves every selected row of its range in one
 // parallel pass (row ids in order in each slice's part of the row-id buffer)
 // to the output. The CTA holding the last range records the total.
 __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid_constant__ SelectParams p,
                                                                    const int32_t* rowlist, int32_t* out_rowids,
-                                                                   uint64_t* range_status, uint32_t* range_ticket) {
+                                                                   const unsigned int* __restrict__ range_totals) {
   __shared__ int s_w[kSelThreads / 32 + 1];
   __shared__ int s_pref[kSelThreads + 1];
-  __shared__ uint32_t s_range;
-  __shared__ uint64_t s_base;
   const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
   const int64_t n_tiles = (n_rows + kPwRows - 1) / kPwRows;
-  const int64_t n_ranges = (n_tiles + kSelThreads - 1) / kSelThreads;
+  const int64_t n_ranges = (n_tiles + kGatherSlices - 1) / kGatherSlices;
   const uint32_t* counts = reinterpret_cast<const uint32_t*>(p.tile_status);  // uint32, from select_probe_kernel
-  for (;;) {
-    if (threadIdx.x == 0) s_range = atomicAdd(range_ticket, 1u);
-    __syncthreads();
-    const int64_t r = s_range;
-    if (r >= n_ranges) break;
-    const int64_t t0 = r * kSelThreads;
-    const int64_t t1 = t0 + kSelThreads < n_tiles ? t0 + kSelThreads : n_tiles;
+  for (int64_t r = blockIdx.x; r < n_ranges; r += gridDim.x) {
+    int64_t part = 0;
+    for (int64_t q = threadIdx.x; q < r; q += kSelThreads) part += range_totals[q];
+    int before;
+    (void)block_exclusive_sum<kSelThreads>(static_cast<int>(part), &before, s_w);
+    __syncthreads();  // s_w is reused
+    const int64_t t0 = r * kGatherSlices;
+    const int64_t t1 = t0 + kGatherSlices < n_tiles ? t0 + kGatherSlices : n_tiles;
     const int nt = static_cast<int>(t1 - t0);
     const int c = threadIdx.x < nt ? static_cast<int>(counts[t0 + threadIdx.x]) : 0;
     int range_total;
     const int excl = block_exclusive_sum<kSelThreads>(c, &range_total, s_w);
     if (threadIdx.x < nt) s_pref[threadIdx.x] = excl;
     if (threadIdx.x == 0) s_pref[nt] = range_total;
-    if (threadIdx.x < 32) {
-      const uint64_t b = lookback_exclusive(range_status, r, static_cast<uint64_t>(range_total), p.status);
-      if (threadIdx.x == 0) s_base = b;
-    }
     __syncthreads();
-    const int64_t base = static_cast<int64_t>(s_base);
+    const int64_t base = before;
     for (int i = threadIdx.x; i < range_total; i += kSelThreads) {
       int lo = 0, hi = nt - 1;  // last slice of the range whose first output is <= i
       while (lo < hi) {
@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid
       if (out_rowids != nullptr) out_rowids[o] = row;
     }
     if (r == n_ranges - 1 && threadIdx.x == 0) p.status->value = base + range_total;
-    __syncthreads();  // s_pref, s_w and s_range are rewritten for the next range
+    __syncthreads();  // s_pref and s_w are rewritten for the next range
   }
 }
 
@@ -1068,15 +1068,19 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     const bool with_pred = spred.n_leaves > 0;
     const int per_sm = select_probe_blocks_per_sm(with_pred, dyn);
     auto rowlist = make_buffer(n * 4, s);
+    const int64_t n_ranges = (n_tiles + kGatherSlices - 1) / kGatherSlices;
+    auto range_totals = make_filled(n_ranges * 4, 0, s);
     {
       const int64_t want = (n_tiles + kPwThreads / 32 - 1) / (kPwThreads / 32);
       const int64_t cap = static_cast<int64_t>(num_sms()) * (per_sm > 0 ? per_sm : 1);
       ProfScope prof("select_probe_kernel", s);
       const int grid = static_cast<int>(want < cap ? want : cap);
       if (with_pred)
-        select_probe_kernel<true><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>());
+        select_probe_kernel<true><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>(),
+                                                                range_totals->as<unsigned int>());
       else
-        select_probe_kernel<false><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>());
+        select_probe_kernel<false><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>(),
+                                                                 range_totals->as<unsigned int>());
       after_launch("select_probe_kernel");
       prof.stop(0);
       // the predicate's columns and the first probe's keys over all rows
@@ -1091,14 +1095,11 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
       prof.set_bytes_model(p.n_dev, n, per_row, &p.status->value, 4.0, scratch, in.rows_owner());
     }
     {
-      // ranges of kSelThreads slices in ticket order, at most four CTAs per SM
-      const int64_t n_ranges = (n_tiles + kSelThreads - 1) / kSelThreads;
-      auto range_scratch = make_filled(64 + n_ranges * 8, 0, s);  // ticket line, then one status word per range
+      // one CTA per range of kGatherSlices slices (grid-stride beyond four per SM)
       const int64_t cap = static_cast<int64_t>(num_sms()) * 4;
       ProfScope prof("select_gather_kernel", s);
-      select_gather_kernel<<<static_cast<int>(n_ranges < cap ? n_ranges : cap), kSelThreads, 0, s>>>(
-          p, rowlist->as<int32_t>(), p.out_rowids, reinterpret_cast<uint64_t*>(range_scratch->as<char>() + 64),
-          range_scratch->as<uint32_t>());
+      select_gather_kernel<<<static_cast<int>(n_ranges < 1 ? 1 : (n_ranges < cap ? n_ranges : cap)), kSelThreads, 0, s>>>(
+          p, rowlist->as<int32_t>(), p.out_rowids, range_totals->as<unsigned int>());
       after_launch("select_gather_kernel");
       prof.stop(0);
       prof.set_bytes_model(nullptr, 0, 0, &p.status->value, 4.0 + proj_read + proj_write, scratch, in.rows_owner());
