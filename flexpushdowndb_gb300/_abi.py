@@ -165,6 +165,12 @@ SIGNATURES = {
         _I32,
         [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A), _I32, _S, _A, ctypes.POINTER(ExecStats), _P],
     ),
+    "gfpdb_plan_prepare": (_I32, [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A),
+                                  ctypes.POINTER(_P)]),
+    "gfpdb_prepared_run": (_I32, [_P, ctypes.POINTER(ExecStats), _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "gfpdb_prepared_layout": (_I32, [_P, _I32, ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.c_char_p, _I64,
+                                     ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "gfpdb_prepared_free": (None, [_P]),
     "gfpdb_plan_validate": (_I32, [ctypes.c_char_p]),
     "gfpdb_graph_cache_clear": (_I32, []),
     "gfpdb_server_create": (_I32, [ctypes.c_char_p, ctypes.POINTER(_P)]),

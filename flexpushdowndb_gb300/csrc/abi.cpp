@@ -284,8 +284,10 @@ TupleSetPtr device_copy(const TupleSet& r, int64_t n, cudaStream_t s) {
 
 // Replay a captured plan. Returns false when a deferred output overflowed
 // (the caller then runs the plan with exact sizes).
-bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowDeviceArray* out, cudaStream_t s,
-                 int64_t* device_ns) {
+// One replay: launch, wait, check every status. Returns false when a
+// deferred output overflowed; else *n_rows is the result's row count (its
+// values in cp.pinned).
+bool replay_graph(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t* n_rows) {
   if (cp.ev[0] == nullptr) {
     GF_CUDA(cudaEventCreate(&cp.ev[0]));
     GF_CUDA(cudaEventCreate(&cp.ev[1]));
@@ -322,8 +324,17 @@ bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowD
   }
   if (!fits) return false;
   const TupleSet& r = *cp.result;
-  int64_t n = cp.count_off >= 0 ? *reinterpret_cast<const int64_t*>(cp.pinned + cp.count_off) : cp.exact_rows;
+  const int64_t n = cp.count_off >= 0 ? *reinterpret_cast<const int64_t*>(cp.pinned + cp.count_off) : cp.exact_rows;
   if (n < 0 || n > r.num_rows()) fail(GFPDB_EDEVICE, "captured plan produced an out-of-range row count");
+  *n_rows = n;
+  return true;
+}
+
+bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowDeviceArray* out, cudaStream_t s,
+                 int64_t* device_ns) {
+  int64_t n = 0;
+  if (!replay_graph(cp, s, device_ns, &n)) return false;
+  const TupleSet& r = *cp.result;
   if (to_host) {
     std::vector<std::vector<const void*>> bufs;
     for (auto& offs : cp.col_off) {
@@ -340,6 +351,31 @@ bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowD
 }
 
 }  // namespace
+
+// A plan bound to its inputs (gfpdb_plan_prepare).
+struct gfpdb_prepared {
+  std::string plan;
+  std::vector<std::string> names;
+  std::vector<const char*> name_ptrs;
+  std::vector<const ArrowSchema*> schemas;
+  std::vector<const ArrowDeviceArray*> arrays;
+  bool graph = false;
+  std::string key;                                // the captured-plan cache key
+  std::shared_ptr<CapturedPlan> cp;               // once captured
+  ArrowSchema res_s{};                            // the last non-replay run's exported result
+  ArrowDeviceArray res_a{};
+  bool has_res = false;
+  bool last_replay = false;
+  int64_t generation = 0;
+
+  void release_result() {
+    if (!has_res) return;
+    if (res_a.array.release) res_a.array.release(&res_a.array);
+    if (res_s.release) res_s.release(&res_s);
+    has_res = false;
+  }
+  ~gfpdb_prepared() { release_result(); }
+};
 
 extern "C" {
 
@@ -933,6 +969,134 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
     }
   });
 }
+
+int32_t gfpdb_plan_prepare(const char* plan_json, int32_t n_tables, const char* const* table_names,
+                           const ArrowSchema* const* schemas, const ArrowDeviceArray* const* arrays,
+                           gfpdb_prepared** out) {
+  return guarded([&] {
+    require(plan_json != nullptr && out != nullptr && n_tables >= 0, "null argument");
+    require(n_tables == 0 || (table_names != nullptr && schemas != nullptr && arrays != nullptr), "null tables");
+    json::Value plan;
+    try {
+      plan = json::parse(plan_json);
+    } catch (const std::exception& e) {
+      fail(GFPDB_EINVAL, e.what());
+    }
+    pop::validate_plan(plan);
+    ensure_device();
+    auto p = std::make_unique<gfpdb_prepared>();
+    p->plan = plan_json;
+    for (int32_t i = 0; i < n_tables; ++i) {
+      require(table_names[i] != nullptr && schemas[i] != nullptr && arrays[i] != nullptr, "null table");
+      p->names.push_back(table_names[i]);
+      p->schemas.push_back(schemas[i]);
+      p->arrays.push_back(arrays[i]);
+    }
+    for (auto& n : p->names) p->name_ptrs.push_back(n.c_str());
+    p->graph = plan.get_bool("cudaGraph", false) && plan.get_bool("deferredSizes", true);
+    if (p->graph) p->key = plan_key(plan_json, n_tables, table_names, arrays);
+    *out = p.release();
+  });
+}
+
+int32_t gfpdb_prepared_run(gfpdb_prepared* p, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows,
+                           int64_t* layout_generation) {
+  return guarded([&] {
+    require(p != nullptr && n_rows != nullptr && layout_generation != nullptr, "null argument");
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = as_stream(stream);
+    auto find_capture = [&] {
+      if (!p->graph || p->cp) return;
+      std::lock_guard<std::mutex> lk(g_graph_mu);
+      auto it = g_graphs.find(p->key);
+      if (it != g_graphs.end()) p->cp = it->second;
+    };
+    find_capture();
+    if (p->cp && p->cp->capturable) {
+      const CopyCounters c0 = copy_counters();
+      const uint64_t launches0 = g_kernel_launches.load();
+      int64_t device_ns = 0, n = 0;
+      if (replay_graph(*p->cp, s, &device_ns, &n)) {
+        p->release_result();
+        if (!p->last_replay) {
+          ++p->generation;
+          p->last_replay = true;
+        }
+        *n_rows = n;
+        *layout_generation = p->generation;
+        if (stats != nullptr) {
+          stats->kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
+          stats->h2d_bytes = copy_counters().h2d - c0.h2d;
+          stats->d2h_bytes = copy_counters().d2h - c0.d2h;
+          stats->num_ops = p->cp->num_ops;
+          stats->messages = p->cp->messages;
+          stats->device_ns = device_ns;
+          stats->elapsed_ns =
+              std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+        }
+        return;
+      }
+    }
+    // the first runs (an ordinary run, then the capture), plans without a
+    // graph, and a replay that overflowed (re-run with exact sizes)
+    p->release_result();
+    const int32_t code = gfpdb_execute_plan(p->plan.c_str(), static_cast<int32_t>(p->names.size()),
+                                            p->name_ptrs.data(), p->schemas.data(), p->arrays.data(), 1, &p->res_s,
+                                            &p->res_a, stats, stream);
+    if (code != GFPDB_OK) fail(code, std::string(gfpdb_last_error()));
+    p->has_res = true;
+    p->last_replay = false;
+    ++p->generation;
+    *n_rows = p->res_a.array.length;
+    *layout_generation = p->generation;
+    find_capture();
+  });
+}
+
+int32_t gfpdb_prepared_layout(const gfpdb_prepared* p, int32_t max_columns, int64_t* capacity, int32_t* n_columns,
+                              char* names, int64_t names_capacity, const void** values, const void** offsets) {
+  return guarded([&] {
+    require(p != nullptr && capacity != nullptr && n_columns != nullptr && names != nullptr && values != nullptr &&
+                offsets != nullptr,
+            "null argument");
+    int64_t at = 0;
+    auto put = [&](const char* str) {
+      const int64_t len = static_cast<int64_t>(std::strlen(str)) + 1;
+      require(at + len <= names_capacity, "column names exceed names_capacity");
+      std::memcpy(names + at, str, static_cast<size_t>(len));
+      at += len;
+    };
+    if (p->last_replay) {
+      const CapturedPlan& cp = *p->cp;
+      const TupleSet& r = *cp.result;
+      require(r.num_columns() <= max_columns, "more columns than max_columns");
+      *capacity = r.num_rows();
+      *n_columns = r.num_columns();
+      for (int i = 0; i < r.num_columns(); ++i) {
+        put(r.field(i).name.c_str());
+        put(dtype_format(r.field(i).type));
+        const auto& offs = cp.col_off[static_cast<size_t>(i)];
+        if (r.field(i).type == DType::Utf8) {
+          offsets[i] = cp.pinned + offs[0];
+          values[i] = cp.pinned + offs[1];
+        } else {
+          values[i] = cp.pinned + offs[0];
+          offsets[i] = nullptr;
+        }
+      }
+      return;
+    }
+    require(p->has_res, "the prepared plan has not run");
+    int64_t n = 0;
+    int32_t device_type = 0;
+    const int32_t code = gfpdb_result_layout(&p->res_s, &p->res_a, max_columns, &n, n_columns, &device_type, names,
+                                             names_capacity, values, offsets);
+    if (code != GFPDB_OK) fail(code, std::string(gfpdb_last_error()));
+    *capacity = n;
+  });
+}
+
+void gfpdb_prepared_free(gfpdb_prepared* p) { delete p; }
 
 int32_t gfpdb_plan_validate(const char* plan_json) {
   return guarded([&] {

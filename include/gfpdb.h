@@ -310,6 +310,29 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
                            struct ArrowSchema* out_schema, struct ArrowDeviceArray* out,
                            gfpdb_exec_stats* stats, void* stream);
 
+/* Prepared plans: a plan bound once to its input tables (which the caller
+ * keeps alive and unchanged), for callers that run one query many times
+ * (a prepared statement). A run leaves its result in host memory owned by
+ * the prepared plan, readable until the next run: gfpdb_prepared_layout
+ * describes it (as gfpdb_result_layout does) and its pointers stay valid for
+ * every later run that reports the same layout generation. With
+ * "cudaGraph" a run after the first two is one graph replay, without the
+ * per-call plan lookup and result export of gfpdb_execute_plan. */
+typedef struct gfpdb_prepared gfpdb_prepared;
+int32_t gfpdb_plan_prepare(const char* plan_json, int32_t n_tables, const char* const* table_names,
+                           const struct ArrowSchema* const* schemas,
+                           const struct ArrowDeviceArray* const* arrays, gfpdb_prepared** out);
+int32_t gfpdb_prepared_run(gfpdb_prepared* plan, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows,
+                           int64_t* layout_generation);
+/* As gfpdb_result_layout for the last run's result, plus its row capacity
+ * (the length the buffers can hold: the most rows any run with this layout
+ * generation can return). */
+int32_t gfpdb_prepared_layout(const gfpdb_prepared* plan, int32_t max_columns, int64_t* capacity,
+                              int32_t* n_columns, char* names, int64_t names_capacity, const void** values,
+                              const void** offsets);
+void gfpdb_prepared_free(gfpdb_prepared* plan);
+
+
 /* Parse and check a plan without running it (host only, no CUDA calls). */
 int32_t gfpdb_plan_validate(const char* plan_json);
 
