@@ -108,37 +108,42 @@ __device__ __forceinline__ void load_chunk(const uint8_t* text, int64_t n, int64
   }
 }
 
-// Bit i set when byte i of the chunk is a separator (delimiter or newline).
-__device__ __forceinline__ uint64_t separator_mask(const uint32_t w[16], uint8_t delim, uint64_t* nl_mask) {
-  uint64_t m = 0, nl = 0;
+// 0x80 in every byte of x that is zero, 0 elsewhere (exact: no carry
+// crosses a byte, since (b & 0x7F) + 0x7F <= 0xFE).
+__device__ __forceinline__ uint32_t zero_byte_bits(uint32_t x) {
+  return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
+}
+
+// Bits 7, 15, 23, 31 of z to bits 0..3 (the four products land on distinct
+// bit positions, so nothing carries into bits 21..24).
+__device__ __forceinline__ uint32_t high_bits_to_nibble(uint32_t z) {
+  return (((z >> 7) * 0x00204081u) >> 21) & 0xFu;
+}
+
+// Bit i set when byte i of the chunk is a separator (delimiter or newline),
+// four bytes at a time.
+__device__ __forceinline__ uint64_t separator_bits(const uint32_t w[16], uint8_t delim) {
+  const uint32_t dpat = static_cast<uint32_t>(delim) * 0x01010101u;
+  uint64_t m = 0;
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const uint32_t c = (w[k] >> (8 * b)) & 0xFFu;
-      const uint64_t bit = uint64_t{1} << (4 * k + b);
-      if (c == delim) m |= bit;
-      if (c == '\n') {
-        m |= bit;
-        nl |= bit;
-      }
-    }
+    const uint32_t z = zero_byte_bits(w[k] ^ dpat) | zero_byte_bits(w[k] ^ 0x0A0A0A0Au);
+    m |= static_cast<uint64_t>(high_bits_to_nibble(z)) << (4 * k);
   }
-  *nl_mask = nl;
   return m;
 }
 
 // (1) per tile: separators, and the position of the last one (-1: none)
 __global__ void __launch_bounds__(kCsvThreads)
     csv_index_kernel(const uint8_t* __restrict__ text, int64_t n, uint8_t delim, int64_t* __restrict__ tile_count,
-                     int64_t* __restrict__ tile_last) {
+                     int64_t* __restrict__ tile_last, uint64_t* __restrict__ chunk_masks) {
   __shared__ int64_t s_w[2 * (kCsvThreads / 32) + 2];
   const int64_t at = static_cast<int64_t>(blockIdx.x) * kCsvTile + static_cast<int64_t>(threadIdx.x) * kCsvChunk;
   uint32_t w[16];
   load_chunk(text, n, at, w);
-  uint64_t nl;
-  uint64_t m = separator_mask(w, delim, &nl);
-  if (at + kCsvChunk > n) m &= n > at ? (~uint64_t{0} >> (64 - (n - at))) : 0;  // bytes past the end are zero anyway
+  uint64_t m = separator_bits(w, delim);
+  if (at + kCsvChunk > n) m &= n > at ? (~uint64_t{0} >> (64 - (n - at))) : 0;  // bytes past the end
+  chunk_masks[at / kCsvChunk] = m;  // one entry per chunk of every tile: kept for csv_fields_kernel
   const int64_t cnt = __popcll(m);
   const int64_t last = m ? at + 63 - __clzll(static_cast<long long>(m)) : -1;
   int64_t total_cnt, max_last;
@@ -204,6 +209,7 @@ struct CsvParams {
   int64_t n;                   // text bytes
   const int64_t* tile_base;    // first separator ordinal of each tile
   const int64_t* tile_prev;    // position of the separator before each tile (-1: none)
+  const uint64_t* chunk_masks; // separator bits of every 64-byte chunk (csv_index_kernel)
   int64_t n_rows;              // data rows (after the header)
   int32_t n_fields;
   int32_t header;              // 1: the first row is skipped
@@ -346,13 +352,9 @@ __global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_co
   const int64_t at = tile0 + static_cast<int64_t>(threadIdx.x) * kCsvChunk;
   uint32_t w[16];
   load_chunk(p.text, p.n, at, w);
-  uint64_t nl;
-  uint64_t m = separator_mask(w, p.delim, &nl);
-  if (at + kCsvChunk > p.n) {
-    const uint64_t valid = p.n > at ? (~uint64_t{0} >> (64 - (p.n - at))) : 0;
-    m &= valid;
-    nl &= valid;
-  }
+  // the separators found by csv_index_kernel (bytes past the end excluded); a
+  // separator is a newline when its byte is one
+  uint64_t m = p.chunk_masks[at / kCsvChunk];
   // the implied newline after an unterminated last line belongs to the chunk
   // holding the last byte
   const bool has_end = p.virtual_end && p.n > at && p.n <= at + kCsvChunk;
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_co
         const int bit = __ffsll(static_cast<long long>(m)) - 1;
         m &= m - 1;
         pos = at + bit;
-        is_nl = (nl >> bit) & 1u;
+        is_nl = p.text[pos] == '\n';
       } else {  // the implied newline
         pos = p.n;
         is_nl = true;
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_co
         const int bit = __ffsll(static_cast<long long>(m)) - 1;
         m &= m - 1;
         rel = static_cast<int32_t>(at - tile0) + bit;
-        is_nl = (nl >> bit) & 1u;
+        is_nl = reinterpret_cast<const uint8_t*>(s_text)[rel] == '\n';  // this thread staged that byte
       } else {
         rel = static_cast<int32_t>(p.n - tile0);
         is_nl = true;
@@ -549,6 +551,7 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   // (1)-(2): separators per tile, their scans, the total
   const int64_t n_tiles = n_bytes > 0 ? (n_bytes + kCsvTile - 1) / kCsvTile : 0;
   auto tiles = make_buffer(std::max<int64_t>(n_tiles, 1) * 16 + 16, s);
+  auto masks = make_buffer(std::max<int64_t>(n_tiles, 1) * kCsvThreads * 8, s);  // one word per chunk of every tile
   int64_t* tile_count = tiles->as<int64_t>();
   int64_t* tile_last = tile_count + std::max<int64_t>(n_tiles, 1);
   int64_t* tot = tile_last + std::max<int64_t>(n_tiles, 1);
@@ -558,7 +561,7 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
     {
       ProfScope prof("csv_index_kernel", s);
       csv_index_kernel<<<static_cast<int>(n_tiles), kCsvThreads, 0, s>>>(text, n_bytes, static_cast<uint8_t>(delimiter),
-                                                                        tile_count, tile_last);
+                                                                        tile_count, tile_last, masks->as<uint64_t>());
       after_launch("csv_index_kernel");
       prof.stop(static_cast<double>(n_bytes));
     }
@@ -586,6 +589,7 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
   p.n = n_bytes;
   p.tile_base = tile_count;
   p.tile_prev = tile_last;
+  p.chunk_masks = masks->as<uint64_t>();
   p.n_rows = n_rows;
   p.n_fields = F;
   p.header = static_cast<int32_t>(skip);
