@@ -433,8 +433,19 @@ __global__ void __launch_bounds__(kCsvThreads) csv_fields_kernel(const __grid_co
   const int R = static_cast<int>((g_end - 1) / F - row0 + 1);
   const int items = F * R;
   const uint8_t* st = reinterpret_cast<const uint8_t*>(s_text);
+  // item i is field i / R of row i % R; advanced per step of kCsvThreads
+  // instead of divided per item
+  const int dc = kCsvThreads / R, dr = kCsvThreads - dc * R;
+  int c_next = static_cast<int>(threadIdx.x) / R;
+  int r_next = static_cast<int>(threadIdx.x) - c_next * R;
   for (int i = threadIdx.x; i < items; i += kCsvThreads) {
-    const int c = i / R, r = i - c * R;
+    const int c = c_next, r = r_next;
+    r_next += dr;
+    c_next += dc;
+    if (r_next >= R) {
+      r_next -= R;
+      ++c_next;
+    }
     const int64_t g = (row0 + r) * F + c;
     if (g < g0 || g >= g_end) continue;
     const int32_t pe = s_pos[c * RS + r];
@@ -624,35 +635,55 @@ TupleSetPtr csv_parse(const char* device_text, int64_t n_bytes, char delimiter, 
     for (auto& f : out_fields) out_w += f.type == DType::Utf8 ? 12 : dtype_width(f.type);
     prof.stop(static_cast<double>(n_bytes) + static_cast<double>(n_rows) * out_w);
   }
-  DevStatus hs;
-  GF_CUDA(cudaMemcpyAsync(&hs, status->data(), sizeof(hs), cudaMemcpyDeviceToHost, s));
-  sync(s);
-  if (hs.code == GFPDB_EINVAL)
-    fail(GFPDB_EINVAL, "malformed CSV field or wrong field count near data row " + std::to_string(hs.detail));
-  raise_device_status(hs, "CSV parse");
-
-  // (5) utf8 bytes
-  std::vector<ColumnPtr> cols;
-  for (size_t k = 0; k < emit.size(); ++k) {
-    if (out_fields[k].type != DType::Utf8) {
-      cols.push_back(make_fixed_column(out_fields[k].type, n_rows, bufs[k]));
-      continue;
+  // (5) utf8 bytes: every utf8 column's length prefix sum, then one
+  // synchronization for the parse status and all their totals (the parse
+  // status first: a malformed text reports as such), then the byte copies
+  std::vector<size_t> utf8;
+  for (size_t k = 0; k < emit.size(); ++k)
+    if (out_fields[k].type == DType::Utf8) utf8.push_back(k);
+  std::vector<BufferPtr> offs(emit.size()), bytes(emit.size());
+  std::vector<int64_t> totals(utf8.size(), 0);
+  {
+    auto sts = make_filled(static_cast<int64_t>(utf8.size() * sizeof(DevStatus)) + 64, 0, s);
+    DevStatus* st = sts->as<DevStatus>();
+    for (size_t u = 0; u < utf8.size(); ++u) {
+      const size_t k = utf8[u];
+      offs[k] = make_buffer((n_rows + 1) * 4, s);
+      exclusive_scan_i32_async(bufs[k]->as<int32_t>(), offs[k]->as<int32_t>(), n_rows, st + u, s);
     }
-    auto offs = make_buffer((n_rows + 1) * 4, s);
-    const int64_t total = exclusive_scan_i32(bufs[k]->as<int32_t>(), offs->as<int32_t>(), n_rows, s);
-    auto bytes = make_buffer(total, s);
+    std::vector<DevStatus> hs(utf8.size() + 1);
+    GF_CUDA(cudaMemcpyAsync(hs.data(), status->data(), sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    if (!utf8.empty())
+      GF_CUDA(cudaMemcpyAsync(hs.data() + 1, st, utf8.size() * sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    sync(s);
+    if (hs[0].code == GFPDB_EINVAL)
+      fail(GFPDB_EINVAL, "malformed CSV field or wrong field count near data row " + std::to_string(hs[0].detail));
+    raise_device_status(hs[0], "CSV parse");
+    for (size_t u = 0; u < utf8.size(); ++u) {
+      raise_device_status(hs[u + 1], "prefix sum");
+      if (hs[u + 1].value > INT32_MAX) fail(GFPDB_EUNSUPPORTED, "utf8 column exceeds 2 GiB of bytes");
+      totals[u] = hs[u + 1].value;
+    }
+  }
+  for (size_t u = 0; u < utf8.size(); ++u) {
+    const size_t k = utf8[u];
+    const int64_t total = totals[u];
+    bytes[k] = make_buffer(total, s);
     if (n_rows > 0 && total > 0) {
       const int64_t groups = (n_rows + 31) / 32;
       int64_t blocks = (groups + kCopyThreads / 32 - 1) / (kCopyThreads / 32);
       int64_t cap = static_cast<int64_t>(num_sms()) * 16;
       ProfScope prof("csv_copy_strings_kernel", s);
       csv_copy_strings_kernel<<<static_cast<int>(blocks < cap ? blocks : cap), kCopyThreads, 0, s>>>(
-          text, sstart[k]->as<int64_t>(), offs->as<int32_t>(), bytes->as<uint8_t>(), n_rows);
+          text, sstart[k]->as<int64_t>(), offs[k]->as<int32_t>(), bytes[k]->as<uint8_t>(), n_rows);
       after_launch("csv_copy_strings_kernel");
       prof.stop(2.0 * static_cast<double>(total) + 12.0 * static_cast<double>(n_rows));
     }
-    cols.push_back(make_utf8_column(n_rows, offs, bytes));
   }
+  std::vector<ColumnPtr> cols;
+  for (size_t k = 0; k < emit.size(); ++k)
+    cols.push_back(out_fields[k].type == DType::Utf8 ? make_utf8_column(n_rows, offs[k], bytes[k])
+                                                     : make_fixed_column(out_fields[k].type, n_rows, bufs[k]));
   return TupleSet::make(std::move(out_fields), std::move(cols), n_rows);
 }
 

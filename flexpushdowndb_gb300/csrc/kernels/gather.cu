@@ -248,6 +248,20 @@ void fill_regions(const FillSpan* spans, int n, cudaStream_t s, int max_blocks) 
   after_launch("fill_regions_kernel");
 }
 
+void exclusive_scan_i32_async(const int32_t* in, int32_t* out, int64_t n, DevStatus* st, cudaStream_t s) {
+  if (n == 0) {
+    GF_CUDA(cudaMemsetAsync(out, 0, 4, s));
+    return;
+  }
+  const int64_t n_tiles = (n + kScanTile - 1) / kScanTile;
+  auto scratch = make_filled(64 + n_tiles * 8, 0, s);  // ticket line, then the tile words
+  uint32_t* ticket = scratch->as<uint32_t>();
+  uint64_t* tiles = reinterpret_cast<uint64_t*>(scratch->as<char>() + 64);
+  int grid = static_cast<int>(n_tiles < num_sms() * 4 ? n_tiles : num_sms() * 4);
+  scan_i32_kernel<<<grid, kScanThreads, 0, s>>>(in, out, n, n_tiles, tiles, ticket, st);
+  after_launch("scan_i32_kernel");
+}  // scratch is freed stream-ordered, after the scan
+
 int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
   if (n == 0) {
     GF_CUDA(cudaMemsetAsync(out, 0, 4, s));

@@ -57,6 +57,10 @@ void copy_h2d(void* dst, const void* src, int64_t bytes, cudaStream_t s);
 // Exclusive prefix sum of n int32 values into n+1 int32 offsets (offsets[n] =
 // total). Returns the total (synchronizes the stream).
 int64_t exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
+// The same without waiting: the total lands in st->value (st zeroed by the
+// caller; a device error in st->code), so that several scans can share one
+// synchronization.
+void exclusive_scan_i32_async(const int32_t* in, int32_t* out, int64_t n, DevStatus* st, cudaStream_t s);
 
 // ------------------------------------------------------------- bloom.cu
 
