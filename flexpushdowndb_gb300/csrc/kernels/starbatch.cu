@@ -372,7 +372,9 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
     // last rows of a partition, global memory)
     auto fk_of = [&](int d, int i) -> int64_t {
       const int64_t r = r0 + i * 32;
-      const int64_t in_smem = sb_seg_bytes(p, d, t.rows) / p.fk_width[d];
+      // rows of the segment in the stage (widths are 4 or 8: a shift, not a
+      // 64-bit division per key)
+      const int64_t in_smem = static_cast<int64_t>(sb_seg_bytes(p, d, t.rows)) >> (p.fk_width[d] == 8 ? 3 : 2);
       const unsigned char* seg = stage + p.seg_off[d];
       if (r < in_smem)
         return p.fk_width[d] == 8 ? reinterpret_cast<const int64_t*>(seg)[r]
