@@ -590,6 +590,11 @@ def _operator_case(args):
         j.put_build(DeviceTable.from_host(build))
         j.finalize_build()
         fn = lambda: j.probe(probe)  # noqa: E731
+        for _ in range(max(2, args.warmup)):
+            fn()
+        ms = _kernel_ms(fn, ("join_probe_kernel", "join_probe_emit_kernel"), args.steps)
+        print(json.dumps({"case": "join", "rows": n, "build_rows": nb, "probe_kernel_ms": ms,
+                          "probes_per_s": n / (ms * 1e-3)}))
     elif args.case == "group":
         t = DeviceTable.from_host(workloads.groupby_table(n, max(1, n // 2)))
         aggs = [ops.aggregate("SUM", "s", col("v")), ops.aggregate("COUNT", "c")]
