@@ -11,9 +11,11 @@
 // decides a match from the slot alone; for 64-bit keys the tag is the high
 // half of the hash and a tag hit is confirmed against the build key column.
 // Duplicate build keys occupy separate slots (multimap semantics). Probing
-// is one thread per probe row walking its run; matches leave through a
-// warp-aggregated atomic cursor as (probe row, build row) pairs that a
-// gather turns into output columns.
+// is one thread per probe row walking its run. Matches collect per warp in
+// shared memory and leave in runs of up to kStage pairs, each run taking its
+// output positions with one atomic on the shared cursor: the cursor is a
+// single address whose atomics the L2 serialises, so one atomic per warp
+// step held a 20M-row probe to the rate of that one address.
 #include "common.cuh"
 #include "launch.h"
 
@@ -60,65 +62,126 @@ __global__ void __launch_bounds__(256)
   if (dup) st->aux[1] = 1;
 }
 
+// Per-warp staging of matches: (probe row, build row) pairs in shared
+// memory, flushed to the output when one more step could overflow the stage
+// and once at the end.
+constexpr int kProbeWarps = 8;   // 256-thread CTAs
+constexpr int kRowsPerLane = 4;  // probe rows a lane walks side by side
+constexpr int kStage = 512;      // staged pairs per warp
+constexpr int64_t kProbeTile = 32 * kRowsPerLane;
+
+struct PairStage {
+  int32_t* p;
+  int32_t* b;
+  int n;  // staged pairs; the same in every lane
+};
+
+__device__ __forceinline__ void stage_pairs(PairStage& sg, bool emit, int lane, int32_t prow, int32_t brow) {
+  const uint32_t em = __ballot_sync(0xffffffffu, emit);
+  if (emit) {
+    const int at = sg.n + __popc(em & ((1u << lane) - 1u));
+    sg.p[at] = prow;
+    sg.b[at] = brow;
+  }
+  sg.n += __popc(em);
+}
+
+// Claims sg.n output positions with one atomic and hands the stage to
+// write(first position, stage, lane).
+template <class Write>
+__device__ __forceinline__ void flush_pairs(PairStage& sg, unsigned long long* cursor, int lane, Write& write) {
+  __syncwarp();
+  unsigned long long at = 0;
+  if (lane == 0) at = atomicAdd(cursor, static_cast<unsigned long long>(sg.n));
+  at = __shfl_sync(0xffffffffu, at, 0);
+  write(static_cast<int64_t>(at), sg, lane);
+  __syncwarp();
+  sg.n = 0;
+}
+
+// The probe loop shared by the pair and the materialising probe. A warp
+// takes tiles of kProbeTile probe rows; each lane walks kRowsPerLane of them
+// (rows lane, lane + 32, ...) side by side, so that its key loads and then
+// each step's slot loads are independent requests in flight together rather
+// than one dependent round trip per row.
+template <class Write>
+__device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const uint64_t* __restrict__ slots,
+                                           uint64_t mask, const DevCol& bkey, int key32, unsigned long long* cursor,
+                                           Write& write) {
+  __shared__ int32_t s_p[kProbeWarps][kStage], s_b[kProbeWarps][kStage];
+  const int lane = threadIdx.x & 31;
+  PairStage sg{s_p[threadIdx.x >> 5], s_b[threadIdx.x >> 5], 0};
+  const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t base = warp_global * kProbeTile; base < n; base += n_warps * kProbeTile) {
+    int64_t k[kRowsPerLane];
+    uint32_t tag[kRowsPerLane];
+    uint64_t slot[kRowsPerLane];
+    unsigned act = 0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerLane; ++j) {
+      const int64_t r = base + j * 32 + lane;
+      k[j] = 0;
+      if (r < n) {
+        k[j] = load_int(pkey, r);
+        act |= 1u << j;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kRowsPerLane; ++j) {
+      const uint64_t h = hash_key(k[j]);
+      tag[j] = key32 ? static_cast<uint32_t>(k[j]) : static_cast<uint32_t>(h >> 32);
+      slot[j] = h & mask;
+    }
+    // A row leaves at an empty slot, or after it has seen every slot.
+    for (uint64_t steps = 1; __any_sync(0xffffffffu, act != 0); ++steps) {
+      uint64_t sv[kRowsPerLane];
+#pragma unroll
+      for (int j = 0; j < kRowsPerLane; ++j)
+        sv[j] = (act >> j & 1u) ? __ldg(reinterpret_cast<const unsigned long long*>(slots + slot[j]))
+                                : static_cast<unsigned long long>(kEmptySlot);
+#pragma unroll
+      for (int j = 0; j < kRowsPerLane; ++j) {
+        bool emit = false;
+        int32_t brow = 0;
+        if (act >> j & 1u) {
+          if (sv[j] == kEmptySlot || steps > mask + 1) {
+            act &= ~(1u << j);
+          } else {
+            if (static_cast<uint32_t>(sv[j] >> 32) == tag[j]) {
+              brow = static_cast<int32_t>(static_cast<uint32_t>(sv[j]));
+              emit = key32 ? true : (load_int(bkey, brow) == k[j]);
+            }
+            slot[j] = (slot[j] + 1) & mask;
+          }
+        }
+        stage_pairs(sg, emit, lane, static_cast<int32_t>(base + j * 32 + lane), brow);
+      }
+      if (sg.n > kStage - 32 * kRowsPerLane) flush_pairs(sg, cursor, lane, write);
+    }
+  }
+  if (sg.n > 0) flush_pairs(sg, cursor, lane, write);
+}
+
 __global__ void __launch_bounds__(256)
     join_probe_kernel(DevCol pkey, int64_t n_cap, const int64_t* n_dev, const uint64_t* __restrict__ slots,
                       uint64_t mask, DevCol bkey, int key32, int32_t* __restrict__ out_p,
                       int32_t* __restrict__ out_b, int64_t cap, DevStatus* st) {
   const int64_t n = clamp_rows(n_dev, n_cap);
-  const int lane = threadIdx.x & 31;
-  const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(&st->value);
-  for (int64_t base = warp_global * 32; base < n; base += n_warps * 32) {
-    const int64_t r = base + lane;
-    bool active = r < n;
-    int64_t k = 0;
-    uint32_t tag = 0;
-    uint64_t slot = 0;
-    if (active) {
-      k = load_int(pkey, r);
-      const uint64_t h = hash_key(k);
-      tag = key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
-      slot = h & mask;
-    }
-    uint64_t steps = 0;
-    while (__any_sync(0xffffffffu, active)) {
-      bool emit = false;
-      int32_t brow = 0;
-      if (active) {
-        const uint64_t s = __ldg(reinterpret_cast<const unsigned long long*>(slots + slot));
-        if (s == kEmptySlot || ++steps > mask + 1) {
-          active = false;
-        } else {
-          if (static_cast<uint32_t>(s >> 32) == tag) {
-            brow = static_cast<int32_t>(static_cast<uint32_t>(s));
-            emit = key32 ? true : (load_int(bkey, brow) == k);
-          }
-          slot = (slot + 1) & mask;
-        }
+  auto write = [&](int64_t at, const PairStage& sg, int lane) {
+    for (int i = lane; i < sg.n; i += 32)
+      if (at + i < cap) {
+        out_p[at + i] = sg.p[i];
+        out_b[at + i] = sg.b[i];
       }
-      const uint32_t em = __ballot_sync(0xffffffffu, emit);
-      if (em != 0) {
-        unsigned long long at = 0;
-        const int leader = __ffs(em) - 1;
-        if (lane == leader) at = atomicAdd(cursor, static_cast<unsigned long long>(__popc(em)));
-        at = __shfl_sync(0xffffffffu, at, leader);
-        if (emit) {
-          const int64_t pos = static_cast<int64_t>(at) + __popc(em & ((1u << lane) - 1u));
-          if (pos < cap) {
-            out_p[pos] = static_cast<int32_t>(r);
-            out_b[pos] = brow;
-          }
-        }
-      }
-    }
-  }
+  };
+  probe_rows(pkey, n, slots, mask, bkey, key32, reinterpret_cast<unsigned long long*>(&st->value), write);
 }
 
-// Probe and materialise in one pass: every match writes its output row
-// directly (probe columns from the probe row, build columns from the build
-// row) at a position claimed with one warp-aggregated atomic, so no pair
-// buffer and no separate gather launch are needed. Fixed-width columns only.
+// Probe and materialise in one pass: every staged match becomes an output
+// row (probe columns from the probe row, build columns from the build row)
+// at the positions its flush claimed, so no pair buffer and no separate
+// gather launch are needed. Fixed-width columns only.
 constexpr int kJoinOutMax = 24;
 
 struct JoinEmitParams {
@@ -138,61 +201,39 @@ struct JoinEmitParams {
   int32_t from_build[kJoinOutMax];
 };
 
-__global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_constant__ JoinEmitParams p) {
-  const int64_t n = clamp_rows(p.n_dev, p.n_cap);
-  const int lane = threadIdx.x & 31;
-  const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(&p.st->value);
-  for (int64_t base = warp_global * 32; base < n; base += n_warps * 32) {
-    const int64_t r = base + lane;
-    bool active = r < n;
-    int64_t k = 0;
-    uint32_t tag = 0;
-    uint64_t slot = 0;
-    if (active) {
-      k = load_int(p.pkey, r);
-      const uint64_t h = hash_key(k);
-      tag = p.key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
-      slot = h & p.mask;
+// One column of a flush: eight gathers in flight per lane, then the stores.
+template <class T>
+__device__ __forceinline__ void copy_staged(const T* __restrict__ src, T* __restrict__ dst, const int32_t* idx,
+                                            int n, int64_t at, int64_t cap, int lane) {
+  constexpr int kU = 8;
+  for (int i0 = 0; i0 < n; i0 += 32 * kU) {
+    T v[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = i0 + u * 32 + lane;
+      if (i < n) v[u] = __ldg(src + idx[i]);
     }
-    uint64_t steps = 0;
-    while (__any_sync(0xffffffffu, active)) {
-      bool emit = false;
-      int32_t brow = 0;
-      if (active) {
-        const uint64_t s = __ldg(reinterpret_cast<const unsigned long long*>(p.slots + slot));
-        if (s == kEmptySlot || ++steps > p.mask + 1) {
-          active = false;
-        } else {
-          if (static_cast<uint32_t>(s >> 32) == tag) {
-            brow = static_cast<int32_t>(static_cast<uint32_t>(s));
-            emit = p.key32 ? true : (load_int(p.bkey, brow) == k);
-          }
-          slot = (slot + 1) & p.mask;
-        }
-      }
-      const uint32_t em = __ballot_sync(0xffffffffu, emit);
-      if (em != 0) {
-        unsigned long long at = 0;
-        const int leader = __ffs(em) - 1;
-        if (lane == leader) at = atomicAdd(cursor, static_cast<unsigned long long>(__popc(em)));
-        at = __shfl_sync(0xffffffffu, at, leader);
-        if (emit) {
-          const int64_t pos = static_cast<int64_t>(at) + __popc(em & ((1u << lane) - 1u));
-          if (pos < p.cap) {
-            for (int c = 0; c < p.n_out; ++c) {
-              const int64_t from = p.from_build[c] ? brow : r;
-              if (p.width[c] == 8)
-                static_cast<long long*>(p.dst[c])[pos] = __ldg(static_cast<const long long*>(p.src[c]) + from);
-              else
-                static_cast<int*>(p.dst[c])[pos] = __ldg(static_cast<const int*>(p.src[c]) + from);
-            }
-          }
-        }
-      }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = i0 + u * 32 + lane;
+      if (i < n && at + i < cap) dst[at + i] = v[u];
     }
   }
+}
+
+__global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_constant__ JoinEmitParams p) {
+  const int64_t n = clamp_rows(p.n_dev, p.n_cap);
+  auto write = [&](int64_t at, const PairStage& sg, int lane) {
+    for (int c = 0; c < p.n_out; ++c) {
+      const int32_t* idx = p.from_build[c] ? sg.b : sg.p;
+      if (p.width[c] == 8)
+        copy_staged(static_cast<const long long*>(p.src[c]), static_cast<long long*>(p.dst[c]), idx, sg.n, at, p.cap,
+                    lane);
+      else
+        copy_staged(static_cast<const int*>(p.src[c]), static_cast<int*>(p.dst[c]), idx, sg.n, at, p.cap, lane);
+    }
+  };
+  probe_rows(p.pkey, n, p.slots, p.mask, p.bkey, p.key32, reinterpret_cast<unsigned long long*>(&p.st->value), write);
 }
 
 // A chain of joins in one pass. Each lane walks its input row through the
@@ -301,14 +342,26 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
   }
 }
 
-// Grid-stride launches: four CTAs per SM keep the atomics and probes busy,
-// and a launch sized for a large row capacity of which few rows arrive
+// Grid-stride launches: four CTAs per SM keep the build's atomics busy, and
+// a launch sized for a large row capacity of which few rows arrive
 // (deferred inputs) dispatches fewer empty CTAs.
-int grid_for(int64_t n) {
-  int64_t blocks = (n + 255) / 256;
-  int64_t cap = static_cast<int64_t>(num_sms()) * 4;
+int grid_for(int64_t n, int per_sm = 4, int64_t rows_per_block = 256) {
+  int64_t blocks = (n + rows_per_block - 1) / rows_per_block;
+  int64_t cap = static_cast<int64_t>(num_sms()) * per_sm;
   if (blocks > cap) blocks = cap;
   return static_cast<int>(blocks < 1 ? 1 : blocks);
+}
+
+// The probes' warps wait on table loads, so their grids fill every SM with
+// as many CTAs as fit at once (one wave, no tail).
+template <class Kernel>
+int probe_grid(Kernel kernel, int64_t n) {
+  static const int per_sm = [kernel] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0) != cudaSuccess || b < 1) b = 4;
+    return b;
+  }();
+  return grid_for(n, per_sm, kProbeWarps * kProbeTile);
 }
 
 }  // namespace
@@ -389,7 +442,7 @@ std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet
     if (attempt > 0) GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
     if (n > 0 && t.build->num_rows() > 0) {
       ProfScope prof("join_probe_emit_kernel", s);
-      join_probe_emit_kernel<<<grid_for(n), 256, 0, s>>>(p);
+      join_probe_emit_kernel<<<probe_grid(join_probe_emit_kernel, n), 256, 0, s>>>(p);
       after_launch("join_probe_emit_kernel");
       prof.stop(0);
       double w_out = 0;
@@ -538,7 +591,7 @@ void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, 
     if (attempt > 0) GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
     if (n > 0 && t.build->num_rows() > 0) {
       ProfScope prof("join_probe_kernel", s);
-      join_probe_kernel<<<grid_for(n), 256, 0, s>>>(pk, n, probe.rows_dev(), t.slots->as<uint64_t>(),
+      join_probe_kernel<<<probe_grid(join_probe_kernel, n), 256, 0, s>>>(pk, n, probe.rows_dev(), t.slots->as<uint64_t>(),
                                                    t.capacity - 1, bkc, key32 ? 1 : 0, (*probe_idx)->as<int32_t>(),
                                                    (*build_idx)->as<int32_t>(), cap, status->as<DevStatus>());
       after_launch("join_probe_kernel");
