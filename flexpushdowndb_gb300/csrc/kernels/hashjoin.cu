@@ -63,10 +63,10 @@ __global__ void __launch_bounds__(256)
 }
 
 // Per-warp staging of matches: (probe row, build row) pairs in shared
-// memory, flushed to the output when one more step could overflow the stage
-// and once at the end.
+// memory, flushed to the output when fewer than 32 free places remain (one
+// staging round adds at most 32) and once at the end.
 constexpr int kProbeWarps = 8;   // 256-thread CTAs
-constexpr int kRowsPerLane = 4;  // probe rows a lane walks side by side
+constexpr int kRowsPerLane = 2;  // probe rows a lane walks side by side
 constexpr int kStage = 512;      // staged pairs per warp
 constexpr int64_t kProbeTile = 32 * kRowsPerLane;
 
@@ -99,11 +99,24 @@ __device__ __forceinline__ void flush_pairs(PairStage& sg, unsigned long long* c
   sg.n = 0;
 }
 
+// The slot value at index q (0..3) of a four-slot group held as two 16-byte
+// halves.
+__device__ __forceinline__ uint64_t group_slot(const ulonglong2& lo, const ulonglong2& hi, int q) {
+  const unsigned long long a = (q & 1) ? lo.y : lo.x;
+  const unsigned long long b = (q & 1) ? hi.y : hi.x;
+  return (q & 2) ? b : a;
+}
+
 // The probe loop shared by the pair and the materialising probe. A warp
 // takes tiles of kProbeTile probe rows; each lane walks kRowsPerLane of them
 // (rows lane, lane + 32, ...) side by side, so that its key loads and then
 // each step's slot loads are independent requests in flight together rather
-// than one dependent round trip per row.
+// than one dependent round trip per row. A step reads the aligned group of
+// four slots (one 32-byte sector) that holds the row's next slot: the run
+// is the same linear probe as the build's, but a warp, which steps until
+// the longest run among its rows has ended, takes a quarter of the steps.
+// In the first group the slots before the row's start slot are not part of
+// its run; a group with an empty slot at or after the start ends the run.
 template <class Write>
 __device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const uint64_t* __restrict__ slots,
                                            uint64_t mask, const DevCol& bkey, int key32, unsigned long long* cursor,
@@ -113,11 +126,15 @@ __device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const 
   PairStage sg{s_p[threadIdx.x >> 5], s_b[threadIdx.x >> 5], 0};
   const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  // A table always keeps empty slots (load factor <= 0.9), so every run
+  // ends within one pass over the groups; the bound only guards the loop.
+  const uint64_t n_groups = (mask + 1) >> 2;
   for (int64_t base = warp_global * kProbeTile; base < n; base += n_warps * kProbeTile) {
     int64_t k[kRowsPerLane];
     uint32_t tag[kRowsPerLane];
-    uint64_t slot[kRowsPerLane];
+    uint64_t grp[kRowsPerLane];
     unsigned act = 0;
+    uint32_t first = 0;  // 4 bits per row: the slots of its first group that are on its run
 #pragma unroll
     for (int j = 0; j < kRowsPerLane; ++j) {
       const int64_t r = base + j * 32 + lane;
@@ -131,33 +148,62 @@ __device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const 
     for (int j = 0; j < kRowsPerLane; ++j) {
       const uint64_t h = hash_key(k[j]);
       tag[j] = key32 ? static_cast<uint32_t>(k[j]) : static_cast<uint32_t>(h >> 32);
-      slot[j] = h & mask;
+      const uint64_t slot = h & mask;
+      grp[j] = slot & ~3ull;
+      first |= ((0xFu << (slot & 3)) & 0xFu) << (4 * j);
     }
-    // A row leaves at an empty slot, or after it has seen every slot.
-    for (uint64_t steps = 1; __any_sync(0xffffffffu, act != 0); ++steps) {
-      uint64_t sv[kRowsPerLane];
-#pragma unroll
-      for (int j = 0; j < kRowsPerLane; ++j)
-        sv[j] = (act >> j & 1u) ? __ldg(reinterpret_cast<const unsigned long long*>(slots + slot[j]))
-                                : static_cast<unsigned long long>(kEmptySlot);
+    for (uint64_t steps = 0; __any_sync(0xffffffffu, act != 0); ++steps) {
+      ulonglong2 lo[kRowsPerLane], hi[kRowsPerLane];
 #pragma unroll
       for (int j = 0; j < kRowsPerLane; ++j) {
-        bool emit = false;
-        int32_t brow = 0;
         if (act >> j & 1u) {
-          if (sv[j] == kEmptySlot || steps > mask + 1) {
-            act &= ~(1u << j);
-          } else {
-            if (static_cast<uint32_t>(sv[j] >> 32) == tag[j]) {
-              brow = static_cast<int32_t>(static_cast<uint32_t>(sv[j]));
-              emit = key32 ? true : (load_int(bkey, brow) == k[j]);
-            }
-            slot[j] = (slot[j] + 1) & mask;
-          }
+          const ulonglong2* g = reinterpret_cast<const ulonglong2*>(slots + grp[j]);
+          lo[j] = __ldg(g);
+          hi[j] = __ldg(g + 1);
         }
-        stage_pairs(sg, emit, lane, static_cast<int32_t>(base + j * 32 + lane), brow);
       }
-      if (sg.n > kStage - 32 * kRowsPerLane) flush_pairs(sg, cursor, lane, write);
+#pragma unroll
+      for (int j = 0; j < kRowsPerLane; ++j) {
+        uint32_t mm = 0;  // matching slots of the group that lie on the run
+        if (act >> j & 1u) {
+          const uint32_t valid = steps == 0 ? (first >> (4 * j)) & 0xFu : 0xFu;
+          uint32_t eb = 0, tb = 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const uint64_t v = group_slot(lo[j], hi[j], q);
+            if (v == kEmptySlot)
+              eb |= 1u << q;
+            else if (static_cast<uint32_t>(v >> 32) == tag[j])
+              tb |= 1u << q;
+          }
+          eb &= valid;
+          const int stop = eb ? __ffs(eb) - 1 : 4;
+          mm = tb & valid & ((1u << stop) - 1u);
+          if (!key32) {
+            for (uint32_t t = mm; t != 0; t &= t - 1) {
+              const int q = __ffs(t) - 1;
+              const int32_t b = static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo[j], hi[j], q)));
+              if (load_int(bkey, b) != k[j]) mm &= ~(1u << q);
+            }
+          }
+          if (eb != 0 || steps + 1 > n_groups)
+            act &= ~(1u << j);
+          else
+            grp[j] = (grp[j] + 4) & mask;
+        }
+        // One staged match per lane per round; a group can hold several
+        // copies of a repeated build key.
+        while (__any_sync(0xffffffffu, mm != 0)) {
+          int32_t brow = 0;
+          const bool emit = mm != 0;
+          if (emit) {
+            brow = static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo[j], hi[j], __ffs(mm) - 1)));
+            mm &= mm - 1;
+          }
+          stage_pairs(sg, emit, lane, static_cast<int32_t>(base + j * 32 + lane), brow);
+          if (sg.n > kStage - 32) flush_pairs(sg, cursor, lane, write);
+        }
+      }
     }
   }
   if (sg.n > 0) flush_pairs(sg, cursor, lane, write);
