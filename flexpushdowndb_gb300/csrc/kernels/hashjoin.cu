@@ -65,10 +65,8 @@ __global__ void __launch_bounds__(256)
 // Per-warp staging of matches: (probe row, build row) pairs in shared
 // memory, flushed to the output when fewer than 32 free places remain (one
 // staging round adds at most 32) and once at the end.
-constexpr int kProbeWarps = 8;   // 256-thread CTAs
-constexpr int kRowsPerLane = 2;  // probe rows a lane walks side by side
-constexpr int kStage = 512;      // staged pairs per warp
-constexpr int64_t kProbeTile = 32 * kRowsPerLane;
+constexpr int kProbeWarps = 8;  // 256-thread CTAs
+constexpr int kStage = 512;     // staged pairs per warp
 
 struct PairStage {
   int32_t* p;
@@ -107,103 +105,129 @@ __device__ __forceinline__ uint64_t group_slot(const ulonglong2& lo, const ulong
   return (q & 2) ? b : a;
 }
 
-// The probe loop shared by the pair and the materialising probe. A warp
-// takes tiles of kProbeTile probe rows; each lane walks kRowsPerLane of them
-// (rows lane, lane + 32, ...) side by side, so that its key loads and then
-// each step's slot loads are independent requests in flight together rather
-// than one dependent round trip per row. A step reads the aligned group of
-// four slots (one 32-byte sector) that holds the row's next slot: the run
-// is the same linear probe as the build's, but a warp, which steps until
-// the longest run among its rows has ended, takes a quarter of the steps.
-// In the first group the slots before the row's start slot are not part of
-// its run; a group with an empty slot at or after the start ends the run.
+// The probe loop shared by the pair and the materialising probe.
+//
+// Each warp owns a contiguous range of probe rows and each lane walks one
+// row's run at a time; a lane whose run has ended takes the warp's next row
+// before the next step, so lanes do not sit idle behind the longest run of
+// a fixed tile. The keys of the next 128 rows of the range wait in four
+// registers per lane (a ring of 32-row batches, each loaded three batches
+// ahead of its use), so a new row's key comes from a shuffle rather than a
+// dependent load, and a step's only wait is its table read.
+//
+// A step reads the aligned group of four slots (one 32-byte sector) that
+// holds the run's next slot: the run is the same linear probe as the
+// build's, in about a quarter of the steps. In a run's first group the
+// slots before its start slot are not part of it; an empty slot at or
+// after the start ends the run.
 template <class Write>
 __device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const uint64_t* __restrict__ slots,
                                            uint64_t mask, const DevCol& bkey, int key32, unsigned long long* cursor,
                                            Write& write) {
   __shared__ int32_t s_p[kProbeWarps][kStage], s_b[kProbeWarps][kStage];
   const int lane = threadIdx.x & 31;
+  const uint32_t below = (1u << lane) - 1u;
   PairStage sg{s_p[threadIdx.x >> 5], s_b[threadIdx.x >> 5], 0};
   const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  const int64_t per = ((n + n_warps - 1) / n_warps + 31) & ~static_cast<int64_t>(31);
+  const int64_t begin = warp_global * per < n ? warp_global * per : n;
+  const int64_t end = begin + per < n ? begin + per : n;
   // A table always keeps empty slots (load factor <= 0.9), so every run
   // ends within one pass over the groups; the bound only guards the loop.
   const uint64_t n_groups = (mask + 1) >> 2;
-  for (int64_t base = warp_global * kProbeTile; base < n; base += n_warps * kProbeTile) {
-    int64_t k[kRowsPerLane];
-    uint32_t tag[kRowsPerLane];
-    uint64_t grp[kRowsPerLane];
-    unsigned act = 0;
-    uint32_t first = 0;  // 4 bits per row: the slots of its first group that are on its run
+
+  int64_t ring[4];  // keys of rows ring_base + 32 * b + lane
+  int64_t ring_base = begin;
 #pragma unroll
-    for (int j = 0; j < kRowsPerLane; ++j) {
-      const int64_t r = base + j * 32 + lane;
-      k[j] = 0;
-      if (r < n) {
-        k[j] = load_int(pkey, r);
-        act |= 1u << j;
+  for (int b = 0; b < 4; ++b) {
+    const int64_t r = begin + 32 * b + lane;
+    ring[b] = r < end ? load_int(pkey, r) : 0;
+  }
+  int taken = 0;  // rows of the ring's first batch already handed out (< 32 between steps)
+
+  bool active = false;
+  int32_t row = 0;
+  int64_t k = 0;
+  uint32_t tag = 0, valid = 0;
+  uint64_t grp = 0, steps = 0;
+  while (true) {
+    // Hand the next rows of the range to the lanes without one, in lane
+    // order: the lane of rank i among them takes row ring_base + taken + i.
+    const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+    const int64_t left = end - (ring_base + taken);
+    if (idle == 0xffffffffu && left <= 0) break;
+    if (idle != 0 && left > 0) {
+      const int idx = taken + __popc(idle & below);  // < 64: in the ring's first two batches
+      const int64_t v0 = __shfl_sync(0xffffffffu, ring[0], idx & 31);
+      const int64_t v1 = __shfl_sync(0xffffffffu, ring[1], idx & 31);
+      if (!active && idx - taken < left) {
+        active = true;
+        row = static_cast<int32_t>(ring_base + idx);
+        k = idx < 32 ? v0 : v1;
+        const uint64_t h = hash_key(k);
+        tag = key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
+        const uint64_t slot = h & mask;
+        grp = slot & ~3ull;
+        valid = (0xFu << (slot & 3)) & 0xFu;
+        steps = 0;
+      }
+      const int handed = static_cast<int64_t>(__popc(idle)) < left ? __popc(idle) : static_cast<int>(left);
+      taken += handed;
+      if (taken >= 32) {  // the first batch is used up: shift, fetch the batch after the last
+        ring[0] = ring[1];
+        ring[1] = ring[2];
+        ring[2] = ring[3];
+        const int64_t r = ring_base + 128 + lane;
+        ring[3] = r < end ? load_int(pkey, r) : 0;
+        ring_base += 32;
+        taken -= 32;
       }
     }
+
+    uint32_t mm = 0;  // matching slots of this step's group that lie on the run
+    ulonglong2 lo{0, 0}, hi{0, 0};
+    if (active) {
+      const ulonglong2* g = reinterpret_cast<const ulonglong2*>(slots + grp);
+      lo = __ldg(g);
+      hi = __ldg(g + 1);
+      uint32_t eb = 0, tb = 0;
 #pragma unroll
-    for (int j = 0; j < kRowsPerLane; ++j) {
-      const uint64_t h = hash_key(k[j]);
-      tag[j] = key32 ? static_cast<uint32_t>(k[j]) : static_cast<uint32_t>(h >> 32);
-      const uint64_t slot = h & mask;
-      grp[j] = slot & ~3ull;
-      first |= ((0xFu << (slot & 3)) & 0xFu) << (4 * j);
+      for (int q = 0; q < 4; ++q) {
+        const uint64_t v = group_slot(lo, hi, q);
+        if (v == kEmptySlot)
+          eb |= 1u << q;
+        else if (static_cast<uint32_t>(v >> 32) == tag)
+          tb |= 1u << q;
+      }
+      eb &= valid;
+      const int stop = eb ? __ffs(eb) - 1 : 4;
+      mm = tb & valid & ((1u << stop) - 1u);
+      if (!key32) {
+        for (uint32_t t = mm; t != 0; t &= t - 1) {
+          const int q = __ffs(t) - 1;
+          if (load_int(bkey, static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo, hi, q)))) != k)
+            mm &= ~(1u << q);
+        }
+      }
+      if (eb != 0 || ++steps > n_groups) {
+        active = false;
+      } else {
+        grp = (grp + 4) & mask;
+        valid = 0xFu;
+      }
     }
-    for (uint64_t steps = 0; __any_sync(0xffffffffu, act != 0); ++steps) {
-      ulonglong2 lo[kRowsPerLane], hi[kRowsPerLane];
-#pragma unroll
-      for (int j = 0; j < kRowsPerLane; ++j) {
-        if (act >> j & 1u) {
-          const ulonglong2* g = reinterpret_cast<const ulonglong2*>(slots + grp[j]);
-          lo[j] = __ldg(g);
-          hi[j] = __ldg(g + 1);
-        }
+    // One staged match per lane per round; a group can hold several copies
+    // of a repeated build key.
+    while (__any_sync(0xffffffffu, mm != 0)) {
+      int32_t brow = 0;
+      const bool emit = mm != 0;
+      if (emit) {
+        brow = static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo, hi, __ffs(mm) - 1)));
+        mm &= mm - 1;
       }
-#pragma unroll
-      for (int j = 0; j < kRowsPerLane; ++j) {
-        uint32_t mm = 0;  // matching slots of the group that lie on the run
-        if (act >> j & 1u) {
-          const uint32_t valid = steps == 0 ? (first >> (4 * j)) & 0xFu : 0xFu;
-          uint32_t eb = 0, tb = 0;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const uint64_t v = group_slot(lo[j], hi[j], q);
-            if (v == kEmptySlot)
-              eb |= 1u << q;
-            else if (static_cast<uint32_t>(v >> 32) == tag[j])
-              tb |= 1u << q;
-          }
-          eb &= valid;
-          const int stop = eb ? __ffs(eb) - 1 : 4;
-          mm = tb & valid & ((1u << stop) - 1u);
-          if (!key32) {
-            for (uint32_t t = mm; t != 0; t &= t - 1) {
-              const int q = __ffs(t) - 1;
-              const int32_t b = static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo[j], hi[j], q)));
-              if (load_int(bkey, b) != k[j]) mm &= ~(1u << q);
-            }
-          }
-          if (eb != 0 || steps + 1 > n_groups)
-            act &= ~(1u << j);
-          else
-            grp[j] = (grp[j] + 4) & mask;
-        }
-        // One staged match per lane per round; a group can hold several
-        // copies of a repeated build key.
-        while (__any_sync(0xffffffffu, mm != 0)) {
-          int32_t brow = 0;
-          const bool emit = mm != 0;
-          if (emit) {
-            brow = static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo[j], hi[j], __ffs(mm) - 1)));
-            mm &= mm - 1;
-          }
-          stage_pairs(sg, emit, lane, static_cast<int32_t>(base + j * 32 + lane), brow);
-          if (sg.n > kStage - 32) flush_pairs(sg, cursor, lane, write);
-        }
-      }
+      stage_pairs(sg, emit, lane, row, brow);
+      if (sg.n > kStage - 32) flush_pairs(sg, cursor, lane, write);
     }
   }
   if (sg.n > 0) flush_pairs(sg, cursor, lane, write);
@@ -407,7 +431,7 @@ int probe_grid(Kernel kernel, int64_t n) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0) != cudaSuccess || b < 1) b = 4;
     return b;
   }();
-  return grid_for(n, per_sm, kProbeWarps * kProbeTile);
+  return grid_for(n, per_sm, kProbeWarps * 256);  // at least 256 rows per warp
 }
 
 }  // namespace
