@@ -603,6 +603,13 @@ def _operator_case(args):
             g = ops.Group(["k"], aggs)
             g.group(t)
             return g.finalise()
+
+        for _ in range(max(2, args.warmup)):
+            fn()
+        from flexpushdowndb_gb300 import _abi
+
+        prof = _kernel_profile(_abi.lib(), _abi, fn, args.steps)
+        print(json.dumps({"case": "group", "rows": n, "kernels_ms": {k: v["ms"] / args.steps for k, v in prof.items()}}))
     elif args.case == "filter":
         from flexpushdowndb_gb300.expression import and_, gte, lt, num_lit
 

@@ -15,11 +15,20 @@
 // (64-bit atomicCAS on keys, 64-bit atomics on accumulators) and merges the
 // table into the global open-addressing table once at the end, so
 // low-cardinality group-bys (a handful to a few thousand groups) cost one
-// global atomic per group per CTA rather than per row. Rows whose key does
+// global atomic per group per CTA rather than per row.
+//
+// Table size: at most half full for an upper bound on the groups (groups so
+// far plus the batch's rows). A large batch whose rows are known on the host
+// is first counted with a HyperLogLog sketch of its keys, and the table is
+// sized for that estimate instead: a batch of 20M rows over 2M distinct
+// keys then gets a table that fits the L2 rather than one of 64M slots
+// whose every access misses it. Rows whose key does
 // not fit the shared table go straight to the global table. Integer sums are
 // 64-bit two's-complement additions, which are associative and commutative,
 // so results are bit-exact whatever order the atomics land in.
+#include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "eval.cuh"
 #include "launch.h"
@@ -109,22 +118,19 @@ __device__ __forceinline__ void acc_combine(unsigned long long* addr, int fn, in
   }
 }
 
-// Global slot of a key; claims an empty slot for a new key. Returns
-// UINT64_MAX (and raises GFPDB_ENOMEM) if the table is full.
-__device__ __forceinline__ uint64_t global_slot(const GroupParams& p, uint64_t key) {
-  if (key == kEmptySlot) {
-    if (atomicExch(reinterpret_cast<unsigned long long*>(&p.st->aux[1]), 1ull) == 0ull)
-      atomicAdd(reinterpret_cast<unsigned long long*>(&p.st->aux[0]), 1ull);
-    return p.mask + 1;
-  }
-  uint64_t slot = hash_key(static_cast<int64_t>(key)) & p.mask;
+// Global slot of a key that is not the all-ones word, continuing from its
+// home slot `slot` whose content `s` the caller has already read; claims an
+// empty slot for a new key. Returns UINT64_MAX (and raises GFPDB_ENOMEM) if
+// the table is full.
+__device__ __forceinline__ uint64_t global_slot_from(const GroupParams& p, uint64_t key, uint64_t slot, uint64_t s,
+                                                     unsigned long long* claims) {
   for (uint64_t i = 0; i <= p.mask; ++i) {
-    uint64_t s = *reinterpret_cast<volatile uint64_t*>(p.keys + slot);
+    if (i > 0) s = *reinterpret_cast<volatile uint64_t*>(p.keys + slot);
     if (s == kEmptySlot) {
       s = atomicCAS(reinterpret_cast<unsigned long long*>(p.keys + slot), static_cast<unsigned long long>(kEmptySlot),
                     static_cast<unsigned long long>(key));
       if (s == kEmptySlot) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&p.st->aux[0]), 1ull);
+        atomicAdd(claims, 1ull);
         return slot;
       }
     }
@@ -133,6 +139,22 @@ __device__ __forceinline__ uint64_t global_slot(const GroupParams& p, uint64_t k
   }
   raise_status(p.st, GFPDB_ENOMEM, 20);
   return UINT64_MAX;
+}
+
+// The all-ones key has its own slot at index capacity.
+__device__ __forceinline__ uint64_t special_slot(const GroupParams& p) {
+  if (atomicExch(reinterpret_cast<unsigned long long*>(&p.st->aux[1]), 1ull) == 0ull)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&p.st->aux[0]), 1ull);
+  return p.mask + 1;
+}
+
+// `claims` counts the groups this call creates: a CTA's shared-memory
+// counter, added to the table's count once per CTA (one global address
+// taking an atomic per new group would serialise the L2 on it).
+__device__ __forceinline__ uint64_t global_slot(const GroupParams& p, uint64_t key, unsigned long long* claims) {
+  if (key == kEmptySlot) return special_slot(p);
+  const uint64_t slot = hash_key(static_cast<int64_t>(key)) & p.mask;
+  return global_slot_from(p, key, slot, *reinterpret_cast<volatile uint64_t*>(p.keys + slot), claims);
 }
 
 __device__ __forceinline__ unsigned long long row_value(const GroupParams& p, const AccDev& a, int64_t row) {
@@ -151,13 +173,15 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
   // A grid sized for a capacity can be far larger than the rows that arrive:
   // CTAs without rows leave before touching shared memory (uniform per CTA).
   if (static_cast<int64_t>(blockIdx.x) * kGroupThreads >= n_rows) return;
+  __shared__ unsigned long long s_claims;
+  if (threadIdx.x == 0) s_claims = 0;
   if (p.use_smem) {
     for (int i = threadIdx.x; i < p.sm_slots; i += kGroupThreads) {
       s_keys[i] = kEmptySlot;
       for (int a = 0; a < p.n_acc; ++a) s_acc[i * p.n_acc + a] = acc_init(p.acc[a].fn, p.acc[a].vt);
     }
-    __syncthreads();
   }
+  __syncthreads();
   const int64_t stride = static_cast<int64_t>(gridDim.x) * kGroupThreads;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * kGroupThreads + threadIdx.x; r < n_rows; r += stride) {
     const uint64_t key = pack_key(p, r);
@@ -186,7 +210,7 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
       for (int a = 0; a < p.n_acc; ++a)
         acc_combine(s_acc + found * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, row_value(p, p.acc[a], r));
     } else {
-      const uint64_t g = global_slot(p, key);
+      const uint64_t g = global_slot(p, key, &s_claims);
       if (g != UINT64_MAX)
         for (int a = 0; a < p.n_acc; ++a)
           acc_combine(p.accs + g * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, row_value(p, p.acc[a], r));
@@ -207,10 +231,40 @@ __global__ void __launch_bounds__(kGroupThreads) group_update_kernel(const __gri
     __syncthreads();
     for (int j = threadIdx.x; j < occupied; j += kGroupThreads) {
       const int i = s_occ[j];
-      const uint64_t g = global_slot(p, s_keys[i]);
+      const uint64_t g = global_slot(p, s_keys[i], &s_claims);
       if (g == UINT64_MAX) continue;
       for (int a = 0; a < p.n_acc; ++a) acc_combine(p.accs + g * p.n_acc + a, p.acc[a].fn, p.acc[a].vt, s_acc[i * p.n_acc + a]);
     }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_claims != 0)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&p.st->aux[0]), s_claims);
+}
+
+// HyperLogLog sketch (Flajolet, Fusy, Gandouet, Meunier 2007) of a batch's
+// packed keys: 2^12 registers, each the largest leading-zero rank + 1 of
+// the hashes that fall in it. Registers gather per CTA in shared memory.
+constexpr int kSketchBits = 12;
+constexpr int kSketchRegs = 1 << kSketchBits;
+
+__global__ void __launch_bounds__(256) group_sketch_kernel(const __grid_constant__ GroupParams p,
+                                                           unsigned* __restrict__ regs) {
+  __shared__ unsigned s_regs[kSketchRegs];
+  for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) s_regs[i] = 0;
+  __syncthreads();
+  const int64_t n = clamp_rows(p.n_dev, p.n_rows);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    // a hash unrelated to the slot hash (another constant before the mixer)
+    const uint64_t h = mix64(pack_key(p, r) ^ 0xd6e8feb86659fd93ull);
+    const unsigned idx = static_cast<unsigned>(h >> (64 - kSketchBits));
+    const unsigned rank = static_cast<unsigned>(__clzll((h << kSketchBits) | (1ull << (kSketchBits - 1)))) + 1u;
+    if (rank > s_regs[idx]) atomicMax(&s_regs[idx], rank);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) {
+    const unsigned v = s_regs[i];
+    if (v > *reinterpret_cast<volatile unsigned*>(regs + i)) atomicMax(regs + i, v);
   }
 }
 
@@ -458,6 +512,15 @@ int grid_for(int64_t n) {
   return static_cast<int>(blocks < 1 ? 1 : blocks);
 }
 
+// Tables above this many slots (32 MB of keys) are sized by a sketch when
+// the batch allows it.
+constexpr uint64_t kSketchMinSlots = 1ull << 22;
+
+bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus c = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &c) == cudaSuccess && c != cudaStreamCaptureStatusNone;
+}
+
 uint64_t next_pow2(uint64_t x) {
   uint64_t c = 1;
   while (c < x) c <<= 1;
@@ -469,6 +532,36 @@ DevStatus read_status(const DevStatus* d, cudaStream_t s) {
   GF_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
   sync(s);
   return h;
+}
+
+// Distinct keys of a batch, estimated from its HyperLogLog sketch (the raw
+// estimate alpha_m m^2 / sum 2^-M[j], with linear counting over the empty
+// registers in the small range); standard error about 1.04 / sqrt(2^12).
+double sketch_distinct(const GroupParams& p, int64_t n, cudaStream_t s) {
+  auto regs = make_filled(kSketchRegs * 4, 0, s);
+  // enough CTAs to stream the keys at full occupancy (16 KB of registers
+  // each); their merges mostly find the global registers already as large
+  int64_t blocks = (n + 1023) / 1024;
+  if (blocks > static_cast<int64_t>(num_sms()) * 8) blocks = static_cast<int64_t>(num_sms()) * 8;
+  {
+    ProfScope prof("group_sketch_kernel", s);
+    group_sketch_kernel<<<static_cast<int>(blocks < 1 ? 1 : blocks), 256, 0, s>>>(p, regs->as<unsigned>());
+    after_launch("group_sketch_kernel");
+    prof.stop(static_cast<double>(n) * 8);
+  }
+  std::vector<unsigned> h(kSketchRegs);
+  GF_CUDA(cudaMemcpyAsync(h.data(), regs->data(), kSketchRegs * 4, cudaMemcpyDeviceToHost, s));
+  sync(s);
+  double sum = 0;
+  int zeros = 0;
+  for (unsigned v : h) {
+    sum += std::ldexp(1.0, -static_cast<int>(v));
+    zeros += v == 0 ? 1 : 0;
+  }
+  const double m = kSketchRegs;
+  double e = 0.7213 / (1.0 + 1.079 / m) * m * m / sum;
+  if (e <= 2.5 * m && zeros > 0) e = m * std::log(m / zeros);
+  return e;
 }
 
 class StringDict {
@@ -720,6 +813,31 @@ class GroupTable {
     const TupleSet& ts = *tsp;
     const int64_t n = ts.num_rows();
     if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "group-by batch must have fewer than 2^31 rows");
+
+    GroupParams* pp = new GroupParams;
+    std::unique_ptr<GroupParams> holder(pp);
+    GroupParams& p = *pp;
+    std::memset(&p, 0, sizeof(p));
+    p.n_rows = n;
+    p.n_dev = ts.rows_dev();
+    p.n_keys = static_cast<int32_t>(group_cols.size());
+    p.n_acc = static_cast<int32_t>(accs.size());
+    std::vector<BufferPtr> code_bufs;
+    if (n > 0) {
+      for (int k = 0; k < p.n_keys; ++k) {
+        const auto& c = ts.column(group_cols[k]);
+        if (c->type != key_types[k]) fail(GFPDB_EINVAL, "group key column changed type between batches");
+        p.key_bits[k] = key_bits[k];
+        if (c->type == DType::Utf8) {
+          auto codes = dicts[k]->encode(*c, s);
+          code_bufs.push_back(codes);
+          p.key_cols[k] = DevCol{codes->data(), nullptr, CT_I32, 0};
+        } else {
+          p.key_cols[k] = DevCol{c->data, nullptr, static_cast<int32_t>(c->type), 0};
+        }
+      }
+    }
+
     // Size the table so that it stays at most half full.
     int64_t bound = groups_upper + n;
     if (hint > 0 && bound > hint) bound = groups_upper > hint ? groups_upper : hint;
@@ -733,30 +851,22 @@ class GroupTable {
       if (hint > 0 && bound > hint) bound = groups_upper > hint ? groups_upper : hint;
       want = next_pow2(static_cast<uint64_t>(2 * bound < 1024 ? 1024 : 2 * bound));
     }
+    if (want > cap && want > kSketchMinSlots && hint == 0 && n > 0 && p.n_keys > 0 && ts.exact() &&
+        !deferred_mode() && !stream_capturing(s)) {
+      // A large table for a batch whose rows are on the host: size it for
+      // the batch's estimated distinct keys (with a quarter to spare) over
+      // the exact groups so far instead of its row count.
+      const double est = sketch_distinct(p, n, s);
+      int64_t fresh = static_cast<int64_t>(est * 1.25) + 1024;
+      if (fresh > n) fresh = n;
+      const int64_t known = cap > 0 ? groups_upper : 0;  // exact: read above
+      const int64_t b2 = known + fresh;
+      const uint64_t w2 = next_pow2(static_cast<uint64_t>(2 * b2 < 1024 ? 1024 : 2 * b2));
+      if (w2 < want) want = w2 > cap ? w2 : cap;
+    }
     if (want > cap) init_table(want, s);
     if (n == 0) return;
 
-    GroupParams* pp = new GroupParams;
-    std::unique_ptr<GroupParams> holder(pp);
-    GroupParams& p = *pp;
-    std::memset(&p, 0, sizeof(p));
-    p.n_rows = n;
-    p.n_dev = ts.rows_dev();
-    p.n_keys = static_cast<int32_t>(group_cols.size());
-    p.n_acc = static_cast<int32_t>(accs.size());
-    std::vector<BufferPtr> code_bufs;
-    for (int k = 0; k < p.n_keys; ++k) {
-      const auto& c = ts.column(group_cols[k]);
-      if (c->type != key_types[k]) fail(GFPDB_EINVAL, "group key column changed type between batches");
-      p.key_bits[k] = key_bits[k];
-      if (c->type == DType::Utf8) {
-        auto codes = dicts[k]->encode(*c, s);
-        code_bufs.push_back(codes);
-        p.key_cols[k] = DevCol{codes->data(), nullptr, CT_I32, 0};
-      } else {
-        p.key_cols[k] = DevCol{c->data, nullptr, static_cast<int32_t>(c->type), 0};
-      }
-    }
     for (int a = 0; a < p.n_acc; ++a) p.acc[a] = accs[a];
     bind_columns(slots, ts, p.cols, kMaxCols);
     p.prog = prog;
@@ -774,7 +884,12 @@ class GroupTable {
     p.sm_slots = sm_slots;
     const size_t dyn = p.use_smem ? static_cast<size_t>(sm_slots) * per_slot : 0;
     int64_t blocks = (n + kGroupThreads * 16 - 1) / (kGroupThreads * 16);
-    int64_t max_blocks = static_cast<int64_t>(num_sms()) * 4;
+    // one wave: as many CTAs as fit on every SM at once
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, group_update_kernel, kGroupThreads, dyn) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    int64_t max_blocks = static_cast<int64_t>(num_sms()) * per_sm;
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
     ProfScope prof("group_update_kernel", s);

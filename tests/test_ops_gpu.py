@@ -170,6 +170,25 @@ def test_group_parity(gpu, n, groups, hint):
     assert got.sorted_rows() == want.sorted_rows()
 
 
+def test_group_sketch_sized_table_two_batches(gpu):
+    # Batches large enough that the table is sized from a distinct-key sketch
+    # rather than the row count; the second batch overlaps the first's keys
+    # and re-sizes from the exact group count plus its own sketch.
+    rng = np.random.default_rng(77)
+    n = 2_200_000
+    parts = [Table([Column("g", "int64", rng.integers(lo, lo + 1_000_000, n) * 7919),
+                    Column("v", "int64", rng.integers(-10**12, 10**12, n))]) for lo in (0, 500_000)]
+    aggs = [{"function": "SUM", "name": "s", "expr": col("v")}, {"function": "COUNT", "name": "c"}]
+    g = ops.Group(["g"], aggs)
+    for p in parts:
+        g.group(DeviceTable.from_host(p))
+    got = g.finalise()
+    allt = Table([Column(c, "int64", np.concatenate([p[c] for p in parts])) for c in ("g", "v")])
+    want = oops.group_by(allt, ["g"], aggs)
+    assert got.num_rows == want.num_rows
+    assert got.sorted_rows() == want.sorted_rows()
+
+
 def test_group_two_keys_utf8_key_and_batches(gpu):
     rng = np.random.default_rng(9)
     parts = []
