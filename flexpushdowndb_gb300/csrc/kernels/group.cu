@@ -347,49 +347,71 @@ __device__ __forceinline__ void store_typed(void* dst, int64_t pos, int type, in
   else static_cast<int*>(dst)[pos] = static_cast<int32_t>(v);
 }
 
+// Each warp lists the live slots of kSteps consecutive 32-slot steps with
+// one atomic on the output counter. Large tables take several steps per
+// atomic (one address taking an atomic per 32 slots would queue them);
+// small ones one step per warp, so that more warps share the few slots.
+constexpr uint64_t kFinalChunkedSlots = 1ull << 20;
+
+template <int kSteps>
 __global__ void __launch_bounds__(256) group_finalize_kernel(const __grid_constant__ FinalParams p) {
   const int lane = threadIdx.x & 31;
+  const uint32_t below = (1u << lane) - 1u;
   const uint64_t n_slots = p.cap + 1;
   const uint64_t warp0 = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
-  for (uint64_t base = warp0 * 32; base < n_slots; base += n_warps * 32) {
-    const uint64_t i = base + lane;
-    bool live = false;
-    uint64_t key = 0;
-    if (i < p.cap) {
-      key = p.keys[i];
-      live = key != kEmptySlot;
-    } else if (i == p.cap) {
-      key = kEmptySlot;
-      live = *p.special_dev != 0;
-    }
-    const uint32_t m = __ballot_sync(0xffffffffu, live);
-    if (m == 0) continue;
-    unsigned long long at = 0;
-    const int leader = __ffs(m) - 1;
-    if (lane == leader) at = atomicAdd(p.counter, static_cast<unsigned long long>(__popc(m)));
-    at = __shfl_sync(0xffffffffu, at, leader);
-    if (!live) continue;
-    const int64_t pos = static_cast<int64_t>(at) + __popc(m & ((1u << lane) - 1u));
-    if (p.n_keys == 1) {
-      const int64_t v = p.key_bits[0] == 64 ? static_cast<int64_t>(key) : static_cast<int32_t>(static_cast<uint32_t>(key));
-      store_typed(p.key_dst[0], pos, p.key_type[0], v);
-    } else if (p.n_keys == 2) {
-      store_typed(p.key_dst[0], pos, p.key_type[0], static_cast<int32_t>(static_cast<uint32_t>(key >> 32)));
-      store_typed(p.key_dst[1], pos, p.key_type[1], static_cast<int32_t>(static_cast<uint32_t>(key)));
-    }
-    for (int j = 0; j < p.n_out; ++j) {
-      const OutAggDev& o = p.outs[j];
-      const unsigned long long a = p.accs[i * p.n_acc + o.a0];
-      if (o.kind == 0) {
-        store_typed(o.dst, pos, o.out_type, static_cast<int64_t>(a));
-      } else {
-        const unsigned long long c = p.accs[i * p.n_acc + o.a1];
-        const double s = o.vt == VT_F64 ? __longlong_as_double(static_cast<long long>(a))
-                                        : static_cast<double>(static_cast<long long>(a));
-        const double avg = c == 0 ? 0.0 : s / static_cast<double>(c);
-        static_cast<double*>(o.dst)[pos] = avg;
+  constexpr uint64_t kChunk = 32 * kSteps;
+  for (uint64_t base = warp0 * kChunk; base < n_slots; base += n_warps * kChunk) {
+    uint64_t key[kSteps];
+    uint32_t m[kSteps];
+    int total = 0;
+#pragma unroll
+    for (int k = 0; k < kSteps; ++k) {
+      const uint64_t i = base + k * 32 + lane;
+      bool live = false;
+      key[k] = 0;
+      if (i < p.cap) {
+        key[k] = p.keys[i];
+        live = key[k] != kEmptySlot;
+      } else if (i == p.cap) {
+        key[k] = kEmptySlot;
+        live = *p.special_dev != 0;
       }
+      m[k] = __ballot_sync(0xffffffffu, live);
+      total += __popc(m[k]);
+    }
+    if (total == 0) continue;
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(p.counter, static_cast<unsigned long long>(total));
+    at = __shfl_sync(0xffffffffu, at, 0);
+#pragma unroll
+    for (int k = 0; k < kSteps; ++k) {
+      if (m[k] >> lane & 1u) {
+        const uint64_t i = base + k * 32 + lane;
+        const int64_t pos = static_cast<int64_t>(at) + __popc(m[k] & below);
+        if (p.n_keys == 1) {
+          const int64_t v = p.key_bits[0] == 64 ? static_cast<int64_t>(key[k])
+                                                : static_cast<int32_t>(static_cast<uint32_t>(key[k]));
+          store_typed(p.key_dst[0], pos, p.key_type[0], v);
+        } else if (p.n_keys == 2) {
+          store_typed(p.key_dst[0], pos, p.key_type[0], static_cast<int32_t>(static_cast<uint32_t>(key[k] >> 32)));
+          store_typed(p.key_dst[1], pos, p.key_type[1], static_cast<int32_t>(static_cast<uint32_t>(key[k])));
+        }
+        for (int j = 0; j < p.n_out; ++j) {
+          const OutAggDev& o = p.outs[j];
+          const unsigned long long a = p.accs[i * p.n_acc + o.a0];
+          if (o.kind == 0) {
+            store_typed(o.dst, pos, o.out_type, static_cast<int64_t>(a));
+          } else {
+            const unsigned long long c = p.accs[i * p.n_acc + o.a1];
+            const double s = o.vt == VT_F64 ? __longlong_as_double(static_cast<long long>(a))
+                                            : static_cast<double>(static_cast<long long>(a));
+            const double avg = c == 0 ? 0.0 : s / static_cast<double>(c);
+            static_cast<double*>(o.dst)[pos] = avg;
+          }
+        }
+      }
+      at += __popc(m[k]);
     }
   }
 }
@@ -952,8 +974,15 @@ class GroupTable {
     }
     auto counter = make_filled(8, 0, s);
     fp.counter = counter->as<unsigned long long>();
-    group_finalize_kernel<<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(fp);
-    after_launch("group_finalize_kernel");
+    {
+      ProfScope prof("group_finalize_kernel", s);
+      if (cap + 1 >= kFinalChunkedSlots)
+        group_finalize_kernel<8><<<grid_for(static_cast<int64_t>((cap + 1) / 8)), 256, 0, s>>>(fp);
+      else
+        group_finalize_kernel<1><<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(fp);
+      after_launch("group_finalize_kernel");
+      prof.stop(static_cast<double>(cap + 1) * 8);
+    }
     std::vector<ColumnPtr> cols;
     for (size_t k = 0; k < group_cols.size(); ++k) {
       if (key_types[k] == DType::Utf8) cols.push_back(dicts[k]->decode(key_out[k]->as<int32_t>(), n_groups, s));

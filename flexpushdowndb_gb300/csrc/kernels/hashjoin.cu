@@ -311,8 +311,8 @@ __global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_const
 // per step; a match at an inner level moves it to the next level (whose key
 // comes from the input row or an earlier match), a match at the last level
 // emits an output row, and the end of a run returns it to the level before,
-// whose run it continues. The warp steps together so that emitted rows still
-// take their output positions with one atomic per warp and step.
+// whose run it continues. The warp steps together so that emitted rows can
+// be staged with one ballot per step.
 struct ChainLevel {
   const uint64_t* slots;
   uint64_t mask;
@@ -338,12 +338,42 @@ struct ChainParams {
   int32_t from[kJoinOutMax];  // 0: the input row; l + 1: the build row of level l
 };
 
+// kStaged: output rows collect per warp in shared memory as the row index of
+// every level (input row, then each join's build row) and leave in runs,
+// each run taking its positions with one atomic on the shared cursor (for
+// large inputs, whose per-step atomics would queue on that one address).
+// Otherwise a warp step's rows are written at once with one atomic per step
+// (small inputs, where the final flush would only add a round trip).
+constexpr int kChainStage = 128;
+constexpr int64_t kChainStagedRows = 1 << 20;
+
+template <bool kStaged>
 __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__ ChainParams p) {
   const int64_t n = clamp_rows(p.n_dev, p.n_cap);
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int64_t warp_global = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   unsigned long long* cursor = reinterpret_cast<unsigned long long*>(&p.st->value);
+  __shared__ int32_t s_rows[kStaged ? kProbeWarps : 1][kJoinChainMax + 1][kStaged ? kChainStage : 1];
+  int staged = 0;  // the same in every lane
+  auto flush = [&]() {
+    __syncwarp();
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(cursor, static_cast<unsigned long long>(staged));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    for (int c = 0; c < p.n_out; ++c) {
+      const int32_t* idx = s_rows[warp][p.from[c]];
+      if (p.width[c] == 8)
+        copy_staged(static_cast<const long long*>(p.src[c]), static_cast<long long*>(p.dst[c]), idx, staged,
+                    static_cast<int64_t>(at), p.cap, lane);
+      else
+        copy_staged(static_cast<const int*>(p.src[c]), static_cast<int*>(p.dst[c]), idx, staged,
+                    static_cast<int64_t>(at), p.cap, lane);
+    }
+    __syncwarp();
+    staged = 0;
+  };
   for (int64_t base = warp_global * 32; base < n; base += n_warps * 32) {
     const int64_t r = base + lane;
     bool active = r < n;
@@ -390,7 +420,14 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
         }
       }
       const uint32_t em = __ballot_sync(0xffffffffu, emit);
-      if (em != 0) {
+      if constexpr (kStaged) {
+        if (emit) {
+          const int at = staged + __popc(em & ((1u << lane) - 1u));
+          for (int l = 0; l <= p.n_levels; ++l) s_rows[warp][l][at] = static_cast<int32_t>(rows[l]);
+        }
+        staged += __popc(em);
+        if (staged > kChainStage - 32) flush();
+      } else if (em != 0) {
         unsigned long long at = 0;
         const int leader = __ffs(em) - 1;
         if (lane == leader) at = atomicAdd(cursor, static_cast<unsigned long long>(__popc(em)));
@@ -410,6 +447,7 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
       }
     }
   }
+  if (kStaged && staged > 0) flush();
 }
 
 // Grid-stride launches: four CTAs per SM keep the build's atomics busy, and
@@ -604,7 +642,10 @@ std::vector<ColumnPtr> join_chain_materialize(const std::vector<const JoinTable*
     if (attempt > 0) GF_CUDA(cudaMemsetAsync(status->data(), 0, sizeof(DevStatus), s));
     if (n > 0 && !empty_build) {
       ProfScope prof("join_chain_kernel", s);
-      join_chain_kernel<<<grid_for(n), 256, 0, s>>>(p);
+      if (n >= kChainStagedRows)
+        join_chain_kernel<true><<<grid_for(n), 256, 0, s>>>(p);
+      else
+        join_chain_kernel<false><<<grid_for(n), 256, 0, s>>>(p);
       after_launch("join_chain_kernel");
       prof.stop(0);
       double w_out = 0;

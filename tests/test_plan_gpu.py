@@ -267,6 +267,21 @@ def test_join_chain_snowflake_duplicates(gpu, dup, project_utf8, graph):
         assert r.stats["num_ops"] == (5 if fuse else 6)
 
 
+def test_join_chain_large_input_staged_output(gpu):
+    """A chain over more than a million input rows stages its output rows
+    per warp before writing them: same rows as the oracle, with repeated
+    build keys so that a warp flushes many times."""
+    from oracle import ops as oops
+
+    tabs = _snowflake_tables(1_100_000, 4242, 2)
+    j1 = oops.hash_join(tabs["a"], tabs["fact"], "a_pk", "fk_a", ["v", "w", "a_link", "a_x"])
+    want = oops.hash_join(tabs["b"], j1, "b_pk", "a_link", ["v", "a_x", "b_y", "w"])
+    r = plan.execute(_snowflake_plan(False, True), tabs)
+    assert r.stats["num_ops"] == 5
+    assert r.table.num_rows == want.num_rows
+    assert r.table.sorted_rows() == want.sorted_rows()
+
+
 @pytest.mark.parametrize("graph", [False, True])
 def test_prepared_plan_matches_execute(gpu, graph):
     """PreparedPlan (bound inputs, one-call result import) returns what
