@@ -625,18 +625,17 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const ArrowSchema* schema, co
     cudaStream_t s = as_stream(stream);
     auto ts = import_tupleset(schema, batch, s);
     const int pk = ts->require_column(join->probe_key);
-    BufferPtr pidx, bidx;
-    int64_t n = 0;
-    join_probe_pairs(join->table, *ts, pk, &pidx, &bidx, &n, s);
     auto needed = [&](const std::string& c) {
       return join->all_columns || std::find(join->needed.begin(), join->needed.end(), c) != join->needed.end();
     };
-    std::vector<GatherSpec> specs;
     std::vector<Field> fields;
+    std::vector<int> pcols, bcols;
+    bool fixed = true;
     for (int i = 0; i < ts->num_columns(); ++i)
       if (needed(ts->field(i).name)) {
         fields.push_back(ts->field(i));
-        specs.push_back(GatherSpec{ts->column(i).get(), pidx->as<int32_t>()});
+        pcols.push_back(i);
+        fixed &= ts->field(i).type != DType::Utf8;
       }
     const TupleSet& b = *join->table.build;
     for (int i = 0; i < b.num_columns(); ++i)
@@ -644,9 +643,22 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const ArrowSchema* schema, co
         for (auto& f : fields)
           if (f.name == b.field(i).name) fail(GFPDB_EINVAL, "column '" + f.name + "' is on both join sides");
         fields.push_back(b.field(i));
-        specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
+        bcols.push_back(i);
+        fixed &= b.field(i).type != DType::Utf8;
       }
-    auto cols = gather_columns(specs, n, s);
+    int64_t n = 0;
+    std::vector<ColumnPtr> cols;
+    if (fixed) {
+      // fixed-width outputs: probe and materialise in one kernel
+      cols = join_probe_materialize(join->table, *ts, pk, pcols, bcols, &n, s, nullptr, nullptr);
+    } else {
+      BufferPtr pidx, bidx;
+      join_probe_pairs(join->table, *ts, pk, &pidx, &bidx, &n, s);
+      std::vector<GatherSpec> specs;
+      for (int i : pcols) specs.push_back(GatherSpec{ts->column(i).get(), pidx->as<int32_t>()});
+      for (int i : bcols) specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
+      cols = gather_columns(specs, n, s);
+    }
     export_tupleset(TupleSet::make(std::move(fields), std::move(cols), n), out_schema, out, false, s);
     sync(s);
   });

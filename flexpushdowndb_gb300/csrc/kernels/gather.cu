@@ -32,10 +32,12 @@ __global__ void __launch_bounds__(256) gather_fixed_kernel(const __grid_constant
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     for (int c = 0; c < p.n_cols; ++c) {
       const int32_t i = __ldg(p.idx[c] + r);
+      // streaming (evict-first) stores: the gathered rows should not push
+      // the gathered-from columns out of the L2
       if (p.width[c] == 8) {
-        static_cast<long long*>(p.dst[c])[r] = __ldg(static_cast<const long long*>(p.src[c]) + i);
+        __stcs(static_cast<long long*>(p.dst[c]) + r, __ldg(static_cast<const long long*>(p.src[c]) + i));
       } else {
-        static_cast<int*>(p.dst[c])[r] = __ldg(static_cast<const int*>(p.src[c]) + i);
+        __stcs(static_cast<int*>(p.dst[c]) + r, __ldg(static_cast<const int*>(p.src[c]) + i));
       }
     }
   }

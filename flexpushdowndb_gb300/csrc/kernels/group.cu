@@ -68,14 +68,21 @@ struct GroupParams {
   Program prog;
 };
 
+// A batch's columns are read once: streaming loads (evict-first) leave the
+// L2 to the table, which every row revisits.
+__device__ __forceinline__ int64_t load_int_stream(const DevCol& c, int64_t row) {
+  if (c.type == CT_I64) return __ldcs(static_cast<const long long*>(c.data) + row);
+  return __ldcs(static_cast<const int*>(c.data) + row);
+}
+
 __device__ __forceinline__ uint64_t pack_key(const GroupParams& p, int64_t row) {
   if (p.n_keys == 0) return 0;  // a non-grouped aggregate: one group
   if (p.n_keys == 1) {
-    const int64_t v = load_int(p.key_cols[0], row);
+    const int64_t v = load_int_stream(p.key_cols[0], row);
     return p.key_bits[0] == 64 ? static_cast<uint64_t>(v) : static_cast<uint64_t>(static_cast<uint32_t>(v));
   }
-  const uint32_t a = static_cast<uint32_t>(load_int(p.key_cols[0], row));
-  const uint32_t b = static_cast<uint32_t>(load_int(p.key_cols[1], row));
+  const uint32_t a = static_cast<uint32_t>(load_int_stream(p.key_cols[0], row));
+  const uint32_t b = static_cast<uint32_t>(load_int_stream(p.key_cols[1], row));
   return (static_cast<uint64_t>(a) << 32) | b;
 }
 
@@ -159,6 +166,12 @@ __device__ __forceinline__ uint64_t global_slot(const GroupParams& p, uint64_t k
 
 __device__ __forceinline__ unsigned long long row_value(const GroupParams& p, const AccDev& a, int64_t row) {
   if (a.fn == AGG_COUNT || a.fn == AGG_COUNT_STAR) return 1ull;
+  if (a.in.kind == OPND_COL) {  // a plain column (float64 as its bits), streamed
+    const DevCol& c = p.cols[a.in.col];
+    if (c.type == CT_I64 || c.type == CT_F64)
+      return static_cast<unsigned long long>(__ldcs(static_cast<const long long*>(c.data) + row));
+    return static_cast<unsigned long long>(static_cast<int64_t>(__ldcs(static_cast<const int*>(c.data) + row)));
+  }
   return static_cast<unsigned long long>(operand_row(p.prog, p.cols, a.in, row, p.st));
 }
 

@@ -105,6 +105,13 @@ __device__ __forceinline__ uint64_t group_slot(const ulonglong2& lo, const ulong
   return (q & 2) ? b : a;
 }
 
+// A probe key, streamed (evict-first): each probe row is read once, and the
+// L2 is better spent on the table.
+__device__ __forceinline__ int64_t load_key_stream(const DevCol& c, int64_t row) {
+  if (c.type == CT_I64) return __ldcs(static_cast<const long long*>(c.data) + row);
+  return __ldcs(static_cast<const int*>(c.data) + row);
+}
+
 // The probe loop shared by the pair and the materialising probe.
 //
 // Each warp owns a contiguous range of probe rows and each lane walks one
@@ -142,7 +149,7 @@ __device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const 
 #pragma unroll
   for (int b = 0; b < 4; ++b) {
     const int64_t r = begin + 32 * b + lane;
-    ring[b] = r < end ? load_int(pkey, r) : 0;
+    ring[b] = r < end ? load_key_stream(pkey, r) : 0;
   }
   int taken = 0;  // rows of the ring's first batch already handed out (< 32 between steps)
 
@@ -179,7 +186,7 @@ __device__ __forceinline__ void probe_rows(const DevCol& pkey, int64_t n, const 
         ring[1] = ring[2];
         ring[2] = ring[3];
         const int64_t r = ring_base + 128 + lane;
-        ring[3] = r < end ? load_int(pkey, r) : 0;
+        ring[3] = r < end ? load_key_stream(pkey, r) : 0;
         ring_base += 32;
         taken -= 32;
       }
@@ -241,8 +248,8 @@ __global__ void __launch_bounds__(256)
   auto write = [&](int64_t at, const PairStage& sg, int lane) {
     for (int i = lane; i < sg.n; i += 32)
       if (at + i < cap) {
-        out_p[at + i] = sg.p[i];
-        out_b[at + i] = sg.b[i];
+        __stcs(out_p + at + i, sg.p[i]);
+        __stcs(out_b + at + i, sg.b[i]);
       }
   };
   probe_rows(pkey, n, slots, mask, bkey, key32, reinterpret_cast<unsigned long long*>(&st->value), write);
@@ -271,22 +278,25 @@ struct JoinEmitParams {
   int32_t from_build[kJoinOutMax];
 };
 
-// One column of a flush: eight gathers in flight per lane, then the stores.
+// One column of a flush: eight gathers in flight per lane, then the stores,
+// which stream (evict-first): the output is written once and read by later
+// kernels, while the L2 should keep the hash table and the build columns
+// that the probes and gathers revisit.
 template <class T>
 __device__ __forceinline__ void copy_staged(const T* __restrict__ src, T* __restrict__ dst, const int32_t* idx,
-                                            int n, int64_t at, int64_t cap, int lane) {
+                                            int n, int64_t at, int64_t cap, int lane, bool stream_src) {
   constexpr int kU = 8;
   for (int i0 = 0; i0 < n; i0 += 32 * kU) {
     T v[kU];
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       const int i = i0 + u * 32 + lane;
-      if (i < n) v[u] = __ldg(src + idx[i]);
+      if (i < n) v[u] = stream_src ? __ldcs(src + idx[i]) : __ldg(src + idx[i]);
     }
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       const int i = i0 + u * 32 + lane;
-      if (i < n && at + i < cap) dst[at + i] = v[u];
+      if (i < n && at + i < cap) __stcs(dst + at + i, v[u]);
     }
   }
 }
@@ -296,11 +306,14 @@ __global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_const
   auto write = [&](int64_t at, const PairStage& sg, int lane) {
     for (int c = 0; c < p.n_out; ++c) {
       const int32_t* idx = p.from_build[c] ? sg.b : sg.p;
+      // probe rows are read once (streamed); build rows are revisited
+      const bool stream_src = !p.from_build[c];
       if (p.width[c] == 8)
         copy_staged(static_cast<const long long*>(p.src[c]), static_cast<long long*>(p.dst[c]), idx, sg.n, at, p.cap,
-                    lane);
+                    lane, stream_src);
       else
-        copy_staged(static_cast<const int*>(p.src[c]), static_cast<int*>(p.dst[c]), idx, sg.n, at, p.cap, lane);
+        copy_staged(static_cast<const int*>(p.src[c]), static_cast<int*>(p.dst[c]), idx, sg.n, at, p.cap, lane,
+                    stream_src);
     }
   };
   probe_rows(p.pkey, n, p.slots, p.mask, p.bkey, p.key32, reinterpret_cast<unsigned long long*>(&p.st->value), write);
@@ -364,12 +377,13 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
     at = __shfl_sync(0xffffffffu, at, 0);
     for (int c = 0; c < p.n_out; ++c) {
       const int32_t* idx = s_rows[warp][p.from[c]];
+      const bool stream_src = p.from[c] == 0;  // the input row: read once
       if (p.width[c] == 8)
         copy_staged(static_cast<const long long*>(p.src[c]), static_cast<long long*>(p.dst[c]), idx, staged,
-                    static_cast<int64_t>(at), p.cap, lane);
+                    static_cast<int64_t>(at), p.cap, lane, stream_src);
       else
         copy_staged(static_cast<const int*>(p.src[c]), static_cast<int*>(p.dst[c]), idx, staged,
-                    static_cast<int64_t>(at), p.cap, lane);
+                    static_cast<int64_t>(at), p.cap, lane, stream_src);
     }
     __syncwarp();
     staged = 0;
