@@ -168,6 +168,8 @@ SIGNATURES = {
     "gfpdb_plan_prepare": (_I32, [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A),
                                   ctypes.POINTER(_P)]),
     "gfpdb_prepared_run": (_I32, [_P, ctypes.POINTER(ExecStats), _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "gfpdb_prepared_launch": (_I32, [_P, _P]),
+    "gfpdb_prepared_wait": (_I32, [_P, ctypes.POINTER(ExecStats), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "gfpdb_prepared_layout": (_I32, [_P, _I32, ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.c_char_p, _I64,
                                      ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "gfpdb_prepared_free": (None, [_P]),

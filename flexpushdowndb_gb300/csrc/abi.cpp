@@ -287,7 +287,11 @@ TupleSetPtr device_copy(const TupleSet& r, int64_t n, cudaStream_t s) {
 // One replay: launch, wait, check every status. Returns false when a
 // deferred output overflowed; else *n_rows is the result's row count (its
 // values in cp.pinned).
-bool replay_graph(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t* n_rows) {
+// A replay in two halves: the launch (the graph between two events on the
+// stream) and the finish (wait for the second event, read the statuses the
+// graph packed into page-locked memory). Between them the caller may launch
+// other work, another prepared plan's replay included.
+void replay_launch(CapturedPlan& cp, cudaStream_t s) {
   if (cp.ev[0] == nullptr) {
     GF_CUDA(cudaEventCreate(&cp.ev[0]));
     GF_CUDA(cudaEventCreate(&cp.ev[1]));
@@ -296,6 +300,11 @@ bool replay_graph(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t*
   GF_CUDA(cudaGraphLaunch(cp.exec, s));
   GF_CUDA(cudaEventRecord(cp.ev[1], s));
   count_launch(cp.kernels);
+}
+
+// False when a deferred size overflowed: the caller re-runs the plan with
+// exact sizes.
+bool replay_finish(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t* n_rows) {
   // A replay is short: poll its end instead of sleeping in a blocking wait,
   // which would add the thread's wake-up to every query; after about two
   // milliseconds fall back to the blocking wait.
@@ -328,6 +337,11 @@ bool replay_graph(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t*
   if (n < 0 || n > r.num_rows()) fail(GFPDB_EDEVICE, "captured plan produced an out-of-range row count");
   *n_rows = n;
   return true;
+}
+
+bool replay_graph(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t* n_rows) {
+  replay_launch(cp, s);
+  return replay_finish(cp, s, device_ns, n_rows);
 }
 
 bool replay_plan(CapturedPlan& cp, bool to_host, ArrowSchema* out_schema, ArrowDeviceArray* out, cudaStream_t s,
@@ -367,6 +381,20 @@ struct gfpdb_prepared {
   bool has_res = false;
   bool last_replay = false;
   int64_t generation = 0;
+  // a launched run not yet waited for: none, a graph replay in flight, or a
+  // run that completed inside the launch (the first runs, an uncaptured plan)
+  enum Pending { kNone, kReplay, kDone } pending = kNone;
+  void* stream = nullptr;
+  std::chrono::steady_clock::time_point t0;
+  gfpdb_exec_stats done_stats{};
+  int64_t rows = 0;
+
+  void find_capture() {
+    if (!graph || cp) return;
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    auto it = g_graphs.find(key);
+    if (it != g_graphs.end()) cp = it->second;
+  }
 
   void release_result() {
     if (!has_res) return;
@@ -1011,24 +1039,58 @@ int32_t gfpdb_plan_prepare(const char* plan_json, int32_t n_tables, const char* 
   });
 }
 
-int32_t gfpdb_prepared_run(gfpdb_prepared* p, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows,
-                           int64_t* layout_generation) {
+}  // extern "C"
+
+namespace {
+
+// An ordinary (non-replay) run of a prepared plan: its result is exported
+// into the prepared plan's host buffers; afterwards the plan's capture, if
+// one was made, is picked up for later launches.
+void run_prepared_exact(gfpdb_prepared* p, gfpdb_exec_stats* stats) {
+  p->release_result();
+  const int32_t code = gfpdb_execute_plan(p->plan.c_str(), static_cast<int32_t>(p->names.size()),
+                                          p->name_ptrs.data(), p->schemas.data(), p->arrays.data(), 1, &p->res_s,
+                                          &p->res_a, stats, p->stream);
+  if (code != GFPDB_OK) fail(code, std::string(gfpdb_last_error()));
+  p->has_res = true;
+  p->last_replay = false;
+  ++p->generation;
+  p->rows = p->res_a.array.length;
+  p->find_capture();
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gfpdb_prepared_launch(gfpdb_prepared* p, void* stream) {
+  return guarded([&] {
+    require(p != nullptr, "null argument");
+    require(p->pending == gfpdb_prepared::kNone, "the prepared plan's last launch has not been waited for");
+    p->t0 = std::chrono::steady_clock::now();
+    p->stream = stream;
+    p->find_capture();
+    if (p->cp && p->cp->capturable) {
+      replay_launch(*p->cp, as_stream(stream));
+      p->pending = gfpdb_prepared::kReplay;
+      return;
+    }
+    // the first runs (an ordinary run, then the capture) and plans without
+    // a graph complete here
+    run_prepared_exact(p, &p->done_stats);
+    p->pending = gfpdb_prepared::kDone;
+  });
+}
+
+int32_t gfpdb_prepared_wait(gfpdb_prepared* p, gfpdb_exec_stats* stats, int64_t* n_rows, int64_t* layout_generation) {
   return guarded([&] {
     require(p != nullptr && n_rows != nullptr && layout_generation != nullptr, "null argument");
-    const auto t0 = std::chrono::steady_clock::now();
-    cudaStream_t s = as_stream(stream);
-    auto find_capture = [&] {
-      if (!p->graph || p->cp) return;
-      std::lock_guard<std::mutex> lk(g_graph_mu);
-      auto it = g_graphs.find(p->key);
-      if (it != g_graphs.end()) p->cp = it->second;
-    };
-    find_capture();
-    if (p->cp && p->cp->capturable) {
-      const CopyCounters c0 = copy_counters();
-      const uint64_t launches0 = g_kernel_launches.load();
+    require(p->pending != gfpdb_prepared::kNone, "no launched run to wait for");
+    const auto kind = p->pending;
+    p->pending = gfpdb_prepared::kNone;
+    if (kind == gfpdb_prepared::kReplay) {
       int64_t device_ns = 0, n = 0;
-      if (replay_graph(*p->cp, s, &device_ns, &n)) {
+      if (replay_finish(*p->cp, as_stream(p->stream), &device_ns, &n)) {
         p->release_result();
         if (!p->last_replay) {
           ++p->generation;
@@ -1037,32 +1099,33 @@ int32_t gfpdb_prepared_run(gfpdb_prepared* p, gfpdb_exec_stats* stats, void* str
         *n_rows = n;
         *layout_generation = p->generation;
         if (stats != nullptr) {
-          stats->kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
-          stats->h2d_bytes = copy_counters().h2d - c0.h2d;
-          stats->d2h_bytes = copy_counters().d2h - c0.d2h;
+          // this replay's own figures (the process-wide counters would also
+          // count another prepared plan's replay launched in between)
+          stats->kernel_launches = static_cast<int64_t>(p->cp->kernels);
+          stats->h2d_bytes = p->cp->h2d;
+          stats->d2h_bytes = p->cp->pinned_bytes;
           stats->num_ops = p->cp->num_ops;
           stats->messages = p->cp->messages;
           stats->device_ns = device_ns;
           stats->elapsed_ns =
-              std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+              std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - p->t0).count();
         }
         return;
       }
+      // a deferred size overflowed: run once more with exact sizes
+      run_prepared_exact(p, &p->done_stats);
     }
-    // the first runs (an ordinary run, then the capture), plans without a
-    // graph, and a replay that overflowed (re-run with exact sizes)
-    p->release_result();
-    const int32_t code = gfpdb_execute_plan(p->plan.c_str(), static_cast<int32_t>(p->names.size()),
-                                            p->name_ptrs.data(), p->schemas.data(), p->arrays.data(), 1, &p->res_s,
-                                            &p->res_a, stats, stream);
-    if (code != GFPDB_OK) fail(code, std::string(gfpdb_last_error()));
-    p->has_res = true;
-    p->last_replay = false;
-    ++p->generation;
-    *n_rows = p->res_a.array.length;
+    if (stats != nullptr) *stats = p->done_stats;
+    *n_rows = p->rows;
     *layout_generation = p->generation;
-    find_capture();
   });
+}
+
+int32_t gfpdb_prepared_run(gfpdb_prepared* p, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows,
+                           int64_t* layout_generation) {
+  const int32_t code = gfpdb_prepared_launch(p, stream);
+  if (code != GFPDB_OK) return code;
+  return gfpdb_prepared_wait(p, stats, n_rows, layout_generation);
 }
 
 int32_t gfpdb_prepared_layout(const gfpdb_prepared* p, int32_t max_columns, int64_t* capacity, int32_t* n_columns,

@@ -165,9 +165,12 @@ class PreparedPlan:
         _abi.check(L.gfpdb_plan_prepare(self.text, len(inp.names), inp.c_names, inp.c_schemas, inp.c_arrays,
                                         ctypes.byref(self._h)))
         self._run, self._layout, self._free = L.gfpdb_prepared_run, L.gfpdb_prepared_layout, L.gfpdb_prepared_free
+        self._launch, self._wait = L.gfpdb_prepared_launch, L.gfpdb_prepared_wait
         self._stats = _abi.ExecStats()
         self._n, self._gen = ctypes.c_int64(), ctypes.c_int64()
         self._args = (self._h, ctypes.byref(self._stats), stream, ctypes.byref(self._n), ctypes.byref(self._gen))
+        self._launch_args = (self._h, stream)
+        self._wait_args = (self._h, ctypes.byref(self._stats), ctypes.byref(self._n), ctypes.byref(self._gen))
         self._seen_gen = -1
         self._cols = []  # per column: (name, type, values view or None, offsets view or None, data pointer)
 
@@ -195,6 +198,20 @@ class PreparedPlan:
 
     def execute(self) -> Result:
         _abi.check(self._run(*self._args))
+        return self._result()
+
+    def launch(self) -> None:
+        """Start a run and return (gfpdb_prepared_launch); wait() finishes
+        it. Two prepared plans of one query whose texts differ in
+        "graphInstance" can be launched back to back, each waited for while
+        the other runs."""
+        _abi.check(self._launch(*self._launch_args))
+
+    def wait(self) -> Result:
+        _abi.check(self._wait(*self._wait_args))
+        return self._result()
+
+    def _result(self) -> Result:
         if self._gen.value != self._seen_gen:
             self._refresh()
         n = self._n.value

@@ -324,6 +324,17 @@ int32_t gfpdb_plan_prepare(const char* plan_json, int32_t n_tables, const char* 
                            const struct ArrowDeviceArray* const* arrays, gfpdb_prepared** out);
 int32_t gfpdb_prepared_run(gfpdb_prepared* plan, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows,
                            int64_t* layout_generation);
+/* gfpdb_prepared_run in two halves. launch starts the run on the stream and
+ * returns; a replay is then in flight (the first runs, and plans without a
+ * graph, complete inside launch). wait finishes it and reports as
+ * gfpdb_prepared_run does. Between them the caller may launch other work:
+ * two prepared plans of one query, whose texts differ only in a
+ * "graphInstance" number (so that each captures its own graph, scratch and
+ * result buffers), can run back to back on one stream while the host reads
+ * the other's result. One launch at a time per prepared plan. */
+int32_t gfpdb_prepared_launch(gfpdb_prepared* plan, void* stream);
+int32_t gfpdb_prepared_wait(gfpdb_prepared* plan, gfpdb_exec_stats* stats, int64_t* n_rows,
+                            int64_t* layout_generation);
 /* As gfpdb_result_layout for the last run's result, plus its row capacity
  * (the length the buffers can hold: the most rows any run with this layout
  * generation can return). */

@@ -296,6 +296,41 @@ def test_prepared_plan_matches_execute(gpu, graph):
         assert got.names == want.names
         assert got.sorted_rows() == want.sorted_rows()
 
+def test_prepared_plans_launched_back_to_back(gpu):
+    """Two prepared plans of the star query (graph instances 0 and 1, so each
+    has its own capture) launched alternately on one stream, each waited for
+    while the other runs: every result, through the first runs, the captures
+    and the replays, matches the oracle; a second launch before the wait and
+    a wait without a launch are errors."""
+    from flexpushdowndb_gb300 import _abi
+
+    tabs = workloads.star_tables(fact_rows=300_000, seed=43)
+    want = queries.star_query(tabs).sorted_rows()
+    inputs = plan.PreparedInputs(tabs)
+    base = json.loads(_with_options(workloads.star_plan(), cudaGraph=True))
+    pps = [plan.PreparedPlan(json.dumps(dict(base, graphInstance=i)), inputs) for i in (0, 1)]
+    pps[0].launch()
+    for k in range(1, 9):
+        pps[k % 2].launch()
+        r = pps[(k - 1) % 2].wait()
+        assert r.table.sorted_rows() == want
+    r = pps[0].wait()
+    assert r.table.sorted_rows() == want
+    assert r.stats["device_ns"] > 0  # a replay
+    # a replay's stats are its own, not the other instance's as well
+    alone = plan.PreparedPlan(json.dumps(dict(base, graphInstance=2)), inputs)
+    for _ in range(3):
+        r_alone = alone.execute()
+    for k in ("kernel_launches", "h2d_bytes", "d2h_bytes", "num_ops"):
+        assert r.stats[k] == r_alone.stats[k], k
+    pps[1].launch()
+    with pytest.raises(_abi.GfpdbError):
+        pps[1].launch()
+    assert pps[1].wait().table.sorted_rows() == want
+    with pytest.raises(_abi.GfpdbError):
+        pps[1].wait()
+
+
 def test_prepared_star_plan_through_capture_and_replays(gpu):
     """A prepared star plan: the first runs take the ordinary path (run,
     then capture), later ones replay the graph; every result matches the
