@@ -851,19 +851,28 @@ __global__ void __launch_bounds__(kLiteThreads) select_lite_kernel(const __grid_
     const int64_t base = static_cast<int64_t>(s_base);
     if (mask != 0) {
       const int64_t out0 = base + excl;
+      // four output columns at a time: their loads (16-byte vectors on full
+      // groups) in flight together, then the compacted stores
 #pragma unroll 1
-      for (int j = 0; j < p.n_out; ++j) {
-        const LiteOut& oc = p.outs[j];
-        int o = 0;
-        if (oc.width == 8) {
+      for (int j0 = 0; j0 < p.n_out; j0 += 4) {
+        int64_t v[4][kLiteItems];
 #pragma unroll
-          for (int k = 0; k < kLiteItems; ++k)
-            if ((mask >> k) & 1u)
-              static_cast<long long*>(oc.dst)[out0 + o++] = __ldg(static_cast<const long long*>(oc.src) + row0 + k);
-        } else {
+        for (int jj = 0; jj < 4; ++jj)
+          if (j0 + jj < p.n_out) lite_load4(p.outs[j0 + jj].src, p.outs[j0 + jj].width == 8, row0, mask, full, v[jj]);
 #pragma unroll
-          for (int k = 0; k < kLiteItems; ++k)
-            if ((mask >> k) & 1u) static_cast<int*>(oc.dst)[out0 + o++] = __ldg(static_cast<const int*>(oc.src) + row0 + k);
+        for (int jj = 0; jj < 4; ++jj) {
+          if (j0 + jj >= p.n_out) break;
+          const LiteOut& oc = p.outs[j0 + jj];
+          int o = 0;
+          if (oc.width == 8) {
+#pragma unroll
+            for (int k = 0; k < kLiteItems; ++k)
+              if ((mask >> k) & 1u) static_cast<long long*>(oc.dst)[out0 + o++] = v[jj][k];
+          } else {
+#pragma unroll
+            for (int k = 0; k < kLiteItems; ++k)
+              if ((mask >> k) & 1u) static_cast<int*>(oc.dst)[out0 + o++] = static_cast<int>(v[jj][k]);
+          }
         }
       }
       if (p.out_rowids != nullptr) {
@@ -905,6 +914,7 @@ bool lite_params(const SelectParams& p, LiteParams& lp) {
   if (p.n_out > kLiteMaxOut) return false;
   lp.n_out = p.n_out;
   for (int j = 0; j < p.n_out; ++j) {
+    if (!aligned(p.outs[j].src)) return false;  // read with 16-byte vectors
     lp.outs[j].src = p.outs[j].src;
     lp.outs[j].dst = p.outs[j].dst;
     lp.outs[j].width = p.outs[j].width;
