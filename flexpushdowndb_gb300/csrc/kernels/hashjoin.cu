@@ -320,8 +320,10 @@ __global__ void __launch_bounds__(256) join_probe_emit_kernel(const __grid_const
 }
 
 // A chain of joins in one pass. Each lane walks its input row through the
-// levels like a depth-first search: at its current level it reads one slot
-// per step; a match at an inner level moves it to the next level (whose key
+// levels like a depth-first search: at its current level it reads, per
+// step, the aligned four-slot group holding its run's next slot (and knows
+// the run is over, without another read, when an empty slot follows the
+// match in that group); a match at an inner level moves it to the next level (whose key
 // comes from the input row or an earlier match), a match at the last level
 // emits an output row, and the end of a run returns it to the level before,
 // whose run it continues. The warp steps together so that emitted rows can
@@ -396,6 +398,7 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
     int64_t key[kJoinChainMax];
     uint32_t tag[kJoinChainMax];
     int lvl = 0;
+    uint32_t ended = 0;  // levels whose run is known to have ended
     rows[0] = r;
     auto start_level = [&](int l) {
       const ChainLevel& L = p.lv[l];
@@ -407,30 +410,69 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
       tag[l] = L.key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
       slot[l] = h & L.mask;
       steps[l] = 0;
+      ended &= ~(1u << l);
     };
     if (active) start_level(0);
     while (__any_sync(0xffffffffu, active)) {
       bool emit = false;
       if (active) {
         const ChainLevel& L = p.lv[lvl];
-        const uint64_t sv = __ldg(reinterpret_cast<const unsigned long long*>(L.slots + slot[lvl]));
-        if (sv == kEmptySlot || ++steps[lvl] > L.mask + 1) {
-          if (lvl == 0) active = false;  // the input row is done
-          else --lvl;                    // back to the previous level's run
-        } else {
-          slot[lvl] = (slot[lvl] + 1) & L.mask;
-          if (static_cast<uint32_t>(sv >> 32) == tag[lvl]) {
-            const int32_t brow = static_cast<int32_t>(static_cast<uint32_t>(sv));
-            if (L.key32 || load_int(L.bkey, brow) == key[lvl]) {
-              rows[lvl + 1] = brow;
-              if (lvl == p.n_levels - 1) {
-                emit = true;  // and the last level's run continues next step
-              } else {
-                ++lvl;
-                start_level(lvl);
-              }
+        bool run_over = (ended >> lvl & 1u) != 0;
+        if (!run_over) {
+          // the aligned four-slot group (one sector) holding the run's next
+          // slot: the first match at or after it that precedes an empty slot
+          const uint64_t s0 = slot[lvl];
+          const int q0 = static_cast<int>(s0 & 3);
+          const uint64_t g = s0 & ~3ull;
+          const ulonglong2* gp = reinterpret_cast<const ulonglong2*>(L.slots + g);
+          const ulonglong2 lo = __ldg(gp), hi = __ldg(gp + 1);
+          uint32_t eb = 0, tb = 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const uint64_t v = group_slot(lo, hi, q);
+            if (v == kEmptySlot)
+              eb |= 1u << q;
+            else if (static_cast<uint32_t>(v >> 32) == tag[lvl])
+              tb |= 1u << q;
+          }
+          const uint32_t from = (0xFu << q0) & 0xFu;
+          eb &= from;
+          const int stop = eb ? __ffs(eb) - 1 : 4;
+          tb &= from & ((1u << stop) - 1u);
+          int m = -1;
+          int32_t brow = 0;
+          for (; tb != 0; tb &= tb - 1) {
+            const int q = __ffs(tb) - 1;
+            const int32_t b = static_cast<int32_t>(static_cast<uint32_t>(group_slot(lo, hi, q)));
+            if (L.key32 || load_int(L.bkey, b) == key[lvl]) {
+              m = q;
+              brow = b;
+              break;
             }
           }
+          steps[lvl] += static_cast<uint64_t>(4 - q0);
+          if (m >= 0) {
+            slot[lvl] = (g + m + 1) & L.mask;
+            // the run ends in this group when an empty slot follows the
+            // match with no other candidate (a repeated key) before it; tb
+            // still holds the match and the candidates after it
+            if (eb != 0 && (tb >> (m + 1)) == 0) ended |= 1u << lvl;
+            rows[lvl + 1] = brow;
+            if (lvl == p.n_levels - 1) {
+              emit = true;  // and the last level's run continues next step
+            } else {
+              ++lvl;
+              start_level(lvl);
+            }
+          } else if (eb != 0 || steps[lvl] > L.mask + 1) {
+            run_over = true;
+          } else {
+            slot[lvl] = (g + 4) & L.mask;
+          }
+        }
+        if (run_over) {
+          if (lvl == 0) active = false;  // the input row is done
+          else --lvl;                    // back to the previous level's run
         }
       }
       const uint32_t em = __ballot_sync(0xffffffffu, emit);
@@ -449,12 +491,28 @@ __global__ void __launch_bounds__(256) join_chain_kernel(const __grid_constant__
         if (emit) {
           const int64_t pos = static_cast<int64_t>(at) + __popc(em & ((1u << lane) - 1u));
           if (pos < p.cap) {
-            for (int c = 0; c < p.n_out; ++c) {
-              const int64_t from = rows[p.from[c]];
-              if (p.width[c] == 8)
-                static_cast<long long*>(p.dst[c])[pos] = __ldg(static_cast<const long long*>(p.src[c]) + from);
-              else
-                static_cast<int*>(p.dst[c])[pos] = __ldg(static_cast<const int*>(p.src[c]) + from);
+            // four output columns per round: their gathers in flight
+            // together, then the stores
+            for (int c0 = 0; c0 < p.n_out; c0 += 4) {
+              long long v[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                const int c = c0 + j;
+                if (c < p.n_out) {
+                  const int64_t from = rows[p.from[c]];
+                  v[j] = p.width[c] == 8 ? __ldg(static_cast<const long long*>(p.src[c]) + from)
+                                         : static_cast<long long>(__ldg(static_cast<const int*>(p.src[c]) + from));
+                }
+              }
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                const int c = c0 + j;
+                if (c >= p.n_out) break;
+                if (p.width[c] == 8)
+                  static_cast<long long*>(p.dst[c])[pos] = v[j];
+                else
+                  static_cast<int*>(p.dst[c])[pos] = static_cast<int>(v[j]);
+              }
             }
           }
         }
