@@ -145,3 +145,14 @@ def test_result_layout_of_an_exported_table():
                                  ctypes.byref(dev), names, 4096, vals, offs) == _abi.GFPDB_EINVAL
     assert L.gfpdb_result_layout(ex.schema_ptr, ex.array_ptr, 8, ctypes.byref(n), ctypes.byref(nc),
                                  ctypes.byref(dev), names, 4, vals, offs) == _abi.GFPDB_EINVAL
+
+
+def test_prepared_launch_and_wait_argument_errors():
+    """The prepared plan's launch / wait halves check their arguments before
+    touching a device: null handles and outputs are EINVAL."""
+    L = _abi.lib()
+    n, gen = ctypes.c_int64(), ctypes.c_int64()
+    assert L.gfpdb_prepared_launch(None, None) == _abi.GFPDB_EINVAL
+    assert L.gfpdb_prepared_wait(None, None, ctypes.byref(n), ctypes.byref(gen)) == _abi.GFPDB_EINVAL
+    assert L.gfpdb_prepared_run(None, None, None, ctypes.byref(n), ctypes.byref(gen)) == _abi.GFPDB_EINVAL
+    assert b"null" in L.gfpdb_last_error()

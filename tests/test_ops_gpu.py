@@ -131,6 +131,26 @@ def test_join_parity(gpu, build_n, probe_n, dup):
     assert got.sorted_rows() == want.sorted_rows()
 
 
+@pytest.mark.parametrize("build_n,probe_n,dup", [(1000, 50_000, 1), (6000, 400_000, 3), (300_000, 2_000_000, 2)])
+def test_join_fixed_width_outputs_fused_probe(gpu, build_n, probe_n, dup):
+    # only fixed-width outputs: the probe materialises them in one kernel
+    # (staged per warp, one cursor atomic per run), repeated build keys
+    # included
+    rng = np.random.default_rng(build_n + probe_n + dup)
+    bkeys = np.repeat(np.arange(build_n // dup, dtype=np.int64), dup)[:build_n]
+    build = Table([Column("pk", "int32", bkeys), Column("bv", "int64", rng.integers(0, 10**9, len(bkeys)))])
+    probe = Table([Column("fk", "int32", rng.integers(-5, build_n // dup + 5, probe_n)),
+                   Column("pv", "int32", rng.integers(0, 100, probe_n))])
+    j = ops.HashJoin("pk", "fk")
+    j.put_build(build)
+    j.finalize_build()
+    got = j.probe(DeviceTable.from_host(probe))
+    want = oops.hash_join(build, probe, "pk", "fk")
+    assert got.names == want.names == ["fk", "pv", "pk", "bv"]
+    assert got.num_rows == want.num_rows
+    assert got.sorted_rows() == want.sorted_rows()
+
+
 def test_join_int64_keys_and_multiple_build_batches(gpu):
     rng = np.random.default_rng(5)
     b1 = Table([Column("k", "int64", rng.integers(-2**40, 2**40, 3000)), Column("x", "int32", np.arange(3000))])
@@ -185,6 +205,24 @@ def test_group_sketch_sized_table_two_batches(gpu):
     got = g.finalise()
     allt = Table([Column(c, "int64", np.concatenate([p[c] for p in parts])) for c in ("g", "v")])
     want = oops.group_by(allt, ["g"], aggs)
+    assert got.num_rows == want.num_rows
+    assert got.sorted_rows() == want.sorted_rows()
+
+
+def test_group_sketch_sized_table_two_int32_keys(gpu):
+    # two int32 key columns packed into one 64-bit key, a batch large enough
+    # for the sketch-sized table, with MIN / MAX accumulators (which need the
+    # table's init kernel rather than pre-filled memory)
+    rng = np.random.default_rng(78)
+    n = 2_300_000
+    t = Table([Column("a", "int32", rng.integers(-700, 700, n)), Column("b", "int32", rng.integers(0, 1500, n)),
+               Column("v", "int64", rng.integers(-10**9, 10**9, n))])
+    aggs = [{"function": "SUM", "name": "s", "expr": col("v")}, {"function": "MIN", "name": "mn", "expr": col("v")},
+            {"function": "MAX", "name": "mx", "expr": col("v")}, {"function": "COUNT", "name": "c"}]
+    g = ops.Group(["a", "b"], aggs)
+    g.group(DeviceTable.from_host(t))
+    got = g.finalise()
+    want = oops.group_by(t, ["a", "b"], aggs)
     assert got.num_rows == want.num_rows
     assert got.sorted_rows() == want.sorted_rows()
 
