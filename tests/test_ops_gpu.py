@@ -131,7 +131,7 @@ def test_join_parity(gpu, build_n, probe_n, dup):
     assert got.sorted_rows() == want.sorted_rows()
 
 
-@pytest.mark.parametrize("build_n,probe_n,dup", [(1000, 50_000, 1), (6000, 400_000, 3), (300_000, 2_000_000, 2)])
+@pytest.mark.parametrize("build_n,probe_n,dup", [(1000, 50_000, 1), (6000, 400_000, 3), (300_000, 1_200_000, 2)])
 def test_join_fixed_width_outputs_fused_probe(gpu, build_n, probe_n, dup):
     # only fixed-width outputs: the probe materialises them in one kernel
     # (staged per warp, one cursor atomic per run), repeated build keys
