@@ -10,8 +10,10 @@
 // linear probing. For 32-bit keys the tag is the key itself, so a probe
 // decides a match from the slot alone; for 64-bit keys the tag is the high
 // half of the hash and a tag hit is confirmed against the build key column.
-// Duplicate build keys occupy separate slots (multimap semantics). Probing
-// is one thread per probe row walking its run. Matches collect per warp in
+// Duplicate build keys occupy separate slots (multimap semantics). Probing:
+// a lane walks one probe row's run at a time, reading per step the aligned
+// four-slot group (one sector) that holds the run's next slot, and takes the
+// warp's next row as soon as its run ends. Matches collect per warp in
 // shared memory and leave in runs of up to kStage pairs, each run taking its
 // output positions with one atomic on the shared cursor: the cursor is a
 // single address whose atomics the L2 serialises, so one atomic per warp
