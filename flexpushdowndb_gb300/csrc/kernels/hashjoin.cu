@@ -280,14 +280,14 @@ struct JoinEmitParams {
   int32_t from_build[kJoinOutMax];
 };
 
-// One column of a flush: eight gathers in flight per lane, then the stores,
+// One column of a flush: four gathers in flight per lane, then the stores,
 // which stream (evict-first): the output is written once and read by later
 // kernels, while the L2 should keep the hash table and the build columns
 // that the probes and gathers revisit.
 template <class T>
 __device__ __forceinline__ void copy_staged(const T* __restrict__ src, T* __restrict__ dst, const int32_t* idx,
                                             int n, int64_t at, int64_t cap, int lane, bool stream_src) {
-  constexpr int kU = 8;
+  constexpr int kU = 4;
   for (int i0 = 0; i0 < n; i0 += 32 * kU) {
     T v[kU];
 #pragma unroll
