@@ -1171,7 +1171,14 @@ int32_t gfpdb_prepared_layout(const gfpdb_prepared* p, int32_t max_columns, int6
   });
 }
 
-void gfpdb_prepared_free(gfpdb_prepared* p) { delete p; }
+void gfpdb_prepared_free(gfpdb_prepared* p) {
+  if (p == nullptr) return;
+  // a replay launched and never waited for: let it finish before its
+  // captured plan (scratch, result buffers) can go with this handle
+  if (p->pending == gfpdb_prepared::kReplay && p->cp && p->cp->ev[1] != nullptr)
+    (void)cudaEventSynchronize(p->cp->ev[1]);
+  delete p;
+}
 
 int32_t gfpdb_plan_validate(const char* plan_json) {
   return guarded([&] {

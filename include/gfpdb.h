@@ -331,7 +331,8 @@ int32_t gfpdb_prepared_run(gfpdb_prepared* plan, gfpdb_exec_stats* stats, void* 
  * two prepared plans of one query, whose texts differ only in a
  * "graphInstance" number (so that each captures its own graph, scratch and
  * result buffers), can run back to back on one stream while the host reads
- * the other's result. One launch at a time per prepared plan. */
+ * the other's result. One launch at a time per prepared plan; freeing a
+ * prepared plan waits for a launch that was not waited for. */
 int32_t gfpdb_prepared_launch(gfpdb_prepared* plan, void* stream);
 int32_t gfpdb_prepared_wait(gfpdb_prepared* plan, gfpdb_exec_stats* stats, int64_t* n_rows,
                             int64_t* layout_generation);
