@@ -55,6 +55,7 @@ struct CapturedPlan {
   TupleSetPtr result;
   std::vector<DeferredCheck> checks;
   uint64_t kernels = 0;
+  bool in_flight = false;  // launched and not yet finished
   int64_t num_ops = 0, messages = 0, h2d = 0;
   bool capturable = true;
   cudaEvent_t ev[2] = {nullptr, nullptr};  // around a replay: its device time
@@ -292,6 +293,10 @@ TupleSetPtr device_copy(const TupleSet& r, int64_t n, cudaStream_t s) {
 // graph packed into page-locked memory). Between them the caller may launch
 // other work, another prepared plan's replay included.
 void replay_launch(CapturedPlan& cp, cudaStream_t s) {
+  // one replay of a captured plan at a time: a second would share its
+  // scratch, result buffers and events
+  if (cp.in_flight)
+    fail(GFPDB_EINVAL, "this captured plan is already running; prepare the second copy with another \"graphInstance\"");
   if (cp.ev[0] == nullptr) {
     GF_CUDA(cudaEventCreate(&cp.ev[0]));
     GF_CUDA(cudaEventCreate(&cp.ev[1]));
@@ -299,6 +304,7 @@ void replay_launch(CapturedPlan& cp, cudaStream_t s) {
   GF_CUDA(cudaEventRecord(cp.ev[0], s));
   GF_CUDA(cudaGraphLaunch(cp.exec, s));
   GF_CUDA(cudaEventRecord(cp.ev[1], s));
+  cp.in_flight = true;
   count_launch(cp.kernels);
 }
 
@@ -320,6 +326,7 @@ bool replay_finish(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t
       }
     }
   }
+  cp.in_flight = false;
   float ms = 0;
   GF_CUDA(cudaEventElapsedTime(&ms, cp.ev[0], cp.ev[1]));
   *device_ns = static_cast<int64_t>(static_cast<double>(ms) * 1e6);
@@ -1175,8 +1182,10 @@ void gfpdb_prepared_free(gfpdb_prepared* p) {
   if (p == nullptr) return;
   // a replay launched and never waited for: let it finish before its
   // captured plan (scratch, result buffers) can go with this handle
-  if (p->pending == gfpdb_prepared::kReplay && p->cp && p->cp->ev[1] != nullptr)
+  if (p->pending == gfpdb_prepared::kReplay && p->cp && p->cp->ev[1] != nullptr) {
     (void)cudaEventSynchronize(p->cp->ev[1]);
+    p->cp->in_flight = false;
+  }
   delete p;
 }
 

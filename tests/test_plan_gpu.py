@@ -329,6 +329,15 @@ def test_prepared_plans_launched_back_to_back(gpu):
     assert pps[1].wait().table.sorted_rows() == want
     with pytest.raises(_abi.GfpdbError):
         pps[1].wait()
+    # the same text prepared twice shares one capture: while one copy's
+    # replay is in flight the other's launch is refused, not overlapped
+    twin = plan.PreparedPlan(json.dumps(dict(base, graphInstance=0)), inputs)
+    pps[0].launch()
+    with pytest.raises(_abi.GfpdbError) as ei:
+        twin.launch()
+    assert "graphInstance" in ei.value.message
+    assert pps[0].wait().table.sorted_rows() == want
+    assert twin.execute().table.sorted_rows() == want
 
 
 def test_prepared_star_plan_through_capture_and_replays(gpu):
