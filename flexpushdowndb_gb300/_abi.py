@@ -126,6 +126,7 @@ SIGNATURES = {
     "gfpdb_version": (_I32, []),
     "gfpdb_device_init": (_I32, [_I32]),
     "gfpdb_kernel_launch_count": (ctypes.c_uint64, []),
+    "gfpdb_thread_device_alloc_bytes": (_I64, []),
     "gfpdb_memcpy": (_I32, [_P, _P, _I64, _I32, _P]),
     "gfpdb_result_layout": (_I32, [_S, _A, _I32, ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.POINTER(_I32),
                                    ctypes.c_char_p, _I64, ctypes.POINTER(_P), ctypes.POINTER(_P)]),

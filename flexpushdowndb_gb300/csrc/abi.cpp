@@ -311,6 +311,13 @@ void replay_launch(CapturedPlan& cp, cudaStream_t s) {
 // False when a deferred size overflowed: the caller re-runs the plan with
 // exact sizes.
 bool replay_finish(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t* n_rows) {
+  // The replay is over for the plan's bookkeeping on every exit, a failed
+  // completion query included: a later launch must not be refused as
+  // "already running".
+  struct InFlightReset {
+    CapturedPlan& cp;
+    ~InFlightReset() { cp.in_flight = false; }
+  } in_flight_reset{cp};
   // A replay is short: poll its end instead of sleeping in a blocking wait,
   // which would add the thread's wake-up to every query; after about two
   // milliseconds fall back to the blocking wait.
@@ -326,7 +333,6 @@ bool replay_finish(CapturedPlan& cp, cudaStream_t s, int64_t* device_ns, int64_t
       }
     }
   }
-  cp.in_flight = false;
   float ms = 0;
   GF_CUDA(cudaEventElapsedTime(&ms, cp.ev[0], cp.ev[1]));
   *device_ns = static_cast<int64_t>(static_cast<double>(ms) * 1e6);
@@ -426,6 +432,8 @@ int32_t gfpdb_device_init(int32_t device) {
 }
 
 uint64_t gfpdb_kernel_launch_count(void) { return g_kernel_launches.load(); }
+
+int64_t gfpdb_thread_device_alloc_bytes(void) { return thread_alloc_bytes(); }
 
 int32_t gfpdb_result_layout(const ArrowSchema* schema, const ArrowDeviceArray* array, int32_t max_columns,
                             int64_t* n_rows, int32_t* n_columns, int32_t* device_type, char* names,

@@ -1176,10 +1176,13 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
 // ---------------------------------------------------------------------------
 // Filter evaluation that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc at all: code running while a CUDA graph
-// is being captured, engines that hand the library a fixed arena and forbid
-// it from growing the device heap, and embedders whose allocator is owned by
-// another runtime. For them gfpdb_filter_evaluate_noalloc runs the same
+// Some callers cannot call cudaMalloc at all: engines that hand the library
+// a fixed device arena and account for every byte of HBM themselves (a
+// cudaMalloc would grow the device heap behind their back and can fail or
+// stall while they hold the rest of the memory), and embedders whose device
+// memory belongs to another runtime's allocator (a second allocator in the
+// same process fragments and double-counts the pool). For them
+// gfpdb_filter_evaluate_noalloc runs the same
 // select_kernel with its scratch (the call's status block, the tile ticket
 // and one look-back word per 2048-row tile) in the file-scope array below
 // instead of a per-call allocation. The array is sized for
@@ -1240,12 +1243,28 @@ extern "C" int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, con
     if (in->device_type != ARROW_DEVICE_CUDA)
       fail(GFPDB_EINVAL, "gfpdb_filter_evaluate_noalloc needs device-resident input (ARROW_DEVICE_CUDA)");
     const ArrowArray& arr = in->array;
+    if (arr.release == nullptr) fail(GFPDB_EINVAL, "released ArrowArray");
     if (arr.n_children != in_schema->n_children) fail(GFPDB_EINVAL, "ArrowArray child count does not match the schema");
     const int64_t n = arr.length;
-    if (n < 0) fail(GFPDB_EINVAL, "negative row count");
+    if (n < 0 || arr.offset < 0) fail(GFPDB_EINVAL, "negative row count or offset");
     if (n > kNoAllocMaxRows)
       fail(GFPDB_EINVAL, "gfpdb_filter_evaluate_noalloc: " + std::to_string(n) + " rows exceed its maximum of " +
                              std::to_string(kNoAllocMaxRows) + " rows");
+    if (arr.null_count > 0) fail(GFPDB_EUNSUPPORTED, "struct-level nulls are not supported");
+    // The checks import_tupleset makes for gfpdb_filter_evaluate, on every
+    // column the call reads: long enough for the struct's offset + length,
+    // the buffer count of its type, no nulls.
+    auto bound_child = [&](int ci, DType t, const std::string& name) -> const ArrowArray* {
+      const ArrowArray* c = arr.children[ci];
+      if (c == nullptr || c->release == nullptr) fail(GFPDB_EINVAL, "column '" + name + "' is missing or released");
+      if (c->offset < 0 || c->length < arr.offset + n)
+        fail(GFPDB_EINVAL, "column '" + name + "' is shorter than the struct");
+      if (c->n_buffers != (t == DType::Utf8 ? 3 : 2))
+        fail(GFPDB_EINVAL, "column '" + name + "' has the wrong number of buffers for its type");
+      if (c->null_count != 0 && c->buffers[0] != nullptr)
+        fail(GFPDB_EUNSUPPORTED, "column '" + name + "' has nulls; nullable inputs are not supported");
+      return c;
+    };
     int device = 0;
     GF_CUDA(cudaGetDevice(&device));
     // First call on this device: look up the scratch address (no allocation).
@@ -1264,8 +1283,7 @@ extern "C" int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, con
       if (ci < 0) fail(GFPDB_EINVAL, "column '" + pred.slots.names[i] + "' not found in TupleSet");
       const DType t = dtype_from_format(in_schema->children[ci]->format);
       if (t != pred.slots.types[i]) fail(GFPDB_EINVAL, "column '" + pred.slots.names[i] + "' changed type");
-      const ArrowArray* c = arr.children[ci];
-      if (c->null_count != 0 && c->buffers[0] != nullptr) fail(GFPDB_EUNSUPPORTED, "nullable inputs are not supported");
+      const ArrowArray* c = bound_child(ci, t, pred.slots.names[i]);
       const int64_t off = c->offset + arr.offset;
       if (t == DType::Utf8) {
         p.cols[i].offsets = static_cast<const int32_t*>(c->buffers[1]) + off;
@@ -1285,7 +1303,7 @@ extern "C" int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, con
       if (ci < 0) fail(GFPDB_EINVAL, std::string("column '") + project_columns[j] + "' not found in TupleSet");
       const DType t = dtype_from_format(in_schema->children[ci]->format);
       if (t == DType::Utf8) fail(GFPDB_EUNSUPPORTED, "utf8 outputs need allocation; use gfpdb_filter_evaluate");
-      const ArrowArray* c = arr.children[ci];
+      const ArrowArray* c = bound_child(ci, t, project_columns[j]);
       OutCol& oc = p.outs[p.n_out++];
       oc.src = static_cast<const char*>(c->buffers[1]) + (c->offset + arr.offset) * dtype_width(t);
       oc.dst = out_columns[j];

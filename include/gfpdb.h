@@ -70,6 +70,12 @@ int32_t gfpdb_device_init(int32_t device);
 /* Number of kernels this library has launched in this process. */
 uint64_t gfpdb_kernel_launch_count(void);
 
+/* Bytes of device memory the calling thread has taken from the library's
+ * allocator so far (each request rounded up to 256 bytes). A diagnostic with
+ * no counterpart in the reference: a caller checks with it that a call
+ * allocated nothing, or how much a plan's first run allocated. */
+int64_t gfpdb_thread_device_alloc_bytes(void);
+
 /* Stream-ordered copies between host and device memory, for callers that
  * hold raw device buffers (kind: 1 = host->device, 2 = device->host,
  * 3 = device->device). Synchronous when stream is NULL. */
@@ -136,17 +142,23 @@ int32_t gfpdb_filter_evaluate(const gfpdb_filter* filter, const struct ArrowSche
 void gfpdb_filter_free(gfpdb_filter* filter);
 
 /* The filter of gfpdb_filter_evaluate for callers that cannot allocate device
- * memory (code running under CUDA graph capture, engines that own a fixed
- * device arena, embedders whose allocator belongs to another runtime). It has
- * no counterpart in the reference. It allocates nothing: the kernel's scratch
- * (status block, tile ticket, one look-back word per 2048-row tile) lives in a
- * file-scope __device__ array of about 1 MiB that every GPU loading the
- * library keeps until exit, and the caller passes the outputs.
+ * memory: engines that own a fixed device arena and budget every byte of HBM
+ * themselves, and embedders whose device memory belongs to another runtime's
+ * allocator, for whom a cudaMalloc by the library would grow the heap behind
+ * their accounting. It has no counterpart in the reference. It allocates
+ * nothing: the kernel's scratch (status block, tile ticket, one look-back
+ * word per 2048-row tile) lives in a file-scope __device__ array of about
+ * 1 MiB that every GPU loading the library keeps until exit, and the caller
+ * passes the outputs.
  *  - Input must be device-resident (ARROW_DEVICE_CUDA) and at most
  *    268,435,456 rows; larger inputs are rejected with GFPDB_EINVAL.
  *  - out_columns[j] is a device buffer for project_columns[j] with room for
  *    in->array.length values of that column's width; only fixed-width columns
- *    (int32, int64, date32, float64) can be outputs.
+ *    (int32, int64, date32, float64) without nulls can be outputs.
+ *  - The input is checked as gfpdb_filter_evaluate checks it (struct without
+ *    nulls, children at least offset + length long with their buffer counts,
+ *    no nullable columns); a failed check is GFPDB_EINVAL or
+ *    GFPDB_EUNSUPPORTED before any device work.
  *  - *out_num_rows receives the number of selected rows (the call waits for
  *    its stream).
  *  - The first call on a device looks up the array's device address
