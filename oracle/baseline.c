@@ -124,47 +124,132 @@ static int64_t imap_find(const imap* m, int64_t key) {
   return -1;
 }
 
-typedef struct {
-  const orc_star_fact* fact;
-  const bloom* blooms[4];
-  const int* order;
-  int64_t lo, hi;
-  int64_t* out;  /* surviving row ids */
-  int64_t n_out;
-} probe_task;
+/*
+ * The star query over a fact table of one or more partitions. The fact-table
+ * passes (forward bloom probes; backward bloom builds; the 4-way join and
+ * group-by) are split into chunks of at most kChunk rows of one partition
+ * that `threads` POSIX threads take in turn, the way PARALLEL_DEGREE
+ * partitions the reference's scans (one scan operator per partition,
+ * PrePToPTransformer.cpp:1078-1100). Backward filters are built per thread
+ * and OR-ed (the same bits as one build); groups are aggregated per thread
+ * and merged (int64 addition wraps, so the order does not matter).
+ */
+enum { kChunk = 1 << 20 };
 
-static void* probe_range(void* arg) {
-  probe_task* t = (probe_task*)arg;
-  int64_t k = 0;
-  for (int64_t r = t->lo; r < t->hi; ++r) {
-    int ok = 1;
-    for (int j = 0; j < 4 && ok; ++j) {
-      int i = t->order[j];
-      ok = bloom_has(t->blooms[i], t->fact->fk[i][r]);
+typedef struct {
+  int part;
+  int64_t lo, hi;
+  int64_t* out; /* surviving row ids of the chunk */
+  int64_t n_out;
+} chunk;
+
+typedef struct {
+  const orc_star_fact* parts;
+  const orc_star_dim* dims;
+  const bloom* fwd;
+  bloom* bwd;        /* per thread: 4 filters */
+  const imap* dmap;  /* 4 maps: dim key -> dim row */
+  chunk* chunks;
+  int64_t n_chunks;
+  int64_t* next;     /* shared chunk counter */
+  int phase;         /* 0: forward probes, 1: backward builds, 2: join + group */
+  /* phase 2, per thread */
+  imap groups;
+  int32_t *g2, *g4;
+  int64_t *rev, *drev, *cnt;
+  int64_t ng, max_groups;
+} worker;
+
+static const int kOrder[4] = {1, 2, 3, 0}; /* forward pass order 2, 3, 4, 1 */
+
+static void run_chunk(worker* w, chunk* c) {
+  const orc_star_fact* f = &w->parts[c->part];
+  if (w->phase == 0) {
+    int64_t k = 0;
+    for (int64_t r = c->lo; r < c->hi; ++r) {
+      int ok = 1;
+      for (int j = 0; j < 4 && ok; ++j) ok = bloom_has(&w->fwd[kOrder[j]], f->fk[kOrder[j]][r]);
+      if (ok) c->out[k++] = r;
     }
-    if (ok) t->out[k++] = r;
+    c->n_out = k;
+  } else if (w->phase == 1) {
+    for (int64_t k = 0; k < c->n_out; ++k)
+      for (int i = 0; i < 4; ++i) bloom_add(&w->bwd[i], f->fk[i][c->out[k]]);
+  } else {
+    if (w->ng < 0) return;
+    for (int64_t k = 0; k < c->n_out; ++k) {
+      const int64_t r = c->out[k];
+      int64_t dr[4];
+      int ok = 1;
+      for (int i = 0; i < 4 && ok; ++i) {
+        dr[i] = imap_find(&w->dmap[i], f->fk[i][r]);
+        ok = dr[i] >= 0;
+      }
+      if (!ok) continue;
+      const int32_t g2 = w->dims[1].g[dr[1]], g4 = w->dims[3].g[dr[3]];
+      const int64_t key = ((int64_t)(uint32_t)g2 << 32) | (uint32_t)g4;
+      int fresh;
+      const uint64_t s = imap_slot(&w->groups, key, &fresh);
+      if (fresh) {
+        if (w->ng >= w->max_groups) {
+          w->ng = -1;
+          return;
+        }
+        w->groups.vals[s] = w->ng;
+        w->g2[w->ng] = g2;
+        w->g4[w->ng] = g4;
+        w->rev[w->ng] = w->drev[w->ng] = w->cnt[w->ng] = 0;
+        ++w->ng;
+      }
+      const int64_t gi = w->groups.vals[s];
+      const uint64_t p = (uint64_t)f->price[r];
+      w->rev[gi] = (int64_t)((uint64_t)w->rev[gi] + p * (uint64_t)(int64_t)f->qty[r]);
+      w->drev[gi] = (int64_t)((uint64_t)w->drev[gi] + p * (uint64_t)(int64_t)f->disc[r]);
+      w->cnt[gi] += 1;
+    }
   }
-  t->n_out = k;
+}
+
+static void* worker_main(void* arg) {
+  worker* w = (worker*)arg;
+  for (;;) {
+    const int64_t i = __atomic_fetch_add(w->next, 1, __ATOMIC_RELAXED);
+    if (i >= w->n_chunks) break;
+    run_chunk(w, &w->chunks[i]);
+  }
   return NULL;
 }
 
+static void run_phase(worker* ws, int threads, int phase, int64_t* next) {
+  *next = 0;
+  pthread_t* tid = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+  for (int t = 0; t < threads; ++t) {
+    ws[t].phase = phase;
+    if (threads > 1) pthread_create(&tid[t], NULL, worker_main, &ws[t]);
+  }
+  if (threads == 1) worker_main(&ws[0]);
+  for (int t = 0; t < threads && threads > 1; ++t) pthread_join(tid[t], NULL);
+  free(tid);
+}
+
 /*
- * Runs the query and writes one row per group into the out_* arrays
- * (capacity max_groups). Returns the number of groups, or -1 if max_groups
- * is too small.
+ * Runs the query with dimension filters lo[i] <= f <= hi[i] over n_parts fact
+ * partitions and writes one row per group into the out_* arrays (capacity
+ * max_groups). Returns the number of groups, or -1 if max_groups is too
+ * small.
  */
-int64_t orc_star_query(const orc_star_fact* fact, const orc_star_dim* dims, const int32_t* consts, int bits, int nh,
-                       int threads, int32_t* out_g2, int32_t* out_g4, int64_t* out_rev, int64_t* out_drev,
-                       int64_t* out_cnt, int64_t max_groups) {
+int64_t orc_star_query_parts(const orc_star_fact* parts, int n_parts, const orc_star_dim* dims, const int32_t* lo,
+                             const int32_t* hi, int bits, int nh, int threads, int32_t* out_g2, int32_t* out_g4,
+                             int64_t* out_rev, int64_t* out_drev, int64_t* out_cnt, int64_t max_groups) {
   if (threads < 1) threads = 1;
-  /* 1. dim filters: f == const */
+  /* 1. dim filters */
   int64_t* keep[4];
   int64_t nkeep[4];
   for (int i = 0; i < 4; ++i) {
     keep[i] = (int64_t*)malloc(sizeof(int64_t) * (size_t)(dims[i].n + 1));
     nkeep[i] = 0;
     for (int64_t r = 0; r < dims[i].n; ++r)
-      if (dims[i].f[r] == consts[i]) keep[i][nkeep[i]++] = r;
+      if (dims[i].f[r] >= lo[i] && dims[i].f[r] <= hi[i]) keep[i][nkeep[i]++] = r;
   }
   /* 2. forward blooms on the filtered dim keys */
   bloom fwd[4];
@@ -172,91 +257,122 @@ int64_t orc_star_query(const orc_star_fact* fact, const orc_star_dim* dims, cons
     bloom_init(&fwd[i], nkeep[i], bits, nh);
     for (int64_t k = 0; k < nkeep[i]; ++k) bloom_add(&fwd[i], dims[i].pk[keep[i][k]]);
   }
-  /* 3. probe the fact table in parallel (forward pass order 2, 3, 4, 1) */
-  static const int order[4] = {1, 2, 3, 0};
-  pthread_t* tid = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
-  probe_task* tasks = (probe_task*)calloc((size_t)threads, sizeof(probe_task));
-  int64_t per = (fact->n + threads - 1) / threads;
+  /* chunks of every partition */
+  int64_t n_chunks = 0;
+  for (int p = 0; p < n_parts; ++p) n_chunks += (parts[p].n + kChunk - 1) / kChunk;
+  chunk* chunks = (chunk*)calloc((size_t)(n_chunks + 1), sizeof(chunk));
+  int64_t at = 0, survivors = 0;
+  for (int p = 0; p < n_parts; ++p)
+    for (int64_t r = 0; r < parts[p].n; r += kChunk) {
+      chunks[at].part = p;
+      chunks[at].lo = r;
+      chunks[at].hi = r + kChunk < parts[p].n ? r + kChunk : parts[p].n;
+      chunks[at].out = (int64_t*)malloc(sizeof(int64_t) * (size_t)(chunks[at].hi - r));
+      ++at;
+    }
+  int64_t next = 0;
+  worker* ws = (worker*)calloc((size_t)threads, sizeof(worker));
   for (int t = 0; t < threads; ++t) {
-    tasks[t].fact = fact;
-    for (int i = 0; i < 4; ++i) tasks[t].blooms[i] = &fwd[i];
-    tasks[t].order = order;
-    tasks[t].lo = t * per < fact->n ? t * per : fact->n;
-    tasks[t].hi = (t + 1) * per < fact->n ? (t + 1) * per : fact->n;
-    tasks[t].out = (int64_t*)malloc(sizeof(int64_t) * (size_t)(tasks[t].hi - tasks[t].lo + 1));
-    if (threads > 1) pthread_create(&tid[t], NULL, probe_range, &tasks[t]);
+    ws[t].parts = parts;
+    ws[t].dims = dims;
+    ws[t].fwd = fwd;
+    ws[t].chunks = chunks;
+    ws[t].n_chunks = n_chunks;
+    ws[t].next = &next;
   }
-  if (threads == 1) probe_range(&tasks[0]);
-  int64_t survivors = 0;
+  /* 3. forward probes of the fact table (pass order 2, 3, 4, 1) */
+  run_phase(ws, threads, 0, &next);
+  for (int64_t c = 0; c < n_chunks; ++c) survivors += chunks[c].n_out;
+  /* 4. backward blooms on the reduced fact keys (per thread, then OR-ed),
+   *    applied to the filtered dims */
   for (int t = 0; t < threads; ++t) {
-    if (threads > 1) pthread_join(tid[t], NULL);
-    survivors += tasks[t].n_out;
+    ws[t].bwd = (bloom*)malloc(sizeof(bloom) * 4);
+    for (int i = 0; i < 4; ++i) bloom_init(&ws[t].bwd[i], survivors, bits, nh);
   }
-  int64_t* rows = (int64_t*)malloc(sizeof(int64_t) * (size_t)(survivors + 1));
-  int64_t at = 0;
-  for (int t = 0; t < threads; ++t) {
-    memcpy(rows + at, tasks[t].out, sizeof(int64_t) * (size_t)tasks[t].n_out);
-    at += tasks[t].n_out;
-    free(tasks[t].out);
-  }
-  free(tasks);
-  free(tid);
-  /* 4. backward blooms on the reduced fact keys, applied to the dims */
+  run_phase(ws, threads, 1, &next);
   imap dmap[4];
   for (int i = 0; i < 4; ++i) {
-    bloom bwd;
-    bloom_init(&bwd, survivors, bits, nh);
-    for (int64_t k = 0; k < survivors; ++k) bloom_add(&bwd, fact->fk[i][rows[k]]);
+    bloom* b = &ws[0].bwd[i];
+    for (int t = 1; t < threads; ++t)
+      for (uint64_t w = 0; w < b->nblocks * 8; ++w) b->words[w] |= ws[t].bwd[i].words[w];
     imap_init(&dmap[i], nkeep[i]);
     for (int64_t k = 0; k < nkeep[i]; ++k) {
-      int64_t r = keep[i][k];
-      if (!bloom_has(&bwd, dims[i].pk[r])) continue;
+      const int64_t r = keep[i][k];
+      if (!bloom_has(b, dims[i].pk[r])) continue;
       int fresh;
-      uint64_t s = imap_slot(&dmap[i], dims[i].pk[r], &fresh);
-      dmap[i].vals[s] = r;  /* dim keys are unique */
+      const uint64_t s = imap_slot(&dmap[i], dims[i].pk[r], &fresh);
+      dmap[i].vals[s] = r; /* dim keys are unique */
     }
-    free(bwd.words);
+    for (int t = 0; t < threads; ++t) free(ws[t].bwd[i].words);
     free(fwd[i].words);
     free(keep[i]);
   }
-  /* 5. 4-way inner join + group by (d2.g, d4.g) */
+  /* 5. 4-way inner join + group by (d2.g, d4.g), per thread, then merged */
+  const int64_t cap = max_groups > 0 ? max_groups : 1;
+  for (int t = 0; t < threads; ++t) {
+    free(ws[t].bwd);
+    ws[t].dmap = dmap;
+    imap_init(&ws[t].groups, cap);
+    ws[t].g2 = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+    ws[t].g4 = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+    ws[t].rev = (int64_t*)malloc(sizeof(int64_t) * (size_t)cap);
+    ws[t].drev = (int64_t*)malloc(sizeof(int64_t) * (size_t)cap);
+    ws[t].cnt = (int64_t*)malloc(sizeof(int64_t) * (size_t)cap);
+    ws[t].ng = 0;
+    ws[t].max_groups = cap;
+  }
+  run_phase(ws, threads, 2, &next);
   imap groups;
-  imap_init(&groups, max_groups > 0 ? max_groups : 1);
+  imap_init(&groups, cap);
   int64_t ng = 0;
-  for (int64_t k = 0; k < survivors; ++k) {
-    int64_t r = rows[k];
-    int64_t dr[4];
-    int ok = 1;
-    for (int i = 0; i < 4 && ok; ++i) {
-      dr[i] = imap_find(&dmap[i], fact->fk[i][r]);
-      ok = dr[i] >= 0;
+  for (int t = 0; t < threads && ng >= 0; ++t) {
+    if (ws[t].ng < 0) {
+      ng = -1;
+      break;
     }
-    if (!ok) continue;
-    int32_t g2 = dims[1].g[dr[1]], g4 = dims[3].g[dr[3]];
-    int64_t key = ((int64_t)(uint32_t)g2 << 32) | (uint32_t)g4;
-    int fresh;
-    uint64_t s = imap_slot(&groups, key, &fresh);
-    if (fresh) {
-      if (ng >= max_groups) {
-        ng = -1;
-        break;
+    for (int64_t g = 0; g < ws[t].ng; ++g) {
+      const int64_t key = ((int64_t)(uint32_t)ws[t].g2[g] << 32) | (uint32_t)ws[t].g4[g];
+      int fresh;
+      const uint64_t s = imap_slot(&groups, key, &fresh);
+      if (fresh) {
+        if (ng >= max_groups) {
+          ng = -1;
+          break;
+        }
+        groups.vals[s] = ng;
+        out_g2[ng] = ws[t].g2[g];
+        out_g4[ng] = ws[t].g4[g];
+        out_rev[ng] = out_drev[ng] = out_cnt[ng] = 0;
+        ++ng;
       }
-      groups.vals[s] = ng;
-      out_g2[ng] = g2;
-      out_g4[ng] = g4;
-      out_rev[ng] = out_drev[ng] = out_cnt[ng] = 0;
-      ++ng;
+      const int64_t gi = groups.vals[s];
+      out_rev[gi] = (int64_t)((uint64_t)out_rev[gi] + (uint64_t)ws[t].rev[g]);
+      out_drev[gi] = (int64_t)((uint64_t)out_drev[gi] + (uint64_t)ws[t].drev[g]);
+      out_cnt[gi] += ws[t].cnt[g];
     }
-    int64_t gi = groups.vals[s];
-    uint64_t p = (uint64_t)fact->price[r];
-    out_rev[gi] = (int64_t)((uint64_t)out_rev[gi] + p * (uint64_t)(int64_t)fact->qty[r]);
-    out_drev[gi] = (int64_t)((uint64_t)out_drev[gi] + p * (uint64_t)(int64_t)fact->disc[r]);
-    out_cnt[gi] += 1;
   }
   imap_free(&groups);
+  for (int t = 0; t < threads; ++t) {
+    imap_free(&ws[t].groups);
+    free(ws[t].g2);
+    free(ws[t].g4);
+    free(ws[t].rev);
+    free(ws[t].drev);
+    free(ws[t].cnt);
+  }
+  free(ws);
   for (int i = 0; i < 4; ++i) imap_free(&dmap[i]);
-  free(rows);
+  for (int64_t c = 0; c < n_chunks; ++c) free(chunks[c].out);
+  free(chunks);
   return ng;
+}
+
+/* The single-table star query with filters f == consts[i]. */
+int64_t orc_star_query(const orc_star_fact* fact, const orc_star_dim* dims, const int32_t* consts, int bits, int nh,
+                       int threads, int32_t* out_g2, int32_t* out_g4, int64_t* out_rev, int64_t* out_drev,
+                       int64_t* out_cnt, int64_t max_groups) {
+  return orc_star_query_parts(fact, 1, dims, consts, consts, bits, nh, threads, out_g2, out_g4, out_rev, out_drev,
+                              out_cnt, max_groups);
 }
 
 /*

@@ -34,14 +34,16 @@ def lib():
             subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
         _lib = ctypes.CDLL(str(LIB))
         _lib.orc_star_query.restype = ctypes.c_int64
+        _lib.orc_star_query_parts.restype = ctypes.c_int64
     return _lib
 
 
 class StarInputs:
-    """Arrays of a star workload laid out for the C baseline (kept alive)."""
+    """Arrays of a star workload laid out for the C baseline (kept alive):
+    the dimensions d1..d4 and the fact table, or the fact partitions named
+    in `parts`."""
 
-    def __init__(self, tables: dict[str, Table]):
-        f = tables["fact"]
+    def __init__(self, tables: dict[str, Table], parts=("fact",)):
         self.keep = []
 
         def arr(t: Table, name: str, dt):
@@ -49,13 +51,19 @@ class StarInputs:
             self.keep.append(a)
             return a.ctypes.data
 
-        self.fact = _Fact()
-        self.fact.n = f.num_rows
-        for i in range(4):
-            self.fact.fk[i] = arr(f, f"fk{i + 1}", np.int32)
-        self.fact.qty = arr(f, "qty", np.int32)
-        self.fact.price = arr(f, "price_cents", np.int64)
-        self.fact.disc = arr(f, "discount", np.int32)
+        self.n_parts = len(parts)
+        self.parts = (_Fact * len(parts))()
+        for j, name in enumerate(parts):
+            f = tables[name]
+            fp = self.parts[j]
+            fp.n = f.num_rows
+            for i in range(4):
+                fp.fk[i] = arr(f, f"fk{i + 1}", np.int32)
+            fp.qty = arr(f, "qty", np.int32)
+            fp.price = arr(f, "price_cents", np.int64)
+            fp.disc = arr(f, "discount", np.int32)
+        self.fact = self.parts[0]
+        self.rows = sum(self.parts[j].n for j in range(len(parts)))
         self.dims = (_Dim * 4)()
         for i in range(4):
             d = tables[f"d{i + 1}"]
@@ -67,14 +75,23 @@ class StarInputs:
 
 def star_query(inputs: StarInputs, consts=(1, 3, 2, 5), bits: int = 10, nh: int = 3, threads: int | None = None,
                max_groups: int = 4096) -> Table:
+    """The star query with dimension filters f == consts[i]."""
+    return star_query_ranges(inputs, [(c, c) for c in consts], bits, nh, threads, max_groups)
+
+
+def star_query_ranges(inputs: StarInputs, ranges, bits: int = 10, nh: int = 3, threads: int | None = None,
+                      max_groups: int = 4096) -> Table:
+    """The star query with dimension filters lo <= f <= hi over every fact
+    partition of `inputs`, its fact passes on `threads` host threads."""
     threads = threads or os.cpu_count() or 1
-    c = (ctypes.c_int32 * 4)(*consts)
+    lo = (ctypes.c_int32 * 4)(*[int(r[0]) for r in ranges])
+    hi = (ctypes.c_int32 * 4)(*[int(r[1]) for r in ranges])
     g2 = np.zeros(max_groups, np.int32)
     g4 = np.zeros(max_groups, np.int32)
     rev = np.zeros(max_groups, np.int64)
     drev = np.zeros(max_groups, np.int64)
     cnt = np.zeros(max_groups, np.int64)
-    n = lib().orc_star_query(ctypes.byref(inputs.fact), inputs.dims, c, bits, nh, threads,
+    n = lib().orc_star_query_parts(inputs.parts, inputs.n_parts, inputs.dims, lo, hi, bits, nh, threads,
                              g2.ctypes.data_as(ctypes.c_void_p), g4.ctypes.data_as(ctypes.c_void_p),
                              rev.ctypes.data_as(ctypes.c_void_p), drev.ctypes.data_as(ctypes.c_void_p),
                              cnt.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(max_groups))

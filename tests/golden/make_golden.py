@@ -4,7 +4,8 @@ synthetic workloads, an implementation independent of both the oracle and
 the GPU path. Run here (pyarrow is a dependency of this script only; the
 fixtures are what the tests read):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py           # small fixtures
+    python tests/golden/make_golden.py --full    # the workloads at full size
 
 Each fixture records the workload parameters (the inputs are regenerated
 from the seeds by flexpushdowndb_gb300.workloads) and the expected result:
@@ -94,6 +95,14 @@ def star(fact_rows=120_000, seed=2000, consts=(1, 3, 2, 5), ranges=None, parts=N
     return out
 
 
+def decimal_cents(col) -> np.ndarray:
+    """Unscaled values of a decimal128 column (its two's-complement 128-bit
+    storage; every value here fits the low 64 bits)."""
+    a = col.combine_chunks() if hasattr(col, "combine_chunks") else col
+    words = np.frombuffer(a.buffers()[1], dtype=np.int64)
+    return words[2 * a.offset: 2 * (a.offset + len(a)): 2].copy()
+
+
 def csv_scan(rows=20_000, seed=workloads.CSV_SEED):
     text = workloads.lineitem_csv(rows, seed)
     names = [n for n, _ in workloads.LINEITEM_FIELDS]
@@ -104,8 +113,7 @@ def csv_scan(rows=20_000, seed=workloads.CSV_SEED):
     t = pcsv.read_csv(pa.BufferReader(text), read_options=pcsv.ReadOptions(column_names=names),
                       parse_options=pcsv.ParseOptions(delimiter="|"),
                       convert_options=pcsv.ConvertOptions(column_types=types))
-    cents = {n: np.array([int(x.scaleb(2)) for x in t[n].to_pylist()], dtype=np.int64)
-             for n, ty in workloads.LINEITEM_FIELDS if ty.startswith("decimal")}
+    cents = {n: decimal_cents(t[n]) for n, ty in workloads.LINEITEM_FIELDS if ty.startswith("decimal")}
     days = {n: t[n].cast(pa.int32()).to_numpy().astype(np.int64) for n in ("t1", "t2")}
     ints = {n: t[n].to_numpy().astype(np.int64) for n in ("i1", "i2", "i3", "i4")}
     col_sums = {n: int(v.sum()) for n, v in {**ints, **cents, **days}.items()}
@@ -126,7 +134,56 @@ def groupby(rows=300_000, n_keys=1_000_000, seed=5000):
             "sum_counts": int(sum(x[2] for x in r)), "digest": digest(r)}
 
 
+def star_batch(n_parts=64, n_queries=32):
+    """The batched form at full size: every query variant of
+    workloads.batch_queries over the 64-partition fact table, each run as its
+    own chain of Arrow joins and one hash aggregate; per variant its group
+    count, row digest and column sums."""
+    tabs = workloads.batch_tables(n_parts)
+    fact = pa.concat_tables([arrow(tabs[f"p{i}"]) for i in range(n_parts)])
+    dims = {i: arrow(tabs[f"d{i}"]) for i in range(1, 5)}
+    out = []
+    for q in workloads.batch_queries(n_queries):
+        cur = fact
+        for i in range(1, 5):
+            lo, hi = q[i - 1]
+            d = dims[i]
+            f = d[f"d{i}_f"]
+            keep = [f"d{i}_pk", f"d{i}_g"] if i in (2, 4) else [f"d{i}_pk"]
+            d = d.filter(pc.and_(pc.greater_equal(f, lo), pc.less_equal(f, hi))).select(keep)
+            cur = cur.join(d, keys=f"fk{i}", right_keys=f"d{i}_pk", join_type="inner")
+        cur = cur.append_column("rev", pc.multiply(cur["price_cents"], cur["qty"]))
+        cur = cur.append_column("drev", pc.multiply(cur["price_cents"], cur["discount"]))
+        g = cur.group_by(["d2_g", "d4_g"]).aggregate([("rev", "sum"), ("drev", "sum"), ("rev", "count")])
+        names = ["d2_g", "d4_g", "revenue", "discount_revenue", "cnt"]
+        r = rows_of(g.select(["d2_g", "d4_g", "rev_sum", "drev_sum", "rev_count"]).rename_columns(names), names)
+        out.append({"ranges": [list(x) for x in q], "groups": len(r), "digest": digest(r),
+                    "sum_revenue": int(sum(x[2] for x in r)), "sum_discount_revenue": int(sum(x[3] for x in r)),
+                    "sum_cnt": int(sum(x[4] for x in r))})
+        print("variant", len(out), len(r), flush=True)
+    return {"query": "star_batch", "parts": n_parts, "seed": workloads.BATCH_SEED,
+            "fact_rows": fact.num_rows, "columns": ["d2_g", "d4_g", "revenue", "discount_revenue", "cnt"],
+            "variants": out}
+
+
+def full_size():
+    """Fixtures of the workloads at their full sizes (size-independent
+    checksums where the result is large)."""
+    return {
+        "two_table_1m": two_table(fact_rows=1_000_000),
+        "star_6m": star(fact_rows=6_000_000),
+        "csv_scan_6m": csv_scan(rows=6_000_000),
+        "star_batch_64x32": star_batch(),
+    }
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--full":
+        fixtures = full_size()
+        for name, f in fixtures.items():
+            (HERE / f"{name}.json").write_text(json.dumps(f, separators=(",", ":")) + "\n")
+            print(name, len(json.dumps(f)))
+        return
     fixtures = {
         "two_table_50k": two_table(),
         "star_120k": star(),

@@ -181,3 +181,23 @@ def test_c_baselines_golden():
     tabs = workloads.star_tables(fact_rows=f["fact_rows"], seed=f["seed"])
     got = cbaseline.star_query(cbaseline.StarInputs(tabs), consts=tuple(f["consts"]), threads=3)
     assert got.sorted_rows() == rows(f["rows"])
+
+
+def test_c_baseline_full_size_golden():
+    """The C port (the reference arm of the benchmark) at full size: the star
+    query over 6,000,000 fact rows, and all 32 variants of the batched form
+    over its 64 partitions (59,952,713 rows)."""
+    from oracle import cbaseline
+
+    f = fixture("star_6m")
+    tabs = workloads.star_tables(fact_rows=f["fact_rows"], seed=f["seed"])
+    got = cbaseline.star_query(cbaseline.StarInputs(tabs), consts=tuple(f["consts"]))
+    assert got.sorted_rows() == rows(f["rows"])
+    del tabs
+    f = fixture("star_batch_64x32")
+    tabs = workloads.batch_tables(f["parts"])
+    inp = cbaseline.StarInputs(tabs, parts=[f"p{i}" for i in range(f["parts"])])
+    assert inp.rows == f["fact_rows"]
+    for v in f["variants"]:
+        got = cbaseline.star_query_ranges(inp, v["ranges"]).sorted_rows()
+        assert len(got) == v["groups"] and digest(got) == v["digest"]
