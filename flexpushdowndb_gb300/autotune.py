@@ -1,8 +1,8 @@
 """Autotuner for the launch and table parameters of the hot path.
 
 Picks, by measurement on the current GPU:
-  - the batched star engine's items per thread, CTAs per SM and join-table
-    load factor (tune_star_batch);
+  - the batched star engine's items per thread, CTAs per SM, foreign-key
+    pipeline stages and join-table load factor (tune_star_batch);
   - a star plan's bloom bits per key and hash count, hash-join load factor and
     number of streams (tune_star_plan).
 Search is coordinate descent from the defaults: one parameter at a time over
@@ -26,8 +26,9 @@ from . import _abi, batch, plan
 DEFAULT_CACHE = Path(os.environ.get("GFPDB_AUTOTUNE_CACHE", Path.home() / ".cache" / "gfpdb" / "autotune.json"))
 
 BATCH_SPACE = {
-    "itemsPerThread": [1, 2, 4],
-    "blocksPerSm": [2, 3, 4, 6],
+    "itemsPerThread": [2, 4, 8],
+    "blocksPerSm": [1, 2, 3, 4],
+    "stages": [2, 3, 4, 6],
     "loadFactor": [0.3, 0.5, 0.7],
 }
 

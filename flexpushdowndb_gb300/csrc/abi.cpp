@@ -246,8 +246,10 @@ void clear_batches() {
 }
 
 std::shared_ptr<BatchEntry> make_batch(const json::Value& spec, const std::map<std::string, TupleSetPtr>& tables,
-                                       bool use_graph, cudaStream_t s) {
+                                       bool use_graph, cudaStream_t s,
+                                       std::vector<StarBatchHostColumn> host_cols = {}) {
   auto be = std::make_shared<BatchEntry>();
+  be->batch.set_host_columns(std::move(host_cols));
   StarBatchSpec& sp = be->batch.spec();
   auto table = [&](const std::string& name) {
     auto it = tables.find(name);
@@ -989,13 +991,33 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
         fail(GFPDB_EINVAL, e.what());
       }
       std::map<std::string, TupleSetPtr> tables;
+      std::vector<StarBatchHostColumn> host_cols;
+      bool pageable = false;
       for (int32_t i = 0; i < n_tables; ++i) {
-        require(table_names[i] != nullptr, "null table name");
-        if (arrays[i]->device_type != ARROW_DEVICE_CUDA)
-          fail(GFPDB_EINVAL, "batched star inputs must be device-resident");
-        tables[table_names[i]] = import_tupleset(schemas[i], arrays[i], s);
+        require(table_names[i] != nullptr && arrays[i] != nullptr, "null table");
+        const int32_t dt = arrays[i]->device_type;
+        if (dt != ARROW_DEVICE_CUDA && dt != ARROW_DEVICE_CPU && dt != ARROW_DEVICE_CUDA_HOST)
+          fail(GFPDB_EUNSUPPORTED, "unsupported ArrowDeviceArray device_type " + std::to_string(dt));
+        // Host tables get device copies here; every run refreshes the
+        // columns the batch reads from the host buffers.
+        TupleSetPtr t = import_tupleset(schemas[i], arrays[i], s, false);
+        if (dt != ARROW_DEVICE_CUDA) {
+          pageable |= dt == ARROW_DEVICE_CPU;
+          const ArrowArray& a = arrays[i]->array;
+          for (int c = 0; c < t->num_columns(); ++c) {
+            const auto& col = t->column(c);
+            if (col->type == DType::Utf8) continue;
+            const int w = dtype_width(col->type);
+            const ArrowArray* ch = a.children[c];
+            const char* src = static_cast<const char*>(ch->buffers[1]) + (ch->offset + a.offset) * w;
+            if (col->data != src) host_cols.push_back(StarBatchHostColumn{col->data, src, t->num_rows() * w});
+          }
+        }
+        tables[table_names[i]] = t;
       }
-      be = make_batch(spec, tables, use_graph != 0, s);
+      sync(s);  // the first copies have landed
+      // pageable host memory cannot be copied from inside a CUDA graph
+      be = make_batch(spec, tables, use_graph != 0 && !pageable, s, std::move(host_cols));
       remember_batch(key, be);
     }
     if (be->exec != nullptr) {
@@ -1004,6 +1026,7 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
     } else {
       be->batch.run(s);
     }
+    copy_counters().h2d += be->batch.host_bytes();
     DevStatus st;
     GF_CUDA(cudaMemcpyAsync(&st, be->batch.status(), sizeof(st), cudaMemcpyDeviceToHost, s));
     sync(s);

@@ -35,6 +35,8 @@ void parse_star_batch_spec(const json::Value& spec, StarBatchSpec& sp) {
   if (!(sp.load_factor > 0 && sp.load_factor <= 0.9)) fail(GFPDB_EINVAL, "loadFactor must be in (0, 0.9]");
   sp.items_per_thread = static_cast<int>(spec.get_int("itemsPerThread", 2));
   sp.blocks_per_sm = static_cast<int>(spec.get_int("blocksPerSm", 4));
+  sp.stages = static_cast<int>(spec.get_int("stages", 3));
+  if (sp.stages < 2 || sp.stages > 8) fail(GFPDB_EINVAL, "stages must be in [2, 8]");
   if (sp.blocks_per_sm < 1 || sp.blocks_per_sm > 16) fail(GFPDB_EINVAL, "blocksPerSm must be in [1, 16]");
   sp.groups_hint = spec.get_int("groupsHint", 1024);
 }

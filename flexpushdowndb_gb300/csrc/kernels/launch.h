@@ -197,7 +197,18 @@ struct StarBatchSpec {
   double load_factor = 0.5;      // join tables
   int items_per_thread = 2;      // fact rows per consumer thread per tile: 1, 2, 4 or 8
   int blocks_per_sm = 4;         // persistent CTAs per SM
+  int stages = 3;                // foreign-key tiles in flight per CTA (2 to 8)
   int64_t groups_hint = 1024;    // upper bound on groups per query
+};
+
+// A column of a batched star input that lives in host memory: each run
+// copies its bytes from `src` to the device copy at `dst` first (the dimension
+// columns, then the fact partitions in groups, each group's fact pass starting
+// as soon as its copies have landed).
+struct StarBatchHostColumn {
+  const void* dst;
+  const void* src;
+  int64_t bytes;
 };
 
 struct StarBatchState;
@@ -224,6 +235,10 @@ class StarBatch {
   // Device array of kSBMaxQueries + 1 offsets: query q's rows of the result
   // are [off[q], off[q + 1]); valid after run().
   const unsigned long long* query_offsets() const;
+  // Device copies of host-resident input columns, refreshed by every run
+  // (set before prepare()); host_bytes() is what one run copies.
+  void set_host_columns(std::vector<StarBatchHostColumn> cols);
+  int64_t host_bytes() const;
 
  private:
   std::unique_ptr<StarBatchState> st_;

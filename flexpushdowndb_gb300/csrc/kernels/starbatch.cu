@@ -176,9 +176,9 @@ struct SBAgg {
 
 constexpr int kSBConsumerWarps = 8;
 constexpr int kSBFactThreads = (kSBConsumerWarps + 1) * 32;  // consumer warps + one producer warp
-constexpr int kSBStages = 2;
+constexpr int kSBMaxStages = 8;
 constexpr int kSBMaxAggsFact = 4;  // aggregates of a batched star query
-constexpr int kSBBarBytes = 128;  // 2 * kSBStages mbarriers, padded
+constexpr int kSBBarBytes = 128;  // 2 * kSBMaxStages mbarriers
 
 struct SBFactParams {
   SBDimDev dims[kSBMaxDims];
@@ -195,6 +195,7 @@ struct SBFactParams {
   const int64_t* tile_base;  // [n_parts + 1] first tile (kSBConsumerWarps * 32 * items rows) of each partition
   const int64_t* part_rows;  // [n_parts]
   int64_t n_tiles;
+  int64_t tile_begin, tile_end;  // tiles of this launch
   uint64_t* gkeys;               // [gcap] group keys, shared by every query (all-ones = empty)
   unsigned long long* touched;   // [gcap + 1] queries with rows in each group; slot gcap: the all-ones key
   unsigned long long* gaccs;     // [q][gcap + 1][n_aggs]
@@ -204,7 +205,9 @@ struct SBFactParams {
   int32_t seg_off[kSBMaxDims];   // byte offset of dimension d's foreign keys in a stage
   int32_t fk_width[kSBMaxDims];  // 4 or 8
   int32_t masks_off;             // byte offset of the staged query masks in dynamic shared memory
-  int32_t pad;
+  int32_t rings_off;             // byte offset of the consumer warps' rings in dynamic shared memory
+  int32_t n_stages;              // stages in the foreign-key ring (2 to kSBMaxStages)
+  int32_t pad2;
   DevStatus* st;
 };
 
@@ -267,28 +270,133 @@ __device__ __forceinline__ uint32_t sb_seg_bytes(const SBFactParams& p, int d, i
 
 // Stage 2: one persistent pass over every tile of every partition.
 // Warp kSBConsumerWarps is the producer: one lane streams each tile's
-// foreign-key columns into a kSBStages-deep ring of shared-memory stages
-// with cp.async.bulk, completing on the stage's "full" mbarrier. The other
-// warps consume: each takes 32 * ITEMS rows of the tile (lanes on
-// consecutive rows) and releases the stage on its "empty" mbarrier once it
-// has read its foreign keys, so consumer warps drift apart instead of meeting
-// at a block barrier. A consumer first applies the dimensions staged in
-// shared memory (query masks and group values by key), then issues the
-// lookups of the other dimensions one dimension ahead of their use, so their
-// memory latencies overlap. A row that survives every dimension finds its
-// group once in the table shared by all queries and adds its measures to each
-// of its queries' accumulators. Every wait is bounded: on timeout the kernel
-// records GFPDB_ETIMEDOUT and stops.
-template <int ITEMS>
+// foreign-key columns into a ring of p.n_stages shared-memory stages with
+// cp.async.bulk, completing on the stage's "full" mbarrier. The other warps
+// consume: each takes 32 * ITEMS rows of the tile (lanes on consecutive
+// rows) and releases the stage on its "empty" mbarrier once it has read its
+// foreign keys, so consumer warps drift apart instead of meeting at a block
+// barrier.
+//
+// A consumer works in three steps, each with every lane busy:
+//  (1) per row, the dimensions staged in shared memory (query masks and
+//      group values by key); the rows some query still wants are appended
+//      (ballot + prefix) to the warp's first ring;
+//  (2) per 32 ring entries, the other dimensions' lookups in global memory,
+//      the loads of up to four dimensions issued together; the surviving
+//      rows go to the warp's second ring with their group key;
+//  (3) per 32 entries of the second ring, the group slot (one probe of the
+//      table shared by all queries), the measures, and one atomic add per
+//      query and aggregate.
+// Without the rings a warp runs steps (2) and (3) whenever any of its lanes
+// has a surviving row, with the others idle. M is the query mask type: 32
+// bits for batches of at most 32 queries, else 64. Every wait is bounded: on
+// timeout the kernel records GFPDB_ETIMEDOUT and stops.
+constexpr int kSBRing = 64;  // entries of each per-warp ring (two chunks of 32)
+
+template <typename M>
+struct SBRings {
+  // ring 1: rows of the current tile that passed the staged dimensions
+  uint32_t r1[kSBRing];
+  M m1[kSBRing];
+  uint32_t g1a[kSBRing], g1b[kSBRing];
+  // ring 2: surviving rows (partition, row) with their group key
+  uint32_t part2[kSBRing];
+  uint32_t row2[kSBRing];
+  M m2[kSBRing];
+  unsigned long long key2[kSBRing];
+};
+
+template <typename M>
+__device__ __forceinline__ M sb_mask_cast(uint64_t v) {
+  return static_cast<M>(v);
+}
+
+// The group key of a row from its group column values.
+__device__ __forceinline__ uint64_t sb_group_key(int n_group, uint32_t g0, uint32_t g1) {
+  return n_group == 1 ? static_cast<uint64_t>(g0) : n_group == 2 ? (static_cast<uint64_t>(g0) << 32) | g1 : 0ull;
+}
+
+template <typename M>
+__device__ __forceinline__ int sb_ffs(M m) {
+  return sizeof(M) == 8 ? __ffsll(static_cast<long long>(m)) : __ffs(static_cast<int>(m));
+}
+
+// Step (3) for the entries [head, head + n) of ring 2 (n <= 32), one per lane.
+template <typename M>
+__device__ __forceinline__ void sb_update_groups(const SBFactParams& p, SBRings<M>& R, uint32_t head, int n, int lane) {
+  if (lane >= n) return;
+  const uint32_t e = (head + lane) & (kSBRing - 1);
+  M mi = R.m2[e];
+  const int part = static_cast<int>(R.part2[e]);
+  const int64_t row = R.row2[e];
+  const DevCol* cols = p.part_cols + static_cast<int64_t>(part) * p.n_cols;
+  unsigned long long vals[kSBMaxAggsFact];
+#pragma unroll
+  for (int a = 0; a < kSBMaxAggsFact; ++a) {
+    vals[a] = 0;
+    if (a >= p.n_aggs) continue;
+    const SBAgg& g = p.aggs[a];
+    if (g.fn == AGG_COUNT_STAR) {
+      vals[a] = 1ull;
+    } else {
+      uint64_t x = static_cast<uint64_t>(load_int(cols[g.a], row));
+      if (g.b >= 0) x *= static_cast<uint64_t>(load_int(cols[g.b], row));  // int64 wrap
+      vals[a] = x;
+    }
+  }
+  const uint64_t slot = sb_group_slot(p, R.key2[e]);
+  if (slot == UINT64_MAX) return;
+  atomicOr(p.touched + slot, static_cast<unsigned long long>(mi));
+  while (mi != 0) {
+    const int q = sb_ffs(mi) - 1;
+    mi &= mi - 1;
+    unsigned long long* acc =
+        p.gaccs + (static_cast<uint64_t>(q) * (p.gmask + 2) + slot) * static_cast<uint64_t>(p.n_aggs);
+#pragma unroll
+    for (int a = 0; a < kSBMaxAggsFact; ++a)
+      if (a < p.n_aggs) atomicAdd(acc + a, vals[a]);
+  }
+}
+
+// The per-dimension facts a consumer reads per row, gathered once per block
+// into shared memory in probe order: the dimensions staged in shared memory
+// (step 1) and the direct dimensions in global memory (step 2).
+struct SBStagedDim {
+  int32_t d;        // dimension
+  int32_t off;      // byte offset of its query masks in the staged area
+  int32_t seg;      // byte offset of its foreign keys in a stage
+  int32_t w8;       // 8-byte foreign keys
+  int32_t g0, g1;   // byte offsets of the values of group columns 0 / 1 it carries (-1: none)
+  int64_t kmin;
+  uint64_t range;
+};
+
+struct SBGlobalDim {
+  int32_t d;
+  int32_t seg;
+  int32_t w8;
+  int32_t pad;
+  int64_t kmin;
+  uint64_t range;
+  const uint64_t* dq;
+  const int32_t* g0;  // group column 0 / 1 values by key - min (nullptr: not carried)
+  const int32_t* g1;
+};
+
+template <int ITEMS, typename M>
 __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_constant__ SBFactParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* empty = full + kSBStages;
+  uint64_t* empty = full + kSBMaxStages;
   unsigned char* stages = smem + kSBBarBytes;
   unsigned char* staged_dims = smem + p.masks_off;
+  SBRings<M>* rings = reinterpret_cast<SBRings<M>*>(smem + p.rings_off);
   __shared__ int64_t s_kmin[kSBMaxDims];
   __shared__ uint64_t s_range[kSBMaxDims];
   __shared__ int32_t s_off[kSBMaxDims];  // staged: byte offset in staged_dims, else -1
+  __shared__ SBStagedDim s_st[kSBMaxDims];
+  __shared__ SBGlobalDim s_gl[kSBMaxDims];
+  __shared__ int32_t s_nst, s_ngl, s_nhash;
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x < p.n_dims) {
@@ -300,20 +408,56 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
         (dr.range != 0 && D.smem_off >= 0 && dr.range <= static_cast<uint64_t>(D.smem_cap)) ? D.smem_off : -1;
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kSBStages; ++s) {
+    for (int s = 0; s < p.n_stages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kSBConsumerWarps);
     }
     mbar_fence_init();
   }
   __syncthreads();
+  const int gd0 = p.fd.n_group > 0 ? p.fd.group_dim[0] : -1;
+  const int gd1 = p.fd.n_group > 1 ? p.fd.group_dim[1] : -1;
+  if (threadIdx.x == 0) {
+    int nst = 0, ngl = 0, nh = 0;
+    for (int j = 0; j < p.n_dims; ++j) {
+      const int d = p.fd.order[j];
+      const SBDimDev& D = p.dims[d];
+      if (s_off[d] >= 0) {
+        SBStagedDim& S = s_st[nst++];
+        S.d = d;
+        S.off = s_off[d];
+        S.seg = p.seg_off[d];
+        S.w8 = p.fk_width[d] == 8;
+        const int cap = D.smem_cap;
+        S.g0 = d == gd0 ? s_off[d] + cap * static_cast<int>(sizeof(M)) + p.fd.group_idx[0] * cap * 4 : -1;
+        S.g1 = d == gd1 ? s_off[d] + cap * static_cast<int>(sizeof(M)) + p.fd.group_idx[1] * cap * 4 : -1;
+        S.kmin = s_kmin[d];
+        S.range = s_range[d];
+      } else if (s_range[d] != 0) {
+        SBGlobalDim& G = s_gl[ngl++];
+        G.d = d;
+        G.seg = p.seg_off[d];
+        G.w8 = p.fk_width[d] == 8;
+        G.kmin = s_kmin[d];
+        G.range = s_range[d];
+        G.dq = D.dq;
+        G.g0 = d == gd0 ? D.dg[p.fd.group_idx[0]] : nullptr;
+        G.g1 = d == gd1 ? D.dg[p.fd.group_idx[1]] : nullptr;
+      } else {
+        ++nh;
+      }
+    }
+    s_nst = nst;
+    s_ngl = ngl;
+    s_nhash = nh;
+  }
   for (int d = 0; d < p.n_dims; ++d) {
     if (s_off[d] < 0) continue;
     const SBDimDev& D = p.dims[d];
-    uint64_t* q = reinterpret_cast<uint64_t*>(staged_dims + s_off[d]);
-    for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) q[i] = __ldg(D.dq + i);
+    M* q = reinterpret_cast<M*>(staged_dims + s_off[d]);
+    for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) q[i] = sb_mask_cast<M>(__ldg(D.dq + i));
     for (int c = 0; c < D.n_group; ++c) {
-      int32_t* g = reinterpret_cast<int32_t*>(staged_dims + s_off[d] + D.smem_cap * 8 + c * D.smem_cap * 4);
+      int32_t* g = reinterpret_cast<int32_t*>(staged_dims + s_off[d] + D.smem_cap * sizeof(M) + c * D.smem_cap * 4);
       for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) g[i] = __ldg(D.dg[c] + i);
     }
   }
@@ -324,9 +468,9 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
     // ---------------------------------------------------------- producer
     if (lane != 0) return;
     int64_t k = 0;
-    for (int64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x, ++k) {
-      const int s = static_cast<int>(k % kSBStages);
-      if (k >= kSBStages && !mbar_wait(&empty[s], static_cast<uint32_t>((k / kSBStages - 1) & 1))) {
+    for (int64_t tile = p.tile_begin + blockIdx.x; tile < p.tile_end; tile += gridDim.x, ++k) {
+      const int s = static_cast<int>(k % p.n_stages);
+      if (k >= p.n_stages && !mbar_wait(&empty[s], static_cast<uint32_t>((k / p.n_stages - 1) & 1))) {
         raise_status(p.st, GFPDB_ETIMEDOUT, 130);
         break;
       }
@@ -346,184 +490,149 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
     // Copies still in flight land before this CTA exits: wait for the
     // stages issued last (consumers wait on the same phases).
     const int64_t issued = k;
-    for (int64_t j = issued > kSBStages ? issued - kSBStages : 0; j < issued; ++j)
-      if (!mbar_wait(&full[j % kSBStages], static_cast<uint32_t>((j / kSBStages) & 1))) {
+    for (int64_t j = issued > p.n_stages ? issued - p.n_stages : 0; j < issued; ++j)
+      if (!mbar_wait(&full[j % p.n_stages], static_cast<uint32_t>((j / p.n_stages) & 1))) {
         raise_status(p.st, GFPDB_ETIMEDOUT, 131);
         break;
       }
     return;
   }
   // ------------------------------------------------------------ consumers
-  const int gd0 = p.fd.n_group > 0 ? p.fd.group_dim[0] : -1;
-  const int gd1 = p.fd.n_group > 1 ? p.fd.group_dim[1] : -1;
+  SBRings<M>& R = rings[warp];
+  const M qvalid = sb_mask_cast<M>(p.qvalid);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int nst = s_nst, ngl = s_ngl, nhash = s_nhash;
+  uint32_t h2 = 0, t2 = 0;  // ring 2 head / tail (entries t2 - h2), kept across tiles
   int64_t k = 0;
-  for (int64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x, ++k) {
-    const int s = static_cast<int>(k % kSBStages);
+  for (int64_t tile = p.tile_begin + blockIdx.x; tile < p.tile_end; tile += gridDim.x, ++k) {
+    const int s = static_cast<int>(k % p.n_stages);
     const SBTile t = sb_tile(p, tile, kTileRows, &part);
     const DevCol* cols = p.part_cols + static_cast<int64_t>(t.part) * p.n_cols;
-    const bool ok = mbar_wait(&full[s], static_cast<uint32_t>((k / kSBStages) & 1));
+    const bool ok = mbar_wait(&full[s], static_cast<uint32_t>((k / p.n_stages) & 1));
     if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform exit
       if (lane == 0) raise_status(p.st, GFPDB_ETIMEDOUT, 132);
       break;
     }
     const unsigned char* stage = stages + static_cast<int64_t>(s) * p.stage_bytes;
-    const int64_t r0 = static_cast<int64_t>(warp) * 32 * ITEMS + lane;  // row within the tile of item 0
-    // this lane's foreign key of dimension d, item i (stage or, for the
+    // a full tile of a 16-byte-aligned partition is wholly in the stage
+    const bool whole = p.staged && t.rows == kTileRows;
+    // foreign key of dimension d for row r of the tile (stage or, for the
     // last rows of a partition, global memory)
-    auto fk_of = [&](int d, int i) -> int64_t {
-      const int64_t r = r0 + i * 32;
-      // rows of the segment in the stage (widths are 4 or 8: a shift, not a
-      // 64-bit division per key)
-      const int64_t in_smem = static_cast<int64_t>(sb_seg_bytes(p, d, t.rows)) >> (p.fk_width[d] == 8 ? 3 : 2);
-      const unsigned char* seg = stage + p.seg_off[d];
-      if (r < in_smem)
-        return p.fk_width[d] == 8 ? reinterpret_cast<const int64_t*>(seg)[r]
-                                  : static_cast<int64_t>(reinterpret_cast<const int32_t*>(seg)[r]);
+    auto fk_of = [&](int d, int seg_off, bool w8, int64_t r) -> int64_t {
+      const unsigned char* seg = stage + seg_off;
+      if (whole || r < (static_cast<int64_t>(sb_seg_bytes(p, d, t.rows)) >> (w8 ? 3 : 2)))
+        return w8 ? reinterpret_cast<const int64_t*>(seg)[r] : static_cast<int64_t>(reinterpret_cast<const int32_t*>(seg)[r]);
       return load_int(cols[p.fd.fk_col[d]], t.start + r);
     };
-    uint64_t m[ITEMS];
-    uint32_t g0[ITEMS], g1[ITEMS];  // group column values
-    bool any = false;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      m[i] = r0 + i * 32 < t.rows ? p.qvalid : 0ull;
-      any |= m[i] != 0;
-      g0[i] = g1[i] = 0;
-    }
-    // (a) dimensions staged in shared memory, in probe order, early exit
-    for (int j = 0; j < p.n_dims && __any_sync(0xffffffffu, any); ++j) {
-      const int d = p.fd.order[j];
-      const int off = s_off[d];
-      if (off < 0) continue;
-      const uint64_t kmin = static_cast<uint64_t>(s_kmin[d]);
-      const uint64_t range = s_range[d];
-      const uint64_t* sq = reinterpret_cast<const uint64_t*>(staged_dims + off);
-      const int cap = p.dims[d].smem_cap;
-      const int c0 = d == gd0 ? p.fd.group_idx[0] : -1, c1 = d == gd1 ? p.fd.group_idx[1] : -1;
-      any = false;
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        if (m[i] == 0) continue;
-        const uint64_t idx = static_cast<uint64_t>(fk_of(d, i)) - kmin;
-        m[i] &= idx < range ? sq[idx] : 0ull;
-        if (m[i] != 0) {
-          if (c0 >= 0) g0[i] = reinterpret_cast<const uint32_t*>(staged_dims + off + cap * 8 + c0 * cap * 4)[idx];
-          if (c1 >= 0) g1[i] = reinterpret_cast<const uint32_t*>(staged_dims + off + cap * 8 + c1 * cap * 4)[idx];
-        }
-        any |= m[i] != 0;
+    // Step (2) for ring-1 entries [h1, h1 + n): global-memory dimensions.
+    auto probe_global = [&](uint32_t h1, int n) {
+      M m = 0;
+      uint32_t g0 = 0, g1 = 0, r = 0;
+      if (lane < n) {
+        const uint32_t e = (h1 + lane) & (kSBRing - 1);
+        r = R.r1[e];
+        m = R.m1[e];
+        g0 = R.g1a[e];
+        g1 = R.g1b[e];
       }
-    }
-    // (b) direct dimensions in global memory: each dimension's loads are
-    // issued before the previous dimension's results are applied
-    {
-      uint64_t pq[ITEMS];
-      uint32_t pg0[ITEMS], pg1[ITEMS];
-      bool have = false, pk0 = false, pk1 = false;
-      for (int j = 0; j < p.n_dims && __any_sync(0xffffffffu, any); ++j) {
-        const int d = p.fd.order[j];
-        if (s_off[d] >= 0 || s_range[d] == 0) continue;
+      // direct dimensions, four at a time: every load of the four issued
+      // before any is used
+      for (int j0 = 0; j0 < ngl; j0 += 4) {
+        uint64_t dq[4];
+        uint32_t dg0[4], dg1[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          dq[u] = ~0ull;
+          dg0[u] = dg1[u] = 0;
+          if (j0 + u >= ngl || m == 0) continue;
+          const SBGlobalDim& G = s_gl[j0 + u];
+          const uint64_t idx = static_cast<uint64_t>(fk_of(G.d, G.seg, G.w8, r)) - static_cast<uint64_t>(G.kmin);
+          dq[u] = 0;
+          if (idx < G.range) {
+            dq[u] = __ldg(reinterpret_cast<const unsigned long long*>(G.dq + idx));
+            if (G.g0 != nullptr) dg0[u] = static_cast<uint32_t>(__ldg(G.g0 + idx));
+            if (G.g1 != nullptr) dg1[u] = static_cast<uint32_t>(__ldg(G.g1 + idx));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (j0 + u >= ngl) break;
+          const SBGlobalDim& G = s_gl[j0 + u];
+          m &= sb_mask_cast<M>(dq[u]);
+          if (G.g0 != nullptr) g0 = dg0[u];
+          if (G.g1 != nullptr) g1 = dg1[u];
+        }
+      }
+      // dimensions looked up by hash (sparse keys)
+      for (int d = 0; nhash > 0 && d < p.n_dims; ++d) {
+        if (s_range[d] != 0 || m == 0) continue;
         const SBDimDev& D = p.dims[d];
-        const uint64_t kmin = static_cast<uint64_t>(s_kmin[d]);
-        const uint64_t range = s_range[d];
-        const int c0 = d == gd0 ? p.fd.group_idx[0] : -1, c1 = d == gd1 ? p.fd.group_idx[1] : -1;
-        uint64_t cq[ITEMS];
-        uint32_t cg0[ITEMS], cg1[ITEMS];
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-          cq[i] = 0;
-          cg0[i] = cg1[i] = 0;
-          if (m[i] == 0) continue;
-          const uint64_t idx = static_cast<uint64_t>(fk_of(d, i)) - kmin;
-          if (idx < range) {
-            cq[i] = __ldg(reinterpret_cast<const unsigned long long*>(D.dq + idx));
-            if (c0 >= 0) cg0[i] = static_cast<uint32_t>(__ldg(D.dg[c0] + idx));
-            if (c1 >= 0) cg1[i] = static_cast<uint32_t>(__ldg(D.dg[c1] + idx));
-          }
-        }
-        if (have) {
-          any = false;
-#pragma unroll
-          for (int i = 0; i < ITEMS; ++i) {
-            m[i] &= pq[i];
-            if (pk0) g0[i] = pg0[i];
-            if (pk1) g1[i] = pg1[i];
-            any |= m[i] != 0;
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-          pq[i] = cq[i];
-          pg0[i] = cg0[i];
-          pg1[i] = cg1[i];
-        }
-        pk0 = c0 >= 0;
-        pk1 = c1 >= 0;
-        have = true;
-      }
-      if (have) {
-        any = false;
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-          m[i] &= pq[i];
-          if (pk0) g0[i] = pg0[i];
-          if (pk1) g1[i] = pg1[i];
-          any |= m[i] != 0;
+        const int64_t dr = sb_lookup(D, fk_of(d, p.seg_off[d], p.fk_width[d] == 8, r));
+        m &= dr >= 0 ? sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.qmask + dr))) : M(0);
+        if (m != 0) {
+          if (d == gd0) g0 = static_cast<uint32_t>(load_int(D.group[p.fd.group_idx[0]], dr));
+          if (d == gd1) g1 = static_cast<uint32_t>(load_int(D.group[p.fd.group_idx[1]], dr));
         }
       }
-    }
-    // (c) dimensions looked up by hash (sparse keys)
-    for (int j = 0; j < p.n_dims && __any_sync(0xffffffffu, any); ++j) {
-      const int d = p.fd.order[j];
-      if (s_range[d] != 0) continue;
-      const SBDimDev& D = p.dims[d];
-      const int c0 = d == gd0 ? p.fd.group_idx[0] : -1, c1 = d == gd1 ? p.fd.group_idx[1] : -1;
-      any = false;
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i) {
-        if (m[i] == 0) continue;
-        const int64_t r = sb_lookup(D, fk_of(d, i));
-        m[i] &= r >= 0 ? __ldg(reinterpret_cast<const unsigned long long*>(D.qmask + r)) : 0ull;
-        if (m[i] != 0) {
-          if (c0 >= 0) g0[i] = static_cast<uint32_t>(load_int(D.group[c0], r));
-          if (c1 >= 0) g1[i] = static_cast<uint32_t>(load_int(D.group[c1], r));
+      // survivors into ring 2
+      const unsigned b = __ballot_sync(0xffffffffu, m != 0);
+      if (m != 0) {
+        const uint32_t e = (t2 + __popc(b & lt_mask)) & (kSBRing - 1);
+        R.part2[e] = static_cast<uint32_t>(t.part);
+        R.row2[e] = static_cast<uint32_t>(t.start + r);
+        R.m2[e] = m;
+        R.key2[e] = sb_group_key(p.fd.n_group, g0, g1);
+      }
+      t2 += __popc(b);
+      __syncwarp();
+      if (t2 - h2 >= 32) {
+        sb_update_groups<M>(p, R, h2, 32, lane);
+        h2 += 32;
+        __syncwarp();
+      }
+    };
+    uint32_t h1 = 0, t1 = 0;
+#pragma unroll 1
+    for (int i = 0; i < ITEMS; ++i) {
+      const int64_t r = static_cast<int64_t>(warp) * 32 * ITEMS + i * 32 + lane;  // row within the tile
+      M m = r < t.rows ? qvalid : M(0);
+      uint32_t g0 = 0, g1 = 0;
+      // Step (1): dimensions staged in shared memory, in probe order
+      for (int j = 0; j < nst; ++j) {
+        const SBStagedDim& S = s_st[j];
+        if (m != 0) {
+          const uint64_t idx = static_cast<uint64_t>(fk_of(S.d, S.seg, S.w8, r)) - static_cast<uint64_t>(S.kmin);
+          m &= idx < S.range ? reinterpret_cast<const M*>(staged_dims + S.off)[idx] : M(0);
+          if (m != 0 && S.g0 >= 0) g0 = reinterpret_cast<const uint32_t*>(staged_dims + S.g0)[idx];
+          if (m != 0 && S.g1 >= 0) g1 = reinterpret_cast<const uint32_t*>(staged_dims + S.g1)[idx];
         }
-        any |= m[i] != 0;
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, m != 0);
+      if (m != 0) {
+        const uint32_t e = (t1 + __popc(b & lt_mask)) & (kSBRing - 1);
+        R.r1[e] = static_cast<uint32_t>(r);
+        R.m1[e] = m;
+        R.g1a[e] = g0;
+        R.g1b[e] = g1;
+      }
+      t1 += __popc(b);
+      __syncwarp();
+      if (t1 - h1 >= 32) {
+        probe_global(h1, 32);
+        h1 += 32;
       }
     }
+    if (t1 != h1) probe_global(h1, static_cast<int>(t1 - h1));  // the tile's last rows of ring 1
     // Every foreign key this warp needs from the stage has been read.
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
-    if (!any) continue;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      uint64_t mi = m[i];
-      if (mi == 0) continue;
-      const int64_t row = t.start + r0 + i * 32;
-      uint64_t key = 0;
-      if (p.fd.n_group == 1) key = g0[i];
-      else if (p.fd.n_group == 2) key = (static_cast<uint64_t>(g0[i]) << 32) | g1[i];
-      unsigned long long vals[kSBMaxAggsFact];
-      for (int a = 0; a < p.n_aggs; ++a) {
-        const SBAgg& g = p.aggs[a];
-        if (g.fn == AGG_COUNT_STAR) {
-          vals[a] = 1ull;
-        } else {
-          uint64_t x = static_cast<uint64_t>(load_int(cols[g.a], row));
-          if (g.b >= 0) x *= static_cast<uint64_t>(load_int(cols[g.b], row));  // int64 wrap
-          vals[a] = x;
-        }
-      }
-      const uint64_t slot = sb_group_slot(p, key);
-      if (slot == UINT64_MAX) continue;
-      atomicOr(p.touched + slot, static_cast<unsigned long long>(mi));
-      while (mi != 0) {
-        const int q = __ffsll(static_cast<long long>(mi)) - 1;
-        mi &= mi - 1;
-        unsigned long long* acc =
-            p.gaccs + (static_cast<uint64_t>(q) * (p.gmask + 2) + slot) * static_cast<uint64_t>(p.n_aggs);
-        for (int a = 0; a < p.n_aggs; ++a) atomicAdd(acc + a, vals[a]);
-      }
-    }
+  }
+  // the warp's last surviving rows
+  while (t2 != h2) {
+    const int n = t2 - h2 < 32 ? static_cast<int>(t2 - h2) : 32;
+    sb_update_groups<M>(p, R, h2, n, lane);
+    h2 += n;
+    __syncwarp();
   }
 }
 
@@ -621,7 +730,8 @@ struct StarBatchState {
   BufferPtr tables_buf, masks_buf, dq_buf, drow_buf, dg_buf, krange_buf, gkeys_buf, touched_buf, gaccs_buf, misc_buf, meta_buf,
       out_q;
   BufferPtr out_g[2], out_a[kMaxAggs];
-  size_t fact_smem = 0;  // staged query masks, bytes per block
+  size_t fact_smem = 0;  // dynamic shared memory of a fact-stage block
+  int mask_bytes = 8;    // query mask width in the fact stage (4: at most 32 queries)
   std::vector<char> host_meta;
   DType group_types[2] = {DType::Int32, DType::Int32};
   uint64_t gcap = 0;
@@ -631,6 +741,25 @@ struct StarBatchState {
   unsigned long long* qcursor = nullptr;
   unsigned long long* qoff = nullptr;
   size_t ranges_host_off = 0;  // byte offset of the query ranges in host_meta / meta_buf
+  // host-resident inputs
+  struct Copy {
+    void* dst;
+    const void* src;
+    int64_t bytes;
+  };
+  std::vector<StarBatchHostColumn> host_cols;
+  std::vector<Copy> dim_copies;
+  std::vector<std::vector<Copy>> group_copies;  // per group of partitions
+  struct TileGroup {
+    int64_t begin, end, rows;
+  };
+  std::vector<TileGroup> group_tiles;
+  int64_t host_bytes = 0;
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> events;  // start, dimensions, then one per group
+
+  ~StarBatchState();
+  void plan_host_copies();
 
   void prepare(cudaStream_t s);
   void run(cudaStream_t s);
@@ -654,6 +783,81 @@ void StarBatch::set_ranges(const std::vector<std::vector<std::pair<int64_t, int6
   st_->set_ranges(q, s);
 }
 const unsigned long long* StarBatch::query_offsets() const { return st_->qoff; }
+void StarBatch::set_host_columns(std::vector<StarBatchHostColumn> cols) { st_->host_cols = std::move(cols); }
+int64_t StarBatch::host_bytes() const { return st_->host_bytes; }
+
+StarBatchState::~StarBatchState() {
+  for (cudaEvent_t e : events) (void)cudaEventDestroy(e);
+  if (copy_stream != nullptr) (void)cudaStreamDestroy(copy_stream);
+}
+
+// Which host columns each run copies, and in which order: the dimensions'
+// key, filter and group columns first, then the fact columns partition by
+// partition in up to kSBCopyGroups groups of about equal rows; the fact pass
+// runs once per group, after that group's copies.
+constexpr int kSBCopyGroups = 8;
+
+void StarBatchState::plan_host_copies() {
+  dim_copies.clear();
+  group_copies.clear();
+  group_tiles.clear();
+  host_bytes = 0;
+  if (host_cols.empty()) return;
+  auto add = [&](std::vector<Copy>& out, const void* dst, int64_t bytes) {
+    if (bytes <= 0) return;
+    for (const Copy& c : out)
+      if (c.dst == dst) return;  // a column used twice is copied once
+    for (const auto& h : host_cols)
+      if (h.dst == dst && h.bytes >= bytes) {
+        out.push_back(Copy{const_cast<void*>(dst), h.src, bytes});
+        host_bytes += bytes;
+        return;
+      }
+    // not in the list: the column is device-resident
+  };
+  for (size_t d = 0; d < dim_tables.size(); ++d) {
+    const TupleSet& t = *dim_tables[d];
+    const auto& ds = spec.dims[d];
+    const int64_t n = t.num_rows();
+    for (const std::string& c : {ds.key, ds.filter}) {
+      const auto& col = t.column(c);
+      add(dim_copies, col->data, n * dtype_width(col->type));
+    }
+    for (const auto& g : spec.group)
+      if (g.dim == static_cast<int>(d)) {
+        const auto& col = t.column(g.column);
+        add(dim_copies, col->data, n * dtype_width(col->type));
+      }
+  }
+  const int groups = static_cast<int>(std::min<size_t>(kSBCopyGroups, parts.size()));
+  const int64_t tile_rows = static_cast<int64_t>(kSBConsumerWarps) * 32 * spec.items_per_thread;
+  int64_t tiles = 0, rows_done = 0;
+  size_t pi = 0;
+  for (int g = 0; g < groups; ++g) {
+    std::vector<Copy> cs;
+    const int64_t tile_begin = tiles, rows_begin = rows_done;
+    const int64_t target = fact_rows * (g + 1) / groups;
+    while (pi < parts.size() && (rows_done < target || g == groups - 1)) {
+      const TupleSet& t = *parts[pi];
+      for (const std::string& c : fact_cols) {
+        const auto& col = t.column(c);
+        add(cs, col->data, t.num_rows() * dtype_width(col->type));
+      }
+      rows_done += t.num_rows();
+      tiles += (t.num_rows() + tile_rows - 1) / tile_rows;
+      ++pi;
+    }
+    if (tiles == tile_begin && cs.empty()) continue;
+    group_copies.push_back(std::move(cs));
+    group_tiles.push_back(TileGroup{tile_begin, tiles, rows_done - rows_begin});
+  }
+  if (copy_stream == nullptr) GF_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+  while (events.size() < group_copies.size() + 2) {
+    cudaEvent_t e = nullptr;
+    GF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    events.push_back(e);
+  }
+}
 
 void StarBatchState::prepare(cudaStream_t s) {
   if (spec.dims.empty() || spec.dims.size() > static_cast<size_t>(kSBMaxDims))
@@ -713,6 +917,8 @@ void StarBatchState::prepare(cudaStream_t s) {
       fk_width[d] = w;
       aligned &= reinterpret_cast<uintptr_t>(col->data) % 16 == 0;
     }
+    if (t.num_rows() > static_cast<int64_t>(UINT32_MAX))
+      fail(GFPDB_EUNSUPPORTED, "a batched star partition holds at most 4,294,967,295 rows");
     hbase[pi] = tiles;
     hrows[pi] = t.num_rows();
     tiles += (t.num_rows() + tile_rows - 1) / tile_rows;
@@ -730,7 +936,8 @@ void StarBatchState::prepare(cudaStream_t s) {
   }
   fact_params.staged = aligned ? 1 : 0;
   fact_params.stage_bytes = static_cast<int32_t>(stage_bytes);
-  const int64_t masks_off = kSBBarBytes + kSBStages * stage_bytes;
+  fact_params.n_stages = spec.stages;
+  const int64_t masks_off = kSBBarBytes + spec.stages * stage_bytes;
   fact_params.masks_off = static_cast<int32_t>(masks_off);
   // dimensions
   std::memset(&dims_params, 0, sizeof(dims_params));
@@ -780,20 +987,26 @@ void StarBatchState::prepare(cudaStream_t s) {
   for (int d = 0; d < nd; ++d) by_rows[d] = d;
   std::stable_sort(by_rows.begin(), by_rows.end(),
                    [&](int a, int b) { return dims_params.dims[a].rows < dims_params.dims[b].rows; });
+  // Query masks are 32 bits wide for batches of at most 32 queries.
+  mask_bytes = nq <= 32 ? 4 : 8;
+  const int64_t rings_bytes =
+      static_cast<int64_t>(kSBConsumerWarps) * (mask_bytes == 4 ? sizeof(SBRings<uint32_t>) : sizeof(SBRings<uint64_t>));
   const int64_t block_target = std::min<int64_t>(kSBSmemBudget / std::max(1, spec.blocks_per_sm), kSBSmemPerBlockMax);
-  const int64_t budget = std::max<int64_t>(0, block_target - masks_off);
+  const int64_t budget = std::max<int64_t>(0, block_target - masks_off - rings_bytes);
   int64_t staged = 0;  // bytes
   for (int d = 0; d < nd; ++d) dims_params.dims[d].smem_off = -1;
   for (int d : by_rows) {
     SBDimDev& D = dims_params.dims[d];
     const int64_t keys = (D.rows + 7) / 8 * 8;  // a dense key range needs one entry per row
-    const int64_t bytes = keys * (8 + 4 * D.n_group);  // query masks, then each group column
+    const int64_t bytes = keys * (mask_bytes + 4 * D.n_group);  // query masks, then each group column
     if (D.rows == 0 || staged + bytes > budget) continue;
     D.smem_off = static_cast<int32_t>(staged);
     D.smem_cap = static_cast<int32_t>(keys);
     staged += bytes;
   }
-  fact_smem = static_cast<size_t>(masks_off + staged);
+  const int64_t rings_off = (masks_off + staged + 15) / 16 * 16;
+  fact_params.rings_off = static_cast<int32_t>(rings_off);
+  fact_smem = static_cast<size_t>(rings_off + rings_bytes);
   if (fact_smem > static_cast<size_t>(kSBSmemMaxDynamic))
     fail(GFPDB_EUNSUPPORTED, "itemsPerThread needs more shared memory than a block can have for these key widths");
   // Probe order: as given (a permutation of the dimensions), else the staged
@@ -913,37 +1126,80 @@ void StarBatchState::prepare(cudaStream_t s) {
   qcursor = qcount + kSBMaxQueries;
   qoff = qcursor + kSBMaxQueries;
   ranges_host_off = hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8;
+  fact_params.tile_begin = 0;
+  fact_params.tile_end = n_tiles;
+  plan_host_copies();
 }
 
 // Launches with at most as many blocks as are resident at once: tiles are
 // striped over the grid, so a block that had to wait for a free SM would
 // finish its stripe after everyone else.
-template <int ITEMS>
+template <int ITEMS, typename M>
 static void launch_fact_items(const SBFactParams& p, size_t smem, int grid, cudaStream_t s) {
   // Opt in once to the largest dynamic size this engine asks for (static
   // plus dynamic shared memory above 48 KB needs it).
   static std::once_flag configured;
   std::call_once(configured, [] {
-    GF_CUDA(cudaFuncSetAttribute(sb_fact_kernel<ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GF_CUDA(cudaFuncSetAttribute(sb_fact_kernel<ITEMS, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(kSBSmemMaxDynamic)));
   });
   int per_sm = 0;
-  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sb_fact_kernel<ITEMS>, kSBFactThreads, smem));
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sb_fact_kernel<ITEMS, M>, kSBFactThreads, smem));
   if (per_sm < 1) fail(GFPDB_EUNSUPPORTED, "the batched fact stage does not fit on an SM with these settings");
   const int resident = per_sm * num_sms();
-  sb_fact_kernel<ITEMS><<<grid < resident ? grid : resident, kSBFactThreads, smem, s>>>(p);
+  sb_fact_kernel<ITEMS, M><<<grid < resident ? grid : resident, kSBFactThreads, smem, s>>>(p);
 }
 
-void StarBatchState::launch_fact(int grid, cudaStream_t s) {
-  switch (fact_params.items) {
-    case 1: launch_fact_items<1>(fact_params, fact_smem, grid, s); break;
-    case 2: launch_fact_items<2>(fact_params, fact_smem, grid, s); break;
-    case 4: launch_fact_items<4>(fact_params, fact_smem, grid, s); break;
-    default: launch_fact_items<8>(fact_params, fact_smem, grid, s); break;
+template <typename M>
+static void launch_fact_mask(const SBFactParams& p, size_t smem, int grid, cudaStream_t s) {
+  switch (p.items) {
+    case 1: launch_fact_items<1, M>(p, smem, grid, s); break;
+    case 2: launch_fact_items<2, M>(p, smem, grid, s); break;
+    case 4: launch_fact_items<4, M>(p, smem, grid, s); break;
+    default: launch_fact_items<8, M>(p, smem, grid, s); break;
   }
 }
 
+void StarBatchState::launch_fact(int grid, cudaStream_t s) {
+  if (mask_bytes == 4)
+    launch_fact_mask<uint32_t>(fact_params, fact_smem, grid, s);
+  else
+    launch_fact_mask<uint64_t>(fact_params, fact_smem, grid, s);
+}
+
+// The fact pass over tiles [begin, end), which hold `rows` fact rows.
+static void fact_pass(StarBatchState& b, int64_t begin, int64_t end, int64_t rows, cudaStream_t s) {
+  if (end <= begin) return;
+  int64_t grid = static_cast<int64_t>(num_sms()) * b.spec.blocks_per_sm;
+  if (grid > end - begin) grid = end - begin;
+  b.fact_params.tile_begin = begin;
+  b.fact_params.tile_end = end;
+  ProfScope prof("sb_fact_kernel", s);
+  b.launch_fact(static_cast<int>(grid), s);
+  after_launch("sb_fact_kernel");
+  // algorithmic bytes: every foreign key of every fact row of these tiles
+  // read once (the measures of the few surviving rows are not counted)
+  double fk_bytes = 0;
+  for (int d = 0; d < b.fact_params.n_dims; ++d) fk_bytes += b.fact_params.fk_width[d];
+  prof.stop(static_cast<double>(rows) * fk_bytes);
+}
+
 void StarBatchState::run(cudaStream_t s) {
+  const bool host = !dim_copies.empty() || !group_copies.empty();
+  if (host) {
+    // host-resident inputs: copies on their own stream, forked from s (the
+    // caller counts host_bytes per run: a captured run copies too)
+    GF_CUDA(cudaEventRecord(events[0], s));
+    GF_CUDA(cudaStreamWaitEvent(copy_stream, events[0], 0));
+    for (const Copy& c : dim_copies)
+      GF_CUDA(cudaMemcpyAsync(c.dst, c.src, static_cast<size_t>(c.bytes), cudaMemcpyHostToDevice, copy_stream));
+    GF_CUDA(cudaEventRecord(events[1], copy_stream));
+    for (size_t g = 0; g < group_copies.size(); ++g) {
+      for (const Copy& c : group_copies[g])
+        GF_CUDA(cudaMemcpyAsync(c.dst, c.src, static_cast<size_t>(c.bytes), cudaMemcpyHostToDevice, copy_stream));
+      GF_CUDA(cudaEventRecord(events[2 + g], copy_stream));
+    }
+  }
   // clear: join tables to empty, group keys to empty, accumulators / status / counters to zero
   GF_CUDA(cudaMemsetAsync(tables_buf->data(), 0xFF, tables_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(dq_buf->data(), 0, dq_buf->size(), s));
@@ -955,6 +1211,7 @@ void StarBatchState::run(cudaStream_t s) {
   GF_CUDA(cudaMemsetAsync(gaccs_buf->data(), 0, gaccs_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(misc_buf->data(), 0, misc_buf->size(), s));
   const int sms = num_sms();
+  if (host) GF_CUDA(cudaStreamWaitEvent(s, events[1], 0));  // the dimensions have landed
   {
     int64_t max_rows = 1;
     for (int d = 0; d < dims_params.n_dims; ++d) max_rows = std::max<int64_t>(max_rows, dims_params.dims[d].rows);
@@ -975,17 +1232,13 @@ void StarBatchState::run(cudaStream_t s) {
     after_launch("sb_dims_kernel");
     prof.stop(static_cast<double>(dims_params.total_rows) * 12.0);
   }
-  if (n_tiles > 0) {
-    int64_t grid = static_cast<int64_t>(sms) * spec.blocks_per_sm;
-    if (grid > n_tiles) grid = n_tiles;
-    ProfScope prof("sb_fact_kernel", s);
-    launch_fact(static_cast<int>(grid), s);
-    after_launch("sb_fact_kernel");
-    // algorithmic bytes: every foreign key of every fact row read once (the
-    // measures of the few surviving rows are not counted)
-    double fk_bytes = 0;
-    for (int d = 0; d < fact_params.n_dims; ++d) fk_bytes += fact_params.fk_width[d];
-    prof.stop(static_cast<double>(fact_rows) * fk_bytes);
+  if (host) {
+    for (size_t g = 0; g < group_tiles.size(); ++g) {
+      GF_CUDA(cudaStreamWaitEvent(s, events[2 + g], 0));
+      fact_pass(*this, group_tiles[g].begin, group_tiles[g].end, group_tiles[g].rows, s);
+    }
+  } else {
+    fact_pass(*this, 0, n_tiles, fact_rows, s);
   }
   {
     SBFinalParams fp;

@@ -383,9 +383,15 @@ int32_t gfpdb_graph_cache_clear(void);
  *                   {"function": "COUNT", "name": "cnt"}],                  (1 to 4)
  *    "queries": [[[lo, hi], ...one range per dimension...], ...],   (1 to 64)
  *    "probeOrder": [1, 2, 3, 0], "loadFactor": 0.5, "itemsPerThread": 2,
- *    "blocksPerSm": 4, "groupsHint": 1024}
+ *    "blocksPerSm": 4, "stages": 3, "groupsHint": 1024}
  * probeOrder (optional) lists every dimension once; without it the smallest
- * dimensions go first. itemsPerThread is 1, 2, 4 or 8. Dimensions with
+ * dimensions go first. itemsPerThread is 1, 2, 4 or 8; stages (2 to 8) is
+ * the depth of each block's foreign-key copy pipeline. Tables may be
+ * device-resident or in host memory: a run then first copies every column
+ * the batch reads to the device (the dimensions, then the fact partitions in
+ * groups, each group's fact pass starting as its copies land; the copied
+ * bytes are reported in stats->h2d_bytes), so changes to the host buffers
+ * between runs are seen. Pageable host tables run without a graph. Dimensions with
  * dense keys (max - min + 1 within the join table's capacity) are looked up
  * by direct address, the others by hash; the choice is made on the device
  * each run and never changes results. The result has a query_id column, then the group columns, then the

@@ -150,3 +150,46 @@ def test_batch_unaligned_columns(gpu):
     got = batch.split_by_query(batch.star_batch(workloads.star_batch_spec(parts, qs), plan.PreparedInputs(dev)).table)
     for q, ranges in enumerate(qs):
         assert got.get(q, []) == queries.star_query_ranges(tabs, parts, ranges).sorted_rows(), f"query {q}"
+
+
+@pytest.mark.parametrize("pinned,use_graph", [(True, True), (True, False), (False, True)])
+def test_batch_host_inputs_are_copied_every_run(gpu, pinned, use_graph):
+    """Host-resident tables: every run copies the columns the batch reads
+    (dimensions, then the fact partitions in groups, each group's fact pass
+    after its copies), so a change to the host buffers between runs shows up
+    in the next result; the copied bytes are counted."""
+    from flexpushdowndb_gb300.tupleset import export_host
+
+    tabs, parts, qs = small_batch(n_parts=11, n_queries=7, seed=4050)
+    exported = {k: export_host(v, pinned=pinned) for k, v in tabs.items()}
+    inputs = plan.PreparedInputs(exported)
+    spec = workloads.star_batch_spec(parts, qs)
+    dev = batch.split_by_query(batch.star_batch(spec, device(tabs)).table)
+    for _ in range(3):
+        r = batch.star_batch(spec, inputs, use_graph=use_graph)
+        assert batch.split_by_query(r.table) == dev
+    # the batch reads fk1..fk4, qty, price_cents, discount and each dimension's key, filter and group column
+    fact_bytes = sum(tabs[p].num_rows * 32 for p in parts)
+    dim_bytes = sum(tabs[f"d{i}"].num_rows * 4 * (3 if i in (2, 4) else 2) for i in range(1, 5))
+    assert r.stats["h2d_bytes"] == fact_bytes + dim_bytes
+    # change one partition's quantities and one dimension's filter column in the host buffers
+    changed = dict(tabs)
+    p3, d2 = tabs["p3"], tabs["d2"]
+    new_qty = (p3["qty"] * 3 + 1).astype(np.int32)
+    new_f = ((d2["d2_f"] + 17) % 100).astype(np.int32)
+    changed["p3"] = Table([Column(c.name, c.type, new_qty if c.name == "qty" else c.values) for c in p3.columns])
+    changed["d2"] = Table([Column(c.name, c.type, new_f if c.name == "d2_f" else c.values) for c in d2.columns])
+    _overwrite_host(exported["p3"], "qty", new_qty)
+    _overwrite_host(exported["d2"], "d2_f", new_f)
+    got = batch.split_by_query(batch.star_batch(spec, inputs, use_graph=use_graph).table)
+    for q, ranges in enumerate(qs):
+        assert got.get(q, []) == queries.star_query_ranges(changed, parts, ranges).sorted_rows(), f"query {q}"
+
+
+def _overwrite_host(ex, column, values):
+    """Write new values into an exported host table's column buffer."""
+    import ctypes
+
+    names = [ex.schema.children[i].contents.name.decode() for i in range(ex.schema.n_children)]
+    child = ex.array.array.children[names.index(column)].contents
+    ctypes.memmove(child.buffers[1], np.ascontiguousarray(values).ctypes.data, values.nbytes)
