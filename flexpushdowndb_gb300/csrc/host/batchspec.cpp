@@ -37,6 +37,7 @@ void parse_star_batch_spec(const json::Value& spec, StarBatchSpec& sp) {
   sp.blocks_per_sm = static_cast<int>(spec.get_int("blocksPerSm", 4));
   sp.stages = static_cast<int>(spec.get_int("stages", 3));
   if (sp.stages < 2 || sp.stages > 8) fail(GFPDB_EINVAL, "stages must be in [2, 8]");
+  sp.direct = spec.get_bool("direct", true);
   if (sp.blocks_per_sm < 1 || sp.blocks_per_sm > 16) fail(GFPDB_EINVAL, "blocksPerSm must be in [1, 16]");
   sp.groups_hint = spec.get_int("groupsHint", 1024);
 }

@@ -198,6 +198,7 @@ struct StarBatchSpec {
   int items_per_thread = 2;      // fact rows per consumer thread per tile: 1, 2, 4 or 8
   int blocks_per_sm = 4;         // persistent CTAs per SM
   int stages = 3;                // foreign-key tiles in flight per CTA (2 to 8)
+  bool direct = true;            // int32 keys in aligned columns: the direct fact pass
   int64_t groups_hint = 1024;    // upper bound on groups per query
 };
 

@@ -52,6 +52,7 @@ struct SBDimDev {
   uint64_t* dq;          // direct: query mask per key - min (0 = no row)
   uint32_t* drow;        // direct: row per key - min (all-ones = no row)
   int32_t* dg[2];        // direct: group column values per key - min
+  uint8_t* dclass;       // direct: segment class per key - min (kSBNoRow: no selected row)
   unsigned long long* kmin_u;  // key range, order-preserving unsigned (key ^ sign bit)
   unsigned long long* kmax_u;
   int32_t key32;
@@ -60,12 +61,39 @@ struct SBDimDev {
   int32_t smem_cap;      // keys staged when the key range fits (a multiple of 8)
 };
 
+// The queries' ranges on one dimension's filter column, as segments: the
+// distinct range ends (every lo and hi + 1) cut the values into at most
+// 2 * kSBMaxQueries + 1 segments, and within a segment every value is
+// selected by the same queries. A row's query mask is then cmask[its
+// segment], so a dimension row is described by one byte (its segment class)
+// instead of a 4- or 8-byte mask: staged in shared memory, a dimension takes
+// a quarter to an eighth of the room.
+constexpr int kSBMaxBounds = 2 * kSBMaxQueries;
+constexpr int kSBNoRow = 255;  // class of a key with no selected dimension row (mask 0)
+
+struct SBSegments {
+  int64_t n_bounds;
+  int64_t bounds[kSBMaxBounds];   // ascending, distinct
+  unsigned long long cmask[256];  // segment (number of bounds <= value) -> query mask; kSBNoRow: 0
+};
+
+// Segment of value v: the number of bounds <= v (binary search).
+__device__ __forceinline__ int sb_segment(const SBSegments& S, int64_t v) {
+  int lo = 0, hi = static_cast<int>(S.n_bounds);
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (S.bounds[mid] <= v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 struct SBDimsParams {
   SBDimDev dims[kSBMaxDims];
   int32_t n_dims;
   int32_t n_queries;
   int64_t total_rows;
-  const int64_t* ranges;  // [q][d][2] (lo, hi)
+  const SBSegments* segs;  // [dimension]
   DevStatus* st;
 };
 
@@ -116,11 +144,8 @@ __global__ void __launch_bounds__(kSBThreads) sb_dims_kernel(const __grid_consta
     const SBDimDev& D = p.dims[d];
     const int64_t r = i - D.row_base;
     const int64_t v = load_int(D.filter, r);
-    uint64_t m = 0;
-    for (int q = 0; q < p.n_queries; ++q) {
-      const int64_t* rg = p.ranges + (static_cast<int64_t>(q) * kSBMaxDims + d) * 2;
-      if (rg[0] <= v && v <= rg[1]) m |= 1ull << q;
-    }
+    const int seg = sb_segment(p.segs[d], v);
+    const uint64_t m = p.segs[d].cmask[seg];
     D.qmask[r] = m;
     if (m == 0) continue;
     const int64_t k = load_int(D.key, r);
@@ -131,6 +156,7 @@ __global__ void __launch_bounds__(kSBThreads) sb_dims_kernel(const __grid_consta
         raise_status(p.st, GFPDB_EINVAL, 100 + d);  // repeated dimension key
       } else {
         D.dq[idx] = m;
+        D.dclass[idx] = static_cast<uint8_t>(seg);
         for (int c = 0; c < D.n_group; ++c) D.dg[c][idx] = static_cast<int32_t>(load_int(D.group[c], r));
       }
       continue;
@@ -178,7 +204,7 @@ constexpr int kSBConsumerWarps = 8;
 constexpr int kSBFactThreads = (kSBConsumerWarps + 1) * 32;  // consumer warps + one producer warp
 constexpr int kSBMaxStages = 8;
 constexpr int kSBMaxAggsFact = 4;  // aggregates of a batched star query
-constexpr int kSBBarBytes = 128;  // 2 * kSBMaxStages mbarriers
+constexpr int kSBBarBytes = 256;  // 2 * kSBMaxStages mbarriers, then the staging barrier
 
 struct SBFactParams {
   SBDimDev dims[kSBMaxDims];
@@ -196,6 +222,7 @@ struct SBFactParams {
   const int64_t* part_rows;  // [n_parts]
   int64_t n_tiles;
   int64_t tile_begin, tile_end;  // tiles of this launch
+  const SBSegments* segs;        // [dimension]
   uint64_t* gkeys;               // [gcap] group keys, shared by every query (all-ones = empty)
   unsigned long long* touched;   // [gcap + 1] queries with rows in each group; slot gcap: the all-ones key
   unsigned long long* gaccs;     // [q][gcap + 1][n_aggs]
@@ -278,27 +305,36 @@ __device__ __forceinline__ uint32_t sb_seg_bytes(const SBFactParams& p, int d, i
 // barrier.
 //
 // A consumer works in three steps, each with every lane busy:
-//  (1) per row, the dimensions staged in shared memory (query masks and
-//      group values by key); the rows some query still wants are appended
-//      (ballot + prefix) to the warp's first ring;
-//  (2) per 32 ring entries, the other dimensions' lookups in global memory,
-//      the loads of up to four dimensions issued together; the surviving
-//      rows go to the warp's second ring with their group key;
+//  (1) per row, the dimensions staged in shared memory: a byte per key (its
+//      segment class) and the class -> query mask table, plus the group
+//      values the dimension carries; the rows some query still wants are
+//      appended (ballot + prefix) to the warp's first ring together with
+//      their index into each direct dimension in global memory, so the ring
+//      outlives the tile's stage;
+//  (2) per 32 entries of that ring, those dimensions' lookups, all of an
+//      entry's loads issued together; the surviving rows go to the warp's
+//      second ring with their group key;
 //  (3) per 32 entries of the second ring, the group slot (one probe of the
 //      table shared by all queries), the measures, and one atomic add per
 //      query and aggregate.
-// Without the rings a warp runs steps (2) and (3) whenever any of its lanes
-// has a surviving row, with the others idle. M is the query mask type: 32
-// bits for batches of at most 32 queries, else 64. Every wait is bounded: on
-// timeout the kernel records GFPDB_ETIMEDOUT and stops.
-constexpr int kSBRing = 64;  // entries of each per-warp ring (two chunks of 32)
+// Steps (2) and (3) wait for 32 entries, across tiles, so their memory
+// round trips are paid once per 32 rows that need them, not once per tile.
+// M is the query mask type: 32 bits for batches of at most 32 queries, else
+// 64. Every wait is bounded: on timeout the kernel records GFPDB_ETIMEDOUT
+// and stops.
+constexpr int kSBRing = 64;     // entries of each per-warp ring (two chunks of 32)
+constexpr int kSBRingDims = 2;  // direct dimensions whose lookups wait in ring 1
+constexpr int kSBFastStaged = 3;  // staged dimensions the 32-bit fast path handles
 
 template <typename M>
 struct SBRings {
-  // ring 1: rows of the current tile that passed the staged dimensions
-  uint32_t r1[kSBRing];
+  // ring 1: rows that passed the staged dimensions, with their index into
+  // each direct dimension still to look up (all-ones: key out of its range)
+  uint32_t part1[kSBRing];
+  uint32_t row1[kSBRing];
   M m1[kSBRing];
   uint32_t g1a[kSBRing], g1b[kSBRing];
+  uint32_t idx1[kSBRingDims][kSBRing];
   // ring 2: surviving rows (partition, row) with their group key
   uint32_t part2[kSBRing];
   uint32_t row2[kSBRing];
@@ -363,10 +399,12 @@ __device__ __forceinline__ void sb_update_groups(const SBFactParams& p, SBRings<
 // (step 1) and the direct dimensions in global memory (step 2).
 struct SBStagedDim {
   int32_t d;        // dimension
-  int32_t off;      // byte offset of its query masks in the staged area
+  int32_t tab;      // byte offset of its class -> query mask table in the staged area
+  int32_t cls;      // byte offset of its segment class per key
   int32_t seg;      // byte offset of its foreign keys in a stage
   int32_t w8;       // 8-byte foreign keys
   int32_t g0, g1;   // byte offsets of the values of group columns 0 / 1 it carries (-1: none)
+  int32_t pad;
   int64_t kmin;
   uint64_t range;
 };
@@ -383,8 +421,64 @@ struct SBGlobalDim {
   const int32_t* g1;
 };
 
+// Step (2) for the entries [h1, h1 + n) of ring 1 (n <= 32), one per lane;
+// survivors go to ring 2, which is worked off 32 entries at a time.
+template <typename M>
+__device__ __forceinline__ void sb_probe_global(const SBFactParams& p, SBRings<M>& R, const SBGlobalDim* gl, int nring,
+                                             uint32_t h1, int n, uint32_t& h2, uint32_t& t2, int lane) {
+  const uint32_t e1 = (h1 + lane) & (kSBRing - 1);
+  M m = 0;
+  uint32_t g0 = 0, g1 = 0, part = 0, row = 0;
+  if (lane < n) {
+    m = R.m1[e1];
+    g0 = R.g1a[e1];
+    g1 = R.g1b[e1];
+    part = R.part1[e1];
+    row = R.row1[e1];
+  }
+  uint64_t dq[kSBRingDims];
+  uint32_t dg0[kSBRingDims], dg1[kSBRingDims];
+#pragma unroll
+  for (int u = 0; u < kSBRingDims; ++u) {
+    dq[u] = ~0ull;
+    dg0[u] = dg1[u] = 0;
+    if (u >= nring || m == 0) continue;
+    const SBGlobalDim& G = gl[u];
+    const uint32_t idx = R.idx1[u][e1];
+    dq[u] = 0;
+    if (idx != 0xFFFFFFFFu) {
+      dq[u] = sizeof(M) == 4 ? static_cast<uint64_t>(__ldg(reinterpret_cast<const unsigned*>(G.dq) + 2 * idx))
+                             : __ldg(reinterpret_cast<const unsigned long long*>(G.dq) + idx);
+      if (G.g0 != nullptr) dg0[u] = static_cast<uint32_t>(__ldg(G.g0 + idx));
+      if (G.g1 != nullptr) dg1[u] = static_cast<uint32_t>(__ldg(G.g1 + idx));
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kSBRingDims; ++u) {
+    if (u >= nring) continue;
+    m &= sb_mask_cast<M>(dq[u]);
+    if (gl[u].g0 != nullptr) g0 = dg0[u];
+    if (gl[u].g1 != nullptr) g1 = dg1[u];
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, m != 0);
+  if (m != 0) {
+    const uint32_t e = (t2 + __popc(b & ((1u << lane) - 1u))) & (kSBRing - 1);
+    R.part2[e] = part;
+    R.row2[e] = row;
+    R.m2[e] = m;
+    R.key2[e] = sb_group_key(p.fd.n_group, g0, g1);
+  }
+  t2 += __popc(b);
+  __syncwarp();
+  if (t2 - h2 >= 32) {
+    sb_update_groups<M>(p, R, h2, 32, lane);
+    h2 += 32;
+    __syncwarp();
+  }
+}
+
 template <int ITEMS, typename M>
-__global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_constant__ SBFactParams p) {
+__global__ void __launch_bounds__(kSBFactThreads, 3) sb_fact_kernel(const __grid_constant__ SBFactParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + kSBMaxStages;
@@ -397,6 +491,13 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
   __shared__ SBStagedDim s_st[kSBMaxDims];
   __shared__ SBGlobalDim s_gl[kSBMaxDims];
   __shared__ int32_t s_nst, s_ngl, s_nhash;
+  // The 32-bit fast path's facts (int32 keys, at most kSBFastStaged staged
+  // dimensions): per staged dimension its foreign-key segment, smallest key,
+  // key range, class table, classes and group values (byte offsets); per
+  // ring dimension its segment, smallest key and range.
+  __shared__ uint32_t s_fst[kSBFastStaged][8];
+  __shared__ uint32_t s_frd[kSBRingDims][4];
+  __shared__ int32_t s_fast;
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x < p.n_dims) {
@@ -407,11 +508,13 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
     s_off[threadIdx.x] =
         (dr.range != 0 && D.smem_off >= 0 && dr.range <= static_cast<uint64_t>(D.smem_cap)) ? D.smem_off : -1;
   }
+  uint64_t* staging = full + 2 * kSBMaxStages;
   if (threadIdx.x == 0) {
     for (int s = 0; s < p.n_stages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kSBConsumerWarps);
     }
+    mbar_init(staging, 1);
     mbar_fence_init();
   }
   __syncthreads();
@@ -423,14 +526,18 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
       const int d = p.fd.order[j];
       const SBDimDev& D = p.dims[d];
       if (s_off[d] >= 0) {
+        // staged layout: the class -> mask table (256 masks), each group
+        // column's values, then the classes (one byte per key)
         SBStagedDim& S = s_st[nst++];
+        const int cap = D.smem_cap;
+        const int tab = 256 * static_cast<int>(sizeof(M));
         S.d = d;
-        S.off = s_off[d];
+        S.tab = s_off[d];
+        S.g0 = d == gd0 ? s_off[d] + tab + p.fd.group_idx[0] * cap * 4 : -1;
+        S.g1 = d == gd1 ? s_off[d] + tab + p.fd.group_idx[1] * cap * 4 : -1;
+        S.cls = s_off[d] + tab + D.n_group * cap * 4;
         S.seg = p.seg_off[d];
         S.w8 = p.fk_width[d] == 8;
-        const int cap = D.smem_cap;
-        S.g0 = d == gd0 ? s_off[d] + cap * static_cast<int>(sizeof(M)) + p.fd.group_idx[0] * cap * 4 : -1;
-        S.g1 = d == gd1 ? s_off[d] + cap * static_cast<int>(sizeof(M)) + p.fd.group_idx[1] * cap * 4 : -1;
         S.kmin = s_kmin[d];
         S.range = s_range[d];
       } else if (s_range[d] != 0) {
@@ -450,17 +557,58 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
     s_nst = nst;
     s_ngl = ngl;
     s_nhash = nh;
+    // fast path: int32 foreign keys and key ranges of every staged and ring
+    // dimension, at most kSBFastStaged staged dimensions, no extra lookups
+    bool fast = nst <= kSBFastStaged && ngl <= kSBRingDims && nh == 0;
+    for (int j = 0; j < nst && fast; ++j) {
+      const SBStagedDim& S = s_st[j];
+      fast = !S.w8 && S.kmin >= INT32_MIN && S.kmin <= INT32_MAX && S.range <= (1ull << 31);
+      uint32_t* f = s_fst[j];
+      f[0] = static_cast<uint32_t>(S.seg);
+      f[1] = static_cast<uint32_t>(static_cast<int32_t>(S.kmin));
+      f[2] = static_cast<uint32_t>(S.range);
+      f[3] = static_cast<uint32_t>(S.tab);
+      f[4] = static_cast<uint32_t>(S.cls);
+      f[5] = static_cast<uint32_t>(S.g0 >= 0 ? S.g0 : S.g1);  // the group column it carries, if any
+      f[6] = S.g0 >= 0 ? 0u : S.g1 >= 0 ? 1u : 2u;              // which (2: none)
+      f[7] = S.g0 >= 0 && S.g1 >= 0 ? static_cast<uint32_t>(S.g1) : 0xFFFFFFFFu;  // both: the second
+    }
+    for (int u = 0; u < ngl && fast; ++u) {
+      const SBGlobalDim& G = s_gl[u];
+      fast = !G.w8 && G.kmin >= INT32_MIN && G.kmin <= INT32_MAX && G.range <= (1ull << 31);
+      s_frd[u][0] = static_cast<uint32_t>(G.seg);
+      s_frd[u][1] = static_cast<uint32_t>(static_cast<int32_t>(G.kmin));
+      s_frd[u][2] = static_cast<uint32_t>(G.range);
+    }
+    s_fast = fast ? 1 : 0;
+  }
+  // Staging: each staged dimension's classes and group values arrive by
+  // bulk copies (16-byte multiples: the device arrays and the staged area
+  // hold whole multiples of 16 keys), the class -> mask tables by loads.
+  if (threadIdx.x == 0) {
+    uint32_t bytes = 0;
+    for (int d = 0; d < p.n_dims; ++d) {
+      if (s_off[d] < 0) continue;
+      const uint32_t keys = static_cast<uint32_t>((s_range[d] + 15) / 16 * 16);
+      bytes += keys * (1 + 4 * p.dims[d].n_group);
+    }
+    mbar_arrive_expect_tx(staging, bytes);
+    for (int d = 0; d < p.n_dims; ++d) {
+      if (s_off[d] < 0) continue;
+      const SBDimDev& D = p.dims[d];
+      const int cap = D.smem_cap;
+      const uint32_t keys = static_cast<uint32_t>((s_range[d] + 15) / 16 * 16);
+      for (int c = 0; c < D.n_group; ++c)
+        bulk_g2s(staged_dims + s_off[d] + 256 * sizeof(M) + c * cap * 4, D.dg[c], keys * 4, staging);
+      bulk_g2s(staged_dims + s_off[d] + 256 * sizeof(M) + D.n_group * cap * 4, D.dclass, keys, staging);
+    }
   }
   for (int d = 0; d < p.n_dims; ++d) {
     if (s_off[d] < 0) continue;
-    const SBDimDev& D = p.dims[d];
-    M* q = reinterpret_cast<M*>(staged_dims + s_off[d]);
-    for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) q[i] = sb_mask_cast<M>(__ldg(D.dq + i));
-    for (int c = 0; c < D.n_group; ++c) {
-      int32_t* g = reinterpret_cast<int32_t*>(staged_dims + s_off[d] + D.smem_cap * sizeof(M) + c * D.smem_cap * 4);
-      for (uint64_t i = threadIdx.x; i < s_range[d]; i += kSBFactThreads) g[i] = __ldg(D.dg[c] + i);
-    }
+    M* tab = reinterpret_cast<M*>(staged_dims + s_off[d]);
+    for (int i = threadIdx.x; i < 256; i += kSBFactThreads) tab[i] = sb_mask_cast<M>(p.segs[d].cmask[i]);
   }
+  if (!mbar_wait(staging, 0)) raise_status(p.st, GFPDB_ETIMEDOUT, 133);
   __syncthreads();  // the last block-wide barrier: roles split below
   constexpr int64_t kTileRows = static_cast<int64_t>(kSBConsumerWarps) * 32 * ITEMS;
   int part = 0;
@@ -502,7 +650,10 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
   const M qvalid = sb_mask_cast<M>(p.qvalid);
   const unsigned lt_mask = (1u << lane) - 1u;
   const int nst = s_nst, ngl = s_ngl, nhash = s_nhash;
-  uint32_t h2 = 0, t2 = 0;  // ring 2 head / tail (entries t2 - h2), kept across tiles
+  const int nring = ngl < kSBRingDims ? ngl : kSBRingDims;  // direct dimensions looked up in step (2)
+  const bool fast = s_fast != 0;
+  uint32_t h1 = 0, t1 = 0;  // ring 1 head / tail, kept across tiles
+  uint32_t h2 = 0, t2 = 0;  // ring 2 head / tail
   int64_t k = 0;
   for (int64_t tile = p.tile_begin + blockIdx.x; tile < p.tile_end; tile += gridDim.x, ++k) {
     const int s = static_cast<int>(k % p.n_stages);
@@ -524,74 +675,58 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
         return w8 ? reinterpret_cast<const int64_t*>(seg)[r] : static_cast<int64_t>(reinterpret_cast<const int32_t*>(seg)[r]);
       return load_int(cols[p.fd.fk_col[d]], t.start + r);
     };
-    // Step (2) for ring-1 entries [h1, h1 + n): global-memory dimensions.
-    auto probe_global = [&](uint32_t h1, int n) {
-      M m = 0;
-      uint32_t g0 = 0, g1 = 0, r = 0;
-      if (lane < n) {
-        const uint32_t e = (h1 + lane) & (kSBRing - 1);
-        r = R.r1[e];
-        m = R.m1[e];
-        g0 = R.g1a[e];
-        g1 = R.g1b[e];
-      }
-      // direct dimensions, four at a time: every load of the four issued
-      // before any is used
-      for (int j0 = 0; j0 < ngl; j0 += 4) {
-        uint64_t dq[4];
-        uint32_t dg0[4], dg1[4];
+    if (fast && whole) {
+      // 32-bit fast path: the whole tile is in the stage, keys are int32
+#pragma unroll 1
+      for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t r = static_cast<uint32_t>(warp * 32 * ITEMS + i * 32 + lane);
+        M m = qvalid;
+        uint32_t g0 = 0, g1 = 0;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          dq[u] = ~0ull;
-          dg0[u] = dg1[u] = 0;
-          if (j0 + u >= ngl || m == 0) continue;
-          const SBGlobalDim& G = s_gl[j0 + u];
-          const uint64_t idx = static_cast<uint64_t>(fk_of(G.d, G.seg, G.w8, r)) - static_cast<uint64_t>(G.kmin);
-          dq[u] = 0;
-          if (idx < G.range) {
-            dq[u] = __ldg(reinterpret_cast<const unsigned long long*>(G.dq + idx));
-            if (G.g0 != nullptr) dg0[u] = static_cast<uint32_t>(__ldg(G.g0 + idx));
-            if (G.g1 != nullptr) dg1[u] = static_cast<uint32_t>(__ldg(G.g1 + idx));
+        for (int j = 0; j < kSBFastStaged; ++j) {
+          if (j >= nst || m == 0) continue;
+          const uint32_t* f = s_fst[j];
+          const int32_t fk = reinterpret_cast<const int32_t*>(stage + f[0])[r];
+          const int32_t kmin = static_cast<int32_t>(f[1]);
+          const uint32_t idx = static_cast<uint32_t>(fk) - static_cast<uint32_t>(kmin);
+          M q = 0;
+          if (fk >= kmin && idx < f[2]) q = reinterpret_cast<const M*>(staged_dims + f[3])[staged_dims[f[4] + idx]];
+          m &= q;
+          if (m != 0 && f[6] != 2u) {
+            const uint32_t gv = reinterpret_cast<const uint32_t*>(staged_dims + f[5])[idx];
+            if (f[6] == 0u) g0 = gv;
+            else g1 = gv;
+            if (f[7] != 0xFFFFFFFFu) g1 = reinterpret_cast<const uint32_t*>(staged_dims + f[7])[idx];
           }
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          if (j0 + u >= ngl) break;
-          const SBGlobalDim& G = s_gl[j0 + u];
-          m &= sb_mask_cast<M>(dq[u]);
-          if (G.g0 != nullptr) g0 = dg0[u];
-          if (G.g1 != nullptr) g1 = dg1[u];
-        }
-      }
-      // dimensions looked up by hash (sparse keys)
-      for (int d = 0; nhash > 0 && d < p.n_dims; ++d) {
-        if (s_range[d] != 0 || m == 0) continue;
-        const SBDimDev& D = p.dims[d];
-        const int64_t dr = sb_lookup(D, fk_of(d, p.seg_off[d], p.fk_width[d] == 8, r));
-        m &= dr >= 0 ? sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.qmask + dr))) : M(0);
+        const unsigned b = __ballot_sync(0xffffffffu, m != 0);
         if (m != 0) {
-          if (d == gd0) g0 = static_cast<uint32_t>(load_int(D.group[p.fd.group_idx[0]], dr));
-          if (d == gd1) g1 = static_cast<uint32_t>(load_int(D.group[p.fd.group_idx[1]], dr));
+          const uint32_t e = (t1 + __popc(b & lt_mask)) & (kSBRing - 1);
+          R.part1[e] = static_cast<uint32_t>(t.part);
+          R.row1[e] = static_cast<uint32_t>(t.start) + r;
+          R.m1[e] = m;
+          R.g1a[e] = g0;
+          R.g1b[e] = g1;
+#pragma unroll
+          for (int u = 0; u < kSBRingDims; ++u) {
+            if (u >= nring) continue;
+            const int32_t fk = reinterpret_cast<const int32_t*>(stage + s_frd[u][0])[r];
+            const int32_t kmin = static_cast<int32_t>(s_frd[u][1]);
+            const uint32_t idx = static_cast<uint32_t>(fk) - static_cast<uint32_t>(kmin);
+            R.idx1[u][e] = fk >= kmin && idx < s_frd[u][2] ? idx : 0xFFFFFFFFu;
+          }
+        }
+        t1 += __popc(b);
+        __syncwarp();
+        if (t1 - h1 >= 32) {
+          sb_probe_global<M>(p, R, s_gl, nring, h1, 32, h2, t2, lane);
+          h1 += 32;
         }
       }
-      // survivors into ring 2
-      const unsigned b = __ballot_sync(0xffffffffu, m != 0);
-      if (m != 0) {
-        const uint32_t e = (t2 + __popc(b & lt_mask)) & (kSBRing - 1);
-        R.part2[e] = static_cast<uint32_t>(t.part);
-        R.row2[e] = static_cast<uint32_t>(t.start + r);
-        R.m2[e] = m;
-        R.key2[e] = sb_group_key(p.fd.n_group, g0, g1);
-      }
-      t2 += __popc(b);
       __syncwarp();
-      if (t2 - h2 >= 32) {
-        sb_update_groups<M>(p, R, h2, 32, lane);
-        h2 += 32;
-        __syncwarp();
-      }
-    };
-    uint32_t h1 = 0, t1 = 0;
+      if (lane == 0) mbar_arrive(&empty[s]);
+      continue;
+    }
 #pragma unroll 1
     for (int i = 0; i < ITEMS; ++i) {
       const int64_t r = static_cast<int64_t>(warp) * 32 * ITEMS + i * 32 + lane;  // row within the tile
@@ -602,32 +737,307 @@ __global__ void __launch_bounds__(kSBFactThreads) sb_fact_kernel(const __grid_co
         const SBStagedDim& S = s_st[j];
         if (m != 0) {
           const uint64_t idx = static_cast<uint64_t>(fk_of(S.d, S.seg, S.w8, r)) - static_cast<uint64_t>(S.kmin);
-          m &= idx < S.range ? reinterpret_cast<const M*>(staged_dims + S.off)[idx] : M(0);
+          m &= idx < S.range ? reinterpret_cast<const M*>(staged_dims + S.tab)[staged_dims[S.cls + idx]] : M(0);
           if (m != 0 && S.g0 >= 0) g0 = reinterpret_cast<const uint32_t*>(staged_dims + S.g0)[idx];
           if (m != 0 && S.g1 >= 0) g1 = reinterpret_cast<const uint32_t*>(staged_dims + S.g1)[idx];
         }
       }
+      // direct dimensions past the ring's kSBRingDims, and dimensions looked
+      // up by hash (sparse keys): per row, here
+      for (int j = nring; m != 0 && j < ngl + (nhash > 0 ? p.n_dims : 0); ++j) {
+        const bool hashed = j >= ngl;
+        const int d = hashed ? j - ngl : s_gl[j].d;
+        if (hashed && s_range[d] != 0) continue;
+        const SBDimDev& D = p.dims[d];
+        const int64_t key = fk_of(d, p.seg_off[d], p.fk_width[d] == 8, r);
+        int64_t dr = -1;
+        M q = 0;
+        if (hashed) {
+          dr = sb_lookup(D, key);
+          if (dr >= 0) q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.qmask + dr)));
+        } else {
+          const uint64_t idx = static_cast<uint64_t>(key) - static_cast<uint64_t>(s_kmin[d]);
+          if (idx < s_range[d]) {
+            q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.dq + idx)));
+            dr = static_cast<int64_t>(idx);
+          }
+        }
+        m &= q;
+        if (m != 0 && d == gd0)
+          g0 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[0]], dr) : __ldg(D.dg[p.fd.group_idx[0]] + dr));
+        if (m != 0 && d == gd1)
+          g1 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[1]], dr) : __ldg(D.dg[p.fd.group_idx[1]] + dr));
+      }
       const unsigned b = __ballot_sync(0xffffffffu, m != 0);
       if (m != 0) {
         const uint32_t e = (t1 + __popc(b & lt_mask)) & (kSBRing - 1);
-        R.r1[e] = static_cast<uint32_t>(r);
+        R.part1[e] = static_cast<uint32_t>(t.part);
+        R.row1[e] = static_cast<uint32_t>(t.start + r);
         R.m1[e] = m;
         R.g1a[e] = g0;
         R.g1b[e] = g1;
+        for (int u = 0; u < nring; ++u) {
+          const SBGlobalDim& G = s_gl[u];
+          const uint64_t idx = static_cast<uint64_t>(fk_of(G.d, G.seg, G.w8, r)) - static_cast<uint64_t>(G.kmin);
+          R.idx1[u][e] = idx < G.range ? static_cast<uint32_t>(idx) : 0xFFFFFFFFu;
+        }
       }
       t1 += __popc(b);
       __syncwarp();
       if (t1 - h1 >= 32) {
-        probe_global(h1, 32);
+        sb_probe_global<M>(p, R, s_gl, nring, h1, 32, h2, t2, lane);
         h1 += 32;
       }
     }
-    if (t1 != h1) probe_global(h1, static_cast<int>(t1 - h1));  // the tile's last rows of ring 1
     // Every foreign key this warp needs from the stage has been read.
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
-  // the warp's last surviving rows
+  // the warp's last rows: ring 1, then ring 2
+  while (t1 != h1) {
+    const int n = t1 - h1 < 32 ? static_cast<int>(t1 - h1) : 32;
+    sb_probe_global<M>(p, R, s_gl, nring, h1, n, h2, t2, lane);
+    h1 += n;
+  }
+  while (t2 != h2) {
+    const int n = t2 - h2 < 32 ? static_cast<int>(t2 - h2) : 32;
+    sb_update_groups<M>(p, R, h2, n, lane);
+    h2 += n;
+    __syncwarp();
+  }
+}
+
+// Stage 2, direct form: for int32 foreign and dimension keys in 16-byte
+// aligned columns. Every warp takes whole tiles (256 * ITEMS rows) in turn
+// and reads each 128-row slice of a tile itself, four consecutive rows per
+// lane by 16-byte loads: no producer warp, no copy stages and no waits
+// between warps, so the shared memory goes to the staged dimensions (up to
+// kSBFastStaged of them) and the rings, and each block stages them once for
+// all its warps. Steps (1)-(3) are those of sb_fact_kernel; step (1) runs
+// in 32-bit arithmetic on the lane's four rows.
+constexpr int kSBDirectWarps = 16;
+constexpr int kSBDirectThreads = kSBDirectWarps * 32;
+constexpr int kSBSlice = 128;  // rows per warp step: four per lane
+
+struct SBShared {
+  int64_t kmin[kSBMaxDims];
+  uint64_t range[kSBMaxDims];
+  int32_t off[kSBMaxDims];  // staged: byte offset in the staged area, else -1
+  SBGlobalDim gl[kSBMaxDims];
+  // staged dimensions in probe order: foreign-key column slot, smallest key,
+  // key range, class table, classes, group value offsets (-1: none)
+  int32_t st_col[kSBFastStaged];
+  int32_t st_kmin[kSBFastStaged];
+  uint32_t st_range[kSBFastStaged];
+  int32_t st_tab[kSBFastStaged], st_cls[kSBFastStaged], st_g0[kSBFastStaged], st_g1[kSBFastStaged];
+  int32_t rg_col[kSBRingDims];  // ring dimensions' foreign-key column slots
+  int32_t nst, ngl, nhash;
+};
+
+template <int ITEMS, typename M>
+__global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(const __grid_constant__ SBFactParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t staging;
+  __shared__ SBShared sh;
+  unsigned char* staged_dims = smem + p.masks_off;
+  SBRings<M>* rings = reinterpret_cast<SBRings<M>*>(smem + p.rings_off);
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int gd0 = p.fd.n_group > 0 ? p.fd.group_dim[0] : -1;
+  const int gd1 = p.fd.n_group > 1 ? p.fd.group_dim[1] : -1;
+  if (threadIdx.x < p.n_dims) {
+    const SBDimDev& D = p.dims[threadIdx.x];
+    const SBDirect dr = sb_direct(D);
+    sh.kmin[threadIdx.x] = dr.kmin;
+    sh.range[threadIdx.x] = dr.range;
+    sh.off[threadIdx.x] =
+        (dr.range != 0 && D.smem_off >= 0 && dr.range <= static_cast<uint64_t>(D.smem_cap)) ? D.smem_off : -1;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&staging, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nst = 0, ngl = 0, nh = 0;
+    uint32_t bytes = 0;
+    for (int j = 0; j < p.n_dims; ++j) {
+      const int d = p.fd.order[j];
+      const SBDimDev& D = p.dims[d];
+      if (sh.off[d] >= 0 && nst < kSBFastStaged) {
+        // staged layout: the class -> mask table (256 masks), each group
+        // column's values, then the classes (one byte per key)
+        const int cap = D.smem_cap;
+        const int tab = 256 * static_cast<int>(sizeof(M));
+        const int o = sh.off[d];
+        sh.st_col[nst] = p.fd.fk_col[d];
+        sh.st_kmin[nst] = static_cast<int32_t>(sh.kmin[d]);
+        sh.st_range[nst] = static_cast<uint32_t>(sh.range[d]);
+        sh.st_tab[nst] = o;
+        sh.st_g0[nst] = d == gd0 ? o + tab + p.fd.group_idx[0] * cap * 4 : -1;
+        sh.st_g1[nst] = d == gd1 ? o + tab + p.fd.group_idx[1] * cap * 4 : -1;
+        sh.st_cls[nst] = o + tab + D.n_group * cap * 4;
+        const uint32_t keys = static_cast<uint32_t>((sh.range[d] + 15) / 16 * 16);
+        bytes += keys * (1 + 4 * D.n_group);
+        ++nst;
+      } else if (sh.range[d] != 0) {
+        sh.off[d] = -1;  // looked up in global memory
+        SBGlobalDim& G = sh.gl[ngl];
+        G.d = d;
+        G.seg = 0;
+        G.w8 = 0;
+        G.kmin = sh.kmin[d];
+        G.range = sh.range[d];
+        G.dq = D.dq;
+        G.g0 = d == gd0 ? D.dg[p.fd.group_idx[0]] : nullptr;
+        G.g1 = d == gd1 ? D.dg[p.fd.group_idx[1]] : nullptr;
+        if (ngl < kSBRingDims) sh.rg_col[ngl] = p.fd.fk_col[d];
+        ++ngl;
+      } else {
+        ++nh;
+      }
+    }
+    sh.nst = nst;
+    sh.ngl = ngl;
+    sh.nhash = nh;
+    // classes and group values of the staged dimensions by bulk copies
+    // (16-byte multiples: the device arrays and the staged area hold whole
+    // multiples of 16 keys)
+    mbar_arrive_expect_tx(&staging, bytes);
+    for (int j = 0; j < p.n_dims; ++j) {
+      const int d = p.fd.order[j];
+      if (sh.off[d] < 0) continue;
+      const SBDimDev& D = p.dims[d];
+      const int cap = D.smem_cap;
+      const uint32_t keys = static_cast<uint32_t>((sh.range[d] + 15) / 16 * 16);
+      for (int c = 0; c < D.n_group; ++c)
+        bulk_g2s(staged_dims + sh.off[d] + 256 * sizeof(M) + c * cap * 4, D.dg[c], keys * 4, &staging);
+      bulk_g2s(staged_dims + sh.off[d] + 256 * sizeof(M) + D.n_group * cap * 4, D.dclass, keys, &staging);
+    }
+  }
+  __syncthreads();
+  for (int d = 0; d < p.n_dims; ++d) {
+    if (sh.off[d] < 0) continue;
+    M* tab = reinterpret_cast<M*>(staged_dims + sh.off[d]);
+    for (int i = threadIdx.x; i < 256; i += kSBDirectThreads) tab[i] = sb_mask_cast<M>(p.segs[d].cmask[i]);
+  }
+  if (!mbar_wait(&staging, 0)) raise_status(p.st, GFPDB_ETIMEDOUT, 134);
+  __syncthreads();
+
+  SBRings<M>& R = rings[warp];
+  const M qvalid = sb_mask_cast<M>(p.qvalid);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int nst = sh.nst, ngl = sh.ngl, nhash = sh.nhash;
+  const int nring = ngl < kSBRingDims ? ngl : kSBRingDims;
+  const bool extra = ngl > nring || nhash > 0;  // lookups step (1) makes per row
+  uint32_t h1 = 0, t1 = 0, h2 = 0, t2 = 0;
+  constexpr int64_t kTileRows = static_cast<int64_t>(kSBConsumerWarps) * 32 * ITEMS;
+  int part = 0;
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * kSBDirectWarps;
+  for (int64_t tile = p.tile_begin + static_cast<int64_t>(blockIdx.x) * kSBDirectWarps + warp; tile < p.tile_end;
+       tile += nwarps) {
+    const SBTile t = sb_tile(p, tile, kTileRows, &part);
+    const DevCol* cols = p.part_cols + static_cast<int64_t>(t.part) * p.n_cols;
+    for (int64_t sub = 0; sub < t.rows; sub += kSBSlice) {
+      const int64_t row0 = t.start + sub;  // the slice's first row in the partition
+      const int nrows = t.rows - sub < kSBSlice ? static_cast<int>(t.rows - sub) : kSBSlice;
+      const int r4 = lane * 4;  // the lane's first row in the slice
+      // foreign keys of the lane's four rows: staged and ring dimensions
+      int4 fs[kSBFastStaged], fr[kSBRingDims];
+      auto load4 = [&](int col) -> int4 {
+        const int32_t* c = static_cast<const int32_t*>(cols[col].data) + row0 + r4;
+        if (nrows == kSBSlice) return __ldg(reinterpret_cast<const int4*>(c));
+        int4 v = make_int4(0, 0, 0, 0);
+        if (r4 + 0 < nrows) v.x = __ldg(c + 0);
+        if (r4 + 1 < nrows) v.y = __ldg(c + 1);
+        if (r4 + 2 < nrows) v.z = __ldg(c + 2);
+        if (r4 + 3 < nrows) v.w = __ldg(c + 3);
+        return v;
+      };
+#pragma unroll
+      for (int j = 0; j < kSBFastStaged; ++j) fs[j] = j < nst ? load4(sh.st_col[j]) : make_int4(0, 0, 0, 0);
+#pragma unroll
+      for (int u = 0; u < kSBRingDims; ++u) fr[u] = u < nring ? load4(sh.rg_col[u]) : make_int4(0, 0, 0, 0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int rin = r4 + k;
+        M m = rin < nrows ? qvalid : M(0);
+        uint32_t g0 = 0, g1 = 0;
+        // Step (1): the staged dimensions, in probe order
+#pragma unroll
+        for (int j = 0; j < kSBFastStaged; ++j) {
+          if (j >= nst || m == 0) continue;
+          const int32_t fk = k == 0 ? fs[j].x : k == 1 ? fs[j].y : k == 2 ? fs[j].z : fs[j].w;
+          const int32_t kmin = sh.st_kmin[j];
+          const uint32_t idx = static_cast<uint32_t>(fk) - static_cast<uint32_t>(kmin);
+          M q = 0;
+          if (fk >= kmin && idx < sh.st_range[j])
+            q = reinterpret_cast<const M*>(staged_dims + sh.st_tab[j])[staged_dims[sh.st_cls[j] + idx]];
+          m &= q;
+          if (m != 0 && sh.st_g0[j] >= 0) g0 = reinterpret_cast<const uint32_t*>(staged_dims + sh.st_g0[j])[idx];
+          if (m != 0 && sh.st_g1[j] >= 0) g1 = reinterpret_cast<const uint32_t*>(staged_dims + sh.st_g1[j])[idx];
+        }
+        // direct dimensions past the ring's, and dimensions looked up by
+        // hash (sparse keys): per row, here
+        if (extra && m != 0) {
+          for (int j = nring; m != 0 && j < ngl + (nhash > 0 ? p.n_dims : 0); ++j) {
+            const bool hashed = j >= ngl;
+            const int d = hashed ? j - ngl : sh.gl[j].d;
+            if (hashed && sh.range[d] != 0) continue;
+            const SBDimDev& D = p.dims[d];
+            const int64_t key = load_int(cols[p.fd.fk_col[d]], row0 + rin);
+            int64_t dr = -1;
+            M q = 0;
+            if (hashed) {
+              dr = sb_lookup(D, key);
+              if (dr >= 0) q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.qmask + dr)));
+            } else {
+              const uint64_t idx = static_cast<uint64_t>(key) - static_cast<uint64_t>(sh.kmin[d]);
+              if (idx < sh.range[d]) {
+                q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.dq + idx)));
+                dr = static_cast<int64_t>(idx);
+              }
+            }
+            m &= q;
+            if (m != 0 && d == gd0)
+              g0 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[0]], dr)
+                                                : __ldg(D.dg[p.fd.group_idx[0]] + dr));
+            if (m != 0 && d == gd1)
+              g1 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[1]], dr)
+                                                : __ldg(D.dg[p.fd.group_idx[1]] + dr));
+          }
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, m != 0);
+        if (m != 0) {
+          const uint32_t e = (t1 + __popc(b & lt_mask)) & (kSBRing - 1);
+          R.part1[e] = static_cast<uint32_t>(t.part);
+          R.row1[e] = static_cast<uint32_t>(row0 + rin);
+          R.m1[e] = m;
+          R.g1a[e] = g0;
+          R.g1b[e] = g1;
+#pragma unroll
+          for (int u = 0; u < kSBRingDims; ++u) {
+            if (u >= nring) continue;
+            const int32_t fk = k == 0 ? fr[u].x : k == 1 ? fr[u].y : k == 2 ? fr[u].z : fr[u].w;
+            const uint64_t idx = static_cast<uint64_t>(static_cast<int64_t>(fk) - sh.gl[u].kmin);
+            R.idx1[u][e] = idx < sh.gl[u].range ? static_cast<uint32_t>(idx) : 0xFFFFFFFFu;
+          }
+        }
+        t1 += __popc(b);
+        __syncwarp();
+        if (t1 - h1 >= 32) {
+          sb_probe_global<M>(p, R, sh.gl, nring, h1, 32, h2, t2, lane);
+          h1 += 32;
+        }
+      }
+    }
+  }
+  // the warp's last rows: ring 1, then ring 2
+  while (t1 != h1) {
+    const int n = t1 - h1 < 32 ? static_cast<int>(t1 - h1) : 32;
+    sb_probe_global<M>(p, R, sh.gl, nring, h1, n, h2, t2, lane);
+    h1 += n;
+  }
   while (t2 != h2) {
     const int n = t2 - h2 < 32 ? static_cast<int>(t2 - h2) : 32;
     sb_update_groups<M>(p, R, h2, n, lane);
@@ -721,17 +1131,49 @@ uint64_t pow2_at_least(uint64_t x) {
 
 using namespace sb;
 
+// Segments of every dimension from the queries' ranges (query q, dimension
+// d: lo <= value <= hi; an empty range selects nothing).
+static void fill_segments(const std::vector<std::vector<std::pair<int64_t, int64_t>>>& queries, int nd,
+                          SBSegments* out) {
+  for (int d = 0; d < nd; ++d) {
+    SBSegments& S = out[d];
+    std::memset(&S, 0, sizeof(S));
+    std::vector<int64_t> b;
+    for (const auto& q : queries) {
+      const int64_t lo = q[d].first, hi = q[d].second;
+      if (lo > hi) continue;
+      b.push_back(lo);
+      if (hi != INT64_MAX) b.push_back(hi + 1);
+    }
+    std::sort(b.begin(), b.end());
+    b.erase(std::unique(b.begin(), b.end()), b.end());
+    S.n_bounds = static_cast<int64_t>(b.size());  // at most 2 per query
+    for (size_t i = 0; i < b.size(); ++i) S.bounds[i] = b[i];
+    // segment k holds the values v with b[k - 1] <= v < b[k]; segment 0
+    // (below every lo) and the last (from the last hi + 1 on) select nothing
+    for (size_t k = 1; k <= b.size(); ++k) {
+      const int64_t v = b[k - 1];  // every value of segment k is selected like this one
+      unsigned long long m = 0;
+      for (size_t qi = 0; qi < queries.size(); ++qi)
+        if (queries[qi][d].first <= v && v <= queries[qi][d].second) m |= 1ull << qi;
+      S.cmask[k] = m;
+    }
+    S.cmask[kSBNoRow] = 0;
+  }
+}
+
 struct StarBatchState {
   StarBatchSpec spec;
   std::vector<TupleSetPtr> parts, dim_tables;
   std::vector<std::string> fact_cols;
   SBDimsParams dims_params;
   SBFactParams fact_params;
-  BufferPtr tables_buf, masks_buf, dq_buf, drow_buf, dg_buf, krange_buf, gkeys_buf, touched_buf, gaccs_buf, misc_buf, meta_buf,
+  BufferPtr tables_buf, masks_buf, dq_buf, drow_buf, dg_buf, dclass_buf, krange_buf, gkeys_buf, touched_buf, gaccs_buf, misc_buf, meta_buf,
       out_q;
   BufferPtr out_g[2], out_a[kMaxAggs];
   size_t fact_smem = 0;  // dynamic shared memory of a fact-stage block
   int mask_bytes = 8;    // query mask width in the fact stage (4: at most 32 queries)
+  bool direct = false;   // the fact stage runs sb_fact_direct_kernel
   std::vector<char> host_meta;
   DType group_types[2] = {DType::Int32, DType::Int32};
   uint64_t gcap = 0;
@@ -937,8 +1379,6 @@ void StarBatchState::prepare(cudaStream_t s) {
   fact_params.staged = aligned ? 1 : 0;
   fact_params.stage_bytes = static_cast<int32_t>(stage_bytes);
   fact_params.n_stages = spec.stages;
-  const int64_t masks_off = kSBBarBytes + spec.stages * stage_bytes;
-  fact_params.masks_off = static_cast<int32_t>(masks_off);
   // dimensions
   std::memset(&dims_params, 0, sizeof(dims_params));
   int64_t base = 0;
@@ -987,22 +1427,33 @@ void StarBatchState::prepare(cudaStream_t s) {
   for (int d = 0; d < nd; ++d) by_rows[d] = d;
   std::stable_sort(by_rows.begin(), by_rows.end(),
                    [&](int a, int b) { return dims_params.dims[a].rows < dims_params.dims[b].rows; });
+  // The direct form (sb_fact_direct_kernel) when every foreign key and
+  // dimension key is int32 and the foreign-key columns are 16-byte aligned;
+  // else the copy pipeline (sb_fact_kernel).
+  direct = spec.direct && aligned;
+  for (int d = 0; d < nd; ++d) direct = direct && fk_width[d] == 4 && dims_params.dims[d].key32;
+  const int64_t masks_off = direct ? 0 : kSBBarBytes + spec.stages * stage_bytes;
+  fact_params.masks_off = static_cast<int32_t>(masks_off);
   // Query masks are 32 bits wide for batches of at most 32 queries.
   mask_bytes = nq <= 32 ? 4 : 8;
-  const int64_t rings_bytes =
-      static_cast<int64_t>(kSBConsumerWarps) * (mask_bytes == 4 ? sizeof(SBRings<uint32_t>) : sizeof(SBRings<uint64_t>));
+  const int64_t rings_bytes = static_cast<int64_t>(direct ? kSBDirectWarps : kSBConsumerWarps) *
+                              (mask_bytes == 4 ? sizeof(SBRings<uint32_t>) : sizeof(SBRings<uint64_t>));
   const int64_t block_target = std::min<int64_t>(kSBSmemBudget / std::max(1, spec.blocks_per_sm), kSBSmemPerBlockMax);
   const int64_t budget = std::max<int64_t>(0, block_target - masks_off - rings_bytes);
   int64_t staged = 0;  // bytes
+  int n_staged = 0;
   for (int d = 0; d < nd; ++d) dims_params.dims[d].smem_off = -1;
   for (int d : by_rows) {
     SBDimDev& D = dims_params.dims[d];
-    const int64_t keys = (D.rows + 7) / 8 * 8;  // a dense key range needs one entry per row
-    const int64_t bytes = keys * (mask_bytes + 4 * D.n_group);  // query masks, then each group column
+    if (direct && n_staged == kSBFastStaged) break;
+    const int64_t keys = (D.rows + 15) / 16 * 16;  // a dense key range needs one entry per row
+    // the class -> mask table, each group column's values, one class byte per key
+    const int64_t bytes = 256 * mask_bytes + keys * (1 + 4 * D.n_group);
     if (D.rows == 0 || staged + bytes > budget) continue;
     D.smem_off = static_cast<int32_t>(staged);
     D.smem_cap = static_cast<int32_t>(keys);
     staged += bytes;
+    ++n_staged;
   }
   const int64_t rings_off = (masks_off + staged + 15) / 16 * 16;
   fact_params.rings_off = static_cast<int32_t>(rings_off);
@@ -1049,6 +1500,7 @@ void StarBatchState::prepare(cudaStream_t s) {
   int64_t group_words = 0;
   for (int d = 0; d < nd; ++d) group_words += static_cast<int64_t>(dims_params.dims[d].mask + 1) * dims_params.dims[d].n_group;
   dg_buf = make_buffer(std::max<int64_t>(group_words, 1) * 4, s);
+  dclass_buf = make_buffer(table_words, s);
   krange_buf = make_buffer(2 * kSBMaxDims * 8, s);
   masks_buf = make_buffer(std::max<int64_t>(mask_words, 1) * 8, s);
   gkeys_buf = make_buffer(static_cast<int64_t>(gcap) * 8, s);
@@ -1057,7 +1509,7 @@ void StarBatchState::prepare(cudaStream_t s) {
   // status block, output count, then per-query counts, cursors and offsets
   misc_buf = make_buffer(sizeof(DevStatus) + 64 + 8 * (3 * kSBMaxQueries + 1), s);
   meta_buf = make_buffer(static_cast<int64_t>(hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8 +
-                                              kSBMaxQueries * kSBMaxDims * 16),
+                                              kSBMaxDims * sizeof(SBSegments)),
                          s);
   out_cap = gslots;
   out_q = make_buffer(out_cap * 4, s);
@@ -1071,6 +1523,7 @@ void StarBatchState::prepare(cudaStream_t s) {
     D.qmask = masks_buf->as<uint64_t>() + moff;
     D.dq = dq_buf->as<uint64_t>() + toff;
     D.drow = drow_buf->as<uint32_t>() + toff;
+    D.dclass = dclass_buf->as<uint8_t>() + toff;
     for (int c = 0; c < D.n_group; ++c) {
       D.dg[c] = dg_buf->as<int32_t>() + goff;
       goff += static_cast<int64_t>(D.mask + 1);
@@ -1087,21 +1540,16 @@ void StarBatchState::prepare(cudaStream_t s) {
   DevCol* dcols = reinterpret_cast<DevCol*>(meta);
   int64_t* dbase = reinterpret_cast<int64_t*>(meta + hcols.size() * sizeof(DevCol));
   int64_t* drows = dbase + hbase.size();
-  int64_t* dranges = drows + hrows.size();
-  dims_params.ranges = dranges;
+  SBSegments* dsegs = reinterpret_cast<SBSegments*>(drows + hrows.size());
+  dims_params.segs = dsegs;
   // Metadata goes up once, from host memory that this object keeps (so a
   // captured graph never needs it again).
   host_meta.assign(meta_buf->size(), 0);
   std::memcpy(host_meta.data(), hcols.data(), hcols.size() * sizeof(DevCol));
   std::memcpy(host_meta.data() + hcols.size() * sizeof(DevCol), hbase.data(), hbase.size() * 8);
   std::memcpy(host_meta.data() + hcols.size() * sizeof(DevCol) + hbase.size() * 8, hrows.data(), hrows.size() * 8);
-  int64_t* hr = reinterpret_cast<int64_t*>(host_meta.data() + hcols.size() * sizeof(DevCol) + hbase.size() * 8 +
-                                           hrows.size() * 8);
-  for (int q = 0; q < nq; ++q)
-    for (int d = 0; d < nd; ++d) {
-      hr[(q * kSBMaxDims + d) * 2] = spec.queries[q][d].first;
-      hr[(q * kSBMaxDims + d) * 2 + 1] = spec.queries[q][d].second;
-    }
+  ranges_host_off = hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8;
+  fill_segments(spec.queries, nd, reinterpret_cast<SBSegments*>(host_meta.data() + ranges_host_off));
   GF_CUDA(cudaMemcpyAsync(meta, host_meta.data(), host_meta.size(), cudaMemcpyHostToDevice, s));
   sync(s);
   fact_params.n_dims = nd;
@@ -1120,12 +1568,12 @@ void StarBatchState::prepare(cudaStream_t s) {
   fact_params.gmask = gcap - 1;
   fact_params.touched = touched_buf->as<unsigned long long>();
   fact_params.st = st;
+  fact_params.segs = dsegs;
   for (int d = 0; d < nd; ++d) fact_params.dims[d] = dims_params.dims[d];
   counter = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus));
   qcount = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus) + 64);
   qcursor = qcount + kSBMaxQueries;
   qoff = qcursor + kSBMaxQueries;
-  ranges_host_off = hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8;
   fact_params.tile_begin = 0;
   fact_params.tile_end = n_tiles;
   plan_host_copies();
@@ -1160,7 +1608,42 @@ static void launch_fact_mask(const SBFactParams& p, size_t smem, int grid, cudaS
   }
 }
 
+template <int ITEMS, typename M>
+static void launch_direct_items(const SBFactParams& p, size_t smem, int64_t tiles, cudaStream_t s) {
+  static std::once_flag configured;
+  std::call_once(configured, [] {
+    GF_CUDA(cudaFuncSetAttribute(sb_fact_direct_kernel<ITEMS, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(kSBSmemMaxDynamic)));
+  });
+  int per_sm = 0;
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sb_fact_direct_kernel<ITEMS, M>, kSBDirectThreads,
+                                                        smem));
+  if (per_sm < 1) fail(GFPDB_EUNSUPPORTED, "the batched fact stage does not fit on an SM with these settings");
+  int64_t grid = static_cast<int64_t>(per_sm) * num_sms();
+  const int64_t need = (tiles + kSBDirectWarps - 1) / kSBDirectWarps;
+  if (grid > need) grid = need;
+  sb_fact_direct_kernel<ITEMS, M><<<static_cast<int>(grid), kSBDirectThreads, smem, s>>>(p);
+}
+
+template <typename M>
+static void launch_direct_mask(const SBFactParams& p, size_t smem, int64_t tiles, cudaStream_t s) {
+  switch (p.items) {
+    case 1: launch_direct_items<1, M>(p, smem, tiles, s); break;
+    case 2: launch_direct_items<2, M>(p, smem, tiles, s); break;
+    case 4: launch_direct_items<4, M>(p, smem, tiles, s); break;
+    default: launch_direct_items<8, M>(p, smem, tiles, s); break;
+  }
+}
+
 void StarBatchState::launch_fact(int grid, cudaStream_t s) {
+  if (direct) {
+    const int64_t tiles = fact_params.tile_end - fact_params.tile_begin;
+    if (mask_bytes == 4)
+      launch_direct_mask<uint32_t>(fact_params, fact_smem, tiles, s);
+    else
+      launch_direct_mask<uint64_t>(fact_params, fact_smem, tiles, s);
+    return;
+  }
   if (mask_bytes == 4)
     launch_fact_mask<uint32_t>(fact_params, fact_smem, grid, s);
   else
@@ -1204,6 +1687,7 @@ void StarBatchState::run(cudaStream_t s) {
   GF_CUDA(cudaMemsetAsync(tables_buf->data(), 0xFF, tables_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(dq_buf->data(), 0, dq_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(drow_buf->data(), 0xFF, drow_buf->size(), s));
+  GF_CUDA(cudaMemsetAsync(dclass_buf->data(), kSBNoRow, dclass_buf->size(), s));
   GF_CUDA(cudaMemsetAsync(krange_buf->data(), 0xFF, kSBMaxDims * 8, s));  // minima
   GF_CUDA(cudaMemsetAsync(krange_buf->as<char>() + kSBMaxDims * 8, 0, kSBMaxDims * 8, s));  // maxima
   GF_CUDA(cudaMemsetAsync(gkeys_buf->data(), 0xFF, gkeys_buf->size(), s));
@@ -1275,16 +1759,16 @@ void StarBatchState::set_ranges(const std::vector<std::vector<std::pair<int64_t,
   const int nq = static_cast<int>(spec.queries.size());
   const int nd = static_cast<int>(spec.dims.size());
   if (static_cast<int>(q.size()) > nq) fail(GFPDB_EINVAL, "more queries than the batch was prepared for");
-  int64_t* hr = reinterpret_cast<int64_t*>(host_meta.data() + ranges_host_off);
-  for (int i = 0; i < nq; ++i)
-    for (int d = 0; d < nd; ++d) {
-      const bool used = i < static_cast<int>(q.size());
-      if (used && static_cast<int>(q[i].size()) != nd) fail(GFPDB_EINVAL, "each query needs one range per dimension");
-      hr[(i * kSBMaxDims + d) * 2] = used ? q[i][d].first : 1;  // unused slot: the empty range [1, 0]
-      hr[(i * kSBMaxDims + d) * 2 + 1] = used ? q[i][d].second : 0;
-    }
+  std::vector<std::vector<std::pair<int64_t, int64_t>>> all(nq);
+  for (int i = 0; i < nq; ++i) {
+    const bool used = i < static_cast<int>(q.size());
+    if (used && static_cast<int>(q[i].size()) != nd) fail(GFPDB_EINVAL, "each query needs one range per dimension");
+    // an unused slot: the empty range [1, 0] on every dimension
+    all[i] = used ? q[i] : std::vector<std::pair<int64_t, int64_t>>(nd, std::make_pair(int64_t{1}, int64_t{0}));
+  }
+  fill_segments(all, nd, reinterpret_cast<SBSegments*>(host_meta.data() + ranges_host_off));
   GF_CUDA(cudaMemcpyAsync(meta_buf->as<char>() + ranges_host_off, host_meta.data() + ranges_host_off,
-                          static_cast<size_t>(nq) * kSBMaxDims * 16, cudaMemcpyHostToDevice, s));
+                          static_cast<size_t>(nd) * sizeof(SBSegments), cudaMemcpyHostToDevice, s));
   sync(s);  // host_meta may be rewritten by the next call
 }
 

@@ -193,3 +193,19 @@ def _overwrite_host(ex, column, values):
     names = [ex.schema.children[i].contents.name.decode() for i in range(ex.schema.n_children)]
     child = ex.array.array.children[names.index(column)].contents
     ctypes.memmove(child.buffers[1], np.ascontiguousarray(values).ctypes.data, values.nbytes)
+
+
+@pytest.mark.parametrize("direct", [True, False])
+@pytest.mark.parametrize("items,blocks", [(1, 1), (2, 2), (8, 3)])
+def test_batch_direct_and_pipelined_fact_passes(gpu, direct, items, blocks):
+    """The two forms of the fact pass (warps reading their own rows, or a
+    copy pipeline feeding consumer warps) give every query its oracle rows,
+    with partitions whose sizes leave ragged slices and tiles."""
+    tabs, parts, qs = small_batch(n_parts=5, n_queries=33, seed=4060)  # 33 queries: 64-bit masks
+    dev = device(tabs)
+    for nq in (33, 9):  # and 32-bit masks
+        spec = dict(workloads.star_batch_spec(parts, qs[:nq], items_per_thread=items, blocks_per_sm=blocks),
+                    direct=direct)
+        got = batch.split_by_query(batch.star_batch(spec, dev).table)
+        for q in range(nq):
+            assert got.get(q, []) == queries.star_query_ranges(tabs, parts, qs[q]).sorted_rows(), f"query {q}"
