@@ -423,7 +423,7 @@ struct SBGlobalDim {
 
 // Step (2) for the entries [h1, h1 + n) of ring 1 (n <= 32), one per lane;
 // survivors go to ring 2, which is worked off 32 entries at a time.
-template <typename M>
+template <typename M, bool LOAD_FK = false>
 __device__ __forceinline__ void sb_probe_global(const SBFactParams& p, SBRings<M>& R, const SBGlobalDim* gl, int nring,
                                              uint32_t h1, int n, uint32_t& h2, uint32_t& t2, int lane) {
   const uint32_t e1 = (h1 + lane) & (kSBRing - 1);
@@ -444,7 +444,18 @@ __device__ __forceinline__ void sb_probe_global(const SBFactParams& p, SBRings<M
     dg0[u] = dg1[u] = 0;
     if (u >= nring || m == 0) continue;
     const SBGlobalDim& G = gl[u];
-    const uint32_t idx = R.idx1[u][e1];
+    uint32_t idx;
+    if (LOAD_FK) {
+      // the entry's foreign key of this dimension, read from its column
+      // (int32 keys: the direct form)
+      const int32_t fk =
+          __ldg(static_cast<const int32_t*>(p.part_cols[static_cast<int64_t>(part) * p.n_cols + p.fd.fk_col[G.d]].data) +
+                row);
+      const uint64_t i64 = static_cast<uint64_t>(static_cast<int64_t>(fk) - G.kmin);
+      idx = i64 < G.range ? static_cast<uint32_t>(i64) : 0xFFFFFFFFu;
+    } else {
+      idx = R.idx1[u][e1];
+    }
     dq[u] = 0;
     if (idx != 0xFFFFFFFFu) {
       dq[u] = sizeof(M) == 4 ? static_cast<uint64_t>(__ldg(reinterpret_cast<const unsigned*>(G.dq) + 2 * idx))
@@ -830,9 +841,42 @@ struct SBShared {
   int32_t st_kmin[kSBFastStaged];
   uint32_t st_range[kSBFastStaged];
   int32_t st_tab[kSBFastStaged], st_cls[kSBFastStaged], st_g0[kSBFastStaged], st_g1[kSBFastStaged];
-  int32_t rg_col[kSBRingDims];  // ring dimensions' foreign-key column slots
   int32_t nst, ngl, nhash;
 };
+
+// Step (1)'s lookups of a row in the dimensions the direct form cannot
+// stage or ring: direct dimensions past the ring's kSBRingDims, and
+// dimensions looked up by hash (sparse keys).
+template <typename M>
+__device__ __forceinline__ void sb_extra_lookups(const SBFactParams& p, const SBShared& sh, const DevCol* cols, int64_t row,
+                                              int nring, M& m, uint32_t& g0, uint32_t& g1) {
+  const int gd0 = p.fd.n_group > 0 ? p.fd.group_dim[0] : -1;
+  const int gd1 = p.fd.n_group > 1 ? p.fd.group_dim[1] : -1;
+  for (int j = nring; m != 0 && j < sh.ngl + (sh.nhash > 0 ? p.n_dims : 0); ++j) {
+    const bool hashed = j >= sh.ngl;
+    const int d = hashed ? j - sh.ngl : sh.gl[j].d;
+    if (hashed && sh.range[d] != 0) continue;
+    const SBDimDev& D = p.dims[d];
+    const int64_t key = load_int(cols[p.fd.fk_col[d]], row);
+    int64_t dr = -1;
+    M q = 0;
+    if (hashed) {
+      dr = sb_lookup(D, key);
+      if (dr >= 0) q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.qmask + dr)));
+    } else {
+      const uint64_t idx = static_cast<uint64_t>(key) - static_cast<uint64_t>(sh.kmin[d]);
+      if (idx < sh.range[d]) {
+        q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.dq + idx)));
+        dr = static_cast<int64_t>(idx);
+      }
+    }
+    m &= q;
+    if (m != 0 && d == gd0)
+      g0 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[0]], dr) : __ldg(D.dg[p.fd.group_idx[0]] + dr));
+    if (m != 0 && d == gd1)
+      g1 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[1]], dr) : __ldg(D.dg[p.fd.group_idx[1]] + dr));
+  }
+}
 
 template <int ITEMS, typename M>
 __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(const __grid_constant__ SBFactParams p) {
@@ -891,7 +935,6 @@ __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(con
         G.dq = D.dq;
         G.g0 = d == gd0 ? D.dg[p.fd.group_idx[0]] : nullptr;
         G.g1 = d == gd1 ? D.dg[p.fd.group_idx[1]] : nullptr;
-        if (ngl < kSBRingDims) sh.rg_col[ngl] = p.fd.fk_col[d];
         ++ngl;
       } else {
         ++nh;
@@ -943,7 +986,7 @@ __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(con
       const int nrows = t.rows - sub < kSBSlice ? static_cast<int>(t.rows - sub) : kSBSlice;
       const int r4 = lane * 4;  // the lane's first row in the slice
       // foreign keys of the lane's four rows: staged and ring dimensions
-      int4 fs[kSBFastStaged], fr[kSBRingDims];
+      int4 fs[kSBFastStaged];
       auto load4 = [&](int col) -> int4 {
         const int32_t* c = static_cast<const int32_t*>(cols[col].data) + row0 + r4;
         if (nrows == kSBSlice) return __ldg(reinterpret_cast<const int4*>(c));
@@ -956,57 +999,41 @@ __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(con
       };
 #pragma unroll
       for (int j = 0; j < kSBFastStaged; ++j) fs[j] = j < nst ? load4(sh.st_col[j]) : make_int4(0, 0, 0, 0);
+      // Step (1): the staged dimensions in probe order, each one's facts
+      // read once for the lane's four rows
+      M mk[4];
+      uint32_t g0k[4], g1k[4];
 #pragma unroll
-      for (int u = 0; u < kSBRingDims; ++u) fr[u] = u < nring ? load4(sh.rg_col[u]) : make_int4(0, 0, 0, 0);
+      for (int k = 0; k < 4; ++k) {
+        mk[k] = r4 + k < nrows ? qvalid : M(0);
+        g0k[k] = g1k[k] = 0;
+      }
+#pragma unroll
+      for (int j = 0; j < kSBFastStaged; ++j) {
+        if (j >= nst) break;
+        const int32_t kmin = sh.st_kmin[j];
+        const uint32_t range = sh.st_range[j];
+        const M* tab = reinterpret_cast<const M*>(staged_dims + sh.st_tab[j]);
+        const uint8_t* cls = staged_dims + sh.st_cls[j];
+        const int go0 = sh.st_g0[j], go1 = sh.st_g1[j];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int32_t fk = k == 0 ? fs[j].x : k == 1 ? fs[j].y : k == 2 ? fs[j].z : fs[j].w;
+          const uint32_t idx = static_cast<uint32_t>(fk) - static_cast<uint32_t>(kmin);
+          const bool in = mk[k] != 0 && fk >= kmin && idx < range;
+          mk[k] = in ? mk[k] & tab[cls[idx]] : M(0);
+          if (mk[k] != 0 && go0 >= 0) g0k[k] = reinterpret_cast<const uint32_t*>(staged_dims + go0)[idx];
+          if (mk[k] != 0 && go1 >= 0) g1k[k] = reinterpret_cast<const uint32_t*>(staged_dims + go1)[idx];
+        }
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int rin = r4 + k;
-        M m = rin < nrows ? qvalid : M(0);
-        uint32_t g0 = 0, g1 = 0;
-        // Step (1): the staged dimensions, in probe order
-#pragma unroll
-        for (int j = 0; j < kSBFastStaged; ++j) {
-          if (j >= nst || m == 0) continue;
-          const int32_t fk = k == 0 ? fs[j].x : k == 1 ? fs[j].y : k == 2 ? fs[j].z : fs[j].w;
-          const int32_t kmin = sh.st_kmin[j];
-          const uint32_t idx = static_cast<uint32_t>(fk) - static_cast<uint32_t>(kmin);
-          M q = 0;
-          if (fk >= kmin && idx < sh.st_range[j])
-            q = reinterpret_cast<const M*>(staged_dims + sh.st_tab[j])[staged_dims[sh.st_cls[j] + idx]];
-          m &= q;
-          if (m != 0 && sh.st_g0[j] >= 0) g0 = reinterpret_cast<const uint32_t*>(staged_dims + sh.st_g0[j])[idx];
-          if (m != 0 && sh.st_g1[j] >= 0) g1 = reinterpret_cast<const uint32_t*>(staged_dims + sh.st_g1[j])[idx];
-        }
+        M m = mk[k];
+        uint32_t g0 = g0k[k], g1 = g1k[k];
         // direct dimensions past the ring's, and dimensions looked up by
-        // hash (sparse keys): per row, here
-        if (extra && m != 0) {
-          for (int j = nring; m != 0 && j < ngl + (nhash > 0 ? p.n_dims : 0); ++j) {
-            const bool hashed = j >= ngl;
-            const int d = hashed ? j - ngl : sh.gl[j].d;
-            if (hashed && sh.range[d] != 0) continue;
-            const SBDimDev& D = p.dims[d];
-            const int64_t key = load_int(cols[p.fd.fk_col[d]], row0 + rin);
-            int64_t dr = -1;
-            M q = 0;
-            if (hashed) {
-              dr = sb_lookup(D, key);
-              if (dr >= 0) q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.qmask + dr)));
-            } else {
-              const uint64_t idx = static_cast<uint64_t>(key) - static_cast<uint64_t>(sh.kmin[d]);
-              if (idx < sh.range[d]) {
-                q = sb_mask_cast<M>(__ldg(reinterpret_cast<const unsigned long long*>(D.dq + idx)));
-                dr = static_cast<int64_t>(idx);
-              }
-            }
-            m &= q;
-            if (m != 0 && d == gd0)
-              g0 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[0]], dr)
-                                                : __ldg(D.dg[p.fd.group_idx[0]] + dr));
-            if (m != 0 && d == gd1)
-              g1 = static_cast<uint32_t>(hashed ? load_int(D.group[p.fd.group_idx[1]], dr)
-                                                : __ldg(D.dg[p.fd.group_idx[1]] + dr));
-          }
-        }
+        // hash (sparse keys): per row, out of line
+        if (extra && m != 0) sb_extra_lookups<M>(p, sh, cols, row0 + rin, nring, m, g0, g1);
         const unsigned b = __ballot_sync(0xffffffffu, m != 0);
         if (m != 0) {
           const uint32_t e = (t1 + __popc(b & lt_mask)) & (kSBRing - 1);
@@ -1015,18 +1042,11 @@ __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(con
           R.m1[e] = m;
           R.g1a[e] = g0;
           R.g1b[e] = g1;
-#pragma unroll
-          for (int u = 0; u < kSBRingDims; ++u) {
-            if (u >= nring) continue;
-            const int32_t fk = k == 0 ? fr[u].x : k == 1 ? fr[u].y : k == 2 ? fr[u].z : fr[u].w;
-            const uint64_t idx = static_cast<uint64_t>(static_cast<int64_t>(fk) - sh.gl[u].kmin);
-            R.idx1[u][e] = idx < sh.gl[u].range ? static_cast<uint32_t>(idx) : 0xFFFFFFFFu;
-          }
         }
         t1 += __popc(b);
         __syncwarp();
         if (t1 - h1 >= 32) {
-          sb_probe_global<M>(p, R, sh.gl, nring, h1, 32, h2, t2, lane);
+          sb_probe_global<M, true>(p, R, sh.gl, nring, h1, 32, h2, t2, lane);
           h1 += 32;
         }
       }
@@ -1035,7 +1055,7 @@ __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(con
   // the warp's last rows: ring 1, then ring 2
   while (t1 != h1) {
     const int n = t1 - h1 < 32 ? static_cast<int>(t1 - h1) : 32;
-    sb_probe_global<M>(p, R, sh.gl, nring, h1, n, h2, t2, lane);
+    sb_probe_global<M, true>(p, R, sh.gl, nring, h1, n, h2, t2, lane);
     h1 += n;
   }
   while (t2 != h2) {
