@@ -182,6 +182,14 @@ SIGNATURES = {
     "gfpdb_server_wait": (_I32, [_P, ctypes.c_uint64, _I64, _S, _A, ctypes.POINTER(RequestStats)]),
     "gfpdb_server_get_stats": (_I32, [_P, ctypes.POINTER(ServerStats)]),
     "gfpdb_server_destroy": (_I32, [_P]),
+    "gfpdb_batch_prepare": (_I32, [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A),
+                                   ctypes.POINTER(_P)]),
+    "gfpdb_batch_launch": (_I32, [_P, _P]),
+    "gfpdb_batch_wait": (_I32, [_P, ctypes.POINTER(ExecStats), ctypes.POINTER(_I64)]),
+    "gfpdb_batch_run": (_I32, [_P, ctypes.POINTER(ExecStats), _P, ctypes.POINTER(_I64)]),
+    "gfpdb_batch_layout": (_I32, [_P, _I32, ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.c_char_p, _I64,
+                                  ctypes.POINTER(_P)]),
+    "gfpdb_batch_free": (None, [_P]),
     "gfpdb_star_batch": (
         _I32,
         [ctypes.c_char_p, _I32, _CP, ctypes.POINTER(_S), ctypes.POINTER(_A), _I32, _I32, _S, _A,

@@ -220,6 +220,7 @@ struct BatchEntry {
   StarBatch batch;
   cudaGraphExec_t exec = nullptr;
   uint64_t kernels = 0;
+  std::vector<CopySpan> spans;  // a prepared batch's result pack
   ~BatchEntry() {
     if (exec) (void)cudaGraphExecDestroy(exec);
   }
@@ -243,6 +244,42 @@ void remember_batch(const std::string& key, std::shared_ptr<BatchEntry> be) {
 void clear_batches() {
   std::lock_guard<std::mutex> lk(g_batch_mu);
   g_batches.clear();
+}
+
+// The input tables of a batched star query: device tables are used in
+// place; host tables get device copies here, and every run refreshes the
+// columns the batch reads from the host buffers (host_cols).
+struct BatchInputs {
+  std::map<std::string, TupleSetPtr> tables;
+  std::vector<StarBatchHostColumn> host_cols;
+  bool pageable = false;  // some host table is in pageable memory
+};
+
+BatchInputs import_batch_inputs(int32_t n_tables, const char* const* table_names, const ArrowSchema* const* schemas,
+                                const ArrowDeviceArray* const* arrays, cudaStream_t s) {
+  BatchInputs in;
+  for (int32_t i = 0; i < n_tables; ++i) {
+    require(table_names[i] != nullptr && arrays[i] != nullptr, "null table");
+    const int32_t dt = arrays[i]->device_type;
+    if (dt != ARROW_DEVICE_CUDA && dt != ARROW_DEVICE_CPU && dt != ARROW_DEVICE_CUDA_HOST)
+      fail(GFPDB_EUNSUPPORTED, "unsupported ArrowDeviceArray device_type " + std::to_string(dt));
+    TupleSetPtr t = import_tupleset(schemas[i], arrays[i], s, false);
+    if (dt != ARROW_DEVICE_CUDA) {
+      in.pageable |= dt == ARROW_DEVICE_CPU;
+      const ArrowArray& a = arrays[i]->array;
+      for (int c = 0; c < t->num_columns(); ++c) {
+        const auto& col = t->column(c);
+        if (col->type == DType::Utf8) continue;
+        const int w = dtype_width(col->type);
+        const ArrowArray* ch = a.children[c];
+        const char* src = static_cast<const char*>(ch->buffers[1]) + (ch->offset + a.offset) * w;
+        if (col->data != src) in.host_cols.push_back(StarBatchHostColumn{col->data, src, t->num_rows() * w});
+      }
+    }
+    in.tables[table_names[i]] = t;
+  }
+  sync(s);  // the first copies have landed
+  return in;
 }
 
 std::shared_ptr<BatchEntry> make_batch(const json::Value& spec, const std::map<std::string, TupleSetPtr>& tables,
@@ -990,34 +1027,9 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
       } catch (const std::exception& e) {
         fail(GFPDB_EINVAL, e.what());
       }
-      std::map<std::string, TupleSetPtr> tables;
-      std::vector<StarBatchHostColumn> host_cols;
-      bool pageable = false;
-      for (int32_t i = 0; i < n_tables; ++i) {
-        require(table_names[i] != nullptr && arrays[i] != nullptr, "null table");
-        const int32_t dt = arrays[i]->device_type;
-        if (dt != ARROW_DEVICE_CUDA && dt != ARROW_DEVICE_CPU && dt != ARROW_DEVICE_CUDA_HOST)
-          fail(GFPDB_EUNSUPPORTED, "unsupported ArrowDeviceArray device_type " + std::to_string(dt));
-        // Host tables get device copies here; every run refreshes the
-        // columns the batch reads from the host buffers.
-        TupleSetPtr t = import_tupleset(schemas[i], arrays[i], s, false);
-        if (dt != ARROW_DEVICE_CUDA) {
-          pageable |= dt == ARROW_DEVICE_CPU;
-          const ArrowArray& a = arrays[i]->array;
-          for (int c = 0; c < t->num_columns(); ++c) {
-            const auto& col = t->column(c);
-            if (col->type == DType::Utf8) continue;
-            const int w = dtype_width(col->type);
-            const ArrowArray* ch = a.children[c];
-            const char* src = static_cast<const char*>(ch->buffers[1]) + (ch->offset + a.offset) * w;
-            if (col->data != src) host_cols.push_back(StarBatchHostColumn{col->data, src, t->num_rows() * w});
-          }
-        }
-        tables[table_names[i]] = t;
-      }
-      sync(s);  // the first copies have landed
+      BatchInputs in = import_batch_inputs(n_tables, table_names, schemas, arrays, s);
       // pageable host memory cannot be copied from inside a CUDA graph
-      be = make_batch(spec, tables, use_graph != 0 && !pageable, s, std::move(host_cols));
+      be = make_batch(spec, in.tables, use_graph != 0 && !in.pageable, s, std::move(in.host_cols));
       remember_batch(key, be);
     }
     if (be->exec != nullptr) {
@@ -1047,6 +1059,200 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
     }
   });
 }
+
+// ------------------------------------------------------- prepared batches
+
+struct gfpdb_batch {
+  std::shared_ptr<BatchEntry> be;
+  TupleSetPtr result;       // the batch's device result view
+  char* pinned = nullptr;   // status, row count and result columns, packed by the run
+  int64_t pinned_bytes = 0;
+  int64_t status_off = 0, count_off = 0;
+  std::vector<int64_t> col_off;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool in_flight = false;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;  // kernels per run
+  ~gfpdb_batch() {
+    if (in_flight && ev[1] != nullptr) (void)cudaEventSynchronize(ev[1]);
+    for (auto e : ev)
+      if (e) (void)cudaEventDestroy(e);
+    be.reset();
+    if (pinned) (void)cudaFreeHost(pinned);
+  }
+};
+
+namespace {
+
+// One run of a prepared batch on stream s: the stages, then the pack of its
+// status, row count and result columns into page-locked memory.
+void batch_run_and_pack(gfpdb_batch& b, const std::vector<CopySpan>& spans, cudaStream_t s) {
+  b.be->batch.run(s);
+  pack_spans(spans, b.pinned, s);
+}
+
+}  // namespace
+
+int32_t gfpdb_batch_prepare(const char* spec_json, int32_t n_tables, const char* const* table_names,
+                            const ArrowSchema* const* schemas, const ArrowDeviceArray* const* arrays,
+                            gfpdb_batch** out) {
+  return guarded([&] {
+    require(spec_json != nullptr && out != nullptr, "null argument");
+    ensure_device();
+    cudaStream_t s = nullptr;
+    json::Value spec;
+    try {
+      spec = json::parse(spec_json);
+    } catch (const std::exception& e) {
+      fail(GFPDB_EINVAL, e.what());
+    }
+    BatchInputs in = import_batch_inputs(n_tables, table_names, schemas, arrays, s);
+    auto b = std::make_unique<gfpdb_batch>();
+    b->be = make_batch(spec, in.tables, false, s, std::move(in.host_cols));
+    b->result = b->be->batch.result_view();
+    const TupleSet& r = *b->result;
+    std::vector<CopySpan> spans;
+    int64_t off = 0;
+    auto add = [&](const void* src, int64_t bytes) {
+      const int64_t o = off;
+      spans.push_back(CopySpan{src, bytes, o});
+      off += (bytes + 255) / 256 * 256;
+      return o;
+    };
+    b->status_off = add(b->be->batch.status(), sizeof(DevStatus));
+    b->count_off = add(r.rows_dev(), sizeof(int64_t));
+    for (int i = 0; i < r.num_columns(); ++i) {
+      const auto& c = r.column(i);
+      b->col_off.push_back(add(c->data, r.num_rows() * dtype_width(c->type)));
+    }
+    b->pinned_bytes = off;
+    GF_CUDA(cudaMallocHost(reinterpret_cast<void**>(&b->pinned), static_cast<size_t>(off)));
+    std::memset(b->pinned, 0, static_cast<size_t>(off));
+    GF_CUDA(cudaEventCreate(&b->ev[0]));
+    GF_CUDA(cudaEventCreate(&b->ev[1]));
+    if (!in.pageable) {
+      // capture the run and the pack as one graph (pageable host memory
+      // cannot be copied from inside a graph: such batches run uncaptured)
+      cudaStream_t cs = nullptr;
+      GF_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      const uint64_t k0 = g_kernel_launches.load();
+      cudaGraph_t graph = nullptr;
+      bool ok = true;
+      GF_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      try {
+        batch_run_and_pack(*b, spans, cs);
+      } catch (const std::exception&) {
+        ok = false;
+      }
+      if (cudaStreamEndCapture(cs, &graph) != cudaSuccess) ok = false;
+      if (ok && cudaGraphInstantiate(&b->be->exec, graph, 0) != cudaSuccess) ok = false;
+      if (graph) (void)cudaGraphDestroy(graph);
+      (void)cudaGetLastError();
+      (void)cudaStreamDestroy(cs);
+      b->launches = static_cast<int64_t>(g_kernel_launches.load() - k0);
+      if (!ok) fail(GFPDB_ECUDA, "capturing the batched star query failed");
+    }
+    b->be->spans = std::move(spans);
+    *out = b.release();
+  });
+}
+
+int32_t gfpdb_batch_launch(gfpdb_batch* b, void* stream) {
+  return guarded([&] {
+    require(b != nullptr, "null argument");
+    if (b->in_flight) fail(GFPDB_EINVAL, "this prepared batch is already running; prepare a second copy");
+    cudaStream_t s = as_stream(stream);
+    GF_CUDA(cudaEventRecord(b->ev[0], s));
+    const uint64_t k0 = g_kernel_launches.load();
+    if (b->be->exec != nullptr) {
+      GF_CUDA(cudaGraphLaunch(b->be->exec, s));
+      count_launch(static_cast<uint64_t>(b->launches));
+    } else {
+      batch_run_and_pack(*b, b->be->spans, s);
+      b->launches = static_cast<int64_t>(g_kernel_launches.load() - k0);
+    }
+    GF_CUDA(cudaEventRecord(b->ev[1], s));
+    b->stream = s;
+    b->in_flight = true;
+  });
+}
+
+int32_t gfpdb_batch_wait(gfpdb_batch* b, gfpdb_exec_stats* stats, int64_t* n_rows) {
+  return guarded([&] {
+    require(b != nullptr && n_rows != nullptr, "null argument");
+    if (!b->in_flight) fail(GFPDB_EINVAL, "the prepared batch has no run to wait for");
+    const auto t0 = std::chrono::steady_clock::now();
+    {
+      struct Reset {
+        gfpdb_batch* b;
+        ~Reset() { b->in_flight = false; }
+      } reset{b};
+      // a batch is short: poll its end, then fall back to a blocking wait
+      for (;;) {
+        const cudaError_t q = cudaEventQuery(b->ev[1]);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) GF_CUDA(q);
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(2000)) {
+          GF_CUDA(cudaEventSynchronize(b->ev[1]));
+          break;
+        }
+      }
+    }
+    const DevStatus& st = *reinterpret_cast<const DevStatus*>(b->pinned + b->status_off);
+    if (st.code == GFPDB_EINVAL && st.detail >= 100 && st.detail < 110)
+      fail(GFPDB_EINVAL, "batched star query: dimension " + std::to_string(st.detail - 100) + " repeats a key");
+    raise_device_status(st, "batched star query");
+    const int64_t n = *reinterpret_cast<const int64_t*>(b->pinned + b->count_off);
+    if (n < 0 || n > b->result->num_rows()) fail(GFPDB_EDEVICE, "batched star query produced an out-of-range row count");
+    *n_rows = n;
+    copy_counters().h2d += b->be->batch.host_bytes();
+    copy_counters().d2h += b->pinned_bytes;
+    if (stats != nullptr) {
+      float ms = 0;
+      GF_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+      stats->device_ns = static_cast<int64_t>(static_cast<double>(ms) * 1e6);
+      stats->kernel_launches = b->launches;
+      stats->h2d_bytes = b->be->batch.host_bytes();
+      stats->d2h_bytes = b->pinned_bytes;
+      stats->num_ops = 3;
+      stats->messages = 0;
+      stats->elapsed_ns =
+          std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    }
+  });
+}
+
+int32_t gfpdb_batch_run(gfpdb_batch* b, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows) {
+  const int32_t rc = gfpdb_batch_launch(b, stream);
+  if (rc != GFPDB_OK) return rc;
+  return gfpdb_batch_wait(b, stats, n_rows);
+}
+
+int32_t gfpdb_batch_layout(const gfpdb_batch* b, int32_t max_columns, int64_t* capacity, int32_t* n_columns,
+                           char* names, int64_t names_capacity, const void** values) {
+  return guarded([&] {
+    require(b != nullptr && capacity != nullptr && n_columns != nullptr && names != nullptr && values != nullptr,
+            "null argument");
+    const TupleSet& r = *b->result;
+    require(r.num_columns() <= max_columns, "more columns than max_columns");
+    int64_t at = 0;
+    auto put = [&](const char* str) {
+      const int64_t len = static_cast<int64_t>(std::strlen(str)) + 1;
+      require(at + len <= names_capacity, "column names exceed names_capacity");
+      std::memcpy(names + at, str, static_cast<size_t>(len));
+      at += len;
+    };
+    *capacity = r.num_rows();
+    *n_columns = r.num_columns();
+    for (int i = 0; i < r.num_columns(); ++i) {
+      put(r.field(i).name.c_str());
+      put(dtype_format(r.field(i).type));
+      values[i] = b->pinned + b->col_off[static_cast<size_t>(i)];
+    }
+  });
+}
+
+void gfpdb_batch_free(gfpdb_batch* b) { delete b; }
 
 int32_t gfpdb_plan_prepare(const char* plan_json, int32_t n_tables, const char* const* table_names,
                            const ArrowSchema* const* schemas, const ArrowDeviceArray* const* arrays,

@@ -403,6 +403,31 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
                          int32_t use_graph, int32_t result_to_host, struct ArrowSchema* out_schema,
                          struct ArrowDeviceArray* out, gfpdb_exec_stats* stats, void* stream);
 
+/* Prepared batches: a batched star query bound once to its tables (which
+ * the caller keeps alive and unchanged in place; host tables are re-read by
+ * every run), for callers that run the same batch of queries repeatedly.
+ * Prepare captures the stages and a pack of the result into page-locked host
+ * memory as one CUDA graph; a run is one graph launch (gfpdb_batch_launch
+ * returns at once) and a wait for it (gfpdb_batch_wait: status and row
+ * count), and the result is read through gfpdb_batch_layout's pointers
+ * (query_id, group columns, aggregates; rows [0, n_rows)), valid until the
+ * next run. One run at a time per prepared batch: two prepared copies can be
+ * launched back to back, each waited for while the other runs. The same
+ * kernels as gfpdb_star_batch (above), without its per-call lookup, device
+ * synchronizations and result export. */
+typedef struct gfpdb_batch gfpdb_batch;
+int32_t gfpdb_batch_prepare(const char* spec_json, int32_t n_tables, const char* const* table_names,
+                            const struct ArrowSchema* const* schemas, const struct ArrowDeviceArray* const* arrays,
+                            gfpdb_batch** out);
+int32_t gfpdb_batch_launch(gfpdb_batch* batch, void* stream);
+int32_t gfpdb_batch_wait(gfpdb_batch* batch, gfpdb_exec_stats* stats, int64_t* n_rows);
+int32_t gfpdb_batch_run(gfpdb_batch* batch, gfpdb_exec_stats* stats, void* stream, int64_t* n_rows);
+/* Names and Arrow formats ("name\0format\0" pairs) and host pointers of the
+ * result columns (all fixed-width), and the row capacity. */
+int32_t gfpdb_batch_layout(const gfpdb_batch* batch, int32_t max_columns, int64_t* capacity, int32_t* n_columns,
+                           char* names, int64_t names_capacity, const void** values);
+void gfpdb_batch_free(gfpdb_batch* batch);
+
 /* ------------------------------------------------------------ request server */
 
 /* The serving form: a request server on one GPU with an HBM-resident column

@@ -209,3 +209,44 @@ def test_batch_direct_and_pipelined_fact_passes(gpu, direct, items, blocks):
         got = batch.split_by_query(batch.star_batch(spec, dev).table)
         for q in range(nq):
             assert got.get(q, []) == queries.star_query_ranges(tabs, parts, qs[q]).sorted_rows(), f"query {q}"
+
+
+def test_prepared_batch_launch_wait(gpu):
+    """Prepared batches (gfpdb_batch_prepare / launch / wait): results equal
+    the one-call form's; two prepared copies run back to back; a second
+    launch before the wait is refused, and so is a wait with nothing
+    launched."""
+    tabs, parts, qs = small_batch(n_parts=7, n_queries=12, seed=4070)
+    dev = device(tabs)
+    spec = workloads.star_batch_spec(parts, qs)
+    want = batch.split_by_query(batch.star_batch(spec, dev).table)
+    a, b = batch.PreparedBatch(spec, dev), batch.PreparedBatch(spec, dev)
+    for _ in range(2):
+        assert batch.split_by_query(a.execute().table) == want
+    a.launch()
+    for k in range(5):
+        (b if k % 2 == 0 else a).launch()
+        r = (a if k % 2 == 0 else b).wait()
+        assert batch.split_by_query(r.table) == want
+    assert batch.split_by_query(b.wait().table) == want
+    b.launch()
+    with pytest.raises(GfpdbError):
+        b.launch()
+    b.wait()
+    with pytest.raises(GfpdbError):
+        b.wait()
+    # host inputs (pinned): re-read by every run
+    from flexpushdowndb_gb300.tupleset import export_host
+
+    exported = {k: export_host(v, pinned=True) for k, v in tabs.items()}
+    h = batch.PreparedBatch(spec, plan.PreparedInputs(exported))
+    r = h.execute()
+    assert batch.split_by_query(r.table) == want
+    assert r.stats["h2d_bytes"] > 0
+    new_qty = (tabs["p2"]["qty"] + 5).astype(np.int32)
+    _overwrite_host(exported["p2"], "qty", new_qty)
+    changed = dict(tabs)
+    changed["p2"] = Table([Column(c.name, c.type, new_qty if c.name == "qty" else c.values) for c in tabs["p2"].columns])
+    got = batch.split_by_query(h.execute().table)
+    for q, ranges in enumerate(qs):
+        assert got.get(q, []) == queries.star_query_ranges(changed, parts, ranges).sorted_rows(), f"query {q}"
