@@ -20,10 +20,12 @@ runs; the sequential figure (one at a time) is reported beside it.
   plain : the same 32 queries, each its own physical plan (scans, filters,
           bloom predicate transfer, four hash joins, group-by) launched
           operator by operator: the drop-in per-query path;
-  e2e   : the same call with the tables in pinned host memory: each step
-          copies every column the batch reads (1.92 GB) to the device, the
-          fact pass of each group of partitions starting as its copies land,
-          and reads the result back.
+  e2e   : the same prepared batches with the tables in pinned host
+          memory: each step copies the columns the fact pass reads in full
+          (the dimensions and the staged dimensions' foreign keys, 0.72 GB),
+          the fact pass of each group of partitions starting as its copies
+          land, reads the columns it needs for a few rows only in place, and
+          reads the result back.
 Every query's result is compared with Arrow's (a committed fixture) and with
 its plain plan's. The dominant kernel's roofline comes from a profiled pass
 (CUDA events around every launch on its stream).
@@ -1006,8 +1008,10 @@ def main():
                 "h2d_bytes_per_step": e2e_stats["h2d_bytes"], "d2h_bytes_per_step": e2e_stats["d2h_bytes"],
                 "ms_per_step": 1e3 * e2e_s,
                 "path": "prepared batches over pinned host tables (two copies on two streams, launched alternately): "
-                        "every step copies each column the batch reads, the fact pass of each group of partitions "
-                        "starting as its copies land, and reads its result"},
+                        "every step copies the dimension columns and the foreign keys the fact pass reads in full, "
+                        "the fact pass of each group of partitions starting as its copies land, reads the other "
+                        "fact columns (read for some rows only) in place over NVLink-C2C, and reads its result",
+                "h2d_bytes": "copied bytes + one 32-byte sector per row and column read in place (an upper bound)"},
         "gpu_launches": launches,
         "roofline": roofline,
         "kernels": {n: {"launches_per_step": v["launches"] / 3, "us_per_step": 1e3 * v["ms"] / 3}

@@ -1038,10 +1038,13 @@ int32_t gfpdb_star_batch(const char* spec_json, int32_t n_tables, const char* co
     } else {
       be->batch.run(s);
     }
-    copy_counters().h2d += be->batch.host_bytes();
     DevStatus st;
+    unsigned long long gathered[2] = {0, 0};
     GF_CUDA(cudaMemcpyAsync(&st, be->batch.status(), sizeof(st), cudaMemcpyDeviceToHost, s));
+    GF_CUDA(cudaMemcpyAsync(gathered, be->batch.gathered(), sizeof(gathered), cudaMemcpyDeviceToHost, s));
     sync(s);
+    // bytes from host memory: the copies, and the reads in place
+    copy_counters().h2d += be->batch.host_bytes() + be->batch.in_place_bytes(gathered[0], gathered[1]);
     if (st.code == GFPDB_EINVAL && st.detail >= 100 && st.detail < 110)
       fail(GFPDB_EINVAL, "batched star query: dimension " + std::to_string(st.detail - 100) + " repeats a key");
     raise_device_status(st, "batched star query");
@@ -1067,7 +1070,7 @@ struct gfpdb_batch {
   TupleSetPtr result;       // the batch's device result view
   char* pinned = nullptr;   // status, row count and result columns, packed by the run
   int64_t pinned_bytes = 0;
-  int64_t status_off = 0, count_off = 0;
+  int64_t status_off = 0, count_off = 0, gathered_off = 0;
   std::vector<int64_t> col_off;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   bool in_flight = false;
@@ -1120,6 +1123,7 @@ int32_t gfpdb_batch_prepare(const char* spec_json, int32_t n_tables, const char*
       return o;
     };
     b->status_off = add(b->be->batch.status(), sizeof(DevStatus));
+    b->gathered_off = add(b->be->batch.gathered(), 2 * sizeof(unsigned long long));
     b->count_off = add(r.rows_dev(), sizeof(int64_t));
     for (int i = 0; i < r.num_columns(); ++i) {
       const auto& c = r.column(i);
@@ -1205,14 +1209,17 @@ int32_t gfpdb_batch_wait(gfpdb_batch* b, gfpdb_exec_stats* stats, int64_t* n_row
     const int64_t n = *reinterpret_cast<const int64_t*>(b->pinned + b->count_off);
     if (n < 0 || n > b->result->num_rows()) fail(GFPDB_EDEVICE, "batched star query produced an out-of-range row count");
     *n_rows = n;
-    copy_counters().h2d += b->be->batch.host_bytes();
+    // bytes from host memory: the copies, and the reads in place
+    const unsigned long long* g = reinterpret_cast<const unsigned long long*>(b->pinned + b->gathered_off);
+    const int64_t h2d = b->be->batch.host_bytes() + b->be->batch.in_place_bytes(g[0], g[1]);
+    copy_counters().h2d += h2d;
     copy_counters().d2h += b->pinned_bytes;
     if (stats != nullptr) {
       float ms = 0;
       GF_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
       stats->device_ns = static_cast<int64_t>(static_cast<double>(ms) * 1e6);
       stats->kernel_launches = b->launches;
-      stats->h2d_bytes = b->be->batch.host_bytes();
+      stats->h2d_bytes = h2d;
       stats->d2h_bytes = b->pinned_bytes;
       stats->num_ops = 3;
       stats->messages = 0;

@@ -108,6 +108,9 @@ ColumnPtr make_utf8_column(int64_t length, BufferPtr offsets, BufferPtr bytes);
 // arrays are borrowed (the caller keeps them alive for the duration of the
 // call) unless copy_device is set; host arrays are copied to the device on
 // stream `s`.
+// Device address of page-locked host memory (nullptr for pageable memory).
+const void* device_view_of_host(const void* p);
+
 TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* array, cudaStream_t s,
                             bool copy_device = false);
 std::vector<Field> import_schema(const ArrowSchema* schema);

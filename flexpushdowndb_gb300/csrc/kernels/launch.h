@@ -240,6 +240,11 @@ class StarBatch {
   // (set before prepare()); host_bytes() is what one run copies.
   void set_host_columns(std::vector<StarBatchHostColumn> cols);
   int64_t host_bytes() const;
+  // Two device counters of the last run: rows that reached the lookups in
+  // global memory, and rows that reached the group updates; and the bytes
+  // such rows read in place from host memory (columns not copied).
+  const unsigned long long* gathered() const;
+  int64_t in_place_bytes(uint64_t ring_rows, uint64_t survivor_rows) const;
 
  private:
   std::unique_ptr<StarBatchState> st_;

@@ -223,6 +223,7 @@ struct SBFactParams {
   int64_t n_tiles;
   int64_t tile_begin, tile_end;  // tiles of this launch
   const SBSegments* segs;        // [dimension]
+  unsigned long long* gathered;  // rows that reached step (2), and step (3)
   uint64_t* gkeys;               // [gcap] group keys, shared by every query (all-ones = empty)
   unsigned long long* touched;   // [gcap + 1] queries with rows in each group; slot gcap: the all-ones key
   unsigned long long* gaccs;     // [q][gcap + 1][n_aggs]
@@ -816,6 +817,10 @@ __global__ void __launch_bounds__(kSBFactThreads, 3) sb_fact_kernel(const __grid
     h2 += n;
     __syncwarp();
   }
+  if (lane == 0) {
+    atomicAdd(p.gathered, static_cast<unsigned long long>(t1));
+    atomicAdd(p.gathered + 1, static_cast<unsigned long long>(t2));
+  }
 }
 
 // Stage 2, direct form: for int32 foreign and dimension keys in 16-byte
@@ -1064,6 +1069,10 @@ __global__ void __launch_bounds__(kSBDirectThreads, 2) sb_fact_direct_kernel(con
     h2 += n;
     __syncwarp();
   }
+  if (lane == 0) {
+    atomicAdd(p.gathered, static_cast<unsigned long long>(t1));
+    atomicAdd(p.gathered + 1, static_cast<unsigned long long>(t2));
+  }
 }
 
 struct SBFinalParams {
@@ -1217,6 +1226,9 @@ struct StarBatchState {
   };
   std::vector<TileGroup> group_tiles;
   int64_t host_bytes = 0;
+  std::vector<char> in_place;       // per fact column: read in place from page-locked host memory
+  int n_in_place_fk = 0, n_in_place_measures = 0;
+  unsigned long long* gathered = nullptr;
   cudaStream_t copy_stream = nullptr;
   std::vector<cudaEvent_t> events;  // start, dimensions, then one per group
 
@@ -1247,6 +1259,12 @@ void StarBatch::set_ranges(const std::vector<std::vector<std::pair<int64_t, int6
 const unsigned long long* StarBatch::query_offsets() const { return st_->qoff; }
 void StarBatch::set_host_columns(std::vector<StarBatchHostColumn> cols) { st_->host_cols = std::move(cols); }
 int64_t StarBatch::host_bytes() const { return st_->host_bytes; }
+const unsigned long long* StarBatch::gathered() const { return st_->gathered; }
+int64_t StarBatch::in_place_bytes(uint64_t ring_rows, uint64_t survivor_rows) const {
+  // one 32-byte sector per row and column read in place (an upper bound:
+  // rows that share a sector are counted once each)
+  return static_cast<int64_t>(32 * (ring_rows * st_->n_in_place_fk + survivor_rows * st_->n_in_place_measures));
+}
 
 StarBatchState::~StarBatchState() {
   for (cudaEvent_t e : events) (void)cudaEventDestroy(e);
@@ -1301,8 +1319,9 @@ void StarBatchState::plan_host_copies() {
     const int64_t target = fact_rows * (g + 1) / groups;
     while (pi < parts.size() && (rows_done < target || g == groups - 1)) {
       const TupleSet& t = *parts[pi];
-      for (const std::string& c : fact_cols) {
-        const auto& col = t.column(c);
+      for (size_t c = 0; c < fact_cols.size(); ++c) {
+        if (!in_place.empty() && in_place[c]) continue;
+        const auto& col = t.column(fact_cols[c]);
         add(cs, col->data, t.num_rows() * dtype_width(col->type));
       }
       rows_done += t.num_rows();
@@ -1527,7 +1546,7 @@ void StarBatchState::prepare(cudaStream_t s) {
   touched_buf = make_buffer(static_cast<int64_t>(gcap + 1) * 8, s);
   gaccs_buf = make_buffer(gslots * 8 * na, s);
   // status block, output count, then per-query counts, cursors and offsets
-  misc_buf = make_buffer(sizeof(DevStatus) + 64 + 8 * (3 * kSBMaxQueries + 1), s);
+  misc_buf = make_buffer(sizeof(DevStatus) + 64 + 8 * (3 * kSBMaxQueries + 1) + 16, s);
   meta_buf = make_buffer(static_cast<int64_t>(hcols.size() * sizeof(DevCol) + hbase.size() * 8 + hrows.size() * 8 +
                                               kSBMaxDims * sizeof(SBSegments)),
                          s);
@@ -1562,6 +1581,40 @@ void StarBatchState::prepare(cudaStream_t s) {
   int64_t* drows = dbase + hbase.size();
   SBSegments* dsegs = reinterpret_cast<SBSegments*>(drows + hrows.size());
   dims_params.segs = dsegs;
+  // Host-resident fact columns that the direct fact pass reads only for
+  // some rows (the foreign keys of dimensions it does not stage, and the
+  // measures) are read in place from page-locked host memory; the columns
+  // it reads in full are copied by every run (plan_host_copies).
+  in_place.assign(nc, 0);
+  n_in_place_fk = n_in_place_measures = 0;
+  if (direct && !host_cols.empty()) {
+    for (int c = 0; c < nc; ++c) {
+      bool fk = false, staged_fk = false;
+      for (int d = 0; d < nd; ++d)
+        if (fk_slot[d] == c) {
+          fk = true;
+          staged_fk |= dims_params.dims[d].smem_off >= 0;
+        }
+      if (staged_fk) continue;
+      std::vector<const void*> views(parts.size(), nullptr);
+      bool ok = true;
+      for (size_t pi = 0; pi < parts.size() && ok; ++pi) {
+        const auto& col = parts[pi]->column(fact_cols[c]);
+        const StarBatchHostColumn* h = nullptr;
+        for (const auto& hc : host_cols)
+          if (hc.dst == col->data) h = &hc;
+        views[pi] = h != nullptr ? device_view_of_host(h->src) : nullptr;
+        ok = views[pi] != nullptr;
+      }
+      if (!ok) continue;
+      for (size_t pi = 0; pi < parts.size(); ++pi) hcols[pi * nc + c].data = views[pi];
+      in_place[c] = 1;
+      if (fk)
+        ++n_in_place_fk;
+      else
+        ++n_in_place_measures;
+    }
+  }
   // Metadata goes up once, from host memory that this object keeps (so a
   // captured graph never needs it again).
   host_meta.assign(meta_buf->size(), 0);
@@ -1594,6 +1647,8 @@ void StarBatchState::prepare(cudaStream_t s) {
   qcount = reinterpret_cast<unsigned long long*>(misc + sizeof(DevStatus) + 64);
   qcursor = qcount + kSBMaxQueries;
   qoff = qcursor + kSBMaxQueries;
+  gathered = qoff + kSBMaxQueries + 1;
+  fact_params.gathered = gathered;
   fact_params.tile_begin = 0;
   fact_params.tile_end = n_tiles;
   plan_host_copies();
