@@ -569,7 +569,8 @@ def run_case(args):
         tabs = workloads.batch_tables(args.parts)
         parts = [f"p{i}" for i in range(args.parts)]
         dev = plan.PreparedInputs({k: DeviceTable.from_host(v) for k, v in tabs.items()})
-        spec = workloads.star_batch_spec(parts, workloads.batch_queries(32))
+        spec = dict(workloads.star_batch_spec(parts, workloads.batch_queries(32), items_per_thread=args.items,
+                                              blocks_per_sm=args.bps), stages=args.stages)
         fn = lambda: batch.star_batch(spec, dev, use_graph=False).table  # noqa: E731
         args.rows = sum(tabs[p].num_rows for p in parts)
         return _time_case(args, fn)
@@ -765,6 +766,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | plan-timeline | batch | join | group | csv")
     ap.add_argument("--parts", type=int, default=64, help="fact partitions of the batch case")
+    ap.add_argument("--items", type=int, default=2, help="itemsPerThread of the batch case")
+    ap.add_argument("--bps", type=int, default=2, help="blocksPerSm of the batch case")
+    ap.add_argument("--stages", type=int, default=3, help="stages of the batch case")
     ap.add_argument("--rows", type=int, default=STAR_FACT_ROWS)
     ap.add_argument("--streams", type=int, default=4, help="plan streams for --case plan-timeline")
     ap.add_argument("--no-star-plan", action="store_true", help="skip the single star query section")

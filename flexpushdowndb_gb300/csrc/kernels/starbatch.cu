@@ -1732,9 +1732,10 @@ static void fact_pass(StarBatchState& b, int64_t begin, int64_t end, int64_t row
   if (grid > end - begin) grid = end - begin;
   b.fact_params.tile_begin = begin;
   b.fact_params.tile_end = end;
-  ProfScope prof("sb_fact_kernel", s);
+  const char* name = b.direct ? "sb_fact_direct_kernel" : "sb_fact_kernel";
+  ProfScope prof(name, s);
   b.launch_fact(static_cast<int>(grid), s);
-  after_launch("sb_fact_kernel");
+  after_launch(name);
   // algorithmic bytes: every foreign key of every fact row of these tiles
   // read once (the measures of the few surviving rows are not counted)
   double fk_bytes = 0;
