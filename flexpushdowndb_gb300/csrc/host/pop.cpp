@@ -637,6 +637,105 @@ class GroupPOp : public PhysicalOp {
   std::shared_ptr<GroupTable> table_;
 };
 
+// ProjectPOp (fpdb-executor/src/physical/project/ProjectPOp.cpp:48-149):
+// each TupleSet leaves as its pass-through columns under their new names,
+// then one column per expression (evaluated by project_kernel, compiled
+// against the first TupleSet's schema, as the reference builds its projector
+// on the first message). The reference buffers rows up to DefaultBufferSize
+// before projecting; a projection is row-wise, so each TupleSet is projected
+// as it arrives, with the same rows out.
+class ProjectPOp : public PhysicalOp {
+ public:
+  ProjectPOp(std::string name, std::vector<ExprPtr> exprs, std::vector<std::string> expr_names,
+             std::vector<std::pair<std::string, std::string>> pairs)
+      : PhysicalOp(std::move(name), "ProjectPOp"), exprs_(std::move(exprs)), expr_names_(std::move(expr_names)),
+        pairs_(std::move(pairs)) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      const TupleSet& in = *m.tuples;
+      if (!compiled_ && !exprs_.empty()) {
+        for (size_t i = 0; i < exprs_.size(); ++i) {
+          DType t = DType::Int64;
+          spec_.ops.push_back(compile_value(exprs_[i], in.fields(), spec_.prog, spec_.slots, &t));
+          spec_.types.push_back(t);
+          spec_.names.push_back(expr_names_[i]);
+        }
+        compiled_ = true;
+      }
+      std::vector<Field> fields;
+      std::vector<ColumnPtr> cols;
+      for (const auto& pr : pairs_) {
+        const int ci = in.require_column(pr.first);
+        fields.push_back(Field{pr.second, in.field(ci).type});
+        cols.push_back(in.column(ci));
+      }
+      if (!exprs_.empty()) {
+        TupleSetPtr e = project_columns(spec_, in, ctx()->stream());
+        for (int i = 0; i < e->num_columns(); ++i) {
+          fields.push_back(e->field(i));
+          cols.push_back(e->column(i));
+        }
+      }
+      Message out;
+      out.type = MessageType::TUPLESET;
+      out.tuples = in.exact() ? TupleSet::make(std::move(fields), std::move(cols), in.num_rows())
+                              : TupleSet::make_deferred(std::move(fields), std::move(cols), in.num_rows(),
+                                                        in.rows_owner(), in.rows_dev());
+      ctx()->tell(out);
+    } else if (m.type == MessageType::COMPLETE) {
+      if (is_producer_complete(*this)) ctx()->notifyComplete();
+    }
+  }
+
+ private:
+  std::vector<ExprPtr> exprs_;
+  std::vector<std::string> expr_names_;
+  std::vector<std::pair<std::string, std::string>> pairs_;
+  ProjectSpec spec_;
+  bool compiled_ = false;
+};
+
+// LimitSortPOp (fpdb-executor/src/physical/limitsort/LimitSortPOp.cpp:44-142):
+// the k first rows in sort-key order of everything it receives, projected to
+// projectColumnNames, sent once all producers are complete. The reference
+// re-selects k after every TupleSet; the k first rows of all of them are the
+// same rows, selected here once (select_k_kernel) when the input is complete.
+class LimitSortPOp : public PhysicalOp {
+ public:
+  LimitSortPOp(std::string name, int64_t k, std::vector<SortKeySpec> keys)
+      : PhysicalOp(std::move(name), "LimitSortPOp"), k_(k), keys_(std::move(keys)) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      received_.push_back(m.tuples);
+    } else if (m.type == MessageType::COMPLETE) {
+      if (!is_producer_complete(*this)) return;
+      if (received_.empty()) {
+        ctx()->notifyError("Result not produced yet");  // as the reference: no input, no result
+        return;
+      }
+      TupleSetPtr all = received_.size() == 1 ? received_[0] : TupleSet::concatenate(received_, ctx()->stream());
+      TupleSetPtr r = select_k(all, keys_, k_, ctx()->stream());
+      if (!projectColumnNames_.empty()) r = r->project_exist(projectColumnNames_);
+      Message out;
+      out.type = MessageType::TUPLESET;
+      out.tuples = r;
+      ctx()->tell(out);
+      ctx()->notifyComplete();
+    }
+  }
+
+  void clear() override { received_.clear(); }
+
+ private:
+  int64_t k_;
+  std::vector<SortKeySpec> keys_;
+  std::vector<TupleSetPtr> received_;
+};
+
 // Parses delimited text into a TupleSet: the CSV branch of the reference's
 // file scans (FileScanAbstractPOp::readAndSendTuples reading through
 // CSVReader::read, fpdb-tuple/src/csv/CSVReader.cpp:15-21), reading the text
@@ -1077,6 +1176,37 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
     } else {
       op = std::make_unique<GroupPOp>(name, o.str_list("groupColumnNames"), aggs, o.get_int("groupsHint", 0));
     }
+  } else if (type == "ProjectPOp") {
+    std::vector<ExprPtr> exprs;
+    std::vector<std::string> expr_names;
+    if (o.contains("exprs"))
+      for (auto& e : o.at("exprs").array()) {
+        exprs.push_back(parse_expr(e.at("expr")));
+        expr_names.push_back(e.at("name").str());
+      }
+    std::vector<std::pair<std::string, std::string>> pairs;
+    if (o.contains("projectColumnNamePairs"))
+      for (auto& pr : o.at("projectColumnNamePairs").array()) {
+        if (pr.kind != json::Value::Array || pr.a.size() != 2)
+          fail(GFPDB_EINVAL, "ProjectPOp '" + name + "': projectColumnNamePairs holds [input, output] pairs");
+        pairs.emplace_back(pr.a[0].str(), pr.a[1].str());
+      }
+    if (exprs.size() > static_cast<size_t>(kMaxProjOut))
+      fail(GFPDB_EUNSUPPORTED, "ProjectPOp '" + name + "': more than 16 expressions");
+    op = std::make_unique<ProjectPOp>(name, std::move(exprs), std::move(expr_names), std::move(pairs));
+  } else if (type == "LimitSortPOp") {
+    std::vector<SortKeySpec> keys;
+    for (auto& k : o.at("sortKeys").array()) {
+      const std::string order = k.get_str("order", "ASC");
+      if (order != "ASC" && order != "DESC")
+        fail(GFPDB_EINVAL, "LimitSortPOp '" + name + "': sort order is ASC or DESC");
+      keys.push_back(SortKeySpec{k.at("name").str(), order == "DESC"});
+    }
+    const int64_t k = o.get_int("k", -1);
+    if (keys.empty() || keys.size() > static_cast<size_t>(kMaxSortKeys))
+      fail(GFPDB_EUNSUPPORTED, "LimitSortPOp '" + name + "': 1 to 4 sort keys");
+    if (k < 0 || k > 1024) fail(GFPDB_EUNSUPPORTED, "LimitSortPOp '" + name + "': k must be in [0, 1024]");
+    op = std::make_unique<LimitSortPOp>(name, k, std::move(keys));
   } else if (type == "CollatePOp") {
     op = std::make_unique<CollatePOp>(name);
   } else {

@@ -250,6 +250,30 @@ class StarBatch {
   std::unique_ptr<StarBatchState> st_;
 };
 
+// ------------------------------------------------------------ project.cu
+
+constexpr int kMaxProjOut = 16;
+constexpr int kMaxSortKeys = 4;
+
+// Value expressions compiled against one input schema (ProjectPOp).
+struct ProjectSpec {
+  Program prog{};
+  ColumnSlots slots;
+  std::vector<Operand> ops;
+  std::vector<DType> types;
+  std::vector<std::string> names;
+};
+// One new column per expression, rows as the input's (deferred sizes kept).
+TupleSetPtr project_columns(const ProjectSpec& spec, const TupleSet& in, cudaStream_t s);
+
+struct SortKeySpec {
+  std::string column;
+  bool descending;
+};
+// The first k rows of the input in key order (ties by input row), at most
+// 1,024; synchronizes when the input's size is deferred.
+TupleSetPtr select_k(const TupleSetPtr& in, const std::vector<SortKeySpec>& keys, int64_t k, cudaStream_t s);
+
 // --------------------------------------------------------------- csv.cu
 
 struct CsvField {

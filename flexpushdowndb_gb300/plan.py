@@ -103,6 +103,26 @@ class Plan:
             op["columns"] = list(columns)
         return self._add(op)
 
+    def project(self, name: str, producer: str, exprs: Sequence[tuple[str, Expr]] = (),
+                pairs: Sequence[tuple[str, str]] = ()) -> str:
+        """ProjectPOp: pass-through columns renamed (input, output), then one
+        column per (name, expression)."""
+        self._add({"type": "ProjectPOp", "name": name, "exprs": [{"name": n, "expr": e} for n, e in exprs],
+                   "projectColumnNamePairs": [[a, b] for a, b in pairs]})
+        self.connect(producer, name)
+        return name
+
+    def limit_sort(self, name: str, producer: str, k: int, sort_keys: Sequence[tuple[str, str]],
+                   project: Sequence[str] | None = None) -> str:
+        """LimitSortPOp: the first k rows by (column, "ASC" | "DESC") keys."""
+        op = {"type": "LimitSortPOp", "name": name, "k": k,
+              "sortKeys": [{"name": c, "order": o} for c, o in sort_keys]}
+        if project is not None:
+            op["projectColumnNames"] = list(project)
+        self._add(op)
+        self.connect(producer, name)
+        return name
+
     def collate(self, name: str, producer: str) -> str:
         self._add({"type": "CollatePOp", "name": name})
         self.connect(producer, name)

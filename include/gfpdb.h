@@ -307,9 +307,10 @@ typedef struct gfpdb_exec_stats {
                                 copy (CUDA events); 0 for other runs */
 } gfpdb_exec_stats;
 
-/* Run a physical plan of the reference's operators (TableScanPOp, FilterPOp,
- * BloomFilterCreatePOp, BloomFilterUsePOp, HashJoinArrowPOp, GroupPOp,
- * ProjectPOp, CollatePOp) on one GPU, delivering START / TUPLESET /
+/* Run a physical plan of the reference's operators (TableScanPOp, CsvScanPOp,
+ * FilterPOp, BloomFilterCreatePOp, BloomFilterUsePOp, HashJoinArrowPOp,
+ * GroupPOp, AggregatePOp, ProjectPOp, LimitSortPOp, CollatePOp) on one GPU,
+ * delivering START / TUPLESET /
  * BLOOM_FILTER / COMPLETE messages between them in the reference's protocol,
  * and return the CollatePOp's TupleSet. Input tables are named; host tables
  * are copied to the device by their scan operator. With result_to_host != 0

@@ -20,6 +20,14 @@ Each function follows the reference operator it names:
                   Sum.cpp:63-74, Count.cpp:91-104).
   csv_parse     - CSVToArrowSIMDChunkParser.cpp:183-374 field rules, with
                   decimals as exact scaled int64 and dates as date32.
+  project       - ProjectPOp::projectAndSendTuples
+                  (fpdb-executor/src/physical/project/ProjectPOp.cpp:98-145):
+                  the renamed pass-through columns, then one column per
+                  expression.
+  limit_sort    - LimitSortPOp::selectK
+                  (fpdb-executor/src/physical/limitsort/LimitSortPOp.cpp:97-135,
+                  arrow::compute::SelectKUnstable + Take): the first k rows in
+                  key order; ties kept in input order.
 """
 
 from __future__ import annotations
@@ -257,3 +265,37 @@ def csv_parse(text: bytes, fields: list[tuple[str, str]], columns=None, delimite
         else:
             out.append(Column(name, ty, [int(x) for x in raw]))
     return Table(out)
+
+
+# ----------------------------------------------------------- project / sort
+
+
+def project(table: Table, exprs=(), pairs=()) -> Table:
+    cols = []
+    for a, b in pairs:
+        c = table.column(a)
+        cols.append(Column(b, c.type, c.values))
+    for name, e in exprs:
+        v, ty = _expr.value(e, table)
+        cols.append(Column(name, ty, v))
+    return Table(cols)
+
+
+def limit_sort(table: Table, k: int, sort_keys) -> Table:
+    """sort_keys: (column, "ASC" | "DESC") pairs."""
+    import functools
+
+    cols = {n: table[n] for n, _ in sort_keys}
+
+    def cmp(a, b):
+        for n, order in sort_keys:
+            x, y = cols[n][a], cols[n][b]
+            if isinstance(x, str):
+                x, y = x.encode(), y.encode()
+            r = int(x > y) - int(x < y)
+            if r:
+                return -r if order == "DESC" else r
+        return (a > b) - (a < b)
+
+    idx = sorted(range(table.num_rows), key=functools.cmp_to_key(cmp))[:k]
+    return take(table, np.array(idx, dtype=np.int64))

@@ -156,3 +156,29 @@ def test_prepared_launch_and_wait_argument_errors():
     assert L.gfpdb_prepared_wait(None, None, ctypes.byref(n), ctypes.byref(gen)) == _abi.GFPDB_EINVAL
     assert L.gfpdb_prepared_run(None, None, None, ctypes.byref(n), ctypes.byref(gen)) == _abi.GFPDB_EINVAL
     assert b"null" in L.gfpdb_last_error()
+
+
+def test_plan_validation_project_and_limit_sort():
+    from flexpushdowndb_gb300.expression import col, divide
+
+    p = plan.Plan()
+    p.scan("scan", "t")
+    p.project("proj", "scan", [("x", divide(col("a"), col("b")))], [("a", "a2")])
+    p.limit_sort("top", "proj", 10, [("x", "DESC"), ("a2", "ASC")])
+    p.collate("collate", "top")
+    plan.validate(p)
+    for k, order in ((1025, "ASC"), (-1, "ASC"), (10, "SIDEWAYS")):
+        q = plan.Plan()
+        q.scan("scan", "t")
+        q.limit_sort("top", "scan", k, [("a", order)])
+        q.collate("collate", "top")
+        with pytest.raises(Exception):
+            plan.validate(q)
+
+
+def test_oracle_limit_sort_is_stable():
+    from oracle import ops as oops
+
+    t = Table([Column("a", "int32", [3, 1, 3, 2, 1]), Column("i", "int32", [0, 1, 2, 3, 4])])
+    assert oops.limit_sort(t, 3, [("a", "DESC")]).rows() == [(3, 0), (3, 2), (2, 3)]
+    assert oops.limit_sort(t, 2, [("a", "ASC")]).rows() == [(1, 1), (1, 4)]
