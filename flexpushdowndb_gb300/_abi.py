@@ -143,15 +143,15 @@ SIGNATURES = {
     "gfpdb_filter_evaluate": (_I32, [_P, _S, _A, _CP, _I32, _S, _A, _P]),
     "gfpdb_filter_free": (None, [_P]),
     "gfpdb_filter_evaluate_noalloc": (_I32, [_P, _S, _A, _CP, _I32, ctypes.POINTER(_P), ctypes.POINTER(_I64), _P]),
-    "gfpdb_bloom_create": (_I32, [_S, ctypes.POINTER(_A), _I32, ctypes.c_char_p, _I32, _I32, ctypes.POINTER(_P), _P]),
-    "gfpdb_bloom_use": (_I32, [_P, _S, _A, ctypes.c_char_p, _S, _A, _P]),
+    "gfpdb_bloom_create": (_I32, [_S, ctypes.POINTER(_A), _I32, _CP, _I32, _I32, _I32, ctypes.POINTER(_P), _P]),
+    "gfpdb_bloom_use": (_I32, [_P, _S, _A, _CP, _I32, _S, _A, _P]),
     "gfpdb_bloom_info": (
         _I32,
         [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_P)],
     ),
     "gfpdb_bloom_free": (None, [_P]),
     "gfpdb_select": (_I32, [_P, _I32, ctypes.POINTER(_P), _CP, _S, _A, _CP, _I32, _S, _A, _P]),
-    "gfpdb_hashjoin_create": (_I32, [_I32, ctypes.c_char_p, ctypes.c_char_p, _CP, _I32, ctypes.c_double, ctypes.POINTER(_P)]),
+    "gfpdb_hashjoin_create": (_I32, [_I32, _CP, _CP, _I32, _CP, _I32, ctypes.c_double, ctypes.POINTER(_P)]),
     "gfpdb_hashjoin_put_build": (_I32, [_P, _S, _A, _P]),
     "gfpdb_hashjoin_finalize_build": (_I32, [_P, _P]),
     "gfpdb_hashjoin_probe": (_I32, [_P, _S, _A, _S, _A, _P]),
@@ -160,6 +160,8 @@ SIGNATURES = {
     "gfpdb_group_create": (_I32, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "gfpdb_group_update": (_I32, [_P, _S, _A, _P]),
     "gfpdb_group_finalize": (_I32, [_P, _S, _A, _P]),
+    "gfpdb_group_clear": (_I32, [_P]),
+    "gfpdb_hashjoin_clear": (_I32, [_P]),
     "gfpdb_group_free": (None, [_P]),
     "gfpdb_csv_read": (_I32, [_P, _I64, _I32, ctypes.c_char, _I32, _S, _CP, _I32, _S, _A, _P]),
     "gfpdb_execute_plan": (

@@ -590,19 +590,25 @@ void gfpdb_filter_free(gfpdb_filter* filter) { delete filter; }
 // ------------------------------------------------------------------- bloom
 
 int32_t gfpdb_bloom_create(const ArrowSchema* schema, const ArrowDeviceArray* const* batches, int32_t n_batches,
-                           const char* key_column, int32_t bits_per_key, int32_t num_hashes, gfpdb_bloom** out,
-                           void* stream) {
+                           const char* const* key_columns, int32_t n_keys, int32_t bits_per_key, int32_t num_hashes,
+                           gfpdb_bloom** out, void* stream) {
   return guarded([&] {
-    require(out != nullptr && key_column != nullptr && n_batches >= 0, "bad bloom_create arguments");
+    require(out != nullptr && key_columns != nullptr && n_batches >= 0, "bad bloom_create arguments");
+    if (n_keys < 1 || n_keys > kMaxKeyColumns) fail(GFPDB_EINVAL, "a bloom filter key has 1 to 8 columns");
     ensure_device();
     cudaStream_t s = as_stream(stream);
+    const std::vector<std::string> keys = names_of(key_columns, n_keys);
     std::vector<TupleSetPtr> keep;
     std::vector<const Column*> parts;
     for (int32_t i = 0; i < n_batches; ++i) {
-      keep.push_back(import_tupleset(schema, batches[i], s));
-      parts.push_back(keep.back()->column(key_column).get());
+      TupleSetPtr t = import_tupleset(schema, batches[i], s);
+      // several key columns: the filter holds their composite
+      if (n_keys > 1) t = with_composite_key(t, keys, kBuildKeyColumn, "", s);
+      keep.push_back(t);
+      parts.push_back(t->column(n_keys > 1 ? std::string(kBuildKeyColumn) : keys[0]).get());
     }
     auto b = std::make_unique<gfpdb_bloom>();
+    b->key_columns = n_keys;
     b->bloom = bloom_build(parts, bits_per_key, num_hashes, s);
     sync(s);  // borrowed inputs may be released after return
     *out = b.release();
@@ -610,10 +616,27 @@ int32_t gfpdb_bloom_create(const ArrowSchema* schema, const ArrowDeviceArray* co
 }
 
 int32_t gfpdb_bloom_use(const gfpdb_bloom* bloom, const ArrowSchema* in_schema, const ArrowDeviceArray* in,
-                        const char* key_column, ArrowSchema* out_schema, ArrowDeviceArray* out, void* stream) {
-  const gfpdb_bloom* blooms[1] = {bloom};
-  const char* cols[1] = {key_column};
-  return gfpdb_select(nullptr, 1, blooms, cols, in_schema, in, nullptr, -1, out_schema, out, stream);
+                        const char* const* key_columns, int32_t n_keys, ArrowSchema* out_schema,
+                        ArrowDeviceArray* out, void* stream) {
+  if (bloom != nullptr && key_columns != nullptr && n_keys == 1 && bloom->key_columns == 1) {
+    const gfpdb_bloom* blooms[1] = {bloom};
+    return gfpdb_select(nullptr, 1, blooms, key_columns, in_schema, in, nullptr, -1, out_schema, out, stream);
+  }
+  return guarded([&] {
+    require(bloom != nullptr && key_columns != nullptr && out_schema != nullptr && out != nullptr, "null argument");
+    if (n_keys != bloom->key_columns)
+      fail(GFPDB_EINVAL, "the filter was built over " + std::to_string(bloom->key_columns) + " key columns, not " +
+                             std::to_string(n_keys));
+    ensure_device();
+    cudaStream_t s = as_stream(stream);
+    TupleSetPtr ts = import_tupleset(in_schema, in, s);
+    std::vector<std::string> all;
+    for (int i = 0; i < ts->num_columns(); ++i) all.push_back(ts->field(i).name);
+    TupleSetPtr keyed = with_composite_key(ts, names_of(key_columns, n_keys), kProbeKeyColumn, "", s);
+    TupleSetPtr r = select_rows(*keyed, nullptr, {BloomProbe{bloom->bloom, kProbeKeyColumn}}, all, false, s);
+    export_tupleset(resolved(r, s), out_schema, out, false, s);
+    sync(s);
+  });
 }
 
 int32_t gfpdb_bloom_info(const gfpdb_bloom* bloom, int64_t* num_blocks, int64_t* num_keys, int32_t* valid,
@@ -657,16 +680,17 @@ int32_t gfpdb_select(const gfpdb_filter* filter, int32_t n_blooms, const gfpdb_b
 
 // --------------------------------------------------------------- hash join
 
-int32_t gfpdb_hashjoin_create(int32_t join_type, const char* build_key, const char* probe_key,
-                              const char* const* needed_columns, int32_t n_needed, double load_factor,
-                              gfpdb_hashjoin** out) {
+int32_t gfpdb_hashjoin_create(int32_t join_type, const char* const* build_keys, const char* const* probe_keys,
+                              int32_t n_keys, const char* const* needed_columns, int32_t n_needed,
+                              double load_factor, gfpdb_hashjoin** out) {
   return guarded([&] {
-    require(out != nullptr && build_key != nullptr && probe_key != nullptr, "null argument");
+    require(out != nullptr && build_keys != nullptr && probe_keys != nullptr, "null argument");
+    if (n_keys < 1 || n_keys > kMaxKeyColumns) fail(GFPDB_EINVAL, "a join key has 1 to 8 columns");
     if (join_type != GFPDB_JOIN_INNER) fail(GFPDB_EUNSUPPORTED, "only inner joins run on the GPU path");
     auto j = std::make_unique<gfpdb_hashjoin>();
     j->join_type = join_type;
-    j->build_key = build_key;
-    j->probe_key = probe_key;
+    j->build_keys = names_of(build_keys, n_keys);
+    j->probe_keys = names_of(probe_keys, n_keys);
     j->all_columns = needed_columns == nullptr || n_needed < 0;
     if (!j->all_columns) j->needed = names_of(needed_columns, n_needed);
     j->load_factor = load_factor > 0 ? load_factor : 0.5;
@@ -691,9 +715,7 @@ int32_t gfpdb_hashjoin_finalize_build(gfpdb_hashjoin* join, void* stream) {
     if (join->built) return;
     if (join->build.empty()) fail(GFPDB_EINVAL, "no build-side input");
     cudaStream_t s = as_stream(stream);
-    join->table.build = TupleSet::concatenate(join->build, s);
-    join->table.key_col = join->table.build->require_column(join->build_key);
-    join_build_table(join->table, join->load_factor, s);
+    join->table = pop::build_join_table(TupleSet::concatenate(join->build, s), join->build_keys, join->load_factor, s);
     join->build.clear();
     join->built = true;
   });
@@ -706,42 +728,19 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const ArrowSchema* schema, co
     if (!join->built) fail(GFPDB_EINVAL, "probe before finalize_build");
     cudaStream_t s = as_stream(stream);
     auto ts = import_tupleset(schema, batch, s);
-    const int pk = ts->require_column(join->probe_key);
-    auto needed = [&](const std::string& c) {
-      return join->all_columns || std::find(join->needed.begin(), join->needed.end(), c) != join->needed.end();
-    };
-    std::vector<Field> fields;
-    std::vector<int> pcols, bcols;
-    bool fixed = true;
-    for (int i = 0; i < ts->num_columns(); ++i)
-      if (needed(ts->field(i).name)) {
-        fields.push_back(ts->field(i));
-        pcols.push_back(i);
-        fixed &= ts->field(i).type != DType::Utf8;
-      }
-    const TupleSet& b = *join->table.build;
-    for (int i = 0; i < b.num_columns(); ++i)
-      if (needed(b.field(i).name)) {
-        for (auto& f : fields)
-          if (f.name == b.field(i).name) fail(GFPDB_EINVAL, "column '" + f.name + "' is on both join sides");
-        fields.push_back(b.field(i));
-        bcols.push_back(i);
-        fixed &= b.field(i).type != DType::Utf8;
-      }
-    int64_t n = 0;
-    std::vector<ColumnPtr> cols;
-    if (fixed) {
-      // fixed-width outputs: probe and materialise in one kernel
-      cols = join_probe_materialize(join->table, *ts, pk, pcols, bcols, &n, s, nullptr, nullptr);
+    // output: the probe side's needed columns, then the build side's
+    // (HashJoinArrowKernel.cpp:148-162); every column when none are named
+    std::vector<std::string> proj;
+    if (join->all_columns) {
+      for (int i = 0; i < ts->num_columns(); ++i) proj.push_back(ts->field(i).name);
+      const TupleSet& b = *join->table.build;
+      for (int i = 0; i < b.num_columns(); ++i)
+        if (!is_internal_key_column(b.field(i).name)) proj.push_back(b.field(i).name);
     } else {
-      BufferPtr pidx, bidx;
-      join_probe_pairs(join->table, *ts, pk, &pidx, &bidx, &n, s);
-      std::vector<GatherSpec> specs;
-      for (int i : pcols) specs.push_back(GatherSpec{ts->column(i).get(), pidx->as<int32_t>()});
-      for (int i : bcols) specs.push_back(GatherSpec{b.column(i).get(), bidx->as<int32_t>()});
-      cols = gather_columns(specs, n, s);
+      proj = join->needed;
     }
-    export_tupleset(TupleSet::make(std::move(fields), std::move(cols), n), out_schema, out, false, s);
+    TupleSetPtr r = resolved(pop::join_probe_keys("hash join", join->table, proj, join->probe_keys, ts, s), s);
+    export_tupleset(r, out_schema, out, false, s);
     sync(s);
   });
 }
@@ -759,6 +758,15 @@ int32_t gfpdb_hashjoin_info(const gfpdb_hashjoin* join, int64_t* build_rows, int
         *max_probe = st.aux[0];
       }
     }
+  });
+}
+
+int32_t gfpdb_hashjoin_clear(gfpdb_hashjoin* join) {
+  return guarded([&] {
+    require(join != nullptr, "null argument");
+    join->build.clear();
+    join->table = JoinTable{};
+    join->built = false;
   });
 }
 
@@ -792,7 +800,10 @@ int32_t gfpdb_group_create(const char* group_spec_json, gfpdb_group** out) {
       aggs.push_back(g);
     }
     auto g = std::make_unique<gfpdb_group>();
-    g->table = group_table_create(spec.str_list("groupColumnNames"), aggs, spec.get_int("groupsHint", 0));
+    g->group_cols = spec.str_list("groupColumnNames");
+    g->aggs = aggs;
+    g->hint = spec.get_int("groupsHint", 0);
+    g->table = group_table_create(g->group_cols, g->aggs, g->hint);
     *out = g.release();
   });
 }
@@ -814,6 +825,13 @@ int32_t gfpdb_group_finalize(gfpdb_group* group, ArrowSchema* out_schema, ArrowD
     cudaStream_t s = as_stream(stream);
     export_tupleset(group_table_finalize(*group->table, s), out_schema, out, false, s);
     sync(s);
+  });
+}
+
+int32_t gfpdb_group_clear(gfpdb_group* group) {
+  return guarded([&] {
+    require(group != nullptr, "null argument");
+    group->table = group_table_create(group->group_cols, group->aggs, group->hint);
   });
 }
 

@@ -31,6 +31,8 @@ LeafOp negate(LeafOp op) {
     case LO_FALSE: return LO_TRUE;
     case LO_STR_EQ: return LO_STR_NE;
     case LO_STR_NE: return LO_STR_EQ;
+    case LO_STRCOL_EQ: return LO_STRCOL_NE;
+    case LO_STRCOL_NE: return LO_STRCOL_EQ;
   }
   return op;
 }
@@ -415,7 +417,16 @@ Leaf compare_leaf(const ExprPtr& e, LeafOp op, const std::vector<Field>& schema,
     if (op != LO_EQ && op != LO_NE) fail(GFPDB_EUNSUPPORTED, "only = and != compare strings");
     if (a->kind == Expr::StrLiteral) return string_leaf(b, a->str, op == LO_EQ, schema, p, slots);
     if (b->kind == Expr::StrLiteral) return string_leaf(a, b->str, op == LO_EQ, schema, p, slots);
-    fail(GFPDB_EUNSUPPORTED, "string comparison needs a string literal operand");
+    if (a->kind == Expr::Column && b->kind == Expr::Column && ta == DType::Utf8 && tb == DType::Utf8) {
+      Leaf l{};
+      l.op = op == LO_EQ ? LO_STRCOL_EQ : LO_STRCOL_NE;
+      l.lhs.kind = OPND_COL;
+      l.lhs.col = static_cast<int16_t>(slots.slot_for(a->name, DType::Utf8));
+      l.rhs.kind = OPND_COL;
+      l.rhs.col = static_cast<int16_t>(slots.slot_for(b->name, DType::Utf8));
+      return l;
+    }
+    fail(GFPDB_EUNSUPPORTED, "string comparison needs a string literal or two string columns");
   }
   DType ct = (ta == DType::Float64 || tb == DType::Float64) ? DType::Float64 : DType::Int64;
   Leaf l{};

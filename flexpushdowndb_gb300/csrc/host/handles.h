@@ -12,11 +12,12 @@ struct gfpdb_filter {
 
 struct gfpdb_bloom {
   gfpdb::BloomPtr bloom;
+  int32_t key_columns = 1;  // the filter holds the composite of this many key columns
 };
 
 struct gfpdb_hashjoin {
   int32_t join_type = GFPDB_JOIN_INNER;
-  std::string build_key, probe_key;
+  std::vector<std::string> build_keys, probe_keys;
   std::vector<std::string> needed;
   bool all_columns = true;
   double load_factor = 0.5;
@@ -27,4 +28,8 @@ struct gfpdb_hashjoin {
 
 struct gfpdb_group {
   std::shared_ptr<gfpdb::GroupTable> table;
+  // the spec, to start a fresh table on clear
+  std::vector<std::string> group_cols;
+  std::vector<gfpdb::GroupAggregate> aggs;
+  int64_t hint = 0;
 };

@@ -361,16 +361,94 @@ TupleSetPtr probe_join(const std::string& join_name, const JoinTable& table, con
   return TupleSet::make(std::move(fields), std::move(cols), n);
 }
 
+}  // namespace
+
+// The join table over a build side: keyed on its single key column, or on
+// the composite of several (with the key columns aliased for the equality
+// check that probe_join_multi makes).
+JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::string>& keys, double load_factor,
+                           cudaStream_t s) {
+  JoinTable t;
+  t.build = keys.size() == 1 ? build : with_composite_key(build, keys, kBuildKeyColumn, kBuildKeyAlias, s);
+  t.key_col = t.build->require_column(keys.size() == 1 ? keys[0] : std::string(kBuildKeyColumn));
+  join_build_table(t, load_factor, s);
+  return t;
+}
+
+namespace {
+
+// A join on several key columns (HashJoinPredicate's column lists,
+// fpdb-executor/include/fpdb/executor/physical/join/hashjoin/HashJoinPredicate.h:25-26),
+// over a table built on the build side's composite key (with its key columns
+// aliased, build_join_table): the probe side gets its composite, the join
+// pairs composites, and a selection keeps the rows whose key columns are
+// equal pairwise, so composite collisions cannot add rows. The output is the
+// single-key join's: probe then build columns, filtered to `proj`.
+TupleSetPtr probe_join_multi(const std::string& join_name, const JoinTable& table,
+                             const std::vector<std::string>& proj, const std::vector<std::string>& probe_keys,
+                             const TupleSetPtr& ts, cudaStream_t stream) {
+  TupleSetPtr pk = with_composite_key(ts, probe_keys, kProbeKeyColumn, "", stream);
+  const TupleSet& b = *table.build;
+  std::vector<std::string> wanted;  // requested output columns
+  if (proj.empty()) {
+    for (int i = 0; i < ts->num_columns(); ++i) wanted.push_back(ts->field(i).name);
+    for (int i = 0; i < b.num_columns(); ++i)
+      if (!is_internal_key_column(b.field(i).name)) wanted.push_back(b.field(i).name);
+  } else {
+    wanted = proj;
+  }
+  std::vector<std::string> with_keys = wanted;
+  for (const auto& k : probe_keys)
+    if (std::find(with_keys.begin(), with_keys.end(), k) == with_keys.end()) with_keys.push_back(k);
+  for (size_t i = 0; i < probe_keys.size(); ++i) with_keys.push_back(kBuildKeyAlias + std::to_string(i));
+  TupleSetPtr joined = probe_join(join_name, table, with_keys, kProbeKeyColumn, pk, stream);
+  auto conj = std::make_shared<Expr>();
+  conj->kind = Expr::And;
+  for (size_t i = 0; i < probe_keys.size(); ++i) {
+    auto l = std::make_shared<Expr>();
+    l->kind = Expr::Column;
+    l->name = probe_keys[i];
+    auto r = std::make_shared<Expr>();
+    r->kind = Expr::Column;
+    r->name = kBuildKeyAlias + std::to_string(i);
+    auto eq = std::make_shared<Expr>();
+    eq->kind = Expr::Compare;
+    eq->cmp = LO_EQ;
+    eq->kids = {l, r};
+    conj->kids.push_back(eq);
+  }
+  const CompiledPredicate pred = compile_predicate(conj, joined->fields());
+  std::vector<std::string> out_cols;  // the join's order (probe, then build) of the requested columns
+  for (int i = 0; i < joined->num_columns(); ++i) {
+    const std::string& n = joined->field(i).name;
+    if (std::find(wanted.begin(), wanted.end(), n) != wanted.end()) out_cols.push_back(n);
+  }
+  return select_rows(*joined, &pred, {}, out_cols, false, stream);
+}
+
+}  // namespace
+
+TupleSetPtr join_probe_keys(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
+                            const std::vector<std::string>& probe_keys, const TupleSetPtr& ts, cudaStream_t s) {
+  return probe_keys.size() == 1 ? probe_join(join_name, table, proj, probe_keys[0], ts, s)
+                                : probe_join_multi(join_name, table, proj, probe_keys, ts, s);
+}
+
+namespace {
+
 // HashJoinArrowPOp (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowPOp.cpp:85-153):
 // routes TupleSets by sender to the build or probe side, builds the table
 // once every build producer is complete, probes as probe input arrives.
 class HashJoinArrowPOp : public PhysicalOp {
  public:
   HashJoinArrowPOp(std::string name, std::vector<std::string> build_producers, std::vector<std::string> probe_producers,
-                   std::string build_key, std::string probe_key, double load_factor)
+                   std::vector<std::string> build_keys, std::vector<std::string> probe_keys, double load_factor)
       : PhysicalOp(std::move(name), "HashJoinArrowPOp"), build_producers_(std::move(build_producers)),
-        probe_producers_(std::move(probe_producers)), build_key_(std::move(build_key)),
-        probe_key_(std::move(probe_key)), load_factor_(load_factor) {}
+        probe_producers_(std::move(probe_producers)), build_keys_(std::move(build_keys)),
+        probe_keys_(std::move(probe_keys)), load_factor_(load_factor) {
+    if (build_keys_.empty() || build_keys_.size() != probe_keys_.size())
+      fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': as many probe keys as build keys, at least one");
+  }
 
   void onReceive(const Envelope& env) override {
     const Message& m = env.getMessage();
@@ -411,9 +489,8 @@ class HashJoinArrowPOp : public PhysicalOp {
 
   void finalizeBuild() {
     if (build_.empty()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': no build-side input");
-    table_.build = TupleSet::concatenate(build_, ctx()->stream());
-    table_.key_col = table_.build->require_column(build_key_);
-    join_build_table(table_, load_factor_, ctx()->stream());
+    table_ = build_join_table(TupleSet::concatenate(build_, ctx()->stream()), build_keys_, load_factor_,
+                              ctx()->stream());
     build_.clear();
     built_ = true;
   }
@@ -421,12 +498,14 @@ class HashJoinArrowPOp : public PhysicalOp {
   void probe(const TupleSetPtr& ts) {
     Message out;
     out.type = MessageType::TUPLESET;
-    out.tuples = probe_join(name_, table_, projectColumnNames_, probe_key_, ts, ctx()->stream());
+    out.tuples = probe_keys_.size() == 1
+                     ? probe_join(name_, table_, projectColumnNames_, probe_keys_[0], ts, ctx()->stream())
+                     : probe_join_multi(name_, table_, projectColumnNames_, probe_keys_, ts, ctx()->stream());
     ctx()->tell(out);
   }
 
   std::vector<std::string> build_producers_, probe_producers_;
-  std::string build_key_, probe_key_;
+  std::vector<std::string> build_keys_, probe_keys_;
   double load_factor_;
   std::vector<TupleSetPtr> build_, probe_buffer_;
   JoinTable table_;
@@ -1105,9 +1184,14 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
   } else if (type == "HashJoinArrowPOp") {
     std::string jt = o.get_str("joinType", "INNER");
     if (jt != "INNER") fail(GFPDB_EUNSUPPORTED, "join type '" + jt + "' (only INNER runs on the GPU path)");
+    // one key column per side ("buildKey" / "probeKey") or lists of them
+    // ("buildKeys" / "probeKeys", HashJoinPredicate.h:25-26)
+    std::vector<std::string> bk = o.contains("buildKeys") ? o.str_list("buildKeys")
+                                                          : std::vector<std::string>{o.at("buildKey").str()};
+    std::vector<std::string> pk = o.contains("probeKeys") ? o.str_list("probeKeys")
+                                                          : std::vector<std::string>{o.at("probeKey").str()};
     op = std::make_unique<HashJoinArrowPOp>(name, o.str_list("buildProducers"), o.str_list("probeProducers"),
-                                            o.at("buildKey").str(), o.at("probeKey").str(),
-                                            o.get_num("loadFactor", 0.5));
+                                            std::move(bk), std::move(pk), o.get_num("loadFactor", 0.5));
   } else if (type == "HashJoinChainPOp") {
     std::vector<ChainJoinSpec> joins;
     for (auto& j : o.at("joins").array()) {
@@ -1335,7 +1419,8 @@ json::Value fuse_join_chains(const json::Value& plan) {
   if (ops_v == nullptr) return out;
   auto& ops = ops_v->a;
   auto is_join = [](const json::Value& o) {
-    return o.at("type").str() == "HashJoinArrowPOp" && o.get_str("joinType", "INNER") == "INNER";
+    return o.at("type").str() == "HashJoinArrowPOp" && o.get_str("joinType", "INNER") == "INNER" &&
+           !o.contains("buildKeys");  // multi-column keys join one at a time
   };
   auto index_of = [&](const std::string& name) {
     for (size_t i = 0; i < ops.size(); ++i)

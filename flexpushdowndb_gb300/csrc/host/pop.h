@@ -220,6 +220,13 @@ class Execution {
   std::vector<DeferredCheck> captured_checks_;
 };
 
+// Join tables and probes on one or several key columns (the C ABI's hash
+// join and HashJoinArrowPOp share them).
+JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::string>& keys, double load_factor,
+                           cudaStream_t s);
+TupleSetPtr join_probe_keys(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
+                            const std::vector<std::string>& probe_keys, const TupleSetPtr& ts, cudaStream_t s);
+
 // Build an Execution from a JSON plan (format documented with
 // gfpdb_execute_plan in include/gfpdb.h).
 std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream);

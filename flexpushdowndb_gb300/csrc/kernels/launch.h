@@ -250,6 +250,20 @@ class StarBatch {
   std::unique_ptr<StarBatchState> st_;
 };
 
+// --------------------------------------------------------------- keys.cu
+
+constexpr int kMaxKeyColumns = 8;
+// Names of the columns multi-column joins add internally.
+constexpr const char* kBuildKeyColumn = "__gfpdb_bkey";
+constexpr const char* kProbeKeyColumn = "__gfpdb_pkey";
+constexpr const char* kBuildKeyAlias = "__gfpdb_bk";
+// `t` plus an int64 column `name` combining the hashes of the key columns
+// (equal keys, equal values), and with a non-empty alias_prefix the key
+// columns again under the names alias_prefix + "0", "1", ... (same buffers).
+TupleSetPtr with_composite_key(const TupleSetPtr& t, const std::vector<std::string>& keys, const std::string& name,
+                               const std::string& alias_prefix, cudaStream_t s);
+bool is_internal_key_column(const std::string& name);
+
 // ------------------------------------------------------------ project.cu
 
 constexpr int kMaxProjOut = 16;

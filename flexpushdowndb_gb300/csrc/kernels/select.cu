@@ -190,6 +190,22 @@ __device__ __forceinline__ uint32_t leaf8(const SelectParams& p, const Leaf& L, 
     }
     return r;
   }
+  if (L.op == LO_STRCOL_EQ || L.op == LO_STRCOL_NE) {
+    const DevCol& c1 = p.cols[L.lhs.col];
+    const DevCol& c2 = p.cols[L.rhs.col];
+    const uint8_t* s1 = static_cast<const uint8_t*>(c1.data);
+    const uint8_t* s2 = static_cast<const uint8_t*>(c2.data);
+    uint32_t r = 0;
+    for (int k = 0; k < kSelItems; ++k) {
+      if (!((need >> k) & 1u)) continue;
+      const int32_t b1 = c1.offsets[row0 + k], e1 = c1.offsets[row0 + k + 1];
+      const int32_t b2 = c2.offsets[row0 + k], e2 = c2.offsets[row0 + k + 1];
+      bool eq = (e1 - b1) == (e2 - b2);
+      for (int32_t i = 0; eq && i < e1 - b1; ++i) eq = s1[b1 + i] == s2[b2 + i];
+      if (eq == (L.op == LO_STRCOL_EQ)) r |= 1u << k;
+    }
+    return r;
+  }
   int64_t a[8], b[8];
   operand8(p, L.lhs, row0, need, vec, a);
   operand8(p, L.rhs, row0, need, vec, b);

@@ -52,7 +52,8 @@ struct Operand {
 enum LeafOp : int8_t {
   LO_LT = 0, LO_LE, LO_GT, LO_GE, LO_EQ, LO_NE,
   LO_TRUE, LO_FALSE,
-  LO_STR_EQ, LO_STR_NE  // utf8 column vs utf8 literal held in the string pool
+  LO_STR_EQ, LO_STR_NE,     // utf8 column vs utf8 literal held in the string pool
+  LO_STRCOL_EQ, LO_STRCOL_NE  // utf8 column vs utf8 column (lhs.col, rhs.col)
 };
 
 struct Leaf {

@@ -37,6 +37,10 @@ def _names(cols: Sequence[str] | None):
     return _abi.cstr_array(list(cols)), len(cols)
 
 
+def _key_list(k) -> list[str]:
+    return [k] if isinstance(k, str) else list(k)
+
+
 def init(device: int = 0) -> None:
     _abi.check(_abi.lib().gfpdb_device_init(device))
 
@@ -70,14 +74,18 @@ class Filter:
 class BloomFilter:
     """Blocked bloom filter built on the device (BloomFilterCreateArrowKernel)."""
 
-    def __init__(self, batches: Sequence, key_column: str, bits_per_key: int = 10, num_hashes: int = 3, stream=None):
+    def __init__(self, batches: Sequence, key_column: str | Sequence[str], bits_per_key: int = 10,
+                 num_hashes: int = 3, stream=None):
+        """key_column: one column name, or a list of them (the filter holds
+        their composite)."""
         exs = [_export(b) for b in batches]
         if not exs:
             raise ValueError("BloomFilter needs at least one batch (the schema comes from it)")
         arr = (ctypes.POINTER(_abi.ArrowDeviceArray) * len(exs))(*[e.array_ptr for e in exs])
+        keys = _key_list(key_column)
         self._h = ctypes.c_void_p()
-        _abi.check(_abi.lib().gfpdb_bloom_create(exs[0].schema_ptr, arr, len(exs), key_column.encode(), bits_per_key,
-                                                 num_hashes, ctypes.byref(self._h), stream))
+        _abi.check(_abi.lib().gfpdb_bloom_create(exs[0].schema_ptr, arr, len(exs), _abi.cstr_array(keys), len(keys),
+                                                 bits_per_key, num_hashes, ctypes.byref(self._h), stream))
 
     def info(self) -> dict:
         nb, nk = ctypes.c_int64(), ctypes.c_int64()
@@ -96,10 +104,11 @@ class BloomFilter:
             _abi.check(_abi.lib().gfpdb_memcpy(out.ctypes.data, info["device_ptr"], out.nbytes, 2, None))
         return out
 
-    def use(self, table, key_column: str, stream=None) -> Table:
+    def use(self, table, key_column: str | Sequence[str], stream=None) -> Table:
         ex = _export(table)
+        keys = _key_list(key_column)
         s, a = new_output()
-        _abi.check(_abi.lib().gfpdb_bloom_use(self._h, ex.schema_ptr, ex.array_ptr, key_column.encode(),
+        _abi.check(_abi.lib().gfpdb_bloom_use(self._h, ex.schema_ptr, ex.array_ptr, _abi.cstr_array(keys), len(keys),
                                               ctypes.byref(s), ctypes.byref(a), stream))
         return import_result(s, a)
 
@@ -126,11 +135,17 @@ def select(table, predicate: Filter | None = None, blooms: Sequence[tuple[BloomF
 class HashJoin:
     """Inner hash join (HashJoinArrowKernel). Output: probe columns, then build columns."""
 
-    def __init__(self, build_key: str, probe_key: str, needed: Sequence[str] | None = None, load_factor: float = 0.5):
+    def __init__(self, build_key: str | Sequence[str], probe_key: str | Sequence[str],
+                 needed: Sequence[str] | None = None, load_factor: float = 0.5):
+        """Keys: one column per side, or equally long lists (build_key[i]
+        matches probe_key[i])."""
         names, n = _names(needed)
+        bk, pk = _key_list(build_key), _key_list(probe_key)
+        if len(bk) != len(pk):
+            raise ValueError("as many probe key columns as build key columns")
         self._h = ctypes.c_void_p()
-        _abi.check(_abi.lib().gfpdb_hashjoin_create(0, build_key.encode(), probe_key.encode(), names, n, load_factor,
-                                                    ctypes.byref(self._h)))
+        _abi.check(_abi.lib().gfpdb_hashjoin_create(0, _abi.cstr_array(bk), _abi.cstr_array(pk), len(bk), names, n,
+                                                    load_factor, ctypes.byref(self._h)))
 
     def put_build(self, table, stream=None) -> None:
         ex = _export(table)
@@ -145,6 +160,10 @@ class HashJoin:
         _abi.check(_abi.lib().gfpdb_hashjoin_probe(self._h, ex.schema_ptr, ex.array_ptr, ctypes.byref(s),
                                                    ctypes.byref(a), stream))
         return import_result(s, a)
+
+    def clear(self) -> None:
+        """Drop the build side and the table (HashJoinArrowKernel::clear)."""
+        _abi.check(_abi.lib().gfpdb_hashjoin_clear(self._h))
 
     def info(self) -> dict:
         b, c, m = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
@@ -175,6 +194,10 @@ class Group:
     def group(self, table, stream=None) -> None:
         ex = _export(table)
         _abi.check(_abi.lib().gfpdb_group_update(self._h, ex.schema_ptr, ex.array_ptr, stream))
+
+    def clear(self) -> None:
+        """Drop every group (GroupAbstractKernel::clear)."""
+        _abi.check(_abi.lib().gfpdb_group_clear(self._h))
 
     def finalise(self, stream=None) -> Table:
         s, a = new_output()

@@ -174,8 +174,9 @@ int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, const struct A
 /* ------------------------------------------------------------------ bloom */
 
 /* Build a blocked bloom filter (256-bit blocks, `num_hashes` bits per key set
- * inside one block, sized `bits_per_key` bits per key) over the key column of
- * one or more TupleSets. Replaces BloomFilterCreateArrowKernel::buildBloomFilter
+ * inside one block, sized `bits_per_key` bits per key) over the key of one or
+ * more TupleSets: one column, or the composite of n_keys columns (the
+ * reference's bloomFilterColumnNames, BloomFilterCreatePOp.cpp:17-22). Replaces BloomFilterCreateArrowKernel::buildBloomFilter
  * (fpdb-executor/src/physical/bloomfilter/BloomFilterCreateArrowKernel.cpp:17-34)
  * and ArrowBloomFilter::build (.../bloomfilter/ArrowBloomFilter.cpp:29-75).
  * Above GFPDB_BLOOM_MAX_INPUT_SIZE keys the filter is marked invalid and every
@@ -185,14 +186,15 @@ int32_t gfpdb_filter_evaluate_noalloc(const gfpdb_filter* filter, const struct A
 #define GFPDB_BLOOM_MAX_INPUT_SIZE 20000000
 int32_t gfpdb_bloom_create(const struct ArrowSchema* schema,
                            const struct ArrowDeviceArray* const* batches, int32_t n_batches,
-                           const char* key_column, int32_t bits_per_key, int32_t num_hashes,
-                           gfpdb_bloom** out, void* stream);
+                           const char* const* key_columns, int32_t n_keys, int32_t bits_per_key,
+                           int32_t num_hashes, gfpdb_bloom** out, void* stream);
 
-/* Keep the rows whose key column may be in the filter; all columns are kept.
- * Replaces BloomFilterUseKernel::filter(tupleSet, bloomFilter, columnNames)
- * (fpdb-executor/src/physical/bloomfilter/BloomFilterUseKernel.cpp:12-32). */
+/* Keep the rows whose key may be in the filter; all columns are kept. The
+ * key columns (1 to 8, as many as the filter was built over) are named in
+ * key_columns. Replaces BloomFilterUseKernel::filter(tupleSet, bloomFilter,
+ * columnNames) (fpdb-executor/src/physical/bloomfilter/BloomFilterUseKernel.cpp:12-32). */
 int32_t gfpdb_bloom_use(const gfpdb_bloom* bloom, const struct ArrowSchema* in_schema,
-                        const struct ArrowDeviceArray* in, const char* key_column,
+                        const struct ArrowDeviceArray* in, const char* const* key_columns, int32_t n_keys,
                         struct ArrowSchema* out_schema, struct ArrowDeviceArray* out, void* stream);
 
 /* Filter structure, for tests and for shipping a filter to another device:
@@ -218,14 +220,18 @@ int32_t gfpdb_select(const gfpdb_filter* filter, int32_t n_blooms, const gfpdb_b
 
 /* -------------------------------------------------------------- hash join */
 
-/* Create a hash join with the given key columns (one key column per side).
+/* Create a hash join on n_keys key columns per side (1 to 8; build_keys[i]
+ * matches probe_keys[i], HashJoinPredicate(leftColumnNames,
+ * rightColumnNames), fpdb-executor/include/fpdb/executor/physical/join/hashjoin/HashJoinPredicate.h:25-26;
+ * several columns are joined on a composite of their hashes and the rows
+ * whose key columns differ are then dropped, so the result is exact).
  * Output columns are the probe side's needed columns followed by the build
  * side's, as HashJoinArrowKernel::makeOutputSchema orders them
  * (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:148-162).
  * `needed_columns` NULL / n_needed < 0 keeps every column.
  * Replaces HashJoinArrowKernel::make (HashJoinArrowKernel.h:48-54). */
-int32_t gfpdb_hashjoin_create(int32_t join_type, const char* build_key, const char* probe_key,
-                              const char* const* needed_columns, int32_t n_needed,
+int32_t gfpdb_hashjoin_create(int32_t join_type, const char* const* build_keys, const char* const* probe_keys,
+                              int32_t n_keys, const char* const* needed_columns, int32_t n_needed,
                               double load_factor, gfpdb_hashjoin** out);
 
 /* Append a build-side TupleSet. Replaces HashJoinArrowKernel::joinBuildTupleSet
@@ -247,6 +253,11 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const struct ArrowSchema* sch
 /* Build-table statistics: rows, slots, longest probe run seen while building. */
 int32_t gfpdb_hashjoin_info(const gfpdb_hashjoin* join, int64_t* build_rows, int64_t* capacity,
                             int64_t* max_probe);
+
+/* Drop the build input and the table, so the join can take a new build side.
+ * Replaces HashJoinArrowKernel::clear (HashJoinArrowKernel.h:56, the
+ * PhysicalOp::clear seam, fpdb-executor/include/fpdb/executor/physical/PhysicalOp.h:84). */
+int32_t gfpdb_hashjoin_clear(gfpdb_hashjoin* join);
 
 void gfpdb_hashjoin_free(gfpdb_hashjoin* join);
 
@@ -274,6 +285,11 @@ int32_t gfpdb_group_update(gfpdb_group* group, const struct ArrowSchema* schema,
  * (GroupAbstractKernel.h:39; GroupArrowKernel.cpp:41-68). */
 int32_t gfpdb_group_finalize(gfpdb_group* group, struct ArrowSchema* out_schema,
                              struct ArrowDeviceArray* out, void* stream);
+
+/* Drop every group, so the same spec starts over. Replaces
+ * GroupAbstractKernel::clear
+ * (fpdb-executor/include/fpdb/executor/physical/group/GroupAbstractKernel.h:44). */
+int32_t gfpdb_group_clear(gfpdb_group* group);
 
 void gfpdb_group_free(gfpdb_group* group);
 

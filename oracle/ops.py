@@ -158,6 +158,28 @@ def hash_join(build: Table, probe: Table, build_key: str, probe_key: str, needed
 # ------------------------------------------------------------------- group
 
 
+def hash_join_keys(build: Table, probe: Table, build_keys, probe_keys, needed=None) -> Table:
+    """Inner join on several key columns (HashJoinPredicate's column lists,
+    fpdb-executor/include/fpdb/executor/physical/join/hashjoin/HashJoinPredicate.h:25-26):
+    every (probe, build) pair whose key columns are equal pairwise; probe
+    columns then build columns."""
+    bk = list(zip(*[build[k] if isinstance(build[k], list) else build[k].tolist() for k in build_keys]))
+    pk = list(zip(*[probe[k] if isinstance(probe[k], list) else probe[k].tolist() for k in probe_keys]))
+    index: dict = {}
+    for r, k in enumerate(bk):
+        index.setdefault(k, []).append(r)
+    pi, bi = [], []
+    for r, k in enumerate(pk):
+        for b in index.get(k, ()):
+            pi.append(r)
+            bi.append(b)
+    pnames = [n for n in probe.names if needed is None or n in needed]
+    bnames = [n for n in build.names if needed is None or n in needed]
+    p = take(probe, np.array(pi, dtype=np.int64), pnames if needed is not None else None)
+    b = take(build, np.array(bi, dtype=np.int64), bnames if needed is not None else None)
+    return Table(p.columns + b.columns)
+
+
 def group_by(table: Table, group_cols: list[str], aggregates: list[dict]) -> Table:
     """aggregates: [{"function": SUM|COUNT|MIN|MAX|AVG, "name": .., "expr": ..}]"""
     n = table.num_rows

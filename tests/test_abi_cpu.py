@@ -107,8 +107,12 @@ def test_group_spec_errors():
 def test_hashjoin_rejects_outer_joins():
     L = _abi.lib()
     h = ctypes.c_void_p()
-    rc = L.gfpdb_hashjoin_create(3, b"a", b"b", None, -1, 0.5, ctypes.byref(h))
+    rc = L.gfpdb_hashjoin_create(3, _abi.cstr_array(["a"]), _abi.cstr_array(["b"]), 1, None, -1, 0.5, ctypes.byref(h))
     assert rc == _abi.GFPDB_EUNSUPPORTED
+    for n in (0, 9):  # a key has 1 to 8 columns
+        keys = _abi.cstr_array(["a"] * max(n, 1))
+        rc = L.gfpdb_hashjoin_create(0, keys, keys, n, None, -1, 0.5, ctypes.byref(h))
+        assert rc == _abi.GFPDB_EINVAL
 
 
 def test_export_host_roundtrip_structure():

@@ -7,7 +7,7 @@ and group outputs have no order and are compared as sorted multisets.
 import numpy as np
 import pytest
 
-from flexpushdowndb_gb300 import ops, workloads
+from flexpushdowndb_gb300 import GfpdbError, ops, workloads
 from flexpushdowndb_gb300.expression import (and_, cast, col, divide, eq, gt, gte, in_, isNull, lt, lte, minus, neq,
                                              not_, num_lit, or_, plus, str_lit, times)
 from flexpushdowndb_gb300.tupleset import Column, DeviceTable, Table
@@ -549,3 +549,99 @@ def test_select_large_predicate_with_probes(gpu):
     pred = and_(gt(col("qty"), num_lit(10)), lte(num_lit(3), col("discount")))
     got = ops.select(DeviceTable.from_host(fact), ops.Filter(pred, fact), blooms)
     assert got.rows() == oops.filter_table(seq, pred).rows()
+
+
+def test_group_and_join_clear(gpu):
+    """clear() (GroupAbstractKernel.h:44, HashJoinArrowKernel.h:56): a
+    cleared group-by starts over with the same spec, a cleared join takes a
+    new build side."""
+    from flexpushdowndb_gb300.expression import col as c_
+    from flexpushdowndb_gb300.ops import aggregate
+
+    rng = np.random.default_rng(31)
+    t1 = Table([Column("k", "int32", rng.integers(0, 50, 5000)), Column("v", "int64", rng.integers(0, 100, 5000))])
+    t2 = Table([Column("k", "int32", rng.integers(0, 9, 700)), Column("v", "int64", rng.integers(0, 100, 700))])
+    g = ops.Group(["k"], [aggregate("SUM", "s", c_("v")), aggregate("COUNT", "n")])
+    g.group(DeviceTable.from_host(t1))
+    g.clear()
+    g.group(DeviceTable.from_host(t2))
+    want = oops.group_by(t2, ["k"], [{"function": "SUM", "name": "s", "expr": c_("v")},
+                                     {"function": "COUNT", "name": "n"}])
+    assert g.finalise().sorted_rows() == want.sorted_rows()
+    b1 = Table([Column("bk", "int32", np.arange(100)), Column("bv", "int64", np.arange(100) * 3)])
+    b2 = Table([Column("bk", "int32", np.arange(50, 60)), Column("bv", "int64", np.arange(10) * 7)])
+    probe = Table([Column("pk", "int32", rng.integers(0, 120, 2000))])
+    j = ops.HashJoin("bk", "pk")
+    j.put_build(DeviceTable.from_host(b1))
+    j.finalize_build()
+    j.probe(DeviceTable.from_host(probe))
+    j.clear()
+    j.put_build(DeviceTable.from_host(b2))
+    j.finalize_build()
+    got = j.probe(DeviceTable.from_host(probe))
+    assert got.sorted_rows() == oops.hash_join(b2, probe, "bk", "pk").sorted_rows()
+
+
+def _two_key_tables(seed, n_build=3000, n_probe=40_000, utf8=False, wide=False):
+    rng = np.random.default_rng(seed)
+    words = [f"k{i}" for i in range(13)]
+    bk1 = rng.integers(0, 60, n_build)
+    bk2 = rng.integers(0, 70, n_build)
+    build = [Column("b1", "int64" if wide else "int32", bk1 * (10**10 if wide else 1)),
+             Column("b2", "int32", bk2), Column("bv", "int64", rng.integers(0, 10**9, n_build))]
+    probe = [Column("p1", "int64" if wide else "int32", rng.integers(0, 66, n_probe) * (10**10 if wide else 1)),
+             Column("p2", "int32", rng.integers(0, 75, n_probe)), Column("pv", "int32", np.arange(n_probe))]
+    if utf8:
+        build.append(Column("bs", "utf8", [words[i] for i in rng.integers(0, 13, n_build)]))
+        probe.append(Column("ps", "utf8", [words[i] for i in rng.integers(0, 13, n_probe)]))
+    return Table(build), Table(probe)
+
+
+@pytest.mark.parametrize("utf8,wide", [(False, False), (True, False), (False, True)])
+def test_two_key_join_matches_oracle(gpu, utf8, wide):
+    """Joins on two (or three, with a utf8 column) key columns: repeated keys
+    on both sides, int64 keys with values past 32 bits, utf8 keys; every pair
+    of rows whose key columns are equal, and no other (HashJoinPredicate.h:25-26)."""
+    build, probe = _two_key_tables(77 + utf8 + 2 * wide, utf8=utf8, wide=wide)
+    bk, pk = ["b1", "b2"] + (["bs"] if utf8 else []), ["p1", "p2"] + (["ps"] if utf8 else [])
+    needed = ["pv", "p1", "bv", "b2"] + (["ps"] if utf8 else [])
+    j = ops.HashJoin(bk, pk, needed)
+    j.put_build(DeviceTable.from_host(build))
+    j.finalize_build()
+    got = j.probe(DeviceTable.from_host(probe))
+    want = oops.hash_join_keys(build, probe, bk, pk, needed)
+    assert got.names == want.names
+    assert got.sorted_rows() == want.sorted_rows()
+
+
+def test_two_key_bloom_filter(gpu):
+    """A bloom filter over two key columns: every probe row whose key pair is
+    in the build side passes (no false negatives); few others do."""
+    build, probe = _two_key_tables(91, n_build=2000, n_probe=100_000)
+    bf = ops.BloomFilter([build], ["b1", "b2"])
+    kept = bf.use(DeviceTable.from_host(probe), ["p1", "p2"])
+    inside = set(zip(build["b1"].tolist(), build["b2"].tolist()))
+    pairs = list(zip(probe["p1"].tolist(), probe["p2"].tolist()))
+    want_rows = {r for r, k in enumerate(pairs) if k in inside}
+    kept_rows = set(kept["pv"].tolist())
+    assert want_rows <= kept_rows
+    assert len(kept_rows - want_rows) / max(1, len(pairs) - len(want_rows)) < 0.035
+    with pytest.raises(GfpdbError):
+        bf.use(DeviceTable.from_host(probe), "p1")  # built over two columns
+
+
+def test_two_key_join_in_a_plan(gpu):
+    from flexpushdowndb_gb300 import plan
+
+    build, probe = _two_key_tables(93)
+    p = plan.Plan()
+    p.scan("sb", "b")
+    p.scan("sp", "p")
+    p._add({"type": "HashJoinArrowPOp", "name": "j", "buildProducers": ["sb"], "probeProducers": ["sp"],
+            "buildKeys": ["b1", "b2"], "probeKeys": ["p1", "p2"], "projectColumnNames": ["pv", "bv"]})
+    p.connect("sb", "j")
+    p.connect("sp", "j")
+    p.collate("c", "j")
+    got = plan.execute(p, {"b": build, "p": probe}).table
+    want = oops.hash_join_keys(build, probe, ["b1", "b2"], ["p1", "p2"], ["pv", "bv"])
+    assert got.sorted_rows() == want.sorted_rows()
