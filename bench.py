@@ -574,7 +574,7 @@ def run_case(args):
         fn = lambda: batch.star_batch(spec, dev, use_graph=False).table  # noqa: E731
         args.rows = sum(tabs[p].num_rows for p in parts)
         return _time_case(args, fn)
-    if args.case in ("join", "group", "csv", "filter"):
+    if args.case in ("join", "group", "csv", "filter", "shuffle", "group2"):
         return _operator_case(args)
     tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
     fact = DeviceTable.from_host(tabs["fact"])
@@ -613,7 +613,11 @@ def _operator_case(args):
     `csv`: the lineitem text of args.rows rows parsed on the device;
     `filter`: a two-comparison range conjunction (~2% of rows) over an int32
     and an int64 column of args.rows rows, projecting an int32 and an int64
-    column; prints the kernel's algorithmic GB/s beside the call time."""
+    column; `shuffle`: args.rows rows (Zipf(1.1) int64 key over args.rows / 2
+    values, an int64 and an int32 column) hash-partitioned on the key into
+    args.slots slots; `group2`: the `group` workload as a one-phase plan and
+    as a two-phase plan (4 partial group-bys, shuffles, args.slots reduce
+    group-bys); prints the kernels' algorithmic GB/s beside the call time."""
     import numpy as np
 
     from flexpushdowndb_gb300 import ops, workloads
@@ -654,6 +658,56 @@ def _operator_case(args):
 
         prof = _kernel_profile(_abi.lib(), _abi, fn, args.steps)
         print(json.dumps({"case": "group", "rows": n, "kernels_ms": {k: v["ms"] / args.steps for k, v in prof.items()}}))
+    elif args.case == "shuffle":
+        keys = workloads.zipf_keys(n, max(1, n // 2), seed=7001)
+        t = DeviceTable.from_host(Table([Column("k", "int64", keys), Column("v", "int64", rng.integers(0, 10**9, n)),
+                                         Column("p", "int32", rng.integers(0, 100, n))]))
+        fn = lambda: ops.shuffle(t, ["k"], args.slots)  # noqa: E731
+        for _ in range(max(2, args.warmup)):
+            fn()
+        from flexpushdowndb_gb300 import _abi
+
+        prof = _kernel_profile(_abi.lib(), _abi, fn, args.steps)
+        kern = {k: v["ms"] / args.steps for k, v in prof.items()}
+        ms = sum(kern.get(k, 0.0) for k in ("shuffle_count_kernel", "scan_i32_kernel", "shuffle_scatter_kernel"))
+        # the key read twice (count, scatter), every column read and written once
+        algo = n * (8 + 8 + 2 * (8 + 8 + 4))
+        print(json.dumps({"case": "shuffle", "rows": n, "slots": args.slots, "kernels_ms": kern, "shuffle_ms": ms,
+                          "algorithmic_gbs": algo / (ms * 1e6), "rows_per_s": n / (ms * 1e-3)}))
+        return
+    elif args.case == "group2":
+        from flexpushdowndb_gb300 import plan
+
+        whole = workloads.groupby_table(n, max(1, n // 2))
+        aggs = [ops.aggregate("SUM", "s", col("v")), ops.aggregate("COUNT", "c")]
+        one = plan.Plan()
+        one.scan("scan", "t")
+        one.group("g", "scan", ["k"], aggs)
+        one.collate("collate", "g")
+        two = plan.Plan()
+        scans = [two.scan(f"scan{i}", f"t{i}") for i in range(4)]
+        two._add({"type": "CollatePOp", "name": "collate"})
+        for r in two.group_two_phase("g", scans, ["k"], aggs, args.slots):
+            two.connect(r, "collate")
+        quarter = (n + 3) // 4
+        inputs1 = plan.PreparedInputs({"t": DeviceTable.from_host(whole)})
+        inputs2 = plan.PreparedInputs({f"t{i}": DeviceTable.from_host(whole.slice(i * quarter, min(n, (i + 1) * quarter)))
+                                       for i in range(4)})
+        res = {}
+        for label, p, inp in (("one_phase", one, inputs1), ("two_phase", two, inputs2)):
+            fn = lambda: plan.execute(p, inp, result_to_host=False)  # noqa: E731
+            for _ in range(max(2, args.warmup)):
+                out = fn()
+            import torch
+
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                out = fn()
+            torch.cuda.synchronize()
+            res[label] = {"ms_per_call": 1e3 * (time.perf_counter() - t0) / args.steps, "groups": out.table.num_rows}
+        print(json.dumps({"case": "group2", "rows": n, "reduce_groups": args.slots, **res}))
+        return
     elif args.case == "filter":
         from flexpushdowndb_gb300.expression import and_, gte, lt, num_lit
 
@@ -766,6 +820,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, help="profiling case: select | select4 | plan | plan-graph | plan-timeline | batch | join | group | csv")
     ap.add_argument("--parts", type=int, default=64, help="fact partitions of the batch case")
+    ap.add_argument("--slots", type=int, default=256, help="slots of the shuffle case, reduce group-bys of group2")
     ap.add_argument("--items", type=int, default=2, help="itemsPerThread of the batch case")
     ap.add_argument("--bps", type=int, default=2, help="blocksPerSm of the batch case")
     ap.add_argument("--stages", type=int, default=3, help="stages of the batch case")

@@ -150,6 +150,7 @@ SIGNATURES = {
         [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_P)],
     ),
     "gfpdb_bloom_free": (None, [_P]),
+    "gfpdb_shuffle": (_I32, [_S, _A, _CP, _I32, _I64, _S, _A, ctypes.POINTER(_I64), _P]),
     "gfpdb_select": (_I32, [_P, _I32, ctypes.POINTER(_P), _CP, _S, _A, _CP, _I32, _S, _A, _P]),
     "gfpdb_hashjoin_create": (_I32, [_I32, _CP, _CP, _I32, _CP, _I32, ctypes.c_double, ctypes.POINTER(_P)]),
     "gfpdb_hashjoin_put_build": (_I32, [_P, _S, _A, _P]),

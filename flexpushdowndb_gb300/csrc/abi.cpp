@@ -653,6 +653,25 @@ int32_t gfpdb_bloom_info(const gfpdb_bloom* bloom, int64_t* num_blocks, int64_t*
 
 void gfpdb_bloom_free(gfpdb_bloom* bloom) { delete bloom; }
 
+// ----------------------------------------------------------------- shuffle
+
+int32_t gfpdb_shuffle(const ArrowSchema* in_schema, const ArrowDeviceArray* in, const char* const* key_columns,
+                      int32_t n_keys, int64_t num_slots, ArrowSchema* out_schema, ArrowDeviceArray* out,
+                      int64_t* slot_offsets, void* stream) {
+  return guarded([&] {
+    require(key_columns != nullptr && out_schema != nullptr && out != nullptr && slot_offsets != nullptr,
+            "null argument");
+    require(n_keys >= 1 && n_keys <= kMaxKeyColumns, "a shuffle key has 1 to 8 columns");
+    require(num_slots >= 1 && num_slots <= kShuffleMaxSlots, "shuffle slots must be 1 to 1024");
+    ensure_device();
+    cudaStream_t s = as_stream(stream);
+    TupleSetPtr ts = import_tupleset(in_schema, in, s);
+    ShuffleResult r = shuffle_rows(ts, names_of(key_columns, n_keys), num_slots, s);
+    export_tupleset(r.rows, out_schema, out, false, s);
+    std::copy(r.offsets.begin(), r.offsets.end(), slot_offsets);
+  });
+}
+
 // ------------------------------------------------------------ fused select
 
 int32_t gfpdb_select(const gfpdb_filter* filter, int32_t n_blooms, const gfpdb_bloom* const* blooms,
@@ -783,22 +802,7 @@ int32_t gfpdb_group_create(const char* group_spec_json, gfpdb_group** out) {
     } catch (const std::exception& e) {
       fail(GFPDB_EINVAL, e.what());
     }
-    std::vector<GroupAggregate> aggs;
-    for (auto& a : spec.at("aggregates").array()) {
-      GroupAggregate g;
-      const std::string f = a.at("function").str();
-      if (f == "SUM") g.fn = AGG_SUM;
-      else if (f == "COUNT") g.fn = AGG_COUNT;
-      else if (f == "MIN") g.fn = AGG_MIN;
-      else if (f == "MAX") g.fn = AGG_MAX;
-      else if (f == "AVG") g.fn = AGG_AVG;
-      else fail(GFPDB_EUNSUPPORTED, "aggregate function '" + f + "'");
-      g.name = a.at("name").str();
-      if (a.contains("expr") && a.at("expr").kind != json::Value::Null) g.expr = parse_expr(a.at("expr"));
-      else if (g.fn == AGG_COUNT) g.fn = AGG_COUNT_STAR;
-      else fail(GFPDB_EINVAL, "aggregate '" + g.name + "' needs an expr");
-      aggs.push_back(g);
-    }
+    std::vector<GroupAggregate> aggs = pop::parse_aggregates(spec.at("aggregates"));
     auto g = std::make_unique<gfpdb_group>();
     g->group_cols = spec.str_list("groupColumnNames");
     g->aggs = aggs;

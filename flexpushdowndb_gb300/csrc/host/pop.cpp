@@ -112,18 +112,7 @@ class TableScanPOp : public PhysicalOp {
   }
 
  private:
-  static TupleSetPtr slice(const TupleSetPtr& ts, int64_t at, int64_t len) {
-    std::vector<ColumnPtr> cols;
-    for (int i = 0; i < ts->num_columns(); ++i) {
-      const auto& c = ts->column(i);
-      auto s = std::make_shared<Column>(*c);
-      s->length = len;
-      if (c->type == DType::Utf8) s->offsets = c->offsets + at;
-      else s->data = static_cast<const char*>(c->data) + at * dtype_width(c->type);
-      cols.push_back(s);
-    }
-    return TupleSet::make(ts->fields(), std::move(cols), len);
-  }
+  static TupleSetPtr slice(const TupleSetPtr& ts, int64_t at, int64_t len) { return slice_rows(ts, at, len); }
   void send(const TupleSetPtr& ts) {
     Message out;
     out.type = MessageType::TUPLESET;
@@ -716,6 +705,50 @@ class GroupPOp : public PhysicalOp {
   std::shared_ptr<GroupTable> table_;
 };
 
+// ShufflePOp (fpdb-executor/src/physical/shuffle/ShufflePOp.cpp:91-172): every
+// TupleSet it receives is hash-partitioned on the shuffle columns into one
+// slot per consumer (slot i goes to the i-th consumer in the plan's order,
+// the reference's consumerVec_), and the slots are buffered. Once all
+// producers are complete, each consumer gets its slot's rows as one TupleSet
+// (empty when no row hashed there), as the reference's forced send on
+// completion does; the reference also sends a slot early once it holds
+// DefaultBufferSize rows, which changes no consumer's result.
+class ShufflePOp : public PhysicalOp {
+ public:
+  ShufflePOp(std::string name, std::vector<std::string> cols)
+      : PhysicalOp(std::move(name), "ShufflePOp"), cols_(std::move(cols)) {}
+
+  void onReceive(const Envelope& env) override {
+    const Message& m = env.getMessage();
+    if (m.type == MessageType::TUPLESET) {
+      const int64_t slots = static_cast<int64_t>(consumers().size());
+      if (slots == 0) fail(GFPDB_EINVAL, "ShufflePOp '" + name_ + "' has no consumers");
+      buffers_.resize(slots);
+      TupleSetPtr in = m.tuples;
+      if (!projectColumnNames_.empty()) in = in->project_exist(projectColumnNames_);
+      ShuffleResult r = shuffle_rows(in, cols_, slots, ctx()->stream());
+      for (int64_t i = 0; i < slots; ++i)
+        buffers_[i].push_back(slice_rows(r.rows, r.offsets[i], r.offsets[i + 1] - r.offsets[i]));
+    } else if (m.type == MessageType::COMPLETE) {
+      if (!is_producer_complete(*this)) return;
+      for (size_t i = 0; i < buffers_.size(); ++i) {
+        Message out;
+        out.type = MessageType::TUPLESET;
+        out.tuples = buffers_[i].size() == 1 ? buffers_[i][0] : TupleSet::concatenate(buffers_[i], ctx()->stream());
+        ctx()->tell(out, {consumers()[i]});
+      }
+      buffers_.clear();
+      ctx()->notifyComplete();
+    }
+  }
+
+  void clear() override { buffers_.clear(); }
+
+ private:
+  std::vector<std::string> cols_;
+  std::vector<std::vector<TupleSetPtr>> buffers_;
+};
+
 // ProjectPOp (fpdb-executor/src/physical/project/ProjectPOp.cpp:48-149):
 // each TupleSet leaves as its pass-through columns under their new names,
 // then one column per expression (evaluated by project_kernel, compiled
@@ -888,10 +921,26 @@ AggFn agg_fn(const std::string& f) {
   if (f == "MIN" || f == "min" || f == "Min") return AGG_MIN;
   if (f == "MAX" || f == "max" || f == "Max") return AGG_MAX;
   if (f == "AVG" || f == "avg" || f == "Avg") return AGG_AVG;
+  if (f == "AVG_REDUCE" || f == "AvgReduce") return AGG_AVG_REDUCE;
   fail(GFPDB_EUNSUPPORTED, "aggregate function '" + f + "'");
 }
 
 }  // namespace
+
+std::vector<GroupAggregate> parse_aggregates(const json::Value& list) {
+  std::vector<GroupAggregate> aggs;
+  for (auto& a : list.array()) {
+    GroupAggregate g;
+    g.fn = agg_fn(a.at("function").str());
+    g.name = a.at("name").str();
+    if (a.contains("expr") && a.at("expr").kind != json::Value::Null) g.expr = parse_expr(a.at("expr"));
+    else if (g.fn == AGG_COUNT) g.fn = AGG_COUNT_STAR;
+    else if (g.fn != AGG_AVG_REDUCE) fail(GFPDB_EINVAL, "aggregate '" + g.name + "' needs an expr");
+    if (g.fn == AGG_AVG_REDUCE && g.expr) fail(GFPDB_EINVAL, "AVG_REDUCE '" + g.name + "' takes no expression");
+    aggs.push_back(g);
+  }
+  return aggs;
+}
 
 // --------------------------------------------------------------- Execution
 
@@ -1244,15 +1293,7 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
     cs->setExecution(exec);
     op = std::move(cs);
   } else if (type == "GroupPOp" || type == "AggregatePOp") {
-    std::vector<GroupAggregate> aggs;
-    for (auto& a : o.at("aggregates").array()) {
-      GroupAggregate g;
-      g.fn = agg_fn(a.at("function").str());
-      g.name = a.at("name").str();
-      if (a.contains("expr") && a.at("expr").kind != json::Value::Null) g.expr = parse_expr(a.at("expr"));
-      else if (g.fn == AGG_COUNT) g.fn = AGG_COUNT_STAR;
-      aggs.push_back(g);
-    }
+    std::vector<GroupAggregate> aggs = parse_aggregates(o.at("aggregates"));
     if (type == "AggregatePOp") {
       // AggregatePOp (fpdb-executor/src/physical/aggregate/AggregatePOp.cpp:57-153):
       // the non-grouped aggregate, run as a group-by with one implicit group.
@@ -1291,6 +1332,15 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
       fail(GFPDB_EUNSUPPORTED, "LimitSortPOp '" + name + "': 1 to 4 sort keys");
     if (k < 0 || k > 1024) fail(GFPDB_EUNSUPPORTED, "LimitSortPOp '" + name + "': k must be in [0, 1024]");
     op = std::make_unique<LimitSortPOp>(name, k, std::move(keys));
+  } else if (type == "ShufflePOp") {
+    std::vector<std::string> cols = o.str_list("shuffleColumnNames");
+    if (cols.empty() || cols.size() > static_cast<size_t>(kMaxKeyColumns))
+      fail(GFPDB_EINVAL, "ShufflePOp '" + name + "' shuffles on 1 to 8 columns");
+    if (!o.contains("consumers") || o.at("consumers").array().empty())
+      fail(GFPDB_EINVAL, "ShufflePOp '" + name + "' needs consumers (one slot each)");
+    if (static_cast<int64_t>(o.at("consumers").array().size()) > kShuffleMaxSlots)
+      fail(GFPDB_EINVAL, "ShufflePOp '" + name + "' has more consumers than shuffle slots");
+    op = std::make_unique<ShufflePOp>(name, std::move(cols));
   } else if (type == "CollatePOp") {
     op = std::make_unique<CollatePOp>(name);
   } else {

@@ -227,6 +227,11 @@ JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::stri
 TupleSetPtr join_probe_keys(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
                             const std::vector<std::string>& probe_keys, const TupleSetPtr& ts, cudaStream_t s);
 
+// Aggregate functions of a group-by spec: [{"function", "name", "expr"}],
+// functions SUM, COUNT (without expr: count of rows), MIN, MAX, AVG and
+// AVG_REDUCE (no expr; the second phase of a parallel AVG).
+std::vector<GroupAggregate> parse_aggregates(const json::Value& list);
+
 // Build an Execution from a JSON plan (format documented with
 // gfpdb_execute_plan in include/gfpdb.h).
 std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream);

@@ -52,6 +52,30 @@ __device__ __forceinline__ int64_t load_int(const DevCol& c, int64_t row) {
   return __ldg(static_cast<const int*>(c.data) + row);
 }
 
+// Hash of one row's key of n columns: integers by value (int32 and int64
+// columns with equal values agree), utf8 by bytes, each column's hash folded
+// in with a boost-style combine and a full mix. The composite join / bloom
+// keys and the shuffle's slot assignment both use it.
+constexpr uint64_t kRowKeySeed = 0x243f6a8885a308d3ull;
+__device__ __forceinline__ uint64_t row_key_combine(uint64_t h, uint64_t v) {
+  return mix64(h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2)));
+}
+__device__ __forceinline__ uint64_t row_key_hash(const DevCol* cols, int n, int64_t row) {
+  uint64_t h = kRowKeySeed;
+  for (int c = 0; c < n; ++c) {
+    const DevCol& col = cols[c];
+    uint64_t v;
+    if (col.type == CT_UTF8) {
+      const int32_t b = col.offsets[row], e = col.offsets[row + 1];
+      v = hash_bytes(static_cast<const uint8_t*>(col.data) + b, e - b);
+    } else {
+      v = hash_key(load_int(col, row));
+    }
+    h = row_key_combine(h, v);
+  }
+  return h;
+}
+
 __device__ __forceinline__ int64_t load_as_i64_bits(const DevCol& c, int64_t row) {
   if (c.type == CT_I64 || c.type == CT_F64) return __ldg(static_cast<const long long*>(c.data) + row);
   return __ldg(static_cast<const int*>(c.data) + row);

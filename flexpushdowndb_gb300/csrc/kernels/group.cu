@@ -757,7 +757,29 @@ class GroupTable {
         accs.push_back(d);
         return static_cast<int32_t>(accs.size() - 1);
       };
-      if (a.fn == AGG_COUNT_STAR || (a.fn == AGG_COUNT && !a.expr)) {
+      if (a.fn == AGG_AVG_REDUCE) {
+        // AvgReduce (fpdb-executor/src/physical/aggregate/function/AvgReduce.cpp:21-84):
+        // the first phase's AVG_INTERMEDIATE_SUM_<name> and
+        // AVG_INTERMEDIATE_COUNT_<name> columns, each summed, divided at
+        // finalisation.
+        auto column = [](const std::string& n) {
+          auto e = std::make_shared<Expr>();
+          e->kind = Expr::Column;
+          e->name = n;
+          return ExprPtr(e);
+        };
+        DType sum_t, cnt_t;
+        Operand sum_in = compile_value(column(kAvgIntermediateSum + a.name), ts.fields(), prog, slots, &sum_t);
+        Operand cnt_in = compile_value(column(kAvgIntermediateCount + a.name), ts.fields(), prog, slots, &cnt_t);
+        if (cnt_t == DType::Float64 || cnt_t == DType::Utf8 || sum_t == DType::Utf8)
+          fail(GFPDB_EINVAL, "AVG_REDUCE '" + a.name + "' needs a numeric sum and an integer count column");
+        o.kind = 1;
+        o.vt = sum_t == DType::Float64 ? VT_F64 : VT_I64;
+        o.a0 = add_acc(AGG_SUM, o.vt, sum_in);
+        o.a1 = add_acc(AGG_SUM, VT_I64, cnt_in);
+        o.out_type = static_cast<int8_t>(DType::Float64);
+        out_types.push_back(DType::Float64);
+      } else if (a.fn == AGG_COUNT_STAR || (a.fn == AGG_COUNT && !a.expr)) {
         Operand none{};
         none.kind = OPND_LIT;
         o.kind = 0;

@@ -33,22 +33,8 @@ __global__ void __launch_bounds__(256) key_hash_kernel(const __grid_constant__ K
   int64_t n = p.n;
   if (p.n_dev != nullptr && *p.n_dev < n) n = *p.n_dev;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
-    uint64_t h = 0x243f6a8885a308d3ull;
-    for (int c = 0; c < p.n_cols; ++c) {
-      const DevCol& col = p.cols[c];
-      uint64_t v;
-      if (col.type == CT_UTF8) {
-        const int32_t b = col.offsets[row], e = col.offsets[row + 1];
-        v = hash_bytes(static_cast<const uint8_t*>(col.data) + b, e - b);
-      } else {
-        v = hash_key(load_int(col, row));
-      }
-      // boost-style combine, then a full mix per column
-      h = mix64(h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2)));
-    }
-    p.out[row] = static_cast<int64_t>(h);
-  }
+  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride)
+    p.out[row] = static_cast<int64_t>(row_key_hash(p.cols, p.n_cols, row));
 }
 
 }  // namespace

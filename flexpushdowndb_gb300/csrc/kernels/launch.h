@@ -150,6 +150,12 @@ std::vector<ColumnPtr> join_chain_materialize(const std::vector<const JoinTable*
 
 // ------------------------------------------------------------- group.cu
 
+// Column-name prefixes of a parallel AVG's intermediate sum and count
+// (AggregatePrePFunction::AVG_INTERMEDIATE_*_COLUMN_PREFIX,
+// fpdb-plan/include/fpdb/plan/prephysical/AggregatePrePFunction.h:25-26).
+constexpr const char* kAvgIntermediateSum = "AVG_INTERMEDIATE_SUM_";
+constexpr const char* kAvgIntermediateCount = "AVG_INTERMEDIATE_COUNT_";
+
 struct GroupAggregate {
   AggFn fn;
   std::string name;
@@ -263,6 +269,21 @@ constexpr const char* kBuildKeyAlias = "__gfpdb_bk";
 TupleSetPtr with_composite_key(const TupleSetPtr& t, const std::vector<std::string>& keys, const std::string& name,
                                const std::string& alias_prefix, cudaStream_t s);
 bool is_internal_key_column(const std::string& name);
+
+// ------------------------------------------------------------ shuffle.cu
+
+constexpr int64_t kShuffleMaxSlots = 1024;
+// The rows of a TupleSet in slot order (slot i = rows [offsets[i],
+// offsets[i+1])), input order kept within a slot; a row's slot is a hash of
+// its key columns. Synchronizes `s`.
+struct ShuffleResult {
+  TupleSetPtr rows;
+  std::vector<int64_t> offsets;  // num_slots + 1
+};
+ShuffleResult shuffle_rows(const TupleSetPtr& in, const std::vector<std::string>& keys, int64_t num_slots,
+                           cudaStream_t s);
+// Rows [at, at + len) of an exact TupleSet, sharing its buffers.
+TupleSetPtr slice_rows(const TupleSetPtr& ts, int64_t at, int64_t len);
 
 // ------------------------------------------------------------ project.cu
 

@@ -98,7 +98,10 @@ struct Program {
 };
 
 // Aggregate input: an operand evaluated per row (count(*) has kind OPND_LIT).
-enum AggFn : int8_t { AGG_SUM = 0, AGG_COUNT = 1, AGG_MIN = 2, AGG_MAX = 3, AGG_COUNT_STAR = 4, AGG_AVG = 5 };
+enum AggFn : int8_t {
+  AGG_SUM = 0, AGG_COUNT = 1, AGG_MIN = 2, AGG_MAX = 3, AGG_COUNT_STAR = 4, AGG_AVG = 5,
+  AGG_AVG_REDUCE = 6  // second phase of a parallel AVG: sum of partial sums / sum of partial counts
+};
 
 struct AggSpec {
   int8_t fn;  // AggFn

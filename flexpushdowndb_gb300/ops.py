@@ -118,6 +118,25 @@ class BloomFilter:
             self._h = ctypes.c_void_p()
 
 
+def shuffle(table, key_columns: str | Sequence[str], num_slots: int, stream=None) -> tuple[Table, list[int]]:
+    """Hash-partition the rows into num_slots slots (gfpdb_shuffle,
+    ShuffleKernel2::shuffle): the rows slot by slot, and the num_slots + 1
+    slot offsets."""
+    ex = _export(table)
+    keys = _key_list(key_columns)
+    offs = (ctypes.c_int64 * (num_slots + 1))()
+    s, a = new_output()
+    _abi.check(_abi.lib().gfpdb_shuffle(ex.schema_ptr, ex.array_ptr, _abi.cstr_array(keys), len(keys), num_slots,
+                                        ctypes.byref(s), ctypes.byref(a), offs, stream))
+    return import_result(s, a), list(offs)
+
+
+def shuffle_split(table, key_columns: str | Sequence[str], num_slots: int, stream=None) -> list[Table]:
+    """The same as one Table per slot (the reference's vector of TupleSets)."""
+    rows, offs = shuffle(table, key_columns, num_slots, stream)
+    return [rows.slice(offs[i], offs[i + 1]) for i in range(num_slots)]
+
+
 def select(table, predicate: Filter | None = None, blooms: Sequence[tuple[BloomFilter, str]] = (),
            project: Sequence[str] | None = None, stream=None) -> Table:
     """Fused predicate + bloom probes + compaction (gfpdb_select)."""

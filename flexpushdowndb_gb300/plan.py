@@ -93,6 +93,37 @@ class Plan:
         self.connect(producer, name)
         return name
 
+    def shuffle(self, name: str, producer: str, columns: Sequence[str], consumers: Sequence[str] = ()) -> str:
+        """ShufflePOp: rows hash-partitioned on `columns`, slot i to the i-th
+        consumer (consumers may also be connected later, in slot order)."""
+        self._add({"type": "ShufflePOp", "name": name, "shuffleColumnNames": list(columns)})
+        self.connect(producer, name)
+        for c in consumers:
+            self.connect(name, c)
+        return name
+
+    def group_two_phase(self, name: str, producers: Sequence[str], group_columns: Sequence[str],
+                        aggregates: Sequence[dict], parallel_degree: int) -> list[str]:
+        """The parallel group-by of PrePToPTransformer::transformGroupTwoPhase
+        (fpdb-executor/src/physical/transform/PrePToPTransformer.cpp:434-580):
+        a partial GroupPOp per producer, a ShufflePOp on the group columns
+        after each, and `parallel_degree` reduce GroupPOps fed by every
+        shuffle. AVG becomes an intermediate SUM and COUNT, reduced by
+        AVG_REDUCE; SUM and COUNT reduce by SUM, MIN and MAX by themselves
+        (PrePToPTransformerUtil.cpp:63-124). Returns the reduce ops' names,
+        each holding a disjoint set of groups."""
+        partial, reduce = partial_aggregates(aggregates), reduce_aggregates(aggregates)
+        reduces = [f"{name}-reduce-{i}" for i in range(parallel_degree)]
+        shuffles = []
+        for i, p in enumerate(producers):
+            g = self.group(f"{name}-{i}", p, group_columns, partial)
+            shuffles.append(self.shuffle(f"{name}-shuffle-{i}", g, group_columns))
+        for r in reduces:
+            self._add({"type": "GroupPOp", "name": r, "groupColumnNames": list(group_columns), "aggregates": reduce})
+            for sh in shuffles:
+                self.connect(sh, r)
+        return reduces
+
     def csv_scan(self, name: str, table: str, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
                  delimiter: str = ",", header: bool = False) -> str:
         """Parse the text held by input `table` (one utf8 value, see
@@ -130,6 +161,37 @@ class Plan:
 
     def to_json(self) -> str:
         return json.dumps({"ops": self.ops}, separators=(",", ":"))
+
+
+def partial_aggregates(aggregates: Sequence[dict]) -> list[dict]:
+    """The first phase of a parallel aggregate
+    (PrePToPTransformerUtil::transformAggFunction with a reduce op,
+    fpdb-executor/src/physical/transform/PrePToPTransformerUtil.cpp:63-96):
+    AVG becomes a SUM and a COUNT into its intermediate columns, the others
+    stay as they are."""
+    out = []
+    for a in aggregates:
+        if a["function"].upper() == "AVG":
+            out.append({"function": "SUM", "name": "AVG_INTERMEDIATE_SUM_" + a["name"], "expr": a["expr"]})
+            out.append({"function": "COUNT", "name": "AVG_INTERMEDIATE_COUNT_" + a["name"], "expr": a["expr"]})
+        else:
+            out.append(dict(a))
+    return out
+
+
+def reduce_aggregates(aggregates: Sequence[dict]) -> list[dict]:
+    """The second phase (PrePToPTransformerUtil::transformAggReduceFunction,
+    PrePToPTransformerUtil.cpp:98-124): SUM and COUNT reduce by SUM of the
+    partial column, MIN and MAX by themselves, AVG by AVG_REDUCE."""
+    out = []
+    for a in aggregates:
+        fn, name = a["function"].upper(), a["name"]
+        if fn == "AVG":
+            out.append({"function": "AVG_REDUCE", "name": name})
+        else:
+            out.append({"function": "SUM" if fn in ("SUM", "COUNT") else fn, "name": name,
+                        "expr": {"type": "Column", "columnName": name}})
+    return out
 
 
 def validate(plan: Plan | str) -> None:

@@ -109,6 +109,18 @@ class Table:
             n += c.values[0].nbytes + c.values[1].nbytes if c.type == "utf8" else c.values.nbytes
         return n
 
+    @staticmethod
+    def concat(tables: Sequence["Table"]) -> "Table":
+        """Row-wise concatenation of tables with the same columns."""
+        cols = []
+        for i, c in enumerate(tables[0].columns):
+            parts = [t.columns[i] for t in tables]
+            if c.type == "utf8":
+                cols.append(Column(c.name, c.type, sum((p.to_list() for p in parts), [])))
+            else:
+                cols.append(Column(c.name, c.type, np.concatenate([p.values for p in parts])))
+        return Table(cols)
+
     def slice(self, start: int, stop: int) -> "Table":
         out = []
         for c in self.columns:

@@ -205,6 +205,22 @@ int32_t gfpdb_bloom_info(const gfpdb_bloom* bloom, int64_t* num_blocks, int64_t*
 
 void gfpdb_bloom_free(gfpdb_bloom* bloom);
 
+/* ------------------------------------------------------------------ shuffle */
+
+/* Hash-partition the rows of a TupleSet into num_slots slots (1 to 1024) by
+ * n_keys key columns (1 to 8; integer, date32 or utf8): the output holds
+ * every input row once, slot by slot, input order kept within a slot; slot i
+ * is rows [slot_offsets[i], slot_offsets[i+1]) (num_slots + 1 entries
+ * written). Equal keys always share a slot; integer keys hash by value, so
+ * int32 and int64 columns of equal values agree.
+ * Replaces ShuffleKernel2::shuffle(columnNames, numSlots, tupleSet)
+ * (fpdb-executor/src/physical/shuffle/ShuffleKernel2.cpp:28-125), whose
+ * vector of per-slot TupleSets is the output sliced at slot_offsets. */
+int32_t gfpdb_shuffle(const struct ArrowSchema* in_schema, const struct ArrowDeviceArray* in,
+                      const char* const* key_columns, int32_t n_keys, int64_t num_slots,
+                      struct ArrowSchema* out_schema, struct ArrowDeviceArray* out, int64_t* slot_offsets,
+                      void* stream);
+
 /* ----------------------------------------------- fused scan (filter+bloom) */
 
 /* One fused pass over a TupleSet: an optional compiled predicate AND a chain

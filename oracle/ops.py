@@ -24,6 +24,13 @@ Each function follows the reference operator it names:
                   (fpdb-executor/src/physical/project/ProjectPOp.cpp:98-145):
                   the renamed pass-through columns, then one column per
                   expression.
+  shuffle       - ShuffleKernel2::shuffle
+                  (fpdb-executor/src/physical/shuffle/ShuffleKernel2.cpp:28-125):
+                  every row once, slot by slot, input order kept within a
+                  slot. The slot function is this project's (a mix of the
+                  rows' key hash, below); the reference's is Arrow's
+                  HashMultiColumn, and which slot a key lands in changes no
+                  query result.
   limit_sort    - LimitSortPOp::selectK
                   (fpdb-executor/src/physical/limitsort/LimitSortPOp.cpp:97-135,
                   arrow::compute::SelectKUnstable + Take): the first k rows in
@@ -85,6 +92,42 @@ def mix64(k: np.ndarray) -> np.ndarray:
 
 def hash_key(v: np.ndarray) -> np.ndarray:
     return mix64(np.asarray(v).astype(np.int64).view(np.uint64) ^ _U(0x9E3779B97F4A7C15))
+
+
+def hash_bytes(b: bytes) -> int:
+    """FNV-1a over the bytes, then the length folded in and mixed."""
+    h = 0xCBF29CE484222325
+    for x in b:
+        h = ((h ^ x) * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+    return int(mix64(np.array([h ^ len(b)], dtype=np.uint64))[0])
+
+
+def row_key_hash(table: Table, keys) -> np.ndarray:
+    """Per-row hash of a key of several columns (integers by value, utf8 by
+    bytes), each column folded in with a boost-style combine and a mix."""
+    h = np.full(table.num_rows, 0x243F6A8885A308D3, dtype=np.uint64)
+    for k in keys:
+        c = table.column(k)
+        if c.type == "utf8":
+            v = np.array([hash_bytes(s.encode()) for s in c.to_list()], dtype=np.uint64)
+        else:
+            v = hash_key(np.asarray(c.values))
+        with np.errstate(over="ignore"):
+            h = mix64(h ^ (v + _U(0x9E3779B97F4A7C15) + (h << _U(6)) + (h >> _U(2))))
+    return h
+
+
+def shuffle_slots(table: Table, keys, num_slots: int) -> np.ndarray:
+    g = mix64(row_key_hash(table, keys) ^ _U(0x5851F42D4C957F2D))
+    return (((g >> _U(32)) * _U(num_slots)) >> _U(32)).astype(np.int64)
+
+
+def shuffle(table: Table, keys, num_slots: int) -> tuple[Table, list[int]]:
+    """The rows slot by slot (stable), and the num_slots + 1 slot offsets."""
+    slot = shuffle_slots(table, keys, num_slots)
+    order = np.argsort(slot, kind="stable")
+    counts = np.bincount(slot, minlength=num_slots)
+    return take(table, order), [0] + np.cumsum(counts).tolist()
 
 
 def bloom_num_blocks(n_keys: int, bits_per_key: int) -> int:
@@ -181,7 +224,7 @@ def hash_join_keys(build: Table, probe: Table, build_keys, probe_keys, needed=No
 
 
 def group_by(table: Table, group_cols: list[str], aggregates: list[dict]) -> Table:
-    """aggregates: [{"function": SUM|COUNT|MIN|MAX|AVG, "name": .., "expr": ..}]"""
+    """aggregates: [{"function": SUM|COUNT|MIN|MAX|AVG|AVG_REDUCE, "name": .., "expr": ..}]"""
     n = table.num_rows
     keys = [np.array(table[g], dtype=object) if table.column(g).type == "utf8" else table[g] for g in group_cols]
     if n == 0:
@@ -206,6 +249,17 @@ def group_by(table: Table, group_cols: list[str], aggregates: list[dict]) -> Tab
         cols.append(Column(name, c.type, vals if c.type == "utf8" else np.array(vals, dtype=np.int64)))
     for a in aggregates:
         fn = a["function"].upper()
+        if fn == "AVG_REDUCE":
+            # AvgReduce (fpdb-executor/src/physical/aggregate/function/AvgReduce.cpp:21-84)
+            sc, cc = table.column("AVG_INTERMEDIATE_SUM_" + a["name"]), table.column("AVG_INTERMEDIATE_COUNT_" + a["name"])
+            is_f = sc.type == "float64"
+            s = np.zeros(g, dtype=np.float64 if is_f else np.int64)
+            cnt = np.zeros(g, dtype=np.int64)
+            with np.errstate(over="ignore"):
+                np.add.at(s, inv, sc.values)
+                np.add.at(cnt, inv, cc.values)
+            cols.append(Column(a["name"], "float64", s.astype(np.float64) / np.maximum(cnt, 1)))
+            continue
         if fn == "COUNT":
             cnt = np.bincount(inv, minlength=g).astype(np.int64) if g else np.zeros(0, np.int64)
             cols.append(Column(a["name"], "int64", cnt))

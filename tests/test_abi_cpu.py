@@ -186,3 +186,58 @@ def test_oracle_limit_sort_is_stable():
     t = Table([Column("a", "int32", [3, 1, 3, 2, 1]), Column("i", "int32", [0, 1, 2, 3, 4])])
     assert oops.limit_sort(t, 3, [("a", "DESC")]).rows() == [(3, 0), (3, 2), (2, 3)]
     assert oops.limit_sort(t, 2, [("a", "ASC")]).rows() == [(1, 1), (1, 4)]
+
+
+def test_plan_validation_shuffle_and_two_phase():
+    from flexpushdowndb_gb300.expression import col
+
+    aggs = [ops.aggregate("SUM", "s", col("a")), ops.aggregate("AVG", "m", col("b")), ops.aggregate("COUNT", "c")]
+    p = plan.Plan()
+    scans = [p.scan(f"scan{i}", f"t{i}") for i in range(3)]
+    reduces = p.group_two_phase("g", scans, ["k"], aggs, 4)
+    p._add({"type": "CollatePOp", "name": "collate"})
+    for r in reduces:
+        p.connect(r, "collate")
+    plan.validate(p)
+    assert [a["function"] for a in plan.partial_aggregates(aggs)] == ["SUM", "SUM", "COUNT", "COUNT"]
+    assert [a["function"] for a in plan.reduce_aggregates(aggs)] == ["SUM", "AVG_REDUCE", "SUM"]
+    bad = [
+        ('{"ops": [{"type": "TableScanPOp", "name": "s", "table": "t", "consumers": ["sh"]},'
+         ' {"type": "ShufflePOp", "name": "sh", "shuffleColumnNames": ["k"]},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "consumers"),
+        ('{"ops": [{"type": "ShufflePOp", "name": "sh", "shuffleColumnNames": [], "consumers": ["c"]},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "1 to 8"),
+        ('{"ops": [{"type": "GroupPOp", "name": "g", "groupColumnNames": ["k"], "consumers": ["c"],'
+         ' "aggregates": [{"function": "AVG_REDUCE", "name": "m", "expr": {"type": "Column", "columnName": "x"}}]},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "AVG_REDUCE"),
+    ]
+    for text, fragment in bad:
+        with pytest.raises(_abi.GfpdbError) as ei:
+            plan.validate(text)
+        assert fragment in ei.value.message
+
+
+def test_shuffle_argument_checks_without_gpu():
+    """Slot counts and key counts are checked before any device work."""
+    L = _abi.lib()
+    t = export_host(small_table())
+    s, a = _abi.ArrowSchema(), _abi.ArrowDeviceArray()
+    offs = (ctypes.c_int64 * 8)()
+    for keys, slots in ((["a"], 0), (["a"], 1025), ([], 4)):
+        rc = L.gfpdb_shuffle(t.schema_ptr, t.array_ptr, _abi.cstr_array(keys or ["a"]), len(keys), slots,
+                             ctypes.byref(s), ctypes.byref(a), offs, None)
+        assert rc == _abi.GFPDB_EINVAL
+
+
+def test_oracle_shuffle_is_stable_and_complete():
+    from oracle import ops as oops
+
+    t = Table([Column("k", "int32", [5, 1, 5, 2, 1, 5, 9]), Column("i", "int32", list(range(7)))])
+    rows, offs = oops.shuffle(t, ["k"], 3)
+    assert offs[0] == 0 and offs[-1] == 7
+    assert sorted(rows["i"].tolist()) == list(range(7))
+    slots = oops.shuffle_slots(rows, ["k"], 3)
+    assert list(slots) == sorted(slots)
+    for s in range(3):
+        ids = rows["i"][offs[s]:offs[s + 1]].tolist()
+        assert ids == sorted(ids)

@@ -53,6 +53,65 @@ def _rank_main(rank, world, port, out_path):
     dist.destroy_process_group()
 
 
+def test_pack_table_roundtrip():
+    t = Table([Column("a", "int32", [1, -2, 3]), Column("s", "utf8", ["", "xy", "zzz"]),
+               Column("f", "float64", [0.5, 1.5, -2.0]), Column("d", "date32", [1, 2, 3])])
+    u = distributed.unpack_table(distributed.pack_table(t))
+    assert u.names == t.names and u.rows() == t.rows()
+    assert [c.type for c in u.columns] == [c.type for c in t.columns]
+    assert distributed.unpack_table(distributed.pack_table(Table([Column("a", "int64", [])]))).num_rows == 0
+
+
+def _exchange_main(rank, world, port, out_path):
+    """Each rank: a partial group-by of its shard (oracle), the partitioned
+    exchange (oracle shuffle standing in for the device one), the reduce
+    (oracle group-by with the reduce functions)."""
+    import numpy as np
+    import torch.distributed as dist
+
+    from flexpushdowndb_gb300 import plan
+    from flexpushdowndb_gb300.expression import col
+    from oracle import ops as oops
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    n = 60_000
+    keys = workloads.zipf_keys(n, 20_000, seed=77)
+    vals = np.random.default_rng(77).integers(-(2**40), 2**40, n)
+    whole = Table([Column("k", "int64", keys), Column("v", "int64", vals)])
+    aggs = [{"function": "SUM", "name": "s", "expr": col("v")}, {"function": "COUNT", "name": "c"},
+            {"function": "MIN", "name": "lo", "expr": col("v")}, {"function": "AVG", "name": "avg", "expr": col("v")}]
+    mine = Table([Column("k", "int64", keys[rank::world]), Column("v", "int64", vals[rank::world])])
+    partial = oops.group_by(mine, ["k"], plan.partial_aggregates(aggs))
+
+    def shuffle(t, ks, slots):
+        rows, offs = oops.shuffle(t, ks, slots)
+        return [rows.slice(offs[i], offs[i + 1]) for i in range(slots)]
+
+    def reduce(parts, ks, raggs):
+        return oops.group_by(Table.concat(parts), ks, raggs)
+
+    share = distributed.exchange_and_reduce(partial, ["k"], aggs, shuffle=shuffle, reduce=reduce)
+    shares = [None] * world
+    dist.all_gather_object(shares, share.rows())
+    if rank == 0:
+        want = oops.group_by(whole, ["k"], aggs).sorted_rows()
+        got = sorted(sum(shares, []))
+        key_sets = [set(r[0] for r in s) for s in shares]
+        disjoint = all(not (key_sets[i] & key_sets[j]) for i in range(world) for j in range(i + 1, world))
+        with open(out_path, "w") as f:
+            f.write("ok" if got == want and disjoint and all(shares) else "mismatch")
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_partitioned_exchange(tmp_path):
+    torch_mp = pytest.importorskip("torch.multiprocessing")
+    out = tmp_path / "result.txt"
+    torch_mp.spawn(_exchange_main, args=(2, _free_port(), str(out)), nprocs=2, join=True)
+    assert out.read_text() == "ok"
+
+
 def test_two_gloo_ranks_merge_star_partials(tmp_path):
     torch_mp = pytest.importorskip("torch.multiprocessing")
     out = tmp_path / "result.txt"
