@@ -203,6 +203,44 @@ def _pct(xs, q):
     return s[min(len(s) - 1, int(q / 100 * len(s)))]
 
 
+def merge_section(result, dist, barrier, max_over_ranks) -> dict:
+    """Multi-rank: every rank's batch result (its partitions' groups of the
+    32 queries) merged across ranks by the partitioned exchange (device
+    shuffle on (query_id, d2_g, d4_g), one all-to-all, device group-by of
+    the received partial sums), timed with a barrier on both sides; parity:
+    the union of the ranks' shares equals rank 0's host merge of every
+    rank's partial table."""
+    import numpy as np
+
+    from flexpushdowndb_gb300 import distributed
+    from flexpushdowndb_gb300.tupleset import Column, Table
+
+    # a copy: the prepared batch's page-locked result is rewritten by its next run
+    partial = Table([Column(c.name, c.type, c.values if c.type == "utf8" else np.array(c.values))
+                     for c in result.columns])
+    keys = ["query_id", "d2_g", "d4_g"]
+    sums = ["revenue", "discount_revenue", "cnt"]
+    aggs = [{"function": "SUM", "name": n, "expr": {"type": "Column", "columnName": n}} for n in sums]
+    distributed.exchange_and_reduce(partial, keys, aggs)  # warm-up
+    barrier()
+    t0 = time.perf_counter()
+    share = distributed.exchange_and_reduce(partial, keys, aggs)
+    barrier()
+    ms = max_over_ranks(1e3 * (time.perf_counter() - t0))
+    shares = [None] * dist.get_world_size()
+    dist.all_gather_object(shares, share.rows())
+    host = distributed.gather_and_merge(partial, keys, sums)
+    ok = True
+    if dist.get_rank() == 0:
+        ok = sorted(sum(shares, [])) == host.sorted_rows()
+    flag = [ok]
+    dist.broadcast_object_list(flag, src=0)
+    return {"ms": ms, "groups": sum(len(s) for s in shares), "parity": bool(flag[0]),
+            "path": "device shuffle of each rank's partial groups into one slot per rank, all_to_all_single of "
+                    "the slots (NCCL), device group-by of the received partial sums; each rank keeps a disjoint "
+                    "share of the groups"}
+
+
 def star_plan_section(args, L, stream, sptr, world, rank, barrier, max_over_ranks) -> dict:
     """The single star query with bloom predicate transfer (6,000,000 fact
     rows, forward + backward blooms of 10 bits/key and 3 hashes, four hash
@@ -930,6 +968,10 @@ def main():
         launches = (ops.kernel_launches() - launches0) / args.steps
         parity = parity and check(r.table)
         got = batch.split_by_query(r.table)
+        merge = None
+        if dist is not None:
+            merge = merge_section(r.table, dist, barrier, max_over_ranks)
+            parity = parity and merge["parity"]
         # one batch at a time (per-step latency)
         step_ms = []
         for _ in range(args.steps):
@@ -1072,6 +1114,7 @@ def main():
                         "fact columns (read for some rows only) in place over NVLink-C2C, and reads its result",
                 "h2d_bytes": "copied bytes + one 32-byte sector per row and column read in place (an upper bound)"},
         "gpu_launches": launches,
+        "merge": merge,
         "roofline": roofline,
         "kernels": {n: {"launches_per_step": v["launches"] / 3, "us_per_step": 1e3 * v["ms"] / 3}
                     for n, v in kern.items()},

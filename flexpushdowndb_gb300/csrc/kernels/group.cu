@@ -8,8 +8,13 @@
 // Keys: up to two key columns packed into one 64-bit word (32 bits per int32 /
 // date32 column, 64 bits for one int64 column); a utf8 key column is first
 // mapped to dense int32 codes by a device string dictionary that persists
-// across batches. The all-ones word marks an empty slot, so the one key that
-// packs to all-ones gets a dedicated extra slot at index `capacity`.
+// across batches. Wider keys (three to eight columns, or two whose widths add
+// up to more than 64 bits) are written as fixed-width records of their
+// values (utf8 columns by their codes) and mapped to dense int32 codes by the
+// same dictionary over the records, and the table groups by that code; the
+// key columns are recovered from the records at finalisation. The all-ones
+// word marks an empty slot, so the one key that packs to all-ones gets a
+// dedicated extra slot at index `capacity`.
 //
 // Aggregation: each CTA first folds its rows into a shared-memory table
 // (64-bit atomicCAS on keys, 64-bit atomics on accumulators) and merges the
@@ -450,12 +455,15 @@ __device__ __forceinline__ uint64_t dict_hash(const uint8_t* s, int32_t n) {
   return h == kEmptySlot ? kEmptySlot - 1 : h;
 }
 
+// Values are utf8 strings (offs, bytes) or, with offs null, fixed-width
+// records of `width` bytes each.
 __global__ void __launch_bounds__(256) dict_encode_kernel(const int32_t* __restrict__ offs, const uint8_t* __restrict__ bytes,
-                                                          int64_t n, int32_t* __restrict__ out_codes, DictDev d) {
+                                                          int32_t width, int64_t n, int32_t* __restrict__ out_codes,
+                                                          DictDev d) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
-    const int32_t b = offs[r];
-    const int32_t len = offs[r + 1] - b;
+    const int64_t b = offs != nullptr ? offs[r] : r * width;
+    const int32_t len = offs != nullptr ? offs[r + 1] - static_cast<int32_t>(b) : width;
     const uint8_t* str = bytes + b;
     const uint64_t h = dict_hash(str, len);
     uint64_t slot = h & d.mask;
@@ -530,6 +538,44 @@ __global__ void dict_lengths_kernel(const int32_t* codes, int64_t n, const int32
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride)
     lens[r] = code_len[codes[r]];
+}
+
+// Key records: each record's values written at fixed offsets (4-byte words;
+// an 8-byte value as two), and back into columns.
+struct RecordCols {
+  DevCol cols[kMaxKeyColumns];
+  int32_t off[kMaxKeyColumns];    // byte offset of the column in a record
+  int32_t width[kMaxKeyColumns];  // 4 or 8
+  int32_t n_cols;
+  int32_t rec_width;              // multiple of 4
+};
+
+__global__ void group_record_pack_kernel(const __grid_constant__ RecordCols rc, int64_t n, uint32_t* out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int words = rc.rec_width / 4;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    uint32_t* rec = out + r * words;
+    for (int k = 0; k < rc.n_cols; ++k) {
+      const int64_t v = load_int(rc.cols[k], r);
+      rec[rc.off[k] / 4] = static_cast<uint32_t>(v);
+      if (rc.width[k] == 8) rec[rc.off[k] / 4 + 1] = static_cast<uint32_t>(static_cast<uint64_t>(v) >> 32);
+    }
+  }
+}
+
+__global__ void group_record_split_kernel(const __grid_constant__ RecordCols rc, int64_t n, const int32_t* codes,
+                                          const int64_t* code_off, const uint8_t* heap, void* const* dst) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const uint32_t* rec = reinterpret_cast<const uint32_t*>(heap + code_off[codes[r]]);
+    for (int k = 0; k < rc.n_cols; ++k) {
+      const uint32_t lo = rec[rc.off[k] / 4];
+      if (rc.width[k] == 8)
+        static_cast<uint64_t*>(dst[k])[r] = (static_cast<uint64_t>(rec[rc.off[k] / 4 + 1]) << 32) | lo;
+      else
+        static_cast<uint32_t*>(dst[k])[r] = lo;
+    }
+  }
 }
 
 __global__ void dict_copy_kernel(const int32_t* codes, int64_t n, const int64_t* code_off, const uint8_t* heap,
@@ -680,12 +726,27 @@ class StringDict {
     ensure(n, ends[1] - ends[0], s);
     auto codes = make_buffer(n * 4, s);
     if (n > 0) {
-      dict_encode_kernel<<<grid_for(n), 256, 0, s>>>(c.offsets, static_cast<const uint8_t*>(c.data), n,
+      dict_encode_kernel<<<grid_for(n), 256, 0, s>>>(c.offsets, static_cast<const uint8_t*>(c.data), 0, n,
                                                      codes->as<int32_t>(), dev());
       after_launch("dict_encode_kernel");
     }
     codes_upper += n;
     heap_upper += ends[1] - ends[0];
+    return codes;
+  }
+
+  // n records of `width` bytes each (4-byte aligned; the heap keeps every
+  // record at a multiple of its width, so records stay aligned).
+  BufferPtr encode_records(const void* records, int64_t n, int32_t width, cudaStream_t s) {
+    ensure(n, n * width, s);
+    auto codes = make_buffer(n * 4, s);
+    if (n > 0) {
+      dict_encode_kernel<<<grid_for(n), 256, 0, s>>>(nullptr, static_cast<const uint8_t*>(records), width, n,
+                                                     codes->as<int32_t>(), dev());
+      after_launch("dict_encode_kernel");
+    }
+    codes_upper += n;
+    heap_upper += n * width;
     return codes;
   }
 
@@ -727,13 +788,17 @@ class GroupTable {
   Program prog{};
   ColumnSlots slots;
   std::vector<std::unique_ptr<StringDict>> dicts;  // per key column (utf8 only)
+  bool wide = false;                        // keys as records, grouped by record code
+  RecordCols records{};
+  std::unique_ptr<StringDict> record_dict;
 
   BufferPtr keys, accbuf, status, fnvt;
   uint64_t cap = 0;
   int64_t groups_upper = 0;
 
   void compile(const TupleSet& ts) {
-    if (group_cols.size() > 2) fail(GFPDB_EUNSUPPORTED, "group-by over more than two key columns");
+    if (group_cols.size() > static_cast<size_t>(kMaxKeyColumns))
+      fail(GFPDB_EUNSUPPORTED, "group-by over more than 8 key columns");
     int bits = 0;
     for (auto& g : group_cols) {
       DType t = ts.field(ts.require_column(g)).type;
@@ -744,7 +809,17 @@ class GroupTable {
       bits += b;
       dicts.emplace_back(t == DType::Utf8 ? new StringDict() : nullptr);
     }
-    if (bits > 64) fail(GFPDB_EUNSUPPORTED, "group keys wider than 64 bits");
+    if (group_cols.size() > 2 || bits > 64) {
+      wide = true;
+      std::memset(&records, 0, sizeof(records));
+      records.n_cols = static_cast<int32_t>(group_cols.size());
+      for (size_t k = 0; k < group_cols.size(); ++k) {
+        records.off[k] = records.rec_width;
+        records.width[k] = key_types[k] == DType::Int64 ? 8 : 4;  // utf8 columns as their int32 codes
+        records.rec_width += records.width[k];
+      }
+      record_dict.reset(new StringDict());
+    }
     std::memset(&prog, 0, sizeof(prog));
     for (auto& a : aggs) {
       OutAggDev o{};
@@ -865,7 +940,7 @@ class GroupTable {
     const TupleSet* tsp = &batch;
     bool utf8_key = false;
     for (auto t : key_types) utf8_key |= t == DType::Utf8;
-    if (utf8_key && !batch.exact()) {
+    if ((utf8_key || wide) && !batch.exact()) {
       exact_holder = batch.resolve(s);
       tsp = exact_holder.get();
     }
@@ -882,7 +957,28 @@ class GroupTable {
     p.n_keys = static_cast<int32_t>(group_cols.size());
     p.n_acc = static_cast<int32_t>(accs.size());
     std::vector<BufferPtr> code_bufs;
-    if (n > 0) {
+    if (wide && n > 0) {
+      RecordCols rc = records;
+      for (int k = 0; k < rc.n_cols; ++k) {
+        const auto& c = ts.column(group_cols[k]);
+        if (c->type != key_types[k]) fail(GFPDB_EINVAL, "group key column changed type between batches");
+        if (c->type == DType::Utf8) {
+          auto codes = dicts[k]->encode(*c, s);
+          code_bufs.push_back(codes);
+          rc.cols[k] = DevCol{codes->data(), nullptr, CT_I32, 0};
+        } else {
+          rc.cols[k] = DevCol{c->data, nullptr, static_cast<int32_t>(c->type), 0};
+        }
+      }
+      auto recs = make_buffer(n * rc.rec_width, s);
+      group_record_pack_kernel<<<grid_for(n), 256, 0, s>>>(rc, n, recs->as<uint32_t>());
+      after_launch("group_record_pack_kernel");
+      auto codes = record_dict->encode_records(recs->data(), n, rc.rec_width, s);
+      code_bufs.push_back(codes);
+      p.n_keys = 1;
+      p.key_bits[0] = 32;
+      p.key_cols[0] = DevCol{codes->data(), nullptr, CT_I32, 0};
+    } else if (n > 0) {
       for (int k = 0; k < p.n_keys; ++k) {
         const auto& c = ts.column(group_cols[k]);
         if (c->type != key_types[k]) fail(GFPDB_EINVAL, "group key column changed type between batches");
@@ -956,6 +1052,7 @@ class GroupTable {
     after_launch("group_update_kernel");
     double w = 0;
     for (int k = 0; k < p.n_keys; ++k) w += p.key_bits[k] / 8;
+    if (wide) w += records.rec_width - 4;
     for (size_t i = 0; i < slots.types.size(); ++i) w += dtype_width(slots.types[i]);
     prof.stop(static_cast<double>(n) * w);
     if (p.n_dev) prof.set_bytes_model(p.n_dev, n, w, nullptr, 0, ts.rows_owner());
@@ -971,7 +1068,7 @@ class GroupTable {
       fields.push_back(Field{aggs[j].name, compiled ? out_types[j] : DType::Int64});
     if (!compiled || cap == 0) return TupleSet::make_empty(fields, s);
     (void)schema_src;
-    bool utf8_key = false;
+    bool utf8_key = wide;
     for (auto t : key_types) utf8_key |= t == DType::Utf8;
     // Deferred: outputs sized for every slot, the group count stays on the
     // device and the status block is checked at the end of the plan.
@@ -984,6 +1081,8 @@ class GroupTable {
       raise_device_status(h, "group-by");
       for (auto& d : dicts)
         if (d && d->status) raise_device_status(read_status(d->status->as<DevStatus>(), s), "string dictionary");
+      if (record_dict && record_dict->status)
+        raise_device_status(read_status(record_dict->status->as<DevStatus>(), s), "group key dictionary");
       n_groups = h.aux[0];
     }
     FinalParams fp;
@@ -995,7 +1094,15 @@ class GroupTable {
     fp.n_acc = static_cast<int32_t>(accs.size());
     fp.n_keys = static_cast<int32_t>(group_cols.size());
     std::vector<BufferPtr> key_out(group_cols.size());
-    for (size_t k = 0; k < group_cols.size(); ++k) {
+    BufferPtr record_codes;
+    if (wide) {  // the table's key is the record code
+      fp.n_keys = 1;
+      record_codes = make_buffer(n_groups * 4, s);
+      fp.key_dst[0] = record_codes->data();
+      fp.key_type[0] = CT_I32;
+      fp.key_bits[0] = 32;
+    }
+    for (size_t k = 0; k < group_cols.size() && !wide; ++k) {
       DType t = key_types[k] == DType::Utf8 ? DType::Int32 : key_types[k];
       key_out[k] = make_buffer(n_groups * dtype_width(t), s);
       fp.key_dst[k] = key_out[k]->data();
@@ -1019,6 +1126,22 @@ class GroupTable {
         group_finalize_kernel<1><<<grid_for(static_cast<int64_t>(cap + 1)), 256, 0, s>>>(fp);
       after_launch("group_finalize_kernel");
       prof.stop(static_cast<double>(cap + 1) * 8);
+    }
+    if (wide) {
+      std::vector<void*> dst(group_cols.size());
+      for (size_t k = 0; k < group_cols.size(); ++k) {
+        key_out[k] = make_buffer(n_groups * records.width[k], s);
+        dst[k] = key_out[k]->data();
+      }
+      auto dst_dev = make_buffer(static_cast<int64_t>(dst.size() * sizeof(void*)), s);
+      GF_CUDA(cudaMemcpyAsync(dst_dev->data(), dst.data(), dst.size() * sizeof(void*), cudaMemcpyHostToDevice, s));
+      if (n_groups > 0) {
+        group_record_split_kernel<<<grid_for(n_groups), 256, 0, s>>>(
+            records, n_groups, record_codes->as<int32_t>(), record_dict->code_off->as<int64_t>(),
+            record_dict->heap->as<uint8_t>(), dst_dev->as<void*>());
+        after_launch("group_record_split_kernel");
+      }
+      sync(s);  // dst (host vector) is read by the copy above
     }
     std::vector<ColumnPtr> cols;
     for (size_t k = 0; k < group_cols.size(); ++k) {
