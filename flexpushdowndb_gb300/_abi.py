@@ -157,6 +157,7 @@ SIGNATURES = {
     "gfpdb_hashjoin_finalize_build": (_I32, [_P, _P]),
     "gfpdb_hashjoin_probe": (_I32, [_P, _S, _A, _S, _A, _P]),
     "gfpdb_hashjoin_info": (_I32, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "gfpdb_hashjoin_finish": (_I32, [_P, _S, _S, _A, _P]),
     "gfpdb_hashjoin_free": (None, [_P]),
     "gfpdb_group_create": (_I32, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "gfpdb_group_update": (_I32, [_P, _S, _A, _P]),

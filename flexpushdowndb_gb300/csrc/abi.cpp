@@ -500,6 +500,9 @@ int32_t gfpdb_result_layout(const ArrowSchema* schema, const ArrowDeviceArray* a
       put(cs->name != nullptr ? cs->name : "");
       put(cs->format);
       const bool utf8 = std::strcmp(cs->format, "u") == 0;
+      if (ca->null_count != 0 && ca->buffers[0] != nullptr)
+        fail(GFPDB_EUNSUPPORTED, std::string("column '") + (cs->name ? cs->name : "") +
+                                     "' holds nulls; the layout carries values only");
       values[i] = ca->buffers[utf8 ? 2 : 1];
       offsets[i] = utf8 ? ca->buffers[1] : nullptr;
     }
@@ -705,7 +708,10 @@ int32_t gfpdb_hashjoin_create(int32_t join_type, const char* const* build_keys, 
   return guarded([&] {
     require(out != nullptr && build_keys != nullptr && probe_keys != nullptr, "null argument");
     if (n_keys < 1 || n_keys > kMaxKeyColumns) fail(GFPDB_EINVAL, "a join key has 1 to 8 columns");
-    if (join_type != GFPDB_JOIN_INNER) fail(GFPDB_EUNSUPPORTED, "only inner joins run on the GPU path");
+    if (join_type < GFPDB_JOIN_INNER || join_type > GFPDB_JOIN_RIGHT_SEMI)
+      fail(GFPDB_EINVAL, "join type " + std::to_string(join_type));
+    if (join_type != GFPDB_JOIN_INNER && n_keys != 1)
+      fail(GFPDB_EUNSUPPORTED, "outer and semi joins take one key column per side");
     auto j = std::make_unique<gfpdb_hashjoin>();
     j->join_type = join_type;
     j->build_keys = names_of(build_keys, n_keys);
@@ -734,7 +740,8 @@ int32_t gfpdb_hashjoin_finalize_build(gfpdb_hashjoin* join, void* stream) {
     if (join->built) return;
     if (join->build.empty()) fail(GFPDB_EINVAL, "no build-side input");
     cudaStream_t s = as_stream(stream);
-    join->table = pop::build_join_table(TupleSet::concatenate(join->build, s), join->build_keys, join->load_factor, s);
+    join->table = pop::build_join_table(TupleSet::concatenate(join->build, s), join->build_keys, join->load_factor, s,
+                                        pop::join_kind_marks(static_cast<pop::JoinKind>(join->join_type)));
     join->build.clear();
     join->built = true;
   });
@@ -747,6 +754,7 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const ArrowSchema* schema, co
     if (!join->built) fail(GFPDB_EINVAL, "probe before finalize_build");
     cudaStream_t s = as_stream(stream);
     auto ts = import_tupleset(schema, batch, s);
+    if (join->probe_fields.empty()) join->probe_fields = ts->fields();
     // output: the probe side's needed columns, then the build side's
     // (HashJoinArrowKernel.cpp:148-162); every column when none are named
     std::vector<std::string> proj;
@@ -758,7 +766,33 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const ArrowSchema* schema, co
     } else {
       proj = join->needed;
     }
-    TupleSetPtr r = resolved(pop::join_probe_keys("hash join", join->table, proj, join->probe_keys, ts, s), s);
+    const auto kind = static_cast<pop::JoinKind>(join->join_type);
+    TupleSetPtr r = pop::join_probe_kind("hash join", kind, join->table, proj, join->probe_keys, ts, s);
+    if (!r) {  // LEFT_SEMI: rows come from gfpdb_hashjoin_finish
+      std::vector<Field> none;
+      r = TupleSet::make_empty(none, s);
+    }
+    export_tupleset(resolved(r, s), out_schema, out, false, s);
+    sync(s);
+  });
+}
+
+int32_t gfpdb_hashjoin_finish(gfpdb_hashjoin* join, const ArrowSchema* probe_schema, ArrowSchema* out_schema,
+                              ArrowDeviceArray* out, void* stream) {
+  return guarded([&] {
+    require(join != nullptr && out != nullptr && out_schema != nullptr, "null argument");
+    if (!join->built) fail(GFPDB_EINVAL, "finish before finalize_build");
+    cudaStream_t s = as_stream(stream);
+    std::vector<Field> pf = join->probe_fields;
+    if (pf.empty() && probe_schema != nullptr) pf = import_schema(probe_schema);
+    std::vector<std::string> proj;
+    if (!join->all_columns) proj = join->needed;
+    const auto kind = static_cast<pop::JoinKind>(join->join_type);
+    TupleSetPtr r = pop::join_finish_kind("hash join", kind, join->table, pf, proj, s);
+    if (!r) {
+      std::vector<Field> none;
+      r = TupleSet::make_empty(none, s);
+    }
     export_tupleset(r, out_schema, out, false, s);
     sync(s);
   });
@@ -785,6 +819,7 @@ int32_t gfpdb_hashjoin_clear(gfpdb_hashjoin* join) {
     require(join != nullptr, "null argument");
     join->build.clear();
     join->table = JoinTable{};
+    join->probe_fields.clear();
     join->built = false;
   });
 }

@@ -23,6 +23,7 @@ struct gfpdb_hashjoin {
   double load_factor = 0.5;
   std::vector<gfpdb::TupleSetPtr> build;
   gfpdb::JoinTable table;
+  std::vector<gfpdb::Field> probe_fields;  // from the first probed batch
   bool built = false;
 };
 

@@ -356,11 +356,19 @@ TupleSetPtr probe_join(const std::string& join_name, const JoinTable& table, con
 // the composite of several (with the key columns aliased for the equality
 // check that probe_join_multi makes).
 JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::string>& keys, double load_factor,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool mark) {
   JoinTable t;
-  t.build = keys.size() == 1 ? build : with_composite_key(build, keys, kBuildKeyColumn, kBuildKeyAlias, s);
-  t.key_col = t.build->require_column(keys.size() == 1 ? keys[0] : std::string(kBuildKeyColumn));
+  // a utf8 key, like several key columns, is joined on its hash and checked
+  // on the key itself
+  t.composite = keys.size() > 1 || build->field(build->require_column(keys[0])).type == DType::Utf8;
+  t.build = t.composite ? with_composite_key(build, keys, kBuildKeyColumn, kBuildKeyAlias, s) : build;
+  t.key_col = t.build->require_column(t.composite ? std::string(kBuildKeyColumn) : keys[0]);
   join_build_table(t, load_factor, s);
+  if (mark) {
+    if (t.composite)
+      fail(GFPDB_EUNSUPPORTED, "outer and semi joins take one integer key column per side");
+    t.matched = make_filled((t.build->num_rows() > 0 ? t.build->num_rows() : 1) * 4, 0, s);
+  }
   return t;
 }
 
@@ -419,8 +427,118 @@ TupleSetPtr probe_join_multi(const std::string& join_name, const JoinTable& tabl
 
 TupleSetPtr join_probe_keys(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
                             const std::vector<std::string>& probe_keys, const TupleSetPtr& ts, cudaStream_t s) {
-  return probe_keys.size() == 1 ? probe_join(join_name, table, proj, probe_keys[0], ts, s)
-                                : probe_join_multi(join_name, table, proj, probe_keys, ts, s);
+  return !table.composite ? probe_join(join_name, table, proj, probe_keys[0], ts, s)
+                          : probe_join_multi(join_name, table, proj, probe_keys, ts, s);
+}
+
+JoinKind join_kind_from_name(const std::string& name) {
+  if (name == "INNER") return JoinKind::Inner;
+  if (name == "LEFT") return JoinKind::Left;
+  if (name == "RIGHT") return JoinKind::Right;
+  if (name == "FULL") return JoinKind::Full;
+  if (name == "LEFT_SEMI") return JoinKind::LeftSemi;
+  if (name == "RIGHT_SEMI") return JoinKind::RightSemi;
+  fail(GFPDB_EINVAL, "join type '" + name + "' (INNER, LEFT, RIGHT, FULL, LEFT_SEMI or RIGHT_SEMI)");
+}
+
+bool join_kind_marks(JoinKind k) { return k == JoinKind::Left || k == JoinKind::Full || k == JoinKind::LeftSemi; }
+
+namespace {
+
+bool wanted(const std::vector<std::string>& proj, const std::string& c) {
+  return proj.empty() || std::find(proj.begin(), proj.end(), c) != proj.end();
+}
+
+// The join's output columns of one side: (field, source column index).
+std::vector<std::pair<Field, int>> side_columns(const std::vector<Field>& fields, const std::vector<std::string>& proj) {
+  std::vector<std::pair<Field, int>> out;
+  for (size_t i = 0; i < fields.size(); ++i)
+    if (!is_internal_key_column(fields[i].name) && wanted(proj, fields[i].name))
+      out.emplace_back(fields[i], static_cast<int>(i));
+  return out;
+}
+
+// Gathers probe columns by pidx and build columns by bidx (either may be
+// null: that side left out), the build side's indexes possibly -1 (nulls).
+TupleSetPtr join_gather(const std::string& join_name, const TupleSet* probe, const BufferPtr& pidx,
+                        const TupleSet& build, const BufferPtr& bidx, bool build_nulls,
+                        const std::vector<std::string>& proj, int64_t n, cudaStream_t s) {
+  std::vector<Field> fields;
+  std::vector<GatherSpec> specs;
+  if (probe != nullptr)
+    for (auto& [f, i] : side_columns(probe->fields(), proj)) {
+      fields.push_back(f);
+      specs.push_back(GatherSpec{probe->column(i).get(), pidx->as<int32_t>(), false});
+    }
+  if (bidx)
+    for (auto& [f, i] : side_columns(build.fields(), proj)) {
+      for (auto& g : fields)
+        if (g.name == f.name)
+          fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + join_name + "': column '" + f.name + "' is on both sides");
+      fields.push_back(f);
+      specs.push_back(GatherSpec{build.column(i).get(), bidx->as<int32_t>(), build_nulls});
+    }
+  return TupleSet::make(std::move(fields), gather_columns(specs, n, s), n);
+}
+
+}  // namespace
+
+TupleSetPtr join_probe_kind(const std::string& join_name, JoinKind kind, const JoinTable& table,
+                            const std::vector<std::string>& proj, const std::vector<std::string>& probe_keys,
+                            const TupleSetPtr& in, cudaStream_t s) {
+  if (kind == JoinKind::Inner) return join_probe_keys(join_name, table, proj, probe_keys, in, s);
+  if (table.composite) fail(GFPDB_EUNSUPPORTED, "outer and semi joins take one integer key column per side");
+  TupleSetPtr ts = resolved(in, s);
+  const int pk = ts->require_column(probe_keys[0]);
+  int32_t* matched = table.matched ? table.matched->as<int32_t>() : nullptr;
+  BufferPtr pidx, bidx;
+  int64_t n = 0;
+  switch (kind) {
+    case JoinKind::Right:  // every probe row, unmatched ones with a null build side
+    case JoinKind::Full:
+      join_pairs_ordered(table, *ts, pk, true, matched, &pidx, &bidx, &n, s);
+      return join_gather(join_name, ts.get(), pidx, *table.build, bidx, true, proj, n, s);
+    case JoinKind::Left:  // the matches now, the unmatched build rows at the end
+      join_pairs_ordered(table, *ts, pk, false, matched, &pidx, &bidx, &n, s);
+      return join_gather(join_name, ts.get(), pidx, *table.build, bidx, false, proj, n, s);
+    case JoinKind::LeftSemi:  // build rows, emitted at the end
+      join_match(table, *ts, pk, nullptr, false, matched, s);
+      return nullptr;
+    case JoinKind::RightSemi: {  // each probe row with a match, once
+      auto counts = make_buffer((ts->num_rows() > 0 ? ts->num_rows() : 1) * 4, s);
+      join_match(table, *ts, pk, counts->as<int32_t>(), false, nullptr, s);
+      pidx = rows_where(counts->as<int32_t>(), ts->num_rows(), true, &n, s);
+      return join_gather(join_name, ts.get(), pidx, *table.build, nullptr, false, proj, n, s);
+    }
+    default:
+      break;
+  }
+  fail(GFPDB_EINVAL, "unknown join kind");
+}
+
+TupleSetPtr join_finish_kind(const std::string& join_name, JoinKind kind, const JoinTable& table,
+                             const std::vector<Field>& probe_fields, const std::vector<std::string>& proj,
+                             cudaStream_t s) {
+  if (!join_kind_marks(kind)) return nullptr;
+  const int64_t nb = table.build->num_rows();
+  int64_t n = 0;
+  BufferPtr rows = rows_where(table.matched->as<int32_t>(), nb, kind == JoinKind::LeftSemi, &n, s);
+  if (kind == JoinKind::LeftSemi)
+    return join_gather(join_name, nullptr, nullptr, *table.build, rows, false, proj, n, s);
+  // unmatched build rows, their probe columns null
+  TupleSetPtr b = join_gather(join_name, nullptr, nullptr, *table.build, rows, false, proj, n, s);
+  std::vector<Field> fields;
+  std::vector<ColumnPtr> cols;
+  for (auto& [f, i] : side_columns(probe_fields, proj)) {
+    (void)i;
+    fields.push_back(f);
+    cols.push_back(null_column(f.type, n, s));
+  }
+  for (int i = 0; i < b->num_columns(); ++i) {
+    fields.push_back(b->field(i));
+    cols.push_back(b->column(i));
+  }
+  return TupleSet::make(std::move(fields), std::move(cols), n);
 }
 
 namespace {
@@ -431,10 +549,11 @@ namespace {
 class HashJoinArrowPOp : public PhysicalOp {
  public:
   HashJoinArrowPOp(std::string name, std::vector<std::string> build_producers, std::vector<std::string> probe_producers,
-                   std::vector<std::string> build_keys, std::vector<std::string> probe_keys, double load_factor)
+                   std::vector<std::string> build_keys, std::vector<std::string> probe_keys, double load_factor,
+                   JoinKind kind = JoinKind::Inner)
       : PhysicalOp(std::move(name), "HashJoinArrowPOp"), build_producers_(std::move(build_producers)),
         probe_producers_(std::move(probe_producers)), build_keys_(std::move(build_keys)),
-        probe_keys_(std::move(probe_keys)), load_factor_(load_factor) {
+        probe_keys_(std::move(probe_keys)), load_factor_(load_factor), kind_(kind) {
     if (build_keys_.empty() || build_keys_.size() != probe_keys_.size())
       fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': as many probe keys as build keys, at least one");
   }
@@ -460,6 +579,11 @@ class HashJoinArrowPOp : public PhysicalOp {
       }
       if (is_producer_complete(*this)) {
         if (!built_) finalizeBuild();
+        // outer and semi joins: the build rows decided once every probe row is in
+        Message out;
+        out.type = MessageType::TUPLESET;
+        out.tuples = join_finish_kind(name_, kind_, table_, probe_fields_, projectColumnNames_, ctx()->stream());
+        if (out.tuples) ctx()->tell(out);
         ctx()->notifyComplete();
       }
     }
@@ -469,6 +593,7 @@ class HashJoinArrowPOp : public PhysicalOp {
     build_.clear();
     probe_buffer_.clear();
     table_ = JoinTable{};
+    built_ = false;
   }
 
  private:
@@ -479,24 +604,25 @@ class HashJoinArrowPOp : public PhysicalOp {
   void finalizeBuild() {
     if (build_.empty()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': no build-side input");
     table_ = build_join_table(TupleSet::concatenate(build_, ctx()->stream()), build_keys_, load_factor_,
-                              ctx()->stream());
+                              ctx()->stream(), join_kind_marks(kind_));
     build_.clear();
     built_ = true;
   }
 
   void probe(const TupleSetPtr& ts) {
+    if (probe_fields_.empty()) probe_fields_ = ts->fields();
     Message out;
     out.type = MessageType::TUPLESET;
-    out.tuples = probe_keys_.size() == 1
-                     ? probe_join(name_, table_, projectColumnNames_, probe_keys_[0], ts, ctx()->stream())
-                     : probe_join_multi(name_, table_, projectColumnNames_, probe_keys_, ts, ctx()->stream());
-    ctx()->tell(out);
+    out.tuples = join_probe_kind(name_, kind_, table_, projectColumnNames_, probe_keys_, ts, ctx()->stream());
+    if (out.tuples) ctx()->tell(out);
   }
 
   std::vector<std::string> build_producers_, probe_producers_;
   std::vector<std::string> build_keys_, probe_keys_;
   double load_factor_;
+  JoinKind kind_;
   std::vector<TupleSetPtr> build_, probe_buffer_;
+  std::vector<Field> probe_fields_;  // the probe side's schema (null columns of unmatched build rows)
   JoinTable table_;
   bool built_ = false;
 };
@@ -784,6 +910,12 @@ class ProjectPOp : public PhysicalOp {
         cols.push_back(in.column(ci));
       }
       if (!exprs_.empty()) {
+        for (const auto& name : spec_.slots.names) {
+          const int ci = in.column_index(name);
+          if (ci >= 0 && in.column(ci)->valid != nullptr)
+            fail(GFPDB_EUNSUPPORTED, "ProjectPOp '" + name_ + "': an expression over the nullable column '" + name +
+                                         "' (an outer join's output)");
+        }
         TupleSetPtr e = project_columns(spec_, in, ctx()->stream());
         for (int i = 0; i < e->num_columns(); ++i) {
           fields.push_back(e->field(i));
@@ -1160,6 +1292,16 @@ TupleSetPtr Execution::execute() {
     }
     if (msg.type == MessageType::COMPLETE) dst->directory().setComplete(msg.sender);
     try {
+      // Nullable columns (outer-join outputs) go only where they are passed
+      // through unchanged: the collate, and a projection's renamed columns
+      // (ProjectPOp checks its expressions); every other operator's kernels
+      // read values, not nulls, and refuse them.
+      if (msg.type == MessageType::TUPLESET && msg.tuples && has_nulls(*msg.tuples)) {
+        const std::string t = dst->getTypeString();
+        if (t != "CollatePOp" && t != "ProjectPOp")
+          fail(GFPDB_EUNSUPPORTED, t + " '" + dst->name() + "' does not take nullable columns (column '" +
+                                       first_nullable_column(*msg.tuples) + "', an outer join's output)");
+      }
       dst->onReceive(Envelope{msg});
     } catch (const Error& e) {
       code = e.code();
@@ -1231,16 +1373,17 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
       fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name + "': one creator per filter column");
     op = std::make_unique<BloomFilterUsePOp>(name, cols, creators);
   } else if (type == "HashJoinArrowPOp") {
-    std::string jt = o.get_str("joinType", "INNER");
-    if (jt != "INNER") fail(GFPDB_EUNSUPPORTED, "join type '" + jt + "' (only INNER runs on the GPU path)");
+    const JoinKind kind = join_kind_from_name(o.get_str("joinType", "INNER"));
     // one key column per side ("buildKey" / "probeKey") or lists of them
     // ("buildKeys" / "probeKeys", HashJoinPredicate.h:25-26)
     std::vector<std::string> bk = o.contains("buildKeys") ? o.str_list("buildKeys")
                                                           : std::vector<std::string>{o.at("buildKey").str()};
     std::vector<std::string> pk = o.contains("probeKeys") ? o.str_list("probeKeys")
                                                           : std::vector<std::string>{o.at("probeKey").str()};
+    if (kind != JoinKind::Inner && bk.size() != 1)
+      fail(GFPDB_EUNSUPPORTED, "HashJoinArrowPOp '" + name + "': outer and semi joins take one key column per side");
     op = std::make_unique<HashJoinArrowPOp>(name, o.str_list("buildProducers"), o.str_list("probeProducers"),
-                                            std::move(bk), std::move(pk), o.get_num("loadFactor", 0.5));
+                                            std::move(bk), std::move(pk), o.get_num("loadFactor", 0.5), kind);
   } else if (type == "HashJoinChainPOp") {
     std::vector<ChainJoinSpec> joins;
     for (auto& j : o.at("joins").array()) {

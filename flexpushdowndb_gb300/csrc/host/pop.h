@@ -222,10 +222,33 @@ class Execution {
 
 // Join tables and probes on one or several key columns (the C ABI's hash
 // join and HashJoinArrowPOp share them).
+// With `mark` the table keeps a matched flag per build row (outer and semi
+// joins).
 JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::string>& keys, double load_factor,
-                           cudaStream_t s);
+                           cudaStream_t s, bool mark = false);
 TupleSetPtr join_probe_keys(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
                             const std::vector<std::string>& probe_keys, const TupleSetPtr& ts, cudaStream_t s);
+
+// The reference's JoinType (fpdb-plan/include/fpdb/plan/prephysical/JoinType.h:13-20),
+// the values of GFPDB_JOIN_*. LEFT keeps every build row (HashJoinArrowKernel
+// hands Arrow the build side as its right input and asks for RIGHT_OUTER),
+// RIGHT every probe row; LEFT_SEMI emits the build rows with a match,
+// RIGHT_SEMI the probe rows with a match, each with that side's columns only
+// (HashJoinArrowKernel.cpp:164-195).
+enum class JoinKind { Inner = 0, Left = 1, Right = 2, Full = 3, LeftSemi = 4, RightSemi = 5 };
+JoinKind join_kind_from_name(const std::string& name);
+bool join_kind_marks(JoinKind k);  // the table keeps build-row matched flags
+// One probe batch's output rows (null for LEFT_SEMI, whose rows come at the
+// end); non-inner joins take one integer key column per side.
+TupleSetPtr join_probe_kind(const std::string& join_name, JoinKind kind, const JoinTable& table,
+                            const std::vector<std::string>& proj, const std::vector<std::string>& probe_keys,
+                            const TupleSetPtr& ts, cudaStream_t s);
+// The rows emitted once every probe batch is in: the unmatched build rows
+// with null probe columns (LEFT, FULL), the matched build rows (LEFT_SEMI);
+// null for the other kinds. probe_fields: the probe side's schema.
+TupleSetPtr join_finish_kind(const std::string& join_name, JoinKind kind, const JoinTable& table,
+                             const std::vector<Field>& probe_fields, const std::vector<std::string>& proj,
+                             cudaStream_t s);
 
 // Aggregate functions of a group-by spec: [{"function", "name", "expr"}],
 // functions SUM, COUNT (without expr: count of rows), MIN, MAX, AVG and

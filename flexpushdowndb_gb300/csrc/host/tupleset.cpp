@@ -73,6 +73,21 @@ ColumnPtr make_fixed_column(DType t, int64_t length, BufferPtr buf, const void* 
   return c;
 }
 
+ColumnPtr with_validity(const ColumnPtr& c, BufferPtr bits) {
+  auto v = std::make_shared<Column>(*c);
+  v->valid = bits ? bits->as<uint32_t>() : nullptr;
+  v->valid_buf = std::move(bits);
+  return v;
+}
+
+bool has_nulls(const TupleSet& ts) { return !first_nullable_column(ts).empty(); }
+
+std::string first_nullable_column(const TupleSet& ts) {
+  for (int i = 0; i < ts.num_columns(); ++i)
+    if (ts.column(i)->valid != nullptr) return ts.field(i).name;
+  return "";
+}
+
 ColumnPtr make_utf8_column(int64_t length, BufferPtr offsets, BufferPtr bytes) {
   auto c = std::make_shared<Column>();
   c->type = DType::Utf8;
@@ -214,6 +229,13 @@ TupleSetPtr TupleSet::concatenate(const std::vector<TupleSetPtr>& sets, cudaStre
       std::vector<const Column*> parts;
       for (auto& ts : sets) parts.push_back(ts->column(static_cast<int>(ci)).get());
       cols.push_back(concat_utf8(parts, s));
+    }
+    bool nullable = false;
+    for (auto& ts : sets) nullable |= ts->column(static_cast<int>(ci))->valid != nullptr;
+    if (nullable) {
+      std::vector<std::pair<const uint32_t*, int64_t>> parts;
+      for (auto& ts : sets) parts.emplace_back(ts->column(static_cast<int>(ci))->valid, ts->num_rows());
+      cols.back() = with_validity(cols.back(), validity_concat(parts, total, s));
     }
   }
   return make(fields, std::move(cols), total);
@@ -434,6 +456,13 @@ void export_tupleset(const TupleSetPtr& ts_in, ArrowSchema* so, ArrowDeviceArray
         ah->host_allocs.push_back(h);
         ah->child_buffers[i] = {nullptr, h};
       }
+      if (c->valid != nullptr) {
+        const int64_t vb = (n + 7) / 8;
+        void* hv = std::malloc(vb > 0 ? vb : 1);
+        memcpy_d2h(hv, c->valid, vb, s);
+        ah->host_allocs.push_back(hv);
+        ah->child_buffers[i][0] = hv;
+      }
     }
     sync(s);
     ah->ts.reset();
@@ -441,16 +470,16 @@ void export_tupleset(const TupleSetPtr& ts_in, ArrowSchema* so, ArrowDeviceArray
     for (int i = 0; i < nc; ++i) {
       const auto& c = ts->column(i);
       if (c->type == DType::Utf8)
-        ah->child_buffers[i] = {nullptr, c->offsets, c->data};
+        ah->child_buffers[i] = {c->valid, c->offsets, c->data};
       else
-        ah->child_buffers[i] = {nullptr, c->data};
+        ah->child_buffers[i] = {c->valid, c->data};
     }
   }
   for (int i = 0; i < nc; ++i) {
     ArrowArray& c = ah->child_structs[i];
     std::memset(&c, 0, sizeof(c));
     c.length = n;
-    c.null_count = 0;
+    c.null_count = ah->child_buffers[i][0] != nullptr ? -1 : 0;  // -1: not counted
     c.offset = 0;
     c.n_buffers = static_cast<int64_t>(ah->child_buffers[i].size());
     c.buffers = ah->child_buffers[i].data();

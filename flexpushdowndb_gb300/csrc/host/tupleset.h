@@ -33,6 +33,10 @@ struct Column {
   BufferPtr offsets_buf;   // utf8 only
   const void* data = nullptr;        // first value of this column
   const int32_t* offsets = nullptr;  // utf8: length + 1 offsets into `data`
+  // Validity (outer-join outputs only): bit i of the LSB-first words is 1
+  // when row i holds a value (Arrow's bitmap order); none means no nulls.
+  BufferPtr valid_buf;
+  const uint32_t* valid = nullptr;
 
   int64_t value_bytes() const;  // bytes of values (utf8: bytes spanned by offsets)
 };
@@ -101,6 +105,11 @@ inline TupleSetPtr resolved(const TupleSetPtr& ts, cudaStream_t s) { return ts->
 // Column factories.
 ColumnPtr make_fixed_column(DType t, int64_t length, BufferPtr buf, const void* data = nullptr);
 ColumnPtr make_utf8_column(int64_t length, BufferPtr offsets, BufferPtr bytes);
+// The same column with a validity bitmap ((length + 31) / 32 words).
+ColumnPtr with_validity(const ColumnPtr& c, BufferPtr bits);
+// Whether any column may hold nulls (has a validity bitmap).
+bool has_nulls(const TupleSet& ts);
+std::string first_nullable_column(const TupleSet& ts);  // "" when none
 
 // ---- Arrow C Data / Device Data Interface ----
 

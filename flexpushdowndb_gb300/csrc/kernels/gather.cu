@@ -31,13 +31,13 @@ __global__ void __launch_bounds__(256) gather_fixed_kernel(const __grid_constant
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     for (int c = 0; c < p.n_cols; ++c) {
-      const int32_t i = __ldg(p.idx[c] + r);
+      const int32_t i = __ldg(p.idx[c] + r);  // -1: a null (outer joins), stored as 0
       // streaming (evict-first) stores: the gathered rows should not push
       // the gathered-from columns out of the L2
       if (p.width[c] == 8) {
-        __stcs(static_cast<long long*>(p.dst[c]) + r, __ldg(static_cast<const long long*>(p.src[c]) + i));
+        __stcs(static_cast<long long*>(p.dst[c]) + r, i < 0 ? 0ll : __ldg(static_cast<const long long*>(p.src[c]) + i));
       } else {
-        __stcs(static_cast<int*>(p.dst[c]) + r, __ldg(static_cast<const int*>(p.src[c]) + i));
+        __stcs(static_cast<int*>(p.dst[c]) + r, i < 0 ? 0 : __ldg(static_cast<const int*>(p.src[c]) + i));
       }
     }
   }
@@ -48,7 +48,27 @@ __global__ void utf8_lengths_kernel(const int32_t* __restrict__ offs, const int3
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     const int32_t i = idx[r];
-    len[r] = offs[i + 1] - offs[i];
+    len[r] = i < 0 ? 0 : offs[i + 1] - offs[i];
+  }
+}
+
+__global__ void validity_from_index_kernel(const int32_t* __restrict__ idx, int64_t n, uint32_t* __restrict__ out) {
+  const int64_t words = (n + 31) / 32;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < words; w += stride) {
+    uint32_t bits = 0;
+    for (int k = 0; k < 32 && w * 32 + k < n; ++k) bits |= static_cast<uint32_t>(idx[w * 32 + k] >= 0) << k;
+    out[w] = bits;
+  }
+}
+
+// Rows [0, n) of `src` (null: all valid) to rows [at, at + n) of `out`
+// (zeroed beforehand; words shared with a neighbouring part take atomicOr).
+__global__ void validity_copy_kernel(const uint32_t* __restrict__ src, int64_t n, int64_t at, uint32_t* out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const bool v = src == nullptr || ((src[r >> 5] >> (r & 31)) & 1u);
+    if (v) atomicOr(out + ((at + r) >> 5), 1u << ((at + r) & 31));
   }
 }
 
@@ -58,6 +78,7 @@ __global__ void utf8_copy_kernel(const int32_t* __restrict__ src_offs, const uin
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     const int32_t i = idx[r];
+    if (i < 0) continue;
     const int32_t b = src_offs[i];
     const int32_t len = src_offs[i + 1] - b;
     const int32_t o = dst_offs[r];
@@ -348,7 +369,42 @@ std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int6
     }
     out[i] = make_utf8_column(n, offs, bytes);
   }
+  for (size_t i = 0; i < specs.size(); ++i)
+    if (specs[i].may_be_null) out[i] = with_validity(out[i], validity_from_index(specs[i].idx, n, s));
   return out;
+}
+
+BufferPtr validity_from_index(const int32_t* idx, int64_t n, cudaStream_t s) {
+  const int64_t words = (n + 31) / 32;
+  auto bits = make_buffer((words > 0 ? words : 1) * 4, s);
+  if (words > 0) {
+    validity_from_index_kernel<<<grid_for(words, 256), 256, 0, s>>>(idx, n, bits->as<uint32_t>());
+    after_launch("validity_from_index_kernel");
+  }
+  return bits;
+}
+
+BufferPtr validity_concat(const std::vector<std::pair<const uint32_t*, int64_t>>& parts, int64_t total,
+                          cudaStream_t s) {
+  const int64_t words = (total + 31) / 32;
+  auto bits = make_filled((words > 0 ? words : 1) * 4, 0, s);
+  int64_t at = 0;
+  for (const auto& p : parts) {
+    if (p.second > 0) {
+      validity_copy_kernel<<<grid_for(p.second, 256), 256, 0, s>>>(p.first, p.second, at, bits->as<uint32_t>());
+      after_launch("validity_copy_kernel");
+    }
+    at += p.second;
+  }
+  return bits;
+}
+
+ColumnPtr null_column(DType t, int64_t n, cudaStream_t s) {
+  auto bits = make_filled(((n + 31) / 32 > 0 ? (n + 31) / 32 : 1) * 4, 0, s);
+  if (t == DType::Utf8)
+    return with_validity(make_utf8_column(n, make_filled((n + 1) * 4, 0, s), make_buffer(0, s)), bits);
+  return with_validity(make_fixed_column(t, n, make_filled(n * dtype_width(t) > 0 ? n * dtype_width(t) : 8, 0, s)),
+                       bits);
 }
 
 ColumnPtr concat_utf8(const std::vector<const Column*>& parts, cudaStream_t s) {

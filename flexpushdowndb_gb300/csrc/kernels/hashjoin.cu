@@ -807,4 +807,161 @@ void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, 
   fail(GFPDB_EDEVICE, "hash join output size changed between passes");
 }
 
+// ------------------------------------------------------ outer and semi joins
+//
+// The non-inner join types of HashJoinArrowKernel
+// (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:164-195)
+// on the same table: one pass counts each probe row's matches (and can mark
+// the build rows it matched), a prefix sum places every probe row's output,
+// and a second pass writes the (probe row, build row) pairs in probe-row
+// order, a probe row without a match as (row, -1) when it is kept (a null
+// build side). Marked or unmarked build rows are then listed by rows_where.
+
+namespace {
+
+struct MatchParams {
+  DevCol pkey, bkey;
+  const uint64_t* slots;
+  uint64_t mask;
+  int32_t key32;
+  int32_t keep_unmatched;  // a probe row without a match still takes one output pair
+  int64_t n;
+  int32_t* counts;         // output pairs of each probe row, or null
+  int32_t* matched;        // 1 at each build row some probe row matched, or null
+  const int32_t* offs;     // emit: first output pair of each probe row
+  int32_t* out_p;
+  int32_t* out_b;
+};
+
+// Calls f(build row, j) for the j-th match of probe row r; returns the matches.
+template <class F>
+__device__ __forceinline__ int walk_matches(const MatchParams& p, int64_t r, F&& f) {
+  const int64_t k = load_int(p.pkey, r);
+  const uint64_t h = hash_key(k);
+  const uint32_t tag = p.key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
+  uint64_t slot = h & p.mask;
+  int m = 0;
+  for (uint64_t i = 0; i <= p.mask; ++i, slot = (slot + 1) & p.mask) {
+    const uint64_t s = __ldg(p.slots + slot);
+    if (s == kEmptySlot) break;
+    if (static_cast<uint32_t>(s >> 32) != tag) continue;
+    const uint32_t b = static_cast<uint32_t>(s);
+    if (!p.key32 && load_int(p.bkey, b) != k) continue;
+    f(b, m);
+    ++m;
+  }
+  return m;
+}
+
+__global__ void __launch_bounds__(256) join_match_kernel(const __grid_constant__ MatchParams p) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < p.n; r += stride) {
+    const int m = walk_matches(p, r, [&](uint32_t b, int) {
+      if (p.matched != nullptr) p.matched[b] = 1;
+    });
+    if (p.counts != nullptr) p.counts[r] = (p.keep_unmatched && m == 0) ? 1 : m;
+  }
+}
+
+__global__ void __launch_bounds__(256) join_pairs_ordered_kernel(const __grid_constant__ MatchParams p) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < p.n; r += stride) {
+    const int32_t o = p.offs[r];
+    const int m = walk_matches(p, r, [&](uint32_t b, int j) {
+      p.out_p[o + j] = static_cast<int32_t>(r);
+      p.out_b[o + j] = static_cast<int32_t>(b);
+    });
+    if (m == 0 && p.keep_unmatched) {
+      p.out_p[o] = static_cast<int32_t>(r);
+      p.out_b[o] = -1;
+    }
+  }
+}
+
+__global__ void flag_rows_kernel(const int32_t* __restrict__ v, int64_t n, int nonzero, int32_t* __restrict__ sel) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    sel[i] = (v[i] != 0) == (nonzero != 0) ? 1 : 0;
+}
+
+__global__ void flag_scatter_kernel(const int32_t* __restrict__ sel, const int32_t* __restrict__ pos, int64_t n,
+                                    int32_t* __restrict__ rows) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    if (sel[i]) rows[pos[i]] = static_cast<int32_t>(i);
+}
+
+MatchParams match_params(const JoinTable& t, const TupleSet& probe, int probe_key) {
+  const int64_t n = probe.num_rows();
+  if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join probe batch must have fewer than 2^31 rows");
+  const auto& pc = probe.column(probe_key);
+  if (pc->type == DType::Utf8 || pc->type == DType::Float64)
+    fail(GFPDB_EUNSUPPORTED, "hash join keys must be integer columns");
+  const bool key32 = t.key_type != DType::Int64 && pc->type != DType::Int64;
+  if (!key32 && t.key_type != DType::Int64) fail(GFPDB_EUNSUPPORTED, "int64 probe key against an int32 build key");
+  const auto& bk = t.build->column(t.key_col);
+  MatchParams p{};
+  p.pkey = DevCol{pc->data, nullptr, static_cast<int32_t>(pc->type), 0};
+  p.bkey = DevCol{bk->data, nullptr, static_cast<int32_t>(bk->type), 0};
+  p.slots = t.slots->as<uint64_t>();
+  p.mask = t.capacity - 1;
+  p.key32 = key32 ? 1 : 0;
+  p.n = n;
+  return p;
+}
+
+}  // namespace
+
+void join_match(const JoinTable& t, const TupleSet& probe, int probe_key, int32_t* counts, bool keep_unmatched,
+                int32_t* matched, cudaStream_t s) {
+  MatchParams p = match_params(t, probe, probe_key);
+  p.counts = counts;
+  p.keep_unmatched = keep_unmatched ? 1 : 0;
+  p.matched = matched;
+  if (p.n == 0) return;
+  ProfScope prof("join_match_kernel", s);
+  join_match_kernel<<<grid_for(p.n), 256, 0, s>>>(p);
+  after_launch("join_match_kernel");
+  prof.stop(static_cast<double>(p.n) * (dtype_width(probe.column(probe_key)->type) + (counts ? 4 : 0)));
+}
+
+void join_pairs_ordered(const JoinTable& t, const TupleSet& probe, int probe_key, bool keep_unmatched,
+                        int32_t* matched, BufferPtr* pidx, BufferPtr* bidx, int64_t* n_out, cudaStream_t s) {
+  const int64_t n = probe.num_rows();
+  auto counts = make_buffer((n > 0 ? n : 1) * 4, s);
+  auto offs = make_buffer((n + 1) * 4, s);
+  join_match(t, probe, probe_key, counts->as<int32_t>(), keep_unmatched, matched, s);
+  const int64_t total = n > 0 ? exclusive_scan_i32(counts->as<int32_t>(), offs->as<int32_t>(), n, s) : 0;
+  *pidx = make_buffer((total > 0 ? total : 1) * 4, s);
+  *bidx = make_buffer((total > 0 ? total : 1) * 4, s);
+  *n_out = total;
+  if (n == 0) return;
+  MatchParams p = match_params(t, probe, probe_key);
+  p.keep_unmatched = keep_unmatched ? 1 : 0;
+  p.offs = offs->as<int32_t>();
+  p.out_p = (*pidx)->as<int32_t>();
+  p.out_b = (*bidx)->as<int32_t>();
+  ProfScope prof("join_pairs_ordered_kernel", s);
+  join_pairs_ordered_kernel<<<grid_for(n), 256, 0, s>>>(p);
+  after_launch("join_pairs_ordered_kernel");
+  prof.stop(static_cast<double>(n) * (dtype_width(probe.column(probe_key)->type) + 4) + static_cast<double>(total) * 8);
+}
+
+BufferPtr rows_where(const int32_t* v, int64_t n, bool nonzero, int64_t* n_out, cudaStream_t s) {
+  *n_out = 0;
+  if (n == 0) return make_buffer(4, s);
+  auto sel = make_buffer(n * 4, s);
+  auto pos = make_buffer((n + 1) * 4, s);
+  flag_rows_kernel<<<grid_for(n), 256, 0, s>>>(v, n, nonzero ? 1 : 0, sel->as<int32_t>());
+  after_launch("flag_rows_kernel");
+  const int64_t total = exclusive_scan_i32(sel->as<int32_t>(), pos->as<int32_t>(), n, s);
+  auto rows = make_buffer((total > 0 ? total : 1) * 4, s);
+  if (total > 0) {
+    flag_scatter_kernel<<<grid_for(n), 256, 0, s>>>(sel->as<int32_t>(), pos->as<int32_t>(), n, rows->as<int32_t>());
+    after_launch("flag_scatter_kernel");
+  }
+  *n_out = total;
+  return rows;
+}
+
 }  // namespace gfpdb

@@ -20,8 +20,17 @@ ColumnPtr concat_utf8(const std::vector<const Column*>& parts, cudaStream_t s);
 // pass, a prefix sum and a byte copy.
 struct GatherSpec {
   const Column* src;
-  const int32_t* idx;  // row ids into src
+  const int32_t* idx;        // row ids into src
+  bool may_be_null = false;  // idx holds -1 for a null (the output gets a validity bitmap)
 };
+
+// Validity bitmaps ((n + 31) / 32 LSB-first words): bit i set when idx[i] >= 0;
+// the concatenation of parts (a null bitmap pointer: every row valid).
+BufferPtr validity_from_index(const int32_t* idx, int64_t n, cudaStream_t s);
+BufferPtr validity_concat(const std::vector<std::pair<const uint32_t*, int64_t>>& parts, int64_t total,
+                          cudaStream_t s);
+// A column of n nulls.
+ColumnPtr null_column(DType t, int64_t n, cudaStream_t s);
 // With n_dev, n is a capacity and the kernels read the true count from the
 // device (deferred sizes); utf8 columns need an exact n.
 std::vector<ColumnPtr> gather_columns(const std::vector<GatherSpec>& specs, int64_t n, cudaStream_t s,
@@ -111,6 +120,8 @@ struct JoinTable {
   int key_col = -1;
   DType key_type = DType::Int32;
   int64_t max_probe = 0;
+  bool composite = false;   // keyed on the composite of several key columns (or of a utf8 key)
+  BufferPtr matched;        // outer / semi joins: int32 per build row, 1 once a probe row matched it
 };
 
 void join_build_table(JoinTable& t, double load_factor, cudaStream_t s);
@@ -132,6 +143,19 @@ std::vector<ColumnPtr> join_probe_materialize(const JoinTable& t, const TupleSet
 void join_probe_pairs(const JoinTable& t, const TupleSet& probe, int probe_key, BufferPtr* probe_idx,
                       BufferPtr* build_idx, int64_t* n_out, cudaStream_t s, BufferPtr* count_owner = nullptr,
                       const int64_t** count_dev = nullptr);
+
+// Outer and semi joins (exact probe batches). join_match: per probe row its
+// output pairs into counts (matches, or 1 for an unmatched row when
+// keep_unmatched; counts may be null), and 1 into matched[build row] for
+// every build row matched (matched may be null).
+void join_match(const JoinTable& t, const TupleSet& probe, int probe_key, int32_t* counts, bool keep_unmatched,
+                int32_t* matched, cudaStream_t s);
+// The (probe row, build row) pairs in probe-row order; with keep_unmatched
+// a probe row without a match gives (row, -1).
+void join_pairs_ordered(const JoinTable& t, const TupleSet& probe, int probe_key, bool keep_unmatched,
+                        int32_t* matched, BufferPtr* pidx, BufferPtr* bidx, int64_t* n_out, cudaStream_t s);
+// Row ids i < n with v[i] != 0 (nonzero) or v[i] == 0, in order.
+BufferPtr rows_where(const int32_t* v, int64_t n, bool nonzero, int64_t* n_out, cudaStream_t s);
 
 // A chain of inner joins probed in one pass: level l probes tables[l] with a
 // key column taken from the input row (source 0) or from the build row that

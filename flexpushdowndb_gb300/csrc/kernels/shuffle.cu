@@ -381,6 +381,10 @@ TupleSetPtr slice_rows(const TupleSetPtr& ts, int64_t at, int64_t len) {
     const auto& c = ts->column(i);
     auto sl = std::make_shared<Column>(*c);
     sl->length = len;
+    if (c->valid != nullptr) {
+      if (at % 32 != 0) fail(GFPDB_EUNSUPPORTED, "a slice of a nullable column must start at a multiple of 32 rows");
+      sl->valid = c->valid + at / 32;
+    }
     if (c->type == DType::Utf8) sl->offsets = c->offsets + at;
     else sl->data = static_cast<const char*>(c->data) + at * dtype_width(c->type);
     cols.push_back(sl);

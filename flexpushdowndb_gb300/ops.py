@@ -151,20 +151,26 @@ def select(table, predicate: Filter | None = None, blooms: Sequence[tuple[BloomF
     return import_result(s, a)
 
 
+JOIN_TYPES = {"INNER": 0, "LEFT": 1, "RIGHT": 2, "FULL": 3, "LEFT_SEMI": 4, "RIGHT_SEMI": 5}
+
+
 class HashJoin:
-    """Inner hash join (HashJoinArrowKernel). Output: probe columns, then build columns."""
+    """Hash join (HashJoinArrowKernel). Output: probe columns, then build
+    columns (one side only for semi joins)."""
 
     def __init__(self, build_key: str | Sequence[str], probe_key: str | Sequence[str],
-                 needed: Sequence[str] | None = None, load_factor: float = 0.5):
+                 needed: Sequence[str] | None = None, load_factor: float = 0.5, join_type: str = "INNER"):
         """Keys: one column per side, or equally long lists (build_key[i]
-        matches probe_key[i])."""
+        matches probe_key[i]). join_type: the reference's JoinType (LEFT
+        keeps every build row, RIGHT every probe row; the rows the build side
+        decides come from finish())."""
         names, n = _names(needed)
         bk, pk = _key_list(build_key), _key_list(probe_key)
         if len(bk) != len(pk):
             raise ValueError("as many probe key columns as build key columns")
         self._h = ctypes.c_void_p()
-        _abi.check(_abi.lib().gfpdb_hashjoin_create(0, _abi.cstr_array(bk), _abi.cstr_array(pk), len(bk), names, n,
-                                                    load_factor, ctypes.byref(self._h)))
+        _abi.check(_abi.lib().gfpdb_hashjoin_create(JOIN_TYPES[join_type], _abi.cstr_array(bk), _abi.cstr_array(pk),
+                                                    len(bk), names, n, load_factor, ctypes.byref(self._h)))
 
     def put_build(self, table, stream=None) -> None:
         ex = _export(table)
@@ -178,6 +184,15 @@ class HashJoin:
         s, a = new_output()
         _abi.check(_abi.lib().gfpdb_hashjoin_probe(self._h, ex.schema_ptr, ex.array_ptr, ctypes.byref(s),
                                                    ctypes.byref(a), stream))
+        return import_result(s, a)
+
+    def finish(self, probe_schema_of=None, stream=None) -> Table:
+        """The rows the build side decides once every probe batch is in
+        (LEFT / FULL: unmatched build rows, LEFT_SEMI: matched ones)."""
+        ex = _export(probe_schema_of) if probe_schema_of is not None else None
+        s, a = new_output()
+        _abi.check(_abi.lib().gfpdb_hashjoin_finish(self._h, ex.schema_ptr if ex else None, ctypes.byref(s),
+                                                    ctypes.byref(a), stream))
         return import_result(s, a)
 
     def clear(self) -> None:

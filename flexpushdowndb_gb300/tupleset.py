@@ -45,6 +45,7 @@ class Column:
     name: str
     type: str
     values: Any  # np.ndarray (fixed width) or (offsets, bytes) for utf8
+    valid: Any = None  # None (no nulls) or a bool array, False at a null
 
     def __post_init__(self):
         if self.type not in FORMATS:
@@ -59,9 +60,10 @@ class Column:
         return len(self.values[0]) - 1 if self.type == "utf8" else len(self.values)
 
     def to_list(self) -> list:
-        if self.type == "utf8":
-            return utf8_decode(*self.values)
-        return self.values.tolist()
+        vals = utf8_decode(*self.values) if self.type == "utf8" else self.values.tolist()
+        if self.valid is not None:
+            vals = [v if ok else None for v, ok in zip(vals, self.valid.tolist())]
+        return vals
 
 
 class Table:
@@ -100,8 +102,9 @@ class Table:
         return list(zip(*cols)) if cols else []
 
     def sorted_rows(self) -> list[tuple]:
-        """Rows as a sorted multiset (join and group outputs have no order)."""
-        return sorted(self.rows())
+        """Rows as a sorted multiset (join and group outputs have no order);
+        nulls sort after values."""
+        return sorted(self.rows(), key=lambda r: tuple((v is None, 0 if v is None else v) for v in r))
 
     def nbytes(self) -> int:
         n = 0
@@ -130,6 +133,8 @@ class Table:
                 out.append(Column(c.name, c.type, ((o[start : stop + 1] - lo).astype(np.int32), d[lo:hi].copy())))
             else:
                 out.append(Column(c.name, c.type, c.values[start:stop]))
+            if c.valid is not None:
+                out[-1].valid = c.valid[start:stop]
         return Table(out)
 
 
@@ -342,6 +347,9 @@ def import_result(schema: _abi.ArrowSchema, darr: _abi.ArrowDeviceArray, release
         else:
             dt = NP_TYPES[ty]
             cols.append(Column(name, ty, fetch(ca.buffers[1], n * np.dtype(dt).itemsize, dt)))
+        if ca.buffers[0] and ca.null_count != 0:
+            bits = fetch(ca.buffers[0], (n + 7) // 8, np.uint8)
+            cols[-1].valid = np.unpackbits(bits, bitorder="little")[:n].astype(bool)
     if release:
         if darr.array.release:
             darr.array.release(ctypes.pointer(darr.array))

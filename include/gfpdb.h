@@ -47,6 +47,8 @@ extern "C" {
 #define GFPDB_JOIN_LEFT 1
 #define GFPDB_JOIN_RIGHT 2
 #define GFPDB_JOIN_FULL 3
+#define GFPDB_JOIN_LEFT_SEMI 4
+#define GFPDB_JOIN_RIGHT_SEMI 5
 
 typedef struct gfpdb_filter gfpdb_filter;
 typedef struct gfpdb_bloom gfpdb_bloom;
@@ -88,6 +90,8 @@ int32_t gfpdb_memcpy(void* dst, const void* src, int64_t n_bytes, int32_t kind, 
  * values buffer and, for utf8, its offsets buffer (NULL otherwise). Fails
  * with GFPDB_EINVAL when the TupleSet has more than max_columns columns or
  * the names do not fit names_capacity bytes. */
+/* (A column with a validity bitmap, an outer join's output, is refused
+ * with GFPDB_EUNSUPPORTED: the layout carries values only.) */
 int32_t gfpdb_result_layout(const struct ArrowSchema* schema, const struct ArrowDeviceArray* array,
                             int32_t max_columns, int64_t* n_rows, int32_t* n_columns, int32_t* device_type,
                             char* names, int64_t names_capacity, const void** values, const void** offsets);
@@ -241,6 +245,15 @@ int32_t gfpdb_select(const gfpdb_filter* filter, int32_t n_blooms, const gfpdb_b
  * rightColumnNames), fpdb-executor/include/fpdb/executor/physical/join/hashjoin/HashJoinPredicate.h:25-26;
  * several columns are joined on a composite of their hashes and the rows
  * whose key columns differ are then dropped, so the result is exact).
+ * join_type is the reference's JoinType (GFPDB_JOIN_*,
+ * fpdb-plan/include/fpdb/plan/prephysical/JoinType.h:13-20) with its
+ * HashJoinArrowKernel meaning (HashJoinArrowKernel.cpp:164-195): LEFT keeps
+ * every build row, RIGHT every probe row, FULL both (the missing side's
+ * columns null: a validity bitmap in buffers[0], null_count -1), LEFT_SEMI
+ * emits the build rows with a match (build columns only), RIGHT_SEMI the
+ * probe rows with a match (probe columns only). Non-inner joins take one
+ * integer key column per side; the rows decided by the build side (LEFT /
+ * FULL unmatched, LEFT_SEMI) come from gfpdb_hashjoin_finish.
  * Output columns are the probe side's needed columns followed by the build
  * side's, as HashJoinArrowKernel::makeOutputSchema orders them
  * (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:148-162).
@@ -267,6 +280,15 @@ int32_t gfpdb_hashjoin_probe(gfpdb_hashjoin* join, const struct ArrowSchema* sch
                              struct ArrowDeviceArray* out, void* stream);
 
 /* Build-table statistics: rows, slots, longest probe run seen while building. */
+/* Every probe batch is in: emit the rows the build side decides (the
+ * unmatched build rows with null probe columns for LEFT and FULL, the
+ * matched build rows for LEFT_SEMI; no rows for the other types), as
+ * HashJoinArrowKernel::finalizeInput on the probe side flushes Arrow's join
+ * (HashJoinArrowKernel.cpp:100-116). The probe columns' types come from the
+ * probed batches (probe_schema when none was probed; may be NULL). */
+int32_t gfpdb_hashjoin_finish(gfpdb_hashjoin* join, const struct ArrowSchema* probe_schema,
+                              struct ArrowSchema* out_schema, struct ArrowDeviceArray* out, void* stream);
+
 int32_t gfpdb_hashjoin_info(const gfpdb_hashjoin* join, int64_t* build_rows, int64_t* capacity,
                             int64_t* max_probe);
 

@@ -10,6 +10,9 @@ Each function follows the reference operator it names:
                   Carter-Wegman variant draws random hash functions, so only
                   "no false negatives" is shared with it; the bit array here is
                   the exact expected content of the device filter).
+  hash_join_typed - the INNER / LEFT / RIGHT / FULL / LEFT_SEMI / RIGHT_SEMI
+                  joins with the reference's sides (below), nulls as a
+                  validity mask.
   hash_join     - inner join, output probe columns then build columns
                   (HashJoinArrowKernel::makeOutputSchema,
                   fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:148-162),
@@ -196,6 +199,61 @@ def hash_join(build: Table, probe: Table, build_key: str, probe_key: str, needed
             else:
                 cols.append(Column(c.name, c.type, c.values[idx]))
     return Table(cols)
+
+
+def _take_nullable(t: Table, idx: np.ndarray, names) -> list[Column]:
+    """Columns of t at rows idx, a -1 giving a null."""
+    out = []
+    null = idx < 0
+    safe = np.where(null, 0, idx)
+    for c in t.columns:
+        if names is not None and c.name not in names:
+            continue
+        if c.type == "utf8":
+            vals = c.to_list()
+            col = Column(c.name, c.type, ["" if z else vals[i] for i, z in zip(safe.tolist(), null.tolist())])
+        else:
+            col = Column(c.name, c.type, np.where(null, 0, c.values[safe] if len(c.values) else 0))
+        if null.any():
+            col.valid = ~null
+        out.append(col)
+    return out
+
+
+def hash_join_typed(build: Table, probe: Table, build_key: str, probe_key: str, join_type: str,
+                    needed=None) -> Table:
+    """The six join types of HashJoinArrowKernel
+    (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowKernel.cpp:164-195,
+    JoinType.h:13-20; the build side is Arrow's right input): INNER; LEFT
+    keeps every build row (Arrow RIGHT_OUTER), RIGHT every probe row
+    (LEFT_OUTER), FULL both, the missing side null; LEFT_SEMI the build rows
+    with a match (build columns), RIGHT_SEMI the probe rows with a match
+    (probe columns). Row order is not part of the result."""
+    pi, bi = join_indices(build[build_key], probe[probe_key])
+    n_p, n_b = probe.num_rows, build.num_rows
+    if join_type == "RIGHT_SEMI":
+        rows = np.unique(pi)
+        return Table(_take_nullable(probe, rows, needed))
+    if join_type == "LEFT_SEMI":
+        rows = np.unique(bi)
+        return Table(_take_nullable(build, rows, needed))
+    pi, bi = list(pi), list(bi)
+    if join_type in ("RIGHT", "FULL"):
+        hit = np.zeros(n_p, dtype=bool)
+        hit[np.asarray(pi, dtype=np.int64)] = True
+        for r in np.nonzero(~hit)[0].tolist():
+            pi.append(r)
+            bi.append(-1)
+    if join_type in ("LEFT", "FULL"):
+        hit = np.zeros(n_b, dtype=bool)
+        hit[np.asarray([b for b in bi if b >= 0], dtype=np.int64)] = True
+        for r in np.nonzero(~hit)[0].tolist():
+            pi.append(-1)
+            bi.append(r)
+    elif join_type not in ("INNER", "RIGHT"):
+        raise ValueError(join_type)
+    pi, bi = np.asarray(pi, dtype=np.int64), np.asarray(bi, dtype=np.int64)
+    return Table(_take_nullable(probe, pi, needed) + _take_nullable(build, bi, needed))
 
 
 # ------------------------------------------------------------------- group

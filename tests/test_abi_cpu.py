@@ -52,8 +52,10 @@ def test_plan_validation_accepts_workload_plans():
          ' {"type": "CollatePOp", "name": "c"}]}', "Like"),
         ('{"ops": [{"type": "TableScanPOp", "name": "s", "table": "t", "consumers": ["nope"]},'
          ' {"type": "CollatePOp", "name": "c"}]}', "unknown"),
-        ('{"ops": [{"type": "HashJoinArrowPOp", "name": "j", "buildKey": "a", "probeKey": "b", "joinType": "FULL"},'
-         ' {"type": "CollatePOp", "name": "c"}]}', "FULL"),
+        ('{"ops": [{"type": "HashJoinArrowPOp", "name": "j", "buildKey": "a", "probeKey": "b", "joinType": "SIDEWAYS"},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "SIDEWAYS"),
+        ('{"ops": [{"type": "HashJoinArrowPOp", "name": "j", "buildKeys": ["a", "b"], "probeKeys": ["c", "d"],'
+         ' "joinType": "LEFT"}, {"type": "CollatePOp", "name": "c"}]}', "one key column"),
         ("{not json", "JSON"),
     ],
 )
@@ -104,10 +106,17 @@ def test_group_spec_errors():
     ops.Group(["a"], [ops.aggregate("SUM", "s", col("b")), ops.aggregate("COUNT", "c")])
 
 
-def test_hashjoin_rejects_outer_joins():
+def test_hashjoin_create_checks_types_and_keys():
     L = _abi.lib()
     h = ctypes.c_void_p()
-    rc = L.gfpdb_hashjoin_create(3, _abi.cstr_array(["a"]), _abi.cstr_array(["b"]), 1, None, -1, 0.5, ctypes.byref(h))
+    for jt in range(6):  # INNER .. RIGHT_SEMI
+        assert L.gfpdb_hashjoin_create(jt, _abi.cstr_array(["a"]), _abi.cstr_array(["b"]), 1, None, -1, 0.5,
+                                       ctypes.byref(h)) == 0
+        L.gfpdb_hashjoin_free(h)
+    rc = L.gfpdb_hashjoin_create(6, _abi.cstr_array(["a"]), _abi.cstr_array(["b"]), 1, None, -1, 0.5, ctypes.byref(h))
+    assert rc == _abi.GFPDB_EINVAL
+    two = _abi.cstr_array(["a", "b"])
+    rc = L.gfpdb_hashjoin_create(1, two, two, 2, None, -1, 0.5, ctypes.byref(h))  # outer joins: one key column
     assert rc == _abi.GFPDB_EUNSUPPORTED
     for n in (0, 9):  # a key has 1 to 8 columns
         keys = _abi.cstr_array(["a"] * max(n, 1))
@@ -178,6 +187,21 @@ def test_plan_validation_project_and_limit_sort():
         q.collate("collate", "top")
         with pytest.raises(Exception):
             plan.validate(q)
+
+
+def test_oracle_typed_joins():
+    from oracle import ops as oops
+
+    b = Table([Column("k", "int32", [1, 2, 2, 5]), Column("bv", "utf8", ["a", "b", "c", "d"])])
+    p = Table([Column("fk", "int32", [2, 3, 1, 2]), Column("pv", "int64", [10, 20, 30, 40])])
+    inner = [(1, 30, 1, "a"), (2, 10, 2, "b"), (2, 10, 2, "c"), (2, 40, 2, "b"), (2, 40, 2, "c")]
+    assert oops.hash_join_typed(b, p, "k", "fk", "INNER").sorted_rows() == inner
+    assert oops.hash_join_typed(b, p, "k", "fk", "LEFT").sorted_rows() == inner + [(None, None, 5, "d")]
+    assert oops.hash_join_typed(b, p, "k", "fk", "RIGHT").sorted_rows() == inner + [(3, 20, None, None)]
+    assert oops.hash_join_typed(b, p, "k", "fk", "FULL").sorted_rows() == inner + [(3, 20, None, None),
+                                                                                   (None, None, 5, "d")]
+    assert oops.hash_join_typed(b, p, "k", "fk", "LEFT_SEMI").sorted_rows() == [(1, "a"), (2, "b"), (2, "c")]
+    assert oops.hash_join_typed(b, p, "k", "fk", "RIGHT_SEMI").sorted_rows() == [(1, 30), (2, 10), (2, 40)]
 
 
 def test_oracle_limit_sort_is_stable():
