@@ -33,6 +33,8 @@ LeafOp negate(LeafOp op) {
     case LO_STR_NE: return LO_STR_EQ;
     case LO_STRCOL_EQ: return LO_STRCOL_NE;
     case LO_STRCOL_NE: return LO_STRCOL_EQ;
+    case LO_LIKE: return LO_NOT_LIKE;
+    case LO_NOT_LIKE: return LO_LIKE;
   }
   return op;
 }
@@ -165,8 +167,35 @@ ExprPtr parse_expr(const json::Value& v) {
       return e;
     }
   }
-  if (type == "If" || type == "Like" || type == "DateAdd" || type == "DateExtract" || type == "Substr")
-    fail(GFPDB_EUNSUPPORTED, "expression '" + type + "' is not implemented on the GPU path");
+  // DateIntervalType names (fpdb-expression-gandiva/src/DateIntervalType.cpp:11-33)
+  auto interval = [&](const std::string& s) {
+    if (s == "Day") return 0;
+    if (s == "Month") return 1;
+    if (s == "Year") return 2;
+    fail(GFPDB_EINVAL, "unsupported date interval type: '" + s + "'");
+  };
+  if (type == "DateExtract") {  // DateExtract.cpp:45-63: {"dateExpr", "intervalType"}
+    auto e = node(Expr::DateExtract);
+    e->kids.push_back(parse_expr(v.at("dateExpr")));
+    e->interval = interval(v.at("intervalType").str());
+    return e;
+  }
+  if (type == "DateAdd") {  // DateAdd.cpp: {"left", "right", "intervalType"}
+    auto e = binary(Expr::DateAdd);
+    e->interval = interval(v.at("intervalType").str());
+    return e;
+  }
+  if (type == "If") {  // If.cpp:49-88: {"ifExpr", "thenExpr", "elseExpr"}
+    auto e = node(Expr::If);
+    e->kids = {parse_expr(v.at("ifExpr")), parse_expr(v.at("thenExpr")), parse_expr(v.at("elseExpr"))};
+    return e;
+  }
+  if (type == "Like") return binary(Expr::Like);  // Like.cpp: {"left", "right"}
+  if (type == "Substr") {  // Substr.cpp:48-88: {"expr", "fromLit", "forLit"}
+    auto e = node(Expr::Substr);
+    e->kids = {parse_expr(v.at("expr")), parse_expr(v.at("fromLit")), parse_expr(v.at("forLit"))};
+    return e;
+  }
   fail(GFPDB_EINVAL, "unsupported expression type: '" + type + "'");
 }
 
@@ -212,6 +241,23 @@ std::string expr_to_string(const ExprPtr& e) {
       break;
     case Expr::Cast: os << "cast(" << expr_to_string(e->kids[0]) << " as " << dtype_name(e->type) << ")"; break;
     case Expr::In: os << "in(" << expr_to_string(e->kids[0]) << ", " << (e->in_values.size() + e->in_strs.size()) << " values)"; break;
+    case Expr::DateExtract:
+      os << "extract" << (e->interval == 0 ? "Day" : e->interval == 1 ? "Month" : "Year") << "("
+         << expr_to_string(e->kids[0]) << ")";
+      break;
+    case Expr::DateAdd:
+      os << "dateadd" << (e->interval == 0 ? "Day" : e->interval == 1 ? "Month" : "Year") << "("
+         << expr_to_string(e->kids[0]) << ", " << expr_to_string(e->kids[1]) << ")";
+      break;
+    case Expr::If:
+      os << "if(" << expr_to_string(e->kids[0]) << ", " << expr_to_string(e->kids[1]) << ", "
+         << expr_to_string(e->kids[2]) << ")";
+      break;
+    case Expr::Like: os << "(" << expr_to_string(e->kids[0]) << " like " << expr_to_string(e->kids[1]) << ")"; break;
+    case Expr::Substr:
+      os << "substr(" << expr_to_string(e->kids[0]) << ", " << expr_to_string(e->kids[1]) << ", "
+         << expr_to_string(e->kids[2]) << ")";
+      break;
   }
   return os.str();
 }
@@ -255,6 +301,26 @@ DType type_of(const ExprPtr& e, const std::vector<Field>& schema) {
       if (a == DType::Int64 || b == DType::Int64) return DType::Int64;
       return DType::Int32;  // int32 / date32 arithmetic stays 32-bit
     }
+    case Expr::DateExtract: {
+      const DType a = type_of(e->kids[0], schema);
+      if (a != DType::Date32 && a != DType::Int32 && a != DType::Int64)
+        fail(GFPDB_EINVAL, "DateExtract needs a date: " + expr_to_string(e));
+      return DType::Int64;  // extractDay / Month / Year return int64 (DateExtract.cpp:16-24)
+    }
+    case Expr::DateAdd: {
+      const DType a = type_of(e->kids[0], schema), b = type_of(e->kids[1], schema);
+      if ((a != DType::Date32 && a != DType::Int32 && a != DType::Int64) || !is_int_type(b))
+        fail(GFPDB_EINVAL, "DateAdd needs a date and an integer: " + expr_to_string(e));
+      return DType::Date32;
+    }
+    case Expr::If: {
+      const DType t = type_of(e->kids[1], schema), f = type_of(e->kids[2], schema);
+      if (t == DType::Utf8 || f == DType::Utf8) fail(GFPDB_EUNSUPPORTED, "If with utf8 branches");
+      if (t == DType::Float64 || f == DType::Float64) return DType::Float64;
+      if (t == f) return t;
+      return DType::Int64;
+    }
+    case Expr::Substr: return DType::Utf8;
     default: fail(GFPDB_EINVAL, "boolean expression used as a value: " + expr_to_string(e));
   }
 }
@@ -265,6 +331,8 @@ void emit(Program& p, Instr in) {
   if (p.n_instrs >= kMaxInstrs) fail(GFPDB_EUNSUPPORTED, "expression too long for one fused kernel");
   p.instrs[p.n_instrs++] = in;
 }
+
+void emit_bool(const ExprPtr& e, const std::vector<Field>& schema, Program& p, ColumnSlots& slots);
 
 // Emit postfix code computing e as type `want`.
 void emit_value(const ExprPtr& e, DType want, const std::vector<Field>& schema, Program& p, ColumnSlots& slots) {
@@ -324,6 +392,35 @@ void emit_value(const ExprPtr& e, DType want, const std::vector<Field>& schema, 
       }
       break;
     }
+    case Expr::DateExtract: {
+      emit_value(e->kids[0], DType::Int64, schema, p, slots);
+      Instr in{};
+      in.op = IO_EXTRACT;
+      in.vt = VT_I64;
+      in.imm.i = e->interval;
+      emit(p, in);
+      break;
+    }
+    case Expr::DateAdd: {
+      emit_value(e->kids[0], DType::Int64, schema, p, slots);
+      emit_value(e->kids[1], DType::Int64, schema, p, slots);
+      Instr in{};
+      in.op = IO_DATE_ADD;
+      in.vt = VT_I64;
+      in.imm.i = e->interval;
+      emit(p, in);
+      break;
+    }
+    case Expr::If: {
+      emit_bool(e->kids[0], schema, p, slots);
+      emit_value(e->kids[1], have, schema, p, slots);
+      emit_value(e->kids[2], have, schema, p, slots);
+      Instr in{};
+      in.op = IO_SELECT;
+      in.vt = vt_of(have);
+      emit(p, in);
+      break;
+    }
     default: fail(GFPDB_EINVAL, "not a value expression: " + expr_to_string(e));
   }
   // Promote to the requested type.
@@ -360,8 +457,12 @@ Operand operand_for(const ExprPtr& e, DType want, const std::vector<Field>& sche
   int depth = 0, max_depth = 0;
   for (int pc = o.prog_begin; pc < o.prog_begin + o.prog_len; ++pc) {
     const int op = p.instrs[pc].op;
-    if (op == IO_COL || op == IO_LIT) ++depth;
-    else if (op == IO_ADD || op == IO_SUB || op == IO_MUL || op == IO_DIV) --depth;
+    if (op == IO_COL || op == IO_LIT || op == IO_STR_TEST) ++depth;
+    else if (op == IO_ADD || op == IO_SUB || op == IO_MUL || op == IO_DIV || op == IO_DATE_ADD || op == IO_CMP ||
+             op == IO_AND || op == IO_OR)
+      --depth;
+    else if (op == IO_SELECT)
+      depth -= 2;
     if (depth < 1) fail(GFPDB_EINVAL, "internal: malformed arithmetic program");
     max_depth = std::max(max_depth, depth);
   }
@@ -391,22 +492,173 @@ Cnf cross(const Cnf& a, const Cnf& b) {
   return out;
 }
 
-Leaf string_leaf(const ExprPtr& colexpr, const std::string& s, bool eq, const std::vector<Field>& schema, Program& p,
-                 ColumnSlots& slots) {
-  if (colexpr->kind != Expr::Column) fail(GFPDB_EUNSUPPORTED, "string comparison needs a column operand");
-  Leaf l{};
-  l.op = eq ? LO_STR_EQ : LO_STR_NE;
-  l.lhs.kind = OPND_COL;
-  l.lhs.col = static_cast<int16_t>(slots.slot_for(colexpr->name, DType::Utf8));
-  // String literals live in the program's pool; Program::pad holds the
-  // number of pool bytes used so far.
+// String literals live in the program's pool; Program::pad holds the number
+// of pool bytes used so far. Returns the literal's first pool byte.
+int pool_add(Program& p, const std::string& s) {
   const int used = p.pad;
   if (used + static_cast<int>(s.size()) > kStrPool) fail(GFPDB_EUNSUPPORTED, "string literals exceed the pool");
   std::memcpy(p.strpool + used, s.data(), s.size());
-  l.str_begin = static_cast<int16_t>(used);
-  l.str_len = static_cast<int16_t>(s.size());
   p.pad = used + static_cast<int>(s.size());
+  return used;
+}
+
+// The string side of a string test: a utf8 column, or SUBSTRING of one with
+// integer literal bounds (Substr.cpp: substr(expr, fromLit, forLit)).
+struct StringSide {
+  int slot;
+  bool sub = false;
+  int from = 0, len = 0;
+};
+
+StringSide string_side(const ExprPtr& e, const std::vector<Field>& schema, ColumnSlots& slots) {
+  StringSide side{};
+  ExprPtr col = e;
+  if (e->kind == Expr::Substr) {
+    const ExprPtr& f = e->kids[1];
+    const ExprPtr& n = e->kids[2];
+    if (f->kind != Expr::Literal || n->kind != Expr::Literal || f->lit_null || n->lit_null || !is_int_type(f->type) ||
+        !is_int_type(n->type))
+      fail(GFPDB_EUNSUPPORTED, "Substr takes integer literal bounds: " + expr_to_string(e));
+    if (n->lit.i < 0) fail(GFPDB_EINVAL, "Substr length is negative: " + expr_to_string(e));
+    if (f->lit.i < -32768 || f->lit.i > 32767 || n->lit.i > 65535)
+      fail(GFPDB_EUNSUPPORTED, "Substr bounds out of range: " + expr_to_string(e));
+    side.sub = true;
+    side.from = static_cast<int>(f->lit.i);
+    side.len = static_cast<int>(n->lit.i);
+    col = e->kids[0];
+  }
+  if (col->kind != Expr::Column || field_type(schema, col->name) != DType::Utf8)
+    fail(GFPDB_EUNSUPPORTED, "string comparison needs a utf8 column operand: " + expr_to_string(e));
+  side.slot = slots.slot_for(col->name, DType::Utf8);
+  return side;
+}
+
+Leaf string_test_leaf(const ExprPtr& colexpr, const std::string& s, LeafOp op, const std::vector<Field>& schema,
+                      Program& p, ColumnSlots& slots) {
+  const StringSide side = string_side(colexpr, schema, slots);
+  Leaf l{};
+  l.op = op;
+  l.lhs.kind = OPND_COL;
+  l.lhs.col = static_cast<int16_t>(side.slot);
+  if (side.sub) {
+    l.rhs.col = 1;
+    l.rhs.prog_begin = static_cast<int16_t>(side.from);
+    l.rhs.prog_len = static_cast<int16_t>(side.len > 32767 ? 32767 : side.len);
+  }
+  l.str_begin = static_cast<int16_t>(pool_add(p, s));
+  l.str_len = static_cast<int16_t>(s.size());
   return l;
+}
+
+Leaf string_leaf(const ExprPtr& colexpr, const std::string& s, bool eq, const std::vector<Field>& schema, Program& p,
+                 ColumnSlots& slots) {
+  return string_test_leaf(colexpr, s, eq ? LO_STR_EQ : LO_STR_NE, schema, p, slots);
+}
+
+// Like(left, right) (Like.cpp): a utf8 column or substring against a
+// pattern literal.
+Leaf like_leaf(const ExprPtr& e, bool neg, const std::vector<Field>& schema, Program& p, ColumnSlots& slots) {
+  const ExprPtr& pat = e->kids[1];
+  if (pat->kind != Expr::StrLiteral || pat->lit_null) fail(GFPDB_EUNSUPPORTED, "Like needs a pattern literal");
+  return string_test_leaf(e->kids[0], pat->str, neg ? LO_NOT_LIKE : LO_LIKE, schema, p, slots);
+}
+
+void emit_string_test(const Leaf& l, Program& p) {
+  Instr in{};
+  in.op = IO_STR_TEST;
+  in.vt = VT_I64;
+  in.col = l.lhs.col;
+  in.imm.i = static_cast<int64_t>(static_cast<uint8_t>(l.op)) | (static_cast<int64_t>(l.str_begin) << 8) |
+             (static_cast<int64_t>(l.str_len) << 24) | (l.rhs.col == 1 ? (int64_t{1} << 40) : 0);
+  in.pad = static_cast<int32_t>((static_cast<uint32_t>(static_cast<uint16_t>(l.rhs.prog_begin)) << 16) |
+                                static_cast<uint16_t>(l.rhs.prog_len));
+  emit(p, in);
+}
+
+// Push 0 / 1 for a boolean expression (the condition of an If).
+void emit_bool(const ExprPtr& e, const std::vector<Field>& schema, Program& p, ColumnSlots& slots) {
+  auto lit = [&](int64_t v) {
+    Instr in{};
+    in.op = IO_LIT;
+    in.vt = VT_I64;
+    in.imm.i = v;
+    emit(p, in);
+  };
+  auto op0 = [&](InstrOp o) {
+    Instr in{};
+    in.op = o;
+    in.vt = VT_I64;
+    emit(p, in);
+  };
+  switch (e->kind) {
+    case Expr::And:
+    case Expr::Or:
+      for (size_t i = 0; i < e->kids.size(); ++i) {
+        emit_bool(e->kids[i], schema, p, slots);
+        if (i > 0) op0(e->kind == Expr::And ? IO_AND : IO_OR);
+      }
+      return;
+    case Expr::Not:
+      emit_bool(e->kids[0], schema, p, slots);
+      op0(IO_NOT);
+      return;
+    case Expr::Like:
+      emit_string_test(like_leaf(e, false, schema, p, slots), p);
+      return;
+    case Expr::Literal:
+      if (!e->is_bool) fail(GFPDB_EINVAL, "numeric literal used as a condition");
+      lit(e->lit.i != 0 ? 1 : 0);
+      return;
+    case Expr::IsNull: lit(0); return;
+    case Expr::In: {
+      const size_t n = e->type == DType::Utf8 ? e->in_strs.size() : e->in_values.size();
+      if (n == 0) {
+        lit(0);
+        return;
+      }
+      for (size_t i = 0; i < n; ++i) {
+        auto cmp = std::make_shared<Expr>();
+        cmp->kind = Expr::Compare;
+        cmp->cmp = LO_EQ;
+        auto v = std::make_shared<Expr>();
+        if (e->type == DType::Utf8) {
+          v->kind = Expr::StrLiteral;
+          v->str = e->in_strs[i];
+        } else {
+          v->kind = Expr::Literal;
+          v->type = e->type;
+          v->lit = e->in_values[i];
+        }
+        cmp->kids = {e->kids[0], v};
+        emit_bool(cmp, schema, p, slots);
+        if (i > 0) op0(IO_OR);
+      }
+      return;
+    }
+    case Expr::Compare: {
+      const ExprPtr& a = e->kids[0];
+      const ExprPtr& b = e->kids[1];
+      const DType ta = type_of(a, schema), tb = type_of(b, schema);
+      if (ta == DType::Utf8 || tb == DType::Utf8) {
+        if (e->cmp != LO_EQ && e->cmp != LO_NE) fail(GFPDB_EUNSUPPORTED, "only = and != compare strings");
+        const bool eq = e->cmp == LO_EQ;
+        if (b->kind == Expr::StrLiteral) emit_string_test(string_leaf(a, b->str, eq, schema, p, slots), p);
+        else if (a->kind == Expr::StrLiteral) emit_string_test(string_leaf(b, a->str, eq, schema, p, slots), p);
+        else fail(GFPDB_EUNSUPPORTED, "a string comparison in a condition needs a string literal operand");
+        return;
+      }
+      const DType ct = (ta == DType::Float64 || tb == DType::Float64) ? DType::Float64 : DType::Int64;
+      emit_value(a, ct, schema, p, slots);
+      emit_value(b, ct, schema, p, slots);
+      Instr in{};
+      in.op = IO_CMP;
+      in.vt = vt_of(ct);
+      in.imm.i = e->cmp;
+      emit(p, in);
+      return;
+    }
+    default: fail(GFPDB_EINVAL, "not a boolean expression: " + expr_to_string(e));
+  }
 }
 
 Leaf compare_leaf(const ExprPtr& e, LeafOp op, const std::vector<Field>& schema, Program& p, ColumnSlots& slots) {
@@ -417,6 +669,8 @@ Leaf compare_leaf(const ExprPtr& e, LeafOp op, const std::vector<Field>& schema,
     if (op != LO_EQ && op != LO_NE) fail(GFPDB_EUNSUPPORTED, "only = and != compare strings");
     if (a->kind == Expr::StrLiteral) return string_leaf(b, a->str, op == LO_EQ, schema, p, slots);
     if (b->kind == Expr::StrLiteral) return string_leaf(a, b->str, op == LO_EQ, schema, p, slots);
+    if (a->kind == Expr::Substr || b->kind == Expr::Substr)
+      fail(GFPDB_EUNSUPPORTED, "a substring compares with a string literal");
     if (a->kind == Expr::Column && b->kind == Expr::Column && ta == DType::Utf8 && tb == DType::Utf8) {
       Leaf l{};
       l.op = op == LO_EQ ? LO_STRCOL_EQ : LO_STRCOL_NE;
@@ -490,6 +744,7 @@ Cnf to_cnf(const ExprPtr& e, bool neg, const std::vector<Field>& schema, Program
       // Inputs carry no nulls (nullable inputs are rejected at import), so
       // IsNull is false for every row.
       return Cnf{Clause{const_leaf(neg)}};
+    case Expr::Like: return Cnf{Clause{like_leaf(e, neg, schema, p, slots)}};
     case Expr::Literal:
       if (!e->is_bool) fail(GFPDB_EINVAL, "numeric literal used as a predicate");
       return Cnf{Clause{const_leaf((e->lit.i != 0) != neg)}};
@@ -532,6 +787,17 @@ CompiledPredicate compile_predicate(const ExprPtr& e, const std::vector<Field>& 
   cp.prog.clause_begin[simp.size()] = static_cast<int16_t>(nl);
   cp.prog.n_leaves = nl;
   return cp;
+}
+
+bool utf8_source(const ExprPtr& e, const std::vector<Field>& schema, Utf8Source* out) {
+  if (type_of(e, schema) != DType::Utf8) return false;
+  ColumnSlots scratch;
+  const StringSide side = string_side(e, schema, scratch);
+  out->column = scratch.names.at(side.slot);
+  out->sub = side.sub;
+  out->from = side.from;
+  out->len = side.len;
+  return true;
 }
 
 Operand compile_value(const ExprPtr& e, const std::vector<Field>& schema, Program& prog, ColumnSlots& slots,

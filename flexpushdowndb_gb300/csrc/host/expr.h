@@ -31,7 +31,8 @@ struct Expr;
 using ExprPtr = std::shared_ptr<const Expr>;
 
 struct Expr {
-  enum Kind { Column, Literal, StrLiteral, And, Or, Not, Compare, Arith, Cast, In, IsNull };
+  enum Kind { Column, Literal, StrLiteral, And, Or, Not, Compare, Arith, Cast, In, IsNull,
+              DateExtract, DateAdd, If, Like, Substr };
   Kind kind = Literal;
   std::string name;                 // Column
   DType type = DType::Int64;        // Literal type / Cast target / In element type
@@ -42,6 +43,7 @@ struct Expr {
   LeafOp cmp = LO_EQ;               // Compare
   InstrOp arith = IO_ADD;           // Arith
   std::vector<ExprPtr> kids;
+  int interval = 0;                 // DateExtract / DateAdd: 0 Day, 1 Month, 2 Year
   std::vector<Scalar> in_values;    // In over numbers
   std::vector<std::string> in_strs; // In over strings
 };
@@ -69,6 +71,16 @@ CompiledPredicate compile_predicate(const ExprPtr& e, const std::vector<Field>& 
 
 // Lower a value expression to an operand (columns, literals, or a postfix
 // program appended to prog.instrs). Returns the operand and its result type.
+// A utf8-valued expression a projection produces: a utf8 column, or
+// SUBSTRING of one with integer literal bounds (Substr.cpp). Returns false
+// when `e` is not utf8-valued; fails when it is but has another form.
+struct Utf8Source {
+  std::string column;
+  bool sub = false;
+  int from = 0, len = 0;
+};
+bool utf8_source(const ExprPtr& e, const std::vector<Field>& schema, Utf8Source* out);
+
 Operand compile_value(const ExprPtr& e, const std::vector<Field>& schema, Program& prog, ColumnSlots& slots,
                       DType* result_type);
 

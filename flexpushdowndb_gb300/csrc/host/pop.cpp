@@ -894,7 +894,15 @@ class ProjectPOp : public PhysicalOp {
     if (m.type == MessageType::TUPLESET) {
       const TupleSet& in = *m.tuples;
       if (!compiled_ && !exprs_.empty()) {
+        // utf8-valued expressions (a column, a SUBSTRING of one) are cut by
+        // substring_column, the others evaluated by project_kernel
+        utf8_.assign(exprs_.size(), Utf8Source{});
+        is_utf8_.assign(exprs_.size(), false);
         for (size_t i = 0; i < exprs_.size(); ++i) {
+          if (utf8_source(exprs_[i], in.fields(), &utf8_[i])) {
+            is_utf8_[i] = true;
+            continue;
+          }
           DType t = DType::Int64;
           spec_.ops.push_back(compile_value(exprs_[i], in.fields(), spec_.prog, spec_.slots, &t));
           spec_.types.push_back(t);
@@ -916,10 +924,38 @@ class ProjectPOp : public PhysicalOp {
             fail(GFPDB_EUNSUPPORTED, "ProjectPOp '" + name_ + "': an expression over the nullable column '" + name +
                                          "' (an outer join's output)");
         }
-        TupleSetPtr e = project_columns(spec_, in, ctx()->stream());
-        for (int i = 0; i < e->num_columns(); ++i) {
-          fields.push_back(e->field(i));
-          cols.push_back(e->column(i));
+        bool any_utf8 = false;
+        for (size_t i = 0; i < exprs_.size(); ++i) {
+          if (!is_utf8_[i]) continue;
+          any_utf8 = true;
+          const int ci = in.require_column(utf8_[i].column);
+          if (in.column(ci)->valid != nullptr)
+            fail(GFPDB_EUNSUPPORTED, "ProjectPOp '" + name_ + "': an expression over the nullable column '" +
+                                         utf8_[i].column + "' (an outer join's output)");
+        }
+        // utf8 outputs are sized from the exact row count
+        TupleSetPtr exact = any_utf8 && !in.exact() ? in.resolve(ctx()->stream()) : nullptr;
+        const TupleSet& src = exact ? *exact : in;
+        TupleSetPtr e = spec_.ops.empty() ? nullptr : project_columns(spec_, src, ctx()->stream());
+        int fixed_at = 0;
+        for (size_t i = 0; i < exprs_.size(); ++i) {
+          if (is_utf8_[i]) {
+            const Utf8Source& u = utf8_[i];
+            fields.push_back(Field{expr_names_[i], DType::Utf8});
+            cols.push_back(substring_column(*src.column(u.column), src.num_rows(), u.sub, u.from, u.len,
+                                            ctx()->stream()));
+          } else {
+            fields.push_back(e->field(fixed_at));
+            cols.push_back(e->column(fixed_at));
+            ++fixed_at;
+          }
+        }
+        if (exact) {
+          Message out;
+          out.type = MessageType::TUPLESET;
+          out.tuples = TupleSet::make(std::move(fields), std::move(cols), exact->num_rows());
+          ctx()->tell(out);
+          return;
         }
       }
       Message out;
@@ -938,6 +974,8 @@ class ProjectPOp : public PhysicalOp {
   std::vector<std::string> expr_names_;
   std::vector<std::pair<std::string, std::string>> pairs_;
   ProjectSpec spec_;
+  std::vector<Utf8Source> utf8_;
+  std::vector<bool> is_utf8_;
   bool compiled_ = false;
 };
 

@@ -324,6 +324,8 @@ struct ProjectSpec {
 };
 // One new column per expression, rows as the input's (deferred sizes kept).
 TupleSetPtr project_columns(const ProjectSpec& spec, const TupleSet& in, cudaStream_t s);
+// A utf8 column's values, or SUBSTRING(value FROM from FOR len) of each (n exact).
+ColumnPtr substring_column(const Column& c, int64_t n, bool sub, int from, int len, cudaStream_t s);
 
 struct SortKeySpec {
   std::string column;

@@ -173,6 +173,53 @@ int grid_rows(int64_t n) {
 
 }  // namespace
 
+namespace {
+
+__global__ void substr_lengths_kernel(const int32_t* __restrict__ offs, int64_t n, int sub, int from, int len,
+                                      int32_t* __restrict__ out_len) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    int32_t b = offs[r], e = offs[r + 1];
+    if (sub) substring_range(&b, &e, from, len);
+    out_len[r] = e - b;
+  }
+}
+
+__global__ void substr_copy_kernel(const int32_t* __restrict__ offs, const uint8_t* __restrict__ bytes, int64_t n,
+                                   int sub, int from, int len, const int32_t* __restrict__ out_offs,
+                                   uint8_t* __restrict__ out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+    int32_t b = offs[r], e = offs[r + 1];
+    if (sub) substring_range(&b, &e, from, len);
+    const int32_t o = out_offs[r];
+    for (int32_t k = 0; k < e - b; ++k) out[o + k] = bytes[b + k];
+  }
+}
+
+}  // namespace
+
+ColumnPtr substring_column(const Column& c, int64_t n, bool sub, int from, int len, cudaStream_t s) {
+  if (c.type != DType::Utf8) fail(GFPDB_EINVAL, "substring of a column that is not utf8");
+  auto offs = make_buffer((n + 1) * 4, s);
+  int64_t total = 0;
+  if (n > 0) {
+    auto lens = make_buffer(n * 4, s);
+    substr_lengths_kernel<<<grid_rows(n), 256, 0, s>>>(c.offsets, n, sub ? 1 : 0, from, len, lens->as<int32_t>());
+    after_launch("substr_lengths_kernel");
+    total = exclusive_scan_i32(lens->as<int32_t>(), offs->as<int32_t>(), n, s);
+  } else {
+    GF_CUDA(cudaMemsetAsync(offs->data(), 0, 4, s));
+  }
+  auto bytes = make_buffer(total > 0 ? total : 1, s);
+  if (n > 0 && total > 0) {
+    substr_copy_kernel<<<grid_rows(n), 256, 0, s>>>(c.offsets, static_cast<const uint8_t*>(c.data), n, sub ? 1 : 0,
+                                                    from, len, offs->as<int32_t>(), bytes->as<uint8_t>());
+    after_launch("substr_copy_kernel");
+  }
+  return make_utf8_column(n, offs, bytes);
+}
+
 TupleSetPtr project_columns(const ProjectSpec& spec, const TupleSet& in, cudaStream_t s) {
   const int n_out = static_cast<int>(spec.ops.size());
   if (n_out > kMaxProjOut) fail(GFPDB_EUNSUPPORTED, "more than 16 projected expressions in one operator");

@@ -177,16 +177,14 @@ __device__ __forceinline__ uint32_t leaf8(const SelectParams& p, const Leaf& L, 
   if (need == 0) return 0;
   if (L.op == LO_TRUE) return need;
   if (L.op == LO_FALSE) return 0;
-  if (L.op == LO_STR_EQ || L.op == LO_STR_NE) {
+  if (L.op == LO_STR_EQ || L.op == LO_STR_NE || L.op == LO_LIKE || L.op == LO_NOT_LIKE) {
     const DevCol& c = p.cols[L.lhs.col];
-    const uint8_t* bytes = static_cast<const uint8_t*>(c.data);
     uint32_t r = 0;
     for (int k = 0; k < kSelItems; ++k) {
       if (!((need >> k) & 1u)) continue;
-      const int32_t b = c.offsets[row0 + k], e = c.offsets[row0 + k + 1];
-      bool eq = (e - b) == L.str_len;
-      for (int i = 0; eq && i < L.str_len; ++i) eq = bytes[b + i] == static_cast<uint8_t>(p.prog.strpool[L.str_begin + i]);
-      if (eq == (L.op == LO_STR_EQ)) r |= 1u << k;
+      if (string_test(L.op, c, row0 + k, p.prog.strpool + L.str_begin, L.str_len, L.rhs.col == 1, L.rhs.prog_begin,
+                      L.rhs.prog_len))
+        r |= 1u << k;
     }
     return r;
   }

@@ -53,8 +53,13 @@ enum LeafOp : int8_t {
   LO_LT = 0, LO_LE, LO_GT, LO_GE, LO_EQ, LO_NE,
   LO_TRUE, LO_FALSE,
   LO_STR_EQ, LO_STR_NE,     // utf8 column vs utf8 literal held in the string pool
-  LO_STRCOL_EQ, LO_STRCOL_NE  // utf8 column vs utf8 column (lhs.col, rhs.col)
+  LO_STRCOL_EQ, LO_STRCOL_NE, // utf8 column vs utf8 column (lhs.col, rhs.col)
+  LO_LIKE, LO_NOT_LIKE        // utf8 column matched against a LIKE pattern held in the string pool
 };
+// LO_STR_EQ / NE and LO_LIKE / NOT_LIKE may test a substring of the column
+// (SUBSTRING(col FROM f FOR n) = 'x'): then rhs.col is 1, rhs.prog_begin the
+// first position f (1-based, may be <= 0) and rhs.prog_len the length n; an
+// all-zero rhs tests the whole value.
 
 struct Leaf {
   int8_t op;      // LeafOp
@@ -73,7 +78,17 @@ enum InstrOp : int8_t {
   IO_NEG,
   IO_I2F,      // int64 -> double
   IO_F2I,      // double -> int64 (truncation, as castBIGINT)
-  IO_WRAP32    // keep the low 32 bits and sign-extend (int32 arithmetic results)
+  IO_WRAP32,   // keep the low 32 bits and sign-extend (int32 arithmetic results)
+  IO_EXTRACT,  // date32 days -> the day (imm 0), month (1) or year (2) of the date
+  IO_DATE_ADD, // pop n, pop days: days plus n days (imm 0), months (1) or years (2)
+  IO_CMP,      // pop b, pop a: 1 if a <op> b else 0 (imm = LeafOp LO_LT..LO_NE, vt = comparison type)
+  IO_AND, IO_OR,  // pop b, pop a: a and / or b (0 / 1)
+  IO_NOT,      // 1 - a
+  IO_SELECT,   // pop else, pop then, pop cond: cond ? then : else
+  IO_STR_TEST  // push 0 / 1: utf8 column `col` against the string pool (the leaf test of
+               // imm.i & 0xff = LeafOp LO_STR_EQ / NE / LIKE / NOT_LIKE, pool range
+               // (imm.i >> 8) & 0xffff, length (imm.i >> 24) & 0xffff; bit 40 of imm.i set:
+               // a substring, first position (int16) pad >> 16, length pad & 0xffff)
 };
 
 struct Instr {

@@ -104,5 +104,29 @@ def in_(e: Expr, values: list[Any], data_type: str = "int64") -> Expr:
     return {"type": "In", "expr": e, "values": list(values), "dataType": data_type}
 
 
+def date_extract(e: Expr, interval: str) -> Expr:
+    """DateExtract (interval "Day", "Month" or "Year"): an int64 value."""
+    return {"type": "DateExtract", "dateExpr": e, "intervalType": interval}
+
+
+def date_add(date: Expr, n: Expr, interval: str) -> Expr:
+    """DateAdd: date plus n days / months / years (a date32 value)."""
+    return {"type": "DateAdd", "left": date, "right": n, "intervalType": interval}
+
+
+def if_(cond: Expr, then: Expr, otherwise: Expr) -> Expr:
+    return {"type": "If", "ifExpr": cond, "thenExpr": then, "elseExpr": otherwise}
+
+
+def like(e: Expr, pattern: str) -> Expr:
+    """SQL LIKE (% any run, _ one character; no escape character)."""
+    return {"type": "Like", "left": e, "right": str_lit(pattern)}
+
+
+def substr(e: Expr, start: int, length: int) -> Expr:
+    """SUBSTRING(e FROM start FOR length), 1-based."""
+    return {"type": "Substr", "expr": e, "fromLit": num_lit(start, "int64"), "forLit": num_lit(length, "int64")}
+
+
 def to_json(e: Expr) -> str:
     return json.dumps(e, separators=(",", ":"))

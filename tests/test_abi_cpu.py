@@ -48,8 +48,8 @@ def test_plan_validation_accepts_workload_plans():
     [
         ('{"ops": []}', "CollatePOp"),
         ('{"ops": [{"type": "CollatePOp", "name": "c"}, {"type": "CollatePOp", "name": "c"}]}', "duplicate"),
-        ('{"ops": [{"type": "FilterPOp", "name": "f", "predicate": {"type": "Like"}, "consumers": ["c"]},'
-         ' {"type": "CollatePOp", "name": "c"}]}', "Like"),
+        ('{"ops": [{"type": "FilterPOp", "name": "f", "predicate": {"type": "Sqrt"}, "consumers": ["c"]},'
+         ' {"type": "CollatePOp", "name": "c"}]}', "Sqrt"),
         ('{"ops": [{"type": "TableScanPOp", "name": "s", "table": "t", "consumers": ["nope"]},'
          ' {"type": "CollatePOp", "name": "c"}]}', "unknown"),
         ('{"ops": [{"type": "HashJoinArrowPOp", "name": "j", "buildKey": "a", "probeKey": "b", "joinType": "SIDEWAYS"},'
@@ -77,6 +77,12 @@ def small_table():
         and_(gt(col("b"), num_lit(4, "int64")), not_(eq(col("s"), str_lit("y")))),
         or_(in_(col("a"), [1, 3]), lt(times(col("a"), col("b")), num_lit(10, "int64"))),
         gt(col("f"), num_lit(1.0, "float64")),
+        {"type": "Like", "left": col("s"), "right": str_lit("x%")},
+        eq({"type": "Substr", "expr": col("s"), "fromLit": num_lit(1, "int64"), "forLit": num_lit(2, "int64")},
+           str_lit("xy")),
+        gt({"type": "DateExtract", "dateExpr": col("a"), "intervalType": "Year"}, num_lit(1970, "int64")),
+        lt({"type": "If", "ifExpr": eq(col("s"), str_lit("x")), "thenExpr": col("a"), "elseExpr": col("b")},
+           num_lit(3, "int64")),
     ],
 )
 def test_filter_compiles_without_gpu(pred):
@@ -87,7 +93,9 @@ def test_filter_compiles_without_gpu(pred):
     "pred,fragment",
     [
         (lt(col("missing"), num_lit(2)), "missing"),
-        ({"type": "Like", "left": col("s"), "right": str_lit("%x")}, "Like"),
+        ({"type": "Like", "left": col("s"), "right": col("s")}, "pattern"),
+        ({"type": "Like", "left": col("a"), "right": str_lit("%x")}, "utf8"),
+        (eq({"type": "Substr", "expr": col("s"), "fromLit": col("a"), "forLit": num_lit(2)}, str_lit("x")), "literal"),
         (lt(col("s"), str_lit("x")), "strings"),
         (times(col("a"), col("b")), "boolean"),
     ],
