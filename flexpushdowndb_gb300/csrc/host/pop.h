@@ -255,6 +255,10 @@ TupleSetPtr join_finish_kind(const std::string& join_name, JoinKind kind, const 
 // AVG_REDUCE (no expr; the second phase of a parallel AVG).
 std::vector<GroupAggregate> parse_aggregates(const json::Value& list);
 
+// The bloom-filter operators of a join graph's predicate transfer, as JSON
+// (format documented with gfpdb_plan_predicate_transfer in include/gfpdb.h).
+std::string plan_predicate_transfer(const json::Value& spec);
+
 // Build an Execution from a JSON plan (format documented with
 // gfpdb_execute_plan in include/gfpdb.h).
 std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream);

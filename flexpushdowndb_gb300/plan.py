@@ -124,6 +124,35 @@ class Plan:
                 self.connect(sh, r)
         return reduces
 
+    def predicate_transfer(self, tables: dict[str, int | tuple[int, float]], joins: Sequence[dict],
+                           bits_per_key: int = 10, num_hashes: int = 3, prefix: str = "pt") -> dict[str, str]:
+        """Add the bloom-filter predicate transfer of a join graph
+        (gfpdb_plan_predicate_transfer, SmallToLargePredTransOrder):
+        `tables` maps the operator producing each base table to its row
+        count, or to (row count, selectivity of its local filters); `joins` are {"left", "right", "leftColumns", "rightColumns",
+        "joinType"} between those operators. Returns each table operator's
+        last operator, where its joins attach."""
+        def entry(k, v):
+            rows, sel = (v, 1.0) if not isinstance(v, tuple) else v
+            return {"op": k, "rowCount": int(rows), "selectivity": float(sel)}
+
+        spec = json.dumps({"tables": [entry(k, v) for k, v in tables.items()],
+                           "joins": list(joins), "bitsPerKey": bits_per_key, "numHashes": num_hashes,
+                           "namePrefix": prefix}).encode()
+        L = _abi.lib()
+        need = ctypes.c_int64()
+        L.gfpdb_plan_predicate_transfer(spec, None, 0, ctypes.byref(need))
+        if need.value <= 0:
+            _abi.check(L.gfpdb_plan_predicate_transfer(spec, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        _abi.check(L.gfpdb_plan_predicate_transfer(spec, buf, need.value, ctypes.byref(need)))
+        out = json.loads(buf.value.decode())
+        for op in out["ops"]:
+            self._add(op)
+        for producer, consumer in out["edges"]:
+            self.connect(producer, consumer)
+        return out["outputs"]
+
     def csv_scan(self, name: str, table: str, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
                  delimiter: str = ",", header: bool = False) -> str:
         """Parse the text held by input `table` (one utf8 value, see

@@ -171,6 +171,50 @@ def star_plan(consts=STAR_DEFAULT_CONSTS, bits_per_key: int = 10, num_hashes: in
     return p
 
 
+def star_plan_planned(consts=STAR_DEFAULT_CONSTS, fact_rows: int = 6_000_000, bits_per_key: int = 10,
+                      num_hashes: int = 3, ranges=None) -> Plan:
+    """The star query with its bloom predicate transfer derived from the join
+    graph by the planner (Plan.predicate_transfer, SmallToLargePredTransOrder)
+    rather than written out: each dimension's filtered scan and the fact scan
+    are the base tables (row counts, and the dimension filters' selectivity),
+    the four fact-to-dimension joins the graph; the joins and the group-by
+    then attach to each table's last operator."""
+    p = Plan()
+    tables = {}
+    for i in range(1, 5):
+        p.scan(f"scan_d{i}", f"d{i}", [f"d{i}_pk", f"d{i}_f", f"d{i}_g"])
+        keep = [f"d{i}_pk", f"d{i}_g"] if i in (2, 4) else [f"d{i}_pk"]
+        if ranges is not None:
+            lo, hi = ranges[i - 1]
+            pred = and_(gte(col(f"d{i}_f"), num_lit(int(lo), "int32")), lte(col(f"d{i}_f"), num_lit(int(hi), "int32")))
+            sel = (hi - lo + 1) / STAR_FILTER_VALUES[i - 1]
+        else:
+            pred = eq(col(f"d{i}_f"), num_lit(int(consts[i - 1]), "int32"))
+            sel = 1 / STAR_FILTER_VALUES[i - 1]
+        p.filter(f"filter_d{i}", f"scan_d{i}", pred, keep)
+        tables[f"filter_d{i}"] = (STAR_DIM_ROWS[i - 1], sel)
+    fact_cols = ["fk1", "fk2", "fk3", "fk4", "qty", "price_cents", "discount"]
+    p.scan("scan_fact", "fact", fact_cols)
+    tables["scan_fact"] = (fact_rows, 1.0)
+    joins = [{"left": "scan_fact", "right": f"filter_d{i}", "leftColumns": [f"fk{i}"], "rightColumns": [f"d{i}_pk"],
+              "joinType": "INNER"} for i in range(1, 5)]
+    out = p.predicate_transfer(tables, joins, bits_per_key, num_hashes)
+    tail = out["scan_fact"]
+    carried: list[str] = []
+    for i in range(1, 5):
+        fact_cols = [c for c in fact_cols if c != f"fk{i}"]
+        if i in (2, 4):
+            carried.append(f"d{i}_g")
+        tail = p.hash_join(f"join_d{i}", out[f"filter_d{i}"], tail, f"d{i}_pk", f"fk{i}", fact_cols + carried)
+    p.group("group", tail, ["d2_g", "d4_g"], [
+        aggregate("SUM", "revenue", times(col("price_cents"), col("qty"))),
+        aggregate("SUM", "discount_revenue", times(col("price_cents"), col("discount"))),
+        aggregate("COUNT", "cnt"),
+    ], groups_hint=256)
+    p.collate("collate", "group")
+    return p
+
+
 # -------------------------------------------------------------------- batched
 #
 # The batched form: the star query's fact table split into partitions of

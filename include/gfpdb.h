@@ -415,6 +415,21 @@ void gfpdb_prepared_free(gfpdb_prepared* plan);
 /* Parse and check a plan without running it (host only, no CUDA calls). */
 int32_t gfpdb_plan_validate(const char* plan_json);
 
+/* Plan the bloom-filter predicate transfer of a join graph (host only), as
+ * SmallToLargePredTransOrder::orderPredTrans does
+ * (fpdb-executor/src/physical/transform/pred-trans/SmallToLargePredTransOrder.cpp:14-214).
+ * spec_json: {"tables": [{"op": <operator producing the table>, "rowCount": n,
+ *                         "selectivity": fraction its local filters keep (optional, 1)}],
+ *             "joins": [{"left": op, "right": op, "leftColumns": [...], "rightColumns": [...],
+ *                        "joinType": "INNER" | "LEFT" | ...}],
+ *             "bitsPerKey": 10, "numHashes": 3, "namePrefix": "pt"}
+ * Writes {"ops": [BloomFilterCreatePOp / BloomFilterUsePOp operators],
+ * "edges": [[producer, consumer], ...], "outputs": {table op: its last
+ * operator}} (joins attach to the outputs) into out_json when capacity
+ * holds it; *needed is its size with the terminating zero. A join cycle is
+ * GFPDB_EINVAL. */
+int32_t gfpdb_plan_predicate_transfer(const char* spec_json, char* out_json, int64_t capacity, int64_t* needed);
+
 /* Plans run with "cudaGraph": true and batches run with use_graph are kept,
  * keyed by their text and input buffer addresses, so later calls replay them.
  * They reference the caller's input buffers: clear them before freeing those
