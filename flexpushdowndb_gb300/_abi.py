@@ -165,6 +165,8 @@ SIGNATURES = {
     "gfpdb_group_clear": (_I32, [_P]),
     "gfpdb_hashjoin_clear": (_I32, [_P]),
     "gfpdb_group_free": (None, [_P]),
+    "gfpdb_parquet_read": (_I32, [_P, _I64, _CP, _I32, _I64, _I64, _S, _A, _P]),
+    "gfpdb_parquet_read_file": (_I32, [ctypes.c_char_p, _CP, _I32, _I64, _I64, _S, _A, _P]),
     "gfpdb_csv_read": (_I32, [_P, _I64, _I32, ctypes.c_char, _I32, _S, _CP, _I32, _S, _A, _P]),
     "gfpdb_execute_plan": (
         _I32,

@@ -876,6 +876,36 @@ int32_t gfpdb_group_clear(gfpdb_group* group) {
 
 void gfpdb_group_free(gfpdb_group* group) { delete group; }
 
+// ----------------------------------------------------------------- Parquet
+
+int32_t gfpdb_parquet_read(const void* file, int64_t n_bytes, const char* const* columns, int32_t n_columns,
+                           int64_t start_pos, int64_t end_pos, ArrowSchema* out_schema, ArrowDeviceArray* out,
+                           void* stream) {
+  return guarded([&] {
+    require(file != nullptr && out_schema != nullptr && out != nullptr, "null argument");
+    ensure_device();
+    cudaStream_t s = as_stream(stream);
+    std::vector<std::string> names;
+    if (columns != nullptr && n_columns >= 0) names = names_of(columns, n_columns);
+    auto ts = parquet_read(static_cast<const uint8_t*>(file), n_bytes, names, start_pos, end_pos, s);
+    export_tupleset(ts, out_schema, out, false, s);
+  });
+}
+
+int32_t gfpdb_parquet_read_file(const char* path, const char* const* columns, int32_t n_columns, int64_t start_pos,
+                                int64_t end_pos, ArrowSchema* out_schema, ArrowDeviceArray* out, void* stream) {
+  return guarded([&] {
+    require(path != nullptr && out_schema != nullptr && out != nullptr, "null argument");
+    ensure_device();
+    cudaStream_t s = as_stream(stream);
+    std::vector<std::string> names;
+    if (columns != nullptr && n_columns >= 0) names = names_of(columns, n_columns);
+    const std::vector<uint8_t> bytes = pop::read_local_file(path);
+    auto ts = parquet_read(bytes.data(), static_cast<int64_t>(bytes.size()), names, start_pos, end_pos, s);
+    export_tupleset(ts, out_schema, out, false, s);
+  });
+}
+
 // --------------------------------------------------------------------- CSV
 
 int32_t gfpdb_csv_read(const void* text, int64_t n_bytes, int32_t text_device_type, char delimiter, int32_t has_header,

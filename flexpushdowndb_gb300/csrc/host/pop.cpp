@@ -1,6 +1,7 @@
 #include "pop.h"
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 
 namespace gfpdb::pop {
@@ -1061,6 +1062,107 @@ class CsvScanPOp : public PhysicalOp {
   bool header_;
 };
 
+// The bytes of an input table holding one value (a file's contents), in
+// host memory: read in place from a host array, copied from a device one.
+std::vector<uint8_t> input_bytes(const InputTable& in, const std::string& table, cudaStream_t s) {
+  if (in.array != nullptr && (in.array->device_type == ARROW_DEVICE_CPU || in.array->device_type == ARROW_DEVICE_CUDA_HOST)) {
+    const ArrowArray& a = in.array->array;
+    if (a.n_children < 1 || a.children[0]->n_buffers != 3 || a.length != 1)
+      fail(GFPDB_EINVAL, "input '" + table + "' must hold the file as one utf8 value");
+    const ArrowArray* c = a.children[0];
+    const int32_t* offs = static_cast<const int32_t*>(c->buffers[1]) + c->offset + a.offset;
+    const uint8_t* data = static_cast<const uint8_t*>(c->buffers[2]);
+    return std::vector<uint8_t>(data + offs[0], data + offs[1]);
+  }
+  TupleSetPtr ts = in.device ? in.device : import_tupleset(in.schema, in.array, s);
+  ts = resolved(ts, s);
+  if (ts->num_columns() < 1 || ts->field(0).type != DType::Utf8 || ts->num_rows() != 1)
+    fail(GFPDB_EINVAL, "input '" + table + "' must hold the file as one utf8 value");
+  const auto& c = ts->column(0);
+  int32_t off[2];
+  GF_CUDA(cudaMemcpyAsync(off, c->offsets, sizeof(off), cudaMemcpyDeviceToHost, s));
+  sync(s);
+  std::vector<uint8_t> bytes(static_cast<size_t>(off[1] - off[0]));
+  if (!bytes.empty())
+    GF_CUDA(cudaMemcpyAsync(bytes.data(), static_cast<const uint8_t*>(c->data) + off[0], bytes.size(),
+                            cudaMemcpyDeviceToHost, s));
+  sync(s);
+  return bytes;
+}
+
+// ParquetScanPOp: the Parquet file held by an input table decoded into its
+// columns (ParquetReader::read / readRange,
+// fpdb-tuple/src/parquet/ParquetReader.cpp:12-120, as FileScanAbstractPOp
+// reads a Parquet object, FileScanAbstractPOp.cpp:73-130).
+class ParquetScanPOp : public PhysicalOp {
+ public:
+  ParquetScanPOp(std::string name, std::string table, std::vector<std::string> columns, int64_t start, int64_t end)
+      : PhysicalOp(std::move(name), "ParquetScanPOp"), table_(std::move(table)), columns_(std::move(columns)),
+        start_(start), end_(end) {}
+
+  void setExecution(Execution* e) { exec_ = e; }
+
+  void onReceive(const Envelope& env) override {
+    if (env.getMessage().type != MessageType::START) return;
+    const std::vector<uint8_t> bytes = input_bytes(exec_->input(table_), table_, ctx()->stream());
+    Message out;
+    out.type = MessageType::TUPLESET;
+    out.tuples = parquet_read(bytes.data(), static_cast<int64_t>(bytes.size()), columns_, start_, end_,
+                              ctx()->stream());
+    ctx()->tell(out);
+    ctx()->notifyComplete();
+  }
+
+ private:
+  Execution* exec_ = nullptr;
+  std::string table_;
+  std::vector<std::string> columns_;
+  int64_t start_, end_;
+};
+
+// FileScanPOp over a local file (FileScanAbstractPOp::readAndSendTuples with
+// LocalFileScanKernel::scan, fpdb-executor/src/physical/file/FileScanAbstractPOp.cpp:73-130,
+// LocalFileScanKernel.cpp:38-91): the file is read from the file system,
+// then parsed on the device as CSV (csv_parse) or Parquet (parquet_read).
+class FileScanPOp : public PhysicalOp {
+ public:
+  FileScanPOp(std::string name, std::string path, bool parquet, std::vector<std::string> columns, int64_t start,
+              int64_t end, std::vector<CsvField> fields, std::vector<int> emit, char delim, bool header)
+      : PhysicalOp(std::move(name), "FileScanPOp"), path_(std::move(path)), parquet_(parquet),
+        columns_(std::move(columns)), start_(start), end_(end), fields_(std::move(fields)), emit_(std::move(emit)),
+        delim_(delim), header_(header) {}
+
+  void onReceive(const Envelope& env) override {
+    if (env.getMessage().type != MessageType::START) return;
+    const std::vector<uint8_t> bytes = read_local_file(path_);
+    Message out;
+    out.type = MessageType::TUPLESET;
+    if (parquet_) {
+      out.tuples = parquet_read(bytes.data(), static_cast<int64_t>(bytes.size()), columns_, start_, end_,
+                                ctx()->stream());
+    } else {
+      auto text = make_buffer(static_cast<int64_t>(bytes.size()) > 0 ? static_cast<int64_t>(bytes.size()) : 1,
+                              ctx()->stream());
+      copy_h2d(text->data(), bytes.data(), static_cast<int64_t>(bytes.size()), ctx()->stream());
+      out.tuples = csv_parse(text->as<char>(), static_cast<int64_t>(bytes.size()), delim_, header_, fields_, emit_,
+                             ctx()->stream());
+      sync(ctx()->stream());  // `bytes` and `text` go when this returns
+    }
+    ctx()->tell(out);
+    ctx()->notifyComplete();
+  }
+
+ private:
+  std::string path_;
+  bool parquet_;
+  std::vector<std::string> columns_;
+  int64_t start_, end_;
+  std::vector<CsvField> fields_;
+  std::vector<int> emit_;
+  char delim_;
+  bool header_;
+};
+
 // CollatePOp (fpdb-executor/src/physical/collate/CollatePOp.cpp:67-150):
 // concatenates everything it receives into the query result.
 class CollatePOp : public PhysicalOp {
@@ -1096,6 +1198,19 @@ AggFn agg_fn(const std::string& f) {
 }
 
 }  // namespace
+
+std::vector<uint8_t> read_local_file(const std::string& path) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if (f == nullptr) fail(GFPDB_EINVAL, "cannot open '" + path + "'");
+  std::vector<uint8_t> bytes;
+  uint8_t buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) bytes.insert(bytes.end(), buf, buf + got);
+  const bool bad = std::ferror(f) != 0;
+  std::fclose(f);
+  if (bad) fail(GFPDB_EINVAL, "cannot read '" + path + "'");
+  return bytes;
+}
 
 std::vector<GroupAggregate> parse_aggregates(const json::Value& list) {
   std::vector<GroupAggregate> aggs;
@@ -1437,7 +1552,7 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
       joins.push_back(std::move(c));
     }
     op = std::make_unique<HashJoinChainPOp>(name, std::move(joins));
-  } else if (type == "CsvScanPOp") {
+  } else if (type == "CsvScanPOp" || (type == "FileScanPOp" && o.get_str("format", "csv") == "csv")) {
     std::vector<CsvField> fields;
     for (auto& f : o.at("fields").array()) {
       CsvField cf;
@@ -1461,18 +1576,34 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
         int found = -1;
         for (size_t i = 0; i < fields.size(); ++i)
           if (fields[i].name == cn) found = static_cast<int>(i);
-        if (found < 0) fail(GFPDB_EINVAL, "CsvScanPOp '" + name + "': column '" + cn + "' is not a field");
+        if (found < 0) fail(GFPDB_EINVAL, type + " '" + name + "': column '" + cn + "' is not a field");
         emit.push_back(found);
       }
     } else {
       for (size_t i = 0; i < fields.size(); ++i) emit.push_back(static_cast<int>(i));
     }
     const std::string delim = o.get_str("delimiter", ",");
-    if (delim.size() != 1) fail(GFPDB_EINVAL, "CsvScanPOp delimiter must be one byte");
-    auto cs = std::make_unique<CsvScanPOp>(name, o.at("table").str(), std::move(fields), std::move(emit), delim[0],
-                                           o.get_bool("header", false));
-    cs->setExecution(exec);
-    op = std::move(cs);
+    if (delim.size() != 1) fail(GFPDB_EINVAL, type + " delimiter must be one byte");
+    if (type == "FileScanPOp") {
+      op = std::make_unique<FileScanPOp>(name, o.at("path").str(), false, std::vector<std::string>{}, 0, -1,
+                                         std::move(fields), std::move(emit), delim[0], o.get_bool("header", false));
+    } else {
+      auto cs = std::make_unique<CsvScanPOp>(name, o.at("table").str(), std::move(fields), std::move(emit), delim[0],
+                                             o.get_bool("header", false));
+      cs->setExecution(exec);
+      op = std::move(cs);
+    }
+  } else if (type == "FileScanPOp") {
+    const std::string fmt = o.get_str("format", "csv");
+    if (fmt != "parquet") fail(GFPDB_EUNSUPPORTED, "FileScanPOp '" + name + "': format '" + fmt + "' (csv or parquet)");
+    op = std::make_unique<FileScanPOp>(name, o.at("path").str(), true, o.str_list("columns"),
+                                       o.get_int("startPos", 0), o.get_int("finishPos", -1), std::vector<CsvField>{},
+                                       std::vector<int>{}, ',', false);
+  } else if (type == "ParquetScanPOp") {
+    auto ps = std::make_unique<ParquetScanPOp>(name, o.at("table").str(), o.str_list("columns"),
+                                               o.get_int("startPos", 0), o.get_int("finishPos", -1));
+    ps->setExecution(exec);
+    op = std::move(ps);
   } else if (type == "GroupPOp" || type == "AggregatePOp") {
     std::vector<GroupAggregate> aggs = parse_aggregates(o.at("aggregates"));
     if (type == "AggregatePOp") {

@@ -250,6 +250,9 @@ TupleSetPtr join_finish_kind(const std::string& join_name, JoinKind kind, const 
                              const std::vector<Field>& probe_fields, const std::vector<std::string>& proj,
                              cudaStream_t s);
 
+// A file of the local file system, whole (the scan operators' input).
+std::vector<uint8_t> read_local_file(const std::string& path);
+
 // Aggregate functions of a group-by spec: [{"function", "name", "expr"}],
 // functions SUM, COUNT (without expr: count of rows), MIN, MAX, AVG and
 // AVG_REDUCE (no expr; the second phase of a parallel AVG).

@@ -36,12 +36,13 @@ std::map<std::string, std::vector<std::string>> plan_inputs(const json::Value& p
   std::map<std::string, std::vector<std::string>> out;
   for (auto& o : plan.at("ops").array()) {
     const std::string type = o.at("type").str();
-    if (type != "TableScanPOp" && type != "CsvScanPOp") continue;
+    if (type == "FileScanPOp") fail(GFPDB_EUNSUPPORTED, "served requests read registered tables, not files");
+    if (type != "TableScanPOp" && type != "CsvScanPOp" && type != "ParquetScanPOp") continue;
     const std::string t = o.at("table").str();
     auto it = tables.find(t);
     if (it == tables.end()) fail(GFPDB_EINVAL, "request scans table '" + t + "' which is not registered");
     std::vector<std::string> cols;
-    if (type == "CsvScanPOp") {
+    if (type == "CsvScanPOp" || type == "ParquetScanPOp") {  // the file's bytes, one value
       if (it->second.cols.empty()) fail(GFPDB_EINVAL, "table '" + t + "' has no columns");
       cols.push_back(it->second.cols[0].name);
     } else if (o.contains("columns")) {

@@ -294,6 +294,14 @@ TupleSetPtr with_composite_key(const TupleSetPtr& t, const std::vector<std::stri
                                const std::string& alias_prefix, cudaStream_t s);
 bool is_internal_key_column(const std::string& name);
 
+// ------------------------------------------------------------ parquet.cu
+
+// Read the named columns (all when empty) of a Parquet file held in host
+// memory; with start_pos <= end_pos only the row groups whose first column
+// chunk starts in [start_pos, end_pos]. Synchronizes `s`.
+TupleSetPtr parquet_read(const uint8_t* file, int64_t size, const std::vector<std::string>& names, int64_t start_pos,
+                         int64_t end_pos, cudaStream_t s);
+
 // ------------------------------------------------------------ shuffle.cu
 
 constexpr int64_t kShuffleMaxSlots = 1024;

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 import json
+from pathlib import Path
 from typing import Sequence
 
 import numpy as np
@@ -242,6 +243,24 @@ class Group:
         if getattr(self, "_h", None) and self._h.value:
             _abi.lib().gfpdb_group_free(self._h)
             self._h = ctypes.c_void_p()
+
+
+def parquet_read(source, columns: Sequence[str] | None = None, start_pos: int = 0, end_pos: int = -1,
+                 stream=None) -> Table:
+    """Read columns of a Parquet file (gfpdb_parquet_read / _read_file,
+    ParquetReader::read, readRange when start_pos <= end_pos): `source` is
+    the file's bytes or a path of the local file system."""
+    names, n = _names(columns)
+    s, a = new_output()
+    L = _abi.lib()
+    if isinstance(source, (str, Path)):
+        _abi.check(L.gfpdb_parquet_read_file(str(source).encode(), names, n, start_pos, end_pos, ctypes.byref(s),
+                                             ctypes.byref(a), stream))
+    else:
+        buf = np.frombuffer(source, dtype=np.uint8) if isinstance(source, (bytes, bytearray)) else source
+        _abi.check(L.gfpdb_parquet_read(buf.ctypes.data, buf.nbytes, names, n, start_pos, end_pos, ctypes.byref(s),
+                                        ctypes.byref(a), stream))
+    return import_result(s, a)
 
 
 def csv_read(text: bytes | np.ndarray | int, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,

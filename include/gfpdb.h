@@ -331,6 +331,28 @@ int32_t gfpdb_group_clear(gfpdb_group* group);
 
 void gfpdb_group_free(gfpdb_group* group);
 
+/* ---------------------------------------------------------------- Parquet */
+
+/* Read columns of a Parquet file held in host memory (`file`, n_bytes):
+ * `columns` names them (all when n_columns < 0), in that order; with
+ * start_pos <= end_pos only the row groups whose first column chunk starts
+ * within [start_pos, end_pos] (pass 0, -1 for the whole file). Flat schemas
+ * of INT32 (DATE annotated: date32), INT64, DOUBLE and BYTE_ARRAY (utf8)
+ * columns, required or optional without nulls; PLAIN and dictionary
+ * encodings; data pages v1 and v2; uncompressed or snappy. The footer and
+ * page headers are read on the host, the pages decompressed and decoded on
+ * the device. Replaces ParquetReader::read / readRange
+ * (fpdb-tuple/src/parquet/ParquetReader.cpp:12-120) under
+ * LocalParquetReader (fpdb-tuple/src/parquet/LocalParquetReader.cpp:25-59). */
+int32_t gfpdb_parquet_read(const void* file, int64_t n_bytes, const char* const* columns, int32_t n_columns,
+                           int64_t start_pos, int64_t end_pos, struct ArrowSchema* out_schema,
+                           struct ArrowDeviceArray* out, void* stream);
+
+/* The same over a file of the local file system (LocalParquetReader::read). */
+int32_t gfpdb_parquet_read_file(const char* path, const char* const* columns, int32_t n_columns, int64_t start_pos,
+                                int64_t end_pos, struct ArrowSchema* out_schema, struct ArrowDeviceArray* out,
+                                void* stream);
+
 /* -------------------------------------------------------------------- CSV */
 
 /* Parse delimiter-separated text into typed columns. `target_schema` ("+s")
