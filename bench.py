@@ -623,7 +623,7 @@ def run_case(args):
         fn = lambda: batch.star_batch(spec, dev, use_graph=False).table  # noqa: E731
         args.rows = sum(tabs[p].num_rows for p in parts)
         return _time_case(args, fn)
-    if args.case in ("join", "group", "csv", "filter", "shuffle", "group2"):
+    if args.case in ("join", "group", "csv", "filter", "shuffle", "group2", "parquet"):
         return _operator_case(args)
     tabs = workloads.star_tables(fact_rows=args.rows, seed=2000)
     fact = DeviceTable.from_host(tabs["fact"])
@@ -723,6 +723,33 @@ def _operator_case(args):
         algo = n * (8 + 8 + 2 * (8 + 8 + 4))
         print(json.dumps({"case": "shuffle", "rows": n, "slots": args.slots, "kernels_ms": kern, "shuffle_ms": ms,
                           "algorithmic_gbs": algo / (ms * 1e6), "rows_per_s": n / (ms * 1e-3)}))
+        return
+    elif args.case == "parquet":
+        from flexpushdowndb_gb300.parquet_writer import write_parquet
+
+        fact = workloads.star_fact(n, seed=7002)
+        data = np.frombuffer(write_parquet(fact, row_group_rows=1 << 20, page_rows=1 << 17), dtype=np.uint8)
+        import torch
+
+        pinned = torch.empty(data.nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+        pinned[:] = data
+        fn = lambda: ops.parquet_read(pinned)  # noqa: E731
+        got = fn()
+        ok = all(np.array_equal(got[c.name], c.values) for c in fact.columns)
+        for _ in range(max(2, args.warmup)):
+            fn()
+        from flexpushdowndb_gb300 import _abi
+
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prof = _kernel_profile(_abi.lib(), _abi, fn, args.steps)
+        call_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+        kern = {k: v["ms"] / args.steps for k, v in prof.items()}
+        out_bytes = sum(c.values.nbytes for c in fact.columns)
+        print(json.dumps({"case": "parquet", "rows": n, "file_bytes": int(data.nbytes), "parity": bool(ok),
+                          "kernels_ms": kern, "call_ms_with_result_to_host": call_ms,
+                          "decode_ms": sum(kern.values()),
+                          "decode_gbs": (data.nbytes + out_bytes) / (sum(kern.values()) * 1e6)}))
         return
     elif args.case == "group2":
         from flexpushdowndb_gb300 import plan

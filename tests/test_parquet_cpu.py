@@ -48,3 +48,27 @@ def test_parquet_plan_operators_validate():
     q.collate("c", "t")
     with pytest.raises(_abi.GfpdbError):
         plan.validate(q)
+
+
+def test_package_writer_is_read_by_pyarrow():
+    import io
+
+    import numpy as np
+
+    pq = pytest.importorskip("pyarrow.parquet")
+    from flexpushdowndb_gb300.parquet_writer import write_parquet
+    from flexpushdowndb_gb300.tupleset import Column, Table
+
+    n, seed, _, _ = FIXTURES["plain_none_v1"]
+    cols = source(n, seed)
+    t = Table([Column(k, ty, v) for k, (ty, v) in cols.items()])
+    for kw in (dict(), dict(dictionary_max=0), dict(row_group_rows=3000, page_rows=700)):
+        back = pq.read_table(io.BytesIO(write_parquet(t, **kw)))
+        for c in t.columns:
+            got = back.column(c.name).to_pylist()
+            if c.type == "date32":
+                got = [(d - __import__("datetime").date(1970, 1, 1)).days for d in got]
+            if c.type == "float64":
+                assert np.array_equal(np.array(got).view(np.int64), c.values.view(np.int64))
+            else:
+                assert got == c.to_list(), c.name

@@ -125,3 +125,14 @@ def test_csv_file_scan(gpu, tmp_path):
             "columns": ["c", "a"]})
     p.collate("collate", "scan")
     assert plan.execute(p, {}).table.rows() == [("x", 1), ("yy", 2), ("zzz", 3)]
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(dictionary_max=0), dict(row_group_rows=3000, page_rows=700)])
+def test_reads_the_package_writer(gpu, kw):
+    """Files of flexpushdowndb_gb300.parquet_writer (REQUIRED columns,
+    plain or bit-packed dictionary pages) read back as written."""
+    from flexpushdowndb_gb300.parquet_writer import write_parquet
+
+    want = expected("plain_none_v1")
+    got = ops.parquet_read(write_parquet(want, **kw))
+    same(got, want)
