@@ -307,18 +307,31 @@ def star_plan_section(args, L, stream, sptr, world, rank, barrier, max_over_rank
         plain.append(a.elapsed_time(b))
         parity &= res.table.sorted_rows() == wants[k % n_sets]
     sts = [torch.cuda.Stream() for _ in range(2)]
-    epp = prepared(dict(plan_d, cudaGraph=True, hostCopy="engine"), host, sts)
-    barrier()
-    t0 = time.perf_counter()
-    epp[0][0].launch()
-    for k in range(1, steps):
-        epp[k % n_sets][0].launch()
-        r = epp[(k - 1) % n_sets][0].wait()
-        parity &= r.table.sorted_rows() == wants[(k - 1) % n_sets]
-    r = epp[(steps - 1) % n_sets][0].wait()
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks((time.perf_counter() - t0) / steps)
-    barrier()
+
+    def end_to_end(d):
+        nonlocal parity
+        epp = prepared(d, host, sts)
+        barrier()
+        t0 = time.perf_counter()
+        epp[0][0].launch()
+        for k in range(1, steps):
+            epp[k % n_sets][0].launch()
+            r = epp[(k - 1) % n_sets][0].wait()
+            parity &= r.table.sorted_rows() == wants[(k - 1) % n_sets]
+        r = epp[(steps - 1) % n_sets][0].wait()
+        torch.cuda.synchronize()
+        secs = max_over_ranks((time.perf_counter() - t0) / steps)
+        barrier()
+        return secs, r.stats
+
+    copy_s, copy_stats = end_to_end(dict(plan_d, cudaGraph=True, hostCopy="engine"))
+    # hybrid: the fact's first forward probe key (read for every row) copied,
+    # the columns read for surviving rows only read in place
+    hyb = json.loads(json.dumps(plan_d))
+    for o in hyb["ops"]:
+        if o["type"] == "TableScanPOp" and o["table"] == "fact":
+            o["inPlaceColumns"] = [c for c in o["columns"] if c != "fk2"]
+    e2e_s, e2e_stats = end_to_end(dict(hyb, cudaGraph=True, hostCopy="engine"))
     return {
         "workload": "star query with bloom predicate transfer, fact %d rows (SSB-SF1 shape), %d input sets rotated"
                     % (STAR_FACT_ROWS, n_sets),
@@ -327,7 +340,13 @@ def star_plan_section(args, L, stream, sptr, world, rank, barrier, max_over_rank
         "plain": {"fact_rows_per_s": STAR_FACT_ROWS * world / (statistics.mean(plain) / 1e3),
                   "ms_per_step": statistics.mean(plain), "latency_ms": {"p50": _pct(plain, 50), "p99": _pct(plain, 99)}},
         "e2e": {"fact_rows_per_s": STAR_FACT_ROWS * world / e2e_s, "ms_per_step": 1e3 * e2e_s,
-                "h2d_bytes_per_step": r.stats["h2d_bytes"], "d2h_bytes_per_step": r.stats["d2h_bytes"]},
+                "h2d_bytes_per_step": e2e_stats["h2d_bytes"], "d2h_bytes_per_step": e2e_stats["d2h_bytes"],
+                "path": "prepared plans over pinned host tables (two in flight): the dimension tables and the fact's "
+                        "fk2 column (its first forward probe reads every row) copied, the other fact columns (read "
+                        "for surviving rows only) read in place over NVLink-C2C",
+                "h2d_bytes": "copied bytes + the full size of the columns read in place (an upper bound)"},
+        "e2e_copy_all": {"fact_rows_per_s": STAR_FACT_ROWS * world / copy_s, "ms_per_step": 1e3 * copy_s,
+                         "h2d_bytes_per_step": copy_stats["h2d_bytes"], "d2h_bytes_per_step": copy_stats["d2h_bytes"]},
         "l2": "four input sets of 195 MB rotated over the steps (780 MB > 129 MB L2)",
         "parity": parity,
     }
@@ -1024,10 +1043,40 @@ def main():
         # memory (every run copies the columns the batch reads), two copies
         # on two streams launched alternately
         sts = [torch.cuda.Stream() for _ in range(2)]
-        hpreps = [batch.PreparedBatch(spec, host_in, stream=ctypes.c_void_p(st.cuda_stream)) for st in sts]
-        for _ in range(args.warmup):
-            for pb in hpreps:
-                r = pb.execute()
+
+        def host_preps(sp):
+            hp = [batch.PreparedBatch(sp, host_in, stream=ctypes.c_void_p(st.cuda_stream)) for st in sts]
+            for _ in range(args.warmup):
+                for pb in hp:
+                    res = pb.execute()
+            return hp, res
+
+        def pipelined_s(hp, steps):
+            t0 = time.perf_counter()
+            hp[0].launch()
+            for k in range(1, steps):
+                hp[k % 2].launch()
+                hp[(k - 1) % 2].wait()
+            hp[(steps - 1) % 2].wait()
+            torch.cuda.synchronize()
+            return (time.perf_counter() - t0) / steps
+
+        # The tuner measured device-resident inputs; reading host tables in
+        # place favours other launch shapes, so the host-input path takes the
+        # fastest of a few (each checked against the device result).
+        e2e_spec, best = spec, None
+        for cand in (dict(), dict(blocksPerSm=1, stages=4), dict(blocksPerSm=1, stages=3),
+                     dict(blocksPerSm=2, stages=4)):
+            sp = dict(spec, **cand)
+            hp, res = host_preps(sp)
+            parity = parity and batch.split_by_query(res.table) == got
+            t = pipelined_s(hp, 6)
+            if best is None or t < best:
+                best, e2e_spec = t, sp
+            del hp
+        e2e_settings = {k: e2e_spec[k] for k in ("itemsPerThread", "blocksPerSm", "stages", "loadFactor")
+                        if k in e2e_spec}
+        hpreps, r = host_preps(e2e_spec)
         parity = parity and batch.split_by_query(r.table) == got
         barrier()
         t0 = time.perf_counter()
@@ -1150,7 +1199,8 @@ def main():
                         "every step copies the dimension columns and the foreign keys the fact pass reads in full, "
                         "the fact pass of each group of partitions starting as its copies land, reads the other "
                         "fact columns (read for some rows only) in place over NVLink-C2C, and reads its result",
-                "h2d_bytes": "copied bytes + one 32-byte sector per row and column read in place (an upper bound)"},
+                "h2d_bytes": "copied bytes + one 32-byte sector per row and column read in place (an upper bound)",
+                "settings": e2e_settings},
         "gpu_launches": launches,
         "merge": merge,
         "roofline": roofline,

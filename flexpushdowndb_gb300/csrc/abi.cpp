@@ -140,7 +140,9 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
   cp->arena = std::make_unique<Arena>(arena_bytes, nullptr);
   sync(nullptr);
   const uint64_t k0 = g_kernel_launches.load();
-  const int64_t h2d0 = copy_counters().h2d;
+  // host bytes a replay moves: the captured copies, and the page-locked
+  // columns its kernels read in place (their full size: an upper bound)
+  const int64_t h2d0 = copy_counters().h2d + copy_counters().in_place;
   cudaGraph_t graph = nullptr;
   bool ok = true;
   // The buffers the operators want pre-filled (sized by the ordinary run,
@@ -204,7 +206,7 @@ std::shared_ptr<CapturedPlan> capture_plan(const json::Value& plan, const std::m
   if (ok && graph != nullptr && cudaGraphInstantiate(&cp->exec, graph, 0) != cudaSuccess) ok = false;
   if (graph != nullptr) (void)cudaGraphDestroy(graph);
   (void)cudaGetLastError();
-  cp->h2d = copy_counters().h2d - h2d0;
+  cp->h2d = copy_counters().h2d + copy_counters().in_place - h2d0;
   cp->kernels = g_kernel_launches.load() - k0;
   if (!ok) {
     cp->capturable = false;
@@ -980,7 +982,7 @@ int32_t gfpdb_execute_plan(const char* plan_json, int32_t n_tables, const char* 
       if (stats == nullptr) return;
       stats->device_ns = 0;
       stats->kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
-      stats->h2d_bytes = copy_counters().h2d - c0.h2d;
+      stats->h2d_bytes = copy_counters().h2d - c0.h2d + copy_counters().in_place - c0.in_place;
       stats->d2h_bytes = copy_counters().d2h - c0.d2h;
       stats->num_ops = num_ops;
       stats->messages = messages;

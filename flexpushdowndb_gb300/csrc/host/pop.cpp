@@ -91,9 +91,10 @@ bool is_producer_complete(PhysicalOp& op) { return op.ctx()->operatorMap().allCo
 // zero-copy row slices.
 class TableScanPOp : public PhysicalOp {
  public:
-  TableScanPOp(std::string name, std::string table, std::vector<std::string> columns, int64_t chunk_rows)
+  TableScanPOp(std::string name, std::string table, std::vector<std::string> columns, int64_t chunk_rows,
+               std::vector<std::string> in_place = {})
       : PhysicalOp(std::move(name), "TableScanPOp"), table_(std::move(table)), columns_(std::move(columns)),
-        chunk_rows_(chunk_rows) {}
+        in_place_(std::move(in_place)), chunk_rows_(chunk_rows) {}
 
   void setExecution(Execution* e) { exec_ = e; }
 
@@ -101,7 +102,11 @@ class TableScanPOp : public PhysicalOp {
     const Message& m = env.getMessage();
     if (m.type != MessageType::START) return;
     const InputTable& in = exec_->input(table_);
-    TupleSetPtr ts = in.device ? in.device : import_tupleset(in.schema, in.array, ctx()->stream());
+    // host tables: only the scanned columns come over, those named in
+    // inPlaceColumns read in place when the table is page-locked
+    TupleSetPtr ts = in.device ? in.device
+                               : import_tupleset(in.schema, in.array, ctx()->stream(), false,
+                                                 columns_.empty() ? nullptr : &columns_, &in_place_);
     if (!columns_.empty()) ts = ts->project(columns_);
     const int64_t n = ts->num_rows();
     if (chunk_rows_ <= 0 || n <= chunk_rows_) {
@@ -124,6 +129,7 @@ class TableScanPOp : public PhysicalOp {
   Execution* exec_ = nullptr;
   std::string table_;
   std::vector<std::string> columns_;
+  std::vector<std::string> in_place_;
   int64_t chunk_rows_;
 };
 
@@ -1492,7 +1498,7 @@ TupleSetPtr Execution::execute() {
   if (!incomplete.empty()) fail(GFPDB_EINVAL, "plan finished with incomplete operators: " + incomplete);
   if (collate == nullptr) fail(GFPDB_EINVAL, "plan has no CollatePOp");
   stats_.kernel_launches = static_cast<int64_t>(g_kernel_launches.load() - launches0);
-  stats_.h2d_bytes = copy_counters().h2d - c0.h2d;
+  stats_.h2d_bytes = copy_counters().h2d - c0.h2d + copy_counters().in_place - c0.in_place;
   stats_.d2h_bytes = copy_counters().d2h - c0.d2h;
   TupleSetPtr r = collate->tuples();
   if (!r) fail(GFPDB_EINVAL, "CollatePOp received no TupleSet");
@@ -1508,7 +1514,8 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
   const std::string name = o.at("name").str();
   std::unique_ptr<PhysicalOp> op;
   if (type == "TableScanPOp") {
-    auto s = std::make_unique<TableScanPOp>(name, o.at("table").str(), o.str_list("columns"), o.get_int("chunkRows", 0));
+    auto s = std::make_unique<TableScanPOp>(name, o.at("table").str(), o.str_list("columns"), o.get_int("chunkRows", 0),
+                                            o.str_list("inPlaceColumns"));
     s->setExecution(exec);
     op = std::move(s);
   } else if (type == "FilterPOp") {

@@ -73,6 +73,7 @@ void after_launch(const char* kernel_name);
 struct CopyCounters {
   int64_t h2d = 0;
   int64_t d2h = 0;
+  int64_t in_place = 0;  // bytes of page-locked host columns kernels read in place (the columns' size)
 };
 CopyCounters& copy_counters();
 

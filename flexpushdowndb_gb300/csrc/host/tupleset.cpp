@@ -1,5 +1,6 @@
 #include "tupleset.h"
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 
@@ -267,37 +268,46 @@ const void* device_view_of_host(const void* p) {
 }
 
 TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* darr, cudaStream_t s,
-                            bool copy_device) {
-  auto fields = import_schema(schema);
+                            bool copy_device, const std::vector<std::string>* wanted,
+                            const std::vector<std::string>* in_place) {
+  auto all_fields = import_schema(schema);
+  auto listed = [](const std::vector<std::string>* v, const std::string& n) {
+    return v != nullptr && std::find(v->begin(), v->end(), n) != v->end();
+  };
   if (darr == nullptr) fail(GFPDB_EINVAL, "null ArrowDeviceArray");
   const ArrowArray& arr = darr->array;
   if (arr.release == nullptr) fail(GFPDB_EINVAL, "released ArrowArray");
-  if (arr.n_children != static_cast<int64_t>(fields.size()))
-    fail(GFPDB_EINVAL, "ArrowArray child count does not match the schema");
   bool host = darr->device_type == ARROW_DEVICE_CPU || darr->device_type == ARROW_DEVICE_CUDA_HOST;
   if (!host && darr->device_type != ARROW_DEVICE_CUDA)
     fail(GFPDB_EUNSUPPORTED, "unsupported ArrowDeviceArray device_type " + std::to_string(darr->device_type));
   if (arr.null_count > 0) fail(GFPDB_EUNSUPPORTED, "struct-level nulls are not supported");
+  if (arr.n_children != static_cast<int64_t>(all_fields.size()))
+    fail(GFPDB_EINVAL, "ArrowArray child count does not match the schema");
   const int64_t n = arr.length;
   const int64_t soff = arr.offset;
   std::vector<ColumnPtr> cols;
-  for (size_t i = 0; i < fields.size(); ++i) {
+  std::vector<Field> fields;
+  for (size_t i = 0; i < all_fields.size(); ++i) {
+    if (wanted != nullptr && !listed(wanted, all_fields[i].name)) continue;
+    fields.push_back(all_fields[i]);
     const ArrowArray* c = arr.children[i];
-    if (c->length < soff + n) fail(GFPDB_EINVAL, "column '" + fields[i].name + "' is shorter than the struct");
+    if (c->length < soff + n) fail(GFPDB_EINVAL, "column '" + all_fields[i].name + "' is shorter than the struct");
     if (c->null_count != 0 && c->buffers[0] != nullptr)
-      fail(GFPDB_EUNSUPPORTED, "column '" + fields[i].name + "' has nulls; nullable inputs are not supported");
+      fail(GFPDB_EUNSUPPORTED, "column '" + all_fields[i].name + "' has nulls; nullable inputs are not supported");
     const int64_t off = c->offset + soff;
-    DType t = fields[i].type;
+    DType t = all_fields[i].type;
     if (t != DType::Utf8) {
       if (c->n_buffers != 2) fail(GFPDB_EINVAL, "fixed-width column needs 2 buffers");
       int w = dtype_width(t);
       const char* src = static_cast<const char*>(c->buffers[1]) + off * w;
-      const void* zc = host && host_copy_mode() == 2 && !copy_device ? device_view_of_host(src) : nullptr;
+      const bool zero_copy = host && !copy_device && (host_copy_mode() == 2 || listed(in_place, all_fields[i].name));
+      const void* zc = zero_copy ? device_view_of_host(src) : nullptr;
       if (zc != nullptr) {
         // Zero-copy: kernels read the page-locked host column over the
         // chip-to-chip link; only the sectors they touch cross it.
         auto buf = std::make_shared<DeviceBuffer>(const_cast<void*>(zc), n * w);
         cols.push_back(make_fixed_column(t, n, buf));
+        copy_counters().in_place += n * w;
       } else if (host || copy_device) {
         auto buf = make_buffer(n * w, s);
         if (host) {

@@ -120,8 +120,13 @@ std::string first_nullable_column(const TupleSet& ts);  // "" when none
 // Device address of page-locked host memory (nullptr for pageable memory).
 const void* device_view_of_host(const void* p);
 
+// `wanted` (when given) limits the import to those columns (schema order
+// kept); the columns named in `in_place` of a page-locked host table are not
+// copied: kernels read them over the chip-to-chip link (a column of pageable
+// memory is copied all the same).
 TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* array, cudaStream_t s,
-                            bool copy_device = false);
+                            bool copy_device = false, const std::vector<std::string>* wanted = nullptr,
+                            const std::vector<std::string>* in_place = nullptr);
 std::vector<Field> import_schema(const ArrowSchema* schema);
 
 // Export a TupleSet. With to_host, values are copied to host memory (stream

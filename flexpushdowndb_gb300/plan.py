@@ -41,12 +41,17 @@ class Plan:
         if consumer not in cons:
             cons.append(consumer)
 
-    def scan(self, name: str, table: str, columns: Sequence[str] | None = None, chunk_rows: int = 0) -> str:
+    def scan(self, name: str, table: str, columns: Sequence[str] | None = None, chunk_rows: int = 0,
+             in_place: Sequence[str] = ()) -> str:
+        """TableScanPOp. `in_place`: columns of a page-locked host table the
+        kernels read over the chip-to-chip link instead of a copy."""
         op = {"type": "TableScanPOp", "name": name, "table": table}
         if columns:
             op["columns"] = list(columns)
         if chunk_rows:
             op["chunkRows"] = chunk_rows
+        if in_place:
+            op["inPlaceColumns"] = list(in_place)
         return self._add(op)
 
     def filter(self, name: str, producer: str, predicate: Expr, project: Sequence[str] | None = None) -> str:

@@ -351,3 +351,23 @@ def test_prepared_star_plan_through_capture_and_replays(gpu):
     for r in results:
         assert r.table.sorted_rows() == want
     assert results[-1].stats["device_ns"] > 0  # a replay
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_star_plan_with_fact_columns_read_in_place(gpu, graph):
+    """Pinned host inputs, the fact columns other than the first probe key
+    read in place: the same result as device inputs; the declared host bytes
+    count the in-place columns whole."""
+    tabs = workloads.star_tables(fact_rows=500_000, seed=2024)
+    d = json.loads(workloads.star_plan().to_json())
+    for o in d["ops"]:
+        if o["type"] == "TableScanPOp" and o["table"] == "fact":
+            o["inPlaceColumns"] = [c for c in o["columns"] if c != "fk2"]
+    d["cudaGraph"] = graph
+    host = plan.PreparedInputs(tabs, pinned=True)
+    want = queries.star_query(tabs).sorted_rows()
+    for _ in range(3 if graph else 1):
+        res = plan.execute(json.dumps(d), host)
+        assert res.table.sorted_rows() == want
+    fact_bytes = sum(c.values.nbytes for c in tabs["fact"].columns)
+    assert res.stats["h2d_bytes"] >= fact_bytes
