@@ -15,11 +15,11 @@
 //                          4-byte offset) and the warp moves its bytes, 32 at
 //                          a time (copies whose source overlaps their output
 //                          go in steps of the offset);
-//   parquet_pages_kernel   one warp per page: skips (and checks) the
+//   parquet_pages_kernel   one CTA per page: thread 0 skips (and checks) the
 //                          definition levels, walks byte-array lengths (data
-//                          and dictionary pages), and decodes dictionary
-//                          indices run by run (a bit-packed run's values
-//                          extracted by all lanes);
+//                          and dictionary pages) and reads the dictionary
+//                          indices' run headers, up to 256 a round, and every
+//                          thread then decodes the round's indices;
 //   parquet_values_kernel  per data page and value: fixed-width values
 //                          copied or looked up in the dictionary into the
 //                          output column; byte arrays get their source and
@@ -190,13 +190,21 @@ __device__ __forceinline__ bool run_header(const uint8_t* p, int32_t n, int32_t*
   return false;
 }
 
-__global__ void __launch_bounds__(256) parquet_pages_kernel(PageDev* pages, int32_t n_pages, DictArrays dicts,
-                                                            DevStatus* st) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const int64_t warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-  for (int64_t w = warp; w < n_pages; w += warps) {
-    __syncwarp();  // lane 0 may have walked the previous page alone
+constexpr int kPqThreads = 256;
+constexpr int kPqRuns = 256;  // run headers read per round
+
+// One CTA per page. Thread 0 does the sequential parts (definition levels,
+// byte-array lengths, run headers); the dictionary indices of each round of
+// up to kPqRuns runs are then decoded by every thread, a value finding its
+// run by binary search over the runs' first values.
+__global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* pages, int32_t n_pages, DictArrays dicts,
+                                                                   DevStatus* st) {
+  __shared__ int32_t s_first[kPqRuns + 1];  // the page value index each run starts at; then the round's end
+  __shared__ int32_t s_start[kPqRuns];      // bit-packed runs: first byte; RLE runs: -1
+  __shared__ uint32_t s_value[kPqRuns];     // RLE runs: the value
+  __shared__ int32_t s_n, s_ok, s_at, s_done, s_bw;
+  for (int64_t w = blockIdx.x; w < n_pages; w += gridDim.x) {
+    __syncthreads();  // the previous page's shared state is no longer read
     PageDev& pg = pages[w];
     const uint8_t* base;
     int32_t blen;
@@ -208,10 +216,9 @@ __global__ void __launch_bounds__(256) parquet_pages_kernel(PageDev* pages, int3
       base = pg.body + skip;
       blen = pg.body_len - skip;
     }
-    int ok = 1;
-    if (pg.v1_def) {  // 4-byte length, then the levels: every one must be 1 (no nulls)
-      int32_t skip = 0;
-      if (lane == 0) {
+    if (threadIdx.x == 0) {
+      int ok = 1;
+      if (pg.v1_def) {  // 4-byte length, then the levels: every one must be 1 (no nulls)
         ok = 0;
         if (blen >= 4) {
           const int32_t len = static_cast<int32_t>(le32(base));
@@ -247,131 +254,135 @@ __global__ void __launch_bounds__(256) parquet_pages_kernel(PageDev* pages, int3
                 seen += static_cast<int32_t>(h >> 1);
               }
             }
-            skip = 4 + len;
+            base += 4 + len;
+            blen -= 4 + len;
           }
         }
+        if (!ok) raise_status(st, GFPDB_EUNSUPPORTED, 200000 + static_cast<int32_t>(w));  // nulls, or bad levels
       }
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      skip = __shfl_sync(0xffffffffu, skip, 0);
-      if (!ok) {
-        if (lane == 0) raise_status(st, GFPDB_EUNSUPPORTED, 200000 + static_cast<int32_t>(w));  // nulls, or bad levels
-        continue;
-      }
-      base += skip;
-      blen -= skip;
-    }
-    if (lane == 0) {
-      pg.values = base;
-      pg.values_len = blen;
-    }
-    if (pg.type == parquet::PAGE_DICTIONARY) {
-      if (pg.width == 0 && lane == 0) {  // byte-array entries
-        int32_t at = 0;
-        for (int32_t e = 0; e < pg.num_values; ++e) {
-          if (blen - at < 4) {
-            raise_status(st, GFPDB_EINVAL, 300000 + static_cast<int32_t>(w));
-            break;
+      if (ok) {
+        pg.values = base;
+        pg.values_len = blen;
+        const bool bytes_walk = pg.width == 0 && (pg.type == parquet::PAGE_DICTIONARY || pg.encoding == parquet::ENC_PLAIN);
+        if (bytes_walk) {  // byte arrays: each value's address and length
+          const bool dict = pg.type == parquet::PAGE_DICTIONARY;
+          int32_t at = 0;
+          for (int32_t e = 0; e < pg.num_values; ++e) {
+            int32_t len = -1;
+            if (blen - at >= 4) {
+              len = static_cast<int32_t>(le32(base + at));
+              at += 4;
+            }
+            if (len < 0 || len > blen - at) {
+              raise_status(st, GFPDB_EINVAL, (dict ? 300000 : 400000) + static_cast<int32_t>(w));
+              ok = 0;
+              break;
+            }
+            if (dict) {
+              dicts.ptr[pg.dict_base + e] = reinterpret_cast<uint64_t>(base + at);
+              dicts.len[pg.dict_base + e] = len;
+            } else {
+              pg.row_ptr[pg.first_row + e] = reinterpret_cast<uint64_t>(base + at);
+              pg.row_len[pg.first_row + e] = len;
+            }
+            at += len;
           }
-          const int32_t len = static_cast<int32_t>(le32(base + at));
-          at += 4;
-          if (len < 0 || len > blen - at) {
-            raise_status(st, GFPDB_EINVAL, 300000 + static_cast<int32_t>(w));
-            break;
-          }
-          dicts.ptr[pg.dict_base + e] = reinterpret_cast<uint64_t>(base + at);
-          dicts.len[pg.dict_base + e] = len;
-          at += len;
+        } else if (pg.width > 0 && (pg.type == parquet::PAGE_DICTIONARY || pg.encoding == parquet::ENC_PLAIN) &&
+                   static_cast<int64_t>(pg.num_values) * pg.width > blen) {
+          raise_status(st, GFPDB_EINVAL, 400000 + static_cast<int32_t>(w));
+          ok = 0;
         }
-      } else if (pg.width > 0 && lane == 0 && static_cast<int64_t>(pg.num_values) * pg.width > blen) {
-        raise_status(st, GFPDB_EINVAL, 300000 + static_cast<int32_t>(w));
       }
-      continue;
-    }
-    if (pg.encoding == parquet::ENC_PLAIN) {
-      if (pg.width == 0 && lane == 0) {  // byte arrays: each value's address and length
-        int32_t at = 0;
-        for (int32_t i = 0; i < pg.num_values; ++i) {
-          if (blen - at < 4) {
-            raise_status(st, GFPDB_EINVAL, 400000 + static_cast<int32_t>(w));
-            break;
-          }
-          const int32_t len = static_cast<int32_t>(le32(base + at));
-          at += 4;
-          if (len < 0 || len > blen - at) {
-            raise_status(st, GFPDB_EINVAL, 400000 + static_cast<int32_t>(w));
-            break;
-          }
-          pg.row_ptr[pg.first_row + i] = reinterpret_cast<uint64_t>(base + at);
-          pg.row_len[pg.first_row + i] = len;
-          at += len;
-        }
-      } else if (pg.width > 0 && lane == 0 && static_cast<int64_t>(pg.num_values) * pg.width > blen) {
-        raise_status(st, GFPDB_EINVAL, 400000 + static_cast<int32_t>(w));
+      const bool indices = ok && pg.type != parquet::PAGE_DICTIONARY && pg.encoding != parquet::ENC_PLAIN;
+      s_bw = blen > 0 ? base[0] : 99;
+      if (indices && s_bw > 32) {
+        raise_status(st, GFPDB_EINVAL, 500000 + static_cast<int32_t>(w));
+        ok = 0;
       }
-      continue;
+      s_ok = indices ? ok : 0;
+      s_at = 1;
+      s_done = 0;
     }
+    __syncthreads();
+    if (!s_ok) continue;
     // Dictionary indices: a bit-width byte, then RLE / bit-packed hybrid runs.
-    int32_t bw = blen > 0 ? base[0] : 99;
-    if (bw > 32) {
-      if (lane == 0) raise_status(st, GFPDB_EINVAL, 500000 + static_cast<int32_t>(w));
-      continue;
-    }
-    int32_t at = 1, done = 0;
-    const int64_t row0 = pg.first_row;
-    while (done < pg.num_values) {
-      int32_t kind = 0, count = 0, start = 0;
-      uint32_t value = 0;
-      if (lane == 0) {
-        uint32_t h;
-        if (!run_header(base, blen, &at, &h)) {
-          kind = -1;
-        } else if (h & 1) {
-          const int64_t groups = h >> 1;
-          const int64_t bytes = groups * bw;
-          if (bytes > blen - at) {
-            kind = -1;
-          } else {
-            kind = 2;
-            start = at;
-            count = static_cast<int32_t>(groups * 8 < pg.num_values - done ? groups * 8 : pg.num_values - done);
-            at += static_cast<int32_t>(bytes);
+    base = pg.values;
+    blen = pg.values_len;
+    const int32_t bw = s_bw;
+    const uint64_t mask = bw == 32 ? 0xffffffffull : ((1ull << bw) - 1ull);
+    for (;;) {
+      if (threadIdx.x == 0) {
+        int32_t n = 0, at = s_at, done = s_done;
+        while (n < kPqRuns && done < pg.num_values) {
+          uint32_t h;
+          if (!run_header(base, blen, &at, &h)) {
+            s_ok = 0;
+            break;
           }
-        } else {
-          const int32_t vb = (bw + 7) / 8;
-          if (vb > blen - at) {
-            kind = -1;
+          int64_t count;
+          if (h & 1) {
+            const int64_t groups = h >> 1;
+            if (groups * bw > blen - at) {
+              s_ok = 0;
+              break;
+            }
+            s_start[n] = at;
+            at += static_cast<int32_t>(groups * bw);
+            count = groups * 8;
           } else {
-            kind = 1;
-            for (int k = 0; k < vb; ++k) value |= static_cast<uint32_t>(base[at + k]) << (8 * k);
+            const int32_t vb = (bw + 7) / 8;
+            if (vb > blen - at) {
+              s_ok = 0;
+              break;
+            }
+            uint32_t v = 0;
+            for (int k = 0; k < vb; ++k) v |= static_cast<uint32_t>(base[at + k]) << (8 * k);
             at += vb;
-            const int64_t c = h >> 1;
-            count = static_cast<int32_t>(c < pg.num_values - done ? c : pg.num_values - done);
+            s_start[n] = -1;
+            s_value[n] = v;
+            count = h >> 1;
           }
+          if (count <= 0) {
+            s_ok = 0;
+            break;
+          }
+          s_first[n] = done;
+          done += static_cast<int32_t>(count < pg.num_values - done ? count : pg.num_values - done);
+          ++n;
         }
-        if (kind > 0 && count <= 0) kind = -1;
+        s_first[n] = done;
+        s_n = s_ok ? n : 0;
+        s_at = at;
+        s_done = done;
+        if (!s_ok) raise_status(st, GFPDB_EINVAL, 500000 + static_cast<int32_t>(w));
       }
-      kind = __shfl_sync(0xffffffffu, kind, 0);
-      if (kind < 0) {
-        if (lane == 0) raise_status(st, GFPDB_EINVAL, 500000 + static_cast<int32_t>(w));
-        break;
-      }
-      count = __shfl_sync(0xffffffffu, count, 0);
-      if (kind == 1) {
-        value = __shfl_sync(0xffffffffu, value, 0);
-        for (int32_t i = lane; i < count; i += 32) pg.idx[row0 + done + i] = static_cast<int32_t>(value);
-      } else {
-        start = __shfl_sync(0xffffffffu, start, 0);
-        const uint64_t mask = bw == 32 ? 0xffffffffull : ((1ull << bw) - 1ull);
-        for (int32_t i = lane; i < count; i += 32) {
-          const int64_t bit = static_cast<int64_t>(i) * bw;
-          const uint8_t* q = base + start + (bit >> 3);
-          uint64_t v = 0;
+      __syncthreads();
+      const int32_t n = s_n;
+      if (n == 0) break;
+      const int32_t v0 = s_first[0], v1 = s_first[n];
+      for (int32_t v = v0 + static_cast<int32_t>(threadIdx.x); v < v1; v += kPqThreads) {
+        int32_t lo = 0, hi = n - 1;  // the run holding v: the last with s_first <= v
+        while (lo < hi) {
+          const int32_t mid = (lo + hi + 1) >> 1;
+          if (s_first[mid] <= v) lo = mid;
+          else hi = mid - 1;
+        }
+        uint32_t idx;
+        if (s_start[lo] < 0) {
+          idx = s_value[lo];
+        } else {
+          const int64_t bit = static_cast<int64_t>(v - s_first[lo]) * bw;
+          const uint8_t* q = base + s_start[lo] + (bit >> 3);
+          uint64_t x = 0;
           const int nb = (static_cast<int>(bit & 7) + bw + 7) / 8;  // bytes the value spans (within the run)
-          for (int k = 0; k < nb; ++k) v |= static_cast<uint64_t>(q[k]) << (8 * k);
-          pg.idx[row0 + done + i] = static_cast<int32_t>((v >> (bit & 7)) & mask);
+          for (int k = 0; k < nb; ++k) x |= static_cast<uint64_t>(q[k]) << (8 * k);
+          idx = static_cast<uint32_t>((x >> (bit & 7)) & mask);
         }
+        pg.idx[pg.first_row + v] = static_cast<int32_t>(idx);
       }
-      done += count;
+      const bool more = s_done < pg.num_values;
+      __syncthreads();  // the runs are read before thread 0 rewrites them
+      if (!more) break;
     }
   }
 }
@@ -410,7 +421,14 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const PageDev* page
           raise_status(st, GFPDB_EINVAL, 600000 + static_cast<int32_t>(blockIdx.y));
           continue;
         }
-        src = pg.values + i * pg.width;
+        // the value's 4-byte words from the two aligned words around each
+        // (the arena and the inflated buffer carry 16 bytes of tail padding)
+        const uint8_t* sp = pg.values + i * pg.width;
+        const uint32_t* al = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(sp) & ~uintptr_t{3});
+        const uint32_t sh = 8u * static_cast<uint32_t>(reinterpret_cast<uintptr_t>(sp) & 3u);
+        uint32_t* dw = reinterpret_cast<uint32_t*>(pg.fixed_out + row * pg.width);
+        for (int k = 0; k < pg.width / 4; ++k) dw[k] = __funnelshift_r(al[k], al[k + 1], sh);
+        continue;
       }
       copy_value(src, pg.fixed_out + row * pg.width, pg.width);
     } else if (dict) {
@@ -460,7 +478,7 @@ TupleSetPtr parquet_read(const uint8_t* file, int64_t size, const std::vector<st
     chunk_at[c] = arena_bytes;
     arena_bytes += (L.chunks[c].end - L.chunks[c].begin + 15) / 16 * 16;
   }
-  auto arena = make_buffer(arena_bytes > 0 ? arena_bytes : 16, s);
+  auto arena = make_buffer(arena_bytes + 16, s);  // tail padding: 4-byte word reads past a value's end
   for (size_t c = 0; c < L.chunks.size(); ++c)
     copy_h2d(arena->as<uint8_t>() + chunk_at[c], file + L.chunks[c].begin, L.chunks[c].end - L.chunks[c].begin, s);
 
@@ -499,7 +517,7 @@ TupleSetPtr parquet_read(const uint8_t* file, int64_t size, const std::vector<st
     }
     if (pg.type != parquet::PAGE_DICTIONARY) data_list.push_back(static_cast<int32_t>(p));
   }
-  auto inflated = make_buffer(inflate_bytes > 0 ? inflate_bytes : 16, s);
+  auto inflated = make_buffer(inflate_bytes + 16, s);
   for (size_t p = 0; p < L.pages.size(); ++p) {
     const auto& pg = L.pages[p];
     const int c = pg.column;
@@ -559,7 +577,9 @@ TupleSetPtr parquet_read(const uint8_t* file, int64_t size, const std::vector<st
   }
   if (np > 0) {
     ProfScope prof("parquet_pages_kernel", s);
-    parquet_pages_kernel<<<grid_parquet(np * 32), 256, 0, s>>>(pages, static_cast<int32_t>(np), dicts, st);
+    const int64_t most = static_cast<int64_t>(num_sms()) * 8;
+    parquet_pages_kernel<<<static_cast<int>(np < most ? np : most), kPqThreads, 0, s>>>(
+        pages, static_cast<int32_t>(np), dicts, st);
     after_launch("parquet_pages_kernel");
     prof.stop(0.0);
   }
