@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256)
   }
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
-    const uint64_t h = hash_key(load_int(key, r));
+    const uint64_t h = bloom_hash(load_int(key, r));
     uint32_t m[8];
     bloom_masks(h, num_hashes, m);
     uint32_t* blk = blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8;

@@ -23,6 +23,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
 #include <type_traits>
 
 #include "../host/handles.h"
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(kSelThreads) select_kernel(const __grid_consta
 #pragma unroll
       for (int k = 0; k < kSelItems; ++k) {
         if (!((mask >> k) & 1u)) continue;
-        const uint64_t h = hash_key(keys[k]);
+        const uint64_t h = bloom_hash(keys[k]);
         const uint32_t blk = bloom_block_of(h, nb);
         bool ok;
         if (in_smem) {
@@ -449,7 +450,8 @@ constexpr int kPwThreads = 256;                 // 8 warps
 constexpr int kGatherSlices = kSelThreads;     // slices per range of the gather pass (one per thread)
 constexpr int kPwRows = 32 * kSelItems;         // rows per warp slice
 constexpr int64_t kSpMinRows = int64_t{1} << 20;  // below this select_kernel's tiles all start at once
-constexpr int64_t kSpMaxDynamic = 96 * 1024;    // the first filter in shared memory
+constexpr int64_t kSpMaxDynamic = 96 * 1024;    // the staged filters in shared memory
+static_assert(kBloomSmemBudget <= kSpMaxDynamic, "the filters' shared-memory layout fits a probe launch");
 
 // The first probe over a thread's 8 rows: the bloom test of each key with NH
 // hashes, bit positions from the low 32 bits of the key's hash (bloom.cuh).
@@ -461,7 +463,7 @@ __device__ __forceinline__ uint32_t probe8(const uint32_t* blocks, uint32_t nb, 
   uint32_t keep = 0;
 #pragma unroll
   for (int kk = 0; kk < kSelItems; ++kk) {
-    const uint64_t h = hash_key(keys[kk]);
+    const uint64_t h = bloom_hash(keys[kk]);
     const uint32_t* blk = blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8;
     const uint32_t lo = static_cast<uint32_t>(h);
     uint32_t ok = 1u;
@@ -495,14 +497,17 @@ struct StreamPred {
 };
 
 // kPred = false compiles the probe-only form, which needs fewer registers.
-template <bool kPred>
+// kLater: the number of probes after the first (1 to 3, their loop unrolled
+// exactly), 0 for none, -1 for more (a loop over up to kMaxBlooms - 1).
+template <bool kPred, int kLater>
 __global__ void __launch_bounds__(kPwThreads, kPred ? 4 : 5) select_probe_kernel(const __grid_constant__ SelectParams p,
                                                                   const __grid_constant__ StreamPred sp,
                                                                   int32_t* __restrict__ rowlist,
                                                                   unsigned int* __restrict__ range_totals) {
-  extern __shared__ __align__(16) uint32_t s_filter[];  // the first probe's filter, when staged
+  extern __shared__ __align__(16) uint32_t s_filter[];  // the staged filters, at their smem_word
   __shared__ uint16_t s_list[kPwThreads / 32][kPwRows];  // per warp: its slice's survivors
   __shared__ uint32_t s_nblocks[kMaxBlooms];
+  __shared__ const uint32_t* s_blocks[kMaxBlooms];  // each filter's blocks: shared memory when staged
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int64_t n_rows = clamp_rows(p.n_dev, p.n_rows);
@@ -517,10 +522,12 @@ __global__ void __launch_bounds__(kPwThreads, kPred ? 4 : 5) select_probe_kernel
     if (threadIdx.x == 0) s_nblocks[pi] = nb;
     const bool v = b.valid_dev ? (*b.valid_dev != 0) : (b.valid != 0);
     if (v) valid |= 1u << pi;
-    if (pi == 0 && v && b.smem_word >= 0 && nb * 8 <= static_cast<uint32_t>(b.smem_cap_words)) {
-      staged = true;
+    const bool stage = v && b.smem_word >= 0 && nb * 8 <= static_cast<uint32_t>(b.smem_cap_words);
+    if (threadIdx.x == 0) s_blocks[pi] = stage ? s_filter + b.smem_word : b.blocks;
+    if (stage) {
+      if (pi == 0) staged = true;
       const uint4* src = reinterpret_cast<const uint4*>(b.blocks);
-      uint4* dst = reinterpret_cast<uint4*>(s_filter);
+      uint4* dst = reinterpret_cast<uint4*>(s_filter + b.smem_word);
       for (uint32_t i = threadIdx.x; i < nb * 2; i += kPwThreads) dst[i] = __ldg(src + i);
     }
   }
@@ -590,32 +597,30 @@ __global__ void __launch_bounds__(kPwThreads, kPred ? 4 : 5) select_probe_kernel
       __syncwarp();
     }
     // (3) the later probes over the list, compacted in place (order kept: a
-    // compacted position never passes the position it was read from)
-    if (p.n_probes > 1 && n_alive > 0) {
+    // compacted position never passes the position it was read from); each
+    // survivor's later keys are loaded together, the filters tested from
+    // shared memory where staged
+    if (kLater != 0 && n_alive > 0) {
+      constexpr int NL = kLater > 0 ? kLater : kMaxBlooms - 1;
+      const int nl = kLater > 0 ? kLater : p.n_probes - 1;
       int m = 0;
       for (int base = 0; base < n_alive; base += 32) {
         const int idx = base + lane;
         bool alive = idx < n_alive;
         const int r = alive ? list[idx] : 0;
-        int64_t later[kMaxBlooms - 1];
+        int64_t later[NL];
 #pragma unroll
-        for (int j = 0; j < kMaxBlooms - 1; ++j) {
+        for (int j = 0; j < NL; ++j) {
           const int pi = j + 1;
-          later[j] = (alive && pi < p.n_probes && ((valid >> pi) & 1u))
-                         ? load_int(p.cols[p.probes[pi].col], start + r) : 0;
+          later[j] = (j < nl && alive && ((valid >> pi) & 1u)) ? load_int(p.cols[p.probes[pi].col], start + r) : 0;
         }
 #pragma unroll
-        for (int j = 0; j < kMaxBlooms - 1; ++j) {
+        for (int j = 0; j < NL; ++j) {
           const int pi = j + 1;
-          if (alive && pi < p.n_probes && ((valid >> pi) & 1u)) {
-            const BloomDev& b = p.probes[pi];
-            const uint64_t h = hash_key(later[j]);
-            const uint4* words =
-                reinterpret_cast<const uint4*>(b.blocks + static_cast<uint64_t>(bloom_block_of(h, s_nblocks[pi])) * 8);
-            const uint4 lo = __ldg(words);
-            const uint4 hi = __ldg(words + 1);
-            const uint32_t wv[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-            alive = bloom_test(wv, h, b.num_hashes);
+          if (j < nl && alive && ((valid >> pi) & 1u)) {
+            const uint64_t h = bloom_hash(later[j]);
+            const uint32_t* blk = s_blocks[pi] + static_cast<uint64_t>(bloom_block_of(h, s_nblocks[pi])) * 8;
+            alive = bloom_test(blk, h, p.probes[pi].num_hashes);
           }
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, alive);
@@ -691,22 +696,34 @@ __global__ void __launch_bounds__(kSelThreads) select_gather_kernel(const __grid
   }
 }
 
-int select_probe_blocks_per_sm(bool with_pred, size_t dyn) {
+using ProbeKernel = void (*)(SelectParams, StreamPred, int32_t*, unsigned int*);
+
+// The instantiation for a predicate (or none) and a number of later probes.
+ProbeKernel select_probe_fn(bool with_pred, int n_later) {
+  const int k = n_later <= 3 ? n_later : 4;
+  static const ProbeKernel table[2][5] = {
+      {select_probe_kernel<false, 0>, select_probe_kernel<false, 1>, select_probe_kernel<false, 2>,
+       select_probe_kernel<false, 3>, select_probe_kernel<false, -1>},
+      {select_probe_kernel<true, 0>, select_probe_kernel<true, 1>, select_probe_kernel<true, 2>,
+       select_probe_kernel<true, 3>, select_probe_kernel<true, -1>}};
+  return table[with_pred ? 1 : 0][k];
+}
+
+int select_probe_blocks_per_sm(ProbeKernel fn, size_t dyn) {
   static std::mutex mu;
-  static std::map<std::pair<bool, size_t>, int> cache;
-  static bool attr_set[2] = {false, false};
+  static std::map<std::pair<const void*, size_t>, int> cache;
+  static std::set<const void*> attr_set;
   std::lock_guard<std::mutex> lk(mu);
-  const auto key = std::make_pair(with_pred, dyn);
+  const void* f = reinterpret_cast<const void*>(fn);
+  const auto key = std::make_pair(f, dyn);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  const void* fn = with_pred ? reinterpret_cast<const void*>(select_probe_kernel<true>)
-                             : reinterpret_cast<const void*>(select_probe_kernel<false>);
-  if (!attr_set[with_pred]) {
-    GF_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSpMaxDynamic)));
-    attr_set[with_pred] = true;
+  if (!attr_set.count(f)) {
+    GF_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSpMaxDynamic)));
+    attr_set.insert(f);
   }
   int per_sm = 0;
-  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPwThreads, dyn));
+  GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kPwThreads, dyn));
   cache[key] = per_sm;
   return per_sm;
 }
@@ -843,7 +860,7 @@ __global__ void __launch_bounds__(kLiteThreads) select_lite_kernel(const __grid_
 #pragma unroll
       for (int k = 0; k < kLiteItems; ++k) {
         if (!((mask >> k) & 1u)) continue;
-        const uint64_t h = hash_key(keys[k]);
+        const uint64_t h = bloom_hash(keys[k]);
         const uint4* words = reinterpret_cast<const uint4*>(pr.blocks + static_cast<uint64_t>(bloom_block_of(h, nb)) * 8);
         const uint4 lo = __ldg(words);
         const uint4 hi = __ldg(words + 1);
@@ -1088,9 +1105,12 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
     prof.set_bytes_model(p.n_dev, n, read_all, &p.status->value, proj_read + proj_write, scratch, in.rows_owner());
   } else if (n_tiles > 0 && two_pass) {
     // pass 1: probes; each slice's selected row ids into its part of rowlist
-    const size_t dyn = p.probes[0].smem_word >= 0 ? static_cast<size_t>(p.probes[0].smem_cap_words) * 4 : 0;
+    // every filter that fits is staged (the layout stays within
+    // kBloomSmemBudget, which is kSpMaxDynamic)
+    const size_t dyn = static_cast<size_t>(p.smem_words) * 4;
     const bool with_pred = spred.n_leaves > 0;
-    const int per_sm = select_probe_blocks_per_sm(with_pred, dyn);
+    const ProbeKernel fn = select_probe_fn(with_pred, p.n_probes > 0 ? p.n_probes - 1 : 0);
+    const int per_sm = select_probe_blocks_per_sm(fn, dyn);
     auto rowlist = make_buffer(n * 4, s);
     const int64_t n_ranges = (n_tiles + kGatherSlices - 1) / kGatherSlices;
     auto range_totals = make_filled(n_ranges * 4, 0, s);
@@ -1099,12 +1119,7 @@ TupleSetPtr select_rows(const TupleSet& in, const CompiledPredicate* pred, const
       const int64_t cap = static_cast<int64_t>(num_sms()) * (per_sm > 0 ? per_sm : 1);
       ProfScope prof("select_probe_kernel", s);
       const int grid = static_cast<int>(want < cap ? want : cap);
-      if (with_pred)
-        select_probe_kernel<true><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>(),
-                                                                range_totals->as<unsigned int>());
-      else
-        select_probe_kernel<false><<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>(),
-                                                                 range_totals->as<unsigned int>());
+      fn<<<grid, kPwThreads, dyn, s>>>(p, spred, rowlist->as<int32_t>(), range_totals->as<unsigned int>());
       after_launch("select_probe_kernel");
       prof.stop(0);
       // the predicate's columns and the first probe's keys over all rows

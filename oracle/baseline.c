@@ -42,6 +42,11 @@ static uint64_t mix64(uint64_t k) {
 }
 
 static uint64_t hash_key(int64_t v) { return mix64((uint64_t)v ^ 0x9e3779b97f4a7c15ULL); }
+/* the filters' hash: Fibonacci hashing, the high bits folded into the low */
+static uint64_t bloom_hash(int64_t v) {
+  const uint64_t h = (uint64_t)v * 0x9e3779b97f4a7c15ULL;
+  return h ^ (h >> 29);
+}
 
 typedef struct {
   uint32_t* words;
@@ -58,7 +63,7 @@ static void bloom_init(bloom* b, int64_t n, int bits, int nh) {
 }
 
 static void bloom_add(bloom* b, int64_t key) {
-  uint64_t h = hash_key(key);
+  uint64_t h = bloom_hash(key);
   uint64_t blk = ((h >> 32) * b->nblocks) >> 32;
   for (int i = 0; i < b->nh; ++i) {
     uint32_t bit = (uint32_t)(h >> (8 * i)) & 0xFF;
@@ -67,7 +72,7 @@ static void bloom_add(bloom* b, int64_t key) {
 }
 
 static int bloom_has(const bloom* b, int64_t key) {
-  uint64_t h = hash_key(key);
+  uint64_t h = bloom_hash(key);
   uint64_t blk = ((h >> 32) * b->nblocks) >> 32;
   for (int i = 0; i < b->nh; ++i) {
     uint32_t bit = (uint32_t)(h >> (8 * i)) & 0xFF;

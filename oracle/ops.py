@@ -133,6 +133,14 @@ def shuffle(table: Table, keys, num_slots: int) -> tuple[Table, list[int]]:
     return take(table, order), [0] + np.cumsum(counts).tolist()
 
 
+def bloom_hash(v: np.ndarray) -> np.ndarray:
+    """The filter's key hash: a multiply by 2^64 / phi (Fibonacci hashing),
+    then the high bits folded into the low ones (h ^ h >> 29)."""
+    with np.errstate(over="ignore"):
+        h = np.asarray(v).astype(np.int64).view(np.uint64) * _U(0x9E3779B97F4A7C15)
+        return h ^ (h >> _U(29))
+
+
 def bloom_num_blocks(n_keys: int, bits_per_key: int) -> int:
     return max(1, (n_keys * bits_per_key + 255) // 256)
 
@@ -140,7 +148,7 @@ def bloom_num_blocks(n_keys: int, bits_per_key: int) -> int:
 def bloom_words(keys: np.ndarray, bits_per_key: int = 10, num_hashes: int = 3) -> np.ndarray:
     nb = bloom_num_blocks(len(keys), bits_per_key)
     words = np.zeros(nb * 8, dtype=np.uint32)
-    h = hash_key(keys)
+    h = bloom_hash(keys)
     blk = ((h >> _U(32)) * _U(nb)) >> _U(32)
     for i in range(num_hashes):
         b = (h >> _U(8 * i)) & _U(0xFF)
@@ -152,7 +160,7 @@ def bloom_words(keys: np.ndarray, bits_per_key: int = 10, num_hashes: int = 3) -
 
 def bloom_contains(words: np.ndarray, keys: np.ndarray, num_hashes: int = 3) -> np.ndarray:
     nb = len(words) // 8
-    h = hash_key(keys)
+    h = bloom_hash(keys)
     blk = ((h >> _U(32)) * _U(nb)) >> _U(32)
     ok = np.ones(len(keys), dtype=bool)
     for i in range(num_hashes):
