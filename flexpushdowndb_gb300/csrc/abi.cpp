@@ -1535,6 +1535,22 @@ int32_t gfpdb_plan_validate(const char* plan_json) {
   });
 }
 
+int32_t gfpdb_plan_fuse(const char* plan_json, char* out_json, int64_t capacity, int64_t* needed) {
+  return guarded([&] {
+    require(plan_json != nullptr && needed != nullptr, "null argument");
+    json::Value plan;
+    try {
+      plan = json::parse(plan_json);
+    } catch (const std::exception& e) {
+      fail(GFPDB_EINVAL, e.what());
+    }
+    const std::string out = json::dump(pop::fuse_pipelines(plan));
+    *needed = static_cast<int64_t>(out.size()) + 1;
+    if (out_json == nullptr || capacity < *needed) fail(GFPDB_EINVAL, "output buffer too small (see *needed)");
+    std::memcpy(out_json, out.c_str(), out.size() + 1);
+  });
+}
+
 int32_t gfpdb_plan_predicate_transfer(const char* spec_json, char* out_json, int64_t capacity, int64_t* needed) {
   return guarded([&] {
     require(spec_json != nullptr && needed != nullptr, "null argument");

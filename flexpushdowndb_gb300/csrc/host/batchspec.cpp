@@ -90,57 +90,6 @@ cudaGraphExec_t capture_star_batch(StarBatch& b, uint64_t* kernels) {
   return exec;
 }
 
-namespace {
-void dump_to(const json::Value& v, std::string& out) {
-  switch (v.kind) {
-    case json::Value::Null: out += "null"; break;
-    case json::Value::Bool: out += v.b ? "true" : "false"; break;
-    case json::Value::Number:
-      if (v.is_integer) {
-        out += std::to_string(v.i);
-      } else {
-        char buf[40];
-        std::snprintf(buf, sizeof(buf), "%.17g", v.d);
-        out += buf;
-      }
-      break;
-    case json::Value::String:
-      out += '"';
-      for (char c : v.s) {
-        if (c == '"' || c == '\\') out += '\\';
-        out += c;
-      }
-      out += '"';
-      break;
-    case json::Value::Array:
-      out += '[';
-      for (size_t i = 0; i < v.a.size(); ++i) {
-        if (i) out += ',';
-        dump_to(v.a[i], out);
-      }
-      out += ']';
-      break;
-    case json::Value::Object:
-      out += '{';
-      for (size_t i = 0; i < v.o.size(); ++i) {
-        if (i) out += ',';
-        json::Value k;
-        k.kind = json::Value::String;
-        k.s = v.o[i].first;
-        dump_to(k, out);
-        out += ':';
-        dump_to(v.o[i].second, out);
-      }
-      out += '}';
-      break;
-  }
-}
-}  // namespace
-
-std::string json_dump(const json::Value& v) {
-  std::string out;
-  dump_to(v, out);
-  return out;
-}
+std::string json_dump(const json::Value& v) { return json::dump(v); }
 
 }  // namespace gfpdb

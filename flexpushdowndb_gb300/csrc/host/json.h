@@ -6,6 +6,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -232,5 +233,71 @@ class Parser {
 };
 
 inline Value parse(const std::string& text) { return Parser(text).parse(); }
+
+// The value as JSON text (object keys in insertion order; strings escaped,
+// bytes >= 0x80 passed through as they are).
+inline void dump_to(const Value& v, std::string& out) {
+  switch (v.kind) {
+    case Value::Null: out += "null"; break;
+    case Value::Bool: out += v.b ? "true" : "false"; break;
+    case Value::Number: {
+      if (v.is_integer) {
+        out += std::to_string(v.i);
+      } else {
+        char buf[32];
+        std::snprintf(buf, sizeof(buf), "%.17g", v.d);
+        out += buf;
+      }
+      break;
+    }
+    case Value::String: {
+      out += '"';
+      for (char c : v.s) {
+        const unsigned char u = static_cast<unsigned char>(c);
+        if (c == '"' || c == '\\') {
+          out += '\\';
+          out += c;
+        } else if (u < 0x20) {
+          char buf[8];
+          std::snprintf(buf, sizeof(buf), "\\u%04x", u);
+          out += buf;
+        } else {
+          out += c;
+        }
+      }
+      out += '"';
+      break;
+    }
+    case Value::Array: {
+      out += '[';
+      for (size_t k = 0; k < v.a.size(); ++k) {
+        if (k) out += ',';
+        dump_to(v.a[k], out);
+      }
+      out += ']';
+      break;
+    }
+    case Value::Object: {
+      out += '{';
+      for (size_t k = 0; k < v.o.size(); ++k) {
+        if (k) out += ',';
+        Value key;
+        key.kind = Value::String;
+        key.s = v.o[k].first;
+        dump_to(key, out);
+        out += ':';
+        dump_to(v.o[k].second, out);
+      }
+      out += '}';
+      break;
+    }
+  }
+}
+
+inline std::string dump(const Value& v) {
+  std::string out;
+  dump_to(v, out);
+  return out;
+}
 
 }  // namespace gfpdb::json

@@ -173,11 +173,17 @@ class FilterPOp : public PhysicalOp {
 // forwards every TupleSet to its ordinary consumers, keeps the key columns,
 // and once all producers are complete builds the filter on the device and
 // sends it to the BloomFilterUsePOps.
+//
+// The ordinary consumers are every consumer that is not a filter receiver,
+// or, when the plan lists them ("dataConsumers", which the pipeline fusion
+// writes once a join may both take this operator's rows and receive its
+// filter), exactly those.
 class BloomFilterCreatePOp : public PhysicalOp {
  public:
-  BloomFilterCreatePOp(std::string name, std::string column, int bits, int hashes, std::vector<std::string> uses)
+  BloomFilterCreatePOp(std::string name, std::string column, int bits, int hashes, std::vector<std::string> uses,
+                       std::optional<std::vector<std::string>> data_consumers = std::nullopt)
       : PhysicalOp(std::move(name), "BloomFilterCreatePOp"), column_(std::move(column)), bits_(bits),
-        hashes_(hashes), uses_(std::move(uses)) {}
+        hashes_(hashes), uses_(std::move(uses)), data_consumers_(std::move(data_consumers)) {}
 
   void onReceive(const Envelope& env) override {
     const Message& m = env.getMessage();
@@ -185,8 +191,11 @@ class BloomFilterCreatePOp : public PhysicalOp {
       m.tuples->require_column(column_);
       buffered_.push_back(m.tuples);
       std::vector<std::string> pass;
-      for (auto& c : consumers_)
-        if (std::find(uses_.begin(), uses_.end(), c) == uses_.end()) pass.push_back(c);
+      if (data_consumers_)
+        pass = *data_consumers_;
+      else
+        for (auto& c : consumers_)
+          if (std::find(uses_.begin(), uses_.end(), c) == uses_.end()) pass.push_back(c);
       Message out;
       out.type = MessageType::TUPLESET;
       out.tuples = m.tuples;
@@ -213,6 +222,7 @@ class BloomFilterCreatePOp : public PhysicalOp {
   std::string column_;
   int bits_, hashes_;
   std::vector<std::string> uses_;
+  std::optional<std::vector<std::string>> data_consumers_;
   std::vector<TupleSetPtr> buffered_;
 };
 
@@ -359,18 +369,42 @@ TupleSetPtr probe_join(const std::string& join_name, const JoinTable& table, con
 
 }  // namespace
 
+TupleSetPtr filter_build_side(const TupleSetPtr& build, const std::string& key, const std::vector<BloomProbe>& filters,
+                              cudaStream_t s, std::vector<BloomPtr>* in_build) {
+  in_build->clear();
+  if (filters.empty()) return build;
+  bool on_key = !key.empty() && filters.size() <= static_cast<size_t>(kJoinBuildFiltersMax);
+  if (on_key) {
+    const DType kt = build->field(build->require_column(key)).type;
+    on_key = kt == DType::Int32 || kt == DType::Int64 || kt == DType::Date32;
+  }
+  for (auto& f : filters) on_key &= f.column == key;
+  if (on_key) {
+    for (auto& f : filters) in_build->push_back(f.bloom);
+    return build;
+  }
+  return select_rows(*build, nullptr, filters, {}, true, s);
+}
+
 // The join table over a build side: keyed on its single key column, or on
 // the composite of several (with the key columns aliased for the equality
 // check that probe_join_multi makes).
-JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::string>& keys, double load_factor,
-                           cudaStream_t s, bool mark) {
+JoinTable build_join_table(const TupleSetPtr& build_in, const std::vector<std::string>& keys, double load_factor,
+                           cudaStream_t s, bool mark, const std::vector<BloomProbe>& filters) {
   JoinTable t;
+  std::vector<BloomPtr> in_build;
+  TupleSetPtr build = filter_build_side(build_in, keys.size() == 1 && !mark ? keys[0] : std::string(), filters, s,
+                                        &in_build);
+  // A marking join reads its build rows' flags back by row (the rows of an
+  // outer join that no probe row matched): its build side needs its exact
+  // row count, not a device-sized capacity.
+  if (mark) build = resolved(build, s);
   // a utf8 key, like several key columns, is joined on its hash and checked
   // on the key itself
   t.composite = keys.size() > 1 || build->field(build->require_column(keys[0])).type == DType::Utf8;
   t.build = t.composite ? with_composite_key(build, keys, kBuildKeyColumn, kBuildKeyAlias, s) : build;
   t.key_col = t.build->require_column(t.composite ? std::string(kBuildKeyColumn) : keys[0]);
-  join_build_table(t, load_factor, s);
+  join_build_table(t, load_factor, s, in_build);
   if (mark) {
     if (t.composite)
       fail(GFPDB_EUNSUPPORTED, "outer and semi joins take one integer key column per side");
@@ -550,6 +584,52 @@ TupleSetPtr join_finish_kind(const std::string& join_name, JoinKind kind, const 
 
 namespace {
 
+// The bloom filters a join build tests (predicate transfer's backward
+// filters on a dimension, moved into the join by the plan's pipeline fusion,
+// fuse_build_filters): per filter the build column it tests and the
+// BloomFilterCreatePOp that sends it.
+struct BuildFilterSpec {
+  std::vector<std::string> columns, creators;
+  std::vector<BloomPtr> blooms;
+
+  bool takes(const std::string& sender) const {
+    return std::find(creators.begin(), creators.end(), sender) != creators.end();
+  }
+  void receive(const std::string& op, const Message& m) {
+    auto it = std::find(creators.begin(), creators.end(), m.sender);
+    if (it == creators.end()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + op + "': bloom filter from '" + m.sender + "'");
+    blooms[static_cast<size_t>(it - creators.begin())] = m.bloom;
+  }
+  bool ready() const {
+    for (auto& b : blooms)
+      if (!b) return false;
+    return true;
+  }
+  void require_all(const std::string& op) const {
+    if (!ready()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + op + "': producers completed without its bloom filters");
+  }
+  std::vector<BloomProbe> probes() const {
+    std::vector<BloomProbe> p;
+    for (size_t i = 0; i < columns.size(); ++i) p.push_back(BloomProbe{blooms[i], columns[i]});
+    return p;
+  }
+  void reset() {
+    for (auto& b : blooms) b.reset();
+  }
+};
+
+// "buildFilters": [{"column": c, "creator": op}, ...]
+BuildFilterSpec parse_build_filters(const json::Value& o) {
+  BuildFilterSpec f;
+  if (!o.contains("buildFilters")) return f;
+  for (auto& e : o.at("buildFilters").array()) {
+    f.columns.push_back(e.at("column").str());
+    f.creators.push_back(e.at("creator").str());
+  }
+  f.blooms.resize(f.columns.size());
+  return f;
+}
+
 // HashJoinArrowPOp (fpdb-executor/src/physical/join/hashjoin/HashJoinArrowPOp.cpp:85-153):
 // routes TupleSets by sender to the build or probe side, builds the table
 // once every build producer is complete, probes as probe input arrives.
@@ -557,10 +637,10 @@ class HashJoinArrowPOp : public PhysicalOp {
  public:
   HashJoinArrowPOp(std::string name, std::vector<std::string> build_producers, std::vector<std::string> probe_producers,
                    std::vector<std::string> build_keys, std::vector<std::string> probe_keys, double load_factor,
-                   JoinKind kind = JoinKind::Inner)
+                   JoinKind kind = JoinKind::Inner, BuildFilterSpec filters = {})
       : PhysicalOp(std::move(name), "HashJoinArrowPOp"), build_producers_(std::move(build_producers)),
         probe_producers_(std::move(probe_producers)), build_keys_(std::move(build_keys)),
-        probe_keys_(std::move(probe_keys)), load_factor_(load_factor), kind_(kind) {
+        probe_keys_(std::move(probe_keys)), load_factor_(load_factor), kind_(kind), filters_(std::move(filters)) {
     if (build_keys_.empty() || build_keys_.size() != probe_keys_.size())
       fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': as many probe keys as build keys, at least one");
   }
@@ -575,17 +655,16 @@ class HashJoinArrowPOp : public PhysicalOp {
         if (built_) probe(m.tuples);
         else probe_buffer_.push_back(m.tuples);
       }
+    } else if (m.type == MessageType::BLOOM_FILTER) {
+      filters_.receive(name_, m);
+      maybeBuild();
     } else if (m.type == MessageType::COMPLETE) {
-      auto& dir = ctx()->operatorMap();
-      bool build_done = true;
-      for (auto& b : build_producers_) build_done &= dir.isComplete(b);
-      if (build_done && !built_) {
-        finalizeBuild();
-        for (auto& t : probe_buffer_) probe(t);
-        probe_buffer_.clear();
-      }
+      maybeBuild();
       if (is_producer_complete(*this)) {
-        if (!built_) finalizeBuild();
+        if (!built_) {
+          filters_.require_all(name_);
+          finalizeBuild();
+        }
         // outer and semi joins: the build rows decided once every probe row is in
         Message out;
         out.type = MessageType::TUPLESET;
@@ -601,6 +680,7 @@ class HashJoinArrowPOp : public PhysicalOp {
     probe_buffer_.clear();
     table_ = JoinTable{};
     built_ = false;
+    filters_.reset();
   }
 
  private:
@@ -608,10 +688,22 @@ class HashJoinArrowPOp : public PhysicalOp {
     return std::find(build_producers_.begin(), build_producers_.end(), sender) != build_producers_.end();
   }
 
+  // The table is built once every build producer is complete and every
+  // bloom filter the build tests has arrived; buffered probes follow.
+  void maybeBuild() {
+    if (built_ || !filters_.ready()) return;
+    auto& dir = ctx()->operatorMap();
+    for (auto& b : build_producers_)
+      if (!dir.isComplete(b)) return;
+    finalizeBuild();
+    for (auto& t : probe_buffer_) probe(t);
+    probe_buffer_.clear();
+  }
+
   void finalizeBuild() {
     if (build_.empty()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + name_ + "': no build-side input");
     table_ = build_join_table(TupleSet::concatenate(build_, ctx()->stream()), build_keys_, load_factor_,
-                              ctx()->stream(), join_kind_marks(kind_));
+                              ctx()->stream(), join_kind_marks(kind_), filters_.probes());
     build_.clear();
     built_ = true;
   }
@@ -628,6 +720,7 @@ class HashJoinArrowPOp : public PhysicalOp {
   std::vector<std::string> build_keys_, probe_keys_;
   double load_factor_;
   JoinKind kind_;
+  BuildFilterSpec filters_;
   std::vector<TupleSetPtr> build_, probe_buffer_;
   std::vector<Field> probe_fields_;  // the probe side's schema (null columns of unmatched build rows)
   JoinTable table_;
@@ -649,6 +742,7 @@ struct ChainJoinSpec {
   std::string build_key, probe_key;
   double load_factor = 0.5;
   std::vector<std::string> proj;
+  BuildFilterSpec filters;
 };
 
 class HashJoinChainPOp : public PhysicalOp {
@@ -675,21 +769,17 @@ class HashJoinChainPOp : public PhysicalOp {
       if (build) return;
       if (allBuilt()) process(m.tuples);
       else probe_buffer_.push_back(m.tuples);
+    } else if (m.type == MessageType::BLOOM_FILTER) {
+      bool taken = false;
+      for (auto& J : joins_)
+        if (J.filters.takes(m.sender)) {
+          J.filters.receive(J.name, m);
+          taken = true;
+        }
+      if (!taken) fail(GFPDB_EINVAL, "HashJoinChainPOp '" + name_ + "': bloom filter from '" + m.sender + "'");
+      advance();
     } else if (m.type == MessageType::COMPLETE) {
-      auto& dir = ctx()->operatorMap();
-      for (size_t l = 0; l < joins_.size(); ++l) {
-        if (built_[l]) continue;
-        bool done = true;
-        for (auto& b : joins_[l].build_producers) done &= dir.isComplete(b);
-        if (done) finalizeBuild(l);
-      }
-      if (is_producer_complete(*this))
-        for (size_t l = 0; l < joins_.size(); ++l)
-          if (!built_[l]) finalizeBuild(l);
-      if (allBuilt()) {
-        for (auto& t : probe_buffer_) process(t);
-        probe_buffer_.clear();
-      }
+      advance();
       if (is_producer_complete(*this)) {
         joinBuilds();
         // The tables were allocated on the build streams and are freed there
@@ -708,10 +798,31 @@ class HashJoinChainPOp : public PhysicalOp {
     for (auto& b : build_) b.clear();
     probe_buffer_.clear();
     for (auto& t : tables_) t = JoinTable{};
+    for (auto& J : joins_) J.filters.reset();
   }
 
  private:
   bool allBuilt() const { return std::all_of(built_.begin(), built_.end(), [](bool b) { return b; }); }
+
+  // Builds every table whose build side is complete and whose bloom filters
+  // have arrived (all of them once every producer is complete), then runs
+  // the buffered probes when the last table is built.
+  void advance() {
+    auto& dir = ctx()->operatorMap();
+    const bool all_done = is_producer_complete(*this);
+    for (size_t l = 0; l < joins_.size(); ++l) {
+      if (built_[l]) continue;
+      if (all_done) joins_[l].filters.require_all(joins_[l].name);
+      if (!joins_[l].filters.ready()) continue;
+      bool done = true;
+      for (auto& b : joins_[l].build_producers) done &= dir.isComplete(b);
+      if (done || all_done) finalizeBuild(l);
+    }
+    if (allBuilt()) {
+      for (auto& t : probe_buffer_) process(t);
+      probe_buffer_.clear();
+    }
+  }
 
   // Each join's table is built on a stream of its own (its inputs were
   // waited for on this operator's stream, which the build stream joins
@@ -722,9 +833,11 @@ class HashJoinChainPOp : public PhysicalOp {
     if (build_[l].empty()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + J.name + "': no build-side input");
     cudaStream_t bs = ctx()->sideStream(static_cast<int>(l));
     ctx()->streamWait(bs, ctx()->stream());
-    tables_[l].build = TupleSet::concatenate(build_[l], bs);
+    std::vector<BloomPtr> in_build;
+    tables_[l].build = filter_build_side(TupleSet::concatenate(build_[l], bs), J.build_key, J.filters.probes(), bs,
+                                         &in_build);
     tables_[l].key_col = tables_[l].build->require_column(J.build_key);
-    join_build_table(tables_[l], J.load_factor, bs);
+    join_build_table(tables_[l], J.load_factor, bs, in_build);
     build_streams_.push_back(bs);
     if (std::find(used_streams_.begin(), used_streams_.end(), bs) == used_streams_.end()) used_streams_.push_back(bs);
     build_[l].clear();
@@ -1524,7 +1637,10 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
     op = std::make_unique<BloomFilterCreatePOp>(name, o.at("bloomFilterColumn").str(),
                                                 static_cast<int>(o.get_int("bitsPerKey", 10)),
                                                 static_cast<int>(o.get_int("numHashes", 3)),
-                                                o.str_list("bloomFilterUsePOps"));
+                                                o.str_list("bloomFilterUsePOps"),
+                                                o.contains("dataConsumers")
+                                                    ? std::optional<std::vector<std::string>>(o.str_list("dataConsumers"))
+                                                    : std::nullopt);
   } else if (type == "BloomFilterUsePOp") {
     std::vector<std::string> cols = o.contains("bloomFilterColumns") ? o.str_list("bloomFilterColumns")
                                                                      : std::vector<std::string>{o.at("bloomFilterColumn").str()};
@@ -1543,7 +1659,8 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
     if (kind != JoinKind::Inner && bk.size() != 1)
       fail(GFPDB_EUNSUPPORTED, "HashJoinArrowPOp '" + name + "': outer and semi joins take one key column per side");
     op = std::make_unique<HashJoinArrowPOp>(name, o.str_list("buildProducers"), o.str_list("probeProducers"),
-                                            std::move(bk), std::move(pk), o.get_num("loadFactor", 0.5), kind);
+                                            std::move(bk), std::move(pk), o.get_num("loadFactor", 0.5), kind,
+                                            parse_build_filters(o));
   } else if (type == "HashJoinChainPOp") {
     std::vector<ChainJoinSpec> joins;
     for (auto& j : o.at("joins").array()) {
@@ -1556,6 +1673,7 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
       c.probe_key = j.at("probeKey").str();
       c.load_factor = j.get_num("loadFactor", 0.5);
       c.proj = j.str_list("projectColumnNames");
+      c.filters = parse_build_filters(j);
       joins.push_back(std::move(c));
     }
     op = std::make_unique<HashJoinChainPOp>(name, std::move(joins));
@@ -1739,7 +1857,12 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
       if (cons.size() != 1) continue;
       for (size_t j = 0; j < ops.size(); ++j) {
         if (j == i || ops[j].at("type").str() != "BloomFilterUsePOp" || ops[j].at("name").str() != cons[0]) continue;
-        if (producers[cons[0]] != std::vector<std::string>{ops[i].at("name").str()}) break;
+        // the next one's data producers: its producers other than its filters' creators
+        std::vector<std::string> data;
+        const auto cj = creators_of(ops[j]);
+        for (auto& p : producers[cons[0]])
+          if (std::find(cj.begin(), cj.end(), p) == cj.end()) data.push_back(p);
+        if (data != std::vector<std::string>{ops[i].at("name").str()}) break;
         if (creators_of(ops[i]).size() != columns_of(ops[i]).size()) break;
         if (creators_of(ops[j]).size() != columns_of(ops[j]).size()) break;
         first = static_cast<int>(i);
@@ -1758,7 +1881,7 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
     jset(ops[second], "bloomFilterColumns", jlist(cols));
     jset(ops[second], "creators", jlist(crs));
     for (auto& o : ops) {
-      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers"}) {
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"}) {
         json::Value* l = jfind(o, key);
         if (l == nullptr) continue;
         std::vector<std::string> v = o.str_list(key), nv;
@@ -1770,6 +1893,111 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
       }
     }
     ops.erase(ops.begin() + first);
+  }
+  return out;
+}
+
+// Pipeline fusion: a BloomFilterUsePOp whose only consumer is an inner
+// HashJoinArrowPOp on one key column, which takes it on its build side, and
+// whose filters are all on that key, is folded into the join: its data
+// producers feed the join's build side directly, its filters' creators send
+// them to the join ("buildFilters"), and the join build leaves out the rows
+// a filter rejects (join_build_table) instead of a selection pass copying
+// the rows that pass. Results are unchanged: an inner join emits a build row
+// only with a probe row that finds it, and the rows the selection would have
+// dropped are never found. Each creator's ordinary consumers are written out
+// ("dataConsumers") first, since the join may also take the creator's rows.
+json::Value fuse_build_filters(const json::Value& plan) {
+  json::Value out = plan;
+  json::Value* ops_v = jfind(out, "ops");
+  if (ops_v == nullptr) return out;
+  auto& ops = ops_v->a;
+  auto index_of = [&](const std::string& name) {
+    for (size_t i = 0; i < ops.size(); ++i)
+      if (ops[i].at("name").str() == name) return static_cast<int>(i);
+    return -1;
+  };
+  for (;;) {
+    std::map<std::string, std::vector<std::string>> producers, creators;
+    for (auto& o : ops) {
+      for (auto& c : o.str_list("consumers")) producers[c].push_back(o.at("name").str());
+      if (o.at("type").str() == "BloomFilterCreatePOp")
+        for (auto& u : o.str_list("bloomFilterUsePOps")) creators[u].push_back(o.at("name").str());
+    }
+    int use = -1, join = -1;
+    std::vector<std::string> cols, crs;
+    for (size_t i = 0; i < ops.size() && use < 0; ++i) {
+      const json::Value& u = ops[i];
+      if (u.at("type").str() != "BloomFilterUsePOp") continue;
+      const std::string un = u.at("name").str();
+      cols = u.contains("bloomFilterColumns") ? u.str_list("bloomFilterColumns")
+                                              : std::vector<std::string>{u.at("bloomFilterColumn").str()};
+      crs = u.str_list("creators");
+      if (crs.empty()) crs = creators[un];
+      if (crs.size() != cols.size()) continue;
+      auto cons = u.str_list("consumers");
+      if (cons.size() != 1) continue;
+      const int j = index_of(cons[0]);
+      if (j < 0) continue;
+      const json::Value& J = ops[j];
+      if (J.at("type").str() != "HashJoinArrowPOp" || J.get_str("joinType", "INNER") != "INNER" ||
+          J.contains("buildKeys") || !J.contains("buildKey"))
+        continue;
+      auto bp = J.str_list("buildProducers"), pp = J.str_list("probeProducers");
+      if (std::find(bp.begin(), bp.end(), un) == bp.end() || std::find(pp.begin(), pp.end(), un) != pp.end()) continue;
+      const std::string key = J.at("buildKey").str();
+      bool on_key = true;
+      for (auto& c : cols) on_key &= c == key;
+      const size_t have = J.contains("buildFilters") ? J.at("buildFilters").array().size() : 0;
+      if (!on_key || have + cols.size() > static_cast<size_t>(kJoinBuildFiltersMax)) continue;
+      use = static_cast<int>(i);
+      join = j;
+    }
+    if (use < 0) break;
+    const std::string un = ops[use].at("name").str(), jn = ops[join].at("name").str();
+    std::vector<std::string> data;  // the use's data producers
+    for (auto& p : producers[un])
+      if (std::find(crs.begin(), crs.end(), p) == crs.end()) data.push_back(p);
+    for (auto& o : ops) {
+      if (o.at("type").str() != "BloomFilterCreatePOp" || o.contains("dataConsumers")) continue;
+      auto uses = o.str_list("bloomFilterUsePOps");
+      std::vector<std::string> dc;
+      for (auto& c : o.str_list("consumers"))
+        if (std::find(uses.begin(), uses.end(), c) == uses.end()) dc.push_back(c);
+      jset(o, "dataConsumers", jlist(dc));
+    }
+    for (auto& o : ops) {
+      if (&o == &ops[use]) continue;
+      const bool is_creator = std::find(crs.begin(), crs.end(), o.at("name").str()) != crs.end();
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "dataConsumers", "buildProducers"}) {
+        json::Value* l = jfind(o, key);
+        if (l == nullptr) continue;
+        std::vector<std::string> v = o.str_list(key), nv;
+        for (auto& x : v) {
+          std::vector<std::string> ys{x};
+          if (x == un) {
+            if (std::string(key) == "buildProducers") ys = data;
+            else if (std::string(key) == "consumers" && is_creator) ys = {};  // the filter goes by "bloomFilterUsePOps"
+            else ys = {jn};
+          }
+          for (auto& y : ys)
+            if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
+        }
+        *l = jlist(nv);
+      }
+    }
+    json::Value filters;
+    if (ops[join].contains("buildFilters")) filters = ops[join].at("buildFilters");
+    else filters.kind = json::Value::Array;
+    for (size_t k = 0; k < cols.size(); ++k) {
+      json::Value f;
+      f.kind = json::Value::Object;
+      jset(f, "column", jstr(cols[k]));
+      jset(f, "creator", jstr(crs[k]));
+      filters.a.push_back(f);
+    }
+    jset(ops[join], "buildFilters", filters);
+    ops.erase(ops.begin() + use);
   }
   return out;
 }
@@ -1836,7 +2064,8 @@ json::Value fuse_join_chains(const json::Value& plan) {
       const json::Value& o = ops[i];
       json::Value j;
       j.kind = json::Value::Object;
-      for (const char* k : {"name", "buildProducers", "buildKey", "probeKey", "loadFactor", "projectColumnNames", "joinType"})
+      for (const char* k : {"name", "buildProducers", "buildKey", "probeKey", "loadFactor", "projectColumnNames", "joinType",
+                            "buildFilters"})
         if (o.contains(k)) jset(j, k, o.at(k));
       joins.a.push_back(j);
       absorbed.insert(o.at("name").str());
@@ -1852,7 +2081,7 @@ json::Value fuse_join_chains(const json::Value& plan) {
         continue;
       }
       json::Value o = ops[i];
-      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers"}) {
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"}) {
         json::Value* l = jfind(o, key);
         if (l == nullptr) continue;
         std::vector<std::string> v = o.str_list(key), nv;
@@ -1869,9 +2098,13 @@ json::Value fuse_join_chains(const json::Value& plan) {
   return out;
 }
 
+json::Value fuse_pipelines(const json::Value& plan) {
+  return fuse_join_chains(fuse_build_filters(fuse_bloom_chains(plan)));
+}
+
 std::unique_ptr<Execution> build_execution(const json::Value& plan_in, cudaStream_t stream) {
   const bool fuse = plan_in.get_bool("fusePipelines", true);
-  const json::Value plan = fuse ? fuse_join_chains(fuse_bloom_chains(plan_in)) : plan_in;
+  const json::Value plan = fuse ? fuse_pipelines(plan_in) : plan_in;
   auto ex = std::make_unique<Execution>(stream);
   for (auto& o : plan.at("ops").array()) ex->add(make_op(o, ex.get()));
   for (auto& o : plan.at("ops").array()) {

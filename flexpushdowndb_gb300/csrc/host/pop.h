@@ -224,8 +224,18 @@ class Execution {
 // join and HashJoinArrowPOp share them).
 // With `mark` the table keeps a matched flag per build row (outer and semi
 // joins).
+// `filters` are bloom filters the build side's rows must pass (a bloom
+// selection folded into the build): tested in the table build when they are
+// all on the single integer key column and the join keeps no unmatched build
+// rows (no `mark`), otherwise applied by a selection before it.
 JoinTable build_join_table(const TupleSetPtr& build, const std::vector<std::string>& keys, double load_factor,
-                           cudaStream_t s, bool mark = false);
+                           cudaStream_t s, bool mark = false, const std::vector<BloomProbe>& filters = {});
+// The build side with `filters` applied: unchanged with the filters moved
+// into *in_build when every one is on `key` (an int32, int64 or date32
+// column; empty `key`: never) and there are at most kJoinBuildFiltersMax,
+// else the rows that pass them all.
+TupleSetPtr filter_build_side(const TupleSetPtr& build, const std::string& key, const std::vector<BloomProbe>& filters,
+                              cudaStream_t s, std::vector<BloomPtr>* in_build);
 TupleSetPtr join_probe_keys(const std::string& join_name, const JoinTable& table, const std::vector<std::string>& proj,
                             const std::vector<std::string>& probe_keys, const TupleSetPtr& ts, cudaStream_t s);
 
@@ -265,6 +275,11 @@ std::string plan_predicate_transfer(const json::Value& spec);
 // Build an Execution from a JSON plan (format documented with
 // gfpdb_execute_plan in include/gfpdb.h).
 std::unique_ptr<Execution> build_execution(const json::Value& plan, cudaStream_t stream);
+// The plan after pipeline fusion (what build_execution runs when
+// "fusePipelines" is true, the default): bloom selections chained on one
+// input merged, bloom selections feeding only an inner join's build side
+// folded into the join build, chains of inner joins merged.
+json::Value fuse_pipelines(const json::Value& plan);
 void validate_plan(const json::Value& plan);
 
 }  // namespace gfpdb::pop

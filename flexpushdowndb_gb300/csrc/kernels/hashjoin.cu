@@ -18,6 +18,7 @@
 // output positions with one atomic on the shared cursor: the cursor is a
 // single address whose atomics the L2 serialises, so one atomic per warp
 // step held a 20M-row probe to the rate of that one address.
+#include "bloom.cuh"
 #include "common.cuh"
 #include "launch.h"
 
@@ -25,15 +26,48 @@ namespace gfpdb {
 
 namespace {
 
+// Bloom filters the build keys must pass (a backward filter of predicate
+// transfer tested in the build instead of in a selection before it); a
+// filter whose size or validity lives on the device is read there.
+struct BuildFilters {
+  const uint32_t* blocks[kJoinBuildFiltersMax];
+  const uint64_t* nblocks_dev[kJoinBuildFiltersMax];
+  const int32_t* valid_dev[kJoinBuildFiltersMax];
+  uint32_t num_blocks[kJoinBuildFiltersMax];
+  int32_t num_hashes[kJoinBuildFiltersMax];
+  int32_t valid[kJoinBuildFiltersMax];
+  int32_t n;
+};
+
 __global__ void __launch_bounds__(256)
     join_build_kernel(DevCol key, int64_t cap, const int64_t* n_dev, uint64_t* __restrict__ slots, uint64_t mask,
-                      int key32, DevStatus* st) {
+                      int key32, DevStatus* st, BuildFilters bf) {
   const int64_t n = clamp_rows(n_dev, cap);
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   int64_t my_max = 0;
   bool dup = false;
+  uint32_t nblocks[kJoinBuildFiltersMax];
+  bool valid[kJoinBuildFiltersMax];
+#pragma unroll
+  for (int f = 0; f < kJoinBuildFiltersMax; ++f) {
+    valid[f] = false;
+    nblocks[f] = 0;
+    if (f < bf.n) {
+      nblocks[f] = bf.nblocks_dev[f] ? static_cast<uint32_t>(*bf.nblocks_dev[f]) : bf.num_blocks[f];
+      valid[f] = (bf.valid_dev[f] ? (*bf.valid_dev[f] != 0) : (bf.valid[f] != 0)) && nblocks[f] > 0;
+    }
+  }
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
     const int64_t k = load_int(key, r);
+    bool pass = true;
+#pragma unroll
+    for (int f = 0; f < kJoinBuildFiltersMax; ++f)
+      if (valid[f] && pass) {
+        const uint64_t bh = bloom_hash(k);
+        pass = bloom_test(bf.blocks[f] + static_cast<uint64_t>(bloom_block_of(bh, nblocks[f])) * 8, bh,
+                          bf.num_hashes[f]);
+      }
+    if (!pass) continue;  // cannot match a probe row that passed the filter's creator
     const uint64_t h = hash_key(k);
     const uint32_t tag = key32 ? static_cast<uint32_t>(k) : static_cast<uint32_t>(h >> 32);
     const uint64_t packed = (static_cast<uint64_t>(tag) << 32) | static_cast<uint32_t>(r);
@@ -548,7 +582,9 @@ int probe_grid(Kernel kernel, int64_t n) {
 
 }  // namespace
 
-void join_build_table(JoinTable& t, double load_factor, cudaStream_t s) {
+void join_build_table(JoinTable& t, double load_factor, cudaStream_t s, const std::vector<BloomPtr>& filters) {
+  if (filters.size() > static_cast<size_t>(kJoinBuildFiltersMax))
+    fail(GFPDB_EUNSUPPORTED, "a hash join build tests at most 4 bloom filters");
   if (!(load_factor > 0.0 && load_factor <= 0.9)) fail(GFPDB_EINVAL, "hash join load factor must be in (0, 0.9]");
   const int64_t n = t.build->num_rows();
   if (n >= INT32_MAX) fail(GFPDB_EUNSUPPORTED, "hash join build side must have fewer than 2^31 rows");
@@ -563,9 +599,24 @@ void join_build_table(JoinTable& t, double load_factor, cudaStream_t s) {
   if (n > 0) {
     DevCol k{kc->data, nullptr, static_cast<int32_t>(kc->type), 0};
     const int key32 = kc->type != DType::Int64;
+    if (!filters.empty() && (kc->type == DType::Utf8 || kc->type == DType::Float64))
+      fail(GFPDB_EUNSUPPORTED, "bloom filters tested in a hash join build need an integer key");
+    BuildFilters bf{};
+    bf.n = static_cast<int32_t>(filters.size());
+    for (size_t f = 0; f < filters.size(); ++f) {
+      const BloomFilterDev& b = *filters[f];
+      if (b.num_blocks >= (int64_t{1} << 32)) fail(GFPDB_EUNSUPPORTED, "bloom filter too large");
+      bf.blocks[f] = b.blocks ? b.blocks->as<uint32_t>() : nullptr;
+      bf.nblocks_dev[f] = b.nblocks_dev;
+      bf.valid_dev[f] = b.valid_dev;
+      bf.num_blocks[f] = static_cast<uint32_t>(b.num_blocks);
+      bf.num_hashes[f] = b.num_hashes;
+      bf.valid[f] = (b.valid && bf.blocks[f] != nullptr) ? 1 : 0;
+      if (bf.blocks[f] == nullptr) bf.valid_dev[f] = nullptr;
+    }
     ProfScope prof("join_build_kernel", s);
     join_build_kernel<<<grid_for(n), 256, 0, s>>>(k, n, t.build->rows_dev(), t.slots->as<uint64_t>(), cap - 1,
-                                                 key32, st);
+                                                 key32, st, bf);
     after_launch("join_build_kernel");
     prof.stop(static_cast<double>(n) * dtype_width(kc->type));
   }

@@ -124,7 +124,12 @@ struct JoinTable {
   BufferPtr matched;        // outer / semi joins: int32 per build row, 1 once a probe row matched it
 };
 
-void join_build_table(JoinTable& t, double load_factor, cudaStream_t s);
+// `filters` (at most kJoinBuildFiltersMax, integer keys only): bloom filters
+// on the key column; a build row whose key fails one is left out of the
+// table (it stays in t.build but no probe finds it), as if a bloom selection
+// on the key had run before the build.
+constexpr int kJoinBuildFiltersMax = 4;
+void join_build_table(JoinTable& t, double load_factor, cudaStream_t s, const std::vector<BloomPtr>& filters = {});
 
 // Probe `probe` on column `probe_key`; returns matching (probe row, build
 // row) pairs as two device int32 arrays of length *n_out. With count_dev

@@ -233,6 +233,20 @@ def validate(plan: Plan | str) -> None:
     _abi.check(_abi.lib().gfpdb_plan_validate(text.encode()))
 
 
+def fused(plan: Plan | str) -> dict:
+    """The plan after pipeline fusion (gfpdb_plan_fuse, host only): the
+    operators a run with "fusePipelines" (the default) executes."""
+    text = (plan.to_json() if isinstance(plan, Plan) else plan).encode()
+    L = _abi.lib()
+    need = ctypes.c_int64()
+    rc = L.gfpdb_plan_fuse(text, None, 0, ctypes.byref(need))
+    if need.value <= 0:
+        _abi.check(rc)
+    buf = ctypes.create_string_buffer(need.value)
+    _abi.check(L.gfpdb_plan_fuse(text, buf, need.value, ctypes.byref(need)))
+    return json.loads(buf.value.decode())
+
+
 @dataclass
 class Result:
     table: Table

@@ -437,6 +437,18 @@ void gfpdb_prepared_free(gfpdb_prepared* plan);
 /* Parse and check a plan without running it (host only, no CUDA calls). */
 int32_t gfpdb_plan_validate(const char* plan_json);
 
+/* The plan after pipeline fusion (host only, no CUDA calls): what a run
+ * executes when the plan's "fusePipelines" is true (the default). Chains of
+ * BloomFilterUsePOps on one input become one BloomFilterUsePOp; a
+ * BloomFilterUsePOp whose only consumer is an inner HashJoinArrowPOp on one
+ * key column, taking it on its build side, with its filters on that key,
+ * is folded into the join ("buildFilters": the join build leaves out the
+ * rows a filter rejects); chains of inner joins become one HashJoinChainPOp.
+ * Writes the fused plan's JSON into out_json when capacity holds it;
+ * *needed is its size with the terminating zero. The fusion passes replace
+ * no reference interface: the reference runs each operator as planned. */
+int32_t gfpdb_plan_fuse(const char* plan_json, char* out_json, int64_t capacity, int64_t* needed);
+
 /* Plan the bloom-filter predicate transfer of a join graph (host only), as
  * SmallToLargePredTransOrder::orderPredTrans does
  * (fpdb-executor/src/physical/transform/pred-trans/SmallToLargePredTransOrder.cpp:14-214).

@@ -1,0 +1,93 @@
+"""Pipeline fusion (gfpdb_plan_fuse) on CPU: which operators a plan's run
+executes. Bloom selections chained on one input merge; a bloom selection
+feeding only an inner join's build side, on the join key, is folded into the
+join build; chains of inner joins merge; everything else is left alone."""
+
+import json
+
+import pytest
+
+from flexpushdowndb_gb300 import plan, workloads
+
+
+def by_name(fused):
+    return {o["name"]: o for o in fused["ops"]}
+
+
+def test_star_backward_filters_fold_into_join_chain():
+    f = plan.fused(workloads.star_plan())
+    ops = by_name(f)
+    assert len(f["ops"]) == 21
+    assert [o["name"] for o in f["ops"] if o["type"] == "BloomFilterUsePOp"] == ["bf_fwd_use_fk1"]
+    chain = ops["join_d4"]
+    assert chain["type"] == "HashJoinChainPOp"
+    for i, j in enumerate(chain["joins"], start=1):
+        assert j["name"] == f"join_d{i}"
+        # the dimension's rows come straight from the forward filter's creator
+        assert j["buildProducers"] == [f"bf_fwd_create_d{i}"]
+        assert j["buildFilters"] == [{"column": f"d{i}_pk", "creator": f"bf_bwd_create_fk{i}"}]
+        assert ops[f"bf_bwd_create_fk{i}"]["bloomFilterUsePOps"] == ["join_d4"]
+    # the last backward creator both feeds the chain's probe side and sends
+    # it a filter: its rows go by its data consumers
+    assert ops["bf_bwd_create_fk4"]["dataConsumers"] == ["join_d4"]
+    assert chain["probeProducers"] == ["bf_bwd_create_fk4"]
+    assert ops["bf_bwd_create_fk1"]["dataConsumers"] == ["bf_bwd_create_fk2"]
+    plan.validate(json.dumps(f))
+
+
+def test_planned_star_fuses_like_the_written_one():
+    f = plan.fused(workloads.star_plan_planned())
+    assert len(f["ops"]) == 21
+    uses = [o for o in f["ops"] if o["type"] == "BloomFilterUsePOp"]
+    assert len(uses) == 1 and len(uses[0]["creators"]) == 4
+    chain = by_name(f)["join_d4"]
+    assert [j["buildProducers"] for j in chain["joins"]] == [[f"filter_d{i}"] for i in range(1, 5)]
+    assert all(len(j["buildFilters"]) == 1 for j in chain["joins"])
+
+
+def two_table(join_type="INNER", use_column="d_pk", extra_consumer=False, probe_side=False):
+    p = plan.Plan()
+    p.scan("scan_d", "dim", ["d_pk", "d_v"])
+    p.scan("scan_f", "fact", ["fk", "x"])
+    c = p.bloom_create("bw_create", "scan_f", "fk")
+    u = p.bloom_use("bw_use", "scan_d", c, use_column)
+    if probe_side:
+        p.hash_join("join", "bw_create", u, "fk", "d_pk", ["x", "d_v"])
+    else:
+        p.hash_join("join", u, c, "d_pk", "fk", ["x", "d_v"])
+    p.op("join")["joinType"] = join_type
+    p.collate("collate", "join")
+    if extra_consumer:
+        p.collate("collate2", u)
+    return p
+
+
+def test_single_join_folds_its_build_filter():
+    f = plan.fused(two_table())
+    ops = by_name(f)
+    assert "bw_use" not in ops
+    j = ops["join"]
+    assert j["type"] == "HashJoinArrowPOp"
+    assert j["buildProducers"] == ["scan_d"]
+    assert j["buildFilters"] == [{"column": "d_pk", "creator": "bw_create"}]
+    assert ops["bw_create"]["dataConsumers"] == ["join"]
+    assert ops["bw_create"]["bloomFilterUsePOps"] == ["join"]
+    assert ops["scan_d"]["consumers"] == ["join"]
+
+
+@pytest.mark.parametrize("case", ["left", "full", "left_semi", "other_column", "two_consumers", "probe_side"])
+def test_build_filter_not_folded(case):
+    kw = {"left": dict(join_type="LEFT"), "full": dict(join_type="FULL"),
+          "left_semi": dict(join_type="LEFT_SEMI"), "other_column": dict(use_column="d_v"),
+          "two_consumers": dict(extra_consumer=True), "probe_side": dict(probe_side=True)}[case]
+    f = plan.fused(two_table(**kw))
+    ops = by_name(f)
+    assert "bw_use" in ops
+    assert "buildFilters" not in ops["join"]
+
+
+def test_fuse_keeps_plans_without_candidates():
+    p = plan.Plan()
+    p.scan("s", "t", ["a"])
+    p.collate("c", "s")
+    assert plan.fused(p)["ops"] == json.loads(p.to_json())["ops"]

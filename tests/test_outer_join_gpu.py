@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from flexpushdowndb_gb300 import GfpdbError, ops, plan
-from flexpushdowndb_gb300.expression import col, num_lit, plus
+from flexpushdowndb_gb300.expression import col, lt, num_lit, plus
 from flexpushdowndb_gb300.tupleset import Column, Table
 from oracle import ops as oops
 
@@ -94,6 +94,34 @@ def test_join_types_in_plans(gpu, jt, chunk):
     build, probe = sides(5000, 20_000, seed=11)
     got = plan.execute(outer_plan(jt, chunk), {"build": build, "probe": probe}).table
     want = oops.hash_join_typed(build, probe, "bk", "pk", jt)
+    assert got.names == want.names
+    assert got.sorted_rows() == want.sorted_rows()
+
+
+@pytest.mark.parametrize("jt", TYPES)
+def test_join_types_after_a_selection(gpu, jt):
+    """Both sides come from FilterPOps, whose row counts are only known on
+    the device: a join that emits its unmatched build rows reads exactly the
+    selected build rows, none of the selection's spare capacity."""
+    build, probe = sides(6000, 20_000, seed=17)
+    p = plan.Plan()
+    p.scan("b", "build")
+    p.scan("p", "probe")
+    p.filter("fb", "b", lt(col("bv"), num_lit(0, "int64")))
+    p.filter("fp", "p", lt(col("pv"), num_lit(60, "int32")))
+    p._add({"type": "HashJoinArrowPOp", "name": "j", "buildProducers": ["fb"], "probeProducers": ["fp"],
+            "buildKey": "bk", "probeKey": "pk", "joinType": jt})
+    p.connect("fb", "j")
+    p.connect("fp", "j")
+    p.collate("collate", "j")
+    got = plan.execute(p, {"build": build, "probe": probe}).table
+    kb = build["bv"] < 0
+    kp = probe["pv"] < 60
+    sb = Table([Column(c.name, c.type, c.values[kb] if c.type != "utf8" else [v for v, k in zip(c.to_list(), kb) if k])
+                for c in build.columns])
+    sp = Table([Column(c.name, c.type, c.values[kp] if c.type != "utf8" else [v for v, k in zip(c.to_list(), kp) if k])
+                for c in probe.columns])
+    want = oops.hash_join_typed(sb, sp, "bk", "pk", jt)
     assert got.names == want.names
     assert got.sorted_rows() == want.sorted_rows()
 
