@@ -178,17 +178,35 @@ class FilterPOp : public PhysicalOp {
 // or, when the plan lists them ("dataConsumers", which the pipeline fusion
 // writes once a join may both take this operator's rows and receive its
 // filter), exactly those.
+//
+// After pipeline fusion (fuse_creator_chains) one operator may build several
+// filters over the same rows, each on its own column for its own receivers,
+// in one pass (bloom_build_many); each filter's messages name the creator
+// it came from ("origin"), which its receivers know it by.
+struct CreatedFilter {
+  std::string origin;  // the creator's name in the unfused plan
+  std::string column;
+  int bits = 10, hashes = 3;
+  std::vector<std::string> uses;
+};
+
 class BloomFilterCreatePOp : public PhysicalOp {
  public:
-  BloomFilterCreatePOp(std::string name, std::string column, int bits, int hashes, std::vector<std::string> uses,
+  BloomFilterCreatePOp(std::string name, std::vector<CreatedFilter> filters,
                        std::optional<std::vector<std::string>> data_consumers = std::nullopt)
-      : PhysicalOp(std::move(name), "BloomFilterCreatePOp"), column_(std::move(column)), bits_(bits),
-        hashes_(hashes), uses_(std::move(uses)), data_consumers_(std::move(data_consumers)) {}
+      : PhysicalOp(std::move(name), "BloomFilterCreatePOp"), filters_(std::move(filters)),
+        data_consumers_(std::move(data_consumers)) {
+    if (filters_.empty() || filters_.size() > static_cast<size_t>(kBloomBuildManyMax))
+      fail(GFPDB_EINVAL, "BloomFilterCreatePOp '" + name_ + "': 1 to 8 filters");
+    for (auto& f : filters_)
+      for (auto& u : f.uses)
+        if (std::find(uses_.begin(), uses_.end(), u) == uses_.end()) uses_.push_back(u);
+  }
 
   void onReceive(const Envelope& env) override {
     const Message& m = env.getMessage();
     if (m.type == MessageType::TUPLESET) {
-      m.tuples->require_column(column_);
+      for (auto& f : filters_) m.tuples->require_column(f.column);
       buffered_.push_back(m.tuples);
       std::vector<std::string> pass;
       if (data_consumers_)
@@ -202,16 +220,27 @@ class BloomFilterCreatePOp : public PhysicalOp {
       ctx()->tell(out, pass);
     } else if (m.type == MessageType::COMPLETE) {
       if (!is_producer_complete(*this)) return;
-      std::vector<const Column*> parts;
       std::vector<const int64_t*> rows;
-      for (auto& t : buffered_) {
-        parts.push_back(t->column(column_).get());
-        rows.push_back(t->rows_dev());
+      std::vector<std::vector<const Column*>> parts(filters_.size());
+      std::vector<int32_t> bits, hashes;
+      for (auto& t : buffered_) rows.push_back(t->rows_dev());
+      for (size_t f = 0; f < filters_.size(); ++f) {
+        for (auto& t : buffered_) parts[f].push_back(t->column(filters_[f].column).get());
+        bits.push_back(filters_[f].bits);
+        hashes.push_back(filters_[f].hashes);
       }
-      Message out;
-      out.type = MessageType::BLOOM_FILTER;
-      out.bloom = bloom_build(parts, bits_, hashes_, ctx()->stream(), rows);
-      ctx()->tell(out, uses_);
+      std::vector<BloomPtr> blooms;
+      if (filters_.size() == 1)
+        blooms.push_back(bloom_build(parts[0], bits[0], hashes[0], ctx()->stream(), rows));
+      else
+        blooms = bloom_build_many(parts, bits, hashes, ctx()->stream(), rows);
+      for (size_t f = 0; f < filters_.size(); ++f) {
+        Message out;
+        out.type = MessageType::BLOOM_FILTER;
+        out.bloom = blooms[f];
+        if (filters_[f].origin != name_) out.origin = filters_[f].origin;
+        ctx()->tell(out, filters_[f].uses);
+      }
       ctx()->notifyComplete();
     }
   }
@@ -219,9 +248,8 @@ class BloomFilterCreatePOp : public PhysicalOp {
   void clear() override { buffered_.clear(); }
 
  private:
-  std::string column_;
-  int bits_, hashes_;
-  std::vector<std::string> uses_;
+  std::vector<CreatedFilter> filters_;
+  std::vector<std::string> uses_;  // every filter's receivers
   std::optional<std::vector<std::string>> data_consumers_;
   std::vector<TupleSetPtr> buffered_;
 };
@@ -246,8 +274,9 @@ class BloomFilterUsePOp : public PhysicalOp {
     } else if (m.type == MessageType::BLOOM_FILTER) {
       size_t i = 0;
       if (!creators_.empty()) {
-        auto it = std::find(creators_.begin(), creators_.end(), m.sender);
-        if (it == creators_.end()) fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name_ + "': filter from '" + m.sender + "'");
+        const std::string& from = m.origin.empty() ? m.sender : m.origin;
+        auto it = std::find(creators_.begin(), creators_.end(), from);
+        if (it == creators_.end()) fail(GFPDB_EINVAL, "BloomFilterUsePOp '" + name_ + "': filter from '" + from + "'");
         i = static_cast<size_t>(it - creators_.begin());
       }
       blooms_[i] = m.bloom;
@@ -592,12 +621,13 @@ struct BuildFilterSpec {
   std::vector<std::string> columns, creators;
   std::vector<BloomPtr> blooms;
 
-  bool takes(const std::string& sender) const {
-    return std::find(creators.begin(), creators.end(), sender) != creators.end();
+  static const std::string& origin_of(const Message& m) { return m.origin.empty() ? m.sender : m.origin; }
+  bool takes(const Message& m) const {
+    return std::find(creators.begin(), creators.end(), origin_of(m)) != creators.end();
   }
   void receive(const std::string& op, const Message& m) {
-    auto it = std::find(creators.begin(), creators.end(), m.sender);
-    if (it == creators.end()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + op + "': bloom filter from '" + m.sender + "'");
+    auto it = std::find(creators.begin(), creators.end(), origin_of(m));
+    if (it == creators.end()) fail(GFPDB_EINVAL, "HashJoinArrowPOp '" + op + "': bloom filter from '" + origin_of(m) + "'");
     blooms[static_cast<size_t>(it - creators.begin())] = m.bloom;
   }
   bool ready() const {
@@ -772,7 +802,7 @@ class HashJoinChainPOp : public PhysicalOp {
     } else if (m.type == MessageType::BLOOM_FILTER) {
       bool taken = false;
       for (auto& J : joins_)
-        if (J.filters.takes(m.sender)) {
+        if (J.filters.takes(m)) {
           J.filters.receive(J.name, m);
           taken = true;
         }
@@ -1634,10 +1664,23 @@ std::unique_ptr<PhysicalOp> make_op(const json::Value& o, Execution* exec) {
   } else if (type == "FilterPOp") {
     op = std::make_unique<FilterPOp>(name, parse_expr(o.at("predicate")));
   } else if (type == "BloomFilterCreatePOp") {
-    op = std::make_unique<BloomFilterCreatePOp>(name, o.at("bloomFilterColumn").str(),
-                                                static_cast<int>(o.get_int("bitsPerKey", 10)),
-                                                static_cast<int>(o.get_int("numHashes", 3)),
-                                                o.str_list("bloomFilterUsePOps"),
+    // one filter, or several ("filters": [{"origin", "bloomFilterColumn",
+    // "bitsPerKey", "numHashes", "bloomFilterUsePOps"}], fused creators)
+    std::vector<CreatedFilter> filters;
+    auto one = [&](const json::Value& f, const std::string& origin) {
+      CreatedFilter c;
+      c.origin = origin;
+      c.column = f.at("bloomFilterColumn").str();
+      c.bits = static_cast<int>(f.get_int("bitsPerKey", 10));
+      c.hashes = static_cast<int>(f.get_int("numHashes", 3));
+      c.uses = f.str_list("bloomFilterUsePOps");
+      filters.push_back(std::move(c));
+    };
+    if (o.contains("filters"))
+      for (auto& f : o.at("filters").array()) one(f, f.get_str("origin", name));
+    else
+      one(o, name);
+    op = std::make_unique<BloomFilterCreatePOp>(name, std::move(filters),
                                                 o.contains("dataConsumers")
                                                     ? std::optional<std::vector<std::string>>(o.str_list("dataConsumers"))
                                                     : std::nullopt);
@@ -2002,6 +2045,111 @@ json::Value fuse_build_filters(const json::Value& plan) {
   return out;
 }
 
+// Pipeline fusion: BloomFilterCreatePOps over the same rows become one
+// operator that builds all their filters in one pass (bloom_build_many):
+// a creator whose only ordinary consumer is another creator, that one's
+// only producer (a chain, each forwarding the rows to the next), or a
+// creator with no ordinary consumer and another with the same single
+// producer (siblings). The fused operator keeps the second one's name and
+// ordinary consumers; each filter keeps its creator's name as its origin,
+// which its receivers know it by, and goes to the same receivers. Results
+// are unchanged: every filter is built from the same rows as before.
+json::Value fuse_creator_chains(const json::Value& plan) {
+  json::Value out = plan;
+  json::Value* ops_v = jfind(out, "ops");
+  if (ops_v == nullptr) return out;
+  auto& ops = ops_v->a;
+  auto is_creator = [](const json::Value& o) { return o.at("type").str() == "BloomFilterCreatePOp"; };
+  auto index_of = [&](const std::string& name) {
+    for (size_t i = 0; i < ops.size(); ++i)
+      if (ops[i].at("name").str() == name) return static_cast<int>(i);
+    return -1;
+  };
+  auto filters_of = [](const json::Value& c) {
+    if (c.contains("filters")) return c.at("filters").array();
+    json::Value f;
+    f.kind = json::Value::Object;
+    jset(f, "origin", c.at("name"));
+    jset(f, "bloomFilterColumn", c.at("bloomFilterColumn"));
+    for (const char* k : {"bitsPerKey", "numHashes"})
+      if (c.contains(k)) jset(f, k, c.at(k));
+    jset(f, "bloomFilterUsePOps", jlist(c.str_list("bloomFilterUsePOps")));
+    return std::vector<json::Value>{f};
+  };
+  auto data_consumers_of = [](const json::Value& c) {
+    if (c.contains("dataConsumers")) return c.str_list("dataConsumers");
+    auto uses = c.str_list("bloomFilterUsePOps");
+    std::vector<std::string> dc;
+    for (auto& x : c.str_list("consumers"))
+      if (std::find(uses.begin(), uses.end(), x) == uses.end()) dc.push_back(x);
+    return dc;
+  };
+  for (;;) {
+    std::map<std::string, std::vector<std::string>> producers;
+    for (auto& o : ops)
+      for (auto& c : o.str_list("consumers")) producers[c].push_back(o.at("name").str());
+    int a = -1, b = -1;
+    for (size_t i = 0; i < ops.size() && a < 0; ++i) {
+      if (!is_creator(ops[i])) continue;
+      const std::string an = ops[i].at("name").str();
+      const auto dc = data_consumers_of(ops[i]);
+      const size_t na = filters_of(ops[i]).size();
+      if (dc.size() == 1) {  // a chain
+        const int j = index_of(dc[0]);
+        if (j >= 0 && is_creator(ops[j]) && producers[dc[0]] == std::vector<std::string>{an} &&
+            na + filters_of(ops[j]).size() <= static_cast<size_t>(kBloomBuildManyMax)) {
+          a = static_cast<int>(i);
+          b = j;
+        }
+      } else if (dc.empty() && producers[an].size() == 1) {  // siblings
+        for (size_t j = 0; j < ops.size(); ++j) {
+          if (j == i || !is_creator(ops[j]) || producers[ops[j].at("name").str()] != producers[an]) continue;
+          if (na + filters_of(ops[j]).size() > static_cast<size_t>(kBloomBuildManyMax)) continue;
+          a = static_cast<int>(i);
+          b = static_cast<int>(j);
+          break;
+        }
+      }
+    }
+    if (a < 0) break;
+    const std::string an = ops[a].at("name").str(), bn = ops[b].at("name").str();
+    json::Value filters;
+    filters.kind = json::Value::Array;
+    filters.a = filters_of(ops[a]);
+    for (auto& f : filters_of(ops[b])) filters.a.push_back(f);
+    std::vector<std::string> uses, cons;
+    for (auto& f : filters.a)
+      for (auto& u : f.str_list("bloomFilterUsePOps"))
+        if (std::find(uses.begin(), uses.end(), u) == uses.end()) uses.push_back(u);
+    for (const json::Value* o : {&ops[a], &ops[b]})
+      for (auto& c : o->str_list("consumers"))
+        if (c != bn && std::find(cons.begin(), cons.end(), c) == cons.end()) cons.push_back(c);
+    json::Value fused;
+    fused.kind = json::Value::Object;
+    jset(fused, "type", jstr("BloomFilterCreatePOp"));
+    jset(fused, "name", jstr(bn));
+    jset(fused, "filters", filters);
+    jset(fused, "bloomFilterUsePOps", jlist(uses));
+    jset(fused, "dataConsumers", jlist(data_consumers_of(ops[b])));
+    jset(fused, "consumers", jlist(cons));
+    ops[b] = fused;
+    for (auto& o : ops) {
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"}) {
+        json::Value* l = jfind(o, key);
+        if (l == nullptr) continue;
+        std::vector<std::string> v = o.str_list(key), nv;
+        for (auto& x : v) {
+          const std::string y = x == an ? bn : x;
+          if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
+        }
+        *l = jlist(nv);
+      }
+    }
+    ops.erase(ops.begin() + a);
+  }
+  return out;
+}
+
 // Pipeline fusion: a chain of inner HashJoinArrowPOps in which each join's
 // only consumer is the next join, which takes it as its only probe producer,
 // becomes one HashJoinChainPOp (the joins in order, each with its build
@@ -2081,16 +2229,20 @@ json::Value fuse_join_chains(const json::Value& plan) {
         continue;
       }
       json::Value o = ops[i];
-      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"}) {
-        json::Value* l = jfind(o, key);
-        if (l == nullptr) continue;
-        std::vector<std::string> v = o.str_list(key), nv;
-        for (auto& x : v) {
-          const std::string y = absorbed.count(x) ? last : x;
+      auto rename = [&](json::Value& x, const char* key) {
+        json::Value* l = jfind(x, key);
+        if (l == nullptr) return;
+        std::vector<std::string> v = x.str_list(key), nv;
+        for (auto& e : v) {
+          const std::string y = absorbed.count(e) ? last : e;
           if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
         }
         *l = jlist(nv);
-      }
+      };
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"})
+        rename(o, key);
+      if (json::Value* fl = jfind(o, "filters"))  // a fused creator's receivers, filter by filter
+        for (auto& f : fl->a) rename(f, "bloomFilterUsePOps");
       kept.push_back(o);
     }
     ops = kept;
@@ -2099,7 +2251,7 @@ json::Value fuse_join_chains(const json::Value& plan) {
 }
 
 json::Value fuse_pipelines(const json::Value& plan) {
-  return fuse_join_chains(fuse_build_filters(fuse_bloom_chains(plan)));
+  return fuse_join_chains(fuse_creator_chains(fuse_build_filters(fuse_bloom_chains(plan))));
 }
 
 std::unique_ptr<Execution> build_execution(const json::Value& plan_in, cudaStream_t stream) {

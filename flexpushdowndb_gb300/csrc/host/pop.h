@@ -48,6 +48,7 @@ struct Message {
   std::string sender;
   TupleSetPtr tuples;   // TUPLESET
   BloomPtr bloom;       // BLOOM_FILTER
+  std::string origin;   // BLOOM_FILTER: the creator the filter belongs to, when not the sender (fused creators)
   std::string error;    // ERROR
   cudaEvent_t ready = nullptr;  // recorded on the sender's stream after its work for this message
   int stream = 0;               // the sender's stream index

@@ -91,6 +91,14 @@ using BloomPtr = std::shared_ptr<const BloomFilterDev>;
 // that part comes from a deferred TupleSet (its length is then a capacity).
 BloomPtr bloom_build(const std::vector<const Column*>& key_parts, int32_t bits_per_key, int32_t num_hashes,
                      cudaStream_t s, const std::vector<const int64_t*>& part_rows_dev = {});
+// Several filters over the same rows in one pass: key_parts[f] are filter
+// f's key column in each part (every filter's parts the same rows), with its
+// own bits per key and hash count; each filter is the one bloom_build makes
+// from its parts.
+constexpr int kBloomBuildManyMax = 8;
+std::vector<BloomPtr> bloom_build_many(const std::vector<std::vector<const Column*>>& key_parts,
+                                       const std::vector<int32_t>& bits_per_key, const std::vector<int32_t>& num_hashes,
+                                       cudaStream_t s, const std::vector<const int64_t*>& part_rows_dev = {});
 
 // ------------------------------------------------------------- select.cu
 

@@ -107,4 +107,4 @@ def test_star_build_filters_match_oracle(gpu, planned):
     assert sum(1 for o in fused["ops"] if o["type"] == "BloomFilterUsePOp") == 1
     r = plan.execute(p, tabs)
     assert r.table.sorted_rows() == want
-    assert r.stats["num_ops"] == 21
+    assert r.stats["num_ops"] == 18

@@ -17,7 +17,7 @@ def by_name(fused):
 def test_star_backward_filters_fold_into_join_chain():
     f = plan.fused(workloads.star_plan())
     ops = by_name(f)
-    assert len(f["ops"]) == 21
+    assert len(f["ops"]) == 18
     assert [o["name"] for o in f["ops"] if o["type"] == "BloomFilterUsePOp"] == ["bf_fwd_use_fk1"]
     chain = ops["join_d4"]
     assert chain["type"] == "HashJoinChainPOp"
@@ -25,19 +25,20 @@ def test_star_backward_filters_fold_into_join_chain():
         assert j["name"] == f"join_d{i}"
         # the dimension's rows come straight from the forward filter's creator
         assert j["buildProducers"] == [f"bf_fwd_create_d{i}"]
+        # each filter is known by the creator it came from
         assert j["buildFilters"] == [{"column": f"d{i}_pk", "creator": f"bf_bwd_create_fk{i}"}]
-        assert ops[f"bf_bwd_create_fk{i}"]["bloomFilterUsePOps"] == ["join_d4"]
-    # the last backward creator both feeds the chain's probe side and sends
-    # it a filter: its rows go by its data consumers
+    # the backward creators merged into the last one, which both feeds the
+    # chain's probe side and sends it the filters: its rows go by its data
+    # consumers
+    assert ops["bf_bwd_create_fk4"]["bloomFilterUsePOps"] == ["join_d4"]
     assert ops["bf_bwd_create_fk4"]["dataConsumers"] == ["join_d4"]
     assert chain["probeProducers"] == ["bf_bwd_create_fk4"]
-    assert ops["bf_bwd_create_fk1"]["dataConsumers"] == ["bf_bwd_create_fk2"]
     plan.validate(json.dumps(f))
 
 
 def test_planned_star_fuses_like_the_written_one():
     f = plan.fused(workloads.star_plan_planned())
-    assert len(f["ops"]) == 21
+    assert len(f["ops"]) == 18
     uses = [o for o in f["ops"] if o["type"] == "BloomFilterUsePOp"]
     assert len(uses) == 1 and len(uses[0]["creators"]) == 4
     chain = by_name(f)["join_d4"]
@@ -91,3 +92,35 @@ def test_fuse_keeps_plans_without_candidates():
     p.scan("s", "t", ["a"])
     p.collate("c", "s")
     assert plan.fused(p)["ops"] == json.loads(p.to_json())["ops"]
+
+
+def test_creator_chain_and_siblings_merge():
+    f = by_name(plan.fused(workloads.star_plan()))
+    c = f["bf_bwd_create_fk4"]
+    assert [x["origin"] for x in c["filters"]] == [f"bf_bwd_create_fk{i}" for i in range(1, 5)]
+    assert [x["bloomFilterColumn"] for x in c["filters"]] == [f"fk{i}" for i in range(1, 5)]
+    assert all(x["bloomFilterUsePOps"] == ["join_d4"] for x in c["filters"])
+    assert c["dataConsumers"] == ["join_d4"]
+    for i in range(1, 4):
+        assert f"bf_bwd_create_fk{i}" not in f
+    # the forward creators read different dimensions: left alone
+    assert all(f"bf_fwd_create_d{i}" in f for i in range(1, 5))
+    # the planner's backward creators are siblings on the fact's last use
+    g = plan.fused(workloads.star_plan_planned())
+    creators = [o for o in g["ops"] if o["type"] == "BloomFilterCreatePOp" and "filters" in o]
+    assert len(creators) == 1 and len(creators[0]["filters"]) == 4
+    assert len(g["ops"]) == 18
+
+
+def test_creator_merge_limit():
+    p = plan.Plan()
+    p.scan("s", "t", ["k"])
+    p.scan("x", "u", ["k"])
+    prev, tail = "s", "x"
+    for i in range(10):
+        prev = p.bloom_create(f"c{i}", prev, "k")
+        tail = p.bloom_use(f"u{i}", tail, prev, "k")
+    p.collate("collate", tail)
+    f = plan.fused(p)
+    sizes = sorted(len(o.get("filters", [o])) for o in f["ops"] if o["type"] == "BloomFilterCreatePOp")
+    assert sizes == [2, 8]

@@ -117,9 +117,9 @@ def test_bloom_chain_fusion_same_result(gpu, fuse):
     r = plan.execute(_with_options(workloads.star_plan(), fusePipelines=fuse), tabs)
     assert r.table.sorted_rows() == queries.star_query(tabs).sorted_rows()
     # the four forward BloomFilterUsePOps on the fact table fuse into one,
-    # the four backward ones fold into the join builds, the four joins into
-    # one chain
-    assert r.stats["num_ops"] == (21 if fuse else 31)
+    # the four backward ones fold into the join builds, their four creators
+    # into one, the four joins into one chain
+    assert r.stats["num_ops"] == (18 if fuse else 31)
 
 
 def test_duplicate_build_keys_rerun_with_exact_sizes(gpu):
