@@ -108,3 +108,42 @@ def test_star_build_filters_match_oracle(gpu, planned):
     r = plan.execute(p, tabs)
     assert r.table.sorted_rows() == want
     assert r.stats["num_ops"] == 18
+
+
+def two_filter_plan(fuse):
+    """A dimension filtered by two fact tables' keys (two bloom uses in a
+    chain, fused into one use with two probes, folded into the join build
+    as two build filters); the join probes the first fact table."""
+    p = plan.Plan()
+    p.scan("scan_d", "dim", ["d_pk", "d_v"])
+    p.scan("scan_f", "fact", ["fk", "x"])
+    p.scan("scan_g", "fact2", ["gk"])
+    c1 = p.bloom_create("bw1", "scan_f", "fk")
+    c2 = p.bloom_create("bw2", "scan_g", "gk", 6, 2)
+    u1 = p.bloom_use("use1", "scan_d", c1, "d_pk")
+    u2 = p.bloom_use("use2", u1, c2, "d_pk")
+    p.hash_join("join", u2, c1, "d_pk", "fk", ["x", "d_v"])
+    p.collate("collate", "join")
+    d = json.loads(p.to_json())
+    d["fusePipelines"] = fuse
+    return json.dumps(d)
+
+
+@pytest.mark.parametrize("key_type", ["int32", "int64"])
+def test_join_build_with_two_filters(gpu, key_type):
+    tabs = tables(40_000, 200_000, key_type, True, seed=23)
+    rng = np.random.default_rng(5)
+    gk = rng.integers(1, 40_000, 3000)
+    tabs["fact2"] = Table([Column("gk", key_type, gk)])
+    fused = plan.fused(two_filter_plan(True))
+    join = [o for o in fused["ops"] if o["name"] == "join"][0]
+    assert [f["creator"] for f in join["buildFilters"]] == ["bw1", "bw2"]
+    # the second filter keeps the dimension rows the oracle's filter over
+    # fact2's keys keeps, false positives included; the first cannot drop a
+    # row the join would emit
+    keep = oops.bloom_contains(oops.bloom_words(tabs["fact2"]["gk"], 6, 2), tabs["dim"]["d_pk"], 2)
+    dim = Table([Column(c.name, c.type, c.values[keep]) for c in tabs["dim"].columns])
+    want = oops.hash_join(dim, tabs["fact"], "d_pk", "fk", ["x", "d_v"]).sorted_rows()
+    for fuse in (True, False):
+        r = plan.execute(two_filter_plan(fuse), tabs)
+        assert r.table.sorted_rows() == want

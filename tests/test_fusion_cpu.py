@@ -124,3 +124,23 @@ def test_creator_merge_limit():
     f = plan.fused(p)
     sizes = sorted(len(o.get("filters", [o])) for o in f["ops"] if o["type"] == "BloomFilterCreatePOp")
     assert sizes == [2, 8]
+
+
+def test_two_filters_fold_into_one_join_build():
+    p = plan.Plan()
+    p.scan("scan_d", "dim", ["d_pk"])
+    p.scan("scan_f", "fact", ["fk"])
+    p.scan("scan_g", "fact2", ["gk"])
+    c1 = p.bloom_create("bw1", "scan_f", "fk")
+    c2 = p.bloom_create("bw2", "scan_g", "gk")
+    u1 = p.bloom_use("use1", "scan_d", c1, "d_pk")
+    u2 = p.bloom_use("use2", u1, c2, "d_pk")
+    p.hash_join("join", u2, c1, "d_pk", "fk")
+    p.collate("collate", "join")
+    ops = by_name(plan.fused(p))
+    assert "use1" not in ops and "use2" not in ops
+    assert ops["join"]["buildProducers"] == ["scan_d"]
+    assert ops["join"]["buildFilters"] == [{"column": "d_pk", "creator": "bw1"}, {"column": "d_pk", "creator": "bw2"}]
+    # different rows: the two creators stay apart
+    assert "filters" not in ops["bw1"] and "filters" not in ops["bw2"]
+    assert ops["bw1"]["dataConsumers"] == ["join"] and ops["bw2"]["dataConsumers"] == []
