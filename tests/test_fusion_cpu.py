@@ -144,3 +144,30 @@ def test_two_filters_fold_into_one_join_build():
     # different rows: the two creators stay apart
     assert "filters" not in ops["bw1"] and "filters" not in ops["bw2"]
     assert ops["bw1"]["dataConsumers"] == ["join"] and ops["bw2"]["dataConsumers"] == []
+
+
+@pytest.mark.parametrize("make", ["star", "planned", "two_table", "two_filters"])
+def test_fusion_is_idempotent(make):
+    """Fusing a fused plan changes nothing, and the fused plan is valid JSON
+    the plan checker accepts."""
+    if make == "star":
+        text = workloads.star_plan().to_json()
+    elif make == "planned":
+        text = workloads.star_plan_planned().to_json()
+    elif make == "two_table":
+        text = two_table().to_json()
+    else:
+        p = plan.Plan()
+        p.scan("scan_d", "dim", ["d_pk"])
+        p.scan("scan_f", "fact", ["fk"])
+        p.scan("scan_g", "fact2", ["gk"])
+        c1 = p.bloom_create("bw1", "scan_f", "fk")
+        c2 = p.bloom_create("bw2", "scan_g", "gk")
+        u2 = p.bloom_use("use2", p.bloom_use("use1", "scan_d", c1, "d_pk"), c2, "d_pk")
+        p.hash_join("join", u2, c1, "d_pk", "fk")
+        p.collate("collate", "join")
+        text = p.to_json()
+    once = plan.fused(text)
+    twice = plan.fused(json.dumps(once))
+    assert twice == once
+    plan.validate(json.dumps(once))
