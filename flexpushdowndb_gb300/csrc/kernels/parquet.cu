@@ -19,10 +19,11 @@
 //                          definition levels, walks byte-array lengths (data
 //                          and dictionary pages) and reads the dictionary
 //                          indices' run headers, up to 256 a round, and every
-//                          thread then decodes the round's indices;
-//   parquet_values_kernel  per data page and value: fixed-width values
-//                          copied or looked up in the dictionary into the
-//                          output column; byte arrays get their source and
+//                          thread then decodes the round's indices, a
+//                          fixed-width column's straight into its values;
+//   parquet_values_kernel  per plain data page and value: fixed-width values
+//                          copied into the output column; byte arrays (plain
+//                          or dictionary-encoded) get their source and
 //                          length;
 //   then per utf8 column a prefix sum of the lengths and a byte copy.
 #include <cstring>
@@ -190,13 +191,28 @@ __device__ __forceinline__ bool run_header(const uint8_t* p, int32_t n, int32_t*
   return false;
 }
 
+__device__ __forceinline__ void copy_value(const uint8_t* src, uint8_t* dst, int w) {
+  if (w == 8 && !(reinterpret_cast<uintptr_t>(src) & 7)) {
+    *reinterpret_cast<uint64_t*>(dst) = *reinterpret_cast<const uint64_t*>(src);
+  } else if (w == 4 && !(reinterpret_cast<uintptr_t>(src) & 3)) {
+    *reinterpret_cast<uint32_t*>(dst) = *reinterpret_cast<const uint32_t*>(src);
+  } else {
+    for (int k = 0; k < w; ++k) dst[k] = src[k];
+  }
+}
+
 constexpr int kPqThreads = 256;
 constexpr int kPqRuns = 256;  // run headers read per round
 
 // One CTA per page. Thread 0 does the sequential parts (definition levels,
 // byte-array lengths, run headers); the dictionary indices of each round of
 // up to kPqRuns runs are then decoded by every thread, a value finding its
-// run by binary search over the runs' first values.
+// run by binary search over the runs' first values. A fixed-width column's
+// index is looked up in its dictionary page at once and the value written
+// to the output column (the dictionary page's body is read as the host laid
+// it out, not through fields another CTA of this launch sets); a byte-array
+// column's index is kept for parquet_values_kernel, which runs after the
+// dictionary pages' entries are known.
 __global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* pages, int32_t n_pages, DictArrays dicts,
                                                                    DevStatus* st) {
   __shared__ int32_t s_first[kPqRuns + 1];  // the page value index each run starts at; then the round's end
@@ -295,7 +311,7 @@ __global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* page
       }
       const bool indices = ok && pg.type != parquet::PAGE_DICTIONARY && pg.encoding != parquet::ENC_PLAIN;
       s_bw = blen > 0 ? base[0] : 99;
-      if (indices && s_bw > 32) {
+      if (indices && (s_bw > 32 || pg.dict_page < 0 || pg.dict_page >= n_pages)) {
         raise_status(st, GFPDB_EINVAL, 500000 + static_cast<int32_t>(w));
         ok = 0;
       }
@@ -310,6 +326,17 @@ __global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* page
     blen = pg.values_len;
     const int32_t bw = s_bw;
     const uint64_t mask = bw == 32 ? 0xffffffffull : ((1ull << bw) - 1ull);
+    // a fixed-width column's dictionary: its page's values as laid out on
+    // the host (dictionary pages carry no levels), its entry count and bytes
+    const uint8_t* dvals = nullptr;
+    int64_t dlen = 0;
+    int32_t dn = 0;
+    if (pg.width > 0) {
+      const PageDev& dp = pages[pg.dict_page];
+      dvals = dp.snappy ? dp.inflated : dp.body;
+      dlen = dp.snappy ? dp.inflated_len : dp.body_len;
+      dn = dp.num_values;
+    }
     for (;;) {
       if (threadIdx.x == 0) {
         int32_t n = 0, at = s_at, done = s_done;
@@ -378,22 +405,26 @@ __global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* page
           for (int k = 0; k < nb; ++k) x |= static_cast<uint64_t>(q[k]) << (8 * k);
           idx = static_cast<uint32_t>((x >> (bit & 7)) & mask);
         }
-        pg.idx[pg.first_row + v] = static_cast<int32_t>(idx);
+        if (pg.width > 0) {
+          if (idx >= static_cast<uint32_t>(dn) || (static_cast<int64_t>(idx) + 1) * pg.width > dlen) {
+            raise_status(st, GFPDB_EINVAL, 600000 + static_cast<int32_t>(w));
+            continue;
+          }
+          // the value's 4-byte words from the two aligned words around each
+          // (the arena and the inflated buffer carry 16 bytes of tail padding)
+          const uint8_t* sp = dvals + static_cast<int64_t>(idx) * pg.width;
+          const uint32_t* al = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(sp) & ~uintptr_t{3});
+          const uint32_t sh = 8u * static_cast<uint32_t>(reinterpret_cast<uintptr_t>(sp) & 3u);
+          uint32_t* dw = reinterpret_cast<uint32_t*>(pg.fixed_out + (pg.first_row + v) * pg.width);
+          for (int k = 0; k < pg.width / 4; ++k) dw[k] = __funnelshift_r(__ldg(al + k), __ldg(al + k + 1), sh);
+        } else {
+          pg.idx[pg.first_row + v] = static_cast<int32_t>(idx);
+        }
       }
       const bool more = s_done < pg.num_values;
       __syncthreads();  // the runs are read before thread 0 rewrites them
       if (!more) break;
     }
-  }
-}
-
-__device__ __forceinline__ void copy_value(const uint8_t* src, uint8_t* dst, int w) {
-  if (w == 8 && !(reinterpret_cast<uintptr_t>(src) & 7)) {
-    *reinterpret_cast<uint64_t*>(dst) = *reinterpret_cast<const uint64_t*>(src);
-  } else if (w == 4 && !(reinterpret_cast<uintptr_t>(src) & 3)) {
-    *reinterpret_cast<uint32_t*>(dst) = *reinterpret_cast<const uint32_t*>(src);
-  } else {
-    for (int k = 0; k < w; ++k) dst[k] = src[k];
   }
 }
 
@@ -408,29 +439,19 @@ __global__ void __launch_bounds__(256) parquet_values_kernel(const PageDev* page
     const int64_t row = pg.first_row + i;
     if (pg.width > 0) {
       // bounds: a page whose levels or sizes were bad has values_len 0
-      const uint8_t* src;
-      if (dict) {
-        const int32_t e = pg.idx[row];
-        if (e < 0 || e >= dp->num_values || static_cast<int64_t>(e + 1) * pg.width > dp->values_len) {
-          raise_status(st, GFPDB_EINVAL, 600000 + static_cast<int32_t>(blockIdx.y));
-          continue;
-        }
-        src = dp->values + static_cast<int64_t>(e) * pg.width;
-      } else {
-        if ((i + 1) * pg.width > pg.values_len) {
-          raise_status(st, GFPDB_EINVAL, 600000 + static_cast<int32_t>(blockIdx.y));
-          continue;
-        }
-        // the value's 4-byte words from the two aligned words around each
-        // (the arena and the inflated buffer carry 16 bytes of tail padding)
-        const uint8_t* sp = pg.values + i * pg.width;
-        const uint32_t* al = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(sp) & ~uintptr_t{3});
-        const uint32_t sh = 8u * static_cast<uint32_t>(reinterpret_cast<uintptr_t>(sp) & 3u);
-        uint32_t* dw = reinterpret_cast<uint32_t*>(pg.fixed_out + row * pg.width);
-        for (int k = 0; k < pg.width / 4; ++k) dw[k] = __funnelshift_r(al[k], al[k + 1], sh);
+      // plain values only: a fixed-width dictionary page is decoded to its
+      // values by the page pass and never listed here
+      if (dict || (i + 1) * pg.width > pg.values_len) {
+        raise_status(st, GFPDB_EINVAL, 600000 + static_cast<int32_t>(blockIdx.y));
         continue;
       }
-      copy_value(src, pg.fixed_out + row * pg.width, pg.width);
+      // the value's 4-byte words from the two aligned words around each
+      // (the arena and the inflated buffer carry 16 bytes of tail padding)
+      const uint8_t* sp = pg.values + i * pg.width;
+      const uint32_t* al = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(sp) & ~uintptr_t{3});
+      const uint32_t sh = 8u * static_cast<uint32_t>(reinterpret_cast<uintptr_t>(sp) & 3u);
+      uint32_t* dw = reinterpret_cast<uint32_t*>(pg.fixed_out + row * pg.width);
+      for (int k = 0; k < pg.width / 4; ++k) dw[k] = __funnelshift_r(al[k], al[k + 1], sh);
     } else if (dict) {
       const int32_t e = pg.idx[row];
       if (e < 0 || e >= dp->num_values) {
@@ -495,7 +516,7 @@ TupleSetPtr parquet_read(const uint8_t* file, int64_t size, const std::vector<st
     } else {
       fixed[c] = make_buffer((rows > 0 ? rows : 1) * dtype_width(t), s);
     }
-    if (has_dict[c]) idx[c] = make_buffer((rows > 0 ? rows : 1) * 4, s);
+    if (has_dict[c] && t == DType::Utf8) idx[c] = make_buffer((rows > 0 ? rows : 1) * 4, s);
   }
 
   // page descriptors
@@ -515,7 +536,11 @@ TupleSetPtr parquet_read(const uint8_t* file, int64_t size, const std::vector<st
                (v2 ? pg.uncompressed - pg.v2_levels : pg.uncompressed)) {
       fail(GFPDB_EINVAL, "Parquet uncompressed page sizes disagree");
     }
-    if (pg.type != parquet::PAGE_DICTIONARY) data_list.push_back(static_cast<int32_t>(p));
+    // data pages the values pass reads: plain pages, and dictionary-encoded
+    // byte-array pages (a fixed-width column's dictionary indices become
+    // values in the page pass)
+    const bool fixed_dict = L.columns[pg.column].dtype != DType::Utf8 && pg.encoding != parquet::ENC_PLAIN;
+    if (pg.type != parquet::PAGE_DICTIONARY && !fixed_dict) data_list.push_back(static_cast<int32_t>(p));
   }
   auto inflated = make_buffer(inflate_bytes + 16, s);
   for (size_t p = 0; p < L.pages.size(); ++p) {
