@@ -387,6 +387,8 @@ __global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* page
       const int32_t n = s_n;
       if (n == 0) break;
       const int32_t v0 = s_first[0], v1 = s_first[n];
+      // unrolled so that several values' loads are in flight together
+#pragma unroll 4
       for (int32_t v = v0 + static_cast<int32_t>(threadIdx.x); v < v1; v += kPqThreads) {
         int32_t lo = 0, hi = n - 1;  // the run holding v: the last with s_first <= v
         while (lo < hi) {
@@ -402,7 +404,7 @@ __global__ void __launch_bounds__(kPqThreads) parquet_pages_kernel(PageDev* page
           const uint8_t* q = base + s_start[lo] + (bit >> 3);
           uint64_t x = 0;
           const int nb = (static_cast<int>(bit & 7) + bw + 7) / 8;  // bytes the value spans (within the run)
-          for (int k = 0; k < nb; ++k) x |= static_cast<uint64_t>(q[k]) << (8 * k);
+          for (int k = 0; k < nb; ++k) x |= static_cast<uint64_t>(__ldg(q + k)) << (8 * k);
           idx = static_cast<uint32_t>((x >> (bit & 7)) & mask);
         }
         if (pg.width > 0) {
