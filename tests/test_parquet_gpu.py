@@ -136,3 +136,24 @@ def test_reads_the_package_writer(gpu, kw):
     want = expected("plain_none_v1")
     got = ops.parquet_read(write_parquet(want, **kw))
     same(got, want)
+
+
+@pytest.mark.parametrize("ty", ["int32", "int64", "utf8"])
+def test_dictionary_index_out_of_range(gpu, ty, monkeypatch):
+    """A data page whose dictionary index names no dictionary entry (every
+    index one past the value written, so the largest is one past the
+    dictionary; the bit width still holds it) is refused as malformed, for
+    fixed-width columns (decoded to values in the page pass) and byte-array
+    columns (looked up in the values pass) alike."""
+    from flexpushdowndb_gb300 import parquet_writer as pw
+
+    vals = np.arange(3000) % 3  # three distinct values: two-bit indices 0..2
+    column = Column("c", ty, [f"s{v}" for v in vals] if ty == "utf8" else vals)
+    t = Table([column])
+    assert ops.parquet_read(pw.write_parquet(t)).column("c").to_list() == column.to_list()
+    orig = pw._bitpacked
+    monkeypatch.setattr(pw, "_bitpacked", lambda idx, bw: orig(idx + 1, bw))
+    bad = pw.write_parquet(t)
+    with pytest.raises(GfpdbError) as ei:
+        ops.parquet_read(bad)
+    assert "malformed" in ei.value.message
