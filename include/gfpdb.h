@@ -445,8 +445,18 @@ int32_t gfpdb_plan_validate(const char* plan_json);
  * is folded into the join ("buildFilters": the join build leaves out the
  * rows a filter rejects); chains of inner joins become one HashJoinChainPOp.
  * Writes the fused plan's JSON into out_json when capacity holds it;
- * *needed is its size with the terminating zero. The fusion passes replace
- * no reference interface: the reference runs each operator as planned. */
+ * *needed is its size with the terminating zero. Fields the fused operators
+ * carry (a plan may also give them itself):
+ *   HashJoinArrowPOp / a HashJoinChainPOp join: "buildFilters":
+ *     [{"column": build column, "creator": BloomFilterCreatePOp}], bloom
+ *     filters the build side's rows must pass;
+ *   BloomFilterCreatePOp: "filters": [{"origin", "bloomFilterColumn",
+ *     "bitsPerKey", "numHashes", "bloomFilterUsePOps"}] for several filters
+ *     over the same rows (each sent under its origin's name), and
+ *     "dataConsumers": the consumers that take its rows (default: every
+ *     consumer that is not a filter receiver).
+ * The fusion passes replace no reference interface: the reference runs each
+ * operator as planned. */
 int32_t gfpdb_plan_fuse(const char* plan_json, char* out_json, int64_t capacity, int64_t* needed);
 
 /* Plan the bloom-filter predicate transfer of a join graph (host only), as
