@@ -74,10 +74,24 @@ class Plan:
         self.op(creator)["bloomFilterUsePOps"].append(name)
         return name
 
-    def hash_join(self, name: str, build: str, probe: str, build_key: str, probe_key: str,
-                  project: Sequence[str] | None = None, load_factor: float = 0.5) -> str:
+    def hash_join(self, name: str, build: str, probe: str, build_key: str | Sequence[str],
+                  probe_key: str | Sequence[str], project: Sequence[str] | None = None, load_factor: float = 0.5,
+                  join_type: str = "INNER") -> str:
+        """HashJoinArrowPOp. Keys are one column per side, or equal-length
+        lists (HashJoinPredicate's column lists); `join_type` is one of
+        INNER, LEFT (every build row kept), RIGHT (every probe row kept),
+        FULL, LEFT_SEMI (matched build rows), RIGHT_SEMI (matched probe
+        rows)."""
         op = {"type": "HashJoinArrowPOp", "name": name, "buildProducers": [build], "probeProducers": [probe],
-              "buildKey": build_key, "probeKey": probe_key, "joinType": "INNER", "loadFactor": load_factor}
+              "joinType": join_type, "loadFactor": load_factor}
+        if isinstance(build_key, str) and isinstance(probe_key, str):
+            op["buildKey"], op["probeKey"] = build_key, probe_key
+        else:
+            bk = [build_key] if isinstance(build_key, str) else list(build_key)
+            pk = [probe_key] if isinstance(probe_key, str) else list(probe_key)
+            if not bk or len(bk) != len(pk):
+                raise ValueError("a hash join needs as many probe keys as build keys, at least one")
+            op["buildKeys"], op["probeKeys"] = bk, pk
         if project:
             op["projectColumnNames"] = list(project)
         self._add(op)

@@ -7,7 +7,7 @@ import json
 
 import pytest
 
-from flexpushdowndb_gb300 import plan, workloads
+from flexpushdowndb_gb300 import GfpdbError, plan, workloads
 
 
 def by_name(fused):
@@ -53,10 +53,9 @@ def two_table(join_type="INNER", use_column="d_pk", extra_consumer=False, probe_
     c = p.bloom_create("bw_create", "scan_f", "fk")
     u = p.bloom_use("bw_use", "scan_d", c, use_column)
     if probe_side:
-        p.hash_join("join", "bw_create", u, "fk", "d_pk", ["x", "d_v"])
+        p.hash_join("join", "bw_create", u, "fk", "d_pk", ["x", "d_v"], join_type=join_type)
     else:
-        p.hash_join("join", u, c, "d_pk", "fk", ["x", "d_v"])
-    p.op("join")["joinType"] = join_type
+        p.hash_join("join", u, c, "d_pk", "fk", ["x", "d_v"], join_type=join_type)
     p.collate("collate", "join")
     if extra_consumer:
         p.collate("collate2", u)
@@ -171,3 +170,27 @@ def test_fusion_is_idempotent(make):
     twice = plan.fused(json.dumps(once))
     assert twice == once
     plan.validate(json.dumps(once))
+
+
+def test_plan_builder_join_types_and_key_lists():
+    p = plan.Plan()
+    p.scan("a", "ta", ["k1", "k2", "v"])
+    p.scan("b", "tb", ["j1", "j2", "w"])
+    p.hash_join("j", "a", "b", ["k1", "k2"], ["j1", "j2"], ["v", "w", "k1"])
+    p.hash_join("l", "j", "b", "k1", "j1", ["v", "w"], join_type="LEFT")
+    p.collate("c", "l")
+    op = p.op("j")
+    assert op["buildKeys"] == ["k1", "k2"] and op["probeKeys"] == ["j1", "j2"] and op["joinType"] == "INNER"
+    assert "buildKey" not in op
+    assert p.op("l")["joinType"] == "LEFT" and p.op("l")["buildKey"] == "k1"
+    plan.validate(p)
+    with pytest.raises(ValueError):
+        plan.Plan().hash_join("x", "a", "b", ["k1", "k2"], ["j1"])
+    # outer and semi joins take one key column per side
+    q = plan.Plan()
+    q.scan("a", "ta", ["k1", "k2"])
+    q.scan("b", "tb", ["j1", "j2"])
+    q.hash_join("j", "a", "b", ["k1", "k2"], ["j1", "j2"], join_type="LEFT")
+    q.collate("c", "j")
+    with pytest.raises(GfpdbError):
+        plan.validate(q)
