@@ -194,3 +194,63 @@ def test_plan_builder_join_types_and_key_lists():
     q.collate("c", "j")
     with pytest.raises(GfpdbError):
         plan.validate(q)
+
+
+def random_join_tree(seed):
+    """A random join tree over 3-6 tables, planned by the predicate-transfer
+    planner, then joined child after child into the first table's rows."""
+    import random
+
+    rng = random.Random(seed)
+    k = rng.randint(3, 6)
+    types = ["INNER", "INNER", "INNER", "LEFT", "RIGHT", "FULL", "LEFT_SEMI", "RIGHT_SEMI"]
+    p = plan.Plan()
+    tables, joins, edges = {}, [], []
+    for i in range(k):
+        cols = [f"t{i}_pk"] + [f"t{i}_c{j}" for j in range(i + 1, k)]
+        p.scan(f"t{i}", f"table{i}", cols)
+        tables[f"t{i}"] = (rng.choice([50, 500, 5000, 50000, 500000]), rng.choice([1.0, 0.5, 0.1]))
+    for i in range(1, k):
+        parent = rng.randrange(i)
+        jt = rng.choice(types)
+        edges.append((parent, i, jt))
+        joins.append({"left": f"t{parent}", "right": f"t{i}", "leftColumns": [f"t{parent}_c{i}"],
+                      "rightColumns": [f"t{i}_pk"], "joinType": jt})
+    out = p.predicate_transfer(tables, joins)
+    tail = out["t0"]
+    for parent, child, jt in edges:
+        name = f"join{child}"
+        p.hash_join(name, out[f"t{child}"], tail, f"t{child}_pk", f"t{parent}_c{child}", join_type=jt)
+        tail = name
+    p.collate("collate", tail)
+    return p
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_fusion_invariants_on_random_join_trees(seed):
+    p = random_join_tree(seed)
+    plan.validate(p)
+    f = plan.fused(p)
+    plan.validate(json.dumps(f))
+    assert plan.fused(json.dumps(f)) == f
+    ops = by_name(f)
+    # (join, the operator that receives its filters: the join, or its chain)
+    joins = [(o, o["name"]) for o in f["ops"] if o["type"] == "HashJoinArrowPOp"]
+    joins += [(j, o["name"]) for o in f["ops"] if o["type"] == "HashJoinChainPOp" for j in o["joins"]]
+    for j, receiver in joins:
+        for bf in j.get("buildFilters", []):
+            # only inner joins on one key test filters, all on that key
+            assert j.get("joinType", "INNER") == "INNER"
+            assert bf["column"] == j["buildKey"]
+            # the filter's creator (possibly merged into another operator) sends it to this join
+            owner = next(o for o in f["ops"] if o["type"] == "BloomFilterCreatePOp" and
+                         (o["name"] == bf["creator"] or
+                          any(x.get("origin") == bf["creator"] for x in o.get("filters", []))))
+            entries = owner.get("filters") or [dict(owner, origin=owner["name"])]
+            entry = next(x for x in entries if x.get("origin", owner["name"]) == bf["creator"])
+            assert receiver in entry["bloomFilterUsePOps"]
+    # every bloom use left still has a filter for each of its columns
+    for u in (o for o in f["ops"] if o["type"] == "BloomFilterUsePOp"):
+        n = len(u.get("bloomFilterColumns", [u.get("bloomFilterColumn")]))
+        assert len(u.get("creators", [None] * n)) == n
+    assert ops["collate"]["type"] == "CollatePOp"
