@@ -254,3 +254,38 @@ def test_fusion_invariants_on_random_join_trees(seed):
         n = len(u.get("bloomFilterColumns", [u.get("bloomFilterColumn")]))
         assert len(u.get("creators", [None] * n)) == n
     assert ops["collate"]["type"] == "CollatePOp"
+
+
+def test_fused_plan_text_round_trips_awkward_names():
+    """Operator and column names with quotes, backslashes, control
+    characters and non-ASCII bytes come back from gfpdb_plan_fuse as they
+    went in."""
+    names = ['q"uote', "back\\slash", "tab\there", "line\nbreak", "café ☃"]
+    p = plan.Plan()
+    prev = p.scan(names[0], "t", ["k"])
+    for n in names[1:]:
+        prev = p.filter(n, prev, None)
+    p.collate("collate", prev)
+    f = plan.fused(p)
+    assert [o["name"] for o in f["ops"]] == names + ["collate"]
+    assert f == plan.fused(json.dumps(f))
+
+
+def test_plan_fuse_errors():
+    import ctypes
+
+    from flexpushdowndb_gb300 import _abi
+
+    L = _abi.lib()
+    need = ctypes.c_int64()
+    assert L.gfpdb_plan_fuse(b"{not json", None, 0, ctypes.byref(need)) != 0
+    assert "JSON" in L.gfpdb_last_error().decode()
+    text = workloads.star_plan().to_json().encode()
+    rc = L.gfpdb_plan_fuse(text, None, 0, ctypes.byref(need))
+    assert rc != 0 and need.value > 1
+    small = ctypes.create_string_buffer(need.value - 1)
+    assert L.gfpdb_plan_fuse(text, small, need.value - 1, ctypes.byref(need)) != 0
+    buf = ctypes.create_string_buffer(need.value)
+    assert L.gfpdb_plan_fuse(text, buf, need.value, ctypes.byref(need)) == 0
+    assert json.loads(buf.value.decode()) == plan.fused(workloads.star_plan())
+    assert L.gfpdb_plan_fuse(None, None, 0, ctypes.byref(need)) != 0
