@@ -1941,8 +1941,8 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
 }
 
 // Pipeline fusion: a BloomFilterUsePOp whose only consumer is an inner
-// HashJoinArrowPOp on one key column, which takes it on its build side, and
-// whose filters are all on that key, is folded into the join: its data
+// HashJoinArrowPOp on one key column, which takes it as its only build
+// producer, and whose filters are all on that key, is folded into the join: its data
 // producers feed the join's build side directly, its filters' creators send
 // them to the join ("buildFilters"), and the join build leaves out the rows
 // a filter rejects (join_build_table) instead of a selection pass copying
@@ -1986,8 +1986,11 @@ json::Value fuse_build_filters(const json::Value& plan) {
       if (J.at("type").str() != "HashJoinArrowPOp" || J.get_str("joinType", "INNER") != "INNER" ||
           J.contains("buildKeys") || !J.contains("buildKey"))
         continue;
+      // the use must be the build side's only producer: the build tests its
+      // filters on every build row, and rows from another producer were
+      // never filtered
       auto bp = J.str_list("buildProducers"), pp = J.str_list("probeProducers");
-      if (std::find(bp.begin(), bp.end(), un) == bp.end() || std::find(pp.begin(), pp.end(), un) != pp.end()) continue;
+      if (bp != std::vector<std::string>{un} || std::find(pp.begin(), pp.end(), un) != pp.end()) continue;
       const std::string key = J.at("buildKey").str();
       bool on_key = true;
       for (auto& c : cols) on_key &= c == key;

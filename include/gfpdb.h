@@ -441,7 +441,7 @@ int32_t gfpdb_plan_validate(const char* plan_json);
  * executes when the plan's "fusePipelines" is true (the default). Chains of
  * BloomFilterUsePOps on one input become one BloomFilterUsePOp; a
  * BloomFilterUsePOp whose only consumer is an inner HashJoinArrowPOp on one
- * key column, taking it on its build side, with its filters on that key,
+ * key column, taking it as its only build producer, with its filters on that key,
  * is folded into the join ("buildFilters": the join build leaves out the
  * rows a filter rejects); chains of inner joins become one HashJoinChainPOp.
  * Writes the fused plan's JSON into out_json when capacity holds it;

@@ -289,3 +289,20 @@ def test_plan_fuse_errors():
     assert L.gfpdb_plan_fuse(text, buf, need.value, ctypes.byref(need)) == 0
     assert json.loads(buf.value.decode()) == plan.fused(workloads.star_plan())
     assert L.gfpdb_plan_fuse(None, None, 0, ctypes.byref(need)) != 0
+
+
+def test_build_filter_not_folded_beside_another_build_producer():
+    """A join whose build side has a second producer keeps its bloom use:
+    the second producer's rows were never filtered."""
+    p = plan.Plan()
+    p.scan("scan_d", "dim", ["d_pk", "d_v"])
+    p.scan("scan_e", "dim2", ["d_pk", "d_v"])
+    p.scan("scan_f", "fact", ["fk", "x"])
+    c = p.bloom_create("bw_create", "scan_f", "fk")
+    u = p.bloom_use("bw_use", "scan_d", c, "d_pk")
+    p.hash_join("join", u, c, "d_pk", "fk", ["x", "d_v"])
+    p.op("join")["buildProducers"].append("scan_e")
+    p.connect("scan_e", "join")
+    p.collate("collate", "join")
+    ops = by_name(plan.fused(p))
+    assert "bw_use" in ops and "buildFilters" not in ops["join"]
