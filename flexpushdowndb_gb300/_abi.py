@@ -183,6 +183,7 @@ SIGNATURES = {
     "gfpdb_plan_validate": (_I32, [ctypes.c_char_p]),
     "gfpdb_plan_predicate_transfer": (_I32, [ctypes.c_char_p, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)]),
     "gfpdb_plan_fuse": (_I32, [ctypes.c_char_p, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)]),
+    "gfpdb_parquet_layout": (_I32, [_P, _I64, _CP, _I32, _I64, _I64, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)]),
     "gfpdb_graph_cache_clear": (_I32, []),
     "gfpdb_server_create": (_I32, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "gfpdb_server_register_table": (_I32, [_P, ctypes.c_char_p, _S, _A]),

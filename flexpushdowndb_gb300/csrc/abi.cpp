@@ -11,6 +11,7 @@
 #include "../../include/gfpdb.h"
 #include "host/batchspec.h"
 #include "host/handles.h"
+#include "host/parquet_meta.h"
 #include "host/pop.h"
 #include "kernels/launch.h"
 
@@ -891,6 +892,87 @@ int32_t gfpdb_parquet_read(const void* file, int64_t n_bytes, const char* const*
     if (columns != nullptr && n_columns >= 0) names = names_of(columns, n_columns);
     auto ts = parquet_read(static_cast<const uint8_t*>(file), n_bytes, names, start_pos, end_pos, s);
     export_tupleset(ts, out_schema, out, false, s);
+  });
+}
+
+int32_t gfpdb_parquet_layout(const void* file, int64_t n_bytes, const char* const* columns, int32_t n_columns,
+                             int64_t start_pos, int64_t end_pos, char* out_json, int64_t capacity, int64_t* needed) {
+  return guarded([&] {
+    require(file != nullptr && needed != nullptr && n_bytes >= 0, "null argument");
+    std::vector<std::string> names;
+    if (columns != nullptr && n_columns >= 0) names = names_of(columns, n_columns);
+    const parquet::Layout L =
+        parquet::read_layout(static_cast<const uint8_t*>(file), n_bytes, names, start_pos, end_pos);
+    auto num = [](int64_t v) {
+      json::Value x;
+      x.kind = json::Value::Number;
+      x.is_integer = true;
+      x.i = v;
+      return x;
+    };
+    auto str = [](const std::string& v) {
+      json::Value x;
+      x.kind = json::Value::String;
+      x.s = v;
+      return x;
+    };
+    auto obj = [] {
+      json::Value x;
+      x.kind = json::Value::Object;
+      return x;
+    };
+    auto arr = [] {
+      json::Value x;
+      x.kind = json::Value::Array;
+      return x;
+    };
+    json::Value out = obj(), cols = arr(), groups = arr(), chunks = arr(), pages = arr();
+    for (const auto& c : L.columns) {
+      json::Value o = obj();
+      o.o.emplace_back("name", str(c.name));
+      o.o.emplace_back("type", str(dtype_name(c.dtype)));
+      o.o.emplace_back("physicalType", num(c.physical));
+      json::Value req;
+      req.kind = json::Value::Bool;
+      req.b = c.repetition == 0;
+      o.o.emplace_back("required", req);
+      cols.a.push_back(o);
+    }
+    for (const auto& g : L.row_groups) {
+      json::Value o = obj();
+      o.o.emplace_back("offset", num(g.offset));
+      o.o.emplace_back("rows", num(g.rows));
+      groups.a.push_back(o);
+    }
+    for (const auto& c : L.chunks) {
+      json::Value o = obj();
+      o.o.emplace_back("begin", num(c.begin));
+      o.o.emplace_back("end", num(c.end));
+      chunks.a.push_back(o);
+    }
+    for (const auto& p : L.pages) {
+      json::Value o = obj();
+      o.o.emplace_back("column", num(p.column));
+      o.o.emplace_back("chunk", num(p.chunk));
+      o.o.emplace_back("pageType", num(p.type));
+      o.o.emplace_back("encoding", num(p.encoding));
+      o.o.emplace_back("codec", num(p.codec));
+      o.o.emplace_back("offset", num(p.data_offset));
+      o.o.emplace_back("compressedBytes", num(p.compressed));
+      o.o.emplace_back("uncompressedBytes", num(p.uncompressed));
+      o.o.emplace_back("numValues", num(p.num_values));
+      o.o.emplace_back("firstRow", num(p.first_row));
+      pages.a.push_back(o);
+    }
+    out.o.emplace_back("numRows", num(L.num_rows));
+    out.o.emplace_back("columns", cols);
+    out.o.emplace_back("rowGroups", groups);
+    out.o.emplace_back("chunks", chunks);
+    out.o.emplace_back("pages", pages);
+    const std::string text = json::dump(out);
+    *needed = static_cast<int64_t>(text.size()) + 1;
+    if (out_json == nullptr || capacity < *needed) fail(GFPDB_EINVAL, "output buffer too small (see *needed)");
+    std::memcpy(out_json, text.c_str(), text.size() + 1);
   });
 }
 

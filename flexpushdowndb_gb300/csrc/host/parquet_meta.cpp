@@ -9,6 +9,43 @@ namespace gfpdb::parquet {
 
 namespace {
 
+// Well-formed UTF-8 (RFC 3629): no overlong forms, surrogates or code points
+// past U+10FFFF.
+bool valid_utf8(const std::string& s) {
+  const auto* p = reinterpret_cast<const unsigned char*>(s.data());
+  const size_t n = s.size();
+  for (size_t i = 0; i < n;) {
+    const unsigned c = p[i];
+    int len;
+    unsigned cp;
+    if (c < 0x80) {
+      ++i;
+      continue;
+    } else if ((c & 0xE0) == 0xC0) {
+      len = 2;
+      cp = c & 0x1F;
+    } else if ((c & 0xF0) == 0xE0) {
+      len = 3;
+      cp = c & 0x0F;
+    } else if ((c & 0xF8) == 0xF0) {
+      len = 4;
+      cp = c & 0x07;
+    } else {
+      return false;
+    }
+    if (i + static_cast<size_t>(len) > n) return false;
+    for (int k = 1; k < len; ++k) {
+      if ((p[i + k] & 0xC0) != 0x80) return false;
+      cp = (cp << 6) | (p[i + k] & 0x3F);
+    }
+    if ((len == 2 && cp < 0x80) || (len == 3 && cp < 0x800) || (len == 4 && cp < 0x10000) || cp > 0x10FFFF ||
+        (cp >= 0xD800 && cp <= 0xDFFF))
+      return false;
+    i += static_cast<size_t>(len);
+  }
+  return true;
+}
+
 // Thrift compact protocol (the encoding of Parquet's metadata): field
 // headers carry an id delta and a type nibble, integers are zigzag varints,
 // binaries and lists a varint length.
@@ -65,6 +102,14 @@ class Reader {
   }
   bool boolean(int type) { return type == CT_TRUE; }  // a struct field's value is its type
 
+  // An element of a list, set or map: booleans there are one byte each (in
+  // a struct a boolean lives in its field header), so every element consumes
+  // input and a corrupt element count runs into the end of the footer.
+  void skip_element(int type, int depth) {
+    if (type == CT_TRUE || type == CT_FALSE) byte();
+    else skip(type, depth);
+  }
+
   void skip(int type, int depth = 0) {
     if (depth > 32) fail(GFPDB_EINVAL, "Parquet metadata nests too deeply");
     switch (type) {
@@ -82,10 +127,7 @@ class Reader {
       case CT_SET: {
         int elem = 0;
         const int64_t n = list(&elem);
-        for (int64_t i = 0; i < n; ++i) {
-          if (elem == CT_TRUE || elem == CT_FALSE) byte();  // booleans in a list are one byte each
-          else skip(elem, depth + 1);
-        }
+        for (int64_t i = 0; i < n; ++i) skip_element(elem, depth + 1);
         return;
       }
       case CT_MAP: {
@@ -93,8 +135,8 @@ class Reader {
         if (n == 0) return;
         const uint8_t kv = byte();
         for (int64_t i = 0; i < n; ++i) {
-          skip(kv >> 4, depth + 1);
-          skip(kv & 0x0f, depth + 1);
+          skip_element(kv >> 4, depth + 1);
+          skip_element(kv & 0x0f, depth + 1);
         }
         return;
       }
@@ -312,6 +354,8 @@ Layout read_layout(const uint8_t* file, int64_t size, const std::vector<std::str
   // a flat schema: the root, then one leaf per column
   std::vector<SchemaEl> leaves(schema.begin() + 1, schema.end());
   for (auto& e : leaves) {
+    // names travel into Arrow schemas, whose names are UTF-8
+    if (!valid_utf8(e.name)) fail(GFPDB_EINVAL, "Parquet column name is not UTF-8");
     if (e.num_children > 0) fail(GFPDB_EUNSUPPORTED, "nested Parquet columns ('" + e.name + "')");
     if (e.repetition == 2) fail(GFPDB_EUNSUPPORTED, "repeated Parquet column '" + e.name + "'");
   }
@@ -348,6 +392,7 @@ Layout read_layout(const uint8_t* file, int64_t size, const std::vector<std::str
                                   ? first.dict_page_offset
                                   : first.data_page_offset;
     if (start_pos <= end_pos && (first_off < start_pos || first_off > end_pos)) continue;
+    L.row_groups.push_back(RowGroupInfo{first_off, g.num_rows});
     L.num_rows += g.num_rows;
     for (size_t k = 0; k < picked.size(); ++k) {
       const ChunkMeta& m = g.chunks[picked[k]];

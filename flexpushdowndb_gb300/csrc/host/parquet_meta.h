@@ -58,10 +58,18 @@ struct ChunkRange {
   int64_t begin = 0, end = 0;
 };
 
+// A selected row group: the file offset of its first column chunk (the
+// position readRange selects it by) and its rows.
+struct RowGroupInfo {
+  int64_t offset = 0;
+  int64_t rows = 0;
+};
+
 struct Layout {
   std::vector<ColumnInfo> columns;  // the selected columns, in the requested order
   std::vector<PageInfo> pages;
   std::vector<ChunkRange> chunks;
+  std::vector<RowGroupInfo> row_groups;
   int64_t num_rows = 0;             // rows of the selected row groups
 };
 

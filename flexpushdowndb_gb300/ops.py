@@ -263,6 +263,28 @@ def parquet_read(source, columns: Sequence[str] | None = None, start_pos: int = 
     return import_result(s, a)
 
 
+def parquet_layout(source, columns: Sequence[str] | None = None, start_pos: int = 0, end_pos: int = -1) -> dict:
+    """The columns, row groups, column chunks and pages of a Parquet file
+    that parquet_read with the same arguments reads (gfpdb_parquet_layout,
+    host only); `source` is the file's bytes or a path."""
+    import json
+
+    if isinstance(source, (str, Path)):
+        source = Path(source).read_bytes()
+    buf = np.frombuffer(source, dtype=np.uint8) if isinstance(source, (bytes, bytearray)) else source
+    names, n = _names(columns)
+    L = _abi.lib()
+    need = ctypes.c_int64()
+    rc = L.gfpdb_parquet_layout(buf.ctypes.data, buf.nbytes, names, n, start_pos, end_pos, None, 0,
+                                ctypes.byref(need))
+    if need.value <= 0:
+        _abi.check(rc)
+    out = ctypes.create_string_buffer(need.value)
+    _abi.check(L.gfpdb_parquet_layout(buf.ctypes.data, buf.nbytes, names, n, start_pos, end_pos, out, need.value,
+                                      ctypes.byref(need)))
+    return json.loads(out.value.decode())
+
+
 def csv_read(text: bytes | np.ndarray | int, fields: Sequence[tuple[str, str]], columns: Sequence[str] | None = None,
              delimiter: str = ",", has_header: bool = False, device_ptr: int | None = None, stream=None,
              to_host: bool = True):

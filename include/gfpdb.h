@@ -348,6 +348,21 @@ int32_t gfpdb_parquet_read(const void* file, int64_t n_bytes, const char* const*
                            int64_t start_pos, int64_t end_pos, struct ArrowSchema* out_schema,
                            struct ArrowDeviceArray* out, void* stream);
 
+/* The layout of a Parquet file held in host memory (host only, no CUDA
+ * calls), as JSON: {"numRows", "columns": [{"name", "type", "physicalType",
+ * "required"}], "rowGroups": [{"offset", "rows"}], "chunks": [{"begin",
+ * "end"}], "pages": [{"column", "chunk", "pageType", "encoding", "codec",
+ * "offset", "compressedBytes", "uncompressedBytes", "numValues",
+ * "firstRow"}]} for the columns and row groups gfpdb_parquet_read with the
+ * same arguments reads (a row group's offset is the file position of its
+ * first column chunk, which start_pos / end_pos select it by; the reference
+ * splits a file into scan ranges the same way, ParquetReader::readRange,
+ * fpdb-tuple/src/parquet/ParquetReader.cpp:44-77). Files the reader refuses
+ * are refused here with the same error. Written into out_json when capacity
+ * holds it; *needed is its size with the terminating zero. */
+int32_t gfpdb_parquet_layout(const void* file, int64_t n_bytes, const char* const* columns, int32_t n_columns,
+                             int64_t start_pos, int64_t end_pos, char* out_json, int64_t capacity, int64_t* needed);
+
 /* The same over a file of the local file system (LocalParquetReader::read). */
 int32_t gfpdb_parquet_read_file(const char* path, const char* const* columns, int32_t n_columns, int64_t start_pos,
                                 int64_t end_pos, struct ArrowSchema* out_schema, struct ArrowDeviceArray* out,

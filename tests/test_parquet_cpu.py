@@ -72,3 +72,77 @@ def test_package_writer_is_read_by_pyarrow():
                 assert np.array_equal(np.array(got).view(np.int64), c.values.view(np.int64))
             else:
                 assert got == c.to_list(), c.name
+
+
+def test_layout_row_groups_match_pyarrow_metadata():
+    """The host parser's row groups (offset of the first column chunk, rows)
+    are those pyarrow recorded when it wrote each fixture."""
+    from flexpushdowndb_gb300 import ops
+
+    layout = json.loads((GOLDEN / "parquet" / "layout.json").read_text())
+    for name, groups in layout.items():
+        lay = ops.parquet_layout((GOLDEN / "parquet" / f"{name}.parquet").read_bytes())
+        assert [{"offset": g["offset"], "rows": g["rows"]} for g in lay["rowGroups"]] == groups
+        assert lay["numRows"] == sum(g["rows"] for g in groups)
+        # a range read selects the row groups whose first chunk starts inside it
+        if len(groups) > 1:
+            part = ops.parquet_layout((GOLDEN / "parquet" / f"{name}.parquet").read_bytes(), ["i64"],
+                                      groups[1]["offset"], groups[-1]["offset"])
+            assert [g["offset"] for g in part["rowGroups"]] == [g["offset"] for g in groups[1:]]
+            assert [c["name"] for c in part["columns"]] == ["i64"]
+
+
+def _varint(v):
+    out = bytearray()
+    while True:
+        b = v & 0x7F
+        v >>= 7
+        out.append(b | (0x80 if v else 0))
+        if not v:
+            return bytes(out)
+
+
+def test_footer_with_a_huge_boolean_map_is_refused():
+    """An unknown footer field holding a map of 2^40 boolean pairs: each
+    pair is a byte of input, so the count runs into the footer's end at once
+    (it must not be walked pair by pair without reading)."""
+    from flexpushdowndb_gb300 import GfpdbError, ops
+
+    footer = bytes([0x0B]) + _varint(20 << 1) + _varint(1 << 40) + bytes([0x11, 0x01, 0x01, 0x00])
+    data = b"PAR1" + footer + len(footer).to_bytes(4, "little") + b"PAR1"
+    with pytest.raises(GfpdbError):
+        ops.parquet_layout(data)
+
+
+def test_mutated_files_parse_or_are_refused():
+    """Random byte changes in the fixtures' footers, anywhere in the file,
+    in the footer length, and truncations: the host parser reads the file
+    or refuses it with an error, never reading outside the buffer."""
+    import random
+
+    from flexpushdowndb_gb300 import GfpdbError, ops
+
+    files = sorted((GOLDEN / "parquet").glob("*.parquet"))
+    rng = random.Random(2024)
+    outcomes = {"read": 0, "refused": 0}
+    for _ in range(1500):
+        b = bytearray(rng.choice(files).read_bytes())
+        n = len(b)
+        flen = int.from_bytes(b[n - 8:n - 4], "little")
+        mode = rng.random()
+        for _ in range(rng.randint(1, 8)):
+            if mode < 0.6:
+                i = rng.randrange(max(4, n - 8 - flen), n - 8)
+            elif mode < 0.8:
+                i = rng.randrange(n)
+            else:
+                i = rng.randrange(n - 8, n - 4)
+            b[i] = rng.randrange(256)
+        if rng.random() < 0.1:
+            b = b[:rng.randrange(n)]
+        try:
+            ops.parquet_layout(bytes(b))
+            outcomes["read"] += 1
+        except GfpdbError:
+            outcomes["refused"] += 1
+    assert outcomes["read"] > 0 and outcomes["refused"] > 0
