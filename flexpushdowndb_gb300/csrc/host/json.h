@@ -91,6 +91,8 @@ class Parser {
  private:
   const std::string& t_;
   size_t p_ = 0;
+  int depth_ = 0;  // open objects and arrays: the descent is recursive, so bounded
+  static constexpr int kMaxDepth = 512;
 
   [[noreturn]] void fail(const std::string& what) {
     throw std::runtime_error("JSON parse error at offset " + std::to_string(p_) + ": " + what);
@@ -119,6 +121,14 @@ class Parser {
   Value value() {
     char c = peek();
     Value v;
+    if ((c == '{' || c == '[') && ++depth_ > kMaxDepth) fail("nesting deeper than 512 levels");
+    struct Leave {
+      int* d;
+      bool on;
+      ~Leave() {
+        if (on) --*d;
+      }
+    } leave{&depth_, c == '{' || c == '['};
     if (c == '{') {
       v.kind = Value::Object;
       ++p_;

@@ -306,3 +306,49 @@ def test_build_filter_not_folded_beside_another_build_producer():
     p.collate("collate", "join")
     ops = by_name(plan.fused(p))
     assert "bw_use" in ops and "buildFilters" not in ops["join"]
+
+
+def test_deeply_nested_plan_text_is_refused():
+    """The plan reader descends recursively: nesting past 512 levels is an
+    error, not a host stack overflow."""
+    from flexpushdowndb_gb300 import _abi
+
+    for text in ("[" * 200_000, '{"a":' * 200_000, '{"ops": ' + "[" * 600 + "]" * 600 + "}"):
+        assert _abi.lib().gfpdb_plan_validate(text.encode()) != 0
+        assert "nesting" in _abi.lib().gfpdb_last_error().decode()
+    ok = '{"ops": ' + "[" * 100 + "]" * 100 + "}"
+    _abi.lib().gfpdb_plan_validate(ok.encode())  # parses (and is refused only as a plan)
+    assert "nesting" not in _abi.lib().gfpdb_last_error().decode()
+
+
+def test_mutated_plans_validate_or_are_refused():
+    """Random edits of plan texts (bytes changed, dropped, inserted;
+    truncations): the plan checker and the fusion passes return a status,
+    never crash."""
+    import ctypes
+    import random
+
+    from flexpushdowndb_gb300 import _abi
+
+    L = _abi.lib()
+    base = [workloads.star_plan().to_json(), workloads.star_plan_planned().to_json(),
+            workloads.two_table_plan().to_json()]
+    rng = random.Random(77)
+    alphabet = b'{}[]",:0123456789-.eE truefalsnul\\/abcdXYZ\xff'
+    need = ctypes.c_int64()
+    valid = 0
+    for _ in range(1500):
+        b = bytearray(rng.choice(base).encode())
+        for _ in range(rng.randint(1, 6)):
+            r, i = rng.random(), rng.randrange(len(b))
+            if r < 0.5:
+                b[i] = rng.choice(alphabet)
+            elif r < 0.75:
+                del b[i]
+            else:
+                b.insert(i, rng.choice(alphabet))
+        if rng.random() < 0.05:
+            b = b[:rng.randrange(len(b))]
+        valid += L.gfpdb_plan_validate(bytes(b)) == 0
+        L.gfpdb_plan_fuse(bytes(b), None, 0, ctypes.byref(need))
+    assert 0 < valid < 1500
