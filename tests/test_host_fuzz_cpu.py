@@ -158,3 +158,40 @@ def test_random_transfer_specs_plan_or_are_refused():
         else:
             refused += 1
     assert planned > 50 and refused > 50
+
+
+def test_random_group_specs_compile_or_are_refused():
+    L = _abi.lib()
+    rng = random.Random(5)
+    fns = ["SUM", "COUNT", "AVG", "MIN", "MAX", "AVG_REDUCE", "sum", "BOGUS", "", None]
+
+    def expr():
+        return rng.choice([{"type": "Column", "name": rng.choice(["a", "b", ""])},
+                           {"type": "Multiply", "left": {"type": "Column", "name": "a"},
+                            "right": {"type": "Column", "name": "b"}},
+                           {"type": "NumericLiteral", "dataType": "int64", "value": 3}, None, 5, "x",
+                           {"type": "Bogus"}])
+
+    h = ctypes.c_void_p()
+    made = refused = 0
+    for _ in range(1500):
+        aggs = []
+        for _ in range(rng.randint(0, 9)):
+            a = {"function": rng.choice(fns), "name": rng.choice(["s", "c", "", 's"q'])}
+            if rng.random() < 0.7:
+                a["expr"] = expr()
+            if rng.random() < 0.1:
+                a = rng.choice([None, 3, "x", []])
+            aggs.append(a)
+        spec = {"groupColumnNames": [rng.choice(["a", "b", "c", ""]) for _ in range(rng.randint(0, 10))],
+                "aggregates": aggs}
+        if rng.random() < 0.1:
+            spec.pop(rng.choice(list(spec)))
+        if rng.random() < 0.1:
+            spec["groupsHint"] = rng.choice([-1, 0, 2**62, "x"])
+        if L.gfpdb_group_create(json.dumps(spec).encode(), ctypes.byref(h)) == 0:
+            L.gfpdb_group_free(h)
+            made += 1
+        else:
+            refused += 1
+    assert made > 50 and refused > 50
