@@ -1873,11 +1873,7 @@ json::Value* jfind(json::Value& o, const std::string& key) {
 // operator keeps the last one's name, so every reference to the chain's end
 // stays valid. Results are unchanged: a row survives the fused pass exactly
 // when it survives every filter of the chain.
-json::Value fuse_bloom_chains(const json::Value& plan) {
-  json::Value out = plan;
-  json::Value* ops_v = jfind(out, "ops");
-  if (ops_v == nullptr) return out;
-  auto& ops = ops_v->a;
+void fuse_bloom_chains(std::vector<json::Value>& ops) {
   for (;;) {
     std::map<std::string, std::vector<std::string>> producers, creators;
     for (auto& o : ops) {
@@ -1937,7 +1933,6 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
     }
     ops.erase(ops.begin() + first);
   }
-  return out;
 }
 
 // Pipeline fusion: a BloomFilterUsePOp whose only consumer is an inner
@@ -1950,11 +1945,7 @@ json::Value fuse_bloom_chains(const json::Value& plan) {
 // only with a probe row that finds it, and the rows the selection would have
 // dropped are never found. Each creator's ordinary consumers are written out
 // ("dataConsumers") first, since the join may also take the creator's rows.
-json::Value fuse_build_filters(const json::Value& plan) {
-  json::Value out = plan;
-  json::Value* ops_v = jfind(out, "ops");
-  if (ops_v == nullptr) return out;
-  auto& ops = ops_v->a;
+void fuse_build_filters(std::vector<json::Value>& ops) {
   auto index_of = [&](const std::string& name) {
     for (size_t i = 0; i < ops.size(); ++i)
       if (ops[i].at("name").str() == name) return static_cast<int>(i);
@@ -2045,7 +2036,6 @@ json::Value fuse_build_filters(const json::Value& plan) {
     jset(ops[join], "buildFilters", filters);
     ops.erase(ops.begin() + use);
   }
-  return out;
 }
 
 // Pipeline fusion: BloomFilterCreatePOps over the same rows become one
@@ -2057,11 +2047,7 @@ json::Value fuse_build_filters(const json::Value& plan) {
 // ordinary consumers; each filter keeps its creator's name as its origin,
 // which its receivers know it by, and goes to the same receivers. Results
 // are unchanged: every filter is built from the same rows as before.
-json::Value fuse_creator_chains(const json::Value& plan) {
-  json::Value out = plan;
-  json::Value* ops_v = jfind(out, "ops");
-  if (ops_v == nullptr) return out;
-  auto& ops = ops_v->a;
+void fuse_creator_chains(std::vector<json::Value>& ops) {
   auto is_creator = [](const json::Value& o) { return o.at("type").str() == "BloomFilterCreatePOp"; };
   auto index_of = [&](const std::string& name) {
     for (size_t i = 0; i < ops.size(); ++i)
@@ -2150,7 +2136,6 @@ json::Value fuse_creator_chains(const json::Value& plan) {
     }
     ops.erase(ops.begin() + a);
   }
-  return out;
 }
 
 // Pipeline fusion: a chain of inner HashJoinArrowPOps in which each join's
@@ -2161,11 +2146,7 @@ json::Value fuse_creator_chains(const json::Value& plan) {
 // every producer that sent to an earlier join now sends to it. Results are
 // unchanged: the fused operator builds the same tables and emits the last
 // join's rows.
-json::Value fuse_join_chains(const json::Value& plan) {
-  json::Value out = plan;
-  json::Value* ops_v = jfind(out, "ops");
-  if (ops_v == nullptr) return out;
-  auto& ops = ops_v->a;
+void fuse_join_chains(std::vector<json::Value>& ops) {
   auto is_join = [](const json::Value& o) {
     return o.at("type").str() == "HashJoinArrowPOp" && o.get_str("joinType", "INNER") == "INNER" &&
            !o.contains("buildKeys");  // multi-column keys join one at a time
@@ -2188,18 +2169,21 @@ json::Value fuse_join_chains(const json::Value& plan) {
     return j;
   };
   for (;;) {
-    // the first join of a chain: a join no other join feeds as its chain successor
-    int head = -1;
-    for (size_t i = 0; i < ops.size() && head < 0; ++i) {
-      if (next_of(i) < 0) continue;
-      bool fed = false;
-      for (size_t k = 0; k < ops.size(); ++k) fed |= next_of(k) == static_cast<int>(i);
-      if (!fed) head = static_cast<int>(i);
+    // each join's chain successor, then the first join of a chain: a join no
+    // other join feeds as its chain successor
+    std::vector<int> nxt(ops.size());
+    std::vector<bool> fed(ops.size(), false);
+    for (size_t i = 0; i < ops.size(); ++i) {
+      nxt[i] = next_of(i);
+      if (nxt[i] >= 0) fed[static_cast<size_t>(nxt[i])] = true;
     }
+    int head = -1;
+    for (size_t i = 0; i < ops.size() && head < 0; ++i)
+      if (nxt[i] >= 0 && !fed[i]) head = static_cast<int>(i);
     if (head < 0) break;
     std::vector<int> chain{head};
     while (static_cast<int>(chain.size()) < kJoinChainMax) {
-      const int j = next_of(static_cast<size_t>(chain.back()));
+      const int j = nxt[static_cast<size_t>(chain.back())];
       if (j < 0) break;
       chain.push_back(j);
     }
@@ -2226,12 +2210,13 @@ json::Value fuse_join_chains(const json::Value& plan) {
     jset(fused, "consumers", jlist(ops[chain.back()].str_list("consumers")));
     const std::string last = ops[chain.back()].at("name").str();
     std::vector<json::Value> kept;
+    kept.reserve(ops.size());
     for (size_t i = 0; i < ops.size(); ++i) {
       if (absorbed.count(ops[i].at("name").str())) {
-        if (static_cast<int>(i) == chain.back()) kept.push_back(fused);
+        if (static_cast<int>(i) == chain.back()) kept.push_back(std::move(fused));
         continue;
       }
-      json::Value o = ops[i];
+      json::Value o = std::move(ops[i]);
       auto rename = [&](json::Value& x, const char* key) {
         json::Value* l = jfind(x, key);
         if (l == nullptr) return;
@@ -2246,15 +2231,21 @@ json::Value fuse_join_chains(const json::Value& plan) {
         rename(o, key);
       if (json::Value* fl = jfind(o, "filters"))  // a fused creator's receivers, filter by filter
         for (auto& f : fl->a) rename(f, "bloomFilterUsePOps");
-      kept.push_back(o);
+      kept.push_back(std::move(o));
     }
-    ops = kept;
+    ops = std::move(kept);
   }
-  return out;
 }
 
 json::Value fuse_pipelines(const json::Value& plan) {
-  return fuse_join_chains(fuse_creator_chains(fuse_build_filters(fuse_bloom_chains(plan))));
+  json::Value out = plan;  // the passes rewrite the copy's operator list in place
+  json::Value* ops_v = jfind(out, "ops");
+  if (ops_v == nullptr || ops_v->kind != json::Value::Array) return out;
+  fuse_bloom_chains(ops_v->a);
+  fuse_build_filters(ops_v->a);
+  fuse_creator_chains(ops_v->a);
+  fuse_join_chains(ops_v->a);
+  return out;
 }
 
 std::unique_ptr<Execution> build_execution(const json::Value& plan_in, cudaStream_t stream) {
