@@ -1864,6 +1864,38 @@ json::Value* jfind(json::Value& o, const std::string& key) {
   return nullptr;
 }
 
+// Rewrites the operator names listed in o[key] in place: map(name, out)
+// appends what a name becomes (nothing: it is dropped) and returns true when
+// it changes, and only the first occurrence of each name is kept. A list
+// whose names are all strings, none of them changed and none repeated, is
+// already what the rewrite would make, and is left as it is.
+template <class Map>
+void rewrite_names(json::Value& o, const char* key, const Map& map) {
+  json::Value* l = jfind(o, key);
+  if (l == nullptr) return;
+  bool rebuild = l->kind != json::Value::Array;  // str_list below reports it
+  std::vector<std::string> ys;
+  for (size_t i = 0; !rebuild && i < l->a.size(); ++i) {
+    const json::Value& e = l->a[i];
+    if (e.kind != json::Value::String) {
+      rebuild = true;
+      break;
+    }
+    ys.clear();
+    if (map(e.s, ys)) rebuild = true;
+    for (size_t k = 0; k < i && !rebuild; ++k) rebuild = l->a[k].s == e.s;
+  }
+  if (!rebuild) return;
+  std::vector<std::string> nv;
+  for (const auto& x : o.str_list(key)) {
+    ys.clear();
+    if (!map(x, ys)) ys.push_back(x);
+    for (auto& y : ys)
+      if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
+  }
+  *l = jlist(nv);
+}
+
 }  // namespace
 
 // Pipeline fusion: a chain of BloomFilterUsePOps in which each one's only
@@ -1919,18 +1951,14 @@ void fuse_bloom_chains(std::vector<json::Value>& ops) {
     crs.insert(crs.end(), r2.begin(), r2.end());
     jset(ops[second], "bloomFilterColumns", jlist(cols));
     jset(ops[second], "creators", jlist(crs));
-    for (auto& o : ops) {
-      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"}) {
-        json::Value* l = jfind(o, key);
-        if (l == nullptr) continue;
-        std::vector<std::string> v = o.str_list(key), nv;
-        for (auto& x : v) {
-          const std::string y = x == u1 ? u2 : x;
-          if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
-        }
-        *l = jlist(nv);
-      }
-    }
+    auto to_u2 = [&](const std::string& x, std::vector<std::string>& out) {
+      if (x != u1) return false;
+      out.push_back(u2);
+      return true;
+    };
+    for (auto& o : ops)
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"})
+        rewrite_names(o, key, to_u2);
     ops.erase(ops.begin() + first);
   }
 }
@@ -2007,20 +2035,13 @@ void fuse_build_filters(std::vector<json::Value>& ops) {
       if (&o == &ops[use]) continue;
       const bool is_creator = std::find(crs.begin(), crs.end(), o.at("name").str()) != crs.end();
       for (const char* key : {"consumers", "bloomFilterUsePOps", "dataConsumers", "buildProducers"}) {
-        json::Value* l = jfind(o, key);
-        if (l == nullptr) continue;
-        std::vector<std::string> v = o.str_list(key), nv;
-        for (auto& x : v) {
-          std::vector<std::string> ys{x};
-          if (x == un) {
-            if (std::string(key) == "buildProducers") ys = data;
-            else if (std::string(key) == "consumers" && is_creator) ys = {};  // the filter goes by "bloomFilterUsePOps"
-            else ys = {jn};
-          }
-          for (auto& y : ys)
-            if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
-        }
-        *l = jlist(nv);
+        const std::string k = key;
+        rewrite_names(o, key, [&](const std::string& x, std::vector<std::string>& out) {
+          if (x != un) return false;
+          if (k == "buildProducers") out = data;
+          else if (!(k == "consumers" && is_creator)) out.push_back(jn);  // a creator's filter goes by "bloomFilterUsePOps"
+          return true;
+        });
       }
     }
     json::Value filters;
@@ -2122,18 +2143,14 @@ void fuse_creator_chains(std::vector<json::Value>& ops) {
     jset(fused, "dataConsumers", jlist(data_consumers_of(ops[b])));
     jset(fused, "consumers", jlist(cons));
     ops[b] = fused;
-    for (auto& o : ops) {
-      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"}) {
-        json::Value* l = jfind(o, key);
-        if (l == nullptr) continue;
-        std::vector<std::string> v = o.str_list(key), nv;
-        for (auto& x : v) {
-          const std::string y = x == an ? bn : x;
-          if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
-        }
-        *l = jlist(nv);
-      }
-    }
+    auto to_bn = [&](const std::string& x, std::vector<std::string>& out) {
+      if (x != an) return false;
+      out.push_back(bn);
+      return true;
+    };
+    for (auto& o : ops)
+      for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"})
+        rewrite_names(o, key, to_bn);
     ops.erase(ops.begin() + a);
   }
 }
@@ -2217,20 +2234,15 @@ void fuse_join_chains(std::vector<json::Value>& ops) {
         continue;
       }
       json::Value o = std::move(ops[i]);
-      auto rename = [&](json::Value& x, const char* key) {
-        json::Value* l = jfind(x, key);
-        if (l == nullptr) return;
-        std::vector<std::string> v = x.str_list(key), nv;
-        for (auto& e : v) {
-          const std::string y = absorbed.count(e) ? last : e;
-          if (std::find(nv.begin(), nv.end(), y) == nv.end()) nv.push_back(y);
-        }
-        *l = jlist(nv);
+      auto to_last = [&](const std::string& x, std::vector<std::string>& out) {
+        if (!absorbed.count(x)) return false;
+        out.push_back(last);
+        return true;
       };
       for (const char* key : {"consumers", "bloomFilterUsePOps", "buildProducers", "probeProducers", "dataConsumers"})
-        rename(o, key);
+        rewrite_names(o, key, to_last);
       if (json::Value* fl = jfind(o, "filters"))  // a fused creator's receivers, filter by filter
-        for (auto& f : fl->a) rename(f, "bloomFilterUsePOps");
+        for (auto& f : fl->a) rewrite_names(f, "bloomFilterUsePOps", to_last);
       kept.push_back(std::move(o));
     }
     ops = std::move(kept);
