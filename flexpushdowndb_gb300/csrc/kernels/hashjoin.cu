@@ -10,7 +10,9 @@
 // linear probing. For 32-bit keys the tag is the key itself, so a probe
 // decides a match from the slot alone; for 64-bit keys the tag is the high
 // half of the hash and a tag hit is confirmed against the build key column.
-// Duplicate build keys occupy separate slots (multimap semantics). Probing:
+// Duplicate build keys occupy separate slots (multimap semantics). A build
+// may test up to four bloom filters on its key (a bloom selection folded
+// into the join) and leave out the rows that fail one. Probing:
 // a lane walks one probe row's run at a time, reading per step the aligned
 // four-slot group (one sector) that holds the run's next slot, and takes the
 // warp's next row as soon as its run ends. Matches collect per warp in
