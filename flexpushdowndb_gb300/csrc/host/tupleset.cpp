@@ -248,9 +248,13 @@ std::vector<Field> import_schema(const ArrowSchema* schema) {
   if (schema == nullptr || schema->release == nullptr) fail(GFPDB_EINVAL, "null or released ArrowSchema");
   if (schema->format == nullptr || std::strcmp(schema->format, "+s") != 0)
     fail(GFPDB_EINVAL, "a TupleSet schema must be a struct (format \"+s\")");
+  if (schema->n_children < 0 || (schema->n_children > 0 && schema->children == nullptr))
+    fail(GFPDB_EINVAL, "ArrowSchema with a negative child count or without its children");
   std::vector<Field> fields;
   for (int64_t i = 0; i < schema->n_children; ++i) {
     const ArrowSchema* c = schema->children[i];
+    if (c == nullptr || c->release == nullptr)
+      fail(GFPDB_EINVAL, "ArrowSchema child " + std::to_string(i) + " is missing or released");
     fields.push_back(Field{c->name != nullptr ? c->name : "", dtype_from_format(c->format)});
   }
   return fields;
@@ -285,12 +289,16 @@ TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* d
     fail(GFPDB_EINVAL, "ArrowArray child count does not match the schema");
   const int64_t n = arr.length;
   const int64_t soff = arr.offset;
+  if (n < 0 || soff < 0) fail(GFPDB_EINVAL, "ArrowArray with a negative length or offset");
+  if (arr.n_children > 0 && arr.children == nullptr) fail(GFPDB_EINVAL, "ArrowArray without its children");
   std::vector<ColumnPtr> cols;
   std::vector<Field> fields;
   for (size_t i = 0; i < all_fields.size(); ++i) {
     if (wanted != nullptr && !listed(wanted, all_fields[i].name)) continue;
     fields.push_back(all_fields[i]);
     const ArrowArray* c = arr.children[i];
+    if (c == nullptr || c->release == nullptr || c->buffers == nullptr || c->offset < 0)
+      fail(GFPDB_EINVAL, "column '" + all_fields[i].name + "' is missing, released, without buffers or negatively offset");
     if (c->length < soff + n) fail(GFPDB_EINVAL, "column '" + all_fields[i].name + "' is shorter than the struct");
     if (c->null_count != 0 && c->buffers[0] != nullptr)
       fail(GFPDB_EUNSUPPORTED, "column '" + all_fields[i].name + "' has nulls; nullable inputs are not supported");
@@ -298,6 +306,7 @@ TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* d
     DType t = all_fields[i].type;
     if (t != DType::Utf8) {
       if (c->n_buffers != 2) fail(GFPDB_EINVAL, "fixed-width column needs 2 buffers");
+      if (n > 0 && c->buffers[1] == nullptr) fail(GFPDB_EINVAL, "column '" + all_fields[i].name + "' has no values");
       int w = dtype_width(t);
       const char* src = static_cast<const char*>(c->buffers[1]) + off * w;
       const bool zero_copy = host && !copy_device && (host_copy_mode() == 2 || listed(in_place, all_fields[i].name));
@@ -325,9 +334,12 @@ TupleSetPtr import_tupleset(const ArrowSchema* schema, const ArrowDeviceArray* d
       const int32_t* offs = static_cast<const int32_t*>(c->buffers[1]) + off;
       const char* bytes = static_cast<const char*>(c->buffers[2]);
       if (host) {
+        if (c->buffers[1] == nullptr) fail(GFPDB_EINVAL, "utf8 column '" + all_fields[i].name + "' has no offsets");
         // Offsets are rebased to start at 0 so the device copy holds only the
         // bytes this slice spans.
         int32_t first = offs[0], last = offs[n];
+        if (first < 0 || last < first || (last > first && bytes == nullptr))
+          fail(GFPDB_EINVAL, "utf8 column '" + all_fields[i].name + "' has offsets out of order or no bytes");
         std::vector<int32_t> rebased(n + 1);
         for (int64_t k = 0; k <= n; ++k) rebased[k] = offs[k] - first;
         auto ob = make_buffer((n + 1) * 4, s);

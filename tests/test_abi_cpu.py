@@ -273,3 +273,54 @@ def test_oracle_shuffle_is_stable_and_complete():
     for s in range(3):
         ids = rows["i"][offs[s]:offs[s + 1]].tolist()
         assert ids == sorted(ids)
+
+
+def test_malformed_arrow_schemas_are_refused():
+    """A caller's ArrowSchema that breaks the C data interface's rules (no
+    children array behind a positive count, a missing or released child, a
+    negative count, a child without a format) is refused with
+    GFPDB_EINVAL, never dereferenced."""
+    import ctypes
+
+    from flexpushdowndb_gb300.expression import col, lt, num_lit, to_json
+
+    keep = []
+    noop = _abi.SCHEMA_RELEASE(lambda p: None)
+    keep.append(noop)
+
+    def child(fmt, name, released=False):
+        c = _abi.ArrowSchema()
+        c.format = fmt
+        c.name = name
+        c.n_children = 0
+        if not released:
+            c.release = noop
+        keep.append(c)
+        return c
+
+    def parent(children, n=None, null_array=False):
+        s = _abi.ArrowSchema()
+        s.format = b"+s"
+        s.name = b""
+        s.n_children = len(children) if n is None else n
+        if not null_array:
+            arr = (ctypes.POINTER(_abi.ArrowSchema) * max(1, len(children)))()
+            for i, c in enumerate(children):
+                arr[i] = ctypes.pointer(c) if c is not None else ctypes.POINTER(_abi.ArrowSchema)()
+            s.children = ctypes.cast(arr, ctypes.POINTER(ctypes.POINTER(_abi.ArrowSchema)))
+            keep.append(arr)
+        s.release = noop
+        keep.append(s)
+        return s
+
+    pred = to_json(lt(col("a"), num_lit(2))).encode()
+    L = _abi.lib()
+    h = ctypes.c_void_p()
+    good = parent([child(b"i", b"a")])
+    assert L.gfpdb_filter_compile(pred, ctypes.byref(good), ctypes.byref(h)) == 0
+    L.gfpdb_filter_free(h)
+    for bad in (parent([child(b"i", b"a")], null_array=True), parent([None]),
+                parent([child(b"i", b"a", released=True)]), parent([child(b"i", b"a")], n=-1),
+                parent([child(None, b"a")])):
+        rc = L.gfpdb_filter_compile(pred, ctypes.byref(bad), ctypes.byref(h))
+        assert rc == _abi.GFPDB_EINVAL, L.gfpdb_last_error()
